@@ -1,0 +1,218 @@
+/*
+ * simkit_gb300: C ABI of the GB300 backward-Euler stable neo-Hookean FEM path.
+ *
+ * The reference (otmanon/simkit) is a pure-Python library; its "interface"
+ * for this path is a set of Python functions over numpy arrays and scipy
+ * sparse matrices.  Each entry point below replaces one of them (or the
+ * numpy/scipy work inside one of them) and cites it as file:line within the
+ * simkit project.  The Python package simkit_gb300 binds these with ctypes
+ * and keeps simkit's Python signatures on top.
+ *
+ * Conventions
+ *   - Every pointer argument is a DEVICE pointer unless its name ends in _h
+ *     (host).  The caller owns all memory: nothing here allocates device
+ *     memory.  Entry points that need scratch take a workspace pointer whose
+ *     size a matching *_workspace_size() query returns.
+ *   - `stream` is a cudaStream_t passed as void*; 0 is the legacy stream.
+ *     Work is stream-ordered; entry points synchronize only where they must
+ *     return a host scalar (documented per function).
+ *   - Return value: 0 on success, a negative skg_status on failure;
+ *     skg_last_error() returns the message of the calling thread's last error.
+ *   - Positions are simkit's layout: x[3 i + c], float64 (simkit/deformation_jacobian.py:13-16).
+ *   - Element tier F arrays are (t, d, d) row-major float64 (snh.py:65-129).
+ */
+#ifndef SIMKIT_GB300_H_
+#define SIMKIT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum skg_status {
+  SKG_OK = 0,
+  SKG_ERR_ARG = -1,        /* invalid argument (simkit raises ValueError) */
+  SKG_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+  SKG_ERR_NOT_CONVERGED = -3,
+  SKG_ERR_LINESEARCH = -4, /* Armijo search exhausted: simkit returns t = 0 (backtracking_line_search.py:66-67) */
+  SKG_ERR_NONFINITE = -5,  /* NaN/Inf in an energy, gradient or residual */
+  SKG_ERR_TIMEOUT = -6,    /* a bounded grid-wide wait gave up */
+  SKG_ERR_CAPACITY = -7    /* a size exceeds a fixed capacity */
+} skg_status;
+
+typedef enum skg_precision {
+  SKG_FP64 = 0,  /* every kernel in FP64 */
+  SKG_MIXED = 1  /* FP32 element Hessians, SpMV and PCG vectors; FP64 gradient,
+                    residual norms, dot products and energy sums */
+} skg_precision;
+
+/* ---------------------------------------------------------------------- */
+/* errors / version                                                        */
+/* ---------------------------------------------------------------------- */
+int skg_version(void);
+/* Copies the calling thread's last error message into buf (NUL-terminated). */
+int skg_last_error(char* buf_h, size_t len);
+
+/* ---------------------------------------------------------------------- */
+/* element tier: simkit/energies/stable_neo_hookean.py                     */
+/* ---------------------------------------------------------------------- */
+/* psi per element.  Replaces stable_neo_hookean_energy_element_F (snh.py:65-129).
+ * dim 2 or 3; F (t,d,d) f64, mu/lam (t) f64 -> psi (t) f64. precision selects the
+ * arithmetic (inputs and outputs stay f64). */
+int skg_snh_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                             double* psi, int64_t t, void* stream);
+/* PK1 per element.  Replaces stable_neo_hookean_gradient_element_F (snh.py:132-218). */
+int skg_snh_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* P, int64_t t, void* stream);
+/* d*d x d*d Hessian per element, not projected.  Replaces
+ * stable_neo_hookean_hessian_element_F (snh.py:221-443). */
+int skg_snh_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* H, int64_t t, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* psd_project: simkit/psd_project.py:12-47                                */
+/* ---------------------------------------------------------------------- */
+/* Batched eigenvalue floor of symmetric d x d blocks (1 <= d <= 12) by cyclic
+ * Jacobi.  method 0 = 'proj' (floor at 1e-6, :37), 1 = 'abs' (:35).
+ * H and out may alias. */
+int skg_psd_project(const double* H, double* out, int64_t n, int d, int method, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* mesh setup                                                              */
+/* ---------------------------------------------------------------------- */
+/* Per-tet inverse rest edge matrix Dinv (rows = grad N_1..3) and signed volume.
+ * Replaces the per-element D of deformation_jacobian (deformation_jacobian.py:43-61)
+ * and volume/tetrahedron_volumes (volume.py:14-41, tetrahedron_volumes.py:26-27).
+ * X (n,3) f64, T (t,4) i32 -> dinv (9,t) f64 SoA, vol (t) f64. Returns SKG_ERR_ARG
+ * through the status buffer... no: degenerate tets yield inf entries; callers check. */
+int skg_tet_setup(const double* X, const int32_t* T, int64_t n, int64_t t, double* dinv, double* vol,
+                  void* stream);
+
+/* F = J x for the tet operator: F (t,3,3) f64 from positions x (3n) f64.
+ * Replaces the sparse product J @ x (snh.py:499, deformation_jacobian.py example). */
+int skg_tet_deformation_gradient(const int32_t* T, const double* dinv, const double* x, int64_t t,
+                                 double* F, void* stream);
+/* y = J^T vec(P): scatter-free vertex gather (deterministic). P (t,3,3) f64 -> y (3n) f64.
+ * Replaces J.transpose() @ P.reshape(-1,1) (snh.py:501-502). */
+int skg_tet_gradient_scatter(const int32_t* T, const double* dinv, const double* P, const int32_t* v2t_ptr,
+                             const int32_t* v2t, int64_t n, int64_t t, double* y, void* stream);
+
+/* Sparse pattern of K = J^T blockdiag(He) J for a tet mesh, as 3x3 blocks.
+ * Host function (all pointers _h).  Pass 1 (rowptr == NULL): returns the number of
+ * blocks in *n_blocks_h.  Pass 2 fills:
+ *   bsr_rowptr (n+1), bsr_col (nb)  - block CSR, columns sorted ascending
+ *   bsr_diag (n)                    - slot of each diagonal block
+ *   hc_ptr (nb+1), hc_src (16 t)    - per slot, the per-tet blocks summed into it,
+ *                                     encoded tet*16 + code, ordered by tet
+ *   v2t_ptr (n+1), v2t (4 t)        - vertex -> (tet*4 + corner), ordered by tet
+ * Expanded to scalars (row 3v+i, columns 3w+j) the block pattern equals the
+ * pattern scipy produces for J.T @ block_diag(He) @ J (snh.py:536-537) whenever
+ * no assembled entry cancels to exactly zero. */
+int skg_pattern_build(const int32_t* T_h, int64_t n, int64_t t, int64_t* n_blocks_h, int32_t* bsr_rowptr_h,
+                      int32_t* bsr_col_h, int32_t* bsr_diag_h, int32_t* hc_ptr_h, int32_t* hc_src_h,
+                      int32_t* v2t_ptr_h, int32_t* v2t_h);
+
+/* Mesh descriptor used by the assembled tier and the solver (all device pointers). */
+typedef struct skg_tet_mesh {
+  int64_t n_verts;
+  int64_t n_tets;
+  int64_t n_blocks;
+  const int32_t* tets;       /* (t,4) */
+  const double* dinv;        /* (9,t) SoA */
+  const float* dinv32;       /* (9,t) SoA, FP32 copy (mixed precision) */
+  const double* vol;         /* (t) signed rest volume */
+  const double* mu;          /* (t) */
+  const double* lam;         /* (t) */
+  const float* mat32;        /* (3,t): vol, mu, lam in FP32 */
+  const int32_t* bsr_rowptr; /* (n+1) */
+  const int32_t* bsr_col;    /* (nb) */
+  const int32_t* bsr_diag;   /* (n) */
+  const int32_t* hc_ptr;     /* (nb+1) */
+  const int32_t* hc_src;     /* (16t) */
+  const int32_t* v2t_ptr;    /* (n+1) */
+  const int32_t* v2t;        /* (4t) */
+} skg_tet_mesh;
+
+/* Assembled block matrix (3x3 blocks).  Values of block slot s of row v live at
+ * val[9*rowptr[v] + m*K_v + (s - rowptr[v])], m = 3i+j, K_v = rowptr[v+1]-rowptr[v]. */
+
+/* ---------------------------------------------------------------------- */
+/* assembled tier (x variable): snh.py:449-538                             */
+/* ---------------------------------------------------------------------- */
+/* Workspace bytes for the assembled-tier calls and the solver. */
+int64_t skg_assembly_workspace_size(const skg_tet_mesh* mesh, int precision);
+
+/* sum_e vol_e psi(F_e), F = J x.  Replaces stable_neo_hookean_energy_x (snh.py:449-474).
+ * Synchronizes `stream` to return the value in *energy_h. */
+int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h, void* workspace,
+                     void* stream);
+/* J^T vec(vol P).  Replaces stable_neo_hookean_gradient_x (snh.py:477-503). g (3n) f64. */
+int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, void* workspace, void* stream);
+/* J^T blockdiag(psd(vol He)) J as block values.  Replaces stable_neo_hookean_hessian_x
+ * (snh.py:506-538).  precision SKG_FP64 writes val64 (9 nb f64); SKG_MIXED writes val32.
+ * psd != 0 applies simkit's 1e-6 eigenvalue floor to each vol-weighted 9x9 block. */
+int skg_snh_hessian_x(const skg_tet_mesh* mesh, const double* x, int precision, int psd, double* val64,
+                      float* val32, void* workspace, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Newton / backward Euler: solvers/newton.py:7-75, integrators/backward_euler.py:27-91 */
+/* ---------------------------------------------------------------------- */
+typedef struct skg_be_params {
+  double dt;                /* time step h */
+  double tol;               /* relative residual ||g(x)|| / ||g(x_tilde)|| */
+  int32_t max_newton;       /* <= 20 in the standard workloads */
+  int32_t precision;        /* skg_precision */
+  double pcg_rtol;          /* PCG relative tolerance (forcing term) */
+  int32_t pcg_max_iter;
+  int32_t do_line_search;
+  double ls_alpha;          /* Armijo parameter, simkit default 0.01 */
+  double ls_beta;           /* step factor, simkit default 0.5 */
+  int32_t ls_max_iter;      /* simkit default 100 */
+  int32_t pcg_mode;         /* 0 = kernel per phase, 1 = persistent cooperative kernel */
+  double ls_threshold;      /* Armijo slack, simkit default 1e-12 */
+} skg_be_params;
+
+typedef struct skg_be_state {
+  double* u;                /* (3n) displacement from rest at the new step; in: ignored */
+  const double* u_curr;     /* (3n) displacement at step k */
+  const double* u_prev;     /* (3n) displacement at step k-1 */
+  const double* mass;       /* (n) lumped vertex mass */
+  const double* f_ext;      /* (3n) external force */
+  const uint8_t* pinned;    /* (3n) 1 = DOF held at its rest position */
+} skg_be_state;
+
+typedef struct skg_step_info {
+  int32_t newton_iters;
+  int32_t pcg_iters;        /* summed over Newton iterations */
+  int32_t ls_trials;        /* energy evaluations in line searches */
+  int32_t status;           /* skg_status of the step */
+  double residual0;         /* ||g(x_tilde)|| */
+  double residual;          /* final ||g|| / residual0 */
+  double min_alpha;         /* smallest accepted step */
+  double energy;            /* final incremental potential relative to rest */
+} skg_step_info;
+
+int64_t skg_be_workspace_size(const skg_tet_mesh* mesh, int precision);
+/* One backward-Euler step: Newton on the free DOFs from x_tilde = 2 x_k - x_{k-1}
+ * with a block-Jacobi PCG solve per iteration and Armijo backtracking, until the
+ * relative residual is below tol.  Host-synchronizes for its decisions. */
+int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state,
+                void* workspace, skg_step_info* info_h, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* generic sparse solve: replaces spsolve in newton_solver (newton.py:52)   */
+/* ---------------------------------------------------------------------- */
+/* Block-Jacobi PCG on a symmetric 3x3-block matrix in the layout above (FP64 values),
+ * x = A^{-1} b to relative residual rtol. Workspace: skg_pcg_workspace_size. Writes
+ * the iteration count to *iters_h (synchronizes). */
+int64_t skg_pcg_workspace_size(int64_t n_rows_blocks);
+int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                  double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* workspace, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMKIT_GB300_H_ */

@@ -1,0 +1,570 @@
+// Stable neo-Hookean element math shared by every kernel of the FEM path.
+//
+// All routines are plain functions of registers, compiled for the device by
+// nvcc and for the host by g++ (the host build is what the CPU unit tests
+// exercise against the FP64 oracle).  Storage conventions:
+//   * F, G, P, U, V: 3x3 row-major, a[3*i + j] = M_ij.
+//   * F = I + G, where G is the displacement gradient.
+//   * gN[3*a + j] = d N_a / d X_j, the rest-shape gradient of barycentric
+//     coordinate a (a = 0..3), so that F_ij = sum_a x_{a,i} gN[a][j].
+//
+// Energy density (simkit/energies/stable_neo_hookean.py:65-129):
+//   psi = mu/2 (I_C - 3) - mu/2 log(I_C + 1) + lam/2 (J - alpha)^2,
+//   alpha = 1 + 3 mu / (4 lam).
+// PK1 (:132-218): P = A F + D cof F, A = mu I_C/(I_C+1), D = lam (J - alpha).
+// F-Hessian (:221-443): A I + B f f^T + lam c c^T + D d2J/dF2, B = 2 mu/(I_C+1)^2.
+//
+// The displacement forms below rewrite psi - psi(I) and P so that the terms
+// that cancel at rest (A + D = 0 at F = I) are combined symbolically; in
+// FP32 this keeps relative accuracy near rest where the direct forms lose
+// digits to cancellation.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SK_HD __host__ __device__ __forceinline__
+#else
+#define SK_HD inline
+#endif
+
+namespace skg {
+
+template <typename R> SK_HD R sk_sqrt(R x) { return sqrt(x); }
+template <typename R> SK_HD R sk_abs(R x) { return x < R(0) ? -x : x; }
+template <typename R> SK_HD R sk_log1p(R x) { return log1p(x); }
+template <typename R> SK_HD R sk_log(R x) { return log(x); }
+template <typename R> SK_HD R sk_max(R a, R b) { return a > b ? a : b; }
+template <typename R> SK_HD R sk_min(R a, R b) { return a < b ? a : b; }
+#if defined(__CUDACC__)
+template <> SK_HD float sk_sqrt<float>(float x) { return sqrtf(x); }
+template <> SK_HD float sk_log1p<float>(float x) { return log1pf(x); }
+template <> SK_HD float sk_log<float>(float x) { return logf(x); }
+#endif
+
+template <typename R> struct Eps;
+template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; static constexpr int sweeps = 6; };
+template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; static constexpr int sweeps = 10; };
+
+// eigenvalue floor of simkit's psd_project 'proj' (simkit/psd_project.py:37)
+constexpr double kPsdFloor = 1e-6;
+
+// --------------------------------------------------------------------------
+// small linear algebra
+// --------------------------------------------------------------------------
+template <typename R> SK_HD R det3(const R* F) {
+  return F[0] * (F[4] * F[8] - F[5] * F[7]) - F[1] * (F[3] * F[8] - F[5] * F[6]) +
+         F[2] * (F[3] * F[7] - F[4] * F[6]);
+}
+
+// cof(F)_ij = dJ/dF_ij
+template <typename R> SK_HD void cof3(const R* F, R* C) {
+  C[0] = F[4] * F[8] - F[5] * F[7];
+  C[1] = F[5] * F[6] - F[3] * F[8];
+  C[2] = F[3] * F[7] - F[4] * F[6];
+  C[3] = F[2] * F[7] - F[1] * F[8];
+  C[4] = F[0] * F[8] - F[2] * F[6];
+  C[5] = F[1] * F[6] - F[0] * F[7];
+  C[6] = F[1] * F[5] - F[2] * F[4];
+  C[7] = F[2] * F[3] - F[0] * F[5];
+  C[8] = F[0] * F[4] - F[1] * F[3];
+}
+
+// sum of principal 2x2 minors
+template <typename R> SK_HD R minors2(const R* G) {
+  return (G[0] * G[4] - G[1] * G[3]) + (G[0] * G[8] - G[2] * G[6]) + (G[4] * G[8] - G[5] * G[7]);
+}
+
+// phi(z) = z - log(1 + z) >= 0, accurate for small |z|.
+// With w = z / (2 + z): log(1+z) = 2 atanh(w) = 2 (w + w^3/3 + w^5/5 + ...),
+// and z - 2w = z w, so phi = z w - 2 w^3 (1/3 + w^2/5 + w^4/7 + ...), a
+// series with no cancellation; |z| <= 1/2 gives |w| <= 1/3.
+template <typename R> SK_HD R phi_log1p(R z) {
+  if (sk_abs(z) <= R(0.5)) {
+    const R w = z / (R(2) + z);
+    const R w2 = w * w;
+    R s = R(1) / R(23);
+    s = s * w2 + R(1) / R(21);
+    s = s * w2 + R(1) / R(19);
+    s = s * w2 + R(1) / R(17);
+    s = s * w2 + R(1) / R(15);
+    s = s * w2 + R(1) / R(13);
+    s = s * w2 + R(1) / R(11);
+    s = s * w2 + R(1) / R(9);
+    s = s * w2 + R(1) / R(7);
+    s = s * w2 + R(1) / R(5);
+    s = s * w2 + R(1) / R(3);
+    return z * w - R(2) * w * w2 * s;
+  }
+  return z - sk_log1p(z);
+}
+
+// --------------------------------------------------------------------------
+// energy density
+// --------------------------------------------------------------------------
+// direct form, exactly simkit's expression (snh.py:116-126)
+template <typename R> SK_HD R snh_psi(const R* F, R mu, R lam) {
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  const R J = det3(F);
+  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+  const R d = J - alpha;
+  return R(0.5) * mu * (IC - R(3)) - R(0.5) * mu * sk_log(IC + R(1)) + R(0.5) * lam * d * d;
+}
+
+// psi(I + G) - psi(I)
+//   = 3mu/8 (|G|^2 - 2 I2(G) - 2 det G) + mu/2 phi(x/4) + lam/2 y^2,
+// with x = I_C - 3 = 2 tr G + |G|^2 and y = J - 1 = tr G + I2(G) + det G.
+template <typename R> SK_HD R snh_dpsi(const R* G, R mu, R lam) {
+  R g2 = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) g2 += G[k] * G[k];
+  const R tr = G[0] + G[4] + G[8];
+  const R i2 = minors2(G);
+  const R dg = det3(G);
+  const R x = R(2) * tr + g2;
+  const R y = tr + i2 + dg;
+  return R(0.375) * mu * (g2 - R(2) * i2 - R(2) * dg) + R(0.5) * mu * phi_log1p(R(0.25) * x) +
+         R(0.5) * lam * y * y;
+}
+
+// psi(I) = -mu/2 log 4 + lam/2 (1 - alpha)^2, the rest energy density
+template <typename R> SK_HD R snh_psi_rest(R mu, R lam) {
+  const R a1 = R(3) * mu / (R(4) * lam);
+  return R(-0.5) * mu * sk_log(R(4)) + R(0.5) * lam * a1 * a1;
+}
+
+// --------------------------------------------------------------------------
+// first Piola-Kirchhoff stress
+// --------------------------------------------------------------------------
+template <typename R> SK_HD void snh_pk1(const R* F, R mu, R lam, R* P) {
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  const R J = det3(F);
+  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+  const R A = mu * IC / (IC + R(1));
+  const R D = lam * (J - alpha);
+  R C[9];
+  cof3(F, C);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) P[k] = A * F[k] + D * C[k];
+}
+
+// P(I + G) with cof(I + G) = (1 + tr G) I - G^T + cof G and
+// A + D = mu x / (4 (4 + x)) + lam y, D = lam y - 3 mu / 4:
+//   P = (A + D) I + A G + D (tr G I - G^T + cof G).
+template <typename R> SK_HD void snh_pk1_disp(const R* G, R mu, R lam, R* P) {
+  R g2 = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) g2 += G[k] * G[k];
+  const R tr = G[0] + G[4] + G[8];
+  const R x = R(2) * tr + g2;
+  const R y = tr + minors2(G) + det3(G);
+  const R q = mu * x / (R(4) * (R(4) + x));
+  const R ApD = q + lam * y;
+  const R A = R(0.75) * mu + q;
+  const R D = lam * y - R(0.75) * mu;
+  R C[9];
+  cof3(G, C);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int k = 3 * i + j;
+      R v = A * G[k] + D * (C[k] - G[3 * j + i]);
+      if (i == j) v += ApD + D * tr;
+      P[k] = v;
+    }
+}
+
+// --------------------------------------------------------------------------
+// explicit 9x9 F-Hessian, row-major vec(F) (the element tier)
+// --------------------------------------------------------------------------
+template <typename R> SK_HD void snh_hessian9(const R* F, R mu, R lam, R* H) {
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  const R J = det3(F);
+  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+  const R den = IC + R(1);
+  const R A = mu * IC / den;
+  const R B = R(2) * mu / (den * den);
+  const R D = lam * (J - alpha);
+  R C[9];
+  cof3(F, C);
+  for (int p = 0; p < 9; ++p)
+    for (int q = 0; q < 9; ++q) H[9 * p + q] = B * F[p] * F[q] + lam * C[p] * C[q] + (p == q ? A : R(0));
+  // D * d2J/dF_ij dF_kl = D * eps_ikm eps_jln F_mn: nonzero only for i != k, j != l
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) {
+      if (i == k) continue;
+      const int m = 3 - i - k;
+      const R sik = ((k - i + 3) % 3 == 1) ? R(1) : R(-1);  // eps_ikm
+      for (int j = 0; j < 3; ++j)
+        for (int l = 0; l < 3; ++l) {
+          if (j == l) continue;
+          const int n = 3 - j - l;
+          const R sjl = ((l - j + 3) % 3 == 1) ? R(1) : R(-1);
+          H[9 * (3 * i + j) + (3 * k + l)] += D * sik * sjl * F[3 * m + n];
+        }
+    }
+}
+
+// 2D element tier (simkit/energies/stable_neo_hookean.py, dim == 2 branches)
+template <typename R> SK_HD R snh_psi2(const R* F, R mu, R lam) {
+  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const R J = F[0] * F[3] - F[1] * F[2];
+  const R alpha = R(1) + R(2) * mu / (R(3) * lam);
+  const R d = J - alpha;
+  return R(0.5) * mu * (IC - R(2)) - R(0.5) * mu * sk_log(IC + R(1)) + R(0.5) * lam * d * d;
+}
+
+template <typename R> SK_HD void snh_pk1_2(const R* F, R mu, R lam, R* P) {
+  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const R J = F[0] * F[3] - F[1] * F[2];
+  const R alpha = R(1) + R(2) * mu / (R(3) * lam);
+  const R A = mu * IC / (IC + R(1));
+  const R D = lam * (J - alpha);
+  const R C[4] = {F[3], -F[2], -F[1], F[0]};
+  for (int k = 0; k < 4; ++k) P[k] = A * F[k] + D * C[k];
+}
+
+template <typename R> SK_HD void snh_hessian4(const R* F, R mu, R lam, R* H) {
+  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const R J = F[0] * F[3] - F[1] * F[2];
+  const R alpha = R(1) + R(2) * mu / (R(3) * lam);
+  const R den = IC + R(1);
+  const R A = mu * IC / den;
+  const R B = R(2) * mu / (den * den);
+  const R D = lam * (J - alpha);
+  const R C[4] = {F[3], -F[2], -F[1], F[0]};
+  for (int p = 0; p < 4; ++p)
+    for (int q = 0; q < 4; ++q) H[4 * p + q] = B * F[p] * F[q] + lam * C[p] * C[q] + (p == q ? A : R(0));
+  // d2J: (00,11) = (11,00) = +1, (01,10) = (10,01) = -1
+  H[4 * 0 + 3] += D;
+  H[4 * 3 + 0] += D;
+  H[4 * 1 + 2] -= D;
+  H[4 * 2 + 1] -= D;
+}
+
+// --------------------------------------------------------------------------
+// symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations
+// (Golub & Van Loan, Matrix Computations, sec. 8.5).  S = {s00,s01,s02,s11,s12,s22};
+// on return ev[k] are eigenvalues and column k of W (W[3*i+k]) the eigenvector.
+// --------------------------------------------------------------------------
+template <typename R> SK_HD void jacobi_rotate(R& app, R& aqq, R& apq, R& arp, R& arq, R* W, int p, int q) {
+  if (apq == R(0)) return;
+  const R theta = (aqq - app) / (R(2) * apq);
+  const R at = sk_abs(theta);
+  R t = (at > R(1e18)) ? R(0.5) / theta : R(1) / (at + sk_sqrt(at * at + R(1)));
+  if (theta < R(0) && at <= R(1e18)) t = -t;
+  const R c = R(1) / sk_sqrt(t * t + R(1));
+  const R s = t * c;
+  app -= t * apq;
+  aqq += t * apq;
+  apq = R(0);
+  const R g = arp, h = arq;
+  arp = c * g - s * h;
+  arq = s * g + c * h;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R vp = W[3 * i + p], vq = W[3 * i + q];
+    W[3 * i + p] = c * vp - s * vq;
+    W[3 * i + q] = s * vp + c * vq;
+  }
+}
+
+template <typename R> SK_HD void sym3_eig(const R* S, R* ev, R* W) {
+  R a00 = S[0], a01 = S[1], a02 = S[2], a11 = S[3], a12 = S[4], a22 = S[5];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) W[k] = (k % 4 == 0) ? R(1) : R(0);
+  const R scale = sk_abs(a00) + sk_abs(a11) + sk_abs(a22) + sk_abs(a01) + sk_abs(a02) + sk_abs(a12);
+  for (int sweep = 0; sweep < Eps<R>::sweeps; ++sweep) {
+    const R off = sk_abs(a01) + sk_abs(a02) + sk_abs(a12);
+    if (!(off > Eps<R>::v * R(0.25) * scale)) break;
+    jacobi_rotate(a00, a11, a01, a02, a12, W, 0, 1);  // r = 2: a20, a21
+    jacobi_rotate(a00, a22, a02, a01, a12, W, 0, 2);  // r = 1: a10, a12
+    jacobi_rotate(a11, a22, a12, a01, a02, W, 1, 2);  // r = 0: a01, a02
+  }
+  ev[0] = a00;
+  ev[1] = a11;
+  ev[2] = a22;
+}
+
+// --------------------------------------------------------------------------
+// rotation-variant SVD: F = U diag(s) V^T with U, V in SO(3), s0 >= s1 >= |s2|,
+// s2 carrying the sign of det F.  V from the eigenvectors of F^T F, U by
+// Gram-Schmidt on the columns of F V (u2 = u0 x u1 keeps det U = +1).
+// --------------------------------------------------------------------------
+template <typename R> SK_HD void any_perp(const R* a, R* out) {
+  R e[3] = {R(0), R(0), R(0)};
+  e[(sk_abs(a[0]) < R(0.6)) ? 0 : 1] = R(1);
+  R v[3] = {a[1] * e[2] - a[2] * e[1], a[2] * e[0] - a[0] * e[2], a[0] * e[1] - a[1] * e[0]};
+  const R n = sk_sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  out[0] = v[0] / n;
+  out[1] = v[1] / n;
+  out[2] = v[2] / n;
+}
+
+template <typename R> SK_HD void svd3_rv(const R* F, R* U, R* s, R* V) {
+  R S[6];
+  S[0] = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
+  S[1] = F[0] * F[1] + F[3] * F[4] + F[6] * F[7];
+  S[2] = F[0] * F[2] + F[3] * F[5] + F[6] * F[8];
+  S[3] = F[1] * F[1] + F[4] * F[4] + F[7] * F[7];
+  S[4] = F[1] * F[2] + F[4] * F[5] + F[7] * F[8];
+  S[5] = F[2] * F[2] + F[5] * F[5] + F[8] * F[8];
+  R ev[3];
+  sym3_eig(S, ev, V);
+  // sort descending; each swap negates one column so det V stays +1
+#define SK_SWAPCOL(a, b)                                          \
+  {                                                               \
+    R t_ = ev[a]; ev[a] = ev[b]; ev[b] = t_;                      \
+    for (int i_ = 0; i_ < 3; ++i_) {                              \
+      R v_ = V[3 * i_ + a];                                       \
+      V[3 * i_ + a] = -V[3 * i_ + b];                             \
+      V[3 * i_ + b] = v_;                                         \
+    }                                                             \
+  }
+  if (ev[0] < ev[1]) SK_SWAPCOL(0, 1);
+  if (ev[0] < ev[2]) SK_SWAPCOL(0, 2);
+  if (ev[1] < ev[2]) SK_SWAPCOL(1, 2);
+#undef SK_SWAPCOL
+  R b[9];  // B = F V, column k = b[3*i + k]
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) b[3 * i + k] = F[3 * i] * V[k] + F[3 * i + 1] * V[3 + k] + F[3 * i + 2] * V[6 + k];
+  R u0[3] = {b[0], b[3], b[6]};
+  R n0 = sk_sqrt(u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
+  R fscale = R(0);
+  for (int k = 0; k < 9; ++k) fscale = sk_max(fscale, sk_abs(F[k]));
+  const R tiny = Eps<R>::v * Eps<R>::v * (fscale > R(0) ? fscale : R(1));
+  if (n0 > tiny) {
+    u0[0] /= n0; u0[1] /= n0; u0[2] /= n0;
+  } else {
+    n0 = R(0); u0[0] = R(1); u0[1] = R(0); u0[2] = R(0);
+  }
+  R u1[3] = {b[1], b[4], b[7]};
+  const R d01 = u0[0] * u1[0] + u0[1] * u1[1] + u0[2] * u1[2];
+  u1[0] -= d01 * u0[0]; u1[1] -= d01 * u0[1]; u1[2] -= d01 * u0[2];
+  R n1 = sk_sqrt(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+  if (n1 > tiny) {
+    u1[0] /= n1; u1[1] /= n1; u1[2] /= n1;
+  } else {
+    n1 = R(0);
+    any_perp(u0, u1);
+  }
+  const R u2[3] = {u0[1] * u1[2] - u0[2] * u1[1], u0[2] * u1[0] - u0[0] * u1[2], u0[0] * u1[1] - u0[1] * u1[0]};
+  s[0] = n0;
+  s[1] = n1;
+  s[2] = u2[0] * b[2] + u2[1] * b[5] + u2[2] * b[8];
+  for (int i = 0; i < 3; ++i) {
+    U[3 * i + 0] = u0[i];
+    U[3 * i + 1] = u1[i];
+    U[3 * i + 2] = u2[i];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Per-tet Hessian w.r.t. the 12 vertex coordinates:
+//   K = L^T psd(vol * H_F) L, L the lift dF/dx,
+// with psd() the eigenvalue floor of simkit's psd_project applied to the
+// vol-weighted 9x9 block (simkit/energies/stable_neo_hookean.py:531-537).
+//
+// The 9x9 block's eigensystem is analytic in the rotation-variant SVD of F:
+//   twist (i,j):  U (e_i e_j^T - e_j e_i^T) V^T / sqrt2, eigenvalue A + D s_k
+//   flip  (i,j):  U (e_i e_j^T + e_j e_i^T) V^T / sqrt2, eigenvalue A - D s_k
+//   scaling m:    U diag(w_m) V^T, w_m the eigenvectors of the 3x3
+//                 A I + B s s^T + lam c c^T + D [[0,s2,s1],[s2,0,s0],[s1,s0,0]],
+//                 c = (s1 s2, s0 s2, s0 s1)
+// ({i,j,k} = {0,1,2}).  Flooring eigenvalue l at f adds (f - vol l) q q^T,
+// so the projected block is the analytic one plus those rank-1 terms.
+//
+// Lifted, each term is per vertex pair (a,b):
+//   vol A (gN_a . gN_b) I + vol B p_a p_b^T + vol lam c_a c_b^T
+//   + vol D skew(F (gN_a x gN_b)) + sum_m kappa_m r_ma r_mb^T,
+// with p_a = F gN_a, c_a = cof(F) gN_a, r_ma = Q_m gN_a.
+//
+// Output (78 values): diagonal blocks (a,a) a = 0..3 packed upper
+// (xx,xy,xz,yy,yz,zz) at 6a; off-diagonal blocks (a,b), a < b in the order
+// (0,1),(0,2),(0,3),(1,2),(1,3),(2,3), row-major at 24 + 9k.
+// --------------------------------------------------------------------------
+constexpr int kTetHessVals = 78;
+
+SK_HD int offdiag_index(int a, int b) {  // a < b
+  return a == 0 ? (b - 1) : (a == 1 ? (b + 1) : 5);
+}
+
+template <typename R, typename RS>
+SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
+                           R* U, R* s, R* V, R* W, R* lam9) {
+  // SVD in precision RS (double for nearly inverted elements)
+  RS Fs[9], Us[9], ss[3], Vs[9];
+  for (int k = 0; k < 9; ++k) Fs[k] = RS(F[k]);
+  svd3_rv(Fs, Us, ss, Vs);
+  for (int k = 0; k < 9; ++k) { U[k] = R(Us[k]); V[k] = R(Vs[k]); }
+  for (int k = 0; k < 3; ++k) s[k] = R(ss[k]);
+  // twist/flip eigenvalues, pair order (0,1)->k=2, (0,2)->k=1, (1,2)->k=0
+  lam9[0] = A + D * s[2]; lam9[1] = A - D * s[2];
+  lam9[2] = A + D * s[1]; lam9[3] = A - D * s[1];
+  lam9[4] = A + D * s[0]; lam9[5] = A - D * s[0];
+  // scaling block
+  const R c0 = s[1] * s[2], c1 = s[0] * s[2], c2 = s[0] * s[1];
+  RS S3[6];
+  S3[0] = RS(A + B * s[0] * s[0] + lam * c0 * c0);
+  S3[1] = RS(B * s[0] * s[1] + lam * c0 * c1 + D * s[2]);
+  S3[2] = RS(B * s[0] * s[2] + lam * c0 * c2 + D * s[1]);
+  S3[3] = RS(A + B * s[1] * s[1] + lam * c1 * c1);
+  S3[4] = RS(B * s[1] * s[2] + lam * c1 * c2 + D * s[0]);
+  S3[5] = RS(A + B * s[2] * s[2] + lam * c2 * c2);
+  RS evs[3], Ws[9];
+  sym3_eig(S3, evs, Ws);
+  for (int k = 0; k < 3; ++k) lam9[6 + k] = R(evs[k]);
+  for (int k = 0; k < 9; ++k) W[k] = R(Ws[k]);
+  (void)mu; (void)vol;
+}
+
+// F: deformation gradient; gN: 4x3 shape gradients; out: 78 packed values.
+// fallback_J: elements with det F below it run the SVD in FP64.
+template <typename R>
+SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1)) {
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  const R J = det3(F);
+  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+  const R den = IC + R(1);
+  const R A = mu * IC / den;
+  const R B = R(2) * mu / (den * den);
+  const R D = lam * (J - alpha);
+  R C[9];
+  cof3(F, C);
+
+  // per-vertex lifted vectors
+  R p[12], c[12];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      p[3 * a + i] = F[3 * i] * gN[3 * a] + F[3 * i + 1] * gN[3 * a + 1] + F[3 * i + 2] * gN[3 * a + 2];
+      c[3 * a + i] = C[3 * i] * gN[3 * a] + C[3 * i + 1] * gN[3 * a + 1] + C[3 * i + 2] * gN[3 * a + 2];
+    }
+  const R vA = vol * A, vB = vol * B, vL = vol * lam, vD = vol * D;
+
+  // analytic terms
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const R gg = vA * (gN[3 * a] * gN[3 * a] + gN[3 * a + 1] * gN[3 * a + 1] + gN[3 * a + 2] * gN[3 * a + 2]);
+    R* o = out + 6 * a;
+    o[0] = gg + vB * p[3 * a] * p[3 * a] + vL * c[3 * a] * c[3 * a];
+    o[1] = vB * p[3 * a] * p[3 * a + 1] + vL * c[3 * a] * c[3 * a + 1];
+    o[2] = vB * p[3 * a] * p[3 * a + 2] + vL * c[3 * a] * c[3 * a + 2];
+    o[3] = gg + vB * p[3 * a + 1] * p[3 * a + 1] + vL * c[3 * a + 1] * c[3 * a + 1];
+    o[4] = vB * p[3 * a + 1] * p[3 * a + 2] + vL * c[3 * a + 1] * c[3 * a + 2];
+    o[5] = gg + vB * p[3 * a + 2] * p[3 * a + 2] + vL * c[3 * a + 2] * c[3 * a + 2];
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a + 1; b < 4; ++b) {
+      R* o = out + 24 + 9 * offdiag_index(a, b);
+      const R* ga = gN + 3 * a;
+      const R* gb = gN + 3 * b;
+      const R gg = vA * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
+      const R n[3] = {ga[1] * gb[2] - ga[2] * gb[1], ga[2] * gb[0] - ga[0] * gb[2], ga[0] * gb[1] - ga[1] * gb[0]};
+      R w[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) w[i] = vD * (F[3 * i] * n[0] + F[3 * i + 1] * n[1] + F[3 * i + 2] * n[2]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+          o[3 * i + k] = vB * p[3 * a + i] * p[3 * b + k] + vL * c[3 * a + i] * c[3 * b + k] + (i == k ? gg : R(0));
+      // skew(w): (0,1)=w2 (0,2)=-w1 (1,0)=-w2 (1,2)=w0 (2,0)=w1 (2,1)=-w0
+      o[1] += w[2]; o[2] -= w[1];
+      o[3] -= w[2]; o[5] += w[0];
+      o[6] += w[1]; o[7] -= w[0];
+    }
+
+  // eigenvalue floor
+  R U[9], s[3], V[9], W[9], lam9[9];
+  if (J < fallback_J)
+    snh_eigensystem<R, double>(F, mu, lam, vol, A, D, B, U, s, V, W, lam9);
+  else
+    snh_eigensystem<R, R>(F, mu, lam, vol, A, D, B, U, s, V, W, lam9);
+  const R floor_v = R(kPsdFloor);
+  R beta[12];  // beta[3a + n] = v_n . gN_a
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      beta[3 * a + n] = V[n] * gN[3 * a] + V[3 + n] * gN[3 * a + 1] + V[6 + n] * gN[3 * a + 2];
+  const R rs2 = R(0.70710678118654752440);
+#pragma unroll
+  for (int m = 0; m < 9; ++m) {
+    const R kappa = floor_v - vol * lam9[m];
+    if (!(kappa > R(0))) continue;
+    R r[12];
+    if (m < 6) {
+      const int pr = m >> 1;
+      const int i = pr == 2 ? 1 : 0;
+      const int j = pr == 0 ? 1 : 2;
+      const R sg = (m & 1) ? R(1) : R(-1);  // twist: u_i b_j - u_j b_i ; flip: +
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          r[3 * a + d] = rs2 * (U[3 * d + i] * beta[3 * a + j] + sg * U[3 * d + j] * beta[3 * a + i]);
+    } else {
+      const int mm = m - 6;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          r[3 * a + d] = W[mm] * beta[3 * a] * U[3 * d] + W[3 + mm] * beta[3 * a + 1] * U[3 * d + 1] +
+                         W[6 + mm] * beta[3 * a + 2] * U[3 * d + 2];
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      R* o = out + 6 * a;
+      const R* ra = r + 3 * a;
+      o[0] += kappa * ra[0] * ra[0]; o[1] += kappa * ra[0] * ra[1]; o[2] += kappa * ra[0] * ra[2];
+      o[3] += kappa * ra[1] * ra[1]; o[4] += kappa * ra[1] * ra[2]; o[5] += kappa * ra[2] * ra[2];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = a + 1; b < 4; ++b) {
+        R* o = out + 24 + 9 * offdiag_index(a, b);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) o[3 * i + k] += kappa * r[3 * a + i] * r[3 * b + k];
+      }
+  }
+}
+
+// shape gradients from the inverse rest edge matrix: rows of Dinv are
+// gN_1..gN_3 and gN_0 = -(gN_1 + gN_2 + gN_3)
+template <typename R> SK_HD void shape_grads(const R* Dinv, R* gN) {
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    gN[3 + j] = Dinv[j];
+    gN[6 + j] = Dinv[3 + j];
+    gN[9 + j] = Dinv[6 + j];
+    gN[j] = -(Dinv[j] + Dinv[3 + j] + Dinv[6 + j]);
+  }
+}
+
+// G = [du1 du2 du3] Dinv, du_a = u_a - u_0 (edge displacement differences)
+template <typename R> SK_HD void disp_grad(const R* du, const R* Dinv, R* G) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      G[3 * i + j] = du[i] * Dinv[j] + du[3 + i] * Dinv[3 + j] + du[6 + i] * Dinv[6 + j];
+}
+
+}  // namespace skg

@@ -1,0 +1,199 @@
+"""Generate the golden fixtures of the FEM path by running simkit itself.
+
+Usage::
+
+    python tests/golden/make_golden.py [--reference /path/to/simkit/checkout] [--skip-c1]
+
+Every number stored here comes out of the reference's own functions
+(``simkit.energies.stable_neo_hookean``, ``simkit.psd_project``,
+``simkit.deformation_jacobian``, ``simkit.volume``, ``simkit.massmatrix``,
+``simkit.solvers.newton_solver``); inputs are seeded.  The rollout fixtures use
+the harness rules of ``oracle/rollout.py`` (free-DOF elimination, relative
+residual stop) with the reference's math plugged in.
+
+Fixtures written next to this script:
+
+* ``element_3d.npz`` / ``element_2d.npz``: F, mu, lam, vol -> psi, P, He, psd(vol He)
+* ``beam_small.npz``: 4x2x2 jittered beam: J (csc), vol, mass, energy/gradient/Hessian at a perturbed x
+* ``rollout_small.npz``: 6x2x2 beam, 8 backward-Euler steps (positions, iterations, residuals)
+* ``rollout_beam_8x8x32.npz``: the 12,288-tet beam, 60 steps (displacements at a few steps, energies, iterations)
+"""
+
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+
+def _import_reference(path):
+    sys.path.insert(0, path)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        import simkit  # noqa: F401
+        from simkit.energies import stable_neo_hookean as ref_snh
+        from simkit.psd_project import psd_project
+        from simkit.deformation_jacobian import deformation_jacobian
+        from simkit.volume import volume
+        from simkit.massmatrix import massmatrix
+        from simkit.solvers import newton_solver
+    return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
+                volume=volume, massmatrix=massmatrix, newton_solver=newton_solver)
+
+
+def element_cases(rng, d, t_each=32):
+    """Seeded F batches spanning rest, small/large strain, inversion and collapse."""
+    eye = np.eye(d)[None]
+    cases = [
+        np.repeat(eye, 4, axis=0),                                   # exact rest
+        eye + 0.05 * rng.standard_normal((t_each, d, d)),           # the reference test's scale
+        eye + 0.3 * rng.standard_normal((t_each, d, d)),
+        eye + 1.0 * rng.standard_normal((t_each, d, d)),
+    ]
+    inv = eye + 0.2 * rng.standard_normal((t_each, d, d))
+    inv[:, :, 0] *= -1.0                                             # inverted (J < 0)
+    cases.append(inv)
+    col = eye + 0.05 * rng.standard_normal((t_each, d, d))
+    col[:, :, -1] *= 0.05                                           # nearly collapsed (J ~ 0.05)
+    cases.append(col)
+    # random rotations times small stretch
+    q, _ = np.linalg.qr(rng.standard_normal((t_each, d, d)))
+    q *= np.sign(np.linalg.det(q))[:, None, None]
+    cases.append(q @ (eye + 0.02 * rng.standard_normal((t_each, d, d))))
+    F = np.concatenate(cases, axis=0)
+    t = F.shape[0]
+    ym = np.exp(rng.uniform(np.log(1e5), np.log(1e7), size=(t, 1)))
+    pr = rng.uniform(0.30, 0.49, size=(t, 1))
+    mu = ym / (2 * (1 + pr))
+    lam = ym * pr / ((1 + pr) * (1 - 2 * pr))
+    vol = rng.uniform(1e-7, 5e-6, size=(t, 1))
+    return F, mu, lam, vol
+
+
+def make_element(ref, d, out):
+    rng = np.random.default_rng(100 + d)
+    F, mu, lam, vol = element_cases(rng, d)
+    s = ref["snh"]
+    psi = s.stable_neo_hookean_energy_element_F(F, mu, lam)
+    P = s.stable_neo_hookean_gradient_element_F(F, mu, lam)
+    He = s.stable_neo_hookean_hessian_element_F(F, mu, lam)
+    Hp = ref["psd_project"](He * vol.reshape(-1, 1, 1))
+    np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
+
+
+def make_beam_small(ref, out):
+    from simkit_gb300.beams import make_beam
+    rng = np.random.default_rng(7)
+    t = 6 * 4 * 2 * 2
+    ym = np.exp(rng.uniform(np.log(1e5), np.log(1e7), size=t))
+    b = make_beam(4, 2, 2, ym=ym, pr=0.45, jitter=0.1, seed=11)
+    J = ref["deformation_jacobian"](b.X, b.T)
+    vol = ref["volume"](b.X, b.T)
+    M = ref["massmatrix"](b.X, b.T, b.rho)
+    x = b.X + 0.002 * rng.standard_normal(b.X.shape)
+    s = ref["snh"]
+    E = s.stable_neo_hookean_energy_x(x, J, b.mu, b.lam, vol)
+    g = s.stable_neo_hookean_gradient_x(x, J, b.mu, b.lam, vol)
+    K = s.stable_neo_hookean_hessian_x(x, J, b.mu, b.lam, vol).tocsr()
+    K.sort_indices()
+    np.savez_compressed(out, X=b.X, T=b.T, mu=b.mu, lam=b.lam, x=x,
+                        J_data=J.data, J_indices=J.indices, J_indptr=J.indptr, J_shape=np.array(J.shape),
+                        vol=vol, mass=M.diagonal(), energy=np.array(E), gradient=g,
+                        K_data=K.data, K_indices=K.indices, K_indptr=K.indptr)
+
+
+def _reference_rollout(ref, spec, dt, steps, keep=None):
+    """The oracle harness with every FEM routine and the Newton step taken from the reference."""
+    import scipy.sparse as sps
+    from oracle.rollout import BeamRollout
+
+    s = ref["snh"]
+
+    class RefRollout(BeamRollout):
+        def __init__(self):
+            super().__init__(spec.X, spec.T, spec.mu, spec.lam, spec.rho, spec.gravity,
+                             spec.pinned, dt)
+            self.J = ref["deformation_jacobian"](self.X, self.T)
+            self.vol = ref["volume"](self.X, self.T)
+            m = np.asarray(ref["massmatrix"](self.X, self.T, spec.rho).diagonal())
+            self.mass = m
+            self.f_ext = (m[:, None] * spec.gravity[None, :]).reshape(-1, 1)
+            self.M = sps.diags(np.repeat(m, 3)).tocsc()
+            self.Mf = (self.S @ self.M @ self.S.T).tocsc()
+
+        def potential(self, x):
+            return s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
+                - (self.f_ext.T @ x).item()
+
+        def potential_gradient(self, x):
+            return s.stable_neo_hookean_gradient_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
+                - self.f_ext
+
+        def potential_hessian(self, x):
+            return s.stable_neo_hookean_hessian_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
+
+        def elastic_energy(self, x):
+            return s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
+
+    r = RefRollout()
+    x_prev = r.x_rest.copy()
+    x_curr = r.x_rest.copy()
+    us, energies, iters, res_last = {}, [], [], []
+    for k in range(steps):
+        x_next, info = r.step(x_curr, x_prev, newton=ref["newton_solver"])
+        x_prev, x_curr = x_curr, x_next
+        energies.append(r.elastic_energy(x_curr))
+        iters.append(info.iters)
+        res_last.append(info.residuals[-1])
+        if keep is None or (k + 1) in keep:
+            us[k + 1] = (x_curr - r.x_rest).ravel()
+    return us, np.array(energies), np.array(iters), np.array(res_last)
+
+
+def make_rollout_small(ref, out):
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 8)
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
+                        ym=2e5, pr=0.45, dt=1.0 / 60.0)
+
+
+def make_rollout_c1(ref, out):
+    from simkit_gb300.beams import beam_small_steady
+    spec = beam_small_steady()
+    keep = (1, 2, 5, 10, 20, 30, 45, 60)
+    t0 = time.time()
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 60, keep=keep)
+    print(f"  reference 8x8x32 rollout: {time.time() - t0:.1f} s, {it.sum()} Newton iterations")
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dt=1.0 / 60.0)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE", "/root/reference"))
+    ap.add_argument("--skip-c1", action="store_true")
+    a = ap.parse_args()
+    ref = _import_reference(a.reference)
+    make_element(ref, 3, os.path.join(HERE, "element_3d.npz"))
+    make_element(ref, 2, os.path.join(HERE, "element_2d.npz"))
+    make_beam_small(ref, os.path.join(HERE, "beam_small.npz"))
+    make_rollout_small(ref, os.path.join(HERE, "rollout_small.npz"))
+    if not a.skip_c1:
+        make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

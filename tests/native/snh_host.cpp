@@ -1,0 +1,81 @@
+// Host build of the device element math (simkit_gb300/csrc/snh_math.cuh).
+// Test infrastructure: lets the CPU test suite compare the exact functions
+// the kernels run against the FP64 oracle, without a GPU.
+#include "../../simkit_gb300/csrc/snh_math.cuh"
+
+using namespace skg;
+
+template <typename R>
+static void tet_hessian_batch(int64_t t, const double* F, const double* mu, const double* lam,
+                              const double* vol, const double* gN, double* out, double fb) {
+  for (int64_t e = 0; e < t; ++e) {
+    R f[9], g[12], o[kTetHessVals];
+    for (int k = 0; k < 9; ++k) f[k] = R(F[9 * e + k]);
+    for (int k = 0; k < 12; ++k) g[k] = R(gN[12 * e + k]);
+    snh_tet_hessian<R>(f, R(mu[e]), R(lam[e]), R(vol[e]), g, o, R(fb));
+    for (int k = 0; k < kTetHessVals; ++k) out[kTetHessVals * e + k] = double(o[k]);
+  }
+}
+
+template <typename R>
+static void elem_batch(int64_t t, const double* F, const double* mu, const double* lam,
+                       double* psi, double* dpsi, double* P, double* Pd, double* H) {
+  for (int64_t e = 0; e < t; ++e) {
+    R f[9], g[9], p[9], h[81];
+    for (int k = 0; k < 9; ++k) { f[k] = R(F[9 * e + k]); g[k] = f[k] - ((k % 4 == 0) ? R(1) : R(0)); }
+    // G computed from F here; callers that care pass F = I + G exactly representable
+    psi[e] = double(snh_psi<R>(f, R(mu[e]), R(lam[e])));
+    dpsi[e] = double(snh_dpsi<R>(g, R(mu[e]), R(lam[e])));
+    snh_pk1<R>(f, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 9; ++k) P[9 * e + k] = double(p[k]);
+    snh_pk1_disp<R>(g, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 9; ++k) Pd[9 * e + k] = double(p[k]);
+    snh_hessian9<R>(f, R(mu[e]), R(lam[e]), h);
+    for (int k = 0; k < 81; ++k) H[81 * e + k] = double(h[k]);
+  }
+}
+
+template <typename R>
+static void disp_batch(int64_t t, const double* G, const double* mu, const double* lam, double* dpsi, double* Pd) {
+  for (int64_t e = 0; e < t; ++e) {
+    R g[9], p[9];
+    for (int k = 0; k < 9; ++k) g[k] = R(G[9 * e + k]);
+    dpsi[e] = double(snh_dpsi<R>(g, R(mu[e]), R(lam[e])));
+    snh_pk1_disp<R>(g, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 9; ++k) Pd[9 * e + k] = double(p[k]);
+  }
+}
+
+template <typename R>
+static void svd_batch(int64_t t, const double* F, double* U, double* s, double* V) {
+  for (int64_t e = 0; e < t; ++e) {
+    R f[9], u[9], ss[3], v[9];
+    for (int k = 0; k < 9; ++k) f[k] = R(F[9 * e + k]);
+    svd3_rv<R>(f, u, ss, v);
+    for (int k = 0; k < 9; ++k) { U[9 * e + k] = double(u[k]); V[9 * e + k] = double(v[k]); }
+    for (int k = 0; k < 3; ++k) s[3 * e + k] = double(ss[k]);
+  }
+}
+
+extern "C" {
+void h_tet_hessian(int prec, int64_t t, const double* F, const double* mu, const double* lam, const double* vol,
+                   const double* gN, double* out, double fallback_J) {
+  if (prec == 64) tet_hessian_batch<double>(t, F, mu, lam, vol, gN, out, fallback_J);
+  else tet_hessian_batch<float>(t, F, mu, lam, vol, gN, out, fallback_J);
+}
+void h_elem(int prec, int64_t t, const double* F, const double* mu, const double* lam, double* psi, double* dpsi,
+            double* P, double* Pd, double* H) {
+  if (prec == 64) elem_batch<double>(t, F, mu, lam, psi, dpsi, P, Pd, H);
+  else elem_batch<float>(t, F, mu, lam, psi, dpsi, P, Pd, H);
+}
+void h_disp(int prec, int64_t t, const double* G, const double* mu, const double* lam, double* dpsi, double* Pd) {
+  if (prec == 64) disp_batch<double>(t, G, mu, lam, dpsi, Pd);
+  else disp_batch<float>(t, G, mu, lam, dpsi, Pd);
+}
+void h_svd(int prec, int64_t t, const double* F, double* U, double* s, double* V) {
+  if (prec == 64) svd_batch<double>(t, F, U, s, V);
+  else svd_batch<float>(t, F, U, s, V);
+}
+double h_phi(double z) { return phi_log1p<double>(z); }
+float h_phi_f(float z) { return phi_log1p<float>(z); }
+}

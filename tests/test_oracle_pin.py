@@ -1,0 +1,129 @@
+"""Pin the FP64 oracle to fixtures produced by the reference itself.
+
+The fixtures under tests/golden/ were written by tests/golden/make_golden.py,
+which imports simkit and runs its functions.  Every oracle function used as a
+checker by the GPU tests is compared here first.
+"""
+
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sps
+
+from oracle import fem, psd, rollout, snh, solvers
+from simkit_gb300.beams import beam_small_steady, make_beam
+
+from conftest import GOLDEN
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("name,dim", [("element_3d.npz", 3), ("element_2d.npz", 2)])
+def test_element_tier_matches_reference(name, dim):
+    d = _load(name)
+    F, mu, lam, vol = d["F"], d["mu"], d["lam"], d["vol"]
+    assert F.shape[-1] == dim
+    scale = np.abs(d["psi"]).max()
+    assert np.abs(snh.energy_element_F(F, mu, lam) - d["psi"]).max() <= 1e-12 * scale
+    P = snh.gradient_element_F(F, mu, lam)
+    assert _rel(P, d["P"]) < 1e-12
+    He = snh.hessian_element_F(F, mu, lam)
+    # per element, relative to the element's largest entry
+    err = np.abs(He - d["He"]).max(axis=(1, 2)) / np.abs(d["He"]).max(axis=(1, 2))
+    assert err.max() < 1e-12
+    Hp = psd.psd_project(He * vol.reshape(-1, 1, 1))
+    err = np.abs(Hp - d["He_proj"]).max(axis=(1, 2)) / np.abs(d["He_proj"]).max(axis=(1, 2))
+    assert err.max() < 1e-10
+
+
+def test_beam_operators_match_reference():
+    d = _load("beam_small.npz")
+    X, T = d["X"], d["T"]
+    J = fem.deformation_jacobian(X, T)
+    Jr = sps.csc_matrix((d["J_data"], d["J_indices"], d["J_indptr"]), shape=tuple(d["J_shape"]))
+    assert J.shape == Jr.shape
+    # scipy's product leaves column indices unsorted; compare canonical forms
+    J.sort_indices()
+    Jr.sort_indices()
+    assert np.array_equal(J.indptr, Jr.indptr) and np.array_equal(J.indices, Jr.indices)
+    assert _rel(J.data, Jr.data) < 1e-12
+    vol = fem.tet_volumes(X, T)
+    assert _rel(vol, d["vol"]) < 1e-14
+    assert _rel(fem.lumped_mass(X, T, 1000.0), d["mass"]) < 1e-14
+    x = d["x"]
+    E = snh.energy_x(x, J, d["mu"], d["lam"], vol)
+    assert abs(E - float(d["energy"])) <= 1e-12 * abs(float(d["energy"]))
+    g = snh.gradient_x(x, J, d["mu"], d["lam"], vol)
+    assert _rel(g, d["gradient"]) < 1e-10
+    K = snh.hessian_x(x, J, d["mu"], d["lam"], vol)
+    K.sort_indices()
+    assert np.array_equal(K.indptr, d["K_indptr"]) and np.array_equal(K.indices, d["K_indices"])
+    assert _rel(K.data, d["K_data"]) < 1e-10
+
+
+def test_beam_generator_counts():
+    b = beam_small_steady()
+    assert b.n_tets == 12288 and b.n_verts == 2673 and b.pinned.size == 81
+    assert (fem.tet_volumes(b.X, b.T) > 0).all()
+    b2 = make_beam(3, 2, 5, jitter=0.1, seed=1)
+    assert (fem.tet_volumes(b2.X, b2.T) > 0).all()
+    assert np.all(b2.X[b2.pinned, 0] == 0.0)
+
+
+def test_rollout_small_matches_reference():
+    d = _load("rollout_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    r = rollout.from_spec(spec, dt=float(d["dt"]))
+    xs, infos = r.rollout(int(d["steps"].max()))
+    for k, s in enumerate(d["steps"]):
+        u = xs[s] - r.x_rest.ravel()
+        assert _rel(u, d["u"][k]) < 1e-8, s
+    assert [i.iters for i in infos] == list(d["iters"])
+
+
+@pytest.mark.slow
+def test_rollout_8x8x32_first_steps_match_reference():
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    r = rollout.from_spec(spec, dt=float(d["dt"]))
+    xs, infos = r.rollout(2)
+    for k, s in enumerate(d["steps"]):
+        if s > 2:
+            break
+        assert _rel(xs[s] - r.x_rest.ravel(), d["u"][k]) < 1e-8
+    assert [i.iters for i in infos] == list(d["iters"][:2])
+
+
+# behavioural tests of the oracle's solver pieces, mirroring simkit's own
+# tests/test_backtracking_line_search.py and tests/test_solvers.py
+def test_line_search_full_step_on_quadratic():
+    f = lambda x: float(0.5 * np.dot(x, x))
+    x0 = np.array([2.0, -1.0])
+    t, x, fx = solvers.backtracking_line_search(f, x0, x0.copy(), -x0)
+    assert t == 1.0 and np.allclose(x, 0) and fx == 0.0
+
+
+def test_line_search_zero_step_on_ascent():
+    f = lambda x: float(0.5 * np.dot(x, x))
+    t, x, fx = solvers.backtracking_line_search(f, np.array([0.0]), np.array([1.0]), np.array([1.0]), max_iter=5)
+    assert t == 0.0 and x[0] == 0.0
+
+
+def test_newton_exact_on_quadratic():
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((6, 6))
+    Q = A.T @ A + 6 * np.eye(6)
+    b = rng.standard_normal((6, 1))
+    x = solvers.newton_solver(np.zeros_like(b), lambda x: float((0.5 * x.T @ Q @ x + b.T @ x).item()),
+                              lambda x: Q @ x + b, lambda x: Q, max_iter=1)
+    assert np.allclose(x, -np.linalg.solve(Q, b), atol=1e-8)
