@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the backward-Euler stable neo-Hookean path on one GB300.
+
+Workload: the 32 x 32 x 128-cube beam (786,432 tets, 140,481 vertices, rest
+shape jittered by U(-0.1, 0.1) cells, Young's modulus log-uniform [1e5, 1e7]
+per tet, nu = 0.45, rho = 1000, gravity -y, x = 0 face pinned), dt = 1/60,
+Newton to 1e-6 relative residual (<= 20 iterations), FP32 element Hessians
+and SpMV with FP64 gradient, residual, dots and energy sums.
+
+A step is one Newton-converged backward-Euler step.  `value` is steps/s with
+the state resident in HBM; `e2e` is the same metric through the host-buffer
+entry point (positions copied host->device and back inside the timed region).
+Every input of the timed region (matrix 81 MB, per-tet Hessian records
+252 MB) is larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton-converged steps/s & tet-Hessians/s, plain vs batched+learned @1e-6 resid"
+WORKLOAD = "beam 32x32x128 cubes, 786,432 tets, jittered, E log-uniform [1e5,1e7], 1 instance, plain Newton"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_reference_sample(spec, newton_iters_per_step, ls_trials_per_iter, slab_cubes=6, reps=1):
+    """Time simkit's FP64 numpy/scipy algorithm (the oracle restatement) on the host.
+
+    Sample: the first `slab_cubes` layers of cubes along x of the workload beam
+    (slab_cubes * 32 * 32 * 6 tets).  Timed per Newton iteration: Hessian
+    (element Hessians, eigen floor, block_diag, J^T H J), gradient, and one
+    energy per line-search trial, scaled to the full mesh by tet count.  The
+    sparse direct solve (scipy spsolve) is NOT included - on the full mesh it
+    did not finish in 25 minutes - so the resulting steps/s is an upper bound
+    on the reference's speed.
+    """
+    from oracle import fem, snh
+    nx, ny, nz = spec.dims
+    keep_t = 6 * slab_cubes * ny * nz
+    T = spec.T[:keep_t]
+    used = np.unique(T)
+    remap = -np.ones(spec.X.shape[0], np.int64)
+    remap[used] = np.arange(used.size)
+    Ts = remap[T]
+    Xs = spec.X[used]
+    mu, lam = spec.mu[:keep_t], spec.lam[:keep_t]
+    J = fem.deformation_jacobian(Xs, Ts)
+    vol = fem.tet_volumes(Xs, Ts)
+    x = (Xs + 1e-3 * np.random.default_rng(0).standard_normal(Xs.shape)).reshape(-1, 1)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        snh.hessian_x(x, J, mu, lam, vol)
+    th = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        snh.gradient_x(x, J, mu, lam, vol)
+    tg = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        snh.energy_x(x, J, mu, lam, vol)
+    te = (time.perf_counter() - t0) / reps
+    scale = spec.n_tets / keep_t
+    per_iter = scale * (th + tg + te * max(ls_trials_per_iter, 1.0))
+    per_step = per_iter * newton_iters_per_step
+    return {
+        "steps_per_s": 1.0 / per_step,
+        "tet_hessians_per_s": keep_t / th,
+        "s_per_newton_iter_no_solve": per_iter,
+        "sample": (f"{keep_t} tets ({slab_cubes}x{ny}x{nz} cube slab) of the workload beam: Hessian "
+                   f"{th:.3f} s, gradient {tg:.3f} s, energy {te:.3f} s per call, scaled by tet count to "
+                   f"{spec.n_tets} tets and to {newton_iters_per_step:.2f} Newton iterations/step; "
+                   "spsolve excluded (did not finish on the full mesh), so steps/s is an upper bound"),
+        "cores": os.cpu_count(),
+    }
+
+
+# --------------------------------------------------------------- helpers
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def algorithmic_bytes(spec, nb):
+    n, t = spec.n_verts, spec.n_tets
+    return {
+        # SURVEY-defined tet-Hessian unit: tets 16 + shape operator 36 + material 12
+        # + positions 12 n/t + block values written once 4 * 9 nb / t
+        "tet_hessian": 16 + 36 + 12 + 12.0 * n / t + 36.0 * nb / t,
+        # one PCG iteration: block values + column indices + row pointers,
+        # SpMV p read / q write, update x r p q read + x r z write, Jacobi blocks,
+        # direction z p read + p write (12 useful bytes per vertex vector)
+        "pcg_iter": 40.0 * nb + 4.0 * (n + 1) + 24.0 * n + 84.0 * n + 36.0 * n + 36.0 * n,
+    }
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from simkit_gb300.beams import beam_large_jittered
+    spec = beam_large_jittered()
+    # per-step Newton iteration and line-search counts measured by the GPU arm on this workload
+    iters = args.ref_newton_iters
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        info = cpu_reference_sample(spec, iters, 1.0)
+        if k >= args.warmup:
+            vals.append(info["steps_per_s"])
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "fp64 numpy/scipy", "l2": "inputs larger than L2"},
+        "tet_hessians_per_s": info["tet_hessians_per_s"],
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": info["cores"], "kind": "port",
+                         "sample": info["sample"]},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--pcg-mode", type=int, default=1)
+    ap.add_argument("--pcg-rtol", type=float, default=1e-4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-newton-iters", type=float, default=4.0,
+                    help="Newton iterations per step used to scale the CPU reference sample")
+    ap.add_argument("--small", action="store_true", help="use the 8x8x32 beam (quick check)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from simkit_gb300.beams import beam_large_jittered, beam_small_steady
+    from simkit_gb300.solver import BESolver
+
+    # replicas only: every rank runs its own instance of the workload
+    spec = beam_small_steady() if args.small else beam_large_jittered(seed=rank)
+    workload = "beam 8x8x32 cubes, 12,288 tets (quick check)" if args.small else WORKLOAD
+    solver = BESolver.from_spec(spec, precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol,
+                                profile=False)
+    nb = solver.mesh.nb
+    for _ in range(args.warmup):
+        info = solver.step()
+        if not info.converged:
+            raise SystemExit(f"warm-up step did not converge: {info}")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    infos = [solver.step() for _ in range(args.steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clock_info = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    for i in infos:
+        if not i.converged:
+            raise SystemExit(f"timed step did not converge: {i}")
+    steps_total = args.steps * ws
+    value = steps_total / (ms_max / 1000.0)
+    newton = sum(i.newton_iters for i in infos)
+    pcg = sum(i.pcg_iters for i in infos)
+    launches = sum(i.launches for i in infos)
+    tet_hess_per_s = ws * newton * spec.n_tets / (ms_max / 1000.0)
+
+    # profiled pass over the same number of steps (phase times by CUDA events on the launching stream)
+    solver.params.profile = 1
+    pinfos = [solver.step() for _ in range(args.steps)]
+    solver.params.profile = 0
+    tp = {k: sum(getattr(i, f"t_{k}_ms") for i in pinfos) for k in ("hessian", "assemble", "pcg", "gradient", "energy")}
+    p_newton = sum(i.newton_iters for i in pinfos)
+    p_pcg = sum(i.pcg_iters for i in pinfos)
+    hbm, peak_kind = peaks()
+    ab = algorithmic_bytes(spec, nb)
+    pcg_ms_per_iter = tp["pcg"] / max(p_pcg, 1)
+    pcg_gbs = ab["pcg_iter"] / (pcg_ms_per_iter * 1e-3) / 1e9
+    hess_ms_per_launch = (tp["hessian"] + tp["assemble"]) / max(p_newton, 1)
+    hess_gbs = ab["tet_hessian"] * spec.n_tets / (hess_ms_per_launch * 1e-3) / 1e9
+    total_p = sum(tp.values())
+    share = {k: v / total_p for k, v in tp.items()} if total_p > 0 else {}
+    dominant = max(share, key=share.get) if share else "pcg"
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            traffic = json.load(f)
+    except Exception:
+        traffic = None
+    if dominant in ("hessian", "assemble"):
+        roof = {"bound": "hbm", "kernel": "k_tet_hessian + k_assemble", "achieved": hess_gbs, "peak": hbm,
+                "unit": "GB/s", "frac": hess_gbs / hbm,
+                "traffic": (traffic or {}).get("tet_hessian_bytes_per_launch"),
+                "algorithmic_bytes": ab["tet_hessian"] * spec.n_tets, "ms_per_launch": hess_ms_per_launch}
+    else:
+        roof = {"bound": "hbm", "kernel": "k_pcg_persistent (per PCG iteration)", "achieved": pcg_gbs, "peak": hbm,
+                "unit": "GB/s", "frac": pcg_gbs / hbm,
+                "traffic": (traffic or {}).get("pcg_bytes_per_iter"),
+                "algorithmic_bytes": ab["pcg_iter"], "ms_per_launch": pcg_ms_per_iter}
+    roof["peak_kind"] = peak_kind
+    roof["phase_share"] = share
+    roof["secondary"] = {"tet_hessian_assembly_gbs": hess_gbs, "tet_hessian_frac": hess_gbs / hbm,
+                         "pcg_gbs": pcg_gbs, "pcg_frac": pcg_gbs / hbm}
+
+    # end to end through the host-buffer entry point
+    x_curr = solver.positions().reshape(-1, 1)
+    u_prev = solver.u_prev.cpu().numpy()
+    x_prev = (spec.X.reshape(-1) + u_prev).reshape(-1, 1)
+    out = np.empty_like(x_curr)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x_next, info = solver.step_host(x_curr, x_prev, out=out)
+        x_prev, x_curr = x_curr, x_next.copy()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": steps_total / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * 3 * spec.n_verts * 8,
+           "d2h_bytes_per_step": 3 * spec.n_verts * 8}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_info = cpu_reference_sample(spec, newton / args.steps, max(1.0, sum(i.ls_trials for i in infos) / max(newton, 1)))
+        cpu = {"value": cpu_info["steps_per_s"], "unit": "steps/s", "cores": cpu_info["cores"], "kind": "port",
+               "sample": cpu_info["sample"], "tet_hessians_per_s": cpu_info["tet_hessians_per_s"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": workload, "tets": spec.n_tets, "verts": spec.n_verts, "blocks": nb,
+                       "precision": args.precision, "pcg_mode": args.pcg_mode, "pcg_rtol": args.pcg_rtol,
+                       "tol": 1e-6, "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2, no flush"},
+            "tet_hessians_per_s": tet_hess_per_s,
+            "newton_iters_per_step": newton / args.steps,
+            "pcg_iters_per_newton": pcg / max(newton, 1),
+            "gpu_launches": launches,
+            "e2e": e2e,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clock_info,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

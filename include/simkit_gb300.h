@@ -85,8 +85,8 @@ int skg_psd_project(const double* H, double* out, int64_t n, int d, int method, 
 /* Per-tet inverse rest edge matrix Dinv (rows = grad N_1..3) and signed volume.
  * Replaces the per-element D of deformation_jacobian (deformation_jacobian.py:43-61)
  * and volume/tetrahedron_volumes (volume.py:14-41, tetrahedron_volumes.py:26-27).
- * X (n,3) f64, T (t,4) i32 -> dinv (9,t) f64 SoA, vol (t) f64. Returns SKG_ERR_ARG
- * through the status buffer... no: degenerate tets yield inf entries; callers check. */
+ * X (n,3) f64, T (t,4) i32 -> dinv (9,t) f64 SoA, vol (t) f64.  A degenerate rest
+ * tet gives non-finite Dinv entries (simkit's np.linalg.inv raises instead). */
 int skg_tet_setup(const double* X, const int32_t* T, int64_t n, int64_t t, double* dinv, double* vol,
                   void* stream);
 
@@ -128,7 +128,8 @@ typedef struct skg_tet_mesh {
   const float* mat32;        /* (3,t): vol, mu, lam in FP32 */
   const int32_t* bsr_rowptr; /* (n+1) */
   const int32_t* bsr_col;    /* (nb) */
-  const int32_t* bsr_diag;   /* (n) */
+  const int32_t* bsr_diag;   /* (n) slot of the diagonal block of each row */
+  const int32_t* bsr_row;    /* (nb) block row of each slot */
   const int32_t* hc_ptr;     /* (nb+1) */
   const int32_t* hc_src;     /* (16t) */
   const int32_t* v2t_ptr;    /* (n+1) */
@@ -171,7 +172,10 @@ typedef struct skg_be_params {
   double ls_beta;           /* step factor, simkit default 0.5 */
   int32_t ls_max_iter;      /* simkit default 100 */
   int32_t pcg_mode;         /* 0 = kernel per phase, 1 = persistent cooperative kernel */
-  double ls_threshold;      /* Armijo slack, simkit default 1e-12 */
+  double ls_threshold;      /* Armijo slack, simkit default 1e-12; < 0 selects a slack
+                               scaled to the FP32 rounding of the energy sum */
+  int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */
+  int32_t reserved_;
 } skg_be_params;
 
 typedef struct skg_be_state {
@@ -192,6 +196,13 @@ typedef struct skg_step_info {
   double residual;          /* final ||g|| / residual0 */
   double min_alpha;         /* smallest accepted step */
   double energy;            /* final incremental potential relative to rest */
+  int32_t launches;         /* kernels launched by the step */
+  int32_t reserved_;
+  double t_hessian_ms;      /* per-phase device time, filled when params->profile */
+  double t_assemble_ms;
+  double t_pcg_ms;
+  double t_gradient_ms;
+  double t_energy_ms;
 } skg_step_info;
 
 int64_t skg_be_workspace_size(const skg_tet_mesh* mesh, int precision);

@@ -153,7 +153,15 @@ def hessian_x(x, J, mu, lam, vol, psd: bool = True):
     He = hessian_element_F(F, mu, lam) * np.asarray(vol).reshape(-1, 1, 1)
     if psd:
         He = psd_project(He)
-    return (J.T @ sps.block_diag(He) @ J).tocsr()
+    return (J.T @ _block_diag(He) @ J).tocsr()
+
+
+def _block_diag(He):
+    """scipy block_diag of a (t, k, k) stack, as snh.py:536 builds it."""
+    t, k, _ = He.shape
+    r = (np.arange(t)[:, None, None] * k + np.arange(k)[None, :, None]).repeat(k, axis=2)
+    c = (np.arange(t)[:, None, None] * k + np.arange(k)[None, None, :]).repeat(k, axis=1)
+    return sps.csr_matrix((He.ravel(), (r.ravel(), c.ravel())), shape=(t * k, t * k))
 
 
 def element_hessians_projected(x, J, mu, lam, vol) -> np.ndarray:

@@ -1,0 +1,33 @@
+"""simkit_gb300: GB300-native backward-Euler stable neo-Hookean FEM path.
+
+A drop-in for the hot path of otmanon/simkit: the same Python signatures for
+the stable neo-Hookean energy tiers, deformation_jacobian, volume,
+psd_project, backtracking_line_search, newton_solver and backward_euler, with
+the arithmetic in hand-written sm_103a CUDA kernels behind a ctypes C ABI
+(include/simkit_gb300.h).  ``BESolver`` runs whole backward-Euler steps on
+the device.
+"""
+
+from .beams import BeamSpec, beam_batch, beam_large_jittered, beam_small_steady, make_beam  # noqa: F401
+
+_API = {
+    "stable_neo_hookean_energy_element_F", "stable_neo_hookean_gradient_element_F",
+    "stable_neo_hookean_hessian_element_F", "stable_neo_hookean_energy_x", "stable_neo_hookean_gradient_x",
+    "stable_neo_hookean_hessian_x", "stable_neo_hookean_energy", "stable_neo_hookean_gradient",
+    "stable_neo_hookean_hessian", "psd_project", "deformation_jacobian", "volume", "backtracking_line_search",
+    "newton_solver", "backward_euler", "solve_sparse", "BlockMatrix", "DeformationJacobian",
+}
+
+
+def __getattr__(name):
+    # torch and the CUDA library load on first use of an entry point
+    if name in _API:
+        from . import api
+        return getattr(api, name)
+    if name == "BESolver":
+        from .solver import BESolver
+        return BESolver
+    if name == "TetMesh":
+        from .mesh import TetMesh
+        return TetMesh
+    raise AttributeError(name)

@@ -1,0 +1,144 @@
+"""ctypes binding of the C ABI declared in include/simkit_gb300.h.
+
+The shared library is built in-tree (``__graft_entry__.build()`` or
+``python -m simkit_gb300.build``) into ``simkit_gb300/_build/``.  Every
+product entry point of the package goes through this binding; if the library
+is missing the first call raises ``RuntimeError`` - there is no CPU
+fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsimkit_gb300.so")
+
+c_i32 = ctypes.c_int32
+c_i64 = ctypes.c_int64
+c_dbl = ctypes.c_double
+c_vp = ctypes.c_void_p
+
+SKG_OK = 0
+SKG_ERR_ARG = -1
+SKG_ERR_CUDA = -2
+SKG_ERR_NOT_CONVERGED = -3
+SKG_ERR_LINESEARCH = -4
+SKG_ERR_NONFINITE = -5
+SKG_ERR_TIMEOUT = -6
+SKG_ERR_CAPACITY = -7
+
+SKG_FP64 = 0
+SKG_MIXED = 1
+
+STATUS_NAMES = {
+    SKG_OK: "ok", SKG_ERR_ARG: "invalid argument", SKG_ERR_CUDA: "CUDA error",
+    SKG_ERR_NOT_CONVERGED: "not converged", SKG_ERR_LINESEARCH: "line search exhausted",
+    SKG_ERR_NONFINITE: "non-finite value", SKG_ERR_TIMEOUT: "grid wait timed out",
+    SKG_ERR_CAPACITY: "capacity exceeded",
+}
+
+
+class TetMeshC(ctypes.Structure):
+    _fields_ = [
+        ("n_verts", c_i64), ("n_tets", c_i64), ("n_blocks", c_i64),
+        ("tets", c_vp), ("dinv", c_vp), ("dinv32", c_vp), ("vol", c_vp), ("mu", c_vp), ("lam", c_vp),
+        ("mat32", c_vp), ("bsr_rowptr", c_vp), ("bsr_col", c_vp), ("bsr_diag", c_vp), ("bsr_row", c_vp),
+        ("hc_ptr", c_vp), ("hc_src", c_vp), ("v2t_ptr", c_vp), ("v2t", c_vp),
+    ]
+
+
+class BEParamsC(ctypes.Structure):
+    _fields_ = [
+        ("dt", c_dbl), ("tol", c_dbl), ("max_newton", c_i32), ("precision", c_i32), ("pcg_rtol", c_dbl),
+        ("pcg_max_iter", c_i32), ("do_line_search", c_i32), ("ls_alpha", c_dbl), ("ls_beta", c_dbl),
+        ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
+        ("reserved_", c_i32),
+    ]
+
+
+class BEStateC(ctypes.Structure):
+    _fields_ = [("u", c_vp), ("u_curr", c_vp), ("u_prev", c_vp), ("mass", c_vp), ("f_ext", c_vp), ("pinned", c_vp)]
+
+
+class StepInfoC(ctypes.Structure):
+    _fields_ = [
+        ("newton_iters", c_i32), ("pcg_iters", c_i32), ("ls_trials", c_i32), ("status", c_i32),
+        ("residual0", c_dbl), ("residual", c_dbl), ("min_alpha", c_dbl), ("energy", c_dbl),
+        ("launches", c_i32), ("reserved_", c_i32), ("t_hessian_ms", c_dbl), ("t_assemble_ms", c_dbl),
+        ("t_pcg_ms", c_dbl), ("t_gradient_ms", c_dbl), ("t_energy_ms", c_dbl),
+    ]
+
+
+P = ctypes.POINTER
+_SIGNATURES = {
+    "skg_version": (c_i32, []),
+    "skg_last_error": (c_i32, [ctypes.c_char_p, ctypes.c_size_t]),
+    "skg_snh_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_snh_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_snh_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_psd_project": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
+    "skg_tet_setup": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "skg_tet_deformation_gradient": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "skg_tet_gradient_scatter": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp]),
+    "skg_pattern_build": (c_i32, [c_vp, c_i64, c_i64, P(c_i64), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "skg_assembly_workspace_size": (c_i64, [P(TetMeshC), c_i32]),
+    "skg_snh_energy_x": (c_i32, [P(TetMeshC), c_vp, P(c_dbl), c_vp, c_vp]),
+    "skg_snh_gradient_x": (c_i32, [P(TetMeshC), c_vp, c_vp, c_vp, c_vp]),
+    "skg_snh_hessian_x": (c_i32, [P(TetMeshC), c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "skg_be_workspace_size": (c_i64, [P(TetMeshC), c_i32]),
+    "skg_be_step": (c_i32, [P(TetMeshC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC), c_vp]),
+    "skg_pcg_workspace_size": (c_i64, [c_i64]),
+    "skg_pcg_bsr64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp, c_vp]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def exported_symbols():
+    """Names the header declares (used by the ABI tests)."""
+    return list(_SIGNATURES)
+
+
+def load():
+    """Load the in-tree library; raise RuntimeError if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(
+                    f"simkit_gb300: CUDA library not built ({LIB_PATH} missing); run "
+                    "`python -c 'import __graft_entry__ as g; g.build()'` first. There is no CPU fallback.")
+            lib = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+class SimkitGpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    load().skg_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int):
+    if status != SKG_OK:
+        msg = last_error()
+        if status == SKG_ERR_ARG:
+            raise ValueError(msg)
+        raise SimkitGpuError(status, msg)
+    return status

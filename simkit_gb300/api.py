@@ -1,0 +1,405 @@
+"""simkit-compatible entry points of the FEM path, computed on the GPU.
+
+Each function keeps the signature, argument meaning, return types and error
+behaviour of the simkit function it replaces (cited per function).  numpy
+inputs give numpy / scipy outputs, like simkit; torch CUDA tensors stay on the
+device.  All arithmetic runs in the CUDA library (``_lib``); there is no CPU
+fallback - without the library every call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+import scipy.sparse as sps
+import torch
+
+from . import _lib
+from ._lib import SKG_FP64, SKG_MIXED, check
+from .mesh import TetMesh, _ptr, _stream_ptr
+
+_PREC = {"fp64": SKG_FP64, "mixed": SKG_MIXED, "fp32": SKG_MIXED}
+
+
+def _dev(a):
+    """FP64 contiguous CUDA tensor from a numpy array, list or tensor."""
+    if isinstance(a, torch.Tensor):
+        return a.to(device="cuda", dtype=torch.float64).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64))).to("cuda")
+
+
+def _out(t: torch.Tensor, like):
+    return t if isinstance(like, torch.Tensor) else t.cpu().numpy()
+
+
+# --------------------------------------------------------------------------- #
+# element tier: simkit/energies/stable_neo_hookean.py:65-443                  #
+# --------------------------------------------------------------------------- #
+def _elem(fn, F, mu, lam, shape_of, precision):
+    d = F.shape[-1]
+    if d not in (2, 3):
+        raise ValueError("Stable Neo-Hookean supports dim=2 or dim=3")
+    Fd = _dev(F).reshape(-1, d, d)
+    t = Fd.shape[0]
+    mud = _dev(mu).reshape(-1)
+    lamd = _dev(lam).reshape(-1)
+    out = torch.empty(shape_of(t, d), dtype=torch.float64, device="cuda")
+    check(getattr(_lib.load(), fn)(d, _PREC[precision], _ptr(Fd), _ptr(mud), _ptr(lamd), _ptr(out), t, _stream_ptr()))
+    return _out(out, F)
+
+
+def stable_neo_hookean_energy_element_F(F, mu, lam, precision: str = "fp64"):
+    """psi per element, (t, 1).  simkit ``stable_neo_hookean_energy_element_F`` (snh.py:65-129)."""
+    return _elem("skg_snh_energy_element_F", F, mu, lam, lambda t, d: (t, 1), precision)
+
+
+def stable_neo_hookean_gradient_element_F(F, mu, lam, precision: str = "fp64"):
+    """PK1 per element, (t, d, d).  simkit ``stable_neo_hookean_gradient_element_F`` (snh.py:132-218)."""
+    return _elem("skg_snh_gradient_element_F", F, mu, lam, lambda t, d: (t, d, d), precision)
+
+
+def stable_neo_hookean_hessian_element_F(F, mu, lam, precision: str = "fp64"):
+    """(t, d*d, d*d) unprojected blocks.  simkit ``stable_neo_hookean_hessian_element_F`` (snh.py:221-443)."""
+    return _elem("skg_snh_hessian_element_F", F, mu, lam, lambda t, d: (t, d * d, d * d), precision)
+
+
+# --------------------------------------------------------------------------- #
+# psd_project: simkit/psd_project.py:12-47                                    #
+# --------------------------------------------------------------------------- #
+def psd_project(H, method: str = "proj"):
+    """Floor (``'proj'``, 1e-6) or take |.| (``'abs'``) of each block's eigenvalues."""
+    if method not in ("proj", "abs"):
+        raise ValueError("method must be 'proj' or 'abs'")
+    Hd = _dev(H)
+    if Hd.ndim == 2:
+        Hd = Hd[None]
+    n, d, _ = Hd.shape
+    out = torch.empty_like(Hd)
+    check(_lib.load().skg_psd_project(_ptr(Hd), _ptr(out), n, d, 0 if method == "proj" else 1, _stream_ptr()))
+    return _out(out, H)
+
+
+# --------------------------------------------------------------------------- #
+# deformation Jacobian as a device operator                                   #
+# --------------------------------------------------------------------------- #
+class DeformationJacobian:
+    """The per-tet operator behind simkit's sparse J (deformation_jacobian.py:9-87).
+
+    ``J @ x`` gives the stacked F (9t, 1); ``J.T @ y`` gives the vertex gather
+    (3n, 1); ``to_scipy()`` builds the same csc matrix simkit returns.
+    """
+
+    def __init__(self, X, T):
+        X = np.asarray(X, dtype=np.float64)
+        T = np.asarray(T)
+        if X.shape[1] != 3 or T.shape[1] != 4:
+            raise ValueError("the GPU deformation Jacobian supports tetrahedra in 3D")
+        self.mesh = TetMesh(X, T, np.ones(T.shape[0]), np.ones(T.shape[0]))
+        self.shape = (9 * T.shape[0], 3 * X.shape[0])
+
+    @property
+    def T(self):
+        return _Transposed(self)
+
+    def transpose(self):
+        return _Transposed(self)
+
+    def __matmul__(self, x):
+        m = self.mesh
+        xd = _dev(x).reshape(-1)
+        if xd.numel() != 3 * m.n:
+            raise ValueError("dimension mismatch")
+        F = torch.empty(9 * m.t, dtype=torch.float64, device="cuda")
+        check(_lib.load().skg_tet_deformation_gradient(_ptr(m.tets), _ptr(m.dinv), _ptr(xd), m.t, _ptr(F),
+                                                       _stream_ptr()))
+        return _out(F.reshape(-1, 1), x)
+
+    def to_scipy(self) -> sps.csc_matrix:
+        m = self.mesh
+        t = m.t
+        D = m.dinv.cpu().numpy().reshape(9, t).T.reshape(t, 3, 3)    # rows = grad N_1..3
+        G = np.empty((t, 4, 3))
+        G[:, 1:] = D
+        G[:, 0] = -D.sum(axis=1)
+        T = m.T_host.astype(np.int64)
+        e = np.arange(t)[:, None, None, None]
+        i = np.arange(3)[None, :, None, None]
+        j = np.arange(3)[None, None, :, None]
+        rows = np.broadcast_to(9 * e + 3 * i + j, (t, 3, 3, 4))
+        cols = np.broadcast_to(3 * T[:, None, None, :] + i, (t, 3, 3, 4))
+        vals = np.broadcast_to(G.transpose(0, 2, 1)[:, None, :, :], (t, 3, 3, 4))
+        J = sps.csc_matrix((vals.ravel(), (rows.ravel(), cols.ravel())), shape=self.shape)
+        J.eliminate_zeros()
+        return J
+
+    tocsc = to_scipy
+
+
+class _Transposed:
+    def __init__(self, J):
+        self.J = J
+        self.shape = (J.shape[1], J.shape[0])
+
+    def __matmul__(self, y):
+        m = self.J.mesh
+        yd = _dev(y).reshape(-1)
+        if yd.numel() != 9 * m.t:
+            raise ValueError("dimension mismatch")
+        out = torch.empty(3 * m.n, dtype=torch.float64, device="cuda")
+        check(_lib.load().skg_tet_gradient_scatter(_ptr(m.tets), _ptr(m.dinv), _ptr(yd), _ptr(m.v2t_ptr),
+                                                   _ptr(m.v2t), m.n, m.t, _ptr(out), _stream_ptr()))
+        return _out(out.reshape(-1, 1), y)
+
+
+def deformation_jacobian(X, T) -> DeformationJacobian:
+    """GPU operator for simkit ``deformation_jacobian`` (deformation_jacobian.py:9-87)."""
+    return DeformationJacobian(X, T)
+
+
+def volume(X, T):
+    """Signed tet volumes (t, 1).  simkit ``volume`` (volume.py:14-41) for tets."""
+    T = np.asarray(T)
+    if T.shape[1] != 4:
+        raise ValueError("the GPU volume supports tetrahedra")
+    Xd = _dev(X).reshape(-1)
+    Td = torch.from_numpy(np.ascontiguousarray(T.astype(np.int32))).cuda()
+    t = T.shape[0]
+    dinv = torch.empty(9 * t, dtype=torch.float64, device="cuda")
+    vol = torch.empty(t, dtype=torch.float64, device="cuda")
+    check(_lib.load().skg_tet_setup(_ptr(Xd), _ptr(Td), Xd.numel() // 3, t, _ptr(dinv), _ptr(vol), _stream_ptr()))
+    return _out(vol.reshape(-1, 1), X)
+
+
+# --------------------------------------------------------------------------- #
+# assembled tier: simkit/energies/stable_neo_hookean.py:449-538               #
+# --------------------------------------------------------------------------- #
+def _operator(J) -> TetMesh:
+    if isinstance(J, DeformationJacobian):
+        return J.mesh
+    raise TypeError("pass the operator returned by simkit_gb300.deformation_jacobian")
+
+
+def _bind(J, mu, lam, vol) -> TetMesh:
+    m = _operator(J)
+    m.set_material(mu, lam, vol)
+    return m
+
+
+def stable_neo_hookean_energy_x(X, J, mu, lam, vol) -> float:
+    """sum vol psi(J x).  simkit ``stable_neo_hookean_energy_x`` (snh.py:449-474)."""
+    m = _bind(J, mu, lam, vol)
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    e = ctypes.c_double()
+    check(_lib.load().skg_snh_energy_x(ctypes.byref(m.c), _ptr(x), ctypes.byref(e), _ptr(ws), _stream_ptr()))
+    return float(e.value)
+
+
+def stable_neo_hookean_gradient_x(X, J, mu, lam, vol):
+    """J^T vec(vol P), (3n, 1).  simkit ``stable_neo_hookean_gradient_x`` (snh.py:477-503)."""
+    m = _bind(J, mu, lam, vol)
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    g = torch.empty(3 * m.n, dtype=torch.float64, device="cuda")
+    check(_lib.load().skg_snh_gradient_x(ctypes.byref(m.c), _ptr(x), _ptr(g), _ptr(ws), _stream_ptr()))
+    return _out(g.reshape(-1, 1), X)
+
+
+def assemble_hessian_blocks(mesh: TetMesh, X, precision="fp64", psd=True) -> torch.Tensor:
+    """Block values (entry-major layout) of J^T blockdiag(psd(vol He)) J on the device."""
+    prec = _PREC[precision]
+    x = _dev(X).reshape(-1)
+    ws = mesh.workspace(prec)
+    if prec == SKG_FP64:
+        val = torch.empty(9 * mesh.nb, dtype=torch.float64, device="cuda")
+        check(_lib.load().skg_snh_hessian_x(ctypes.byref(mesh.c), _ptr(x), prec, int(psd), _ptr(val), None, _ptr(ws),
+                                            _stream_ptr()))
+    else:
+        val = torch.empty(9 * mesh.nb, dtype=torch.float32, device="cuda")
+        check(_lib.load().skg_snh_hessian_x(ctypes.byref(mesh.c), _ptr(x), prec, int(psd), None, _ptr(val), _ptr(ws),
+                                            _stream_ptr()))
+    return val
+
+
+class BlockMatrix:
+    """Assembled 3x3-block symmetric matrix resident on the GPU."""
+
+    def __init__(self, mesh: TetMesh, val: torch.Tensor):
+        self.mesh = mesh
+        self.val = val
+        self.shape = (3 * mesh.n, 3 * mesh.n)
+
+    def to_scipy(self) -> sps.csr_matrix:
+        return self.mesh.block_values_to_csr(self.val)
+
+    tocsr = to_scipy
+
+    def tocsc(self):
+        return self.to_scipy().tocsc()
+
+
+def stable_neo_hookean_hessian_x(X, J, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(psd(vol He)) J.  simkit ``stable_neo_hookean_hessian_x`` (snh.py:506-538).
+
+    numpy input returns a scipy sparse matrix like simkit; torch input returns
+    a device ``BlockMatrix``.
+    """
+    m = _bind(J, mu, lam, vol)
+    val = assemble_hessian_blocks(m, X, precision=precision, psd=psd)
+    B = BlockMatrix(m, val)
+    return B if isinstance(X, torch.Tensor) else B.to_scipy()
+
+
+def stable_neo_hookean_energy(X, T, mu, lam, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``stable_neo_hookean_energy`` (snh.py:654-679)."""
+    J = deformation_jacobian(X, T)
+    return stable_neo_hookean_energy_x(X if U is None else U, J, mu, lam, volume(X, T))
+
+
+def stable_neo_hookean_gradient(X, T, mu, lam, U: Optional[np.ndarray] = None):
+    """simkit ``stable_neo_hookean_gradient`` (snh.py:682-707)."""
+    J = deformation_jacobian(X, T)
+    return stable_neo_hookean_gradient_x(X if U is None else U, J, mu, lam, volume(X, T))
+
+
+def stable_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``stable_neo_hookean_hessian`` (snh.py:710-737)."""
+    J = deformation_jacobian(X, T)
+    return stable_neo_hookean_hessian_x(X if U is None else U, J, mu, lam, volume(X, T), psd=psd)
+
+
+# --------------------------------------------------------------------------- #
+# linear solve standing in for spsolve (simkit/solvers/newton.py:52)           #
+# --------------------------------------------------------------------------- #
+def solve_sparse(A, b, rtol: float = 1e-12, max_iter: int = 20000):
+    """x = A^{-1} b for symmetric positive definite A by FP64 block-Jacobi PCG on the GPU.
+
+    A may be a scipy sparse matrix, a dense array or a ``BlockMatrix``.
+    """
+    if isinstance(A, BlockMatrix):
+        A = A.to_scipy()
+    if not sps.issparse(A):
+        A = sps.csr_matrix(np.asarray(A, dtype=np.float64))
+    n = A.shape[0]
+    npad = (-n) % 3
+    A = sps.csr_matrix(A, dtype=np.float64)
+    if npad:
+        A = sps.block_diag([A, sps.identity(npad)], format="csr")
+    N = A.shape[0]
+    nbr = N // 3
+    Ab = sps.bsr_matrix(A, blocksize=(3, 3))
+    Ab.sort_indices()
+    # every block row needs its diagonal block
+    rowptr = Ab.indptr.astype(np.int64)
+    cols = Ab.indices.astype(np.int64)
+    data = Ab.data
+    has_diag = np.zeros(nbr, bool)
+    rows_of = np.repeat(np.arange(nbr), np.diff(rowptr))
+    has_diag[rows_of[cols == rows_of]] = True
+    if not has_diag.all():
+        Ab = sps.bsr_matrix(Ab + sps.bsr_matrix((np.zeros((nbr, 3, 3)), np.arange(nbr), np.arange(nbr + 1)),
+                                                shape=Ab.shape), blocksize=(3, 3))
+        Ab.sort_indices()
+        rowptr = Ab.indptr.astype(np.int64)
+        cols = Ab.indices.astype(np.int64)
+        data = Ab.data
+        rows_of = np.repeat(np.arange(nbr), np.diff(rowptr))
+    K = np.diff(rowptr)
+    kloc = np.arange(cols.size) - rowptr[rows_of]
+    val = np.empty(9 * cols.size)
+    for m_ in range(9):
+        val[9 * rowptr[rows_of] + m_ * K[rows_of] + kloc] = data[:, m_ // 3, m_ % 3]
+    bb = np.zeros(N)
+    bv = b.reshape(-1) if not isinstance(b, torch.Tensor) else b.detach().cpu().numpy().reshape(-1)
+    bb[:n] = bv
+    lib = _lib.load()
+    rp_d = torch.from_numpy(rowptr.astype(np.int32)).cuda()
+    col_d = torch.from_numpy(cols.astype(np.int32)).cuda()
+    val_d = torch.from_numpy(val).cuda()
+    b_d = torch.from_numpy(bb).cuda()
+    x_d = torch.empty(N, dtype=torch.float64, device="cuda")
+    ws = torch.empty(int(lib.skg_pcg_workspace_size(nbr)), dtype=torch.uint8, device="cuda")
+    iters = ctypes.c_int32()
+    check(lib.skg_pcg_bsr64(nbr, _ptr(rp_d), _ptr(col_d), _ptr(val_d), _ptr(b_d), _ptr(x_d), rtol, max_iter,
+                            ctypes.byref(iters), _ptr(ws), _stream_ptr()))
+    x = x_d[:n].reshape(-1, 1)
+    return x if isinstance(b, torch.Tensor) else x.cpu().numpy()
+
+
+# --------------------------------------------------------------------------- #
+# line search / Newton / backward Euler                                       #
+# --------------------------------------------------------------------------- #
+def backtracking_line_search(f, x0, g, dx, alpha: float = 0.01, beta: float = 0.5, max_iter: int = 100,
+                             threshold: float = 1e-12):
+    """simkit ``backtracking_line_search`` (backtracking_line_search.py:8-67), same contract:
+    returns (t, x0 + t dx, f) for the first t = beta^k passing Armijo, else (0, x0, f(x0))."""
+    assert alpha > 0 and alpha <= 0.5
+    assert beta > 0 and beta < 1
+    assert np.ndim(x0) == np.ndim(dx)
+    t = 1.0
+    fx0 = f(x0)
+    slope = g.T @ dx
+    for _ in range(max_iter):
+        x = x0 + t * dx
+        fx = f(x)
+        if fx <= fx0 + alpha * t * slope + threshold:
+            return t, x, fx
+        t = beta * t
+    return 0.0, x0, fx0
+
+
+def newton_solver(x0, energy_func, gradient_func, hessian_func, tolerance=1e-6, max_iter=1, do_line_search=True,
+                  return_info=False):
+    """simkit ``newton_solver`` (solvers/newton.py:7-75) with the linear solve on the GPU.
+
+    ``spsolve(H, -g)`` (newton.py:52) is replaced by block-Jacobi PCG to a
+    relative residual of 1e-12 in FP64.
+    """
+    x = x0.copy() if not isinstance(x0, torch.Tensor) else x0.clone()
+    if return_info:
+        info = {"g": [], "dx": [], "alphas": [], "iters": -1}
+    for i in range(max_iter):
+        g = gradient_func(x)
+        H = hessian_func(x)
+        dx = solve_sparse(H, -g).reshape(-1, 1)
+        if do_line_search:
+            alpha, _, _ = backtracking_line_search(energy_func, x, g, dx)
+        else:
+            alpha = 1.0
+        x += alpha * dx
+        if return_info:
+            info["g"].append(g)
+            info["dx"].append(dx)
+            info["alphas"].append(alpha)
+            info["iters"] = i
+        nrm = float(torch.linalg.norm(alpha * dx)) if isinstance(dx, torch.Tensor) else float(np.linalg.norm(alpha * dx))
+        if nrm < tolerance:
+            break
+    if return_info:
+        return x, info
+    return x
+
+
+def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, h, tolerance: float = 1e-6,
+                   max_iter: int = 1, do_line_search: bool = True, return_info: bool = False):
+    """simkit ``backward_euler`` (integrators/backward_euler.py:27-91): minimise
+    V(x) + 1/(2h^2) (x - x~)^T M (x - x~), x~ = 2 x_curr - x_prev, by ``newton_solver``."""
+    x_tilde = x_curr + h * ((x_curr - x_prev) / h)
+
+    def energy(x):
+        d = x - x_tilde
+        return energy_func(x) + float((0.5 * (d.T @ (M @ d)) / h ** 2).item())
+
+    def gradient(x):
+        return gradient_func(x) + (M @ (x - x_tilde)) / h ** 2
+
+    def hessian(x):
+        H = hessian_func(x)
+        if isinstance(H, BlockMatrix):
+            H = H.to_scipy()
+        return H + M / h ** 2
+
+    return newton_solver(x_tilde, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
+                         do_line_search=do_line_search, return_info=return_info)

@@ -1,0 +1,484 @@
+// Assembled tier of the FEM path: per-tet Hessians with the analytic PSD
+// floor, deterministic gather-assembly into the block pattern, FP64 vertex
+// forces and the line-search energy.
+//
+// Data layout in HBM (t tets, n vertices, nb 3x3 blocks):
+//   tets        int4[t]
+//   dinv        R[9][t]   SoA, row c of the 3x3 = grad N_{c+1}
+//   vol/mu/lam  R[t]      (FP32 copies packed as mat32[3][t])
+//   hbuf        R[t][80]  per-tet lifted Hessian, 78 packed values + 2 pad
+//   fbuf        f64[t][12] per-tet vertex forces
+//   val         R[9 nb]   block values, entry-major inside each block row
+//   u           f64[3n]   displacement from rest (or absolute positions)
+//   uh, ul      f32[n][4] hi/lo split of u for FP32 kernels
+#include "assembly.cuh"
+#include "snh_math.cuh"
+
+namespace skg {
+
+// --------------------------------------------------------- tet gathers ---
+// edge displacement differences du[3(a-1)+i] = u_a,i - u_0,i
+__device__ __forceinline__ void tet_du(const double* __restrict__ u, int4 v, double* du) {
+  const int vv[3] = {v.y, v.z, v.w};
+  const double u0 = u[3 * (int64_t)v.x], u1 = u[3 * (int64_t)v.x + 1], u2 = u[3 * (int64_t)v.x + 2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    du[3 * a + 0] = u[3 * (int64_t)vv[a] + 0] - u0;
+    du[3 * a + 1] = u[3 * (int64_t)vv[a] + 1] - u1;
+    du[3 * a + 2] = u[3 * (int64_t)vv[a] + 2] - u2;
+  }
+}
+
+// FP32 differences from the hi/lo split: (h_a - h_0) + (l_a - l_0) is
+// accurate to FP32 relative precision of the difference itself.
+__device__ __forceinline__ void tet_du(const float* __restrict__ uh, const float* __restrict__ ul, int4 v,
+                                       float* du) {
+  const Vec3<float> h0 = ld3(uh, v.x), l0 = ld3(ul, v.x);
+  const int vv[3] = {v.y, v.z, v.w};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const Vec3<float> h = ld3(uh, vv[a]), l = ld3(ul, vv[a]);
+    du[3 * a + 0] = (h.x - h0.x) + (l.x - l0.x);
+    du[3 * a + 1] = (h.y - h0.y) + (l.y - l0.y);
+    du[3 * a + 2] = (h.z - h0.z) + (l.z - l0.z);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void load_dinv(const R* __restrict__ dinv, int64_t t, int64_t e, R* D) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) D[k] = __ldg(dinv + k * t + e);
+}
+
+// -------------------------------------------------------- tet Hessians ---
+template <typename R>
+__global__ void __launch_bounds__(128) k_tet_hessian(TetArgs<R> a, int disp, int project, R* __restrict__ hbuf) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.t) return;
+  const int4 v = __ldg(a.tets + e);
+  R du[9], D[9], G[9], gN[12], out[kTetHessVals];
+  if constexpr (sizeof(R) == 8) {
+    tet_du(a.u, v, du);
+  } else {
+    tet_du(a.uh, a.ul, v, du);
+  }
+  load_dinv(a.dinv, a.t, e, D);
+  disp_grad(du, D, G);
+  if (disp) {
+    G[0] += R(1);
+    G[4] += R(1);
+    G[8] += R(1);
+  }
+  shape_grads(D, gN);
+  const R vol = __ldg(a.vol + e), mu = __ldg(a.mu + e), lam = __ldg(a.lam + e);
+  snh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0);
+  R* o = hbuf + (int64_t)kHStride * e;
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int k = 0; k < kTetHessVals / 2; ++k)
+      reinterpret_cast<float2*>(o)[k] = make_float2(out[2 * k], out[2 * k + 1]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < kTetHessVals / 2; ++k)
+      reinterpret_cast<double2*>(o)[k] = make_double2(out[2 * k], out[2 * k + 1]);
+  }
+}
+
+// ------------------------------------------------------------ assembly ---
+// One thread per block slot: sum the slot's per-tet blocks in list order,
+// add the lumped mass / h^2 on diagonal blocks, apply pinned rows/columns
+// (identity on the diagonal, zero elsewhere) and, for diagonal slots, write
+// the inverse of the 3x3 block for the block-Jacobi preconditioner.
+template <typename R>
+__global__ void k_assemble(AsmArgs<R> a) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= a.nb) return;
+  const int v = __ldg(a.bsr_row + s);
+  const int w = __ldg(a.bsr_col + s);
+  const int rp = __ldg(a.rowptr + v);
+  const int K = __ldg(a.rowptr + v + 1) - rp;
+  const int k = (int)(s - rp);
+  R acc[9];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) acc[m] = R(0);
+  const int c0 = __ldg(a.hc_ptr + s), c1 = __ldg(a.hc_ptr + s + 1);
+  for (int c = c0; c < c1; ++c) {
+    const int code = __ldg(a.hc_src + c);
+    const int64_t e = code >> 4;
+    const int cd = code & 15;
+    const R* h = a.hbuf + (int64_t)kHStride * e;
+    if (cd < 4) {
+      const R* d = h + 6 * cd;
+      const R d0 = d[0], d1 = d[1], d2 = d[2], d3 = d[3], d4 = d[4], d5 = d[5];
+      acc[0] += d0; acc[1] += d1; acc[2] += d2;
+      acc[3] += d1; acc[4] += d3; acc[5] += d4;
+      acc[6] += d2; acc[7] += d4; acc[8] += d5;
+    } else if (cd < 10) {
+      const R* b = h + 24 + 9 * (cd - 4);
+#pragma unroll
+      for (int m = 0; m < 9; ++m) acc[m] += b[m];
+    } else {
+      const R* b = h + 24 + 9 * (cd - 10);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc[3 * i + j] += b[3 * j + i];
+    }
+  }
+  if (v == w && a.mass) {
+    const R m = R(a.mass[v] * a.inv_h2);
+    acc[0] += m; acc[4] += m; acc[8] += m;
+  }
+  if (a.pinned) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (a.pinned[3 * v + i] | a.pinned[3 * w + j]) acc[3 * i + j] = (v == w && i == j) ? R(1) : R(0);
+  }
+  R* dst = a.val + 9 * (int64_t)rp + k;
+#pragma unroll
+  for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+  if (v == w && a.jinv) {
+    R C[9];
+    cof3(acc, C);
+    const R det = acc[0] * C[0] + acc[1] * C[1] + acc[2] * C[2];
+    R* ji = a.jinv + 9 * (int64_t)v;
+    if (det != R(0)) {
+      const R id = R(1) / det;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) ji[3 * i + j] = C[3 * j + i] * id;
+    } else {
+#pragma unroll
+      for (int m = 0; m < 9; ++m) ji[m] = (m % 4 == 0 && acc[m] != R(0)) ? R(1) / acc[m] : R(0);
+    }
+  }
+}
+
+// --------------------------------------------------------- FP64 forces ---
+// f_a = vol P(F) grad N_a per tet, in FP64 (the Newton residual is formed
+// from these; FP32 cannot resolve 1e-6 relative residuals of stiff beams).
+__global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp, double* __restrict__ fbuf) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.t) return;
+  const int4 v = __ldg(a.tets + e);
+  double du[9], D[9], G[9], P[9], gN[12];
+  tet_du(a.u, v, du);
+  load_dinv(a.dinv, a.t, e, D);
+  disp_grad(du, D, G);
+  const double vol = a.vol[e], mu = a.mu[e], lam = a.lam[e];
+  if (disp)
+    snh_pk1_disp<double>(G, mu, lam, P);
+  else
+    snh_pk1<double>(G, mu, lam, P);
+  shape_grads(D, gN);
+  double* f = fbuf + 12 * e;
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      f[3 * b + i] = vol * (P[3 * i] * gN[3 * b] + P[3 * i + 1] * gN[3 * b + 1] + P[3 * i + 2] * gN[3 * b + 2]);
+}
+
+// Vertex gather of the forces in list (tet) order, plus the backward-Euler
+// terms M/h^2 (u - u_tilde) - f_ext when `mass` is set; pinned DOFs are
+// zeroed.  Grid-stride over a fixed grid; ||g||^2 reduced deterministically.
+__global__ void __launch_bounds__(kBlock) k_vertex_gradient(GradArgs a) {
+  double gg[1] = {0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.n; v += stride) {
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int k = __ldg(a.v2t_ptr + v); k < __ldg(a.v2t_ptr + v + 1); ++k) {
+      const int code = __ldg(a.v2t + k);
+      const double* f = a.fbuf + 12 * (int64_t)(code >> 2) + 3 * (code & 3);
+      acc[0] += f[0];
+      acc[1] += f[1];
+      acc[2] += f[2];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const int64_t d = 3 * v + i;
+      double g = acc[i];
+      if (a.mass) g += a.mass[v] * a.inv_h2 * (a.u[d] - a.ut[d]);
+      if (a.f_ext) g -= a.f_ext[d];
+      if (a.pinned && a.pinned[d]) g = 0.0;
+      a.g[d] = g;
+      gg[0] += g * g;
+    }
+  }
+  grid_sum<1, kBlock>(gg, a.partials, a.counter, a.out);
+}
+
+// ----------------------------------------------------------- energies ----
+// Solver energy relative to rest at u + step * dx:
+//   sum_e vol_e (psi(F_e) - psi(I)) + sum_free [m/2h^2 (u+s dx-u~)^2 - f (u+s dx)]
+// plus its magnitude sum |terms| (the FP32 noise scale of the value).
+// Mode DIRECT instead sums vol_e psi(F_e) from absolute positions in FP64
+// (simkit's stable_neo_hookean_energy_x, snh.py:449-474).
+template <typename R, bool DIRECT>
+__global__ void __launch_bounds__(kBlock) k_energy(EnergyArgs<R> a) {
+  double acc[2] = {0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t total = a.tet.t + (DIRECT ? 0 : a.n);
+  const R step = R(a.step);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
+    if (i < a.tet.t) {
+      const int64_t e = i;
+      const int4 v = __ldg(a.tet.tets + e);
+      R du[9], D[9], G[9];
+      if constexpr (sizeof(R) == 8) {
+        tet_du(a.tet.u, v, du);
+      } else {
+        tet_du(a.tet.uh, a.tet.ul, v, du);
+      }
+      if (a.dx && step != R(0)) {
+        const Vec3<R> d0 = ld3(a.dx, v.x);
+        const int vv[3] = {v.y, v.z, v.w};
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const Vec3<R> db = ld3(a.dx, vv[b]);
+          du[3 * b + 0] += step * (db.x - d0.x);
+          du[3 * b + 1] += step * (db.y - d0.y);
+          du[3 * b + 2] += step * (db.z - d0.z);
+        }
+      }
+      load_dinv(a.tet.dinv, a.tet.t, e, D);
+      disp_grad(du, D, G);
+      const R vol = __ldg(a.tet.vol + e), mu = __ldg(a.tet.mu + e), lam = __ldg(a.tet.lam + e);
+      double val;
+      if (DIRECT)
+        val = double(vol) * double(snh_psi<R>(G, mu, lam));
+      else
+        val = double(vol * snh_dpsi<R>(G, mu, lam));
+      acc[0] += val;
+      acc[1] += fabs(val);
+    } else {
+      const int64_t v = i - a.tet.t;
+      Vec3<R> d = {R(0), R(0), R(0)};
+      if (a.dx && step != R(0)) d = ld3(a.dx, v);
+      const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+      const double mh = a.mass[v] * a.inv_h2;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int64_t k = 3 * v + c;
+        if (a.pinned && a.pinned[k]) continue;
+        const double x = a.tet.u[k] + a.step * dd[c];
+        const double r = x - a.ut[k];
+        const double kin = 0.5 * mh * r * r;
+        const double pot = a.f_ext ? -a.f_ext[k] * x : 0.0;
+        acc[0] += kin + pot;
+        acc[1] += kin + fabs(pot);
+      }
+    }
+  }
+  grid_sum<2, kBlock>(acc, a.partials, a.counter, a.out);
+}
+
+// hi/lo split of FP64 positions for the FP32 kernels, padded to 4
+__global__ void k_split(const double* __restrict__ u, int64_t n, float* __restrict__ uh, float* __restrict__ ul) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  float h[3], l[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double x = u[3 * v + c];
+    h[c] = float(x);
+    l[c] = float(x - double(h[c]));
+  }
+  reinterpret_cast<float4*>(uh)[v] = make_float4(h[0], h[1], h[2], 0.f);
+  reinterpret_cast<float4*>(ul)[v] = make_float4(l[0], l[1], l[2], 0.f);
+}
+
+// ------------------------------------------------------------ launchers --
+template <typename R>
+int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s) {
+  if (a.t == 0) return SKG_OK;
+  k_tet_hessian<R><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+template <typename R>
+int launch_assemble(const AsmArgs<R>& a, cudaStream_t s) {
+  if (a.nb == 0) return SKG_OK;
+  k_assemble<R><<<blocks_for(a.nb), kBlock, 0, s>>>(a);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t s) {
+  if (a.t == 0) return SKG_OK;
+  k_tet_forces<<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, fbuf);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+int launch_vertex_gradient(const GradArgs& a, cudaStream_t s) {
+  k_vertex_gradient<<<reduce_blocks(a.n), kBlock, 0, s>>>(a);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+template <typename R>
+int launch_energy(const EnergyArgs<R>& a, bool direct, cudaStream_t s) {
+  const int64_t total = a.tet.t + (direct ? 0 : a.n);
+  if (direct)
+    k_energy<R, true><<<reduce_blocks(total), kBlock, 0, s>>>(a);
+  else
+    k_energy<R, false><<<reduce_blocks(total), kBlock, 0, s>>>(a);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t s) {
+  k_split<<<blocks_for(n), kBlock, 0, s>>>(u, n, uh, ul);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+template int launch_tet_hessian<float>(const TetArgs<float>&, int, int, float*, cudaStream_t);
+template int launch_tet_hessian<double>(const TetArgs<double>&, int, int, double*, cudaStream_t);
+template int launch_assemble<float>(const AsmArgs<float>&, cudaStream_t);
+template int launch_assemble<double>(const AsmArgs<double>&, cudaStream_t);
+template int launch_energy<float>(const EnergyArgs<float>&, bool, cudaStream_t);
+template int launch_energy<double>(const EnergyArgs<double>&, bool, cudaStream_t);
+
+// --------------------------------------------------- workspace layout ----
+Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
+  Carve c(base);
+  Workspace w{};
+  const int64_t t = m->n_tets, n = m->n_verts, nb = m->n_blocks;
+  const bool mixed = precision == SKG_MIXED;
+  w.hbuf32 = mixed ? c.take<float>(kHStride * t) : nullptr;
+  w.hbuf64 = mixed ? nullptr : c.take<double>(kHStride * t);
+  w.fbuf = c.take<double>(12 * t);
+  w.val32 = mixed ? c.take<float>(9 * nb) : nullptr;
+  w.val64 = mixed ? nullptr : c.take<double>(9 * nb);
+  w.jinv32 = mixed ? c.take<float>(9 * n) : nullptr;
+  w.jinv64 = mixed ? nullptr : c.take<double>(9 * n);
+  w.g = c.take<double>(3 * n);
+  w.ut = c.take<double>(3 * n);
+  w.uh = c.take<float>(4 * n);
+  w.ul = c.take<float>(4 * n);
+  for (int k = 0; k < 5; ++k) {
+    w.vec32[k] = mixed ? c.take<float>(4 * n) : nullptr;
+    w.vec64[k] = mixed ? nullptr : c.take<double>(4 * n);
+  }
+  w.partials = c.take<double>(8 * kMaxGrid);
+  w.counter = c.take<unsigned>(16);
+  w.scal = c.take<double>(64);
+  w.bytes = c.off + 256;
+  return w;
+}
+
+}  // namespace skg
+
+using namespace skg;
+
+static TetArgs<double> tet_args64(const skg_tet_mesh* m, const double* u) {
+  TetArgs<double> a{};
+  a.t = m->n_tets;
+  a.tets = reinterpret_cast<const int4*>(m->tets);
+  a.dinv = m->dinv;
+  a.vol = m->vol;
+  a.mu = m->mu;
+  a.lam = m->lam;
+  a.u = u;
+  return a;
+}
+
+namespace skg {
+TetArgs<double> make_tet_args64(const skg_tet_mesh* m, const double* u) { return tet_args64(m, u); }
+TetArgs<float> make_tet_args32(const skg_tet_mesh* m, const double* u, const float* uh, const float* ul) {
+  TetArgs<float> a{};
+  a.t = m->n_tets;
+  a.tets = reinterpret_cast<const int4*>(m->tets);
+  a.dinv = m->dinv32;
+  a.vol = m->mat32;
+  a.mu = m->mat32 + m->n_tets;
+  a.lam = m->mat32 + 2 * m->n_tets;
+  a.u = u;
+  a.uh = uh;
+  a.ul = ul;
+  return a;
+}
+int check_mesh(const skg_tet_mesh* m, int precision) {
+  if (!m) return fail(SKG_ERR_ARG, "mesh is null");
+  if (m->n_verts <= 0 || m->n_tets < 0 || m->n_blocks < m->n_verts)
+    return fail(SKG_ERR_ARG, "mesh sizes are inconsistent");
+  if (!m->tets || !m->dinv || !m->vol || !m->mu || !m->lam || !m->bsr_rowptr || !m->bsr_col || !m->bsr_row ||
+      !m->bsr_diag || !m->hc_ptr || !m->hc_src || !m->v2t_ptr || !m->v2t)
+    return fail(SKG_ERR_ARG, "mesh has a null array");
+  if (precision == SKG_MIXED && (!m->dinv32 || !m->mat32))
+    return fail(SKG_ERR_ARG, "mixed precision needs the FP32 mesh copies");
+  if (precision != SKG_MIXED && precision != SKG_FP64) return fail(SKG_ERR_ARG, "unknown precision %d", precision);
+  return SKG_OK;
+}
+}  // namespace skg
+
+extern "C" {
+
+int64_t skg_assembly_workspace_size(const skg_tet_mesh* mesh, int precision) {
+  if (check_mesh(mesh, precision) != SKG_OK) return -1;
+  return carve_workspace(mesh, precision, nullptr).bytes;
+}
+
+int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h, void* ws, void* stream) {
+  SKG_TRY(check_mesh(mesh, SKG_FP64));
+  if (!x || !ws || !energy_h) return fail(SKG_ERR_ARG, "energy_x: null pointer");
+  cudaStream_t s = as_stream(stream);
+  Workspace w = carve_workspace(mesh, SKG_FP64, ws);
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
+  EnergyArgs<double> a{};
+  a.tet = tet_args64(mesh, x);
+  a.n = mesh->n_verts;
+  a.partials = w.partials;
+  a.counter = w.counter;
+  a.out = w.scal;
+  SKG_TRY(launch_energy<double>(a, true, s));
+  SKG_CUDA(cudaMemcpyAsync(energy_h, w.scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaStreamSynchronize(s));
+  return SKG_OK;
+}
+
+int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, void* ws, void* stream) {
+  SKG_TRY(check_mesh(mesh, SKG_FP64));
+  if (!x || !g || !ws) return fail(SKG_ERR_ARG, "gradient_x: null pointer");
+  cudaStream_t s = as_stream(stream);
+  Workspace w = carve_workspace(mesh, SKG_FP64, ws);
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
+  SKG_TRY(launch_forces(tet_args64(mesh, x), 0, w.fbuf, s));
+  GradArgs ga{};
+  ga.n = mesh->n_verts;
+  ga.v2t_ptr = mesh->v2t_ptr;
+  ga.v2t = mesh->v2t;
+  ga.fbuf = w.fbuf;
+  ga.g = g;
+  ga.partials = w.partials;
+  ga.counter = w.counter;
+  ga.out = w.scal;
+  return launch_vertex_gradient(ga, s);
+}
+
+int skg_snh_hessian_x(const skg_tet_mesh* mesh, const double* x, int precision, int psd, double* val64,
+                      float* val32, void* ws, void* stream) {
+  SKG_TRY(check_mesh(mesh, precision));
+  if (!x || !ws) return fail(SKG_ERR_ARG, "hessian_x: null pointer");
+  cudaStream_t s = as_stream(stream);
+  Workspace w = carve_workspace(mesh, precision, ws);
+  if (precision == SKG_FP64) {
+    if (!val64) return fail(SKG_ERR_ARG, "hessian_x: FP64 needs val64");
+    SKG_TRY(launch_tet_hessian<double>(tet_args64(mesh, x), 0, psd, w.hbuf64, s));
+    AsmArgs<double> aa = make_asm_args<double>(mesh, w.hbuf64, val64, nullptr);
+    return launch_assemble<double>(aa, s);
+  }
+  if (!val32) return fail(SKG_ERR_ARG, "hessian_x: mixed precision needs val32");
+  SKG_TRY(launch_split(x, mesh->n_verts, w.uh, w.ul, s));
+  SKG_TRY(launch_tet_hessian<float>(make_tet_args32(mesh, x, w.uh, w.ul), 0, psd, w.hbuf32, s));
+  AsmArgs<float> aa = make_asm_args<float>(mesh, w.hbuf32, val32, nullptr);
+  return launch_assemble<float>(aa, s);
+}
+
+}  // extern "C"

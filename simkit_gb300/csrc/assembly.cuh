@@ -1,0 +1,124 @@
+// Kernel argument bundles and launchers shared by the assembled tier and the
+// Newton solver.
+#pragma once
+
+#include "common.cuh"
+
+namespace skg {
+
+constexpr int kHStride = 80;     // per-tet Hessian record: 78 values + 2 pad
+constexpr int kMaxGrid = 2048;   // upper bound on grid-stride reduction grids
+
+inline int reduce_blocks(int64_t n) {
+  int64_t b = (n + kBlock - 1) / kBlock;
+  if (b > kReduceBlocks) b = kReduceBlocks;
+  return (int)(b < 1 ? 1 : b);
+}
+
+template <typename R> struct TetArgs {
+  int64_t t;
+  const int4* tets;
+  const R* dinv;
+  const R* vol;
+  const R* mu;
+  const R* lam;
+  const double* u;   // FP64 displacement (or positions), 3n
+  const float* uh;   // FP32 hi/lo split (FP32 kernels only)
+  const float* ul;
+};
+
+template <typename R> struct AsmArgs {
+  int64_t nb;
+  const int32_t* bsr_row;
+  const int32_t* bsr_col;
+  const int32_t* rowptr;
+  const int32_t* hc_ptr;
+  const int32_t* hc_src;
+  const R* hbuf;
+  const double* mass;    // optional: adds mass/h^2 on diagonal blocks
+  double inv_h2;
+  const uint8_t* pinned; // optional: 3n DOF mask
+  R* val;
+  R* jinv;               // optional: block-Jacobi inverses (9n)
+};
+
+struct GradArgs {
+  int64_t n;
+  const int32_t* v2t_ptr;
+  const int32_t* v2t;
+  const double* fbuf;
+  const double* mass;   // optional backward-Euler terms
+  double inv_h2;
+  const double* u;
+  const double* ut;
+  const double* f_ext;
+  const uint8_t* pinned;
+  double* g;
+  double* partials;
+  unsigned* counter;
+  double* out;          // out[0] = ||g||^2
+};
+
+template <typename R> struct EnergyArgs {
+  TetArgs<R> tet;
+  int64_t n;
+  const R* dx;          // optional padded step direction
+  double step;
+  const double* mass;
+  double inv_h2;
+  const double* ut;
+  const double* f_ext;
+  const uint8_t* pinned;
+  double* partials;
+  unsigned* counter;
+  double* out;          // out[0] = energy, out[1] = magnitude
+};
+
+struct Workspace {
+  float* hbuf32;
+  double* hbuf64;
+  double* fbuf;
+  float* val32;
+  double* val64;
+  float* jinv32;
+  double* jinv64;
+  double* g;
+  double* ut;
+  float* uh;
+  float* ul;
+  float* vec32[5];   // PCG x, r, z, p, q (padded)
+  double* vec64[5];
+  double* partials;
+  unsigned* counter;
+  double* scal;
+  int64_t bytes;
+};
+
+Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base);
+int check_mesh(const skg_tet_mesh* m, int precision);
+TetArgs<double> make_tet_args64(const skg_tet_mesh* m, const double* u);
+TetArgs<float> make_tet_args32(const skg_tet_mesh* m, const double* u, const float* uh, const float* ul);
+
+template <typename R>
+inline AsmArgs<R> make_asm_args(const skg_tet_mesh* m, const R* hbuf, R* val, R* jinv) {
+  AsmArgs<R> a{};
+  a.nb = m->n_blocks;
+  a.bsr_row = m->bsr_row;
+  a.bsr_col = m->bsr_col;
+  a.rowptr = m->bsr_rowptr;
+  a.hc_ptr = m->hc_ptr;
+  a.hc_src = m->hc_src;
+  a.hbuf = hbuf;
+  a.val = val;
+  a.jinv = jinv;
+  return a;
+}
+
+template <typename R> int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s);
+template <typename R> int launch_assemble(const AsmArgs<R>& a, cudaStream_t s);
+int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t s);
+int launch_vertex_gradient(const GradArgs& a, cudaStream_t s);
+template <typename R> int launch_energy(const EnergyArgs<R>& a, bool direct, cudaStream_t s);
+int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t s);
+
+}  // namespace skg

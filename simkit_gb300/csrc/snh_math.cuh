@@ -428,8 +428,11 @@ SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
 
 // F: deformation gradient; gN: 4x3 shape gradients; out: 78 packed values.
 // fallback_J: elements with det F below it run the SVD in FP64.
+// floor_v: eigenvalue floor (simkit's 1e-6); project = false skips the
+// projection (simkit's psd=False, snh.py:534).
 template <typename R>
-SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1)) {
+SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1),
+                           bool project = true) {
   R IC = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
@@ -488,6 +491,7 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
       o[6] += w[1]; o[7] -= w[0];
     }
 
+  if (!project) return;
   // eigenvalue floor
   R U[9], s[3], V[9], W[9], lam9[9];
   if (J < fallback_J)

@@ -1,0 +1,749 @@
+// Block-Jacobi preconditioned CG on the assembled 3x3-block matrix, and the
+// Newton / backward-Euler driver that replaces simkit's spsolve-based Newton
+// (simkit/solvers/newton.py:46-69, simkit/integrators/backward_euler.py:76-91).
+//
+// PCG: FP32 (mixed) or FP64 vectors padded to 4 per vertex, FP64 dot
+// products reduced deterministically.  Two execution modes:
+//   mode 0: one kernel per phase (SpMV+dot, update+dots, direction update),
+//           a device-side done flag turns later launches into no-ops and the
+//           host checks it every few iterations;
+//   mode 1: one persistent cooperative kernel for the whole solve, phases
+//           separated by a grid barrier whose waits are bounded.
+#include <math.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "assembly.cuh"
+#include "snh_math.cuh"
+
+namespace skg {
+
+enum ScalarSlot {
+  S_RZ = 0, S_PQ = 1, S_RR = 2, S_BB = 3, S_BETA = 4, S_TOL2 = 5, S_ITERS = 6, S_DONE = 7, S_STATUS = 8,
+  S_MAXIT = 9, S_GG = 10, S_E = 12,      /* 12: energy, 13: magnitude */
+  S_SLOPE = 14, S_TMP = 16,               /* 16..19 scratch reduction outputs */
+  S_BAR_ERR = 24
+};
+
+template <typename R> struct Bsr {
+  int64_t nbr;
+  const int32_t* rowptr;
+  const int32_t* col;
+  const R* val;
+  const R* jinv;
+};
+
+template <typename R> struct PcgVecs {
+  R* x;
+  R* r;
+  R* z;
+  R* p;
+  R* q;
+};
+
+template <typename R>
+__device__ __forceinline__ Vec3<R> jacobi_apply(const R* __restrict__ jinv, int64_t v, Vec3<R> r) {
+  const R* J = jinv + 9 * v;
+  return {J[0] * r.x + J[1] * r.y + J[2] * r.z, J[3] * r.x + J[4] * r.y + J[5] * r.z,
+          J[6] * r.x + J[7] * r.y + J[8] * r.z};
+}
+
+// y_v = sum_k A_vk x_{col_k} for one block row, G lanes per row; returns
+// the row result in every lane of the group.
+// Every lane of the warp must call this (the shuffles use a full mask);
+// lanes whose row is out of range pass valid = false and contribute nothing.
+template <typename R, int G>
+__device__ __forceinline__ Vec3<R> spmv_row(const Bsr<R>& A, const R* __restrict__ xin, int64_t row, int lane,
+                                            bool valid) {
+  const int rp = valid ? __ldg(A.rowptr + row) : 0;
+  const int K = valid ? __ldg(A.rowptr + row + 1) - rp : 0;
+  const R* vals = A.val + 9 * (int64_t)rp;
+  R a0 = 0, a1 = 0, a2 = 0;
+  for (int k = lane; k < K; k += G) {
+    const int c = __ldg(A.col + rp + k);
+    const Vec3<R> xv = ld3c(xin, c);
+    const R m0 = vals[k], m1 = vals[K + k], m2 = vals[2 * K + k];
+    const R m3 = vals[3 * K + k], m4 = vals[4 * K + k], m5 = vals[5 * K + k];
+    const R m6 = vals[6 * K + k], m7 = vals[7 * K + k], m8 = vals[8 * K + k];
+    a0 += m0 * xv.x + m1 * xv.y + m2 * xv.z;
+    a1 += m3 * xv.x + m4 * xv.y + m5 * xv.z;
+    a2 += m6 * xv.x + m7 * xv.y + m8 * xv.z;
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o, G);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o, G);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o, G);
+  }
+  return {a0, a1, a2};
+}
+
+// ------------------------------------------------------ mode 0 kernels ---
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_pcg_init(Bsr<R> A, const double* __restrict__ b, double bsign,
+                                                     const uint8_t* __restrict__ pinned, PcgVecs<R> v,
+                                                     double rtol, int max_iter, double* partials,
+                                                     unsigned* counter, double* scal) {
+  double acc[3] = {0.0, 0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
+    double bb[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      bb[c] = bsign * b[3 * i + c];
+      if (pinned && pinned[3 * i + c]) bb[c] = 0.0;
+    }
+    const Vec3<R> r = {R(bb[0]), R(bb[1]), R(bb[2])};
+    const Vec3<R> z = jacobi_apply(A.jinv, i, r);
+    st3(v.r, i, r);
+    st3(v.z, i, z);
+    st3(v.p, i, z);
+    st3(v.x, i, Vec3<R>{R(0), R(0), R(0)});
+    acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
+    acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+  }
+  acc[2] = acc[1];
+  if (grid_sum<3, kBlock>(acc, partials, counter, scal + S_TMP) && threadIdx.x == 0) {
+    const double rz = scal[S_TMP], rr = scal[S_TMP + 1], bb = scal[S_TMP + 2];
+    scal[S_RZ] = rz;
+    scal[S_RR] = rr;
+    scal[S_BB] = bb;
+    scal[S_TOL2] = rtol * rtol * bb;
+    scal[S_ITERS] = 0.0;
+    scal[S_MAXIT] = max_iter;
+    scal[S_STATUS] = 0.0;
+    scal[S_DONE] = (rr <= rtol * rtol * bb || bb == 0.0 || max_iter <= 0) ? 1.0 : 0.0;
+  }
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(kBlock) k_pcg_spmv(Bsr<R> A, PcgVecs<R> v, double* partials, unsigned* counter,
+                                                     double* scal) {
+  if (*((volatile double*)(scal + S_DONE)) != 0.0) return;
+  double acc[1] = {0.0};
+  const int lane = threadIdx.x & (G - 1);
+  // warp-uniform trip count: each warp covers 32/G consecutive rows per pass
+  const int64_t warp_rows = 32 / G;
+  const int64_t stride = (int64_t)gridDim.x * (blockDim.x / G);
+  const int64_t row0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * warp_rows;
+  for (int64_t base = row0; base < A.nbr; base += stride) {
+    const int64_t row = base + ((threadIdx.x & 31) / G);
+    const bool valid = row < A.nbr;
+    const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
+    if (lane == 0 && valid) {
+      st3(v.q, row, y);
+      const Vec3<R> pv = ld3c(v.p, row);
+      acc[0] += double(pv.x) * y.x + double(pv.y) * y.y + double(pv.z) * y.z;
+    }
+  }
+  if (grid_sum<1, kBlock>(acc, partials, counter, scal + S_PQ) && threadIdx.x == 0) {
+    const double pq = scal[S_PQ];
+    if (!(pq > 0.0) || !isfinite(pq)) {
+      scal[S_DONE] = 1.0;
+      scal[S_STATUS] = isfinite(pq) ? 0.0 : (double)SKG_ERR_NONFINITE;
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_pcg_update(Bsr<R> A, PcgVecs<R> v, double* partials, unsigned* counter,
+                                                       double* scal) {
+  if (*((volatile double*)(scal + S_DONE)) != 0.0) return;
+  const double alpha = scal[S_RZ] / scal[S_PQ];
+  const R a = R(alpha);
+  double acc[2] = {0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
+    Vec3<R> x = ld3c(v.x, i), r = ld3c(v.r, i);
+    const Vec3<R> p = ld3c(v.p, i), q = ld3c(v.q, i);
+    x = {x.x + a * p.x, x.y + a * p.y, x.z + a * p.z};
+    r = {r.x - a * q.x, r.y - a * q.y, r.z - a * q.z};
+    const Vec3<R> z = jacobi_apply(A.jinv, i, r);
+    st3(v.x, i, x);
+    st3(v.r, i, r);
+    st3(v.z, i, z);
+    acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
+    acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+  }
+  if (grid_sum<2, kBlock>(acc, partials, counter, scal + S_TMP) && threadIdx.x == 0) {
+    const double rz = scal[S_TMP], rr = scal[S_TMP + 1];
+    scal[S_BETA] = rz / scal[S_RZ];
+    scal[S_RZ] = rz;
+    scal[S_RR] = rr;
+    const double it = scal[S_ITERS] + 1.0;
+    scal[S_ITERS] = it;
+    if (!isfinite(rr)) {
+      scal[S_STATUS] = (double)SKG_ERR_NONFINITE;
+      scal[S_DONE] = 1.0;
+    } else if (rr <= scal[S_TOL2] || it >= scal[S_MAXIT]) {
+      scal[S_DONE] = 1.0;
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_pcg_direction(int64_t nbr, PcgVecs<R> v, const double* scal) {
+  if (*((volatile const double*)(scal + S_DONE)) != 0.0) return;
+  const R beta = R(scal[S_BETA]);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nbr; i += stride) {
+    const Vec3<R> z = ld3c(v.z, i), p = ld3c(v.p, i);
+    st3(v.p, i, Vec3<R>{z.x + beta * p.x, z.y + beta * p.y, z.z + beta * p.z});
+  }
+}
+
+// ------------------------------------------------------ mode 1 kernel ----
+// Sense-reversing grid barrier.  Every wait is bounded: after kSpinLimit
+// polls the block records SKG_ERR_TIMEOUT and all blocks leave the solve at
+// their next barrier.  The kernel is launched cooperatively, so all blocks
+// are resident and the barrier completes in normal operation.
+constexpr long long kSpinLimit = 1ll << 24;
+
+__device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned* gen, volatile double* err) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == gridDim.x - 1) {
+      *count = 0u;
+      __threadfence();
+      atomicAdd((unsigned*)gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kSpinLimit) {
+          *err = (double)SKG_ERR_TIMEOUT;
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*err != 0.0) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// sum of NV per-block partials in index order, computed redundantly by
+// every block (same order -> same value everywhere)
+template <int NV>
+__device__ __forceinline__ void all_sum(const double* partials, double (&out)[NV]) {
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    s[k] = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s[k] += *((volatile const double*)&partials[k * gridDim.x + i]);
+  }
+  block_sum<NV, kBlock>(s);
+  __shared__ double res[NV];
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) res[k] = s[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) out[k] = res[k];
+  __syncthreads();
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(kBlock) k_pcg_persistent(Bsr<R> A, PcgVecs<R> v, double* partials,
+                                                           unsigned* bar, double* scal) {
+  // partials: 3 buffers of 2*gridDim doubles (pq | rz, rr | spare)
+  double* P1 = partials;
+  double* P2 = partials + 2 * gridDim.x;
+  unsigned* count = bar;
+  volatile unsigned* gen = bar + 1;
+  volatile double* err = scal + S_BAR_ERR;
+  double rz = scal[S_RZ];
+  const double tol2 = scal[S_TOL2];
+  const int max_iter = (int)scal[S_MAXIT];
+  int it = 0;
+  bool done = scal[S_DONE] != 0.0;
+  int status = 0;
+  const int lane = threadIdx.x & (G - 1);
+  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / G);
+  const int64_t row0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * (32 / G);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  double rr = scal[S_RR];
+  while (!done) {
+    // q = A p, pq
+    double acc[2] = {0.0, 0.0};
+    for (int64_t base = row0; base < A.nbr; base += groups) {
+      const int64_t row = base + ((threadIdx.x & 31) / G);
+      const bool valid = row < A.nbr;
+      const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
+      if (lane == 0 && valid) {
+        st3(v.q, row, y);
+        const Vec3<R> pv = ld3c(v.p, row);
+        acc[0] += double(pv.x) * y.x + double(pv.y) * y.y + double(pv.z) * y.z;
+      }
+    }
+    double a1[1] = {acc[0]};
+    block_sum<1, kBlock>(a1);
+    if (threadIdx.x == 0) P1[blockIdx.x] = a1[0];
+    if (!grid_barrier(count, gen, err)) { status = SKG_ERR_TIMEOUT; break; }
+    double pq[1];
+    all_sum<1>(P1, pq);
+    if (!(pq[0] > 0.0) || !isfinite(pq[0])) {
+      status = isfinite(pq[0]) ? 0 : SKG_ERR_NONFINITE;
+      break;
+    }
+    const double alpha = rz / pq[0];
+    const R a = R(alpha);
+    acc[0] = acc[1] = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
+      Vec3<R> x = ld3c(v.x, i), r = ld3c(v.r, i);
+      const Vec3<R> p = ld3c(v.p, i), q = ld3c(v.q, i);
+      x = {x.x + a * p.x, x.y + a * p.y, x.z + a * p.z};
+      r = {r.x - a * q.x, r.y - a * q.y, r.z - a * q.z};
+      const Vec3<R> z = jacobi_apply(A.jinv, i, r);
+      st3(v.x, i, x);
+      st3(v.r, i, r);
+      st3(v.z, i, z);
+      acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
+      acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+    }
+    block_sum<2, kBlock>(acc);
+    if (threadIdx.x == 0) {
+      P2[blockIdx.x] = acc[0];
+      P2[gridDim.x + blockIdx.x] = acc[1];
+    }
+    if (!grid_barrier(count, gen, err)) { status = SKG_ERR_TIMEOUT; break; }
+    double s2[2];
+    all_sum<2>(P2, s2);
+    ++it;
+    rr = s2[1];
+    const double beta = s2[0] / rz;
+    rz = s2[0];
+    if (!isfinite(rr)) { status = SKG_ERR_NONFINITE; break; }
+    if (rr <= tol2 || it >= max_iter) break;
+    const R b = R(beta);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
+      const Vec3<R> z = ld3c(v.z, i), p = ld3c(v.p, i);
+      st3(v.p, i, Vec3<R>{z.x + b * p.x, z.y + b * p.y, z.z + b * p.z});
+    }
+    if (!grid_barrier(count, gen, err)) { status = SKG_ERR_TIMEOUT; break; }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_ITERS] = it;
+    scal[S_RR] = rr;
+    scal[S_RZ] = rz;
+    scal[S_DONE] = 1.0;
+    if (status != 0) scal[S_STATUS] = status;
+    if (*err != 0.0) scal[S_STATUS] = *err;
+  }
+}
+
+// ------------------------------------------------------ small kernels ----
+// u_tilde = 2 u_curr - u_prev (simkit/energies/kinetic.py:87-90), u = u_tilde
+__global__ void k_be_init(const double* __restrict__ uc, const double* __restrict__ up, int64_t m,
+                          double* __restrict__ ut, double* __restrict__ u) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double x = uc[i] + (uc[i] - up[i]);
+  ut[i] = x;
+  u[i] = x;
+}
+
+// u += step * dx on free DOFs
+template <typename R>
+__global__ void k_apply_step(double* __restrict__ u, const R* __restrict__ dx, double step, int64_t n,
+                             const uint8_t* __restrict__ pinned) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const Vec3<R> d = ld3c(dx, v);
+  const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (!(pinned && pinned[3 * v + c])) u[3 * v + c] += step * dd[c];
+}
+
+// g . dx (FP64)
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_dot_g(const double* __restrict__ g, const R* __restrict__ dx, int64_t n,
+                                                  double* partials, unsigned* counter, double* out) {
+  double acc[1] = {0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
+    const Vec3<R> d = ld3c(dx, v);
+    acc[0] += g[3 * v] * double(d.x) + g[3 * v + 1] * double(d.y) + g[3 * v + 2] * double(d.z);
+  }
+  grid_sum<1, kBlock>(acc, partials, counter, out);
+}
+
+// padded vector -> simkit layout (3n), FP64
+template <typename R>
+__global__ void k_unpad(const R* __restrict__ x, int64_t n, double* __restrict__ out) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const Vec3<R> a = ld3c(x, v);
+  out[3 * v] = a.x;
+  out[3 * v + 1] = a.y;
+  out[3 * v + 2] = a.z;
+}
+
+// ---------------------------------------------------------- PCG driver ----
+struct PcgResult {
+  int iters;
+  int status;
+  int launches;
+  double rr, bb;
+};
+
+// Phase timer on the launching stream (CUDA events; only when profiling).
+struct PhaseTimer {
+  bool on = false;
+  cudaStream_t s = 0;
+  cudaEvent_t a = nullptr, b = nullptr;
+  void init(bool enable, cudaStream_t st) {
+    on = enable;
+    s = st;
+    if (on) {
+      static thread_local cudaEvent_t ea = nullptr, eb = nullptr;
+      if (!ea) {
+        cudaEventCreate(&ea);
+        cudaEventCreate(&eb);
+      }
+      a = ea;
+      b = eb;
+    }
+  }
+  void begin() {
+    if (on) cudaEventRecord(a, s);
+  }
+  double end() {
+    if (!on) return 0.0;
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+};
+
+static int g_num_sms = 0;
+
+static int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+constexpr int kG = 8;  // lanes per block row in the SpMV
+
+template <typename R>
+static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
+                     double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
+                     cudaStream_t s, PcgResult* res) {
+  const int rb = reduce_blocks(A.nbr);
+  k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal);
+  SKG_LAUNCHED();
+  res->launches = 1;
+  if (mode == 1) {
+    int per_sm = 0;
+    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<R, kG>, kBlock, 0));
+    int64_t want = (A.nbr * kG + kBlock - 1) / kBlock;
+    int64_t cap = (int64_t)per_sm * num_sms();
+    if (cap > kMaxGrid / 2) cap = kMaxGrid / 2;
+    int grid = (int)(want < cap ? want : cap);
+    if (grid < 1) grid = 1;
+    unsigned* bar = counter + 4;
+    SKG_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+    SKG_CUDA(cudaMemsetAsync(scal + S_BAR_ERR, 0, sizeof(double), s));
+    Bsr<R> a2 = A;
+    PcgVecs<R> v2 = v;
+    double* p2 = partials;
+    double* sc2 = scal;
+    void* args[] = {&a2, &v2, &p2, &bar, &sc2};
+    SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<R, kG>, dim3(grid), dim3(kBlock), args, 0, s));
+    res->launches += 1;
+  } else {
+    const int sb = (int)((A.nbr * kG + kBlock - 1) / kBlock);
+    const int spmv_blocks = sb < 4 * num_sms() * 4 ? sb : 4 * num_sms() * 4;
+    const int chunk = A.nbr > 20000 ? 8 : 16;
+    double hs[2];
+    for (int it = 0; it < max_iter; it += chunk) {
+      for (int c = 0; c < chunk; ++c) {
+        k_pcg_spmv<R, kG><<<spmv_blocks < kMaxGrid ? spmv_blocks : kMaxGrid, kBlock, 0, s>>>(A, v, partials,
+                                                                                          counter, scal);
+        k_pcg_update<R><<<rb, kBlock, 0, s>>>(A, v, partials, counter, scal);
+        k_pcg_direction<R><<<rb, kBlock, 0, s>>>(A.nbr, v, scal);
+      }
+      res->launches += 3 * chunk;
+      SKG_LAUNCHED();
+      SKG_CUDA(cudaMemcpyAsync(hs, scal + S_ITERS, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SKG_CUDA(cudaStreamSynchronize(s));
+      if (hs[1] != 0.0) break;
+    }
+  }
+  double h[10];
+  SKG_CUDA(cudaMemcpyAsync(h, scal, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaStreamSynchronize(s));
+  res->iters = (int)h[S_ITERS];
+  res->status = (int)h[S_STATUS];
+  res->rr = h[S_RR];
+  res->bb = h[S_BB];
+  return SKG_OK;
+}
+
+// ------------------------------------------------------- Newton / BE ------
+static int read_scalars(const double* dev, double* host, int count, cudaStream_t s) {
+  SKG_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaStreamSynchronize(s));
+  return SKG_OK;
+}
+
+template <typename R>
+static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be_state* st, Workspace& w,
+                   skg_step_info* info, cudaStream_t s) {
+  const int64_t n = m->n_verts, nd = 3 * n;
+  const bool mixed = sizeof(R) == 4;
+  const double inv_h2 = 1.0 / (prm->dt * prm->dt);
+  R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
+  R* val = mixed ? (R*)w.val32 : (R*)w.val64;
+  R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
+  PcgVecs<R> pv;
+  R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
+  pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4];
+  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, val, jinv};
+
+  PhaseTimer pt;
+  pt.init(prm->profile != 0, s);
+  info->launches = 0;
+  info->t_hessian_ms = info->t_assemble_ms = info->t_pcg_ms = info->t_gradient_ms = info->t_energy_ms = 0.0;
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
+  k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, w.ut, st->u);
+  SKG_LAUNCHED();
+  info->launches++;
+
+  GradArgs ga{};
+  ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
+  ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
+  ga.partials = w.partials; ga.counter = w.counter; ga.out = w.scal + S_GG;
+
+  EnergyArgs<R> ea{};
+  if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
+  else ea.tet = make_tet_args64(m, st->u);
+  ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  ea.partials = w.partials; ea.counter = w.counter; ea.out = w.scal + S_E;
+
+  auto gradient = [&](double* gg) -> int {
+    pt.begin();
+    SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    SKG_TRY(launch_vertex_gradient(ga, s));
+    info->launches += 2;
+    info->t_gradient_ms += pt.end();
+    return read_scalars(w.scal + S_GG, gg, 1, s);
+  };
+  auto energy = [&](const R* dx, double step, double* e2) -> int {
+    ea.dx = dx;
+    ea.step = step;
+    pt.begin();
+    SKG_TRY(launch_energy<R>(ea, false, s));
+    info->launches++;
+    info->t_energy_ms += pt.end();
+    return read_scalars(w.scal + S_E, e2, 2, s);
+  };
+  auto split = [&]() -> int {
+    if (!mixed) return SKG_OK;
+    info->launches++;
+    return launch_split(st->u, n, w.uh, w.ul, s);
+  };
+
+  info->newton_iters = 0; info->pcg_iters = 0; info->ls_trials = 0; info->status = SKG_OK;
+  info->min_alpha = 1.0;
+  double gg;
+  SKG_TRY(gradient(&gg));
+  const double r0 = sqrt(gg);
+  info->residual0 = r0;
+  info->residual = r0 > 0.0 ? 1.0 : 0.0;
+  if (!isfinite(r0)) {
+    info->status = SKG_ERR_NONFINITE;
+    return SKG_OK;
+  }
+  SKG_TRY(split());
+  double ecur[2];
+  SKG_TRY(energy(nullptr, 0.0, ecur));
+  const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  for (int it = 0; it < prm->max_newton && r0 > 0.0; ++it) {
+    const double res = sqrt(gg) / r0;
+    info->residual = res;
+    if (res < prm->tol) break;
+    // H(u) + M/h^2 with pinned rows/columns, block-Jacobi inverses
+    pt.begin();
+    if constexpr (sizeof(R) == 4) {
+      SKG_TRY(launch_tet_hessian<float>(make_tet_args32(m, st->u, w.uh, w.ul), 1, 1, (float*)hbuf, s));
+    } else {
+      SKG_TRY(launch_tet_hessian<double>(make_tet_args64(m, st->u), 1, 1, (double*)hbuf, s));
+    }
+    info->t_hessian_ms += pt.end();
+    AsmArgs<R> aa = make_asm_args<R>(m, hbuf, val, jinv);
+    aa.mass = st->mass;
+    aa.inv_h2 = inv_h2;
+    aa.pinned = st->pinned;
+    pt.begin();
+    SKG_TRY(launch_assemble<R>(aa, s));
+    info->t_assemble_ms += pt.end();
+    info->launches += 2;
+    // dx = -H^-1 g
+    PcgResult pr{};
+    pt.begin();
+    SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, prm->pcg_rtol, prm->pcg_max_iter, prm->pcg_mode, w.partials,
+                         w.counter, w.scal, s, &pr));
+    info->t_pcg_ms += pt.end();
+    info->launches += pr.launches;
+    info->pcg_iters += pr.iters;
+    if (pr.status != 0) {
+      info->status = pr.status;
+      break;
+    }
+    // Armijo backtracking (simkit/backtracking_line_search.py:56-67)
+    double slope;
+    k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s>>>(w.g, pv.x, n, w.partials, w.counter, w.scal + S_SLOPE);
+    SKG_LAUNCHED();
+    info->launches++;
+    SKG_TRY(read_scalars(w.scal + S_SLOPE, &slope, 1, s));
+    double step = 1.0, enew[2] = {ecur[0], ecur[1]};
+    bool accepted = !prm->do_line_search;
+    if (prm->do_line_search) {
+      const double thr = prm->ls_threshold >= 0.0 ? prm->ls_threshold : 1e-12 + 16.0 * eps_r * ecur[1];
+      for (int k = 0; k < prm->ls_max_iter; ++k) {
+        SKG_TRY(energy(pv.x, step, enew));
+        info->ls_trials++;
+        if (enew[0] <= ecur[0] + prm->ls_alpha * step * slope + thr) {
+          accepted = true;
+          break;
+        }
+        step *= prm->ls_beta;
+      }
+    }
+    info->newton_iters = it + 1;
+    if (!accepted) {
+      // simkit returns t = 0 (backtracking_line_search.py:66-67) and Newton
+      // stops because ||0 * dx|| < tol (newton.py:69)
+      info->status = SKG_ERR_LINESEARCH;
+      break;
+    }
+    k_apply_step<R><<<blocks_for(n), kBlock, 0, s>>>(st->u, pv.x, step, n, st->pinned);
+    SKG_LAUNCHED();
+    info->launches++;
+    if (step < info->min_alpha) info->min_alpha = step;
+    SKG_TRY(split());
+    if (prm->do_line_search) {
+      ecur[0] = enew[0];
+      ecur[1] = enew[1];
+    } else {
+      SKG_TRY(energy(nullptr, 0.0, ecur));
+    }
+    SKG_TRY(gradient(&gg));
+    if (!isfinite(gg)) {
+      info->status = SKG_ERR_NONFINITE;
+      break;
+    }
+    info->residual = sqrt(gg) / r0;
+  }
+  if (info->status == SKG_OK && info->residual >= prm->tol && r0 > 0.0) info->status = SKG_ERR_NOT_CONVERGED;
+  info->energy = ecur[0];
+  return SKG_OK;
+}
+
+}  // namespace skg
+
+using namespace skg;
+
+extern "C" {
+
+int64_t skg_be_workspace_size(const skg_tet_mesh* mesh, int precision) {
+  return skg_assembly_workspace_size(mesh, precision);
+}
+
+int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state, void* workspace,
+                skg_step_info* info_h, void* stream) {
+  if (!params || !state || !workspace || !info_h) return fail(SKG_ERR_ARG, "be_step: null argument");
+  SKG_TRY(check_mesh(mesh, params->precision));
+  if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "be_step: dt must be positive");
+  if (!state->u || !state->u_curr || !state->u_prev || !state->mass) return fail(SKG_ERR_ARG, "be_step: null state");
+  if (params->do_line_search && !(params->ls_alpha > 0.0 && params->ls_alpha <= 0.5))
+    return fail(SKG_ERR_ARG, "line search alpha must lie in (0, 0.5]");
+  if (params->do_line_search && !(params->ls_beta > 0.0 && params->ls_beta < 1.0))
+    return fail(SKG_ERR_ARG, "line search beta must lie in (0, 1)");
+  cudaStream_t s = as_stream(stream);
+  Workspace w = carve_workspace(mesh, params->precision, workspace);
+  if (params->precision == SKG_MIXED) return be_step<float>(mesh, params, state, w, info_h, s);
+  return be_step<double>(mesh, params, state, w, info_h, s);
+}
+
+int64_t skg_pcg_workspace_size(int64_t nbr) {
+  Carve c(nullptr);
+  for (int k = 0; k < 5; ++k) c.take<double>(4 * nbr);
+  c.take<double>(9 * nbr);
+  c.take<double>(8 * kMaxGrid);
+  c.take<unsigned>(16);
+  c.take<double>(64);
+  return c.off + 256;
+}
+
+// Generic symmetric solve for newton_solver's spsolve (newton.py:52): FP64
+// block-Jacobi PCG on a block matrix in the entry-major layout.
+__global__ void k_diag_inverse(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val,
+                               double* jinv) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= nbr) return;
+  const int rp = rowptr[v], K = rowptr[v + 1] - rp;
+  double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < K; ++k)
+    if (col[rp + k] == v)
+      for (int m = 0; m < 9; ++m) a[m] = val[9 * (int64_t)rp + (int64_t)m * K + k];
+  double C[9];
+  cof3(a, C);
+  const double det = a[0] * C[0] + a[1] * C[1] + a[2] * C[2];
+  double* ji = jinv + 9 * v;
+  if (det != 0.0 && isfinite(det)) {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) ji[3 * i + j] = C[3 * j + i] / det;
+  } else {
+    for (int m = 0; m < 9; ++m) ji[m] = (m % 4 == 0 && a[m] != 0.0) ? 1.0 / a[m] : 0.0;
+  }
+}
+
+int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                  double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* workspace, void* stream) {
+  if (nbr <= 0 || !rowptr || !col || !val || !b || !x || !workspace) return fail(SKG_ERR_ARG, "pcg: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  Carve c(workspace);
+  PcgVecs<double> v;
+  v.x = c.take<double>(4 * nbr); v.r = c.take<double>(4 * nbr); v.z = c.take<double>(4 * nbr);
+  v.p = c.take<double>(4 * nbr); v.q = c.take<double>(4 * nbr);
+  double* jinv = c.take<double>(9 * nbr);
+  double* partials = c.take<double>(8 * kMaxGrid);
+  unsigned* counter = c.take<unsigned>(16);
+  double* scal = c.take<double>(64);
+  SKG_CUDA(cudaMemsetAsync(counter, 0, 16 * sizeof(unsigned), s));
+  k_diag_inverse<<<blocks_for(nbr), kBlock, 0, s>>>(nbr, rowptr, col, val, jinv);
+  SKG_LAUNCHED();
+  Bsr<double> A{nbr, rowptr, col, val, jinv};
+  PcgResult pr{};
+  SKG_TRY(pcg_solve<double>(A, b, 1.0, nullptr, v, rtol, max_iter, 1, partials, counter, scal, s, &pr));
+  k_unpad<double><<<blocks_for(nbr), kBlock, 0, s>>>(v.x, nbr, x);
+  SKG_LAUNCHED();
+  SKG_CUDA(cudaStreamSynchronize(s));
+  if (iters_h) *iters_h = pr.iters;
+  if (pr.status != 0) return fail(pr.status, "pcg failed with status %d", pr.status);
+  if (!(pr.rr <= rtol * rtol * pr.bb) && pr.bb > 0.0)
+    return fail(SKG_ERR_NOT_CONVERGED, "pcg reached %d iterations at relative residual %.3e", pr.iters,
+                sqrt(pr.rr / pr.bb));
+  return SKG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+"""Device-resident tet mesh: rest-shape operator, material and sparsity maps.
+
+One ``TetMesh`` replaces what simkit precomputes per mesh for this path:
+``deformation_jacobian`` (``simkit/deformation_jacobian.py:9-87``) becomes a
+per-tet inverse rest edge matrix, ``volume`` (``simkit/volume.py:14-41``) a
+per-tet signed volume (both computed by the ``skg_tet_setup`` kernel), and
+the sparsity of ``J^T blockdiag(He) J`` (``snh.py:536-537``) a block pattern
+with deterministic gather maps (``skg_pattern_build``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import TetMeshC, check
+
+
+def _stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class TetMesh:
+    """Rest mesh of n vertices and t tets on one GPU.
+
+    Parameters
+    ----------
+    X : (n, 3) rest positions;  T : (t, 4) tets;  mu, lam : (t,) or (t, 1).
+    """
+
+    def __init__(self, X, T, mu, lam, device="cuda"):
+        lib = _lib.load()
+        X = np.ascontiguousarray(np.asarray(X, dtype=np.float64).reshape(-1, 3))
+        T = np.ascontiguousarray(np.asarray(T).reshape(-1, 4).astype(np.int32))
+        self.n = n = X.shape[0]
+        self.t = t = T.shape[0]
+        if t == 0:
+            raise ValueError("mesh has no tets")
+        if T.min() < 0 or T.max() >= n:
+            raise ValueError("tet indices out of range")
+        self.device = torch.device(device)
+        dev = self.device
+        self.X_host = X
+        self.T_host = T
+        self.X = torch.from_numpy(X.reshape(-1)).to(dev)
+        self.tets = torch.from_numpy(T).to(dev)
+        self.dinv = torch.empty(9 * t, dtype=torch.float64, device=dev)
+        self.vol = torch.empty(t, dtype=torch.float64, device=dev)
+        check(lib.skg_tet_setup(_ptr(self.X), _ptr(self.tets), n, t, _ptr(self.dinv), _ptr(self.vol), _stream_ptr()))
+        self.mu = torch.as_tensor(np.asarray(mu, dtype=np.float64).reshape(-1), device=dev).contiguous()
+        self.lam = torch.as_tensor(np.asarray(lam, dtype=np.float64).reshape(-1), device=dev).contiguous()
+        if self.mu.numel() != t or self.lam.numel() != t:
+            raise ValueError("mu and lam need one value per tet")
+        self.dinv32 = self.dinv.float()
+        self.mat32 = torch.stack([self.vol, self.mu, self.lam]).float().contiguous()
+        # pattern on the host (integer work, once per mesh)
+        nb = ctypes.c_int64(0)
+        Tp = T.ctypes.data_as(ctypes.c_void_p)
+        check(lib.skg_pattern_build(Tp, n, t, ctypes.byref(nb), None, None, None, None, None, None, None))
+        nb = nb.value
+        self.nb = nb
+        rowptr = np.empty(n + 1, np.int32)
+        col = np.empty(nb, np.int32)
+        diag = np.empty(n, np.int32)
+        hc_ptr = np.empty(nb + 1, np.int32)
+        hc_src = np.empty(16 * t, np.int32)
+        v2t_ptr = np.empty(n + 1, np.int32)
+        v2t = np.empty(4 * t, np.int32)
+        a = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+        check(lib.skg_pattern_build(Tp, n, t, ctypes.byref(ctypes.c_int64(0)), a(rowptr), a(col), a(diag),
+                                    a(hc_ptr), a(hc_src), a(v2t_ptr), a(v2t)))
+        self.rowptr_host = rowptr
+        self.col_host = col
+        row = np.repeat(np.arange(n, dtype=np.int32), np.diff(rowptr))
+        up = lambda x: torch.from_numpy(x).to(dev)
+        self.rowptr, self.col, self.diag, self.row = up(rowptr), up(col), up(diag), up(row)
+        self.hc_ptr, self.hc_src, self.v2t_ptr, self.v2t = up(hc_ptr), up(hc_src), up(v2t_ptr), up(v2t)
+        self.c = TetMeshC(
+            n_verts=n, n_tets=t, n_blocks=nb,
+            tets=self.tets.data_ptr(), dinv=self.dinv.data_ptr(), dinv32=self.dinv32.data_ptr(),
+            vol=self.vol.data_ptr(), mu=self.mu.data_ptr(), lam=self.lam.data_ptr(), mat32=self.mat32.data_ptr(),
+            bsr_rowptr=self.rowptr.data_ptr(), bsr_col=self.col.data_ptr(), bsr_diag=self.diag.data_ptr(),
+            bsr_row=self.row.data_ptr(), hc_ptr=self.hc_ptr.data_ptr(), hc_src=self.hc_src.data_ptr(),
+            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr())
+        self._scalar_perm = None
+
+    # ----------------------------------------------------------------- utils
+    def set_material(self, mu, lam, vol=None):
+        """Replace per-tet mu, lam (and quadrature weights vol) in place."""
+        def dev(a):
+            a = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.asarray(a, dtype=np.float64))
+            a = a.to(device=self.device, dtype=torch.float64).reshape(-1)
+            if a.numel() != self.t:
+                raise ValueError("material arrays need one value per tet")
+            return a
+        self.mu.copy_(dev(mu))
+        self.lam.copy_(dev(lam))
+        if vol is not None:
+            self.vol.copy_(dev(vol))
+        self.mat32.copy_(torch.stack([self.vol, self.mu, self.lam]).float())
+
+    def workspace(self, precision) -> torch.Tensor:
+        nbytes = _lib.load().skg_assembly_workspace_size(ctypes.byref(self.c), precision)
+        if nbytes < 0:
+            raise ValueError(_lib.last_error())
+        return torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
+
+    def scalar_pattern(self):
+        """(indptr, indices, perm): scalar CSR pattern of the block matrix and the
+        permutation taking block values (entry-major layout) to CSR data order."""
+        if self._scalar_perm is None:
+            rp = self.rowptr_host.astype(np.int64)
+            col = self.col_host.astype(np.int64)
+            n = self.n
+            K = np.diff(rp)
+            # scalar row 3v+i holds, for blocks k (sorted columns) and j, value
+            # val[9 rp_v + (3i+j) K_v + k]
+            vrow = np.repeat(np.arange(n), K)          # block row of each slot
+            kloc = np.arange(col.size) - rp[vrow]     # local index in its row
+            indptr = np.zeros(3 * n + 1, np.int64)
+            indptr[1:] = np.repeat(3 * K, 3).cumsum()
+            indices = np.empty(9 * col.size, np.int64)
+            perm = np.empty(9 * col.size, np.int64)
+            for i in range(3):
+                # position of (slot, i, j) in CSR: indptr[3v+i] + 3 kloc + j
+                base = indptr[3 * vrow + i] + 3 * kloc
+                for j in range(3):
+                    indices[base + j] = 3 * col + j
+                    perm[base + j] = 9 * rp[vrow] + (3 * i + j) * K[vrow] + kloc
+            self._scalar_perm = (indptr, indices, perm)
+        return self._scalar_perm
+
+    def block_values_to_csr(self, val: torch.Tensor):
+        """scipy CSR (3n x 3n) from device block values."""
+        import scipy.sparse as sps
+        indptr, indices, perm = self.scalar_pattern()
+        data = val.double().cpu().numpy()[perm]
+        return sps.csr_matrix((data, indices, indptr), shape=(3 * self.n, 3 * self.n))

@@ -1,0 +1,159 @@
+"""Device-resident backward-Euler rollout of one elastic body.
+
+``BESolver.step()`` is one call of simkit's ``backward_euler`` (
+``simkit/integrators/backward_euler.py:27-91``) with the stable neo-Hookean
+closures, gravity, pinned DOFs held at rest, and Newton iterated until the
+relative residual ``||g(x)|| / ||g(x_tilde)||`` falls below ``tol`` - all on
+the GPU through ``skg_be_step``.  Positions stay in HBM between steps.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import BEParamsC, BEStateC, StepInfoC, check, SKG_FP64, SKG_MIXED
+from .mesh import TetMesh, _stream_ptr
+
+PRECISIONS = {"fp64": SKG_FP64, "mixed": SKG_MIXED}
+
+
+@dataclass
+class StepInfo:
+    newton_iters: int
+    pcg_iters: int
+    ls_trials: int
+    status: int
+    residual0: float
+    residual: float
+    min_alpha: float
+    energy: float
+    launches: int = 0
+    t_hessian_ms: float = 0.0
+    t_assemble_ms: float = 0.0
+    t_pcg_ms: float = 0.0
+    t_gradient_ms: float = 0.0
+    t_energy_ms: float = 0.0
+
+    @property
+    def converged(self) -> bool:
+        return self.status == 0
+
+
+def lumped_mass(X, T, rho) -> np.ndarray:
+    """sum over incident tets of rho vol / 4 (simkit/massmatrix.py:40-50)."""
+    e = X[T[:, 1:]] - X[T[:, [0]]]
+    vol = np.linalg.det(e) / 6.0
+    m = np.zeros(X.shape[0])
+    np.add.at(m, T.ravel(), np.repeat(np.asarray(rho, dtype=np.float64) * vol / 4.0, 4))
+    return m
+
+
+class BESolver:
+    """Backward-Euler stepper for one tet mesh on one GPU.
+
+    Parameters
+    ----------
+    X, T, mu, lam : rest mesh and per-tet Lame parameters (simkit conventions)
+    rho : density; gravity : (3,) acceleration; pinned : vertex indices held at rest
+    dt : time step; tol : relative residual stop; max_newton : Newton cap
+    precision : 'mixed' (FP32 Hessian/SpMV, FP64 residual/dots/energy sums) or 'fp64'
+    """
+
+    def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
+                 tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=1e-4, pcg_max_iter=4000, pcg_mode=1,
+                 do_line_search=True, ls_threshold=None, profile=False, device="cuda"):
+        _lib.load()
+        self.mesh = TetMesh(X, T, mu, lam, device=device)
+        m = self.mesh
+        dev = m.device
+        X = m.X_host
+        self.precision = PRECISIONS[precision]
+        mass = lumped_mass(X, m.T_host, rho)
+        self.mass = torch.from_numpy(mass).to(dev)
+        g = np.asarray(gravity, dtype=np.float64)
+        self.f_ext = torch.from_numpy((mass[:, None] * g[None, :]).reshape(-1)).to(dev)
+        pin = np.zeros(3 * m.n, np.uint8)
+        pv = np.asarray(pinned, dtype=np.int64).ravel()
+        pin[(3 * pv[:, None] + np.arange(3)[None, :]).ravel()] = 1
+        self.pinned = torch.from_numpy(pin).to(dev)
+        self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
+        self.u_curr = torch.zeros_like(self.u_prev)
+        self.u_next = torch.zeros_like(self.u_prev)
+        nbytes = _lib.load().skg_be_workspace_size(ctypes.byref(m.c), self.precision)
+        if nbytes < 0:
+            raise ValueError(_lib.last_error())
+        self.workspace = torch.zeros(int(nbytes), dtype=torch.uint8, device=dev)
+        self.params = BEParamsC(
+            dt=dt, tol=tol, max_newton=max_newton, precision=self.precision, pcg_rtol=pcg_rtol,
+            pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
+            ls_max_iter=100, pcg_mode=pcg_mode,
+            ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
+            profile=int(profile))
+        self.steps = 0
+        self._host = None
+
+    @classmethod
+    def from_spec(cls, spec, **kw):
+        return cls(spec.X, spec.T, spec.mu, spec.lam, rho=spec.rho, gravity=spec.gravity, pinned=spec.pinned, **kw)
+
+    def step(self, stream=None) -> StepInfo:
+        st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
+                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr())
+        info = StepInfoC()
+        check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
+                                      ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),
+                                      _stream_ptr(stream)))
+        # rotate history: prev <- curr <- next
+        self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+        self.steps += 1
+        return StepInfo(info.newton_iters, info.pcg_iters, info.ls_trials, info.status, info.residual0,
+                        info.residual, info.min_alpha, info.energy, info.launches, info.t_hessian_ms,
+                        info.t_assemble_ms, info.t_pcg_ms, info.t_gradient_ms, info.t_energy_ms)
+
+    def step_host(self, x_curr: np.ndarray, x_prev: np.ndarray, out: np.ndarray = None, stream=None):
+        """One step with host positions in and out (simkit's backward_euler contract:
+        x_curr, x_prev (3n, 1) float64 -> x_next).  Copies host->device, steps, copies back."""
+        m = self.mesh
+        if self._host is None:
+            self._host = [torch.empty(3 * m.n, dtype=torch.float64, pin_memory=True) for _ in range(3)]
+            self._X = torch.from_numpy(m.X_host.reshape(-1).copy()).to(m.device)
+        hc, hp, hn = self._host
+        hc.numpy()[:] = np.asarray(x_curr, dtype=np.float64).reshape(-1)
+        hp.numpy()[:] = np.asarray(x_prev, dtype=np.float64).reshape(-1)
+        self.u_curr.copy_(hc, non_blocking=True)
+        self.u_prev.copy_(hp, non_blocking=True)
+        self.u_curr.sub_(self._X)
+        self.u_prev.sub_(self._X)
+        info = self.step(stream)
+        self.u_next.copy_(self.u_curr).add_(self._X)      # u_next is scratch after the rotation
+        hn.copy_(self.u_next, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        res = hn.numpy().reshape(-1, 1)
+        if out is not None:
+            out[...] = res
+            return out, info
+        return res.copy(), info
+
+    def displacement(self) -> np.ndarray:
+        return self.u_curr.cpu().numpy().copy()
+
+    def positions(self) -> np.ndarray:
+        return self.mesh.X_host.reshape(-1) + self.displacement()
+
+    def set_state(self, u_curr, u_prev):
+        self.u_curr.copy_(torch.as_tensor(np.asarray(u_curr, dtype=np.float64).reshape(-1)))
+        self.u_prev.copy_(torch.as_tensor(np.asarray(u_prev, dtype=np.float64).reshape(-1)))
+
+    def rollout(self, steps, callback=None):
+        infos = []
+        for k in range(steps):
+            info = self.step()
+            infos.append(info)
+            if callback is not None:
+                callback(k, self, info)
+        return infos

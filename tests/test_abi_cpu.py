@@ -1,0 +1,212 @@
+"""CPU checks of the native boundary: the library builds, loads and exports
+every function the public header declares; the element math the kernels run
+(compiled for the host from the same header) agrees with the oracle."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import psd, snh
+
+HEADER = os.path.join(ROOT, "include", "simkit_gb300.h")
+HOST_SRC = os.path.join(ROOT, "tests", "native", "snh_host.cpp")
+HOST_SO = os.path.join(ROOT, "tests", "_build", "snh_host.so")
+
+
+@pytest.fixture(scope="session")
+def libpath():
+    from simkit_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from simkit_gb300.build import build_library
+        build_library()
+    return _lib.LIB_PATH
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t)\s+(skg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_the_binding():
+    from simkit_gb300 import _lib
+    assert set(declared_functions()) == set(_lib.exported_symbols())
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    lib = ctypes.CDLL(libpath)
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    from simkit_gb300 import _lib
+    assert _lib.load().skg_version() >= 100
+
+
+def test_error_path_without_gpu(libpath):
+    """Argument validation runs before any device work and reports through skg_last_error."""
+    from simkit_gb300 import _lib
+    lib = _lib.load()
+    assert lib.skg_snh_energy_element_F(4, 0, None, None, None, None, 1, None) == _lib.SKG_ERR_ARG
+    assert "dim" in _lib.last_error()
+    assert lib.skg_psd_project(None, None, 1, 13, 0, None) == _lib.SKG_ERR_ARG
+
+
+def test_pattern_builder_matches_scipy():
+    """The host pattern builder reproduces scipy's pattern of J^T blockdiag(He) J."""
+    from simkit_gb300 import _lib
+    from simkit_gb300.beams import make_beam
+    from oracle import fem
+    lib = _lib.load()
+    b = make_beam(3, 2, 4, jitter=0.1, seed=2)
+    T = np.ascontiguousarray(b.T.astype(np.int32))
+    n, t = b.n_verts, b.n_tets
+    nb = ctypes.c_int64()
+    a = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    assert lib.skg_pattern_build(a(T), n, t, ctypes.byref(nb), None, None, None, None, None, None, None) == 0
+    nb = nb.value
+    rp = np.empty(n + 1, np.int32); col = np.empty(nb, np.int32); dg = np.empty(n, np.int32)
+    hp = np.empty(nb + 1, np.int32); hs = np.empty(16 * t, np.int32)
+    vp = np.empty(n + 1, np.int32); vt = np.empty(4 * t, np.int32)
+    assert lib.skg_pattern_build(a(T), n, t, ctypes.byref(ctypes.c_int64()), a(rp), a(col), a(dg), a(hp), a(hs),
+                                 a(vp), a(vt)) == 0
+    J = fem.deformation_jacobian(b.X, b.T)
+    x = b.X + 1e-3 * np.random.default_rng(0).standard_normal(b.X.shape)
+    K = snh.hessian_x(x, J, b.mu, b.lam, fem.tet_volumes(b.X, b.T))
+    K.sort_indices()
+    # expand blocks to scalars
+    rows = []
+    for v in range(n):
+        for i in range(3):
+            rows.append(np.concatenate([[3 * c, 3 * c + 1, 3 * c + 2] for c in col[rp[v]:rp[v + 1]]]))
+    indptr = np.concatenate([[0], np.cumsum([r.size for r in rows])])
+    assert np.array_equal(indptr, K.indptr)
+    assert np.array_equal(np.concatenate(rows), K.indices)
+    assert np.all(col[dg] == np.arange(n))
+    # every (tet, a, b) block appears exactly once, lists ordered by tet
+    assert hp[-1] == 16 * t and np.all(np.diff(hp) > 0)
+    for s in range(nb):
+        tets = hs[hp[s]:hp[s + 1]] >> 4
+        assert np.all(np.diff(tets) > 0)
+    assert vp[-1] == 4 * t
+
+
+def test_pattern_rejects_bad_tets():
+    from simkit_gb300 import _lib
+    lib = _lib.load()
+    T = np.array([[0, 1, 1, 2]], np.int32)
+    nb = ctypes.c_int64()
+    assert lib.skg_pattern_build(T.ctypes.data_as(ctypes.c_void_p), 3, 1, ctypes.byref(nb), None, None, None,
+                                 None, None, None, None) == _lib.SKG_ERR_ARG
+    T = np.array([[0, 1, 2, 7]], np.int32)
+    assert lib.skg_pattern_build(T.ctypes.data_as(ctypes.c_void_p), 4, 1, ctypes.byref(nb), None, None, None,
+                                 None, None, None, None) == _lib.SKG_ERR_ARG
+
+
+# ------------------------------------------------- host build of the kernels' math
+@pytest.fixture(scope="session")
+def hostmath():
+    os.makedirs(os.path.dirname(HOST_SO), exist_ok=True)
+    if not os.path.exists(HOST_SO) or os.path.getmtime(HOST_SO) < max(
+            os.path.getmtime(HOST_SRC), os.path.getmtime(os.path.join(ROOT, "simkit_gb300", "csrc", "snh_math.cuh"))):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", HOST_SO, HOST_SRC])
+    return ctypes.CDLL(HOST_SO)
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _cases(rng, t=300):
+    F = np.eye(3)[None] + np.concatenate([0.05 * rng.standard_normal((t // 4, 3, 3)),
+                                          0.3 * rng.standard_normal((t // 4, 3, 3)),
+                                          1.0 * rng.standard_normal((t // 4, 3, 3)),
+                                          0.2 * rng.standard_normal((t - 3 * (t // 4), 3, 3))])
+    F[3 * (t // 4):, :, 0] *= -1.0       # inverted elements
+    ym = np.exp(rng.uniform(np.log(1e5), np.log(1e7), t))
+    pr = rng.uniform(0.3, 0.49, t)
+    mu, lam = ym / (2 * (1 + pr)), ym * pr / ((1 + pr) * (1 - 2 * pr))
+    vol = rng.uniform(1e-7, 5e-6, t)
+    X = rng.standard_normal((t, 4, 3))
+    E = (X[:, 1:] - X[:, [0]]).transpose(0, 2, 1)
+    Dinv = np.linalg.inv(E)
+    gN = np.empty((t, 4, 3))
+    gN[:, 1:] = Dinv
+    gN[:, 0] = -Dinv.sum(1)
+    return np.ascontiguousarray(F), mu, lam, vol, np.ascontiguousarray(gN)
+
+
+def _unpack78(o):
+    t = o.shape[0]
+    K = np.zeros((t, 12, 12))
+    iu = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+    for a in range(4):
+        for n_, (i, k) in enumerate(iu):
+            K[:, 3 * a + i, 3 * a + k] = o[:, 6 * a + n_]
+            K[:, 3 * a + k, 3 * a + i] = o[:, 6 * a + n_]
+    for q, (a, b) in enumerate([(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]):
+        blk = o[:, 24 + 9 * q:33 + 9 * q].reshape(t, 3, 3)
+        K[:, 3 * a:3 * a + 3, 3 * b:3 * b + 3] = blk
+        K[:, 3 * b:3 * b + 3, 3 * a:3 * a + 3] = blk.transpose(0, 2, 1)
+    return K
+
+
+def lifted_oracle(F, mu, lam, vol, gN):
+    H9p = psd.psd_project(snh.hessian_element_F(F, mu, lam) * vol[:, None, None])
+    t = F.shape[0]
+    return np.einsum("taj,tbl,tijkl->taibk", gN, gN, H9p.reshape(t, 3, 3, 3, 3)).reshape(t, 12, 12)
+
+
+@pytest.mark.parametrize("prec,tol", [(64, 1e-12), (32, 3e-6)])
+def test_tet_hessian_analytic_psd_matches_eigh_floor(hostmath, prec, tol):
+    """Analytic-eigensystem PSD floor + 12x12 lift == simkit's eigh floor of vol*He, lifted."""
+    rng = np.random.default_rng(5)
+    F, mu, lam, vol, gN = _cases(rng)
+    t = F.shape[0]
+    out = np.zeros((t, 78))
+    hostmath.h_tet_hessian(prec, ctypes.c_int64(t), _p(F), _p(mu), _p(lam), _p(vol), _p(gN), _p(out),
+                           ctypes.c_double(0.1))
+    K = _unpack78(out)
+    Ko = lifted_oracle(F, mu, lam, vol, gN)
+    err = np.abs(K - Ko).max(axis=(1, 2)) / np.abs(Ko).max(axis=(1, 2))
+    assert err.max() < tol
+
+
+def test_displacement_forms_match_oracle(hostmath):
+    rng = np.random.default_rng(6)
+    t = 200
+    G = np.concatenate([1e-4 * rng.standard_normal((t // 2, 3, 3)), 0.1 * rng.standard_normal((t // 2, 3, 3))])
+    mu = rng.uniform(3e4, 3e6, t)
+    lam = mu * rng.uniform(1.5, 40, t)
+    d64, P64 = np.zeros(t), np.zeros((t, 9))
+    hostmath.h_disp(64, ctypes.c_int64(t), _p(np.ascontiguousarray(G)), _p(mu), _p(lam), _p(d64), _p(P64))
+    F = np.eye(3)[None] + G
+    rest = snh.energy_element_F(np.repeat(np.eye(3)[None], t, 0), mu, lam).ravel()
+    dpsi = snh.energy_element_F(F, mu, lam).ravel() - rest
+    # the oracle's difference of two O(mu) numbers is itself only good to ~1e-16 |rest|
+    assert np.all(np.abs(d64 - dpsi) <= 1e-9 * np.abs(dpsi) + 1e-15 * np.abs(rest))
+    Po = snh.gradient_element_F(F, mu, lam).reshape(t, 9)
+    assert np.all(np.abs(P64 - Po).max(1) <= 1e-9 * np.abs(Po).max(1) + 1e-15 * mu)
+    # FP32: relative to the element's own scale
+    d32, P32 = np.zeros(t), np.zeros((t, 9))
+    hostmath.h_disp(32, ctypes.c_int64(t), _p(np.ascontiguousarray(G)), _p(mu), _p(lam), _p(d32), _p(P32))
+    assert np.max(np.abs(d32 - d64) / np.abs(d64)) < 2e-5
+    assert np.max(np.abs(P32 - P64).max(1) / np.abs(P64).max(1)) < 2e-5
+
+
+def test_svd_rotation_variant(hostmath):
+    rng = np.random.default_rng(7)
+    F, *_ = _cases(rng, 200)
+    t = F.shape[0]
+    for prec, tol in ((64, 1e-12), (32, 2e-5)):
+        U, s, V = np.zeros((t, 9)), np.zeros((t, 3)), np.zeros((t, 9))
+        hostmath.h_svd(prec, ctypes.c_int64(t), _p(F), _p(U), _p(s), _p(V))
+        U, V = U.reshape(t, 3, 3), V.reshape(t, 3, 3)
+        R = U @ (s[:, :, None] * V.transpose(0, 2, 1))
+        assert np.abs(R - F).max() < tol * np.abs(F).max() * 10
+        assert np.allclose(np.linalg.det(U), 1, atol=1e-4) and np.allclose(np.linalg.det(V), 1, atol=1e-4)
+        assert np.all(s[:, 0] >= s[:, 1] - 1e-6) and np.all(s[:, 1] >= np.abs(s[:, 2]) - 1e-6)
+        assert np.all(np.sign(s[:, 2]) == np.sign(np.linalg.det(F)))

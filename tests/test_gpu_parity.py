@@ -1,0 +1,191 @@
+"""GPU parity of the CUDA path against the FP64 oracle and the reference fixtures.
+
+Tolerances (stated per check):
+* FP64 kernels vs the reference: 1e-12 relative (element tier), 1e-10 (assembled).
+* FP32 ("mixed") element Hessians: 3e-6 relative to the block's largest entry.
+* Rollouts: positions within 1e-5 relative to the reference after every
+  stored step (the stated parity bar), displacements within 1e-3.
+"""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def api():
+    import simkit_gb300 as sk
+    return sk
+
+
+@pytest.mark.parametrize("name", ["element_3d.npz", "element_2d.npz"])
+def test_element_tier_fp64_matches_reference(api, name):
+    d = _load(name)
+    F, mu, lam = d["F"], d["mu"], d["lam"]
+    psi = api.stable_neo_hookean_energy_element_F(F, mu, lam)
+    assert psi.shape == d["psi"].shape
+    assert np.abs(psi - d["psi"]).max() <= 1e-12 * np.abs(d["psi"]).max()
+    P = api.stable_neo_hookean_gradient_element_F(F, mu, lam)
+    assert P.shape == d["P"].shape and _rel(P, d["P"]) < 1e-12
+    H = api.stable_neo_hookean_hessian_element_F(F, mu, lam)
+    err = np.abs(H - d["He"]).max(axis=(1, 2)) / np.abs(d["He"]).max(axis=(1, 2))
+    assert H.shape == d["He"].shape and err.max() < 1e-12
+
+
+@pytest.mark.parametrize("name", ["element_3d.npz", "element_2d.npz"])
+def test_psd_project_matches_reference(api, name):
+    d = _load(name)
+    H = d["He"] * d["vol"].reshape(-1, 1, 1)
+    Hp = api.psd_project(H)
+    err = np.abs(Hp - d["He_proj"]).max(axis=(1, 2)) / np.abs(d["He_proj"]).max(axis=(1, 2))
+    assert err.max() < 1e-9
+    assert np.linalg.eigvalsh(Hp).min() >= 1e-6 - 1e-9 * np.abs(Hp).max()
+
+
+def test_psd_project_small_cases(api):
+    """simkit tests/test_psd_project.py cases: floor holds, batch shape kept."""
+    H = np.array([[1.0, 0.5], [0.5, -0.2]])
+    Hp = api.psd_project(H, method="proj")[0]
+    assert np.all(np.linalg.eigvalsh(Hp) >= 1e-6 - 1e-12)
+    rng = np.random.default_rng(0)
+    H = rng.standard_normal((4, 3, 3))
+    H = H + H.transpose(0, 2, 1)
+    Hp = api.psd_project(H, method="proj")
+    assert Hp.shape == (4, 3, 3) and np.all(np.linalg.eigvalsh(Hp) >= 1e-6 - 1e-12)
+    Ha = api.psd_project(H, method="abs")
+    assert np.allclose(np.sort(np.linalg.eigvalsh(Ha)), np.sort(np.abs(np.linalg.eigvalsh(H))), atol=1e-10)
+
+
+def test_deformation_jacobian_and_volume(api):
+    from oracle import fem
+    d = _load("beam_small.npz")
+    X, T = d["X"], d["T"]
+    J = api.deformation_jacobian(X, T)
+    vol = api.volume(X, T)
+    assert _rel(vol, d["vol"]) < 1e-14
+    x = d["x"]
+    F = (J @ x.reshape(-1, 1)).reshape(-1, 3, 3)
+    Fo = fem.deformation_gradient(X, T, x)
+    assert _rel(F, Fo) < 1e-12
+    Js = J.to_scipy()
+    Jr = fem.deformation_jacobian(X, T)
+    assert abs(Js - Jr).max() < 1e-9 * abs(Jr).max()
+
+
+def test_assembled_tier_matches_reference(api):
+    d = _load("beam_small.npz")
+    X, T = d["X"], d["T"]
+    J = api.deformation_jacobian(X, T)
+    vol = api.volume(X, T)
+    x = d["x"]
+    E = api.stable_neo_hookean_energy_x(x, J, d["mu"], d["lam"], vol)
+    assert abs(E - float(d["energy"])) <= 1e-12 * abs(float(d["energy"]))
+    g = api.stable_neo_hookean_gradient_x(x, J, d["mu"], d["lam"], vol)
+    assert g.shape == d["gradient"].shape and _rel(g, d["gradient"]) < 1e-10
+    K = api.stable_neo_hookean_hessian_x(x, J, d["mu"], d["lam"], vol)
+    K = K.tocsr()
+    K.sort_indices()
+    assert np.array_equal(K.indptr, d["K_indptr"]) and np.array_equal(K.indices, d["K_indices"])
+    assert _rel(K.data, d["K_data"]) < 1e-10
+
+
+def test_mixed_precision_hessian_and_determinism(api):
+    """FP32 Hessian assembly within 3e-6 of the FP64 one; two assemblies are bitwise equal."""
+    from simkit_gb300.mesh import TetMesh
+    from simkit_gb300.beams import make_beam
+    b = make_beam(6, 3, 3, ym=np.exp(np.random.default_rng(1).uniform(np.log(1e5), np.log(1e7), 6 * 54)),
+                  jitter=0.1, seed=3)
+    x = b.X + 2e-3 * np.random.default_rng(2).standard_normal(b.X.shape)
+    m = TetMesh(b.X, b.T, b.mu, b.lam)
+    from simkit_gb300.api import assemble_hessian_blocks
+    v64 = assemble_hessian_blocks(m, x, precision="fp64")
+    v32a = assemble_hessian_blocks(m, x, precision="mixed")
+    v32b = assemble_hessian_blocks(m, x, precision="mixed")
+    assert torch.equal(v32a, v32b)
+    K64 = m.block_values_to_csr(v64)
+    K32 = m.block_values_to_csr(v32a)
+    assert abs(K64 - K32).max() <= 3e-6 * abs(K64).max()
+
+
+def test_pcg_solves_spd_block_system(api):
+    from simkit_gb300.api import solve_sparse
+    import scipy.sparse as sps
+    rng = np.random.default_rng(3)
+    n = 3 * 40
+    A = sps.random(n, n, density=0.05, random_state=4)
+    A = (A @ A.T + sps.eye(n) * 4.0).tocsr()
+    b = rng.standard_normal((n, 1))
+    x = solve_sparse(A, b, rtol=1e-12)
+    assert np.allclose(A @ x, b, atol=1e-8)
+
+
+def test_be_step_fp64_matches_reference_rollout(api):
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision="fp64", pcg_rtol=1e-10)
+    X = spec.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, info
+        k = list(d["steps"]).index(step)
+        u = s.displacement()
+        assert _rel(X + u, X + d["u"][k]) < 1e-7
+        assert _rel(u, d["u"][k]) < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_rollout_8x8x32_matches_reference(api, precision):
+    """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision)
+    X = spec.X.reshape(-1)
+    worst_pos, worst_u = 0.0, 0.0
+    iters = []
+    for step in range(1, 61):
+        info = s.step()
+        iters.append(info.newton_iters)
+        assert info.converged, (step, info)
+        if step in d["steps"]:
+            k = list(d["steps"]).index(step)
+            u = s.displacement()
+            worst_pos = max(worst_pos, _rel(X + u, X + d["u"][k]))
+            worst_u = max(worst_u, _rel(u, d["u"][k]))
+    print(f"\n{precision}: positions rel err {worst_pos:.2e}, displacement rel err {worst_u:.2e}, "
+          f"newton iters {sum(iters)} (reference {int(d['iters'].sum())})")
+    assert worst_pos < 1e-5
+    assert worst_u < 1e-3
+
+
+def test_nonfinite_input_is_reported(api):
+    """A NaN in the state surfaces as a status, not a hang or a silent result."""
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    spec = make_beam(4, 2, 2, ym=2e5)
+    s = BESolver.from_spec(spec, precision="mixed")
+    u = np.zeros(3 * spec.n_verts)
+    u[3 * 40 + 1] = np.nan
+    s.set_state(u, u)
+    info = s.step()
+    assert info.status == -5
