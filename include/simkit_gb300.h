@@ -222,6 +222,22 @@ int64_t skg_pcg_workspace_size(int64_t n_rows_blocks);
 int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
                   double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* workspace, void* stream);
 
+/* Allocation-free form of skg_pcg_bsr64 (no counterpart in the reference: simkit
+ * calls scipy's spsolve, which allocates freely).  For callers that cannot call
+ * cudaMalloc while they solve - a real-time simulation loop that must not stall
+ * on an allocation, or a host program that owns every device buffer and passes
+ * only inputs and outputs.  Its scratch is one fixed device array inside the
+ * library (about 1 MB, held by every GPU that loads the library until exit),
+ * enough for at most skg_pcg_noalloc_max_rows() block rows (4096, i.e. 12,288
+ * unknowns); larger systems return SKG_ERR_CAPACITY.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress) and should
+ * come before any stream capture.  All calls share that array, so calls that
+ * overlap on the GPU race; serialise them.  Allocates no device memory. */
+int64_t skg_pcg_noalloc_max_rows(void);
+int skg_pcg_bsr64_noalloc(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val,
+                          const double* b, double* x, double rtol, int32_t max_iter, int32_t* iters_h,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,8 @@ _SIGNATURES = {
     "skg_be_step": (c_i32, [P(TetMeshC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC), c_vp]),
     "skg_pcg_workspace_size": (c_i64, [c_i64]),
     "skg_pcg_bsr64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp, c_vp]),
+    "skg_pcg_noalloc_max_rows": (c_i64, []),
+    "skg_pcg_bsr64_noalloc": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp]),
 }
 
 _lock = threading.Lock()

@@ -747,3 +747,99 @@ int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of skg_pcg_bsr64.
+//
+// Some callers cannot allocate device memory when they solve: a real-time
+// loop (an interactive simulation frame, a control loop) that must not stall
+// on cudaMalloc, or a host program that owns every device buffer itself and
+// gives this library only its inputs and outputs.  For them the scratch of
+// the solve (five padded PCG vectors, the 3x3 block-Jacobi inverses, the
+// reduction partials, counters and scalars) lives in one file-scope device
+// array sized for at most kNoAllocMaxRows block rows (12,288 unknowns), about
+// 1 MB that every GPU which loads the library holds until the process exits.
+//
+// Host code cannot pass the array's name to a kernel (on the host it is only
+// a stand-in for the device symbol), so the first call on each device looks
+// the address up with cudaGetSymbolAddress while that device is current and
+// caches it; make that first call before any stream capture.  All calls share
+// the one array: two calls that overlap on the GPU (other streams, other host
+// threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace skg {
+
+constexpr int64_t kNoAllocMaxRows = 4096;
+constexpr int64_t al256(int64_t x) { return (x + 255) & ~int64_t(255); }
+constexpr int64_t kNoAllocBytes = 5 * al256(4 * kNoAllocMaxRows * (int64_t)sizeof(double)) +
+                                  al256(9 * kNoAllocMaxRows * (int64_t)sizeof(double)) +
+                                  al256(8 * (int64_t)kMaxGrid * (int64_t)sizeof(double)) +
+                                  al256(16 * (int64_t)sizeof(unsigned)) + al256(64 * (int64_t)sizeof(double));
+
+static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// device address of the scratch array on the current device (looked up once)
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  SKG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SKG_ERR_CAPACITY, "device ordinal %d not supported", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    SKG_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return SKG_OK;
+}
+
+}  // namespace skg
+
+extern "C" {
+
+int64_t skg_pcg_noalloc_max_rows(void) { return kNoAllocMaxRows; }
+
+int skg_pcg_bsr64_noalloc(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                          double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* stream) {
+  if (nbr <= 0 || !rowptr || !col || !val || !b || !x) return fail(SKG_ERR_ARG, "pcg_noalloc: bad arguments");
+  if (nbr > kNoAllocMaxRows)
+    return fail(SKG_ERR_CAPACITY,
+                "pcg_noalloc: %lld block rows exceed the fixed scratch capacity of %lld block rows; "
+                "use skg_pcg_bsr64 with a caller-provided workspace",
+                (long long)nbr, (long long)kNoAllocMaxRows);
+  void* scratch = nullptr;
+  SKG_TRY(noalloc_scratch(&scratch));
+  cudaStream_t s = as_stream(stream);
+  Carve c(scratch);
+  PcgVecs<double> v;
+  v.x = c.take<double>(4 * nbr); v.r = c.take<double>(4 * nbr); v.z = c.take<double>(4 * nbr);
+  v.p = c.take<double>(4 * nbr); v.q = c.take<double>(4 * nbr);
+  double* jinv = c.take<double>(9 * nbr);
+  double* partials = c.take<double>(8 * kMaxGrid);
+  unsigned* counter = c.take<unsigned>(16);
+  double* scal = c.take<double>(64);
+  // the array keeps the previous call's contents: the reduction counters must start at zero
+  SKG_CUDA(cudaMemsetAsync(counter, 0, 16 * sizeof(unsigned), s));
+  k_diag_inverse<<<blocks_for(nbr), kBlock, 0, s>>>(nbr, rowptr, col, val, jinv);
+  SKG_LAUNCHED();
+  Bsr<double> A{nbr, rowptr, col, val, jinv};
+  PcgResult pr{};
+  SKG_TRY(pcg_solve<double>(A, b, 1.0, nullptr, v, rtol, max_iter, 1, partials, counter, scal, s, &pr));
+  k_unpad<double><<<blocks_for(nbr), kBlock, 0, s>>>(v.x, nbr, x);
+  SKG_LAUNCHED();
+  SKG_CUDA(cudaStreamSynchronize(s));
+  if (iters_h) *iters_h = pr.iters;
+  if (pr.status != 0) return fail(pr.status, "pcg failed with status %d", pr.status);
+  if (!(pr.rr <= rtol * rtol * pr.bb) && pr.bb > 0.0)
+    return fail(SKG_ERR_NOT_CONVERGED, "pcg reached %d iterations at relative residual %.3e", pr.iters,
+                sqrt(pr.rr / pr.bb));
+  return SKG_OK;
+}
+
+}  // extern "C"
