@@ -136,9 +136,19 @@ __global__ void k_assemble(AsmArgs<R> a) {
       for (int j = 0; j < 3; ++j)
         if (a.pinned[3 * v + i] | a.pinned[3 * w + j]) acc[3 * i + j] = (v == w && i == j) ? R(1) : R(0);
   }
-  R* dst = a.val + 9 * (int64_t)rp + k;
+  if (a.val) {
+    R* dst = a.val + 9 * (int64_t)rp + k;
 #pragma unroll
-  for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+    for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+  }
+  if (a.rec) {
+    R* r = a.rec + kRec * s;
+#pragma unroll
+    for (int m = 0; m < 9; ++m) r[m] = acc[m];
+    r[9] = col_bits(w, R(0));
+    r[10] = R(0);
+    r[11] = R(0);
+  }
   if (v == w && a.jinv) {
     R C[9];
     cof3(acc, C);
@@ -356,6 +366,8 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   w.fbuf = c.take<double>(12 * t);
   w.val32 = mixed ? c.take<float>(9 * nb) : nullptr;
   w.val64 = mixed ? nullptr : c.take<double>(9 * nb);
+  w.rec32 = mixed ? c.take<float>(kRec * nb) : nullptr;
+  w.rec64 = mixed ? nullptr : c.take<double>(kRec * nb);
   w.jinv32 = mixed ? c.take<float>(9 * n) : nullptr;
   w.jinv64 = mixed ? nullptr : c.take<double>(9 * n);
   w.g = c.take<double>(3 * n);

@@ -38,9 +38,19 @@ template <typename R> struct AsmArgs {
   const double* mass;    // optional: adds mass/h^2 on diagonal blocks
   double inv_h2;
   const uint8_t* pinned; // optional: 3n DOF mask
-  R* val;
+  R* val;                // entry-major block values (9 nb), or null
+  R* rec;                // 12-wide block records (9 values, column bits, 2 pad), or null
   R* jinv;               // optional: block-Jacobi inverses (9n)
 };
+
+// Block record of the solver's SpMV: the 9 row-major entries of a 3x3 block,
+// the block column stored in the bits of entry 9, entries 10-11 zero, so one
+// block is three 16-byte loads (FP32) instead of ten scalar loads.
+constexpr int kRec = 12;
+__device__ __forceinline__ float col_bits(int c, float) { return __int_as_float(c); }
+__device__ __forceinline__ double col_bits(int c, double) { return __longlong_as_double((long long)c); }
+__device__ __forceinline__ int bits_col(float v) { return __float_as_int(v); }
+__device__ __forceinline__ int bits_col(double v) { return (int)__double_as_longlong(v); }
 
 struct GradArgs {
   int64_t n;
@@ -80,6 +90,8 @@ struct Workspace {
   double* fbuf;
   float* val32;
   double* val64;
+  float* rec32;      // solver block records (kRec per block)
+  double* rec64;
   float* jinv32;
   double* jinv64;
   double* g;

@@ -30,9 +30,32 @@ template <typename R> struct Bsr {
   int64_t nbr;
   const int32_t* rowptr;
   const int32_t* col;
-  const R* val;
+  const R* val;    // entry-major values (used when rec is null)
   const R* jinv;
+  const R* rec;    // 12-wide block records (values + column), preferred
 };
+
+// one 3x3 block and its column from a record (three / six 16-byte loads)
+template <typename R> struct Blk { R m[9]; int col; };
+
+__device__ __forceinline__ Blk<float> ld_rec(const float* __restrict__ rec, int64_t s) {
+  const float4* p = reinterpret_cast<const float4*>(rec) + 3 * s;
+  const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.y)};
+}
+__device__ __forceinline__ Blk<double> ld_rec(const double* __restrict__ rec, int64_t s) {
+  const double2* p = reinterpret_cast<const double2*>(rec) + 6 * s;
+  const double2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3), e = __ldg(p + 4);
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(e.y)};
+}
+
+// 3-term dot in the working precision, widened once
+template <typename R> __device__ __forceinline__ double dot3w(Vec3<R> a, Vec3<R> b) {
+  return double(a.x * b.x + a.y * b.y + a.z * b.z);
+}
+template <> __device__ __forceinline__ double dot3w<double>(Vec3<double> a, Vec3<double> b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
 
 template <typename R> struct PcgVecs {
   R* x;
@@ -57,9 +80,19 @@ template <typename R, int G>
 __device__ __forceinline__ Vec3<R> spmv_row(const Bsr<R>& A, const R* __restrict__ xin, int64_t row, int lane,
                                             bool valid) {
   const int rp = valid ? __ldg(A.rowptr + row) : 0;
-  const int K = valid ? __ldg(A.rowptr + row + 1) - rp : 0;
+  int K = valid ? __ldg(A.rowptr + row + 1) - rp : 0;
   const R* vals = A.val + 9 * (int64_t)rp;
   R a0 = 0, a1 = 0, a2 = 0;
+  if (A.rec) {
+    for (int k = lane; k < K; k += G) {
+      const Blk<R> b = ld_rec(A.rec, rp + k);
+      const Vec3<R> xv = ld3c(xin, b.col);
+      a0 += b.m[0] * xv.x + b.m[1] * xv.y + b.m[2] * xv.z;
+      a1 += b.m[3] * xv.x + b.m[4] * xv.y + b.m[5] * xv.z;
+      a2 += b.m[6] * xv.x + b.m[7] * xv.y + b.m[8] * xv.z;
+    }
+    K = 0;
+  }
   for (int k = lane; k < K; k += G) {
     const int c = __ldg(A.col + rp + k);
     const Vec3<R> xv = ld3c(xin, c);
@@ -100,8 +133,8 @@ __global__ void __launch_bounds__(kBlock) k_pcg_init(Bsr<R> A, const double* __r
     st3(v.z, i, z);
     st3(v.p, i, z);
     st3(v.x, i, Vec3<R>{R(0), R(0), R(0)});
-    acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
-    acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+    acc[0] += dot3w(r, z);
+    acc[1] += dot3w(r, r);
   }
   acc[2] = acc[1];
   if (grid_sum<3, kBlock>(acc, partials, counter, scal + S_TMP) && threadIdx.x == 0) {
@@ -133,8 +166,7 @@ __global__ void __launch_bounds__(kBlock) k_pcg_spmv(Bsr<R> A, PcgVecs<R> v, dou
     const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
     if (lane == 0 && valid) {
       st3(v.q, row, y);
-      const Vec3<R> pv = ld3c(v.p, row);
-      acc[0] += double(pv.x) * y.x + double(pv.y) * y.y + double(pv.z) * y.z;
+      acc[0] += dot3w(ld3c(v.p, row), y);
     }
   }
   if (grid_sum<1, kBlock>(acc, partials, counter, scal + S_PQ) && threadIdx.x == 0) {
@@ -163,8 +195,8 @@ __global__ void __launch_bounds__(kBlock) k_pcg_update(Bsr<R> A, PcgVecs<R> v, d
     st3(v.x, i, x);
     st3(v.r, i, r);
     st3(v.z, i, z);
-    acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
-    acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+    acc[0] += dot3w(r, z);
+    acc[1] += dot3w(r, r);
   }
   if (grid_sum<2, kBlock>(acc, partials, counter, scal + S_TMP) && threadIdx.x == 0) {
     const double rz = scal[S_TMP], rr = scal[S_TMP + 1];
@@ -220,7 +252,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned*
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        if (spins > 256) __nanosleep(32);
       }
     }
     __threadfence();
@@ -253,7 +285,7 @@ __device__ __forceinline__ void all_sum(const double* partials, double (&out)[NV
 }
 
 template <typename R, int G>
-__global__ void __launch_bounds__(kBlock) k_pcg_persistent(Bsr<R> A, PcgVecs<R> v, double* partials,
+__global__ void __launch_bounds__(kBlock, 3) k_pcg_persistent(Bsr<R> A, PcgVecs<R> v, double* partials,
                                                            unsigned* bar, double* scal) {
   // partials: 3 buffers of 2*gridDim doubles (pq | rz, rr | spare)
   double* P1 = partials;
@@ -281,8 +313,7 @@ __global__ void __launch_bounds__(kBlock) k_pcg_persistent(Bsr<R> A, PcgVecs<R> 
       const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
       if (lane == 0 && valid) {
         st3(v.q, row, y);
-        const Vec3<R> pv = ld3c(v.p, row);
-        acc[0] += double(pv.x) * y.x + double(pv.y) * y.y + double(pv.z) * y.z;
+        acc[0] += dot3w(ld3c(v.p, row), y);
       }
     }
     double a1[1] = {acc[0]};
@@ -307,8 +338,8 @@ __global__ void __launch_bounds__(kBlock) k_pcg_persistent(Bsr<R> A, PcgVecs<R> 
       st3(v.x, i, x);
       st3(v.r, i, r);
       st3(v.z, i, z);
-      acc[0] += double(r.x) * z.x + double(r.y) * z.y + double(r.z) * z.z;
-      acc[1] += double(r.x) * r.x + double(r.y) * r.y + double(r.z) * r.z;
+      acc[0] += dot3w(r, z);
+      acc[1] += dot3w(r, r);
     }
     block_sum<2, kBlock>(acc);
     if (threadIdx.x == 0) {
@@ -340,6 +371,12 @@ __global__ void __launch_bounds__(kBlock) k_pcg_persistent(Bsr<R> A, PcgVecs<R> 
     if (*err != 0.0) scal[S_STATUS] = *err;
   }
 }
+
+}  // namespace skg
+
+#include "pcg_cluster.cuh"
+
+namespace skg {
 
 // ------------------------------------------------------ small kernels ----
 // u_tilde = 2 u_curr - u_prev (simkit/energies/kinetic.py:87-90), u = u_tilde
@@ -441,16 +478,70 @@ static int num_sms() {
 }
 
 constexpr int kG = 8;  // lanes per block row in the SpMV
+// systems up to this many block rows run PCG on one thread-block cluster
+constexpr int64_t kClusterAutoRows = 24576;
+
+template <typename R>
+static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, R* xout,
+                              double rtol, int max_iter, double* scal, cudaStream_t s) {
+  auto kern = k_pcg_cluster<R, kG>;
+  static thread_local bool configured = false;
+  if (!configured) {
+    SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
+    configured = true;
+  }
+  int csize = A.nbr >= 2048 ? kClusterMax : 8;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = kClusterSmemBudget;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  for (;;) {
+    attr[0].val.clusterDim.x = csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(csize, 1, 1);
+    int nclusters = 0;
+    cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg);
+    if (e == cudaSuccess && nclusters >= 1) break;
+    (void)cudaGetLastError();
+    if (csize <= 2) return fail(SKG_ERR_CUDA, "no thread-block cluster of the PCG kernel fits on this device");
+    csize /= 2;
+  }
+  if (cluster_vec_bytes(A.nbr, csize, (int)sizeof(R)) > kClusterSmemBudget)
+    return fail(SKG_ERR_CAPACITY, "system too large for one cluster");
+  Bsr<R> a2 = A;
+  int smem = kClusterSmemBudget;
+  SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, b, bsign, pinned, xout, rtol, max_iter, scal, smem));
+  return SKG_OK;
+}
+
+// largest system (block rows) the cluster PCG holds in shared memory
+template <typename R> static int64_t cluster_rows_limit() {
+  return (int64_t)kClusterMax * (kClusterSmemBudget / ((5 * 4 + 9) * (int64_t)sizeof(R)));
+}
 
 template <typename R>
 static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
                      cudaStream_t s, PcgResult* res) {
   const int rb = reduce_blocks(A.nbr);
-  k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal);
-  SKG_LAUNCHED();
-  res->launches = 1;
-  if (mode == 1) {
+  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : 1;
+  if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 1;
+  res->launches = 0;
+  if (mode != 2) {
+    k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal);
+    SKG_LAUNCHED();
+    res->launches = 1;
+  }
+  if (mode == 2) {
+    SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s));
+    res->launches += 1;
+  } else if (mode == 1) {
     int per_sm = 0;
     SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<R, kG>, kBlock, 0));
     int64_t want = (A.nbr * kG + kBlock - 1) / kBlock;
@@ -511,12 +602,12 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   const bool mixed = sizeof(R) == 4;
   const double inv_h2 = 1.0 / (prm->dt * prm->dt);
   R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
-  R* val = mixed ? (R*)w.val32 : (R*)w.val64;
+  R* rec = mixed ? (R*)w.rec32 : (R*)w.rec64;
   R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
   PcgVecs<R> pv;
   R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
   pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4];
-  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, val, jinv};
+  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
 
   PhaseTimer pt;
   pt.init(prm->profile != 0, s);
@@ -576,10 +667,32 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   double ecur[2];
   SKG_TRY(energy(nullptr, 0.0, ecur));
   const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  double res_prev = 1.0, eta_prev = 0.0;
   for (int it = 0; it < prm->max_newton && r0 > 0.0; ++it) {
     const double res = sqrt(gg) / r0;
     info->residual = res;
     if (res < prm->tol) break;
+    // PCG forcing term: fixed (pcg_rtol > 0) or Eisenstat-Walker choice 2
+    // (gamma 0.9, exponent 2, safeguarded) capped at |pcg_rtol|, never
+    // tighter than what brings the residual to a quarter of tol
+    double eta = prm->pcg_rtol;
+    if (prm->pcg_rtol < 0.0) {
+      const double eta_max = -prm->pcg_rtol;
+      if (it == 0) {
+        eta = eta_max;
+      } else {
+        const double q = res / res_prev;
+        eta = 0.9 * q * q;
+        const double safe = 0.9 * eta_prev * eta_prev;
+        if (safe > 0.1 && safe > eta) eta = safe;
+      }
+      const double reach = 0.25 * prm->tol / res;
+      if (eta < reach) eta = reach;
+      if (eta > eta_max) eta = eta_max;
+      if (eta < 1e-8) eta = 1e-8;
+    }
+    res_prev = res;
+    eta_prev = eta;
     // H(u) + M/h^2 with pinned rows/columns, block-Jacobi inverses
     pt.begin();
     if constexpr (sizeof(R) == 4) {
@@ -588,7 +701,8 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
       SKG_TRY(launch_tet_hessian<double>(make_tet_args64(m, st->u), 1, 1, (double*)hbuf, s));
     }
     info->t_hessian_ms += pt.end();
-    AsmArgs<R> aa = make_asm_args<R>(m, hbuf, val, jinv);
+    AsmArgs<R> aa = make_asm_args<R>(m, hbuf, nullptr, jinv);
+    aa.rec = rec;
     aa.mass = st->mass;
     aa.inv_h2 = inv_h2;
     aa.pinned = st->pinned;
@@ -599,7 +713,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     // dx = -H^-1 g
     PcgResult pr{};
     pt.begin();
-    SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, prm->pcg_rtol, prm->pcg_max_iter, prm->pcg_mode, w.partials,
+    SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, eta, prm->pcg_max_iter, prm->pcg_mode, w.partials,
                          w.counter, w.scal, s, &pr));
     info->t_pcg_ms += pt.end();
     info->launches += pr.launches;

@@ -62,10 +62,14 @@ class BESolver:
     rho : density; gravity : (3,) acceleration; pinned : vertex indices held at rest
     dt : time step; tol : relative residual stop; max_newton : Newton cap
     precision : 'mixed' (FP32 Hessian/SpMV, FP64 residual/dots/energy sums) or 'fp64'
+    pcg_rtol : PCG relative tolerance; a negative value selects Eisenstat-Walker
+        forcing capped at its magnitude
+    pcg_mode : 0 kernel per phase, 1 grid-persistent, 2 one thread-block
+        cluster, 3 choose by size (cluster up to 24,576 block rows)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
-                 tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=1e-4, pcg_max_iter=4000, pcg_mode=1,
+                 tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
