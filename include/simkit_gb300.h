@@ -171,11 +171,15 @@ typedef struct skg_be_params {
   double ls_alpha;          /* Armijo parameter, simkit default 0.01 */
   double ls_beta;           /* step factor, simkit default 0.5 */
   int32_t ls_max_iter;      /* simkit default 100 */
-  int32_t pcg_mode;         /* 0 = kernel per phase, 1 = persistent cooperative kernel */
+  int32_t pcg_mode;         /* 0 kernel per phase, 1 grid-persistent cooperative kernel,
+                               2 one thread-block cluster, 3 by size (2 up to 24,576 block
+                               rows, else 1), 4 grid-persistent Chronopoulos-Gear form */
   double ls_threshold;      /* Armijo slack, simkit default 1e-12; < 0 selects a slack
                                scaled to the FP32 rounding of the energy sum */
   int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */
-  int32_t reserved_;
+  int32_t pcg_variant;      /* grid-persistent PCG kernel variant 0-8 (lanes per row x rows in
+                               flight: 8x1, 16x1, 8x2, 16x2, 4x2, 4x4, 2x4, 8x4, 2x2), chosen
+                               by the autotuner */
 } skg_be_params;
 
 typedef struct skg_be_state {
@@ -185,6 +189,9 @@ typedef struct skg_be_state {
   const double* mass;       /* (n) lumped vertex mass */
   const double* f_ext;      /* (3n) external force */
   const uint8_t* pinned;    /* (3n) 1 = DOF held at its rest position */
+  const double* u_warm;     /* (3n) optional Newton initial guess (batched step): used per
+                               instance only if its residual is below the residual at
+                               x_tilde; the relative residual stays judged against x_tilde */
 } skg_be_state;
 
 typedef struct skg_step_info {
@@ -197,7 +204,7 @@ typedef struct skg_step_info {
   double min_alpha;         /* smallest accepted step */
   double energy;            /* final incremental potential relative to rest */
   int32_t launches;         /* kernels launched by the step */
-  int32_t reserved_;
+  int32_t warm_used;        /* batched step: 1 if the warm start was kept, 0 if it fell back */
   double t_hessian_ms;      /* per-phase device time, filled when params->profile */
   double t_assemble_ms;
   double t_pcg_ms;
@@ -211,6 +218,31 @@ int64_t skg_be_workspace_size(const skg_tet_mesh* mesh, int precision);
  * relative residual is below tol.  Host-synchronizes for its decisions. */
 int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state,
                 void* workspace, skg_step_info* info_h, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* batched backward Euler: many independent meshes in one solve            */
+/* ---------------------------------------------------------------------- */
+/* The instances are concatenated into one skg_tet_mesh (disjoint vertex and tet
+ * ranges, so its block pattern is block diagonal by instance).  Per instance,
+ * Newton, the forcing term, the Armijo search and the convergence test are
+ * those of skg_be_step; each instance's linear system is solved on a thread-block
+ * cluster taken from a queue ordered largest first.  No counterpart call exists
+ * in simkit (its user loops call backward_euler per mesh, backward_euler.py:27). */
+typedef struct skg_batch {
+  int32_t n_inst;
+  int32_t max_rows;          /* block rows of the largest instance */
+  const int32_t* inst_rows;  /* (n_inst+1) vertex (block-row) offsets */
+  const int32_t* inst_tets;  /* (n_inst+1) tet offsets */
+  const int32_t* vert_inst;  /* (n) instance of each vertex */
+  const int32_t* tet_inst;   /* (t) instance of each tet */
+  const int32_t* order;      /* (n_inst) instances by decreasing size */
+} skg_batch;
+
+int64_t skg_batch_workspace_size(const skg_tet_mesh* mesh, const skg_batch* batch, int precision);
+/* One backward-Euler step of every instance; infos_h[n_inst] per instance, total_h summed. */
+int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
+                        const skg_be_state* state, void* workspace, skg_step_info* infos_h, skg_step_info* total_h,
+                        void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* generic sparse solve: replaces spsolve in newton_solver (newton.py:52)   */
@@ -237,6 +269,47 @@ int64_t skg_pcg_noalloc_max_rows(void);
 int skg_pcg_bsr64_noalloc(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val,
                           const double* b, double* x, double rtol, int32_t max_iter, int32_t* iters_h,
                           void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* learned warm start: BF16 tensor-core MLP pieces (no simkit counterpart)  */
+/* ---------------------------------------------------------------------- */
+/* C[R x Nc] = A[R x L] B[Nc x L]^T on the 5th-generation tensor cores (tcgen05, TMEM
+ * accumulators, TMA-loaded 128-byte-swizzled tiles).  A, B BF16 (row pitches lda, ldb
+ * elements, 16-byte aligned), L a multiple of 64, Nc a multiple of 16 <= 256.
+ * epi 0: FP32 out_f32 (+bias), per split [splits][R][ld_out]; 1: z = acc + bias ->
+ * out_z (bf16), gelu(z) -> out_h (bf16); 2: bf16 out_h (+bias).  err: device int set
+ * to SKG_ERR_TIMEOUT if a bounded wait gave up. */
+int skg_mlp_gemm(const void* A, int64_t R, int64_t lda, const void* B, int Nc, int64_t ldb, int64_t L, int splits,
+                 int epi, const float* bias, float* out_f32, void* out_z, void* out_h, int Nstore, int ld_out,
+                 int* err, void* stream);
+/* dZ = dH * gelu'(Z) elementwise (BF16). */
+int skg_mlp_gelu_backward(const void* dH, const void* Z, int64_t n, void* dZ, void* stream);
+/* out = in^T for a rows x cols BF16 matrix. */
+int skg_mlp_transpose(const void* in, int rows, int cols, int ld_in, void* out, int ld_out, void* stream);
+/* out = sum over splits of part[s] (fixed order). */
+int skg_mlp_reduce_splits(const float* part, int splits, int64_t n, float* out, void* stream);
+/* db[c] = sum over rows of dZ[r][c] (fixed order). */
+int skg_mlp_colsum(const void* dZ, int rows, int cols, int ld, float* db, void* stream);
+/* mean squared error of y against t and its gradient dy (BF16); scratch: 2051 doubles. */
+int skg_mlp_mse(const float* y, int ld_y, const float* t, int rows, int cols, void* dy, int ld_dy, double* scratch,
+                double* loss_h, void* stream);
+/* one Adam step on FP32 weights; refreshes a BF16 copy and optionally its transpose. */
+int skg_mlp_adam(float* w, const float* grad, float* m1, float* m2, int rows, int cols, float lr, float b1, float b2,
+                 float eps, int step, void* w16, int ld16, void* wt16, int ldt, void* stream);
+
+/* MLP input rows [n][64] BF16 for one frame: per-vertex features (rest position,
+ * displacement, last-step velocity and Newton correction in units of 9.8 dt^2,
+ * gravity) and a 32-value per-instance mean-pooled context.  vf (n x 16 f32) and
+ * ctx (n_inst x 32 f32) are caller scratch; corr may be null. */
+int skg_warmstart_features(const double* X, const double* u, const double* u_prev, const double* corr,
+                           const double* f_ext, const double* mass, double dt, int64_t n, const int32_t* inst_rows,
+                           const int32_t* vert_inst, int n_inst, const float* inst_scalars, float* vf, float* ctx,
+                           void* out, void* stream);
+/* u_warm = u_tilde + 9.8 dt^2 * pred[:, 0:3] (pinned DOFs stay at u_tilde). */
+int skg_warmstart_apply(const double* u_tilde, const float* pred, int ld_pred, const uint8_t* pinned, double dt,
+                        int64_t n, double* u_warm, void* stream);
+/* training targets (u_next - u_tilde) / (9.8 dt^2), [n][3] FP32. */
+int skg_warmstart_targets(const double* u_next, const double* u_tilde, double dt, int64_t n, float* t, void* stream);
 
 #ifdef __cplusplus
 }

@@ -55,21 +55,27 @@ class BEParamsC(ctypes.Structure):
         ("dt", c_dbl), ("tol", c_dbl), ("max_newton", c_i32), ("precision", c_i32), ("pcg_rtol", c_dbl),
         ("pcg_max_iter", c_i32), ("do_line_search", c_i32), ("ls_alpha", c_dbl), ("ls_beta", c_dbl),
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
-        ("reserved_", c_i32),
+        ("pcg_variant", c_i32),
     ]
 
 
 class BEStateC(ctypes.Structure):
-    _fields_ = [("u", c_vp), ("u_curr", c_vp), ("u_prev", c_vp), ("mass", c_vp), ("f_ext", c_vp), ("pinned", c_vp)]
+    _fields_ = [("u", c_vp), ("u_curr", c_vp), ("u_prev", c_vp), ("mass", c_vp), ("f_ext", c_vp), ("pinned", c_vp),
+                ("u_warm", c_vp)]
 
 
 class StepInfoC(ctypes.Structure):
     _fields_ = [
         ("newton_iters", c_i32), ("pcg_iters", c_i32), ("ls_trials", c_i32), ("status", c_i32),
         ("residual0", c_dbl), ("residual", c_dbl), ("min_alpha", c_dbl), ("energy", c_dbl),
-        ("launches", c_i32), ("reserved_", c_i32), ("t_hessian_ms", c_dbl), ("t_assemble_ms", c_dbl),
+        ("launches", c_i32), ("warm_used", c_i32), ("t_hessian_ms", c_dbl), ("t_assemble_ms", c_dbl),
         ("t_pcg_ms", c_dbl), ("t_gradient_ms", c_dbl), ("t_energy_ms", c_dbl),
     ]
+
+
+class BatchC(ctypes.Structure):
+    _fields_ = [("n_inst", c_i32), ("max_rows", c_i32), ("inst_rows", c_vp), ("inst_tets", c_vp),
+                ("vert_inst", c_vp), ("tet_inst", c_vp), ("order", c_vp)]
 
 
 P = ctypes.POINTER
@@ -90,8 +96,24 @@ _SIGNATURES = {
     "skg_snh_hessian_x": (c_i32, [P(TetMeshC), c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "skg_be_workspace_size": (c_i64, [P(TetMeshC), c_i32]),
     "skg_be_step": (c_i32, [P(TetMeshC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC), c_vp]),
+    "skg_batch_workspace_size": (c_i64, [P(TetMeshC), P(BatchC), c_i32]),
+    "skg_be_step_batched": (c_i32, [P(TetMeshC), P(BatchC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC),
+                                    P(StepInfoC), c_vp]),
     "skg_pcg_workspace_size": (c_i64, [c_i64]),
     "skg_pcg_bsr64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp, c_vp]),
+    "skg_mlp_gemm": (c_i32, [c_vp, c_i64, c_i64, c_vp, c_i32, c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,
+                             c_i32, c_i32, c_vp, c_vp]),
+    "skg_mlp_gelu_backward": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "skg_mlp_transpose": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_vp, c_i32, c_vp]),
+    "skg_mlp_reduce_splits": (c_i32, [c_vp, c_i32, c_i64, c_vp, c_vp]),
+    "skg_mlp_colsum": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_vp, c_vp]),
+    "skg_mlp_mse": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_i32, c_vp, c_i32, c_vp, P(c_dbl), c_vp]),
+    "skg_mlp_adam": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp]),
+    "skg_warmstart_features": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp, c_i32, c_vp,
+                                       c_vp, c_vp, c_vp, c_vp]),
+    "skg_warmstart_apply": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_dbl, c_i64, c_vp, c_vp]),
+    "skg_warmstart_targets": (c_i32, [c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp]),
     "skg_pcg_noalloc_max_rows": (c_i64, []),
     "skg_pcg_bsr64_noalloc": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp]),
 }

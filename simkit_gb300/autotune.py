@@ -1,0 +1,82 @@
+"""Autotuner for the grid-persistent PCG kernel.
+
+The PCG kernel comes in variants that trade lanes per block row (G) against
+block rows in flight per lane group (U): (8,1), (16,1), (8,2), (16,2),
+(4,2), (4,4), (2,4), (8,4), (2,2).  Which one keeps the most loads in flight without idling lanes
+depends on the row lengths of the mesh and on the device, so the variant is
+picked by timing: each candidate runs one backward-Euler step from the same
+saved state with per-phase CUDA-event timing, and the variant with the
+lowest time per PCG iteration wins.  Results are cached in a JSON file keyed
+by device, system size and precision (``$SIMKIT_GB300_CACHE`` or
+``~/.cache/simkit_gb300/autotune.json``).
+"""
+
+from __future__ import annotations
+
+import json
+import os
+
+import torch
+
+VARIANTS = {0: (8, 1), 1: (16, 1), 2: (8, 2), 3: (16, 2), 4: (4, 2), 5: (4, 4), 6: (2, 4), 7: (8, 4), 8: (2, 2)}
+CLUSTER_ROWS = 24576  # systems up to this size use the one-cluster PCG (no variants)
+
+
+def _cache_path():
+    base = os.environ.get("SIMKIT_GB300_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "simkit_gb300"))
+    return os.path.join(base, "autotune.json")
+
+
+def _load():
+    try:
+        with open(_cache_path()) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _store(table):
+    path = _cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(table, f, indent=1, sort_keys=True)
+    except OSError:
+        pass
+
+
+def _key(solver):
+    bucket = 1 << max(0, int(solver.mesh.n - 1).bit_length())
+    return f"{torch.cuda.get_device_name()}|rows<={bucket}|prec={solver.precision}"
+
+
+def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
+    """Pick the fastest PCG kernel variant for ``solver``; returns (variant, timings_us)."""
+    if solver.params.pcg_mode not in (1, 3) or (solver.params.pcg_mode == 3 and solver.mesh.n <= CLUSTER_ROWS):
+        return solver.params.pcg_variant, {}
+    key = _key(solver)
+    table = _load() if use_cache else {}
+    if key in table:
+        solver.params.pcg_variant = int(table[key]["variant"])
+        return solver.params.pcg_variant, table[key]["us_per_iter"]
+    uc, up = solver.u_curr.clone(), solver.u_prev.clone()
+    steps = solver.steps
+    old_profile = solver.params.profile
+    timings = {}
+    for v in variants:
+        solver.u_curr.copy_(uc)
+        solver.u_prev.copy_(up)
+        solver.params.pcg_variant = v
+        solver.params.profile = 1
+        info = solver.step()
+        timings[v] = 1e3 * info.t_pcg_ms / max(info.pcg_iters, 1)
+    solver.u_curr.copy_(uc)
+    solver.u_prev.copy_(up)
+    solver.steps = steps
+    solver.params.profile = old_profile
+    best = min(timings, key=timings.get)
+    solver.params.pcg_variant = best
+    if use_cache:
+        table[key] = {"variant": best, "us_per_iter": {str(k): v for k, v in timings.items()}}
+        _store(table)
+    return best, timings

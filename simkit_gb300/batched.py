@@ -1,0 +1,124 @@
+"""Batched backward Euler: many independent meshes stepped together on one GPU.
+
+simkit steps one mesh per ``backward_euler`` call
+(``simkit/integrators/backward_euler.py:27-91``).  ``BatchedBESolver`` takes a
+list of meshes of uneven sizes, concatenates them into one device mesh with
+disjoint vertex and tet ranges, and advances all of them by one
+backward-Euler step per call through ``skg_be_step_batched``: the element,
+assembly and gradient kernels run once over the concatenation, and every
+instance gets its own Newton iteration, forcing term, Armijo search and
+convergence test, with its linear system solved on a thread-block cluster
+taken from a largest-first queue.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import BatchC, BEParamsC, BEStateC, StepInfoC, check
+from .mesh import TetMesh, _stream_ptr
+from .solver import PRECISIONS, StepInfo, lumped_mass
+
+
+class BatchedBESolver:
+    """Backward-Euler stepper for a batch of independent tet meshes.
+
+    ``specs`` is a list of objects with ``X, T, mu, lam, rho, gravity,
+    pinned`` (e.g. ``simkit_gb300.beams.BeamSpec``); each keeps its own
+    material, gravity direction and pins.
+    """
+
+    def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
+                 pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda"):
+        _lib.load()
+        self.n_inst = len(specs)
+        if self.n_inst == 0:
+            raise ValueError("empty batch")
+        Xs, Ts, mus, lams, masses, fexts, pins = [], [], [], [], [], [], []
+        rows, tets = [0], [0]
+        for sp in specs:
+            X = np.asarray(sp.X, dtype=np.float64).reshape(-1, 3)
+            T = np.asarray(sp.T).reshape(-1, 4)
+            Xs.append(X)
+            Ts.append(T + rows[-1])
+            mus.append(np.asarray(sp.mu, dtype=np.float64).reshape(-1))
+            lams.append(np.asarray(sp.lam, dtype=np.float64).reshape(-1))
+            m = lumped_mass(X, T, sp.rho)
+            masses.append(m)
+            fexts.append((m[:, None] * np.asarray(sp.gravity, dtype=np.float64)[None, :]).reshape(-1))
+            p = np.zeros(3 * X.shape[0], np.uint8)
+            pv = np.asarray(sp.pinned, dtype=np.int64).ravel()
+            p[(3 * pv[:, None] + np.arange(3)[None, :]).ravel()] = 1
+            pins.append(p)
+            rows.append(rows[-1] + X.shape[0])
+            tets.append(tets[-1] + T.shape[0])
+        self.inst_rows_host = np.array(rows, np.int32)
+        self.inst_tets_host = np.array(tets, np.int32)
+        self.mesh = TetMesh(np.concatenate(Xs), np.concatenate(Ts), np.concatenate(mus), np.concatenate(lams),
+                            device=device)
+        m = self.mesh
+        dev = m.device
+        sizes = np.diff(self.inst_rows_host)
+        up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        self.inst_rows = up(self.inst_rows_host)
+        self.inst_tets = up(self.inst_tets_host)
+        self.vert_inst = up(np.repeat(np.arange(self.n_inst, dtype=np.int32), sizes))
+        self.tet_inst = up(np.repeat(np.arange(self.n_inst, dtype=np.int32), np.diff(self.inst_tets_host)))
+        self.order = up(np.argsort(-sizes, kind="stable").astype(np.int32))
+        self.batch = BatchC(n_inst=self.n_inst, max_rows=int(sizes.max()), inst_rows=self.inst_rows.data_ptr(),
+                            inst_tets=self.inst_tets.data_ptr(), vert_inst=self.vert_inst.data_ptr(),
+                            tet_inst=self.tet_inst.data_ptr(), order=self.order.data_ptr())
+        self.precision = PRECISIONS[precision]
+        self.mass = up(np.concatenate(masses))
+        self.f_ext = up(np.concatenate(fexts))
+        self.pinned = up(np.concatenate(pins))
+        self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
+        self.u_curr = torch.zeros_like(self.u_prev)
+        self.u_next = torch.zeros_like(self.u_prev)
+        nbytes = _lib.load().skg_batch_workspace_size(ctypes.byref(m.c), ctypes.byref(self.batch), self.precision)
+        if nbytes < 0:
+            raise ValueError(_lib.last_error())
+        self.workspace = torch.zeros(int(nbytes), dtype=torch.uint8, device=dev)
+        self.params = BEParamsC(
+            dt=dt, tol=tol, max_newton=max_newton, precision=self.precision, pcg_rtol=pcg_rtol,
+            pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
+            ls_max_iter=100, pcg_mode=2,
+            ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
+            profile=int(profile))
+        self._infos = (StepInfoC * self.n_inst)()
+        self.steps = 0
+
+    @property
+    def n_tets(self):
+        return self.mesh.t
+
+    @property
+    def n_verts(self):
+        return self.mesh.n
+
+    def step(self, stream=None):
+        """Advance every instance one step; returns (per-instance StepInfo list, total StepInfo)."""
+        st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
+                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr())
+        total = StepInfoC()
+        check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
+                                              ctypes.byref(self.params), ctypes.byref(st),
+                                              ctypes.c_void_p(self.workspace.data_ptr()), self._infos,
+                                              ctypes.byref(total), _stream_ptr(stream)))
+        self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+        self.steps += 1
+        conv = lambda c: StepInfo(c.newton_iters, c.pcg_iters, c.ls_trials, c.status, c.residual0, c.residual,
+                                  c.min_alpha, c.energy, c.launches, c.t_hessian_ms, c.t_assemble_ms, c.t_pcg_ms,
+                                  c.t_gradient_ms, c.t_energy_ms)
+        return [conv(c) for c in self._infos], conv(total)
+
+    def displacement(self, inst=None) -> np.ndarray:
+        u = self.u_curr.cpu().numpy()
+        if inst is None:
+            return u.copy()
+        r0, r1 = self.inst_rows_host[inst], self.inst_rows_host[inst + 1]
+        return u[3 * r0:3 * r1].copy()

@@ -55,6 +55,7 @@ template <typename R>
 __global__ void __launch_bounds__(128) k_tet_hessian(TetArgs<R> a, int disp, int project, R* __restrict__ hbuf) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= a.t) return;
+  if (a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]) return;
   const int4 v = __ldg(a.tets + e);
   R du[9], D[9], G[9], gN[12], out[kTetHessVals];
   if constexpr (sizeof(R) == 8) {
@@ -94,6 +95,7 @@ __global__ void k_assemble(AsmArgs<R> a) {
   const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= a.nb) return;
   const int v = __ldg(a.bsr_row + s);
+  if (a.inst_active && !a.inst_active[__ldg(a.vert_inst + v)]) return;
   const int w = __ldg(a.bsr_col + s);
   const int rp = __ldg(a.rowptr + v);
   const int K = __ldg(a.rowptr + v + 1) - rp;
@@ -227,6 +229,54 @@ __global__ void __launch_bounds__(kBlock) k_vertex_gradient(GradArgs a) {
 // plus its magnitude sum |terms| (the FP32 noise scale of the value).
 // Mode DIRECT instead sums vol_e psi(F_e) from absolute positions in FP64
 // (simkit's stable_neo_hookean_energy_x, snh.py:449-474).
+// vol * (psi - psi(I)) of tet e at u + step dx (DIRECT: vol * psi from absolute positions)
+template <typename R, bool DIRECT>
+__device__ __forceinline__ double tet_energy_term(const EnergyArgs<R>& a, int64_t e, R step) {
+  const int4 v = __ldg(a.tet.tets + e);
+  R du[9], D[9], G[9];
+  if constexpr (sizeof(R) == 8) {
+    tet_du(a.tet.u, v, du);
+  } else {
+    tet_du(a.tet.uh, a.tet.ul, v, du);
+  }
+  if (a.dx && step != R(0)) {
+    const Vec3<R> d0 = ld3(a.dx, v.x);
+    const int vv[3] = {v.y, v.z, v.w};
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const Vec3<R> db = ld3(a.dx, vv[b]);
+      du[3 * b + 0] += step * (db.x - d0.x);
+      du[3 * b + 1] += step * (db.y - d0.y);
+      du[3 * b + 2] += step * (db.z - d0.z);
+    }
+  }
+  load_dinv(a.tet.dinv, a.tet.t, e, D);
+  disp_grad(du, D, G);
+  const R vol = __ldg(a.tet.vol + e), mu = __ldg(a.tet.mu + e), lam = __ldg(a.tet.lam + e);
+  if (DIRECT) return double(vol) * double(snh_psi<R>(G, mu, lam));
+  return double(vol * snh_dpsi<R>(G, mu, lam));
+}
+
+// kinetic + gravity terms of vertex v's free DOFs at u + step dx; acc[1] gets magnitudes
+template <typename R>
+__device__ __forceinline__ void vertex_energy_terms(const EnergyArgs<R>& a, int64_t v, double step, double (&acc)[2]) {
+  Vec3<R> d = {R(0), R(0), R(0)};
+  if (a.dx && step != 0.0) d = ld3(a.dx, v);
+  const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+  const double mh = a.mass[v] * a.inv_h2;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int64_t k = 3 * v + c;
+    if (a.pinned && a.pinned[k]) continue;
+    const double x = a.tet.u[k] + step * dd[c];
+    const double r = x - a.ut[k];
+    const double kin = 0.5 * mh * r * r;
+    const double pot = a.f_ext ? -a.f_ext[k] * x : 0.0;
+    acc[0] += kin + pot;
+    acc[1] += kin + fabs(pot);
+  }
+}
+
 template <typename R, bool DIRECT>
 __global__ void __launch_bounds__(kBlock) k_energy(EnergyArgs<R> a) {
   double acc[2] = {0.0, 0.0};
@@ -235,55 +285,41 @@ __global__ void __launch_bounds__(kBlock) k_energy(EnergyArgs<R> a) {
   const R step = R(a.step);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
     if (i < a.tet.t) {
-      const int64_t e = i;
-      const int4 v = __ldg(a.tet.tets + e);
-      R du[9], D[9], G[9];
-      if constexpr (sizeof(R) == 8) {
-        tet_du(a.tet.u, v, du);
-      } else {
-        tet_du(a.tet.uh, a.tet.ul, v, du);
-      }
-      if (a.dx && step != R(0)) {
-        const Vec3<R> d0 = ld3(a.dx, v.x);
-        const int vv[3] = {v.y, v.z, v.w};
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          const Vec3<R> db = ld3(a.dx, vv[b]);
-          du[3 * b + 0] += step * (db.x - d0.x);
-          du[3 * b + 1] += step * (db.y - d0.y);
-          du[3 * b + 2] += step * (db.z - d0.z);
-        }
-      }
-      load_dinv(a.tet.dinv, a.tet.t, e, D);
-      disp_grad(du, D, G);
-      const R vol = __ldg(a.tet.vol + e), mu = __ldg(a.tet.mu + e), lam = __ldg(a.tet.lam + e);
-      double val;
-      if (DIRECT)
-        val = double(vol) * double(snh_psi<R>(G, mu, lam));
-      else
-        val = double(vol * snh_dpsi<R>(G, mu, lam));
+      const double val = tet_energy_term<R, DIRECT>(a, i, step);
       acc[0] += val;
       acc[1] += fabs(val);
     } else {
-      const int64_t v = i - a.tet.t;
-      Vec3<R> d = {R(0), R(0), R(0)};
-      if (a.dx && step != R(0)) d = ld3(a.dx, v);
-      const double dd[3] = {double(d.x), double(d.y), double(d.z)};
-      const double mh = a.mass[v] * a.inv_h2;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int64_t k = 3 * v + c;
-        if (a.pinned && a.pinned[k]) continue;
-        const double x = a.tet.u[k] + a.step * dd[c];
-        const double r = x - a.ut[k];
-        const double kin = 0.5 * mh * r * r;
-        const double pot = a.f_ext ? -a.f_ext[k] * x : 0.0;
-        acc[0] += kin + pot;
-        acc[1] += kin + fabs(pot);
-      }
+      vertex_energy_terms<R>(a, i - a.tet.t, a.step, acc);
     }
   }
   grid_sum<2, kBlock>(acc, a.partials, a.counter, a.out);
+}
+
+// Per-instance energy of a batch: one CTA per instance sums its tets and
+// vertices in a fixed order (deterministic); instances with mask 0 skip.
+// steps[inst] is the trial step of that instance's line search.
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_inst_energy(EnergyArgs<R> a, const int32_t* __restrict__ inst_rows,
+                                                        const int32_t* __restrict__ inst_tets,
+                                                        const uint8_t* __restrict__ mask,
+                                                        const double* __restrict__ steps, double* __restrict__ out2) {
+  const int inst = blockIdx.x;
+  if (mask && !mask[inst]) return;
+  const double stepd = steps ? steps[inst] : 0.0;
+  const R step = R(stepd);
+  double acc[2] = {0.0, 0.0};
+  for (int64_t e = inst_tets[inst] + threadIdx.x; e < inst_tets[inst + 1]; e += blockDim.x) {
+    const double val = tet_energy_term<R, false>(a, e, step);
+    acc[0] += val;
+    acc[1] += fabs(val);
+  }
+  for (int64_t v = inst_rows[inst] + threadIdx.x; v < inst_rows[inst + 1]; v += blockDim.x)
+    vertex_energy_terms<R>(a, v, stepd, acc);
+  block_sum<2, kBlock>(acc);
+  if (threadIdx.x == 0) {
+    out2[2 * inst] = acc[0];
+    out2[2 * inst + 1] = acc[1];
+  }
 }
 
 // hi/lo split of FP64 positions for the FP32 kernels, padded to 4
@@ -342,6 +378,19 @@ int launch_energy(const EnergyArgs<R>& a, bool direct, cudaStream_t s) {
   return SKG_OK;
 }
 
+template <typename R>
+int launch_inst_energy(const EnergyArgs<R>& a, int n_inst, const int32_t* inst_rows, const int32_t* inst_tets,
+                       const uint8_t* mask, const double* steps, double* out2, cudaStream_t s) {
+  if (n_inst <= 0) return SKG_OK;
+  k_inst_energy<R><<<n_inst, kBlock, 0, s>>>(a, inst_rows, inst_tets, mask, steps, out2);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+template int launch_inst_energy<float>(const EnergyArgs<float>&, int, const int32_t*, const int32_t*,
+                                       const uint8_t*, const double*, double*, cudaStream_t);
+template int launch_inst_energy<double>(const EnergyArgs<double>&, int, const int32_t*, const int32_t*,
+                                        const uint8_t*, const double*, double*, cudaStream_t);
+
 int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t s) {
   k_split<<<blocks_for(n), kBlock, 0, s>>>(u, n, uh, ul);
   SKG_LAUNCHED();
@@ -374,7 +423,7 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   w.ut = c.take<double>(3 * n);
   w.uh = c.take<float>(4 * n);
   w.ul = c.take<float>(4 * n);
-  for (int k = 0; k < 5; ++k) {
+  for (int k = 0; k < 6; ++k) {
     w.vec32[k] = mixed ? c.take<float>(4 * n) : nullptr;
     w.vec64[k] = mixed ? nullptr : c.take<double>(4 * n);
   }

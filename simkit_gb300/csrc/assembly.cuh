@@ -25,6 +25,8 @@ template <typename R> struct TetArgs {
   const double* u;   // FP64 displacement (or positions), 3n
   const float* uh;   // FP32 hi/lo split (FP32 kernels only)
   const float* ul;
+  const int32_t* tet_inst;     // optional: instance of each tet (batched solves)
+  const uint8_t* inst_active;  // optional: skip tets of inactive instances
 };
 
 template <typename R> struct AsmArgs {
@@ -41,6 +43,8 @@ template <typename R> struct AsmArgs {
   R* val;                // entry-major block values (9 nb), or null
   R* rec;                // 12-wide block records (9 values, column bits, 2 pad), or null
   R* jinv;               // optional: block-Jacobi inverses (9n)
+  const int32_t* vert_inst;    // optional: instance of each block row (batched solves)
+  const uint8_t* inst_active;  // optional: skip rows of inactive instances
 };
 
 // Block record of the solver's SpMV: the 9 row-major entries of a 3x3 block,
@@ -98,8 +102,8 @@ struct Workspace {
   double* ut;
   float* uh;
   float* ul;
-  float* vec32[5];   // PCG x, r, z, p, q (padded)
-  double* vec64[5];
+  float* vec32[6];   // PCG x, r, z, p, q, s (padded)
+  double* vec64[6];
   double* partials;
   unsigned* counter;
   double* scal;
@@ -132,5 +136,8 @@ int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t
 int launch_vertex_gradient(const GradArgs& a, cudaStream_t s);
 template <typename R> int launch_energy(const EnergyArgs<R>& a, bool direct, cudaStream_t s);
 int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t s);
+template <typename R>
+int launch_inst_energy(const EnergyArgs<R>& a, int n_inst, const int32_t* inst_rows, const int32_t* inst_tets,
+                       const uint8_t* mask, const double* steps, double* out2, cudaStream_t s);
 
 }  // namespace skg

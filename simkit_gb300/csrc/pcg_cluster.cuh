@@ -98,25 +98,28 @@ inline int64_t cluster_vec_bytes(int64_t nbr, int csize, int rsize) {
   return rows_cap * (5 * 4 + 9) * rsize + 16;
 }
 
-// b: right-hand side (3n, simkit layout, FP64) scaled by bsign; pinned DOFs
-// forced to zero.  On return: x (padded, global) and scal[] as the other modes.
+struct ClusterPcgOut {
+  int iters;
+  int status;
+  double rr, rz, bb;
+};
+
+// Solve the system of block rows [gbase, gbase + nbr) (its columns lie in the
+// same range) on the calling cluster.  b: right-hand side (3n, simkit layout,
+// FP64) scaled by bsign, pinned DOFs forced to zero; x written to xout
+// (padded, global rows).  Every thread of every CTA of the cluster must call
+// it; it ends with a cluster barrier, so shared memory may be reused after.
 template <typename R, int G>
-__global__ void __launch_bounds__(kClusterThreads, 1)
-    k_pcg_cluster(Bsr<R> A, const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
-                  R* __restrict__ xout, double rtol, int max_iter, double* scal, int smem_bytes) {
-  cgx::cluster_group cl = cgx::this_cluster();
+__device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
+    cgx::cluster_group& cl, const Bsr<R>& A, int64_t gbase, int64_t nbr, const double* __restrict__ b, double bsign,
+    const uint8_t* __restrict__ pinned, R* __restrict__ xout, double rtol, int max_iter, int smem_bytes,
+    unsigned char* smem_raw, double* pub, double* bcast, uint32_t* pbase) {
   const int crank = (int)cl.block_rank();
   const int csize = (int)cl.num_blocks();
-  const int64_t nbr = A.nbr;
-  const int64_t r0 = cl_row0(nbr, crank, csize);
-  const int64_t r1 = cl_row0(nbr, crank + 1, csize);
+  const int64_t r0 = gbase + cl_row0(nbr, crank, csize);
+  const int64_t r1 = gbase + cl_row0(nbr, crank + 1, csize);
   const int64_t rows_cap = (nbr + csize - 1) / csize;
   const int nr = (int)(r1 - r0);
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double pub[4];
-  __shared__ double bcast[4];
-  __shared__ uint32_t pbase[kClusterMax];
   // vectors of own rows, stride 4 per row; Jacobi inverses 9 per row
   R* sp = reinterpret_cast<R*>(smem_raw);
   R* sx = sp + 4 * rows_cap;
@@ -140,8 +143,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       R* d = srec + kRec * i;
 #pragma unroll
       for (int m = 0; m < 9; ++m) d[m] = bk.m[m];
-      const int o = cl_owner(bk.col, nbr, csize);
-      d[9] = col_bits((int)(pbase[o] + (uint32_t)((bk.col - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R))), R(0));
+      const int64_t lc = bk.col - gbase;
+      const int o = cl_owner(lc, nbr, csize);
+      d[9] = col_bits((int)(pbase[o] + (uint32_t)((lc - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R))), R(0));
       d[10] = R(0);
       d[11] = R(0);
     }
@@ -218,8 +222,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       } else {
         for (int k = lane; k < K; k += G) {
           const Blk<R> bk = ld_rec(A.rec, rp + k);
-          const int o = cl_owner(bk.col, nbr, csize);
-          const uint32_t ad = pbase[o] + (uint32_t)((bk.col - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R));
+          const int64_t lc = bk.col - gbase;
+          const int o = cl_owner(lc, nbr, csize);
+          const uint32_t ad = pbase[o] + (uint32_t)((lc - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R));
           const Vec3<R> xv = ld_cluster3(ad, R(0));
           a0 += bk.m[0] * xv.x + bk.m[1] * xv.y + bk.m[2] * xv.z;
           a1 += bk.m[3] * xv.x + bk.m[4] * xv.y + bk.m[5] * xv.z;
@@ -302,15 +307,80 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     const R* x = sx + 4 * i;
     st3(xout, r0 + i, Vec3<R>{x[0], x[1], x[2]});
   }
-  // no CTA may leave while another still reads its shared memory
+  // no CTA may leave (or reuse its shared memory) while another still reads it
   cl.sync();
-  if (crank == 0 && threadIdx.x == 0) {
-    scal[S_ITERS] = it;
-    scal[S_RR] = rr;
-    scal[S_RZ] = rz;
-    scal[S_BB] = bb;
+  return ClusterPcgOut{it, status, rr, rz, bb};
+}
+
+// one system on one cluster (pcg_mode 2)
+template <typename R, int G>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    k_pcg_cluster(Bsr<R> A, const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
+                  R* __restrict__ xout, double rtol, int max_iter, double* scal, int smem_bytes) {
+  cgx::cluster_group cl = cgx::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double pub[4];
+  __shared__ double bcast[4];
+  __shared__ uint32_t pbase[kClusterMax];
+  const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, 0, A.nbr, b, bsign, pinned, xout, rtol, max_iter,
+                                                  smem_bytes, smem_raw, pub, bcast, pbase);
+  if (cl.block_rank() == 0 && threadIdx.x == 0) {
+    scal[S_ITERS] = o.iters;
+    scal[S_RR] = o.rr;
+    scal[S_RZ] = o.rz;
+    scal[S_BB] = o.bb;
     scal[S_DONE] = 1.0;
-    scal[S_STATUS] = status;
+    scal[S_STATUS] = o.status;
+  }
+}
+
+// Many independent systems (instances), one per cluster at a time: each
+// cluster takes the next instance from a queue ordered largest first and
+// solves it to that instance's tolerance.  inst_rows (n_inst + 1) are the
+// instances' block-row offsets; inactive instances are skipped.
+template <typename R, int G>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    k_pcg_cluster_queue(Bsr<R> A, const int32_t* __restrict__ inst_rows, const int32_t* __restrict__ order,
+                        int n_inst, const uint8_t* __restrict__ active, const double* __restrict__ eta,
+                        const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
+                        R* __restrict__ xout, int max_iter, int32_t* iters_out, int32_t* status_out,
+                        unsigned* queue, int smem_bytes) {
+  cgx::cluster_group cl = cgx::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double pub[4];
+  __shared__ double bcast[4];
+  __shared__ uint32_t pbase[kClusterMax];
+  __shared__ int next_inst;
+  const int csize = (int)cl.num_blocks();
+  for (;;) {
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+      const unsigned idx = atomicAdd(queue, 1u);
+      next_inst = idx < (unsigned)n_inst ? order[idx] : -1;
+    }
+    cl.sync();
+    __shared__ int inst_sh;
+    if (threadIdx.x == 0) inst_sh = *cl.map_shared_rank(&next_inst, 0);
+    __syncthreads();
+    const int inst = inst_sh;
+    cl.sync();  // rank 0 may overwrite next_inst only after every CTA has read it
+    if (inst < 0) break;
+    if (!active[inst]) continue;
+    const int64_t gbase = inst_rows[inst];
+    const int64_t nbr = inst_rows[inst + 1] - gbase;
+    const int64_t rows_cap = (nbr + csize - 1) / csize;
+    if (rows_cap * (5 * 4 + 9) * (int64_t)sizeof(R) + 16 > smem_bytes) {
+      if (cl.block_rank() == 0 && threadIdx.x == 0) {
+        iters_out[inst] = 0;
+        status_out[inst] = SKG_ERR_CAPACITY;
+      }
+      continue;
+    }
+    const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, gbase, nbr, b, bsign, pinned, xout, eta[inst], max_iter,
+                                                    smem_bytes, smem_raw, pub, bcast, pbase);
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+      iters_out[inst] = o.iters;
+      status_out[inst] = o.status;
+    }
   }
 }
 

@@ -60,9 +60,10 @@ template <> __device__ __forceinline__ double dot3w<double>(Vec3<double> a, Vec3
 template <typename R> struct PcgVecs {
   R* x;
   R* r;
-  R* z;
+  R* z;   // preconditioned residual (u in the Chronopoulos-Gear form)
   R* p;
-  R* q;
+  R* q;   // A p (w = A u in the Chronopoulos-Gear form)
+  R* s;   // A p recurrence of the Chronopoulos-Gear form
 };
 
 template <typename R>
@@ -110,6 +111,53 @@ __device__ __forceinline__ Vec3<R> spmv_row(const Bsr<R>& A, const R* __restrict
     a2 += __shfl_xor_sync(0xffffffffu, a2, o, G);
   }
   return {a0, a1, a2};
+}
+
+// U block rows per lane group at once (records only): all U rows' record
+// loads are issued before any row's gathers, so each lane keeps U independent
+// load chains in flight.
+template <typename R, int G, int U>
+__device__ __forceinline__ void spmv_rowsU(const Bsr<R>& A, const R* __restrict__ xin, const int64_t (&row)[U],
+                                           const bool (&valid)[U], int lane, Vec3<R> (&y)[U]) {
+  int p[U], K[U];
+  int kmax = 0;
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    p[u] = valid[u] ? __ldg(A.rowptr + row[u]) : 0;
+    K[u] = valid[u] ? __ldg(A.rowptr + row[u] + 1) - p[u] : 0;
+    kmax = K[u] > kmax ? K[u] : kmax;
+  }
+  R acc[U][3];
+#pragma unroll
+  for (int u = 0; u < U; ++u) acc[u][0] = acc[u][1] = acc[u][2] = R(0);
+  for (int k = lane; k < kmax; k += G) {
+    Blk<R> bk[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      bk[u] = Blk<R>{};
+      if (k < K[u]) bk[u] = ld_rec(A.rec, p[u] + k);
+    }
+    Vec3<R> xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      xv[u] = Vec3<R>{R(0), R(0), R(0)};
+      if (k < K[u]) xv[u] = ld3c(xin, bk[u].col);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      acc[u][0] += bk[u].m[0] * xv[u].x + bk[u].m[1] * xv[u].y + bk[u].m[2] * xv[u].z;
+      acc[u][1] += bk[u].m[3] * xv[u].x + bk[u].m[4] * xv[u].y + bk[u].m[5] * xv[u].z;
+      acc[u][2] += bk[u].m[6] * xv[u].x + bk[u].m[7] * xv[u].y + bk[u].m[8] * xv[u].z;
+    }
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[u][c] += __shfl_xor_sync(0xffffffffu, acc[u][c], o, G);
+#pragma unroll
+  for (int u = 0; u < U; ++u) y[u] = Vec3<R>{acc[u][0], acc[u][1], acc[u][2]};
 }
 
 // ------------------------------------------------------ mode 0 kernels ---
@@ -284,7 +332,7 @@ __device__ __forceinline__ void all_sum(const double* partials, double (&out)[NV
   __syncthreads();
 }
 
-template <typename R, int G>
+template <typename R, int G, int U>
 __global__ void __launch_bounds__(kBlock, 3) k_pcg_persistent(Bsr<R> A, PcgVecs<R> v, double* partials,
                                                            unsigned* bar, double* scal) {
   // partials: 3 buffers of 2*gridDim doubles (pq | rz, rr | spare)
@@ -307,13 +355,33 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_persistent(Bsr<R> A, PcgVecs<
   while (!done) {
     // q = A p, pq
     double acc[2] = {0.0, 0.0};
-    for (int64_t base = row0; base < A.nbr; base += groups) {
-      const int64_t row = base + ((threadIdx.x & 31) / G);
-      const bool valid = row < A.nbr;
-      const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
-      if (lane == 0 && valid) {
-        st3(v.q, row, y);
-        acc[0] += dot3w(ld3c(v.p, row), y);
+    if (U > 1 && A.rec) {
+      for (int64_t base = row0; base < A.nbr; base += U * groups) {
+        int64_t rows[U];
+        bool val[U];
+        Vec3<R> ys[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          rows[u] = base + u * groups + ((threadIdx.x & 31) / G);
+          val[u] = rows[u] < A.nbr;
+        }
+        spmv_rowsU<R, G, U>(A, v.p, rows, val, lane, ys);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (lane == 0 && val[u]) {
+            st3(v.q, rows[u], ys[u]);
+            acc[0] += dot3w(ld3c(v.p, rows[u]), ys[u]);
+          }
+      }
+    } else {
+      for (int64_t base = row0; base < A.nbr; base += groups) {
+        const int64_t row = base + ((threadIdx.x & 31) / G);
+        const bool valid = row < A.nbr;
+        const Vec3<R> y = spmv_row<R, G>(A, v.p, row, lane, valid);
+        if (lane == 0 && valid) {
+          st3(v.q, row, y);
+          acc[0] += dot3w(ld3c(v.p, row), y);
+        }
       }
     }
     double a1[1] = {acc[0]};
@@ -366,6 +434,141 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_persistent(Bsr<R> A, PcgVecs<
     scal[S_ITERS] = it;
     scal[S_RR] = rr;
     scal[S_RZ] = rz;
+    scal[S_DONE] = 1.0;
+    if (status != 0) scal[S_STATUS] = status;
+    if (*err != 0.0) scal[S_STATUS] = *err;
+  }
+}
+
+
+// ------------------------------------------------ mode 4: Chronopoulos-Gear
+// Preconditioned CG in the Chronopoulos-Gear arrangement: the three dot
+// products of an iteration are taken in the same phase as the SpMV, so an
+// iteration has one elementwise phase and one SpMV+dots phase separated by
+// two grid barriers (standard PCG needs three).  Recurrences, with u = M r
+// and w = A u:
+//   p = u + beta p;  s = w + beta s;  x += alpha p;  r -= alpha s;  u = M r
+//   w = A u;  gamma = (r,u), delta = (w,u), rho = (r,r)
+//   beta = gamma / gamma_old;  alpha = gamma / (delta - beta gamma / alpha_old)
+// One CTA of kCgThreads per SM keeps the number of blocks arriving at each
+// barrier at the SM count.
+constexpr int kCgThreads = 768;
+
+template <int NV, int BLOCK>
+__device__ __forceinline__ void all_sum_b(const double* partials, double (&out)[NV]) {
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    s[k] = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK)
+      s[k] += *((volatile const double*)&partials[k * gridDim.x + i]);
+  }
+  block_sum<NV, BLOCK>(s);
+  __shared__ double res[NV];
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) res[k] = s[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) out[k] = res[k];
+  __syncthreads();
+}
+
+template <typename R, int G>
+__device__ __forceinline__ void cg2_spmv_dots(const Bsr<R>& A, const PcgVecs<R>& v, int64_t row0, int64_t stride_rows,
+                                              int lane, double (&acc)[3]) {
+  for (int64_t base = row0; base < A.nbr; base += stride_rows) {
+    const int64_t row = base + ((threadIdx.x & 31) / G);
+    const bool valid = row < A.nbr;
+    const Vec3<R> w = spmv_row<R, G>(A, v.z, row, lane, valid);
+    if (lane == 0 && valid) {
+      st3(v.q, row, w);
+      const Vec3<R> r = ld3c(v.r, row), u = ld3c(v.z, row);
+      acc[0] += dot3w(r, u);
+      acc[1] += dot3w(w, u);
+      acc[2] += dot3w(r, r);
+    }
+  }
+}
+
+template <typename R, int G>
+__global__ void __launch_bounds__(kCgThreads, 1) k_pcg_cg2(Bsr<R> A, PcgVecs<R> v, double* partials, unsigned* bar,
+                                                         double* scal) {
+  unsigned* count = bar;
+  volatile unsigned* gen = bar + 1;
+  volatile double* err = scal + S_BAR_ERR;
+  const double tol2 = scal[S_TOL2];
+  const int max_iter = (int)scal[S_MAXIT];
+  const int lane = threadIdx.x & (G - 1);
+  const int64_t stride_rows = (int64_t)gridDim.x * (blockDim.x / G);
+  const int64_t row0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * (32 / G);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int status = 0, it = 0;
+  double rr = scal[S_RR], gamma = scal[S_RZ];
+  if (scal[S_DONE] == 0.0) {
+    // prologue: w = A u (u = z = M r from the init kernel), gamma, delta
+    double acc[3] = {0.0, 0.0, 0.0};
+    cg2_spmv_dots<R, G>(A, v, row0, stride_rows, lane, acc);
+    block_sum<3, kCgThreads>(acc);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) partials[k * gridDim.x + blockIdx.x] = acc[k];
+    bool ok = grid_barrier(count, gen, err);
+    double sm[3] = {0.0, 0.0, 0.0};
+    if (ok) all_sum_b<3, kCgThreads>(partials, sm);
+    gamma = sm[0];
+    double delta = sm[1];
+    double alpha = gamma / delta;
+    double beta = 0.0;
+    if (!ok) status = SKG_ERR_TIMEOUT;
+    else if (!(delta > 0.0) || !isfinite(delta)) status = isfinite(delta) ? 0 : SKG_ERR_NONFINITE;
+    while (ok && status == 0 && (delta > 0.0)) {
+      // p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = M r
+      const R a = R(alpha), b = R(beta);
+      for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
+        const Vec3<R> u = ld3c(v.z, i), w = ld3c(v.q, i);
+        Vec3<R> p = ld3c(v.p, i), s = ld3c(v.s, i), x = ld3c(v.x, i), r = ld3c(v.r, i);
+        if (it == 0) {
+          p = u;
+          s = w;
+        } else {
+          p = {u.x + b * p.x, u.y + b * p.y, u.z + b * p.z};
+          s = {w.x + b * s.x, w.y + b * s.y, w.z + b * s.z};
+        }
+        x = {x.x + a * p.x, x.y + a * p.y, x.z + a * p.z};
+        r = {r.x - a * s.x, r.y - a * s.y, r.z - a * s.z};
+        st3(v.p, i, p);
+        st3(v.s, i, s);
+        st3(v.x, i, x);
+        st3(v.r, i, r);
+        st3(v.z, i, jacobi_apply(A.jinv, i, r));
+      }
+      ++it;
+      if (!grid_barrier(count, gen, err)) { status = SKG_ERR_TIMEOUT; break; }
+      double acc2[3] = {0.0, 0.0, 0.0};
+      cg2_spmv_dots<R, G>(A, v, row0, stride_rows, lane, acc2);
+      block_sum<3, kCgThreads>(acc2);
+      if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[k * gridDim.x + blockIdx.x] = acc2[k];
+      if (!grid_barrier(count, gen, err)) { status = SKG_ERR_TIMEOUT; break; }
+      all_sum_b<3, kCgThreads>(partials, sm);
+      const double g_new = sm[0];
+      delta = sm[1];
+      rr = sm[2];
+      if (!isfinite(rr) || !isfinite(g_new)) { status = SKG_ERR_NONFINITE; break; }
+      if (rr <= tol2 || it >= max_iter) { gamma = g_new; break; }
+      beta = g_new / gamma;
+      const double den = delta - beta * g_new / alpha;
+      if (!(den > 0.0)) { gamma = g_new; break; }   // loss of positive definiteness: stop with current x
+      alpha = g_new / den;
+      gamma = g_new;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_ITERS] = it;
+    scal[S_RR] = rr;
+    scal[S_RZ] = gamma;
     scal[S_DONE] = 1.0;
     if (status != 0) scal[S_STATUS] = status;
     if (*err != 0.0) scal[S_STATUS] = *err;
@@ -528,7 +731,7 @@ template <typename R> static int64_t cluster_rows_limit() {
 template <typename R>
 static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
-                     cudaStream_t s, PcgResult* res) {
+                     cudaStream_t s, PcgResult* res, int variant = 0) {
   const int rb = reduce_blocks(A.nbr);
   if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : 1;
   if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 1;
@@ -541,10 +744,42 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
   if (mode == 2) {
     SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s));
     res->launches += 1;
-  } else if (mode == 1) {
+  } else if (mode == 4) {
     int per_sm = 0;
-    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<R, kG>, kBlock, 0));
-    int64_t want = (A.nbr * kG + kBlock - 1) / kBlock;
+    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_cg2<R, kG>, kCgThreads, 0));
+    if (per_sm < 1) return fail(SKG_ERR_CUDA, "the PCG kernel does not fit on an SM");
+    int64_t want = (A.nbr * kG + kCgThreads - 1) / kCgThreads;
+    int64_t cap = num_sms();
+    int grid = (int)(want < cap ? want : cap);
+    if (grid < 1) grid = 1;
+    unsigned* bar = counter + 4;
+    SKG_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+    SKG_CUDA(cudaMemsetAsync(scal + S_BAR_ERR, 0, sizeof(double), s));
+    Bsr<R> a2 = A;
+    PcgVecs<R> v2 = v;
+    double* p2 = partials;
+    double* sc2 = scal;
+    void* args[] = {&a2, &v2, &p2, &bar, &sc2};
+    SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_cg2<R, kG>, dim3(grid), dim3(kCgThreads), args, 0, s));
+    res->launches += 1;
+  } else if (mode == 1) {
+    // kernel variant: lanes per row G and rows in flight U (picked by the autotuner)
+    const void* kern = (const void*)k_pcg_persistent<R, 8, 1>;
+    int G = 8;
+    switch (variant) {
+      case 1: kern = (const void*)k_pcg_persistent<R, 16, 1>; G = 16; break;
+      case 2: kern = (const void*)k_pcg_persistent<R, 8, 2>; G = 8; break;
+      case 3: kern = (const void*)k_pcg_persistent<R, 16, 2>; G = 16; break;
+      case 4: kern = (const void*)k_pcg_persistent<R, 4, 2>; G = 4; break;
+      case 5: kern = (const void*)k_pcg_persistent<R, 4, 4>; G = 4; break;
+      case 6: kern = (const void*)k_pcg_persistent<R, 2, 4>; G = 2; break;
+      case 7: kern = (const void*)k_pcg_persistent<R, 8, 4>; G = 8; break;
+      case 8: kern = (const void*)k_pcg_persistent<R, 2, 2>; G = 2; break;
+      default: break;
+    }
+    int per_sm = 0;
+    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0));
+    int64_t want = (A.nbr * G + kBlock - 1) / kBlock;
     int64_t cap = (int64_t)per_sm * num_sms();
     if (cap > kMaxGrid / 2) cap = kMaxGrid / 2;
     int grid = (int)(want < cap ? want : cap);
@@ -557,7 +792,7 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
     double* p2 = partials;
     double* sc2 = scal;
     void* args[] = {&a2, &v2, &p2, &bar, &sc2};
-    SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_persistent<R, kG>, dim3(grid), dim3(kBlock), args, 0, s));
+    SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));
     res->launches += 1;
   } else {
     const int sb = (int)((A.nbr * kG + kBlock - 1) / kBlock);
@@ -606,7 +841,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
   PcgVecs<R> pv;
   R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
-  pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4];
+  pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4]; pv.s = vv[5];
   Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
 
   PhaseTimer pt;
@@ -714,7 +949,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     PcgResult pr{};
     pt.begin();
     SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, eta, prm->pcg_max_iter, prm->pcg_mode, w.partials,
-                         w.counter, w.scal, s, &pr));
+                         w.counter, w.scal, s, &pr, prm->pcg_variant));
     info->t_pcg_ms += pt.end();
     info->launches += pr.launches;
     info->pcg_iters += pr.iters;
@@ -772,6 +1007,374 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   return SKG_OK;
 }
 
+
+// ---------------------------------------------------------------- batched --
+// Many independent meshes (instances) concatenated into one mesh with
+// disjoint vertex and tet ranges.  The element, assembly and gradient kernels
+// run over the concatenation (masked per instance); per-instance sums are one
+// CTA per instance in a fixed order; each instance's PCG runs on a
+// thread-block cluster taken from a largest-first queue; Newton, the forcing
+// term and the line search are per instance.
+
+__global__ void __launch_bounds__(kBlock) k_inst_sumsq(const double* __restrict__ g, const int32_t* __restrict__ rows,
+                                                       double* __restrict__ out) {
+  const int inst = blockIdx.x;
+  double acc[1] = {0.0};
+  for (int64_t d = 3 * (int64_t)rows[inst] + threadIdx.x; d < 3 * (int64_t)rows[inst + 1]; d += blockDim.x)
+    acc[0] += g[d] * g[d];
+  block_sum<1, kBlock>(acc);
+  if (threadIdx.x == 0) out[inst] = acc[0];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_inst_dot(const double* __restrict__ g, const R* __restrict__ dx,
+                                                     const int32_t* __restrict__ rows, const uint8_t* __restrict__ mask,
+                                                     double* __restrict__ out) {
+  const int inst = blockIdx.x;
+  if (mask && !mask[inst]) return;
+  double acc[1] = {0.0};
+  for (int64_t v = rows[inst] + threadIdx.x; v < rows[inst + 1]; v += blockDim.x) {
+    const Vec3<R> d = ld3c(dx, v);
+    acc[0] += g[3 * v] * double(d.x) + g[3 * v + 1] * double(d.y) + g[3 * v + 2] * double(d.z);
+  }
+  block_sum<1, kBlock>(acc);
+  if (threadIdx.x == 0) out[inst] = acc[0];
+}
+
+template <typename R>
+__global__ void k_apply_step_batched(double* __restrict__ u, const R* __restrict__ dx, const double* __restrict__ steps,
+                                     const uint8_t* __restrict__ accept, const int32_t* __restrict__ vert_inst, int64_t n,
+                                     const uint8_t* __restrict__ pinned) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const int inst = vert_inst[v];
+  if (!accept[inst]) return;
+  const double step = steps[inst];
+  const Vec3<R> d = ld3c(dx, v);
+  const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (!(pinned && pinned[3 * v + c])) u[3 * v + c] += step * dd[c];
+}
+
+// u = use[inst] ? u_warm : u_tilde per vertex
+__global__ void k_choose_start(double* __restrict__ u, const double* __restrict__ uw, const double* __restrict__ ut,
+                               const uint8_t* __restrict__ use, const int32_t* __restrict__ vert_inst, int64_t n) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const double* src = use[vert_inst[v]] ? uw : ut;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[3 * v + c] = src[3 * v + c];
+}
+
+struct BatchWs {
+  uint8_t* active;
+  uint8_t* mask;
+  double* eta;
+  double* steps;
+  double* gg;
+  double* slope;
+  double* e2;
+  int32_t* pcg_it;
+  int32_t* pcg_st;
+  unsigned* queue;
+  int64_t bytes;
+};
+
+static BatchWs carve_batch(const skg_tet_mesh* m, const skg_batch* b, int precision, void* base) {
+  Workspace w0 = carve_workspace(m, precision, nullptr);
+  Carve c(base ? static_cast<char*>(base) + w0.bytes : nullptr);
+  const int64_t ni = b->n_inst;
+  BatchWs w{};
+  w.active = c.take<uint8_t>(ni);
+  w.mask = c.take<uint8_t>(ni);
+  w.eta = c.take<double>(ni);
+  w.steps = c.take<double>(ni);
+  w.gg = c.take<double>(ni);
+  w.slope = c.take<double>(ni);
+  w.e2 = c.take<double>(2 * ni);
+  w.pcg_it = c.take<int32_t>(ni);
+  w.pcg_st = c.take<int32_t>(ni);
+  w.queue = c.take<unsigned>(4);
+  w.bytes = w0.bytes + c.off + 256;
+  return w;
+}
+
+template <typename R>
+static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const uint8_t* active, const double* eta,
+                            const double* b, const uint8_t* pinned, R* xout, int max_iter, int32_t* it_out,
+                            int32_t* st_out, unsigned* queue, cudaStream_t s) {
+  auto kern = k_pcg_cluster_queue<R, kG>;
+  static thread_local bool configured = false;
+  if (!configured) {
+    SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
+    configured = true;
+  }
+  // smallest cluster whose shared memory holds the largest instance's vectors
+  int csize = 2;
+  while (csize < kClusterMax && cluster_vec_bytes(bt->max_rows, csize, (int)sizeof(R)) > kClusterSmemBudget) csize *= 2;
+  if (cluster_vec_bytes(bt->max_rows, csize, (int)sizeof(R)) > kClusterSmemBudget)
+    return fail(SKG_ERR_CAPACITY, "batched PCG: an instance of %d block rows exceeds one cluster", bt->max_rows);
+  if (csize < 4) csize = 4;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = kClusterSmemBudget;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(csize, 1, 1);
+  int nclusters = 0;
+  SKG_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
+  if (nclusters < 1) return fail(SKG_ERR_CUDA, "batched PCG: no cluster fits");
+  if (nclusters > bt->n_inst) nclusters = bt->n_inst;
+  cfg.gridDim = dim3(csize * nclusters, 1, 1);
+  SKG_CUDA(cudaMemsetAsync(queue, 0, sizeof(unsigned), s));
+  Bsr<R> a2 = A;
+  SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, bt->inst_rows, bt->order, (int)bt->n_inst, active, eta, b, -1.0, pinned,
+                              xout, max_iter, it_out, st_out, queue, (int)kClusterSmemBudget));
+  return SKG_OK;
+}
+
+template <typename R>
+static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg_be_params* prm,
+                           const skg_be_state* st, void* wsbase, skg_step_info* infos, skg_step_info* total,
+                           cudaStream_t s) {
+  const int64_t n = m->n_verts, nd = 3 * n;
+  const int ni = bt->n_inst;
+  const bool mixed = sizeof(R) == 4;
+  const double inv_h2 = 1.0 / (prm->dt * prm->dt);
+  Workspace w = carve_workspace(m, prm->precision, wsbase);
+  BatchWs bw = carve_batch(m, bt, prm->precision, wsbase);
+  R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
+  R* rec = mixed ? (R*)w.rec32 : (R*)w.rec64;
+  R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
+  R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
+  R* dx = vv[0];
+  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
+  PhaseTimer pt;
+  pt.init(prm->profile != 0, s);
+  *total = skg_step_info{};
+
+  std::vector<uint8_t> active(ni, 0), mask(ni, 0);
+  std::vector<double> g0(ni), gg(ni), eta(ni, 0.0), res_prev(ni, 1.0), eta_prev(ni, 0.0), steps(ni, 1.0),
+      slope(ni), ecur(2 * ni), etry(2 * ni);
+  std::vector<int32_t> pit(ni), pst(ni);
+  for (int i = 0; i < ni; ++i) {
+    infos[i] = skg_step_info{};
+    infos[i].min_alpha = 1.0;
+  }
+
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
+  k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, w.ut, st->u);
+  SKG_LAUNCHED();
+  GradArgs ga{};
+  ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
+  ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
+  ga.partials = w.partials; ga.counter = w.counter; ga.out = w.scal + S_GG;
+  EnergyArgs<R> ea{};
+  if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
+  else ea.tet = make_tet_args64(m, st->u);
+  ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  int launches = 1;
+
+  auto gradient = [&]() -> int {
+    pt.begin();
+    SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    SKG_TRY(launch_vertex_gradient(ga, s));
+    k_inst_sumsq<<<ni, kBlock, 0, s>>>(w.g, bt->inst_rows, bw.gg);
+    SKG_LAUNCHED();
+    launches += 3;
+    total->t_gradient_ms += pt.end();
+    SKG_CUDA(cudaMemcpyAsync(gg.data(), bw.gg, ni * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SKG_CUDA(cudaStreamSynchronize(s));
+    return SKG_OK;
+  };
+  auto energy = [&](const R* d, const double* steps_dev, const uint8_t* mask_dev, double* out_h) -> int {
+    ea.dx = d;
+    pt.begin();
+    SKG_TRY(launch_inst_energy<R>(ea, ni, bt->inst_rows, bt->inst_tets, mask_dev, steps_dev, bw.e2, s));
+    launches++;
+    total->t_energy_ms += pt.end();
+    SKG_CUDA(cudaMemcpyAsync(out_h, bw.e2, 2 * ni * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SKG_CUDA(cudaStreamSynchronize(s));
+    return SKG_OK;
+  };
+  auto split = [&]() -> int {
+    if (!mixed) return SKG_OK;
+    launches++;
+    return launch_split(st->u, n, w.uh, w.ul, s);
+  };
+
+  SKG_TRY(gradient());
+  int n_active = 0;
+  for (int i = 0; i < ni; ++i) {
+    g0[i] = sqrt(gg[i]);
+    infos[i].residual0 = g0[i];
+    infos[i].residual = g0[i] > 0.0 ? 1.0 : 0.0;
+    if (!isfinite(g0[i])) infos[i].status = SKG_ERR_NONFINITE;
+  }
+  if (st->u_warm) {
+    // residual-judged warm start: keep it per instance only if ||g|| drops below ||g(x_tilde)||
+    SKG_CUDA(cudaMemcpyAsync(st->u, st->u_warm, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    SKG_TRY(gradient());
+    for (int i = 0; i < ni; ++i) {
+      const double gw = sqrt(gg[i]);
+      mask[i] = (isfinite(gw) && gw < g0[i]) ? 1 : 0;
+      infos[i].warm_used = mask[i];
+    }
+    SKG_CUDA(cudaMemcpyAsync(bw.mask, mask.data(), ni, cudaMemcpyHostToDevice, s));
+    k_choose_start<<<blocks_for(n), kBlock, 0, s>>>(st->u, st->u_warm, w.ut, bw.mask, bt->vert_inst, n);
+    SKG_LAUNCHED();
+    launches++;
+    SKG_TRY(gradient());
+  }
+  SKG_TRY(split());
+  SKG_TRY(energy(nullptr, nullptr, nullptr, ecur.data()));
+  const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  for (int it = 0; it < prm->max_newton; ++it) {
+    n_active = 0;
+    for (int i = 0; i < ni; ++i) {
+      active[i] = 0;
+      if (infos[i].status != SKG_OK || !(g0[i] > 0.0)) continue;
+      const double res = sqrt(gg[i]) / g0[i];
+      infos[i].residual = res;
+      if (res < prm->tol) continue;
+      double e = prm->pcg_rtol;
+      if (prm->pcg_rtol < 0.0) {
+        const double emax = -prm->pcg_rtol;
+        if (it == 0) {
+          e = emax;
+        } else {
+          const double q = res / res_prev[i];
+          e = 0.9 * q * q;
+          const double safe = 0.9 * eta_prev[i] * eta_prev[i];
+          if (safe > 0.1 && safe > e) e = safe;
+        }
+        const double reach = 0.25 * prm->tol / res;
+        if (e < reach) e = reach;
+        if (e > emax) e = emax;
+        if (e < 1e-8) e = 1e-8;
+      }
+      res_prev[i] = res;
+      eta_prev[i] = e;
+      eta[i] = e;
+      active[i] = 1;
+      ++n_active;
+    }
+    if (n_active == 0) break;
+    SKG_CUDA(cudaMemcpyAsync(bw.active, active.data(), ni, cudaMemcpyHostToDevice, s));
+    SKG_CUDA(cudaMemcpyAsync(bw.eta, eta.data(), ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    // Hessians and assembly of the active instances
+    pt.begin();
+    if constexpr (sizeof(R) == 4) {
+      TetArgs<float> ta = make_tet_args32(m, st->u, w.uh, w.ul);
+      ta.tet_inst = bt->tet_inst;
+      ta.inst_active = bw.active;
+      SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s));
+    } else {
+      TetArgs<double> ta = make_tet_args64(m, st->u);
+      ta.tet_inst = bt->tet_inst;
+      ta.inst_active = bw.active;
+      SKG_TRY(launch_tet_hessian<double>(ta, 1, 1, (double*)hbuf, s));
+    }
+    total->t_hessian_ms += pt.end();
+    AsmArgs<R> aa = make_asm_args<R>(m, hbuf, nullptr, jinv);
+    aa.rec = rec;
+    aa.mass = st->mass;
+    aa.inv_h2 = inv_h2;
+    aa.pinned = st->pinned;
+    aa.vert_inst = bt->vert_inst;
+    aa.inst_active = bw.active;
+    pt.begin();
+    SKG_TRY(launch_assemble<R>(aa, s));
+    total->t_assemble_ms += pt.end();
+    // all active instances' PCG solves, one cluster per instance at a time
+    pt.begin();
+    SKG_TRY(launch_pcg_queue<R>(A, bt, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it,
+                                bw.pcg_st, bw.queue, s));
+    total->t_pcg_ms += pt.end();
+    launches += 3;
+    SKG_CUDA(cudaMemcpyAsync(pit.data(), bw.pcg_it, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    SKG_CUDA(cudaMemcpyAsync(pst.data(), bw.pcg_st, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    k_inst_dot<R><<<ni, kBlock, 0, s>>>(w.g, dx, bt->inst_rows, bw.active, bw.slope);
+    SKG_LAUNCHED();
+    launches++;
+    SKG_CUDA(cudaMemcpyAsync(slope.data(), bw.slope, ni * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SKG_CUDA(cudaStreamSynchronize(s));
+    // line search per instance (simkit/backtracking_line_search.py:56-67)
+    int searching = 0;
+    for (int i = 0; i < ni; ++i) {
+      mask[i] = 0;
+      if (!active[i]) continue;
+      infos[i].pcg_iters += pit[i];
+      infos[i].newton_iters = it + 1;
+      if (pst[i] != 0) {
+        infos[i].status = pst[i];
+        active[i] = 0;
+        continue;
+      }
+      steps[i] = 1.0;
+      mask[i] = 1;
+      ++searching;
+    }
+    std::vector<uint8_t> accept(ni, 0);
+    for (int k = 0; k < prm->ls_max_iter && searching > 0; ++k) {
+      SKG_CUDA(cudaMemcpyAsync(bw.mask, mask.data(), ni, cudaMemcpyHostToDevice, s));
+      SKG_CUDA(cudaMemcpyAsync(bw.steps, steps.data(), ni * sizeof(double), cudaMemcpyHostToDevice, s));
+      SKG_TRY(energy(dx, bw.steps, bw.mask, etry.data()));
+      searching = 0;
+      for (int i = 0; i < ni; ++i) {
+        if (!mask[i]) continue;
+        infos[i].ls_trials++;
+        const double thr =
+            prm->ls_threshold >= 0.0 ? prm->ls_threshold : 1e-12 + 16.0 * eps_r * ecur[2 * i + 1];
+        if (!prm->do_line_search || etry[2 * i] <= ecur[2 * i] + prm->ls_alpha * steps[i] * slope[i] + thr) {
+          accept[i] = 1;
+          mask[i] = 0;
+          ecur[2 * i] = etry[2 * i];
+          ecur[2 * i + 1] = etry[2 * i + 1];
+          if (steps[i] < infos[i].min_alpha) infos[i].min_alpha = steps[i];
+        } else {
+          steps[i] *= prm->ls_beta;
+          ++searching;
+        }
+      }
+    }
+    for (int i = 0; i < ni; ++i)
+      if (mask[i]) {  // exhausted: simkit returns t = 0 and its Newton loop stops
+        infos[i].status = SKG_ERR_LINESEARCH;
+        active[i] = 0;
+      }
+    SKG_CUDA(cudaMemcpyAsync(bw.mask, accept.data(), ni, cudaMemcpyHostToDevice, s));
+    SKG_CUDA(cudaMemcpyAsync(bw.steps, steps.data(), ni * sizeof(double), cudaMemcpyHostToDevice, s));
+    k_apply_step_batched<R><<<blocks_for(n), kBlock, 0, s>>>(st->u, dx, bw.steps, bw.mask, bt->vert_inst, n,
+                                                             st->pinned);
+    SKG_LAUNCHED();
+    launches++;
+    SKG_TRY(split());
+    SKG_TRY(gradient());
+  }
+  for (int i = 0; i < ni; ++i) {
+    if (infos[i].status == SKG_OK && g0[i] > 0.0) {
+      infos[i].residual = sqrt(gg[i]) / g0[i];
+      if (!(infos[i].residual < prm->tol)) infos[i].status = SKG_ERR_NOT_CONVERGED;
+    }
+    infos[i].energy = ecur[2 * i];
+    total->newton_iters += infos[i].newton_iters;
+    total->pcg_iters += infos[i].pcg_iters;
+    total->ls_trials += infos[i].ls_trials;
+    if (infos[i].status != SKG_OK && total->status == SKG_OK) total->status = infos[i].status;
+  }
+  total->launches = launches;
+  return SKG_OK;
+}
+
 }  // namespace skg
 
 using namespace skg;
@@ -796,6 +1399,29 @@ int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg
   Workspace w = carve_workspace(mesh, params->precision, workspace);
   if (params->precision == SKG_MIXED) return be_step<float>(mesh, params, state, w, info_h, s);
   return be_step<double>(mesh, params, state, w, info_h, s);
+}
+
+int64_t skg_batch_workspace_size(const skg_tet_mesh* mesh, const skg_batch* batch, int precision) {
+  if (check_mesh(mesh, precision) != SKG_OK || !batch || batch->n_inst <= 0) return -1;
+  return carve_batch(mesh, batch, precision, nullptr).bytes;
+}
+
+int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
+                        const skg_be_state* state, void* workspace, skg_step_info* infos_h, skg_step_info* total_h,
+                        void* stream) {
+  if (!batch || !params || !state || !workspace || !infos_h || !total_h)
+    return fail(SKG_ERR_ARG, "be_step_batched: null argument");
+  SKG_TRY(check_mesh(mesh, params->precision));
+  if (batch->n_inst <= 0 || !batch->inst_rows || !batch->inst_tets || !batch->vert_inst || !batch->tet_inst ||
+      !batch->order)
+    return fail(SKG_ERR_ARG, "be_step_batched: incomplete batch description");
+  if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "be_step_batched: dt must be positive");
+  if (!state->u || !state->u_curr || !state->u_prev || !state->mass)
+    return fail(SKG_ERR_ARG, "be_step_batched: null state");
+  cudaStream_t s = as_stream(stream);
+  if (params->precision == SKG_MIXED)
+    return be_step_batched<float>(mesh, batch, params, state, workspace, infos_h, total_h, s);
+  return be_step_batched<double>(mesh, batch, params, state, workspace, infos_h, total_h, s);
 }
 
 int64_t skg_pcg_workspace_size(int64_t nbr) {
