@@ -214,6 +214,32 @@ def run_batched(args):
         infos, total = b.step()
         if total.status != 0:
             raise SystemExit(f"batched warm-up step failed: {total}")
+    learned = None
+    fb = None
+    if args.learned:
+        from simkit_gb300 import warmstart as ws
+        t0 = time.perf_counter()
+        train_specs = beam_batch(args.instances, seed=100)
+        tb = BatchedBESolver(train_specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
+        frames, _ = ws.generate_frames(tb, train_specs, args.train_steps)
+        t_gen = time.perf_counter() - t0
+        net = ws.WarmStartMLP(seed=0, lr=1e-3)
+        t0 = time.perf_counter()
+        losses = ws.train(net, tb, frames, epochs=args.epochs, batch_frames=64)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        del frames, tb
+        per_epoch = max(1, len(losses) // max(args.epochs, 1))
+        learned = {"frames": args.instances * args.train_steps, "generate_s": t_gen, "train_s": t_train,
+                   "adam_steps": len(losses), "loss_first_epoch": float(np.mean(losses[:per_epoch])),
+                   "loss_last_epoch": float(np.mean(losses[-per_epoch:]))}
+        fb = ws.FeatureBuilder(b, specs)
+        # the warm-up steps above ran without the network: rebuild the last correction
+        st = b.state()
+        ut = fb.u_tilde()
+        b.step()
+        fb.record_correction(ut)
+        del st
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(0)
@@ -221,8 +247,13 @@ def run_batched(args):
     clocks.start()
     ev0.record(stream)
     totals = []
+    kept = []
     for _ in range(args.steps):
-        infos, total = b.step()
+        if args.learned:
+            infos, total = ws.warm_step(b, fb, net)
+            kept.append(sum(i.warm_used for i in infos) / len(infos))
+        else:
+            infos, total = b.step()
         totals.append(total)
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -232,6 +263,14 @@ def run_batched(args):
         raise SystemExit(f"batched step failed: {[t.status for t in totals]}")
     inst_steps = args.instances * args.steps
     value = inst_steps / (ms / 1000.0)
+    # one extra profiled step (phase times by CUDA events; not part of the timed region)
+    b.params.profile = 1
+    if args.learned:
+        _, prof = ws.warm_step(b, fb, net)
+    else:
+        _, prof = b.step()
+    b.params.profile = 0
+    phase_ms = {k: getattr(prof, f"t_{k}_ms") for k in ("hessian", "assemble", "pcg", "gradient", "energy")}
     newton = sum(t.newton_iters for t in totals)
     tets = b.n_tets
     # plain: the same beams one at a time (sample, state advanced to the same step count)
@@ -255,7 +294,8 @@ def run_batched(args):
         "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": f"{args.instances} beams, nx, ny in 4..16, nz in 8..48, batched plain Newton",
+        "config": {"workload": f"{args.instances} beams, nx, ny in 4..16, nz in 8..48, batched "
+                               + ("+ learned warm start" if args.learned else "plain Newton"),
                    "instances": args.instances, "tets": int(tets), "verts": int(b.n_verts),
                    "precision": args.precision, "pcg_rtol": args.pcg_rtol},
         "tet_hessians_per_s": newton / max(args.instances, 1) * tets / (ms / 1000.0),
@@ -263,8 +303,10 @@ def run_batched(args):
         "plain_single_instance": {"value": plain_value, "unit": "instance-steps/s",
                                   "sample": f"{len(sample)} of the beams stepped alone, {args.steps} steps each"},
         "batched_over_plain": value / plain_value,
-        "phase_ms": {k: sum(getattr(t, f"t_{k}_ms") for t in totals)
-                     for k in ("hessian", "assemble", "pcg", "gradient", "energy")},
+        "learned": learned,
+        "warm_start_kept_fraction": float(np.mean(kept)) if kept else None,
+        "phase_ms_one_step": phase_ms,
+        "newton_iters_profiled_step": prof.newton_iters,
         "gpu_launches": sum(t.launches for t in totals),
         "clocks": clock_info,
     }
@@ -290,6 +332,9 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "batched"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=16)
+    ap.add_argument("--learned", action="store_true", help="batched + learned warm start")
+    ap.add_argument("--train-steps", type=int, default=40)
+    ap.add_argument("--epochs", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -190,8 +190,9 @@ typedef struct skg_be_state {
   const double* f_ext;      /* (3n) external force */
   const uint8_t* pinned;    /* (3n) 1 = DOF held at its rest position */
   const double* u_warm;     /* (3n) optional Newton initial guess (batched step): used per
-                               instance only if its residual is below the residual at
-                               x_tilde; the relative residual stays judged against x_tilde */
+                               instance only if the incremental potential there is below its
+                               value at x_tilde; the relative residual stays judged against
+                               ||g(x_tilde)|| */
 } skg_be_state;
 
 typedef struct skg_step_info {
@@ -239,7 +240,9 @@ typedef struct skg_batch {
 } skg_batch;
 
 int64_t skg_batch_workspace_size(const skg_tet_mesh* mesh, const skg_batch* batch, int precision);
-/* One backward-Euler step of every instance; infos_h[n_inst] per instance, total_h summed. */
+/* One backward-Euler step of every instance; infos_h[n_inst] per instance, total_h summed.
+ * An instance is converged when ||g|| < tol ||g(x_tilde)|| or, for instances that have come to
+ * rest, ||g|| < 1e-10 ||f_ext|| (below that the relative test measures FP64 noise). */
 int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
                         const skg_be_state* state, void* workspace, skg_step_info* infos_h, skg_step_info* total_h,
                         void* stream);
@@ -305,11 +308,14 @@ int skg_warmstart_features(const double* X, const double* u, const double* u_pre
                            const double* f_ext, const double* mass, double dt, int64_t n, const int32_t* inst_rows,
                            const int32_t* vert_inst, int n_inst, const float* inst_scalars, float* vf, float* ctx,
                            void* out, void* stream);
-/* u_warm = u_tilde + 9.8 dt^2 * pred[:, 0:3] (pinned DOFs stay at u_tilde). */
-int skg_warmstart_apply(const double* u_tilde, const float* pred, int ld_pred, const uint8_t* pinned, double dt,
-                        int64_t n, double* u_warm, void* stream);
-/* training targets (u_next - u_tilde) / (9.8 dt^2), [n][3] FP32. */
-int skg_warmstart_targets(const double* u_next, const double* u_tilde, double dt, int64_t n, float* t, void* stream);
+/* u_warm = u_tilde + corr + 9.8 dt^2 * pred[:, 0:3] (pinned DOFs stay at u_tilde): the network
+ * refines the second-order extrapolation u_tilde + corr, corr = the previous step's Newton
+ * correction; corr and pred may be null. */
+int skg_warmstart_apply(const double* u_tilde, const double* corr, const float* pred, int ld_pred,
+                        const uint8_t* pinned, double dt, int64_t n, double* u_warm, void* stream);
+/* training targets (u_next - u_tilde - corr) / (9.8 dt^2), [n][3] FP32 (corr may be null). */
+int skg_warmstart_targets(const double* u_next, const double* u_tilde, const double* corr, double dt, int64_t n,
+                          float* t, void* stream);
 
 #ifdef __cplusplus
 }

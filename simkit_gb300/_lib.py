@@ -112,8 +112,8 @@ _SIGNATURES = {
                              ctypes.c_float, c_i32, c_vp, c_i32, c_vp, c_i32, c_vp]),
     "skg_warmstart_features": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp]),
-    "skg_warmstart_apply": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_dbl, c_i64, c_vp, c_vp]),
-    "skg_warmstart_targets": (c_i32, [c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp]),
+    "skg_warmstart_apply": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_vp, c_dbl, c_i64, c_vp, c_vp]),
+    "skg_warmstart_targets": (c_i32, [c_vp, c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp]),
     "skg_pcg_noalloc_max_rows": (c_i64, []),
     "skg_pcg_bsr64_noalloc": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp]),
 }

@@ -100,10 +100,15 @@ class BatchedBESolver:
     def n_verts(self):
         return self.mesh.n
 
-    def step(self, stream=None):
-        """Advance every instance one step; returns (per-instance StepInfo list, total StepInfo)."""
+    def step(self, u_warm=None, stream=None):
+        """Advance every instance one step; returns (per-instance StepInfo list, total StepInfo).
+
+        ``u_warm`` (3n, device FP64): optional Newton starting displacement, kept per
+        instance only where its residual is below the residual at x_tilde.
+        """
         st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
-                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr())
+                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
+                      u_warm=u_warm.data_ptr() if u_warm is not None else None)
         total = StepInfoC()
         check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
                                               ctypes.byref(self.params), ctypes.byref(st),
@@ -113,8 +118,15 @@ class BatchedBESolver:
         self.steps += 1
         conv = lambda c: StepInfo(c.newton_iters, c.pcg_iters, c.ls_trials, c.status, c.residual0, c.residual,
                                   c.min_alpha, c.energy, c.launches, c.t_hessian_ms, c.t_assemble_ms, c.t_pcg_ms,
-                                  c.t_gradient_ms, c.t_energy_ms)
+                                  c.t_gradient_ms, c.t_energy_ms, c.warm_used)
         return [conv(c) for c in self._infos], conv(total)
+
+    def state(self):
+        return self.u_curr.clone(), self.u_prev.clone()
+
+    def set_state(self, st):
+        self.u_curr.copy_(st[0])
+        self.u_prev.copy_(st[1])
 
     def displacement(self, inst=None) -> np.ndarray:
         u = self.u_curr.cpu().numpy()

@@ -558,27 +558,33 @@ __global__ void k_assemble_features(const float* __restrict__ vf, const float* _
   out[i] = __float2bfloat16(x);
 }
 
-// u_warm = u_tilde + s * pred (pinned DOFs stay at rest), s = 9.8 dt^2
-__global__ void k_apply_prediction(const double* __restrict__ u_tilde, const float* __restrict__ pred, int ld_pred,
-                                   const uint8_t* __restrict__ pinned, double dt, int64_t n, double* __restrict__ uw) {
+// u_warm = u_tilde + corr + s * pred (pinned DOFs stay at rest), s = 9.8 dt^2: the network
+// refines the second-order extrapolation u_tilde + corr (corr = previous Newton correction)
+__global__ void k_apply_prediction(const double* __restrict__ u_tilde, const double* __restrict__ corr,
+                                   const float* __restrict__ pred, int ld_pred, const uint8_t* __restrict__ pinned,
+                                   double dt, int64_t n, double* __restrict__ uw) {
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (v >= n) return;
   const double s = 9.8 * dt * dt;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const int64_t k = 3 * v + c;
-    uw[k] = (pinned && pinned[k]) ? u_tilde[k] : u_tilde[k] + s * (double)pred[(size_t)v * ld_pred + c];
+    const double base = u_tilde[k] + (corr ? corr[k] : 0.0);
+    uw[k] = (pinned && pinned[k]) ? u_tilde[k] : base + (pred ? s * (double)pred[(size_t)v * ld_pred + c] : 0.0);
   }
 }
 
-// target rows: (u_next - u_tilde) / s, FP32 [n][16] (3 used)
-__global__ void k_targets(const double* __restrict__ u_next, const double* __restrict__ u_tilde, double dt, int64_t n,
-                          float* __restrict__ t) {
+// target rows: (u_next - u_tilde - corr) / s, FP32 [n][3]
+__global__ void k_targets(const double* __restrict__ u_next, const double* __restrict__ u_tilde,
+                          const double* __restrict__ corr, double dt, int64_t n, float* __restrict__ t) {
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (v >= n) return;
   const double s = 9.8 * dt * dt;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) t[(size_t)v * 3 + c] = (float)((u_next[3 * v + c] - u_tilde[3 * v + c]) / s);
+  for (int c = 0; c < 3; ++c) {
+    const int64_t k = 3 * v + c;
+    t[(size_t)v * 3 + c] = (float)((u_next[k] - u_tilde[k] - (corr ? corr[k] : 0.0)) / s);
+  }
 }
 
 }  // namespace skg
@@ -600,17 +606,19 @@ int skg_warmstart_features(const double* X, const double* u, const double* u_pre
   return SKG_OK;
 }
 
-int skg_warmstart_apply(const double* u_tilde, const float* pred, int ld_pred, const uint8_t* pinned, double dt,
-                        int64_t n, double* u_warm, void* stream) {
+int skg_warmstart_apply(const double* u_tilde, const double* corr, const float* pred, int ld_pred,
+                        const uint8_t* pinned, double dt, int64_t n, double* u_warm, void* stream) {
   if (n <= 0) return SKG_OK;
-  k_apply_prediction<<<blocks_for(n), kBlock, 0, as_stream(stream)>>>(u_tilde, pred, ld_pred, pinned, dt, n, u_warm);
+  k_apply_prediction<<<blocks_for(n), kBlock, 0, as_stream(stream)>>>(u_tilde, corr, pred, ld_pred, pinned, dt, n,
+                                                                       u_warm);
   SKG_LAUNCHED();
   return SKG_OK;
 }
 
-int skg_warmstart_targets(const double* u_next, const double* u_tilde, double dt, int64_t n, float* t, void* stream) {
+int skg_warmstart_targets(const double* u_next, const double* u_tilde, const double* corr, double dt, int64_t n,
+                          float* t, void* stream) {
   if (n <= 0) return SKG_OK;
-  k_targets<<<blocks_for(n), kBlock, 0, as_stream(stream)>>>(u_next, u_tilde, dt, n, t);
+  k_targets<<<blocks_for(n), kBlock, 0, as_stream(stream)>>>(u_next, u_tilde, corr, dt, n, t);
   SKG_LAUNCHED();
   return SKG_OK;
 }

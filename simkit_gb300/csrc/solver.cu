@@ -1211,31 +1211,42 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     return launch_split(st->u, n, w.uh, w.ul, s);
   };
 
+  // per-instance |f_ext|: the absolute residual floor 1e-10 |f_ext| (far below any physical
+  // force, far above FP64 force-evaluation noise) ends instances that settle at rest, where
+  // 1e-6 of ||g(x_tilde)|| is below the noise of the gradient itself
+  std::vector<double> fnorm(ni);
+  k_inst_sumsq<<<ni, kBlock, 0, s>>>(st->f_ext ? st->f_ext : w.g, bt->inst_rows, bw.gg);
+  SKG_LAUNCHED();
+  SKG_CUDA(cudaMemcpyAsync(fnorm.data(), bw.gg, ni * sizeof(double), cudaMemcpyDeviceToHost, s));
   SKG_TRY(gradient());
   int n_active = 0;
   for (int i = 0; i < ni; ++i) {
+    fnorm[i] = st->f_ext ? sqrt(fnorm[i]) : 0.0;
     g0[i] = sqrt(gg[i]);
     infos[i].residual0 = g0[i];
     infos[i].residual = g0[i] > 0.0 ? 1.0 : 0.0;
     if (!isfinite(g0[i])) infos[i].status = SKG_ERR_NONFINITE;
   }
+  SKG_TRY(split());
+  SKG_TRY(energy(nullptr, nullptr, nullptr, ecur.data()));
   if (st->u_warm) {
-    // residual-judged warm start: keep it per instance only if ||g|| drops below ||g(x_tilde)||
+    // energy-judged warm start: keep it per instance only if the incremental potential
+    // (the function Newton minimises) is lower there than at x_tilde
     SKG_CUDA(cudaMemcpyAsync(st->u, st->u_warm, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    SKG_TRY(gradient());
+    SKG_TRY(split());
+    SKG_TRY(energy(nullptr, nullptr, nullptr, etry.data()));
     for (int i = 0; i < ni; ++i) {
-      const double gw = sqrt(gg[i]);
-      mask[i] = (isfinite(gw) && gw < g0[i]) ? 1 : 0;
+      mask[i] = (isfinite(etry[2 * i]) && etry[2 * i] < ecur[2 * i]) ? 1 : 0;
       infos[i].warm_used = mask[i];
     }
     SKG_CUDA(cudaMemcpyAsync(bw.mask, mask.data(), ni, cudaMemcpyHostToDevice, s));
     k_choose_start<<<blocks_for(n), kBlock, 0, s>>>(st->u, st->u_warm, w.ut, bw.mask, bt->vert_inst, n);
     SKG_LAUNCHED();
     launches++;
+    SKG_TRY(split());
+    SKG_TRY(energy(nullptr, nullptr, nullptr, ecur.data()));
     SKG_TRY(gradient());
   }
-  SKG_TRY(split());
-  SKG_TRY(energy(nullptr, nullptr, nullptr, ecur.data()));
   const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
   for (int it = 0; it < prm->max_newton; ++it) {
     n_active = 0;
@@ -1244,7 +1255,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
       if (infos[i].status != SKG_OK || !(g0[i] > 0.0)) continue;
       const double res = sqrt(gg[i]) / g0[i];
       infos[i].residual = res;
-      if (res < prm->tol) continue;
+      if (res < prm->tol || sqrt(gg[i]) < 1e-10 * fnorm[i]) continue;
       double e = prm->pcg_rtol;
       if (prm->pcg_rtol < 0.0) {
         const double emax = -prm->pcg_rtol;
@@ -1363,7 +1374,8 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   for (int i = 0; i < ni; ++i) {
     if (infos[i].status == SKG_OK && g0[i] > 0.0) {
       infos[i].residual = sqrt(gg[i]) / g0[i];
-      if (!(infos[i].residual < prm->tol)) infos[i].status = SKG_ERR_NOT_CONVERGED;
+      if (!(infos[i].residual < prm->tol) && !(sqrt(gg[i]) < 1e-10 * fnorm[i]))
+        infos[i].status = SKG_ERR_NOT_CONVERGED;
     }
     infos[i].energy = ecur[2 * i];
     total->newton_iters += infos[i].newton_iters;

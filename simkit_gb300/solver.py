@@ -38,6 +38,7 @@ class StepInfo:
     t_pcg_ms: float = 0.0
     t_gradient_ms: float = 0.0
     t_energy_ms: float = 0.0
+    warm_used: int = 0
 
     @property
     def converged(self) -> bool:

@@ -105,3 +105,80 @@ def test_helpers_match_torch(lib):
     torch.nn.functional.gelu(zz, approximate="tanh").backward(dH.float())
     torch.cuda.synchronize()
     assert (dZ.float() - zz.grad).abs().max().item() <= 1e-2 * zz.grad.abs().max().item()
+
+
+def test_mlp_gradients_match_fp64_oracle():
+    """Tensor-core forward/backward of the warm-start MLP vs the FP64 CPU oracle on the same
+    BF16-rounded weights and inputs.  Tolerance 5e-2 (norm-wise, per parameter tensor):
+    activations are stored in BF16 between layers (8-bit mantissa)."""
+    import numpy as np
+    from simkit_gb300.warmstart import WarmStartMLP
+    from oracle import mlp as ref
+    net = WarmStartMLP(seed=3)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    M = 700
+    X = torch.zeros(M, 64, dtype=torch.bfloat16, device="cuda")
+    X[:, :47] = torch.randn(M, 47, generator=g, device="cuda").bfloat16()
+    T = torch.randn(M, 3, generator=g, device="cuda")
+    loss, dY = net.loss_and_grad(X, T)
+    dWs, dbs = net.backward(dY)
+    Ws = [w.bfloat16().double().cpu().numpy() for w in net.W]
+    bs = [b.double().cpu().numpy() for b in net.b]
+    lref, dWr, dbr = ref.loss_and_grads(Ws, bs, X.double().cpu().numpy(), T.double().cpu().numpy())
+    assert abs(loss - lref) <= 2e-2 * abs(lref)
+    for l in range(4):
+        gw = dWs[l].double().cpu().numpy()
+        gb = dbs[l].double().cpu().numpy()
+        if l == 3:
+            gw, gb, rw, rb = gw[:3], gb[:3], dWr[l][:3], dbr[l][:3]
+        else:
+            rw, rb = dWr[l], dbr[l]
+        assert np.linalg.norm(gw - rw) <= 5e-2 * np.linalg.norm(rw), l
+        assert np.linalg.norm(gb - rb) <= 5e-2 * np.linalg.norm(rb) + 1e-12, l
+
+
+def test_warm_start_training_and_effect():
+    """Frames from the plain batched solver train the MLP on the tensor-core kernels (the epoch-mean
+    loss falls); from identical states, steps started from x_tilde, from the second-order
+    extrapolation and from the learned prediction all converge to the same tolerance to the
+    same answer, and the learned start costs no more Newton iterations than the plain one
+    (within Newton's own step-to-step variation)."""
+    import numpy as np
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    from simkit_gb300 import warmstart as ws
+    specs = beam_batch(24, seed=5, nx_range=(4, 8), ny_range=(4, 8), nz_range=(8, 16))
+    solver = BatchedBESolver(specs)
+    frames, fb = ws.generate_frames(solver, specs, 10)
+    net = ws.WarmStartMLP(seed=0)
+    per_epoch = (10 * 24) // 16
+    losses = ws.train(net, solver, frames, epochs=12, batch_frames=16)
+    first, last = np.mean(losses[:per_epoch]), np.mean(losses[-per_epoch:])
+    assert last < first, (first, last)
+    its = {"plain": 0, "extrapolated": 0, "learned": 0}
+    kept = []
+    for _ in range(4):
+        st = solver.state()
+        corr = fb.corr.clone()
+        results = {}
+        for mode in ("plain", "extrapolated", "learned"):
+            solver.set_state(st)
+            fb.corr.copy_(corr)
+            if mode == "plain":
+                ut = fb.u_tilde()
+                infos, tot = solver.step()
+                fb.record_correction(ut)
+            else:
+                infos, tot = ws.warm_step(solver, fb, net if mode == "learned" else None)
+            assert tot.status == 0 and all(i.converged for i in infos), mode
+            its[mode] += tot.newton_iters
+            results[mode] = solver.state()
+            if mode == "learned":
+                kept.append(sum(i.warm_used for i in infos) / len(infos))
+        # the start changes the iteration count, not the converged answer
+        d = (results["learned"][0] - results["plain"][0]).abs().max().item()
+        assert d <= 1e-6 * results["plain"][0].abs().max().item() + 1e-12
+    print(f"\nloss {first:.3e} -> {last:.3e}; newton iterations {its}; prediction kept {np.mean(kept):.2f}")
+    # the prediction is only kept where it lowers the incremental potential, so it cannot
+    # make an instance worse by more than Newton's own variation; allow that margin
+    assert its["learned"] <= its["plain"] * 1.05 + 2
