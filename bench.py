@@ -214,6 +214,9 @@ def run_batched(args):
         infos, total = b.step()
         if total.status != 0:
             raise SystemExit(f"batched warm-up step failed: {total}")
+    # cluster-size policy of the batched PCG (untimed; cached per device and batch)
+    from simkit_gb300.autotune import tune_batch_policy
+    policy, policy_ms = tune_batch_policy(b, use_cache=not args.retune)
     learned = None
     fb = None
     if args.learned:
@@ -300,6 +303,8 @@ def run_batched(args):
                    "precision": args.precision, "pcg_rtol": args.pcg_rtol},
         "tet_hessians_per_s": newton / max(args.instances, 1) * tets / (ms / 1000.0),
         "newton_iters_per_instance_step": newton / inst_steps,
+        "pcg_iters_per_instance_step": sum(t.pcg_iters for t in totals) / inst_steps,
+        "batch_policy": {"vec_kb": policy[0], "min_cluster": policy[1], "step_ms_by_policy": policy_ms},
         "plain_single_instance": {"value": plain_value, "unit": "instance-steps/s",
                                   "sample": f"{len(sample)} of the beams stepped alone, {args.steps} steps each"},
         "batched_over_plain": value / plain_value,

@@ -180,6 +180,12 @@ typedef struct skg_be_params {
   int32_t pcg_variant;      /* grid-persistent PCG kernel variant 0-8 (lanes per row x rows in
                                flight: 8x1, 16x1, 8x2, 16x2, 4x2, 4x4, 2x4, 8x4, 2x2), chosen
                                by the autotuner */
+  int32_t batch_min_cluster; /* batched PCG: smallest thread-block cluster an instance gets (1, 2,
+                               4, 8 or 16; 0 = 4); each instance gets the smallest power of two
+                               at least this large whose CTAs hold its vectors */
+  int32_t batch_vec_kb;     /* batched PCG: the cluster size is the smallest whose per-CTA vectors
+                               take at most this many KiB of shared memory, leaving the rest for
+                               block records (0 = 170); if none does, the smallest that fits */
 } skg_be_params;
 
 typedef struct skg_be_state {

@@ -1,5 +1,6 @@
-"""Autotuner for the grid-persistent PCG kernel.
+"""Autotuners for the PCG kernels.
 
+Single systems: the grid-persistent PCG kernel
 The PCG kernel comes in variants that trade lanes per block row (G) against
 block rows in flight per lane group (U): (8,1), (16,1), (8,2), (16,2),
 (4,2), (4,4), (2,4), (8,4), (2,2).  Which one keeps the most loads in flight without idling lanes
@@ -9,6 +10,13 @@ saved state with per-phase CUDA-event timing, and the variant with the
 lowest time per PCG iteration wins.  Results are cached in a JSON file keyed
 by device, system size and precision (``$SIMKIT_GB300_CACHE`` or
 ``~/.cache/simkit_gb300/autotune.json``).
+
+Batches: the cluster-size policy of the batched PCG (the per-CTA shared-memory
+cap for vectors and the smallest cluster an instance gets) decides how many
+instances solve at once and whether their block records stay in shared
+memory; candidates are timed over one whole batched step from the same saved
+state, and the fastest is cached by device, instance count, total rows and
+precision.
 """
 
 from __future__ import annotations
@@ -80,3 +88,47 @@ def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
         table[key] = {"variant": best, "us_per_iter": {str(k): v for k, v in timings.items()}}
         _store(table)
     return best, timings
+
+
+BATCH_POLICIES = ((60, 1), (60, 4), (170, 1), (170, 4), (220, 4))  # (vector KiB cap, smallest cluster)
+
+
+def _batch_key(bsolver):
+    return (f"{torch.cuda.get_device_name()}|batch={bsolver.n_inst}|rows={bsolver.mesh.n}"
+            f"|prec={bsolver.precision}")
+
+
+def tune_batch_policy(bsolver, policies=BATCH_POLICIES, use_cache=True):
+    """Pick the batched PCG cluster policy for ``bsolver`` (a BatchedBESolver) by timing one
+    step per candidate from the same state; returns ((vec_kb, min_cluster), timings_ms)."""
+    key = _batch_key(bsolver)
+    table = _load() if use_cache else {}
+    if key in table:
+        vk, mc = table[key]["policy"]
+        bsolver.params.batch_vec_kb, bsolver.params.batch_min_cluster = int(vk), int(mc)
+        return (int(vk), int(mc)), table[key]["ms"]
+    st = bsolver.state()
+    steps = bsolver.steps
+    timings = {}
+    stream = torch.cuda.current_stream()
+    for vk, mc in policies:
+        bsolver.params.batch_vec_kb, bsolver.params.batch_min_cluster = vk, mc
+        best = None
+        for _ in range(2):
+            bsolver.set_state(st)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            bsolver.step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        timings[f"{vk},{mc}"] = best
+    bsolver.set_state(st)
+    bsolver.steps = steps
+    vk, mc = map(int, min(timings, key=timings.get).split(","))
+    bsolver.params.batch_vec_kb, bsolver.params.batch_min_cluster = vk, mc
+    if use_cache:
+        table[key] = {"policy": [vk, mc], "ms": timings}
+        _store(table)
+    return (vk, mc), timings

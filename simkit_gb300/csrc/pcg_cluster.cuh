@@ -1,21 +1,33 @@
-// PCG on one thread-block cluster, for systems small enough that grid-wide
+// PCG on thread-block clusters, for systems small enough that grid-wide
 // synchronisation and L2 round trips dominate a PCG iteration (on the
 // 12,288-tet beam the grid-persistent kernel spends 24 of 43 cycles per
 // instruction at grid barriers and moves its whole working set through L2).
 //
 // Layout: the cluster's CTAs split the block rows into contiguous ranges.
-// Each CTA keeps the PCG vectors of its own rows (x, r, z, p, q and the 3x3
-// block-Jacobi inverses) in shared memory; the SpMV gathers p of
-// neighbouring rows from the owning CTA through distributed shared memory
-// (ld.shared::cluster).  When a CTA's rows fit, their block values are staged
-// in shared memory once per solve (the matrix is constant during a solve) and
-// their column indices are replaced by the shared::cluster addresses of the
-// p entries they multiply (mapa), so an iteration touches no global memory.
+// Each CTA keeps the PCG vectors of its own rows in shared memory: z and two
+// buffers of the search direction p interleaved per row (so one address
+// reaches all three), x, r, q = A p and the 3x3 block-Jacobi inverses.  The
+// SpMV gathers neighbouring rows' z and previous p from the owning CTA through
+// distributed shared memory (ld.shared::cluster), or from its own shared
+// memory for its own rows.  When a CTA's rows fit, their block values are
+// staged in shared memory once per solve (the matrix is constant during a
+// solve) with the column index replaced by the shared::cluster address of the
+// column's z|p row (mapa), so an iteration touches no global memory.
 //
-// Synchronisation: the hardware cluster barrier (barrier.cluster arrive /
-// wait with release / acquire semantics) separates phases.  Dot products are
-// reduced per CTA, published in shared memory and summed by every CTA over
-// all ranks with a fixed shuffle tree, so all CTAs hold bitwise the same
+// One iteration has two cluster barriers, one per dependent reduction
+// (p.q, then r.z and r.r): the direction p_k = z_k + beta_k p_{k-1} is never
+// published before the SpMV that uses it; every CTA rebuilds the p_j it
+// gathers from z_j and p_{k-1, j} with the same rounding as the owner, which
+// writes p_k into the other buffer.  This is the standard PCG recurrence, not
+// a reformulation, so the iterates equal the three-barrier form's.
+//
+// Dot products: FP64 for FP64 systems.  For FP32 systems each thread
+// accumulates the exact FP32 products (fma splits each product into two
+// floats) in a double-float pair with Knuth's TwoSum, and pairs are combined
+// by TwoSum: a 48-bit significand, far beyond the FP32 vectors, at FP32
+// instruction rates (the FP64 pipe of this part has 64-cycle dependent
+// latency and 1/71 of the FP32 throughput).  Reductions run in a fixed order
+// and every CTA sums all partials itself, so all CTAs hold bitwise the same
 // scalars and take the same branches.
 #pragma once
 
@@ -26,8 +38,16 @@ namespace skg {
 namespace cgx = cooperative_groups;
 
 constexpr int kClusterThreads = 512;
+constexpr int kClusterWarps = kClusterThreads / 32;
 constexpr int kClusterMax = 16;                 // non-portable cluster size
-constexpr int kClusterSmemBudget = 200 * 1024;  // dynamic shared memory per CTA
+constexpr int kClusterSmemBudget = 220 * 1024;  // dynamic shared memory per CTA
+// batched PCG defaults (measured on 512 beams of 324 to 13,056 block rows): the cluster size is
+// the smallest of at least kClusterMinDefault CTAs whose per-CTA vectors take at most
+// kClusterVecTarget bytes, the rest of the shared memory holding block records
+constexpr int kClusterVecTarget = 170 * 1024;
+constexpr int kClusterMinDefault = 4;
+// shared-memory values per block row: z|p0|p1 (12), x (4), r (4), q (4), Jacobi inverse (9)
+constexpr int kClusterVals = 33;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -49,53 +69,171 @@ __device__ __forceinline__ Vec3<double> ld_cluster3(uint32_t addr, double) {
   asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(c), "=d"(d) : "r"(addr + 16) : "memory");
   return {a, b, c};
 }
-__device__ __forceinline__ double ld_cluster_f64(uint32_t addr) {
+__device__ __forceinline__ Vec3<float> lds3(const unsigned char* p, float) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  return {a.x, a.y, a.z};
+}
+__device__ __forceinline__ Vec3<double> lds3(const unsigned char* p, double) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0];
+  const double b = reinterpret_cast<const double*>(p)[2];
+  return {a.x, a.y, b};
+}
+
+// ---- dot-product accumulators ----------------------------------------------
+
+template <typename R> struct Dacc;
+template <> struct __align__(8) Dacc<double> { double v; };
+template <> struct __align__(8) Dacc<float> { float hi, lo; };
+
+__device__ __forceinline__ void dacc_zero(Dacc<double>& a) { a.v = 0.0; }
+__device__ __forceinline__ void dacc_zero(Dacc<float>& a) { a.hi = 0.f; a.lo = 0.f; }
+
+// Knuth's TwoSum: s + e == a + b exactly (explicit rounding: never contracted or reordered)
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bv = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+  return make_float2(s, e);
+}
+// (hi, lo) pairs: hi carries the running FP32 sum, lo the exact rounding errors of
+// every addition into hi (Neumaier-style compensation), so hi + lo is the sum to
+// about 2^-48 of the magnitudes summed
+__device__ __forceinline__ Dacc<float> dacc_add(Dacc<float> a, Dacc<float> b) {
+  const float2 s = two_sum(a.hi, b.hi);
+  return {s.x, __fadd_rn(s.y, __fadd_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ Dacc<double> dacc_add(Dacc<double> a, Dacc<double> b) { return {a.v + b.v}; }
+
+// a += x . y over three components; each product is split exactly by fma
+__device__ __forceinline__ void dacc_dot3(Dacc<float>& a, Vec3<float> x, Vec3<float> y) {
+  const float p0 = __fmul_rn(x.x, y.x), p1 = __fmul_rn(x.y, y.y), p2 = __fmul_rn(x.z, y.z);
+  const float e0 = __fmaf_rn(x.x, y.x, -p0), e1 = __fmaf_rn(x.y, y.y, -p1), e2 = __fmaf_rn(x.z, y.z, -p2);
+  const float2 s0 = two_sum(a.hi, p0);
+  const float2 s1 = two_sum(s0.x, p1);
+  const float2 s2 = two_sum(s1.x, p2);
+  a.hi = s2.x;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(__fadd_rn(e0, __fadd_rn(e1, e2)), __fadd_rn(s0.y, __fadd_rn(s1.y, s2.y))));
+}
+__device__ __forceinline__ void dacc_dot3(Dacc<double>& a, Vec3<double> x, Vec3<double> y) {
+  a.v = fma(x.z, y.z, fma(x.y, y.y, fma(x.x, y.x, a.v)));
+}
+
+__device__ __forceinline__ Dacc<float> dacc_shfl_down(Dacc<float> a, int o) {
+  return {__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+}
+__device__ __forceinline__ Dacc<double> dacc_shfl_down(Dacc<double> a, int o) {
+  return {__shfl_down_sync(0xffffffffu, a.v, o)};
+}
+__device__ __forceinline__ Dacc<float> dacc_bcast(Dacc<float> a) {
+  return {__shfl_sync(0xffffffffu, a.hi, 0), __shfl_sync(0xffffffffu, a.lo, 0)};
+}
+__device__ __forceinline__ Dacc<double> dacc_bcast(Dacc<double> a) { return {__shfl_sync(0xffffffffu, a.v, 0)}; }
+
+__device__ __forceinline__ void dacc_poison(Dacc<float>& a) { a.hi = __int_as_float(0x7fc00000); }
+__device__ __forceinline__ void dacc_poison(Dacc<double>& a) { a.v = __longlong_as_double(0x7ff8000000000000ll); }
+__device__ __forceinline__ double dacc_value(Dacc<float> a) { return double(a.hi) + double(a.lo); }
+__device__ __forceinline__ double dacc_value(Dacc<double> a) { return a.v; }
+// rounded to the working precision
+__device__ __forceinline__ float dacc_r(Dacc<float> a) { return __fadd_rn(a.hi, a.lo); }
+__device__ __forceinline__ double dacc_r(Dacc<double> a) { return a.v; }
+
+__device__ __forceinline__ Dacc<float> ld_cluster_dacc(uint32_t addr, float) {
+  float a, b;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(a), "=f"(b) : "r"(addr) : "memory");
+  return {a, b};
+}
+__device__ __forceinline__ Dacc<double> ld_cluster_dacc(uint32_t addr, double) {
   double v;
   asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
-  return v;
+  return {v};
 }
 
-// Sum of NV values published by every CTA of the cluster (pub[k] in each
-// CTA's shared memory), computed in a fixed order; result in out[] for every
-// thread of the CTA.  Caller guarantees a cluster barrier since publication.
-template <int NV>
-__device__ __forceinline__ void cluster_allsum(const double* pub, int csize, double* bcast, double (&out)[NV]) {
-  if (threadIdx.x < 32) {
+// tree sum over the first `width` lanes (a power of two) in a fixed order, result in lane 0
+template <typename R, int W> __device__ __forceinline__ Dacc<R> dacc_tree(Dacc<R> a) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double v = 0.0;
-      if ((int)threadIdx.x < csize) v = ld_cluster_f64(cluster_map(smem_addr(pub + k), threadIdx.x));
-      v = warp_sum(v);
-      if (threadIdx.x == 0) bcast[k] = v;
-    }
+  for (int o = W / 2; o > 0; o >>= 1) a = dacc_add(a, dacc_shfl_down(a, o));
+  return a;
+}
+
+// barrier over the cluster (a single-CTA "cluster" needs only the CTA barrier)
+__device__ __forceinline__ void csync(cgx::cluster_group& cl, int csize) {
+  if (csize > 1)
+    cl.sync();
+  else
+    __syncthreads();
+}
+
+// ---- bulk copies into shared memory (TMA, non-tensor form) -------------------
+
+constexpr int kRingMax = 8;                   // ring slots for streamed block records
+// blocks per lane in flight in the SpMV (fewer for FP64 records, which take twice the registers)
+template <typename R> constexpr int kUof = sizeof(R) == 4 ? 4 : 2;
+constexpr int kWaitTries = 1 << 20;           // bound on mbarrier polls (each try_wait also blocks a while)
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// bounded wait for phase `parity` of the barrier to complete; false if it never did
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (int i = 0; i < kWaitTries; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+    if (ok) return true;
   }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) out[k] = bcast[k];
+  return false;
 }
+// global -> this CTA's shared memory, completion counted on `bar` (16-byte aligned, size multiple of 16)
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// generic-proxy writes to global memory become visible to later bulk copies
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-// staged record from shared memory (three / six 16-byte loads)
+// ---- block records ------------------------------------------------------------
+
+// Record slot 10 (a pad slot the assembly leaves zero) receives, at the start of
+// each solve, the shared::cluster address of the z|p row of the block's column;
+// slot 9 (the column) is left intact.
 __device__ __forceinline__ Blk<float> ld_srec(const float* srec, int64_t i) {
   const float4* p = reinterpret_cast<const float4*>(srec) + 3 * i;
   const float4 a = p[0], b = p[1], c = p[2];
-  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.y)};
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z)};
 }
 __device__ __forceinline__ Blk<double> ld_srec(const double* srec, int64_t i) {
   const double2* p = reinterpret_cast<const double2*>(srec) + 6 * i;
-  const double2 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4];
-  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(e.y)};
+  const double2 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4], f = p[5];
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x)};
+}
+// the same from global memory with plain loads (the address slot was written in this kernel,
+// so not through the read-only path)
+__device__ __forceinline__ Blk<float> ld_grec(const float* rec, int64_t i) {
+  const float4* p = reinterpret_cast<const float4*>(rec) + 3 * i;
+  const float4 a = p[0], b = p[1], c = p[2];
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z)};
+}
+__device__ __forceinline__ Blk<double> ld_grec(const double* rec, int64_t i) {
+  const double2* p = reinterpret_cast<const double2*>(rec) + 6 * i;
+  const double2 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4], f = p[5];
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x)};
 }
 
-// first row owned by cluster rank j, and the owner of row c
-__device__ __forceinline__ int64_t cl_row0(int64_t nbr, int j, int csize) { return nbr * j / csize; }
-__device__ __forceinline__ int cl_owner(int64_t c, int64_t nbr, int csize) {
-  return (int)(((c + 1) * csize + nbr - 1) / nbr) - 1;
-}
-
-// Shared memory the kernel needs for its vectors, per CTA.
-inline int64_t cluster_vec_bytes(int64_t nbr, int csize, int rsize) {
+// Shared memory the kernel needs for its vectors and local row offsets, per CTA.
+__host__ __device__ inline int64_t cluster_vec_bytes(int64_t nbr, int csize, int rsize) {
   const int64_t rows_cap = (nbr + csize - 1) / csize;
-  return rows_cap * (5 * 4 + 9) * rsize + 16;
+  return ((rows_cap * kClusterVals * rsize + 15) & ~int64_t(15)) + ((4 * (rows_cap + 1) + 127) & ~int64_t(127));
 }
 
 struct ClusterPcgOut {
@@ -104,55 +242,181 @@ struct ClusterPcgOut {
   double rr, rz, bb;
 };
 
+// Static shared memory of a cluster PCG kernel.
+template <typename R> struct ClusterShared {
+  Dacc<R> pub[2][2];                  // CTA totals: [0] p.q, [1] r.z and r.r
+  Dacc<R> wsum[2][kClusterWarps];     // warp totals
+  uint64_t mbar[kRingMax];            // record ring (slot 0 alone when the records are resident)
+  uint32_t zbase[kClusterMax];        // shared::cluster address of each rank's z|p rows
+  int32_t rowb[kClusterMax + 1];      // first local row of each rank
+  int32_t maxblk;                     // most blocks in one chunk of rows
+  int32_t err;                        // a bounded wait gave up
+};
+
+// Totals over every thread of the cluster of NV accumulators, returned to every
+// thread, in a fixed order (all CTAs get bitwise the same values): warp trees,
+// the CTA's warp totals by warp 0, then each CTA's total read by every warp
+// after the cluster barrier.  The barrier also orders the shared-memory writes
+// of the phase before the call before everything after it.  A pub slot is
+// rewritten only after the next cluster barrier.
+template <typename R, int NV>
+__device__ __forceinline__ void cluster_total(cgx::cluster_group& cl, int csize, Dacc<R> (&v)[NV], Dacc<R>* pub,
+                                              Dacc<R> (*wsum)[kClusterWarps]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const Dacc<R> w = dacc_tree<R, 32>(v[k]);
+    if (lane == 0) wsum[k][wid] = w;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      Dacc<R> x;
+      dacc_zero(x);
+      if (lane < kClusterWarps) x = wsum[k][lane];
+      x = dacc_tree<R, kClusterWarps>(x);
+      if (lane == 0) pub[k] = x;
+    }
+  }
+  csync(cl, csize);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    Dacc<R> y;
+    dacc_zero(y);
+    if (lane < csize) y = csize > 1 ? ld_cluster_dacc(cluster_map(smem_addr(pub + k), lane), R(0)) : pub[k];
+    v[k] = dacc_bcast(dacc_tree<R, kClusterMax>(y));
+  }
+}
+
+// the search direction p = z + beta p_prev, rounded identically wherever it is formed
+__device__ __forceinline__ float pdir(float z, float pp, float beta) { return __fmaf_rn(beta, pp, z); }
+__device__ __forceinline__ double pdir(double z, double pp, double beta) { return __fma_rn(beta, pp, z); }
+template <typename R> __device__ __forceinline__ Vec3<R> pdir3(Vec3<R> z, Vec3<R> pp, R beta) {
+  return {pdir(z.x, pp.x, beta), pdir(z.y, pp.y, beta), pdir(z.z, pp.z, beta)};
+}
+
+// owner rank of local row c (rowb: first row of each rank)
+__device__ __forceinline__ int cl_owner(int c, const int32_t* rowb, int csize, float inv) {
+  int o = min(csize - 1, (int)((float)c * inv));
+  while (o > 0 && c < rowb[o]) --o;
+  while (o < csize - 1 && c >= rowb[o + 1]) ++o;
+  return o;
+}
+
 // Solve the system of block rows [gbase, gbase + nbr) (its columns lie in the
 // same range) on the calling cluster.  b: right-hand side (3n, simkit layout,
 // FP64) scaled by bsign, pinned DOFs forced to zero; x written to xout
-// (padded, global rows).  Every thread of every CTA of the cluster must call
-// it; it ends with a cluster barrier, so shared memory may be reused after.
+// (padded, global rows).  rec: the block records of A (slot 10 of the own rows'
+// records is written).  Every thread of every CTA of the cluster must call it;
+// it ends with a cluster barrier, so shared memory may be reused after.
+//
+// Block records reach shared memory by bulk copies in chunks of one pass of
+// rows: all at once when the CTA's records fit beside its vectors (then an
+// iteration reads no global memory), else through a ring of kRingMax slots at
+// most, refilled while later chunks (and, at the end of an iteration, the
+// reductions and vector updates) are processed.  Without room for two slots
+// the records are read from global memory.
 template <typename R, int G>
 __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
-    cgx::cluster_group& cl, const Bsr<R>& A, int64_t gbase, int64_t nbr, const double* __restrict__ b, double bsign,
-    const uint8_t* __restrict__ pinned, R* __restrict__ xout, double rtol, int max_iter, int smem_bytes,
-    unsigned char* smem_raw, double* pub, double* bcast, uint32_t* pbase) {
+    cgx::cluster_group& cl, const Bsr<R>& A, R* rec, int64_t gbase, int64_t nbr, const double* __restrict__ b,
+    double bsign, const uint8_t* __restrict__ pinned, R* __restrict__ xout, double rtol, int max_iter,
+    int smem_bytes, unsigned char* smem_raw, ClusterShared<R>& sh) {
   const int crank = (int)cl.block_rank();
   const int csize = (int)cl.num_blocks();
-  const int64_t r0 = gbase + cl_row0(nbr, crank, csize);
-  const int64_t r1 = gbase + cl_row0(nbr, crank + 1, csize);
+  const int64_t r0 = gbase + nbr * crank / csize;
+  const int64_t r1 = gbase + nbr * (crank + 1) / csize;
   const int64_t rows_cap = (nbr + csize - 1) / csize;
   const int nr = (int)(r1 - r0);
-  // vectors of own rows, stride 4 per row; Jacobi inverses 9 per row
-  R* sp = reinterpret_cast<R*>(smem_raw);
-  R* sx = sp + 4 * rows_cap;
+  constexpr int ZP = 12;  // z | p0 | p1, 4 values each
+  constexpr uint32_t kRowBytes = ZP * sizeof(R);
+  constexpr uint32_t kRecBytes = kRec * sizeof(R);
+  R* szp = reinterpret_cast<R*>(smem_raw);
+  R* sx = szp + ZP * rows_cap;
   R* sr = sx + 4 * rows_cap;
-  R* sz = sr + 4 * rows_cap;
-  R* sq = sz + 4 * rows_cap;
+  R* sq = sr + 4 * rows_cap;
   R* sj = sq + 4 * rows_cap;
-  // block records of own rows (column field replaced by the cluster address of p[col])
-  const int64_t vec_bytes = ((int64_t)(reinterpret_cast<unsigned char*>(sj + 9 * rows_cap) - smem_raw) + 15) & ~int64_t(15);
+  int32_t* srp = reinterpret_cast<int32_t*>(smem_raw + ((rows_cap * kClusterVals * (int64_t)sizeof(R) + 15) & ~int64_t(15)));
+  const int64_t vec_bytes = cluster_vec_bytes(nbr, csize, (int)sizeof(R));
   R* srec = reinterpret_cast<R*>(smem_raw + vec_bytes);
+  const unsigned char* zp_local = smem_raw;
+  const uint32_t my_cbase = csize > 1 ? cluster_map(smem_addr(szp), crank) : smem_addr(szp);
+  const uint32_t my_span = (uint32_t)(nr * kRowBytes);
+  const int tid = threadIdx.x;
+  const int rows_per_pass = blockDim.x / G;
 
-  if ((int)threadIdx.x < csize) pbase[threadIdx.x] = cluster_map(smem_addr(sp), threadIdx.x);
+  if (tid < csize) sh.zbase[tid] = csize > 1 ? cluster_map(smem_addr(szp), tid) : smem_addr(szp);
+  if (tid <= csize) sh.rowb[tid] = (int32_t)(nbr * tid / csize);
+  if (tid == 0) {
+    sh.maxblk = 0;
+    sh.err = 0;
+  }
+  const float inv = (float)csize / (float)nbr;
   const int b0 = __ldg(A.rowptr + r0);
-  const int b1 = __ldg(A.rowptr + r1);
-  const int64_t nblk = b1 - b0;
-  const bool stage = vec_bytes + nblk * (int64_t)(kRec * sizeof(R)) <= (int64_t)smem_bytes;
+  const int nblk = __ldg(A.rowptr + r1) - b0;
+  for (int i = tid; i <= nr; i += blockDim.x) srp[i] = __ldg(A.rowptr + r0 + i) - b0;
   __syncthreads();
-  if (stage) {
-    for (int64_t i = threadIdx.x; i < nblk; i += blockDim.x) {
-      const Blk<R> bk = ld_rec(A.rec, b0 + i);
-      R* d = srec + kRec * i;
-#pragma unroll
-      for (int m = 0; m < 9; ++m) d[m] = bk.m[m];
-      const int64_t lc = bk.col - gbase;
-      const int o = cl_owner(lc, nbr, csize);
-      d[9] = col_bits((int)(pbase[o] + (uint32_t)((lc - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R))), R(0));
-      d[10] = R(0);
-      d[11] = R(0);
+  // gather addresses into slot 10 of the own rows' records; chunk sizes
+  for (int i = tid; i < nblk; i += blockDim.x) {
+    R* rc = rec + (int64_t)kRec * (b0 + i);
+    const int lc = bits_col(rc[9]) - (int)gbase;
+    const int o = cl_owner(lc, sh.rowb, csize, inv);
+    rc[10] = col_bits((int)(sh.zbase[o] + (uint32_t)(lc - sh.rowb[o]) * kRowBytes), R(0));
+  }
+  const int nchunks = (nr + rows_per_pass - 1) / rows_per_pass;
+  {
+    int mb = 0;
+    for (int c = tid; c < nchunks; c += blockDim.x)
+      mb = max(mb, srp[min(nr, (c + 1) * rows_per_pass)] - srp[c * rows_per_pass]);
+    if (mb > 0) atomicMax(&sh.maxblk, mb);
+  }
+  fence_proxy_async();
+  __syncthreads();
+  const int64_t avail = (int64_t)smem_bytes - vec_bytes;
+  const bool resident = (int64_t)nblk * kRecBytes <= avail;
+  const uint32_t slot_bytes = (uint32_t)(((int64_t)sh.maxblk * kRecBytes + 127) & ~int64_t(127));
+  int ring = 0;
+  if (!resident && nchunks > 0) {
+    const int64_t d = avail / (slot_bytes > 0 ? slot_bytes : 1);
+    ring = (int)(d > kRingMax ? kRingMax : d);
+    if (ring < 2) ring = 0;
+  }
+  auto chunk_rows = [&](int c, int& lo, int& hi) {
+    lo = c * rows_per_pass;
+    hi = min(nr, lo + rows_per_pass);
+  };
+  // issue j-th ring fill: chunk j mod nchunks into slot j mod ring
+  auto issue = [&](int j) {
+    const int c = j % nchunks, sl = j % ring;
+    int lo, hi;
+    chunk_rows(c, lo, hi);
+    const uint32_t bytes = (uint32_t)(srp[hi] - srp[lo]) * kRecBytes;
+    unsigned char* dst = reinterpret_cast<unsigned char*>(srec) + (int64_t)sl * slot_bytes;
+    mbar_expect_tx(&sh.mbar[sl], bytes);
+    bulk_copy(dst, rec + (int64_t)kRec * (b0 + srp[lo]), bytes, &sh.mbar[sl]);
+  };
+  if (tid == 0) {
+    if (resident && nblk > 0) {
+      mbar_init(&sh.mbar[0], 1);
+      fence_mbar_init();
+      mbar_expect_tx(&sh.mbar[0], (uint32_t)nblk * kRecBytes);
+      for (int c = 0; c < nchunks; ++c) {
+        int lo, hi;
+        chunk_rows(c, lo, hi);
+        bulk_copy(reinterpret_cast<unsigned char*>(srec) + (int64_t)srp[lo] * kRecBytes,
+                  rec + (int64_t)kRec * (b0 + srp[lo]), (uint32_t)(srp[hi] - srp[lo]) * kRecBytes, &sh.mbar[0]);
+      }
+    } else if (ring) {
+      for (int k = 0; k < ring; ++k) mbar_init(&sh.mbar[k], 1);
+      fence_mbar_init();
+      for (int j = 0; j < ring; ++j) issue(j);
     }
   }
-  // init: x = 0, r = bsign * b (pinned -> 0), z = p = Jinv r
-  double acc[2] = {0.0, 0.0};
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+  // init: x = 0, r = bsign * b (pinned -> 0), z = Jinv r, p_{-1} = 0
+  Dacc<R> s2[2];
+  dacc_zero(s2[0]);
+  dacc_zero(s2[1]);
+  for (int i = tid; i < nr; i += blockDim.x) {
     const int64_t g = r0 + i;
     R rv[3];
 #pragma unroll
@@ -167,68 +431,98 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
       jl[m] = A.jinv[9 * g + m];
       sj[9 * i + m] = jl[m];
     }
-    const R z0 = jl[0] * rv[0] + jl[1] * rv[1] + jl[2] * rv[2];
-    const R z1 = jl[3] * rv[0] + jl[4] * rv[1] + jl[5] * rv[2];
-    const R z2 = jl[6] * rv[0] + jl[7] * rv[1] + jl[8] * rv[2];
+    const Vec3<R> z{jl[0] * rv[0] + jl[1] * rv[1] + jl[2] * rv[2], jl[3] * rv[0] + jl[4] * rv[1] + jl[5] * rv[2],
+                    jl[6] * rv[0] + jl[7] * rv[1] + jl[8] * rv[2]};
+    R* zr = szp + ZP * i;
+    zr[0] = z.x; zr[1] = z.y; zr[2] = z.z; zr[3] = R(0);
+    zr[8] = R(0); zr[9] = R(0); zr[10] = R(0); zr[11] = R(0);
     R* pr = sr + 4 * i;
     pr[0] = rv[0]; pr[1] = rv[1]; pr[2] = rv[2]; pr[3] = R(0);
-    R* pz = sz + 4 * i;
-    pz[0] = z0; pz[1] = z1; pz[2] = z2; pz[3] = R(0);
-    R* pp = sp + 4 * i;
-    pp[0] = z0; pp[1] = z1; pp[2] = z2; pp[3] = R(0);
     R* px = sx + 4 * i;
     px[0] = px[1] = px[2] = px[3] = R(0);
-    acc[0] += double(rv[0]) * z0 + double(rv[1]) * z1 + double(rv[2]) * z2;
-    acc[1] += double(rv[0]) * rv[0] + double(rv[1]) * rv[1] + double(rv[2]) * rv[2];
+    const Vec3<R> r3{rv[0], rv[1], rv[2]};
+    dacc_dot3(s2[0], r3, z);
+    dacc_dot3(s2[1], r3, r3);
   }
-  block_sum<2, kClusterThreads>(acc);
-  if (threadIdx.x == 0) {
-    pub[0] = acc[0];
-    pub[1] = acc[1];
-  }
-  cl.sync();
-  double s2[2];
-  cluster_allsum<2>(pub, csize, bcast, s2);
-  double rz = s2[0], rr = s2[1];
+  cluster_total<R, 2>(cl, csize, s2, sh.pub[1], sh.wsum);
+  Dacc<R> rz = s2[0];
+  double rr = dacc_value(s2[1]);
   const double bb = rr;
   const double tol2 = rtol * rtol * bb;
   bool done = rr <= tol2 || bb == 0.0 || max_iter <= 0;
+  // the per-iteration stop test in the working precision (FP64 compares cost a 64-cycle
+  // dependent latency each on this part); a threshold below the FP32 range keeps its sign
+  R tol2r = R(tol2);
+  if (tol2 > 0.0 && !(tol2r > R(0))) tol2r = R(1e-45f);
+  Dacc<R> rr_acc = s2[1];
   int it = 0, status = 0;
-  const int lane = threadIdx.x & (G - 1);
-  const int rows_per_pass = blockDim.x / G;
-  const int row_off = (threadIdx.x >> 5) * (32 / G) + ((threadIdx.x & 31) / G);
-  cl.sync();  // every CTA has read pub[0..1] before it is rewritten
+  const int lane = tid & (G - 1);
+  const int row_off = (tid >> 5) * (32 / G) + ((tid & 31) / G);
+  R beta = R(0);
+  int cur = 0;        // p_k goes to buffer cur, p_{k-1} is in buffer cur ^ 1
+  int consumed = 0;   // ring fills consumed so far
+  bool waited_resident = false;
   while (!done) {
-    // q = A p on own rows; partial p.q
-    acc[0] = 0.0;
-    for (int pass = 0; pass < nr; pass += rows_per_pass) {
-      const int li = pass + row_off;
-      const bool valid = li < nr;
-      const int64_t row = r0 + li;
-      int rp = b0, K = 0;
-      if (valid) {
-        rp = __ldg(A.rowptr + row);
-        K = __ldg(A.rowptr + row + 1) - rp;
-      }
-      R a0 = 0, a1 = 0, a2 = 0;
-      if (stage) {
-        for (int k = lane; k < K; k += G) {
-          const Blk<R> bk = ld_srec(srec, rp - b0 + k);
-          const Vec3<R> xv = ld_cluster3((uint32_t)bk.col, R(0));
-          a0 += bk.m[0] * xv.x + bk.m[1] * xv.y + bk.m[2] * xv.z;
-          a1 += bk.m[3] * xv.x + bk.m[4] * xv.y + bk.m[5] * xv.z;
-          a2 += bk.m[6] * xv.x + bk.m[7] * xv.y + bk.m[8] * xv.z;
-        }
+    const uint32_t po = (uint32_t)(4 * (1 + (cur ^ 1)) * sizeof(R));  // byte offset of p_{k-1} in a z|p row
+    const int pn = 4 * (1 + cur);
+    auto gather = [&](uint32_t caddr) -> Vec3<R> {
+      const uint32_t d = caddr - my_cbase;
+      Vec3<R> z, pp;
+      if (d < my_span) {
+        z = lds3(zp_local + d, R(0));
+        pp = lds3(zp_local + d + po, R(0));
       } else {
-        for (int k = lane; k < K; k += G) {
-          const Blk<R> bk = ld_rec(A.rec, rp + k);
-          const int64_t lc = bk.col - gbase;
-          const int o = cl_owner(lc, nbr, csize);
-          const uint32_t ad = pbase[o] + (uint32_t)((lc - cl_row0(nbr, o, csize)) * 4 * (int64_t)sizeof(R));
-          const Vec3<R> xv = ld_cluster3(ad, R(0));
-          a0 += bk.m[0] * xv.x + bk.m[1] * xv.y + bk.m[2] * xv.z;
-          a1 += bk.m[3] * xv.x + bk.m[4] * xv.y + bk.m[5] * xv.z;
-          a2 += bk.m[6] * xv.x + bk.m[7] * xv.y + bk.m[8] * xv.z;
+        z = ld_cluster3(caddr, R(0));
+        pp = ld_cluster3(caddr + po, R(0));
+      }
+      return pdir3(z, pp, beta);
+    };
+    // q = A p_k on own rows; p_k written for own rows; partial p.q
+    Dacc<R> pq[1];
+    dacc_zero(pq[0]);
+    bool lost = false;
+    if (resident && nblk > 0 && !waited_resident) {
+      lost = !mbar_wait(&sh.mbar[0], 0);
+      waited_resident = true;
+    }
+    for (int c = 0; c < nchunks; ++c) {
+      const R* base = srec;  // records of the chunk, indexed by block offset within the CTA
+      if (ring) {
+        const int sl = consumed % ring;
+        if (!mbar_wait(&sh.mbar[sl], (uint32_t)((consumed / ring) & 1))) lost = true;
+        int lo, hi;
+        chunk_rows(c, lo, hi);
+        base = reinterpret_cast<const R*>(reinterpret_cast<const unsigned char*>(srec) + (int64_t)sl * slot_bytes) -
+               (int64_t)kRec * srp[lo];
+      }
+      const int li = c * rows_per_pass + row_off;
+      const bool valid = li < nr;
+      int rp = 0, K = 0;
+      if (valid) {
+        rp = srp[li];
+        K = srp[li + 1] - rp;
+      }
+      // kU blocks per lane per round, all loads issued before the products
+      constexpr int kU = kUof<R>;
+      R a0 = 0, a1 = 0, a2 = 0;
+      for (int k0 = lane; k0 < K; k0 += kU * G) {
+        Blk<R> bk[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int k = k0 + u * G;
+          if (k < K) bk[u] = (resident || ring) ? ld_srec(base, rp + k) : ld_grec(rec, b0 + rp + k);
+        }
+        Vec3<R> v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+          if (k0 + u * G < K) v[u] = gather((uint32_t)bk[u].col);
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          if (k0 + u * G < K) {
+            a0 += bk[u].m[0] * v[u].x + bk[u].m[1] * v[u].y + bk[u].m[2] * v[u].z;
+            a1 += bk[u].m[3] * v[u].x + bk[u].m[4] * v[u].y + bk[u].m[5] * v[u].z;
+            a2 += bk[u].m[6] * v[u].x + bk[u].m[7] * v[u].y + bk[u].m[8] * v[u].z;
+          }
         }
       }
 #pragma unroll
@@ -238,78 +532,88 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
         a2 += __shfl_xor_sync(0xffffffffu, a2, o, G);
       }
       if (lane == 0 && valid) {
+        R* zr = szp + ZP * li;
+        const int pold = 12 - pn;  // the other p buffer
+        const Vec3<R> p = pdir3(Vec3<R>{zr[0], zr[1], zr[2]}, Vec3<R>{zr[pold], zr[pold + 1], zr[pold + 2]}, beta);
+        zr[pn] = p.x; zr[pn + 1] = p.y; zr[pn + 2] = p.z; zr[pn + 3] = R(0);
         R* q = sq + 4 * li;
         q[0] = a0; q[1] = a1; q[2] = a2;
-        const R* p = sp + 4 * li;
-        acc[0] += dot3w(Vec3<R>{p[0], p[1], p[2]}, Vec3<R>{a0, a1, a2});
+        dacc_dot3(pq[0], p, Vec3<R>{a0, a1, a2});
+      }
+      if (ring) {
+        __syncthreads();  // every thread is done with the slot
+        if (tid == 0) issue(consumed + ring);
+        ++consumed;
       }
     }
-    double a1v[1] = {acc[0]};
-    block_sum<1, kClusterThreads>(a1v);
-    if (threadIdx.x == 0) pub[2] = a1v[0];
-    cl.sync();
-    double pqv[1];
-    cluster_allsum<1>(pub + 2, csize, bcast, pqv);
-    const double pq = pqv[0];
-    if (!(pq > 0.0) || !isfinite(pq)) {
-      status = isfinite(pq) ? 0 : SKG_ERR_NONFINITE;
+    if (lost) {  // a copy never landed: poison the reduction so every CTA stops here
+      sh.err = 1;
+      dacc_poison(pq[0]);
+    }
+    cluster_total<R, 1>(cl, csize, pq, sh.pub[0], sh.wsum);
+    const R pqr = dacc_r(pq[0]);
+    if (!(pqr > R(0)) || !isfinite(pqr)) {
+      status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
       break;
     }
-    const R a = R(rz / pq);
-    acc[0] = acc[1] = 0.0;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    const R a = dacc_r(rz) / pqr;
+    Dacc<R> u2[2];
+    dacc_zero(u2[0]);
+    dacc_zero(u2[1]);
+    for (int i = tid; i < nr; i += blockDim.x) {
       R* x = sx + 4 * i;
       R* r = sr + 4 * i;
-      const R* p = sp + 4 * i;
+      R* zr = szp + ZP * i;
+      const R* p = zr + pn;
       const R* q = sq + 4 * i;
       const R* J = sj + 9 * i;
       x[0] += a * p[0];
       x[1] += a * p[1];
       x[2] += a * p[2];
-      const R ra = r[0] - a * q[0], rb = r[1] - a * q[1], rc = r[2] - a * q[2];
-      r[0] = ra; r[1] = rb; r[2] = rc;
-      const R z0 = J[0] * ra + J[1] * rb + J[2] * rc;
-      const R z1 = J[3] * ra + J[4] * rb + J[5] * rc;
-      const R z2 = J[6] * ra + J[7] * rb + J[8] * rc;
-      R* z = sz + 4 * i;
-      z[0] = z0; z[1] = z1; z[2] = z2;
-      acc[0] += dot3w(Vec3<R>{ra, rb, rc}, Vec3<R>{z0, z1, z2});
-      acc[1] += dot3w(Vec3<R>{ra, rb, rc}, Vec3<R>{ra, rb, rc});
+      const Vec3<R> rn{r[0] - a * q[0], r[1] - a * q[1], r[2] - a * q[2]};
+      r[0] = rn.x; r[1] = rn.y; r[2] = rn.z;
+      const Vec3<R> z{J[0] * rn.x + J[1] * rn.y + J[2] * rn.z, J[3] * rn.x + J[4] * rn.y + J[5] * rn.z,
+                      J[6] * rn.x + J[7] * rn.y + J[8] * rn.z};
+      zr[0] = z.x; zr[1] = z.y; zr[2] = z.z;
+      dacc_dot3(u2[0], rn, z);
+      dacc_dot3(u2[1], rn, rn);
     }
-    block_sum<2, kClusterThreads>(acc);
-    if (threadIdx.x == 0) {
-      pub[0] = acc[0];
-      pub[1] = acc[1];
-    }
-    cl.sync();
-    cluster_allsum<2>(pub, csize, bcast, s2);
+    cluster_total<R, 2>(cl, csize, u2, sh.pub[1], sh.wsum);
     ++it;
-    rr = s2[1];
-    const double beta = s2[0] / rz;
-    rz = s2[0];
-    if (!isfinite(rr)) {
+    rr_acc = u2[1];
+    const R rrr = dacc_r(u2[1]);
+    const Dacc<R> rz_old = rz;
+    rz = u2[0];
+    if (!isfinite(rrr)) {
       status = SKG_ERR_NONFINITE;
       break;
     }
-    if (rr <= tol2 || it >= max_iter) break;
-    const R bt = R(beta);
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-      R* p = sp + 4 * i;
-      const R* z = sz + 4 * i;
-      p[0] = z[0] + bt * p[0];
-      p[1] = z[1] + bt * p[1];
-      p[2] = z[2] + bt * p[2];
-    }
-    cl.sync();
+    if (rrr <= tol2r || it >= max_iter) break;
+    beta = dacc_r(rz) / dacc_r(rz_old);
+    cur ^= 1;
   }
   // solution to global memory (padded, the layout the line search reads)
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+  for (int i = tid; i < nr; i += blockDim.x) {
     const R* x = sx + 4 * i;
     st3(xout, r0 + i, Vec3<R>{x[0], x[1], x[2]});
   }
+  // let the copies still in flight land before the shared memory is reused
+  if (tid == 0) {
+    bool ok = true;
+    if (ring) {
+      for (int j = consumed; j < consumed + ring; ++j) ok = mbar_wait(&sh.mbar[j % ring], (uint32_t)((j / ring) & 1)) && ok;
+      for (int k = 0; k < ring; ++k) mbar_inval(&sh.mbar[k]);
+    } else if (resident && nblk > 0) {
+      if (!waited_resident) ok = mbar_wait(&sh.mbar[0], 0);
+      mbar_inval(&sh.mbar[0]);
+    }
+    if (!ok) sh.err = 1;
+  }
+  __syncthreads();
+  if (sh.err) status = SKG_ERR_TIMEOUT;
   // no CTA may leave (or reuse its shared memory) while another still reads it
-  cl.sync();
-  return ClusterPcgOut{it, status, rr, rz, bb};
+  csync(cl, csize);
+  return ClusterPcgOut{it, status, dacc_value(rr_acc), dacc_value(rz), bb};
 }
 
 // one system on one cluster (pcg_mode 2)
@@ -319,11 +623,9 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
                   R* __restrict__ xout, double rtol, int max_iter, double* scal, int smem_bytes) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double pub[4];
-  __shared__ double bcast[4];
-  __shared__ uint32_t pbase[kClusterMax];
-  const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, 0, A.nbr, b, bsign, pinned, xout, rtol, max_iter,
-                                                  smem_bytes, smem_raw, pub, bcast, pbase);
+  __shared__ ClusterShared<R> sh;
+  const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, const_cast<R*>(A.rec), 0, A.nbr, b, bsign, pinned, xout,
+                                                  rtol, max_iter, smem_bytes, smem_raw, sh);
   if (cl.block_rank() == 0 && threadIdx.x == 0) {
     scal[S_ITERS] = o.iters;
     scal[S_RR] = o.rr;
@@ -337,46 +639,44 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 // Many independent systems (instances), one per cluster at a time: each
 // cluster takes the next instance from a queue ordered largest first and
 // solves it to that instance's tolerance.  inst_rows (n_inst + 1) are the
-// instances' block-row offsets; inactive instances are skipped.
+// instances' block-row offsets; order lists the n instances this launch
+// serves; inactive instances are skipped.
 template <typename R, int G>
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_pcg_cluster_queue(Bsr<R> A, const int32_t* __restrict__ inst_rows, const int32_t* __restrict__ order,
-                        int n_inst, const uint8_t* __restrict__ active, const double* __restrict__ eta,
+                        int n, const uint8_t* __restrict__ active, const double* __restrict__ eta,
                         const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
                         R* __restrict__ xout, int max_iter, int32_t* iters_out, int32_t* status_out,
                         unsigned* queue, int smem_bytes) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ double pub[4];
-  __shared__ double bcast[4];
-  __shared__ uint32_t pbase[kClusterMax];
+  __shared__ ClusterShared<R> sh;
   __shared__ int next_inst;
+  __shared__ int inst_sh;
   const int csize = (int)cl.num_blocks();
   for (;;) {
     if (cl.block_rank() == 0 && threadIdx.x == 0) {
       const unsigned idx = atomicAdd(queue, 1u);
-      next_inst = idx < (unsigned)n_inst ? order[idx] : -1;
+      next_inst = idx < (unsigned)n ? order[idx] : -1;
     }
-    cl.sync();
-    __shared__ int inst_sh;
-    if (threadIdx.x == 0) inst_sh = *cl.map_shared_rank(&next_inst, 0);
+    csync(cl, csize);
+    if (threadIdx.x == 0) inst_sh = csize > 1 ? *cl.map_shared_rank(&next_inst, 0) : next_inst;
     __syncthreads();
     const int inst = inst_sh;
-    cl.sync();  // rank 0 may overwrite next_inst only after every CTA has read it
+    csync(cl, csize);  // rank 0 may overwrite next_inst only after every CTA has read it
     if (inst < 0) break;
     if (!active[inst]) continue;
     const int64_t gbase = inst_rows[inst];
     const int64_t nbr = inst_rows[inst + 1] - gbase;
-    const int64_t rows_cap = (nbr + csize - 1) / csize;
-    if (rows_cap * (5 * 4 + 9) * (int64_t)sizeof(R) + 16 > smem_bytes) {
+    if (cluster_vec_bytes(nbr, csize, (int)sizeof(R)) > smem_bytes) {
       if (cl.block_rank() == 0 && threadIdx.x == 0) {
         iters_out[inst] = 0;
         status_out[inst] = SKG_ERR_CAPACITY;
       }
       continue;
     }
-    const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, gbase, nbr, b, bsign, pinned, xout, eta[inst], max_iter,
-                                                    smem_bytes, smem_raw, pub, bcast, pbase);
+    const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, const_cast<R*>(A.rec), gbase, nbr, b, bsign, pinned,
+                                                    xout, eta[inst], max_iter, smem_bytes, smem_raw, sh);
     if (cl.block_rank() == 0 && threadIdx.x == 0) {
       iters_out[inst] = o.iters;
       status_out[inst] = o.status;

@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "assembly.cuh"
@@ -680,14 +681,15 @@ static int num_sms() {
   return g_num_sms;
 }
 
-constexpr int kG = 8;  // lanes per block row in the SpMV
+constexpr int kG = 8;   // lanes per block row in the grid SpMV
+constexpr int kGc = 4;  // lanes per block row in the cluster SpMV
 // systems up to this many block rows run PCG on one thread-block cluster
 constexpr int64_t kClusterAutoRows = 24576;
 
 template <typename R>
 static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, R* xout,
                               double rtol, int max_iter, double* scal, cudaStream_t s) {
-  auto kern = k_pcg_cluster<R, kG>;
+  auto kern = k_pcg_cluster<R, kGc>;
   static thread_local bool configured = false;
   if (!configured) {
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -725,7 +727,7 @@ static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, co
 
 // largest system (block rows) the cluster PCG holds in shared memory
 template <typename R> static int64_t cluster_rows_limit() {
-  return (int64_t)kClusterMax * (kClusterSmemBudget / ((5 * 4 + 9) * (int64_t)sizeof(R)));
+  return (int64_t)kClusterMax * (kClusterSmemBudget / (kClusterVals * (int64_t)sizeof(R)));
 }
 
 template <typename R>
@@ -1095,49 +1097,128 @@ static BatchWs carve_batch(const skg_tet_mesh* m, const skg_batch* b, int precis
   w.e2 = c.take<double>(2 * ni);
   w.pcg_it = c.take<int32_t>(ni);
   w.pcg_st = c.take<int32_t>(ni);
-  w.queue = c.take<unsigned>(4);
+  w.queue = c.take<unsigned>(8);
   w.bytes = w0.bytes + c.off + 256;
   return w;
 }
 
+// Streams the batched PCG forks its size classes onto (created once per thread).
+struct ClassStreams {
+  cudaStream_t s[5] = {};
+  cudaEvent_t fork = nullptr, join[5] = {};
+  bool ready = false;
+};
+
+// All active instances' PCG solves.  Each instance gets the smallest cluster
+// (a power of two, at least min_cluster) whose CTAs hold its vectors in shared
+// memory; instances are ordered largest first, so the instances of one cluster
+// size are a contiguous range of the order and each range is one launch of the
+// queue kernel.  The launches run concurrently on their own streams, each with
+// a number of clusters proportional to the block rows of its active instances,
+// so the classes finish together; within a launch, clusters take instances
+// from the range largest first.
 template <typename R>
-static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const uint8_t* active, const double* eta,
+static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t* rows_h, const int32_t* order_h,
+                            const uint8_t* active_h, int min_cluster, int vec_kb, const uint8_t* active,
+                            const double* eta,
                             const double* b, const uint8_t* pinned, R* xout, int max_iter, int32_t* it_out,
-                            int32_t* st_out, unsigned* queue, cudaStream_t s) {
-  auto kern = k_pcg_cluster_queue<R, kG>;
+                            int32_t* st_out, unsigned* queue, cudaStream_t s, int* launches) {
+  auto kern = k_pcg_cluster_queue<R, kGc>;
   static thread_local bool configured = false;
+  static thread_local ClassStreams cs;
   if (!configured) {
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
     configured = true;
   }
-  // smallest cluster whose shared memory holds the largest instance's vectors
-  int csize = 2;
-  while (csize < kClusterMax && cluster_vec_bytes(bt->max_rows, csize, (int)sizeof(R)) > kClusterSmemBudget) csize *= 2;
-  if (cluster_vec_bytes(bt->max_rows, csize, (int)sizeof(R)) > kClusterSmemBudget)
-    return fail(SKG_ERR_CAPACITY, "batched PCG: an instance of %d block rows exceeds one cluster", bt->max_rows);
-  if (csize < 4) csize = 4;
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = csize;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(kClusterThreads, 1, 1);
-  cfg.dynamicSmemBytes = kClusterSmemBudget;
-  cfg.stream = s;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  cfg.gridDim = dim3(csize, 1, 1);
-  int nclusters = 0;
-  SKG_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
-  if (nclusters < 1) return fail(SKG_ERR_CUDA, "batched PCG: no cluster fits");
-  if (nclusters > bt->n_inst) nclusters = bt->n_inst;
-  cfg.gridDim = dim3(csize * nclusters, 1, 1);
-  SKG_CUDA(cudaMemsetAsync(queue, 0, sizeof(unsigned), s));
-  Bsr<R> a2 = A;
-  SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, bt->inst_rows, bt->order, (int)bt->n_inst, active, eta, b, -1.0, pinned,
-                              xout, max_iter, it_out, st_out, queue, (int)kClusterSmemBudget));
+  if (!cs.ready) {
+    for (int c = 0; c < 5; ++c) {
+      SKG_CUDA(cudaStreamCreateWithFlags(&cs.s[c], cudaStreamNonBlocking));
+      SKG_CUDA(cudaEventCreateWithFlags(&cs.join[c], cudaEventDisableTiming));
+    }
+    SKG_CUDA(cudaEventCreateWithFlags(&cs.fork, cudaEventDisableTiming));
+    cs.ready = true;
+  }
+  const int ni = bt->n_inst;
+  if (min_cluster <= 0) min_cluster = kClusterMinDefault;
+  int cmin = 1;
+  while (cmin < min_cluster && cmin < kClusterMax) cmin *= 2;
+  // smallest cluster of at least cmin CTAs whose per-CTA vectors take at most `target`
+  // bytes (the rest holds block records), else the smallest that holds the vectors at all
+  const int64_t target = vec_kb > 0 ? (int64_t)vec_kb * 1024 : (int64_t)kClusterVecTarget;
+  auto need = [&](int inst) {
+    const int64_t rows = rows_h[inst + 1] - rows_h[inst];
+    int c = cmin;
+    while (c < kClusterMax && cluster_vec_bytes(rows, c, (int)sizeof(R)) > target) c *= 2;
+    if (cluster_vec_bytes(rows, c, (int)sizeof(R)) > target) {
+      c = cmin;
+      while (c < kClusterMax && cluster_vec_bytes(rows, c, (int)sizeof(R)) > kClusterSmemBudget) c *= 2;
+    }
+    return c;
+  };
+  // class ranges along the order, with their active block rows
+  int cls_begin[5], cls_end[5], cls_size[5];
+  double cls_rows[5];
+  int ncls = 0;
+  double total_rows = 0.0;
+  // the cluster size never grows along the order (a smaller instance fits wherever a larger
+  // one does), so the classes are at most five contiguous ranges
+  std::vector<int> csz(ni);
+  for (int k = 0; k < ni; ++k) csz[k] = k == 0 ? need(order_h[0]) : std::min(need(order_h[k]), csz[k - 1]);
+  for (int k = 0; k < ni;) {
+    const int c = csz[k];
+    int e = k;
+    double w = 0.0;
+    while (e < ni && csz[e] == c) {
+      const int inst = order_h[e];
+      if (active_h[inst]) w += rows_h[inst + 1] - rows_h[inst];
+      ++e;
+    }
+    if (ncls == 5) return fail(SKG_ERR_ARG, "batched PCG: more than five cluster sizes");
+    cls_begin[ncls] = k;
+    cls_end[ncls] = e;
+    cls_size[ncls] = c;
+    cls_rows[ncls] = w;
+    total_rows += w;
+    ++ncls;
+    k = e;
+  }
+  if (total_rows <= 0.0) return SKG_OK;
+  SKG_CUDA(cudaMemsetAsync(queue, 0, 8 * sizeof(unsigned), s));
+  SKG_CUDA(cudaEventRecord(cs.fork, s));
+  const int sms = num_sms();
+  for (int c = 0; c < ncls; ++c) {
+    if (cls_rows[c] <= 0.0) continue;
+    const int csize = cls_size[c];
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = kClusterSmemBudget;
+    cfg.stream = cs.s[c];
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(csize, 1, 1);
+    int fit = 0;
+    SKG_CUDA(cudaOccupancyMaxActiveClusters(&fit, kern, &cfg));
+    if (fit < 1) return fail(SKG_ERR_CUDA, "batched PCG: no cluster of %d CTAs fits", csize);
+    int nclusters = (int)(sms * cls_rows[c] / total_rows / csize + 0.5);
+    if (nclusters < 1) nclusters = 1;
+    if (nclusters > fit) nclusters = fit;
+    if (nclusters > cls_end[c] - cls_begin[c]) nclusters = cls_end[c] - cls_begin[c];
+    cfg.gridDim = dim3(csize * nclusters, 1, 1);
+    SKG_CUDA(cudaStreamWaitEvent(cs.s[c], cs.fork, 0));
+    Bsr<R> a2 = A;
+    SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, bt->inst_rows, bt->order + cls_begin[c],
+                                cls_end[c] - cls_begin[c], active, eta, b, -1.0, pinned, xout, max_iter, it_out,
+                                st_out, queue + c, (int)kClusterSmemBudget));
+    SKG_CUDA(cudaEventRecord(cs.join[c], cs.s[c]));
+    SKG_CUDA(cudaStreamWaitEvent(s, cs.join[c], 0));
+    ++*launches;
+  }
   return SKG_OK;
 }
 
@@ -1170,6 +1251,10 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     infos[i].min_alpha = 1.0;
   }
 
+  // instance offsets and order on the host (the size classes of the PCG launch)
+  std::vector<int32_t> rows_h(ni + 1), order_h(ni);
+  SKG_CUDA(cudaMemcpyAsync(rows_h.data(), bt->inst_rows, (ni + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaMemcpyAsync(order_h.data(), bt->order, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
   k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, w.ut, st->u);
   SKG_LAUNCHED();
@@ -1307,10 +1392,11 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     total->t_assemble_ms += pt.end();
     // all active instances' PCG solves, one cluster per instance at a time
     pt.begin();
-    SKG_TRY(launch_pcg_queue<R>(A, bt, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it,
-                                bw.pcg_st, bw.queue, s));
+    SKG_TRY(launch_pcg_queue<R>(A, bt, rows_h.data(), order_h.data(), active.data(), prm->batch_min_cluster,
+                                prm->batch_vec_kb, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it, bw.pcg_st,
+                                bw.queue, s, &launches));
     total->t_pcg_ms += pt.end();
-    launches += 3;
+    launches += 2;
     SKG_CUDA(cudaMemcpyAsync(pit.data(), bw.pcg_it, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     SKG_CUDA(cudaMemcpyAsync(pst.data(), bw.pcg_st, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     k_inst_dot<R><<<ni, kBlock, 0, s>>>(w.g, dx, bt->inst_rows, bw.active, bw.slope);
