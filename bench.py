@@ -199,6 +199,69 @@ def run_reference(args):
     return 0
 
 
+def train_warm_start(args):
+    """The warm-start MLP trained on frames the plain batched solver generates on a separate
+    seeded batch of beams (tensor-core forward/backward, Adam).  Returns (net, info)."""
+    import torch
+    from simkit_gb300 import warmstart as ws
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    t0 = time.perf_counter()
+    train_specs = beam_batch(args.instances, seed=100)
+    tb = BatchedBESolver(train_specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
+    frames, _ = ws.generate_frames(tb, train_specs, args.train_steps)
+    t_gen = time.perf_counter() - t0
+    net = ws.WarmStartMLP(seed=0, lr=1e-3)
+    t0 = time.perf_counter()
+    losses = ws.train(net, tb, frames, epochs=args.epochs, batch_frames=64)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del frames, tb
+    per_epoch = max(1, len(losses) // max(args.epochs, 1))
+    return net, {"frames": args.instances * args.train_steps, "generate_s": t_gen, "train_s": t_train,
+                 "adam_steps": len(losses), "loss_first_epoch": float(np.mean(losses[:per_epoch])),
+                 "loss_last_epoch": float(np.mean(losses[-per_epoch:]))}
+
+
+def run_serving(args):
+    """A Poisson stream of beam requests (the 512-beam workload's distribution, 10 steps each)
+    served by continuous batching at cohort granularity for ``--duration`` seconds; latency per
+    request = completion of its 10th step - arrival.  Metric unit: instance-steps/s."""
+    import torch
+    from simkit_gb300.serving import BeamServer, request_stream
+    torch.cuda.set_device(0)
+    net, learned = (None, None)
+    if args.learned:
+        net, learned = train_warm_start(args)
+    reqs = request_stream(args.rate, args.duration, steps=10, seed=0)
+    srv = BeamServer(max_cohort=args.max_cohort, max_live=args.max_live, net=net, precision=args.precision,
+                     pcg_rtol=args.pcg_rtol)
+    # the shape catalog (every nx, ny in 4..16, nz in 8..48) is built before traffic starts
+    catalog = [(a, b, c) for a in range(4, 17) for b in range(4, 17) for c in range(8, 49)]
+    srv.prewarm(catalog)
+    clocks = ClockSampler(0)
+    clocks.start()
+    st = srv.run(reqs, args.duration)
+    clock_info = clocks.stop()
+    sm = st.summary()
+    line = {
+        "metric": METRIC, "value": sm["instance_steps_per_s"], "unit": "instance-steps/s", "n_gpus": 1,
+        "steps": sm["rounds"], "warmup": 0, "ms_per_step": 1e3 * st.elapsed_s / max(sm["rounds"], 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": f"serving: Poisson {args.rate:g} requests/s for {args.duration:g} s, each a beam "
+                               "(nx, ny in 4..16, nz in 8..48) asking for 10 backward-Euler steps"
+                               + (", learned warm start" if args.learned else ", plain Newton"),
+                   "rate": args.rate, "duration_s": args.duration, "max_cohort": args.max_cohort,
+                   "max_live": args.max_live, "precision": args.precision},
+        "serving": sm, "learned": learned, "clocks": clock_info,
+        "catalog": {"shapes": len(srv.cache.shapes), "build_s": srv.prewarm_s,
+                    "device_bytes": srv.cache.bytes},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_batched(args):
     """512 seeded beams (nx, ny in {4..16}, nz in {8..48}, own E, nu, gravity direction),
     all stepped together; compared with stepping a sample of the same beams one at a
@@ -221,21 +284,7 @@ def run_batched(args):
     fb = None
     if args.learned:
         from simkit_gb300 import warmstart as ws
-        t0 = time.perf_counter()
-        train_specs = beam_batch(args.instances, seed=100)
-        tb = BatchedBESolver(train_specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
-        frames, _ = ws.generate_frames(tb, train_specs, args.train_steps)
-        t_gen = time.perf_counter() - t0
-        net = ws.WarmStartMLP(seed=0, lr=1e-3)
-        t0 = time.perf_counter()
-        losses = ws.train(net, tb, frames, epochs=args.epochs, batch_frames=64)
-        torch.cuda.synchronize()
-        t_train = time.perf_counter() - t0
-        del frames, tb
-        per_epoch = max(1, len(losses) // max(args.epochs, 1))
-        learned = {"frames": args.instances * args.train_steps, "generate_s": t_gen, "train_s": t_train,
-                   "adam_steps": len(losses), "loss_first_epoch": float(np.mean(losses[:per_epoch])),
-                   "loss_last_epoch": float(np.mean(losses[-per_epoch:]))}
+        net, learned = train_warm_start(args)
         fb = ws.FeatureBuilder(b, specs)
         # the warm-up steps above ran without the network: rebuild the last correction
         st = b.state()
@@ -334,7 +383,11 @@ def main():
                     help="Newton iterations per step used to scale the CPU reference sample")
     ap.add_argument("--small", action="store_true", help="use the 8x8x32 beam (quick check)")
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
-    ap.add_argument("--workload", default="single", choices=["single", "batched"])
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "serving"])
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: requests per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of traffic")
+    ap.add_argument("--max-cohort", type=int, default=512)
+    ap.add_argument("--max-live", type=int, default=2048)
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--learned", action="store_true", help="batched + learned warm start")
@@ -343,6 +396,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
     if args.workload == "batched":
         return run_batched(args)
 

@@ -56,10 +56,33 @@ class BatchedBESolver:
             pins.append(p)
             rows.append(rows[-1] + X.shape[0])
             tets.append(tets[-1] + T.shape[0])
-        self.inst_rows_host = np.array(rows, np.int32)
-        self.inst_tets_host = np.array(tets, np.int32)
-        self.mesh = TetMesh(np.concatenate(Xs), np.concatenate(Ts), np.concatenate(mus), np.concatenate(lams),
-                            device=device)
+        mesh = TetMesh(np.concatenate(Xs), np.concatenate(Ts), np.concatenate(mus), np.concatenate(lams),
+                       device=device)
+        up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
+        self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
+                    up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
+                    pcg_max_iter, do_line_search, ls_threshold, profile)
+
+    @classmethod
+    def from_device(cls, mesh, inst_rows, inst_tets, mass, f_ext, pinned, dt=1.0 / 60.0, tol=1e-6, max_newton=20,
+                    precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, do_line_search=True, ls_threshold=None,
+                    profile=False):
+        """A batch over an already concatenated device mesh: ``inst_rows`` / ``inst_tets`` (host
+        int arrays, n_inst + 1) delimit the instances; mass (n), f_ext (3n) f64 and pinned (3n) u8
+        are device tensors."""
+        self = cls.__new__(cls)
+        self.n_inst = len(inst_rows) - 1
+        if self.n_inst <= 0:
+            raise ValueError("empty batch")
+        self._setup(mesh, np.asarray(inst_rows, np.int32), np.asarray(inst_tets, np.int32), mass, f_ext, pinned,
+                    dt, tol, max_newton, precision, pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile)
+        return self
+
+    def _setup(self, mesh, inst_rows_host, inst_tets_host, mass, f_ext, pinned, dt, tol, max_newton, precision,
+               pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile):
+        self.inst_rows_host = inst_rows_host
+        self.inst_tets_host = inst_tets_host
+        self.mesh = mesh
         m = self.mesh
         dev = m.device
         sizes = np.diff(self.inst_rows_host)
@@ -73,9 +96,9 @@ class BatchedBESolver:
                             inst_tets=self.inst_tets.data_ptr(), vert_inst=self.vert_inst.data_ptr(),
                             tet_inst=self.tet_inst.data_ptr(), order=self.order.data_ptr())
         self.precision = PRECISIONS[precision]
-        self.mass = up(np.concatenate(masses))
-        self.f_ext = up(np.concatenate(fexts))
-        self.pinned = up(np.concatenate(pins))
+        self.mass = mass
+        self.f_ext = f_ext
+        self.pinned = pinned
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
         self.u_curr = torch.zeros_like(self.u_prev)
         self.u_next = torch.zeros_like(self.u_prev)

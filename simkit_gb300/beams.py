@@ -64,6 +64,47 @@ def beam_mesh(nx: int, ny: int, nz: int, cell: float = 0.025):
     return X, tets.reshape(-1, 4)
 
 
+def beam_meshes(dims, cell: float = 0.025):
+    """Rest positions and tets of several Kuhn-split beams, concatenated.
+
+    ``dims`` is a sequence of (nx, ny, nz).  Returns (X, T, v_off, t_off): beam s
+    owns vertices [v_off[s], v_off[s+1]) and tets [t_off[s], t_off[s+1]), and
+    its slices equal ``beam_mesh(*dims[s], cell)`` with tets offset by v_off[s].
+    All shapes are generated together with integer array arithmetic.
+    """
+    d = np.asarray(dims, dtype=np.int64).reshape(-1, 3)
+    S = d.shape[0]
+    nx, ny, nz = d[:, 0], d[:, 1], d[:, 2]
+    nv = (nx + 1) * (ny + 1) * (nz + 1)
+    nc = nx * ny * nz
+    v_off = np.concatenate([[0], np.cumsum(nv)])
+    c_off = np.concatenate([[0], np.cumsum(nc)])
+    sv = np.repeat(np.arange(S), nv)
+    lv = np.arange(v_off[-1]) - v_off[sv]
+    NY, NZ = ny[sv] + 1, nz[sv] + 1
+    X = np.stack([lv // (NY * NZ), (lv // NZ) % NY, lv % NZ], axis=-1).astype(np.float64) * cell
+    sc = np.repeat(np.arange(S), nc)
+    lc = np.arange(c_off[-1]) - c_off[sc]
+    cy, cz = ny[sc], nz[sc]
+    ci, cj, ck = lc // (cy * cz), (lc // cz) % cy, lc % cz
+    VY, VZ, base = cy + 1, cz + 1, v_off[sc]
+
+    def vid(i, j, k):
+        return (i * VY + j) * VZ + k + base
+
+    T = np.empty((lc.size, 6, 4), dtype=np.int64)
+    for p_idx, p in enumerate(_PERMS):
+        step = np.zeros(3, dtype=np.int64)
+        corners = [vid(ci, cj, ck)]
+        for ax in p:
+            step[ax] += 1
+            corners.append(vid(ci + step[0], cj + step[1], ck + step[2]))
+        if _perm_sign(p) < 0:
+            corners[1], corners[2] = corners[2], corners[1]
+        T[:, p_idx, :] = np.stack(corners, axis=-1)
+    return X, T.reshape(-1, 4), v_off, 6 * c_off
+
+
 @dataclass
 class BeamSpec:
     """One beam instance: rest mesh, material, loading and pins (FP64 host arrays)."""

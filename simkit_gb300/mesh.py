@@ -28,6 +28,55 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+# code of the per-tet block (a, b) in the assembly gather maps: 0..3 diagonal (a, a),
+# 4..9 off-diagonal a < b, 10..15 the transpose of (b, a) for a > b
+def _block_codes():
+    off = lambda a, b: (b - 1) if a == 0 else ((b + 1) if a == 1 else 5)
+    return [a if a == b else (4 + off(a, b) if a < b else 10 + off(b, a)) for a in range(4) for b in range(4)]
+
+
+def device_pattern(tets: torch.Tensor, n: int):
+    """Block pattern and gather maps of a tet mesh built with sorts on the tets' device.
+
+    Same output as ``skg_pattern_build`` (block rows = vertices, columns sorted
+    ascending; per slot the per-tet blocks in tet order; vertex -> tet*4+corner
+    in tet order) for meshes without isolated vertices: one stable sort of the
+    16 t (row, column) keys and one of the 4 t vertex keys.  Returns
+    (rowptr, col, diag, row, hc_ptr, hc_src, v2t_ptr, v2t) as int32 tensors.
+    """
+    dev = tets.device
+    t = tets.shape[0]
+    a = tets.reshape(t, 4).long()
+    vcount = torch.bincount(a.reshape(-1), minlength=n)
+    if vcount.numel() != n or bool((vcount == 0).any()):
+        raise ValueError("device pattern: every vertex must belong to a tet")
+    rows = a[:, :, None].expand(t, 4, 4).reshape(-1)
+    cols = a[:, None, :].expand(t, 4, 4).reshape(-1)
+    codes = torch.tensor(_block_codes(), dtype=torch.long, device=dev)
+    src = (16 * torch.arange(t, device=dev)[:, None] + codes[None, :]).reshape(-1)
+    skey, perm = torch.sort(rows * n + cols, stable=True)
+    hc_src = src[perm].int()
+    new = torch.ones_like(skey, dtype=torch.bool)
+    new[1:] = skey[1:] != skey[:-1]
+    starts = torch.nonzero(new).reshape(-1)
+    ukey = skey[starts]
+    row = (ukey // n)
+    col = (ukey % n)
+    nb = int(starts.numel())
+    hc_ptr = torch.cat([starts, torch.tensor([16 * t], device=dev)]).int()
+    rowptr = torch.zeros(n + 1, dtype=torch.long, device=dev)
+    rowptr[1:] = torch.cumsum(torch.bincount(row, minlength=n), 0)
+    slots = torch.arange(nb, device=dev)
+    diag = torch.empty(n, dtype=torch.long, device=dev)
+    on = row == col
+    diag[row[on]] = slots[on]
+    vkey, vperm = torch.sort(a.reshape(-1), stable=True)
+    v2t = vperm.int()
+    v2t_ptr = torch.zeros(n + 1, dtype=torch.long, device=dev)
+    v2t_ptr[1:] = torch.cumsum(vcount, 0)
+    return (rowptr.int(), col.int(), diag.int(), row.int(), hc_ptr, hc_src, v2t_ptr.int(), v2t)
+
+
 class TetMesh:
     """Rest mesh of n vertices and t tets on one GPU.
 
@@ -35,6 +84,38 @@ class TetMesh:
     ----------
     X : (n, 3) rest positions;  T : (t, 4) tets;  mu, lam : (t,) or (t, 1).
     """
+
+    @classmethod
+    def from_device(cls, X, tets, dinv, vol, mu, lam, pattern):
+        """A mesh from device tensors: X (3n) f64, tets (t, 4) i32, dinv (9t) f64, vol (t) f64,
+        mu, lam (t) f64 and ``pattern`` = (rowptr, col, diag, row, hc_ptr, hc_src, v2t_ptr, v2t)
+        as produced by ``device_pattern`` (or the same maps concatenated with offsets)."""
+        self = cls.__new__(cls)
+        self.device = X.device
+        self.n = X.numel() // 3
+        self.t = tets.shape[0]
+        self.X_host = None
+        self.T_host = None
+        self.X, self.tets, self.dinv, self.vol = X, tets, dinv, vol
+        self.mu, self.lam = mu.contiguous(), lam.contiguous()
+        self.dinv32 = dinv.float()
+        self.mat32 = torch.stack([vol, self.mu, self.lam]).float().contiguous()
+        (self.rowptr, self.col, self.diag, self.row, self.hc_ptr, self.hc_src, self.v2t_ptr, self.v2t) = pattern
+        self.nb = int(self.col.numel())
+        self.rowptr_host = None
+        self.col_host = None
+        self._set_c()
+        self._scalar_perm = None
+        return self
+
+    def _set_c(self):
+        self.c = TetMeshC(
+            n_verts=self.n, n_tets=self.t, n_blocks=self.nb,
+            tets=self.tets.data_ptr(), dinv=self.dinv.data_ptr(), dinv32=self.dinv32.data_ptr(),
+            vol=self.vol.data_ptr(), mu=self.mu.data_ptr(), lam=self.lam.data_ptr(), mat32=self.mat32.data_ptr(),
+            bsr_rowptr=self.rowptr.data_ptr(), bsr_col=self.col.data_ptr(), bsr_diag=self.diag.data_ptr(),
+            bsr_row=self.row.data_ptr(), hc_ptr=self.hc_ptr.data_ptr(), hc_src=self.hc_src.data_ptr(),
+            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr())
 
     def __init__(self, X, T, mu, lam, device="cuda"):
         lib = _lib.load()
@@ -83,13 +164,7 @@ class TetMesh:
         up = lambda x: torch.from_numpy(x).to(dev)
         self.rowptr, self.col, self.diag, self.row = up(rowptr), up(col), up(diag), up(row)
         self.hc_ptr, self.hc_src, self.v2t_ptr, self.v2t = up(hc_ptr), up(hc_src), up(v2t_ptr), up(v2t)
-        self.c = TetMeshC(
-            n_verts=n, n_tets=t, n_blocks=nb,
-            tets=self.tets.data_ptr(), dinv=self.dinv.data_ptr(), dinv32=self.dinv32.data_ptr(),
-            vol=self.vol.data_ptr(), mu=self.mu.data_ptr(), lam=self.lam.data_ptr(), mat32=self.mat32.data_ptr(),
-            bsr_rowptr=self.rowptr.data_ptr(), bsr_col=self.col.data_ptr(), bsr_diag=self.diag.data_ptr(),
-            bsr_row=self.row.data_ptr(), hc_ptr=self.hc_ptr.data_ptr(), hc_src=self.hc_src.data_ptr(),
-            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr())
+        self._set_c()
         self._scalar_perm = None
 
     # ----------------------------------------------------------------- utils
@@ -117,6 +192,9 @@ class TetMesh:
         """(indptr, indices, perm): scalar CSR pattern of the block matrix and the
         permutation taking block values (entry-major layout) to CSR data order."""
         if self._scalar_perm is None:
+            if self.rowptr_host is None:
+                self.rowptr_host = self.rowptr.cpu().numpy()
+                self.col_host = self.col.cpu().numpy()
             rp = self.rowptr_host.astype(np.int64)
             col = self.col_host.astype(np.int64)
             n = self.n

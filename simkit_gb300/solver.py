@@ -45,13 +45,20 @@ class StepInfo:
         return self.status == 0
 
 
+def tet_volumes_host(X, T) -> np.ndarray:
+    """Signed tet volumes (X1-X0) . ((X2-X0) x (X3-X0)) / 6 (simkit/volume.py:14-41)."""
+    a, b, c = (X[T[:, k]] - X[T[:, 0]] for k in (1, 2, 3))
+    det = (a[:, 0] * (b[:, 1] * c[:, 2] - b[:, 2] * c[:, 1]) - a[:, 1] * (b[:, 0] * c[:, 2] - b[:, 2] * c[:, 0])
+           + a[:, 2] * (b[:, 0] * c[:, 1] - b[:, 1] * c[:, 0]))
+    return det / 6.0
+
+
 def lumped_mass(X, T, rho) -> np.ndarray:
-    """sum over incident tets of rho vol / 4 (simkit/massmatrix.py:40-50)."""
-    e = X[T[:, 1:]] - X[T[:, [0]]]
-    vol = np.linalg.det(e) / 6.0
-    m = np.zeros(X.shape[0])
-    np.add.at(m, T.ravel(), np.repeat(np.asarray(rho, dtype=np.float64) * vol / 4.0, 4))
-    return m
+    """sum over incident tets of rho vol / 4 (simkit/massmatrix.py:40-50), in tet order."""
+    T = np.asarray(T)
+    vol = tet_volumes_host(np.asarray(X, dtype=np.float64), T)
+    w = np.repeat(np.asarray(rho, dtype=np.float64) * vol / 4.0, 4)
+    return np.bincount(T.ravel(), weights=w, minlength=X.shape[0])
 
 
 class BESolver:
