@@ -186,6 +186,10 @@ typedef struct skg_be_params {
   int32_t batch_vec_kb;     /* batched PCG: the cluster size is the smallest whose per-CTA vectors
                                take at most this many KiB of shared memory, leaving the rest for
                                block records (0 = 170); if none does, the smallest that fits */
+  int32_t integrator;       /* 0 backward Euler (simkit/integrators/backward_euler.py:27-91);
+                               1 BDF2 (simkit/integrators/bdf2.py:31-101): target from four
+                               displacement levels (simkit/energies/kinetic.py:93-101) and
+                               kinetic factor 9/4; needs u_prev2 and u_prev3 */
 } skg_be_params;
 
 typedef struct skg_be_state {
@@ -199,6 +203,8 @@ typedef struct skg_be_state {
                                instance only if the incremental potential there is below its
                                value at x_tilde; the relative residual stays judged against
                                ||g(x_tilde)|| */
+  const double* u_prev2;    /* (3n) displacement at step k-2 (BDF2 only) */
+  const double* u_prev3;    /* (3n) displacement at step k-3 (BDF2 only) */
 } skg_be_state;
 
 typedef struct skg_step_info {

@@ -1,4 +1,4 @@
-"""Backward-Euler rollout of a pinned beam, as simkit would run it.
+"""Backward-Euler (or BDF2) rollout of a pinned beam, as simkit would run it.
 
 The step is simkit's own composition (``simkit/integrators/backward_euler.py:76-91``
 around ``simkit/solvers/newton.py:46-69``): energy, gradient and Hessian
@@ -14,6 +14,10 @@ well defined:
 2. Relative-residual stop.  ``newton_solver(..., max_iter=1)`` is called
    repeatedly (each call is one reference Newton iteration) until
    ``||g_free(y)|| / ||g_free(y_tilde)|| < tol`` or ``max_newton`` calls.
+
+BDF2 (``simkit/integrators/bdf2.py:31-101``) differs only in the inertial
+target (``kinetic.py:93-101``, from four position levels) and the factor
+c = 9/4 on the kinetic term; from rest every history level is the rest shape.
 """
 
 from __future__ import annotations
@@ -24,7 +28,7 @@ import numpy as np
 import scipy.sparse as sps
 
 from . import fem, snh
-from .solvers import newton_solver, be_target
+from .solvers import BDF2_COEFF, bdf2_target, newton_solver, be_target
 
 
 @dataclass
@@ -78,24 +82,37 @@ class BeamRollout:
     def potential_hessian(self, x):
         return snh.hessian_x(x, self.J, self.mu, self.lam, self.vol)
 
-    def step(self, x_curr, x_prev, newton=newton_solver):
-        """One backward-Euler step; returns (x_next (3n,1), StepInfo)."""
+    # inertial targets (overridable to plug in another implementation of the same formulas)
+    def be_target(self, yc, yp, h):
+        return be_target(yc, yp, h)
+
+    def bdf2_target(self, yc, yp, yp2, yp3, h):
+        return bdf2_target(yc, yp, yp2, yp3, h)
+
+    def step(self, x_curr, x_prev, newton=newton_solver, x_prev2=None, x_prev3=None):
+        """One backward-Euler step, or a BDF2 step when x_prev2 and x_prev3 are given;
+        returns (x_next (3n,1), StepInfo)."""
         h = self.dt
         yc = x_curr[self.free]
         yp = x_prev[self.free]
-        y_tilde = be_target(yc, yp, h)
+        if x_prev2 is None:
+            y_tilde = self.be_target(yc, yp, h)
+            c = 1.0
+        else:
+            y_tilde = self.bdf2_target(yc, yp, x_prev2[self.free], x_prev3[self.free], h)
+            c = BDF2_COEFF
         Mf = self.Mf
 
         def E(y):
             d = y - y_tilde
-            return self.potential(self.full(y)) + float((0.5 * (d.T @ (Mf @ d)) / h ** 2).item())
+            return self.potential(self.full(y)) + float((0.5 * c * (d.T @ (Mf @ d)) / h ** 2).item())
 
         def G(y):
-            return self.S @ self.potential_gradient(self.full(y)) + (Mf @ (y - y_tilde)) / h ** 2
+            return self.S @ self.potential_gradient(self.full(y)) + c * (Mf @ (y - y_tilde)) / h ** 2
 
         def H(y):
             K = self.potential_hessian(self.full(y))
-            return (self.S @ K @ self.S.T + Mf / h ** 2).tocsc()
+            return (self.S @ K @ self.S.T + c * Mf / h ** 2).tocsc()
 
         y = y_tilde.copy()
         g0 = float(np.linalg.norm(G(y)))
@@ -113,17 +130,23 @@ class BeamRollout:
     def elastic_energy(self, x) -> float:
         return snh.energy_x(x, self.J, self.mu, self.lam, self.vol)
 
-    def rollout(self, steps, record=None):
-        """Run ``steps`` steps from rest; returns positions (steps+1, 3n) and per-step infos."""
+    def rollout(self, steps, record=None, integrator="be"):
+        """Run ``steps`` steps from rest ('be' or 'bdf2'); returns positions (steps+1, 3n) and
+        per-step infos."""
+        x_prev3 = self.x_rest.copy()
+        x_prev2 = self.x_rest.copy()
         x_prev = self.x_rest.copy()
         x_curr = self.x_rest.copy()
         xs = [x_curr.ravel().copy()]
         infos = []
         for s in range(steps):
-            x_next, info = self.step(x_curr, x_prev)
+            if integrator == "bdf2":
+                x_next, info = self.step(x_curr, x_prev, x_prev2=x_prev2, x_prev3=x_prev3)
+            else:
+                x_next, info = self.step(x_curr, x_prev)
             infos.append(info)
             xs.append(x_next.ravel().copy())
-            x_prev, x_curr = x_curr, x_next
+            x_prev3, x_prev2, x_prev, x_curr = x_prev2, x_prev, x_curr, x_next
             if record is not None:
                 record(s, x_next, info)
         return np.array(xs), infos

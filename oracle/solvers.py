@@ -91,3 +91,49 @@ def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, 
     x0 = be_target(x_curr, x_prev, h)
     return newton_solver(x0, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
                          do_line_search=do_line_search, return_info=return_info)
+
+
+# BDF2: simkit/integrators/bdf2.py:31-101, simkit/energies/kinetic.py:63-101, 200-279
+BDF2_COEFF = 9.0 / 4.0   # kinetic.py:35
+
+
+def velocity_bdf2(x_curr, x_prev, x_prev2, h):
+    """(3 x_curr - 4 x_prev + x_prev2) / (2h).  Reference: ``kinetic.py:63-84``."""
+    return (3.0 * x_curr - 4.0 * x_prev + x_prev2) / (2.0 * h)
+
+
+def bdf2_target(x_curr, x_prev, x_prev2, x_prev3, h):
+    """(4/3) x_curr - (1/3) x_prev + (8h/9) v_curr - (2h/9) v_prev.  Reference: ``kinetic.py:93-101``."""
+    v_curr = velocity_bdf2(x_curr, x_prev, x_prev2, h)
+    v_prev = velocity_bdf2(x_prev, x_prev2, x_prev3, h)
+    return (4.0 / 3.0) * x_curr - (1.0 / 3.0) * x_prev + (8.0 * h / 9.0) * v_curr - (2.0 * h / 9.0) * v_prev
+
+
+def kinetic_energy_bdf2(x, x_curr, x_prev, x_prev2, x_prev3, M, h):
+    d = x - bdf2_target(x_curr, x_prev, x_prev2, x_prev3, h)
+    return float((0.5 * BDF2_COEFF * (d.T @ (M @ d)) / h ** 2).item())
+
+
+def kinetic_gradient_bdf2(x, x_curr, x_prev, x_prev2, x_prev3, M, h):
+    return BDF2_COEFF * (M @ (x - bdf2_target(x_curr, x_prev, x_prev2, x_prev3, h))) / h ** 2
+
+
+def kinetic_hessian_bdf2(M, h):
+    return BDF2_COEFF * M / h ** 2
+
+
+def bdf2(x_curr, x_prev, x_prev2, x_prev3, energy_func, gradient_func, hessian_func, M, h,
+         tolerance=1e-6, max_iter=1, do_line_search=True, return_info=False):
+    """Reference: ``simkit/integrators/bdf2.py:31-101``."""
+    def energy(x):
+        return energy_func(x) + kinetic_energy_bdf2(x, x_curr, x_prev, x_prev2, x_prev3, M, h)
+
+    def gradient(x):
+        return gradient_func(x) + kinetic_gradient_bdf2(x, x_curr, x_prev, x_prev2, x_prev3, M, h)
+
+    def hessian(x):
+        return hessian_func(x) + kinetic_hessian_bdf2(M, h)
+
+    x0 = bdf2_target(x_curr, x_prev, x_prev2, x_prev3, h)
+    return newton_solver(x0, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
+                         do_line_search=do_line_search, return_info=return_info)

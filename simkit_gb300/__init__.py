@@ -2,7 +2,7 @@
 
 A drop-in for the hot path of otmanon/simkit: the same Python signatures for
 the stable neo-Hookean energy tiers, deformation_jacobian, volume,
-psd_project, backtracking_line_search, newton_solver and backward_euler, with
+psd_project, backtracking_line_search, newton_solver, backward_euler and bdf2, with
 the arithmetic in hand-written sm_103a CUDA kernels behind a ctypes C ABI
 (include/simkit_gb300.h).  ``BESolver`` runs whole backward-Euler steps on
 the device.
@@ -15,7 +15,7 @@ _API = {
     "stable_neo_hookean_hessian_element_F", "stable_neo_hookean_energy_x", "stable_neo_hookean_gradient_x",
     "stable_neo_hookean_hessian_x", "stable_neo_hookean_energy", "stable_neo_hookean_gradient",
     "stable_neo_hookean_hessian", "psd_project", "deformation_jacobian", "volume", "backtracking_line_search",
-    "newton_solver", "backward_euler", "solve_sparse", "BlockMatrix", "DeformationJacobian",
+    "newton_solver", "backward_euler", "bdf2", "solve_sparse", "BlockMatrix", "DeformationJacobian",
 }
 
 
@@ -30,4 +30,7 @@ def __getattr__(name):
     if name == "TetMesh":
         from .mesh import TetMesh
         return TetMesh
+    if name == "BatchedBESolver":
+        from .batched import BatchedBESolver
+        return BatchedBESolver
     raise AttributeError(name)

@@ -55,13 +55,13 @@ class BEParamsC(ctypes.Structure):
         ("dt", c_dbl), ("tol", c_dbl), ("max_newton", c_i32), ("precision", c_i32), ("pcg_rtol", c_dbl),
         ("pcg_max_iter", c_i32), ("do_line_search", c_i32), ("ls_alpha", c_dbl), ("ls_beta", c_dbl),
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
-        ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32),
+        ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
     ]
 
 
 class BEStateC(ctypes.Structure):
     _fields_ = [("u", c_vp), ("u_curr", c_vp), ("u_prev", c_vp), ("mass", c_vp), ("f_ext", c_vp), ("pinned", c_vp),
-                ("u_warm", c_vp)]
+                ("u_warm", c_vp), ("u_prev2", c_vp), ("u_prev3", c_vp)]
 
 
 class StepInfoC(ctypes.Structure):

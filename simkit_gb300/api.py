@@ -403,3 +403,30 @@ def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, 
 
     return newton_solver(x_tilde, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
                          do_line_search=do_line_search, return_info=return_info)
+
+
+def bdf2(x_curr, x_prev, x_prev2, x_prev3, energy_func, gradient_func, hessian_func, M, h, tolerance: float = 1e-6,
+         max_iter: int = 1, do_line_search: bool = True, return_info: bool = False):
+    """simkit ``bdf2`` (integrators/bdf2.py:31-101): minimise V(x) + (9/4)/(2h^2) (x - x~)^T M (x - x~)
+    with the BDF2 target x~ = (4/3) x_curr - (1/3) x_prev + (8h/9) v_curr - (2h/9) v_prev, velocities
+    by the second-order backward difference (energies/kinetic.py:63-101), by ``newton_solver``."""
+    v_curr = (3.0 * x_curr - 4.0 * x_prev + x_prev2) / (2.0 * h)
+    v_prev = (3.0 * x_prev - 4.0 * x_prev2 + x_prev3) / (2.0 * h)
+    x_tilde = (4.0 / 3.0) * x_curr - (1.0 / 3.0) * x_prev + (8.0 * h / 9.0) * v_curr - (2.0 * h / 9.0) * v_prev
+    c = 9.0 / 4.0
+
+    def energy(x):
+        d = x - x_tilde
+        return energy_func(x) + float((0.5 * c * (d.T @ (M @ d)) / h ** 2).item())
+
+    def gradient(x):
+        return gradient_func(x) + c * (M @ (x - x_tilde)) / h ** 2
+
+    def hessian(x):
+        H = hessian_func(x)
+        if isinstance(H, BlockMatrix):
+            H = H.to_scipy()
+        return H + c * M / h ** 2
+
+    return newton_solver(x_tilde, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
+                         do_line_search=do_line_search, return_info=return_info)

@@ -58,6 +58,14 @@ def _key(solver):
     return f"{torch.cuda.get_device_name()}|rows<={bucket}|prec={solver.precision}"
 
 
+def _history(solver):
+    """The solver's displacement levels (current first)."""
+    levels = [solver.u_curr, solver.u_prev]
+    if getattr(solver, "integrator", "be") == "bdf2":
+        levels += [solver.u_prev2, solver.u_prev3]
+    return levels
+
+
 def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
     """Pick the fastest PCG kernel variant for ``solver``; returns (variant, timings_us)."""
     if solver.params.pcg_mode not in (1, 3) or (solver.params.pcg_mode == 3 and solver.mesh.n <= CLUSTER_ROWS):
@@ -67,19 +75,19 @@ def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
     if key in table:
         solver.params.pcg_variant = int(table[key]["variant"])
         return solver.params.pcg_variant, table[key]["us_per_iter"]
-    uc, up = solver.u_curr.clone(), solver.u_prev.clone()
+    hist = [t.clone() for t in _history(solver)]
     steps = solver.steps
     old_profile = solver.params.profile
     timings = {}
     for v in variants:
-        solver.u_curr.copy_(uc)
-        solver.u_prev.copy_(up)
+        for dst, src in zip(_history(solver), hist):
+            dst.copy_(src)
         solver.params.pcg_variant = v
         solver.params.profile = 1
         info = solver.step()
         timings[v] = 1e3 * info.t_pcg_ms / max(info.pcg_iters, 1)
-    solver.u_curr.copy_(uc)
-    solver.u_prev.copy_(up)
+    for dst, src in zip(_history(solver), hist):
+        dst.copy_(src)
     solver.steps = steps
     solver.params.profile = old_profile
     best = min(timings, key=timings.get)

@@ -21,7 +21,7 @@ import torch
 from . import _lib
 from ._lib import BatchC, BEParamsC, BEStateC, StepInfoC, check
 from .mesh import TetMesh, _stream_ptr
-from .solver import PRECISIONS, StepInfo, lumped_mass
+from .solver import INTEGRATORS, PRECISIONS, StepInfo, lumped_mass
 
 
 class BatchedBESolver:
@@ -33,7 +33,8 @@ class BatchedBESolver:
     """
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
-                 pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda"):
+                 pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
+                 integrator="be"):
         _lib.load()
         self.n_inst = len(specs)
         if self.n_inst == 0:
@@ -61,12 +62,12 @@ class BatchedBESolver:
         up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
-                    pcg_max_iter, do_line_search, ls_threshold, profile)
+                    pcg_max_iter, do_line_search, ls_threshold, profile, integrator)
 
     @classmethod
     def from_device(cls, mesh, inst_rows, inst_tets, mass, f_ext, pinned, dt=1.0 / 60.0, tol=1e-6, max_newton=20,
                     precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, do_line_search=True, ls_threshold=None,
-                    profile=False):
+                    profile=False, integrator="be"):
         """A batch over an already concatenated device mesh: ``inst_rows`` / ``inst_tets`` (host
         int arrays, n_inst + 1) delimit the instances; mass (n), f_ext (3n) f64 and pinned (3n) u8
         are device tensors."""
@@ -75,11 +76,12 @@ class BatchedBESolver:
         if self.n_inst <= 0:
             raise ValueError("empty batch")
         self._setup(mesh, np.asarray(inst_rows, np.int32), np.asarray(inst_tets, np.int32), mass, f_ext, pinned,
-                    dt, tol, max_newton, precision, pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile)
+                    dt, tol, max_newton, precision, pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile,
+                    integrator)
         return self
 
     def _setup(self, mesh, inst_rows_host, inst_tets_host, mass, f_ext, pinned, dt, tol, max_newton, precision,
-               pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile):
+               pcg_rtol, pcg_max_iter, do_line_search, ls_threshold, profile, integrator="be"):
         self.inst_rows_host = inst_rows_host
         self.inst_tets_host = inst_tets_host
         self.mesh = mesh
@@ -102,6 +104,11 @@ class BatchedBESolver:
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
         self.u_curr = torch.zeros_like(self.u_prev)
         self.u_next = torch.zeros_like(self.u_prev)
+        if integrator not in INTEGRATORS:
+            raise ValueError(f"integrator must be one of {sorted(INTEGRATORS)}")
+        self.integrator = integrator
+        self.u_prev2 = torch.zeros_like(self.u_prev) if integrator == "bdf2" else None
+        self.u_prev3 = torch.zeros_like(self.u_prev) if integrator == "bdf2" else None
         nbytes = _lib.load().skg_batch_workspace_size(ctypes.byref(m.c), ctypes.byref(self.batch), self.precision)
         if nbytes < 0:
             raise ValueError(_lib.last_error())
@@ -111,7 +118,7 @@ class BatchedBESolver:
             pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
             ls_max_iter=100, pcg_mode=2,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
-            profile=int(profile))
+            profile=int(profile), integrator=INTEGRATORS[integrator])
         self._infos = (StepInfoC * self.n_inst)()
         self.steps = 0
 
@@ -129,15 +136,22 @@ class BatchedBESolver:
         ``u_warm`` (3n, device FP64): optional Newton starting displacement, kept per
         instance only where its residual is below the residual at x_tilde.
         """
+        bdf2 = self.integrator == "bdf2"
         st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
                       mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
-                      u_warm=u_warm.data_ptr() if u_warm is not None else None)
+                      u_warm=u_warm.data_ptr() if u_warm is not None else None,
+                      u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
+                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None)
         total = StepInfoC()
         check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
                                               ctypes.byref(self.params), ctypes.byref(st),
                                               ctypes.c_void_p(self.workspace.data_ptr()), self._infos,
                                               ctypes.byref(total), _stream_ptr(stream)))
-        self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+        if bdf2:
+            self.u_prev3, self.u_prev2, self.u_prev, self.u_curr, self.u_next = (
+                self.u_prev2, self.u_prev, self.u_curr, self.u_next, self.u_prev3)
+        else:
+            self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
         self.steps += 1
         conv = lambda c: StepInfo(c.newton_iters, c.pcg_iters, c.ls_trials, c.status, c.residual0, c.residual,
                                   c.min_alpha, c.energy, c.launches, c.t_hessian_ms, c.t_assemble_ms, c.t_pcg_ms,
@@ -145,11 +159,14 @@ class BatchedBESolver:
         return [conv(c) for c in self._infos], conv(total)
 
     def state(self):
-        return self.u_curr.clone(), self.u_prev.clone()
+        """Clones of the displacement levels (current first; four with BDF2)."""
+        levels = [self.u_curr, self.u_prev] + ([self.u_prev2, self.u_prev3] if self.integrator == "bdf2" else [])
+        return tuple(t.clone() for t in levels)
 
     def set_state(self, st):
-        self.u_curr.copy_(st[0])
-        self.u_prev.copy_(st[1])
+        levels = [self.u_curr, self.u_prev] + ([self.u_prev2, self.u_prev3] if self.integrator == "bdf2" else [])
+        for dst, src in zip(levels, st):
+            dst.copy_(src)
 
     def displacement(self, inst=None) -> np.ndarray:
         u = self.u_curr.cpu().numpy()

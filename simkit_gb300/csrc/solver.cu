@@ -593,6 +593,43 @@ __global__ void k_be_init(const double* __restrict__ uc, const double* __restric
   u[i] = x;
 }
 
+// BDF2 target from four displacement levels, in the order of simkit/energies/kinetic.py:63-101
+// (velocities by the second-order backward difference), u = u_tilde
+__global__ void k_bdf2_init(const double* __restrict__ uc, const double* __restrict__ up,
+                            const double* __restrict__ up2, const double* __restrict__ up3, double h, int64_t m,
+                            double* __restrict__ ut, double* __restrict__ u) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double vc = (3.0 * uc[i] - 4.0 * up[i] + up2[i]) / (2.0 * h);
+  const double vp = (3.0 * up[i] - 4.0 * up2[i] + up3[i]) / (2.0 * h);
+  const double x = (4.0 / 3.0) * uc[i] - (1.0 / 3.0) * up[i] + (8.0 * h / 9.0) * vc - (2.0 * h / 9.0) * vp;
+  ut[i] = x;
+  u[i] = x;
+}
+
+static int check_integrator(const skg_be_params* prm, const skg_be_state* st) {
+  if (prm->integrator != 0 && prm->integrator != 1) return fail(SKG_ERR_ARG, "integrator must be 0 (BE) or 1 (BDF2)");
+  if (prm->integrator == 1 && (!st->u_prev2 || !st->u_prev3))
+    return fail(SKG_ERR_ARG, "BDF2 needs the displacements at steps k-2 and k-3");
+  return SKG_OK;
+}
+
+// inertial target and Newton start of the chosen integrator; returns the kinetic factor c / h^2
+static int launch_target(const skg_be_params* prm, const skg_be_state* st, int64_t nd, double* ut, cudaStream_t s,
+                         double* inv_h2) {
+  const double h = prm->dt;
+  if (prm->integrator == 1) {
+    k_bdf2_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, st->u_prev2, st->u_prev3, h, nd, ut,
+                                                   st->u);
+    *inv_h2 = (9.0 / 4.0) / (h * h);
+  } else {
+    k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, ut, st->u);
+    *inv_h2 = 1.0 / (h * h);
+  }
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
 // u += step * dx on free DOFs
 template <typename R>
 __global__ void k_apply_step(double* __restrict__ u, const R* __restrict__ dx, double step, int64_t n,
@@ -837,7 +874,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
                    skg_step_info* info, cudaStream_t s) {
   const int64_t n = m->n_verts, nd = 3 * n;
   const bool mixed = sizeof(R) == 4;
-  const double inv_h2 = 1.0 / (prm->dt * prm->dt);
+  double inv_h2 = 0.0;  // kinetic factor c / h^2, set with the target
   R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
   R* rec = mixed ? (R*)w.rec32 : (R*)w.rec64;
   R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
@@ -851,8 +888,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   info->launches = 0;
   info->t_hessian_ms = info->t_assemble_ms = info->t_pcg_ms = info->t_gradient_ms = info->t_energy_ms = 0.0;
   SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
-  k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, w.ut, st->u);
-  SKG_LAUNCHED();
+  SKG_TRY(launch_target(prm, st, nd, w.ut, s, &inv_h2));
   info->launches++;
 
   GradArgs ga{};
@@ -1229,7 +1265,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   const int64_t n = m->n_verts, nd = 3 * n;
   const int ni = bt->n_inst;
   const bool mixed = sizeof(R) == 4;
-  const double inv_h2 = 1.0 / (prm->dt * prm->dt);
+  double inv_h2 = 0.0;  // kinetic factor c / h^2, set with the target
   Workspace w = carve_workspace(m, prm->precision, wsbase);
   BatchWs bw = carve_batch(m, bt, prm->precision, wsbase);
   R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
@@ -1256,8 +1292,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   SKG_CUDA(cudaMemcpyAsync(rows_h.data(), bt->inst_rows, (ni + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   SKG_CUDA(cudaMemcpyAsync(order_h.data(), bt->order, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
-  k_be_init<<<blocks_for(nd), kBlock, 0, s>>>(st->u_curr, st->u_prev, nd, w.ut, st->u);
-  SKG_LAUNCHED();
+  SKG_TRY(launch_target(prm, st, nd, w.ut, s, &inv_h2));
   GradArgs ga{};
   ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
   ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
@@ -1489,6 +1524,7 @@ int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg
   SKG_TRY(check_mesh(mesh, params->precision));
   if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "be_step: dt must be positive");
   if (!state->u || !state->u_curr || !state->u_prev || !state->mass) return fail(SKG_ERR_ARG, "be_step: null state");
+  SKG_TRY(check_integrator(params, state));
   if (params->do_line_search && !(params->ls_alpha > 0.0 && params->ls_alpha <= 0.5))
     return fail(SKG_ERR_ARG, "line search alpha must lie in (0, 0.5]");
   if (params->do_line_search && !(params->ls_beta > 0.0 && params->ls_beta < 1.0))
@@ -1516,6 +1552,7 @@ int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const 
   if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "be_step_batched: dt must be positive");
   if (!state->u || !state->u_curr || !state->u_prev || !state->mass)
     return fail(SKG_ERR_ARG, "be_step_batched: null state");
+  SKG_TRY(check_integrator(params, state));
   cudaStream_t s = as_stream(stream);
   if (params->precision == SKG_MIXED)
     return be_step_batched<float>(mesh, batch, params, state, workspace, infos_h, total_h, s);

@@ -20,6 +20,7 @@ from ._lib import BEParamsC, BEStateC, StepInfoC, check, SKG_FP64, SKG_MIXED
 from .mesh import TetMesh, _stream_ptr
 
 PRECISIONS = {"fp64": SKG_FP64, "mixed": SKG_MIXED}
+INTEGRATORS = {"be": 0, "bdf2": 1}
 
 
 @dataclass
@@ -74,11 +75,13 @@ class BESolver:
         forcing capped at its magnitude
     pcg_mode : 0 kernel per phase, 1 grid-persistent, 2 one thread-block
         cluster, 3 choose by size (cluster up to 24,576 block rows)
+    integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
+        (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
-                 do_line_search=True, ls_threshold=None, profile=False, device="cuda"):
+                 do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         m = self.mesh
@@ -96,6 +99,11 @@ class BESolver:
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
         self.u_curr = torch.zeros_like(self.u_prev)
         self.u_next = torch.zeros_like(self.u_prev)
+        if integrator not in INTEGRATORS:
+            raise ValueError(f"integrator must be one of {sorted(INTEGRATORS)}")
+        self.integrator = integrator
+        self.u_prev2 = torch.zeros_like(self.u_prev) if integrator == "bdf2" else None
+        self.u_prev3 = torch.zeros_like(self.u_prev) if integrator == "bdf2" else None
         nbytes = _lib.load().skg_be_workspace_size(ctypes.byref(m.c), self.precision)
         if nbytes < 0:
             raise ValueError(_lib.last_error())
@@ -105,7 +113,7 @@ class BESolver:
             pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
             ls_max_iter=100, pcg_mode=pcg_mode,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
-            profile=int(profile))
+            profile=int(profile), integrator=INTEGRATORS[integrator])
         self.steps = 0
         self._host = None
 
@@ -114,14 +122,21 @@ class BESolver:
         return cls(spec.X, spec.T, spec.mu, spec.lam, rho=spec.rho, gravity=spec.gravity, pinned=spec.pinned, **kw)
 
     def step(self, stream=None) -> StepInfo:
+        bdf2 = self.integrator == "bdf2"
         st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
-                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr())
+                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
+                      u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
+                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None)
         info = StepInfoC()
         check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
                                       ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),
                                       _stream_ptr(stream)))
-        # rotate history: prev <- curr <- next
-        self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+        # rotate history: [prev3 <- prev2 <-] prev <- curr <- next
+        if bdf2:
+            self.u_prev3, self.u_prev2, self.u_prev, self.u_curr, self.u_next = (
+                self.u_prev2, self.u_prev, self.u_curr, self.u_next, self.u_prev3)
+        else:
+            self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
         self.steps += 1
         return StepInfo(info.newton_iters, info.pcg_iters, info.ls_trials, info.status, info.residual0,
                         info.residual, info.min_alpha, info.energy, info.launches, info.t_hessian_ms,
@@ -157,9 +172,18 @@ class BESolver:
     def positions(self) -> np.ndarray:
         return self.mesh.X_host.reshape(-1) + self.displacement()
 
-    def set_state(self, u_curr, u_prev):
-        self.u_curr.copy_(torch.as_tensor(np.asarray(u_curr, dtype=np.float64).reshape(-1)))
-        self.u_prev.copy_(torch.as_tensor(np.asarray(u_prev, dtype=np.float64).reshape(-1)))
+    def set_state(self, u_curr, u_prev, u_prev2=None, u_prev3=None):
+        """Displacement history (host or device arrays); the BDF2 levels k-2 and k-3 are
+        needed with integrator 'bdf2'."""
+        dev = lambda a: torch.as_tensor(np.asarray(a.cpu() if isinstance(a, torch.Tensor) else a,
+                                                   dtype=np.float64).reshape(-1))
+        self.u_curr.copy_(dev(u_curr))
+        self.u_prev.copy_(dev(u_prev))
+        if self.integrator == "bdf2":
+            if u_prev2 is None or u_prev3 is None:
+                raise ValueError("BDF2 needs the displacements at steps k-2 and k-3")
+            self.u_prev2.copy_(dev(u_prev2))
+            self.u_prev3.copy_(dev(u_prev3))
 
     def rollout(self, steps, callback=None):
         infos = []

@@ -17,6 +17,7 @@ Fixtures written next to this script:
 * ``beam_small.npz``: 4x2x2 jittered beam: J (csc), vol, mass, energy/gradient/Hessian at a perturbed x
 * ``rollout_small.npz``: 6x2x2 beam, 8 backward-Euler steps (positions, iterations, residuals)
 * ``rollout_beam_8x8x32.npz``: the 12,288-tet beam, 60 steps (displacements at a few steps, energies, iterations)
+* ``rollout_bdf2_small.npz``: 6x2x2 beam, 8 BDF2 steps from rest (the reference's BDF2 target and coefficient)
 """
 
 from __future__ import annotations
@@ -45,8 +46,9 @@ def _import_reference(path):
         from simkit.volume import volume
         from simkit.massmatrix import massmatrix
         from simkit.solvers import newton_solver
+        from simkit.energies import kinetic
     return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
-                volume=volume, massmatrix=massmatrix, newton_solver=newton_solver)
+                volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic)
 
 
 def element_cases(rng, d, t_each=32):
@@ -110,7 +112,7 @@ def make_beam_small(ref, out):
                         K_data=K.data, K_indices=K.indices, K_indptr=K.indptr)
 
 
-def _reference_rollout(ref, spec, dt, steps, keep=None):
+def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be"):
     """The oracle harness with every FEM routine and the Newton step taken from the reference."""
     import scipy.sparse as sps
     from oracle.rollout import BeamRollout
@@ -143,13 +145,25 @@ def _reference_rollout(ref, spec, dt, steps, keep=None):
         def elastic_energy(self, x):
             return s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
 
+        def be_target(self, yc, yp, h):
+            return ref["kinetic"].be_target(yc, yp, h)
+
+        def bdf2_target(self, yc, yp, yp2, yp3, h):
+            return ref["kinetic"].bdf2_target(yc, yp, yp2, yp3, h)
+
     r = RefRollout()
+    assert ref["kinetic"]._BDF2_COEFF == 9.0 / 4.0
+    x_prev3 = r.x_rest.copy()
+    x_prev2 = r.x_rest.copy()
     x_prev = r.x_rest.copy()
     x_curr = r.x_rest.copy()
     us, energies, iters, res_last = {}, [], [], []
     for k in range(steps):
-        x_next, info = r.step(x_curr, x_prev, newton=ref["newton_solver"])
-        x_prev, x_curr = x_curr, x_next
+        if integrator == "bdf2":
+            x_next, info = r.step(x_curr, x_prev, newton=ref["newton_solver"], x_prev2=x_prev2, x_prev3=x_prev3)
+        else:
+            x_next, info = r.step(x_curr, x_prev, newton=ref["newton_solver"])
+        x_prev3, x_prev2, x_prev, x_curr = x_prev2, x_prev, x_curr, x_next
         energies.append(r.elastic_energy(x_curr))
         iters.append(info.iters)
         res_last.append(info.residuals[-1])
@@ -162,6 +176,16 @@ def make_rollout_small(ref, out):
     from simkit_gb300.beams import make_beam
     spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
     us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 8)
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
+                        ym=2e5, pr=0.45, dt=1.0 / 60.0)
+
+
+def make_rollout_bdf2_small(ref, out):
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 8, integrator="bdf2")
     keys = sorted(us)
     np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
                         energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
@@ -190,6 +214,7 @@ def main():
     make_element(ref, 2, os.path.join(HERE, "element_2d.npz"))
     make_beam_small(ref, os.path.join(HERE, "beam_small.npz"))
     make_rollout_small(ref, os.path.join(HERE, "rollout_small.npz"))
+    make_rollout_bdf2_small(ref, os.path.join(HERE, "rollout_bdf2_small.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)

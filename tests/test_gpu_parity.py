@@ -152,6 +152,67 @@ def test_be_step_fp64_matches_reference_rollout(api):
         assert _rel(u, d["u"][k]) < 1e-4
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_bdf2_step_matches_reference_rollout(api, precision):
+    """BDF2 (simkit/integrators/bdf2.py) on the device against the reference's BDF2 rollout."""
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_bdf2_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    kw = dict(pcg_rtol=1e-10) if precision == "fp64" else {}
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, integrator="bdf2", **kw)
+    X = spec.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, info
+        k = list(d["steps"]).index(step)
+        u = s.displacement()
+        assert _rel(X + u, X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+
+
+def test_bdf2_batched_equals_single(api):
+    """The batched BDF2 step equals single-instance BDF2 steps of the same beams."""
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    from simkit_gb300.solver import BESolver
+    specs = beam_batch(3, seed=2, nx_range=(4, 6), ny_range=(4, 6), nz_range=(8, 12))
+    b = BatchedBESolver(specs, precision="fp64", pcg_rtol=1e-10, integrator="bdf2")
+    singles = [BESolver.from_spec(sp, precision="fp64", pcg_rtol=1e-10, integrator="bdf2") for sp in specs]
+    for _ in range(4):
+        infos, tot = b.step()
+        assert tot.status == 0
+        for i, s1 in enumerate(singles):
+            assert s1.step().converged
+            u = s1.displacement()
+            assert _rel(b.displacement(i), u) < 1e-7
+
+
+def test_drop_in_bdf2_matches_oracle(api):
+    """simkit_gb300.bdf2 with the package's energy closures against the oracle's bdf2."""
+    import scipy.sparse as sps
+    from oracle import fem, solvers as osol, snh as osnh
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(3, 2, 2, ym=3e5, pr=0.4)
+    X, T = spec.X, spec.T
+    J = fem.deformation_jacobian(X, T)
+    vol = fem.tet_volumes(X, T)
+    M = sps.diags(np.repeat(fem.lumped_mass(X, T, 1000.0), 3)).tocsc()
+    dJ = api.deformation_jacobian(X, T)
+    rng = np.random.default_rng(3)
+    h = 1 / 60
+    xs = [X.reshape(-1, 1) + 1e-3 * k * rng.standard_normal((X.size, 1)) for k in range(4)]
+    E = lambda x: api.stable_neo_hookean_energy_x(x, dJ, spec.mu, spec.lam, vol)
+    G = lambda x: api.stable_neo_hookean_gradient_x(x, dJ, spec.mu, spec.lam, vol)
+    H = lambda x: api.stable_neo_hookean_hessian_x(x, dJ, spec.mu, spec.lam, vol)
+    Eo = lambda x: osnh.energy_x(x, J, spec.mu, spec.lam, vol)
+    Go = lambda x: osnh.gradient_x(x, J, spec.mu, spec.lam, vol)
+    Ho = lambda x: osnh.hessian_x(x, J, spec.mu, spec.lam, vol)
+    got = api.bdf2(xs[3], xs[2], xs[1], xs[0], E, G, H, M, h, max_iter=3)
+    ref = osol.bdf2(xs[3], xs[2], xs[1], xs[0], Eo, Go, Ho, M, h, max_iter=3)
+    assert _rel(got, ref) < 1e-9
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_rollout_8x8x32_matches_reference(api, precision):
     """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""
