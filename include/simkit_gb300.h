@@ -72,6 +72,19 @@ int skg_snh_hessian_element_F(int dim, int precision, const double* F, const dou
                               double* H, int64_t t, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* element tier: simkit/energies/macklin_mueller_neo_hookean.py            */
+/* ---------------------------------------------------------------------- */
+/* Same arguments as the stable neo-Hookean element tier.  Replace
+ * macklin_mueller_neo_hookean_energy_element_F (:66-122), _gradient_element_F (:125-185)
+ * and _hessian_element_F (:188-443, not projected). */
+int skg_mmnh_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* psi, int64_t t, void* stream);
+int skg_mmnh_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                                double* P, int64_t t, void* stream);
+int skg_mmnh_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* H, int64_t t, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* psd_project: simkit/psd_project.py:12-47                                */
 /* ---------------------------------------------------------------------- */
 /* Batched eigenvalue floor of symmetric d x d blocks (1 <= d <= 12) by cyclic
@@ -115,6 +128,13 @@ int skg_pattern_build(const int32_t* T_h, int64_t n, int64_t t, int64_t* n_block
                       int32_t* v2t_ptr_h, int32_t* v2t_h);
 
 /* Mesh descriptor used by the assembled tier and the solver (all device pointers). */
+/* Elastic energies of the per-tet kernels (simkit/energies/elastic.py:75 dispatches the same set
+ * by name). */
+typedef enum skg_material {
+  SKG_MAT_STABLE_NEO_HOOKEAN = 0,        /* simkit/energies/stable_neo_hookean.py */
+  SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN = 1 /* simkit/energies/macklin_mueller_neo_hookean.py */
+} skg_material;
+
 typedef struct skg_tet_mesh {
   int64_t n_verts;
   int64_t n_tets;
@@ -134,6 +154,7 @@ typedef struct skg_tet_mesh {
   const int32_t* hc_src;     /* (16t) */
   const int32_t* v2t_ptr;    /* (n+1) */
   const int32_t* v2t;        /* (4t) */
+  int32_t material;          /* skg_material: the elastic energy of every tet */
 } skg_tet_mesh;
 
 /* Assembled block matrix (3x3 blocks).  Values of block slot s of row v live at

@@ -27,7 +27,7 @@ from dataclasses import dataclass
 import numpy as np
 import scipy.sparse as sps
 
-from . import fem, snh
+from . import fem, mmnh, snh
 from .solvers import BDF2_COEFF, bdf2_target, newton_solver, be_target
 
 
@@ -42,7 +42,9 @@ class StepInfo:
 class BeamRollout:
     """FP64 reference rollout of one beam instance."""
 
-    def __init__(self, X, T, mu, lam, rho, gravity, pinned, dt, tol=1e-6, max_newton=20):
+    def __init__(self, X, T, mu, lam, rho, gravity, pinned, dt, tol=1e-6, max_newton=20, material="snh"):
+        # the elastic energy: 'snh' (stable_neo_hookean.py) or 'mmnh' (macklin_mueller_neo_hookean.py)
+        self.energy = {"snh": snh, "mmnh": mmnh}[material]
         self.X = np.asarray(X, dtype=np.float64)
         self.T = np.asarray(T)
         self.mu = np.asarray(mu, dtype=np.float64).reshape(-1, 1)
@@ -74,13 +76,13 @@ class BeamRollout:
         return x
 
     def potential(self, x) -> float:
-        return snh.energy_x(x, self.J, self.mu, self.lam, self.vol) - (self.f_ext.T @ x).item()
+        return self.energy.energy_x(x, self.J, self.mu, self.lam, self.vol) - (self.f_ext.T @ x).item()
 
     def potential_gradient(self, x):
-        return snh.gradient_x(x, self.J, self.mu, self.lam, self.vol) - self.f_ext
+        return self.energy.gradient_x(x, self.J, self.mu, self.lam, self.vol) - self.f_ext
 
     def potential_hessian(self, x):
-        return snh.hessian_x(x, self.J, self.mu, self.lam, self.vol)
+        return self.energy.hessian_x(x, self.J, self.mu, self.lam, self.vol)
 
     # inertial targets (overridable to plug in another implementation of the same formulas)
     def be_target(self, yc, yp, h):
@@ -128,7 +130,7 @@ class BeamRollout:
                                       converged=res[-1] < self.tol)
 
     def elastic_energy(self, x) -> float:
-        return snh.energy_x(x, self.J, self.mu, self.lam, self.vol)
+        return self.energy.energy_x(x, self.J, self.mu, self.lam, self.vol)
 
     def rollout(self, steps, record=None, integrator="be"):
         """Run ``steps`` steps from rest ('be' or 'bdf2'); returns positions (steps+1, 3n) and
@@ -152,6 +154,6 @@ class BeamRollout:
         return np.array(xs), infos
 
 
-def from_spec(spec, dt=1.0 / 60.0, tol=1e-6, max_newton=20) -> BeamRollout:
+def from_spec(spec, dt=1.0 / 60.0, tol=1e-6, max_newton=20, material="snh") -> BeamRollout:
     return BeamRollout(spec.X, spec.T, spec.mu, spec.lam, spec.rho, spec.gravity, spec.pinned,
-                       dt, tol=tol, max_newton=max_newton)
+                       dt, tol=tol, max_newton=max_newton, material=material)

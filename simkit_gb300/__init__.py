@@ -16,6 +16,13 @@ _API = {
     "stable_neo_hookean_hessian_x", "stable_neo_hookean_energy", "stable_neo_hookean_gradient",
     "stable_neo_hookean_hessian", "psd_project", "deformation_jacobian", "volume", "backtracking_line_search",
     "newton_solver", "backward_euler", "bdf2", "solve_sparse", "BlockMatrix", "DeformationJacobian",
+    "macklin_mueller_neo_hookean_energy_element_F", "macklin_mueller_neo_hookean_gradient_element_F",
+    "macklin_mueller_neo_hookean_hessian_element_F", "macklin_mueller_neo_hookean_energy_x",
+    "macklin_mueller_neo_hookean_gradient_x", "macklin_mueller_neo_hookean_hessian_x",
+    "macklin_mueller_neo_hookean_energy", "macklin_mueller_neo_hookean_gradient",
+    "macklin_mueller_neo_hookean_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
+    "elastic_hessian_element_F", "elastic_energy_x", "elastic_gradient_x", "elastic_hessian_x",
+    "elastic_energy", "elastic_gradient", "elastic_hessian",
 }
 
 

@@ -46,7 +46,7 @@ class TetMeshC(ctypes.Structure):
         ("n_verts", c_i64), ("n_tets", c_i64), ("n_blocks", c_i64),
         ("tets", c_vp), ("dinv", c_vp), ("dinv32", c_vp), ("vol", c_vp), ("mu", c_vp), ("lam", c_vp),
         ("mat32", c_vp), ("bsr_rowptr", c_vp), ("bsr_col", c_vp), ("bsr_diag", c_vp), ("bsr_row", c_vp),
-        ("hc_ptr", c_vp), ("hc_src", c_vp), ("v2t_ptr", c_vp), ("v2t", c_vp),
+        ("hc_ptr", c_vp), ("hc_src", c_vp), ("v2t_ptr", c_vp), ("v2t", c_vp), ("material", c_i32),
     ]
 
 
@@ -85,6 +85,9 @@ _SIGNATURES = {
     "skg_snh_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_snh_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_snh_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_mmnh_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_mmnh_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_mmnh_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_psd_project": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "skg_tet_setup": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp]),
     "skg_tet_deformation_gradient": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),

@@ -37,10 +37,10 @@ def _out(t: torch.Tensor, like):
 # --------------------------------------------------------------------------- #
 # element tier: simkit/energies/stable_neo_hookean.py:65-443                  #
 # --------------------------------------------------------------------------- #
-def _elem(fn, F, mu, lam, shape_of, precision):
+def _elem(fn, F, mu, lam, shape_of, precision, name="Stable Neo-Hookean"):
     d = F.shape[-1]
     if d not in (2, 3):
-        raise ValueError("Stable Neo-Hookean supports dim=2 or dim=3")
+        raise ValueError(f"{name} supports dim=2 or dim=3")
     Fd = _dev(F).reshape(-1, d, d)
     t = Fd.shape[0]
     mud = _dev(mu).reshape(-1)
@@ -181,9 +181,10 @@ def _operator(J) -> TetMesh:
     raise TypeError("pass the operator returned by simkit_gb300.deformation_jacobian")
 
 
-def _bind(J, mu, lam, vol) -> TetMesh:
+def _bind(J, mu, lam, vol, material=0) -> TetMesh:
     m = _operator(J)
     m.set_material(mu, lam, vol)
+    m.set_energy(material)
     return m
 
 
@@ -268,6 +269,130 @@ def stable_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, ps
     """simkit ``stable_neo_hookean_hessian`` (snh.py:710-737)."""
     J = deformation_jacobian(X, T)
     return stable_neo_hookean_hessian_x(X if U is None else U, J, mu, lam, volume(X, T), psd=psd)
+
+
+# --------------------------------------------------------------------------- #
+# Macklin-Mueller neo-Hookean: simkit/energies/macklin_mueller_neo_hookean.py  #
+# --------------------------------------------------------------------------- #
+_MM = "Macklin-Mueller Neo-Hookean"
+MATERIALS = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1}
+
+
+def macklin_mueller_neo_hookean_energy_element_F(F, mu, lam, precision: str = "fp64"):
+    """psi per element, (t, 1).  simkit ``macklin_mueller_neo_hookean_energy_element_F`` (:66-122)."""
+    return _elem("skg_mmnh_energy_element_F", F, mu, lam, lambda t, d: (t, 1), precision, _MM)
+
+
+def macklin_mueller_neo_hookean_gradient_element_F(F, mu, lam, precision: str = "fp64"):
+    """PK1 per element, (t, d, d).  simkit ``macklin_mueller_neo_hookean_gradient_element_F`` (:125-185)."""
+    return _elem("skg_mmnh_gradient_element_F", F, mu, lam, lambda t, d: (t, d, d), precision, _MM)
+
+
+def macklin_mueller_neo_hookean_hessian_element_F(F, mu, lam, precision: str = "fp64"):
+    """(t, d*d, d*d) unprojected blocks.  simkit ``macklin_mueller_neo_hookean_hessian_element_F`` (:188-374)."""
+    return _elem("skg_mmnh_hessian_element_F", F, mu, lam, lambda t, d: (t, d * d, d * d), precision, _MM)
+
+
+def macklin_mueller_neo_hookean_energy_x(X, J, mu, lam, vol) -> float:
+    """sum vol psi(J x).  simkit ``macklin_mueller_neo_hookean_energy_x`` (:484-509)."""
+    m = _bind(J, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"])
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    e = ctypes.c_double()
+    check(_lib.load().skg_snh_energy_x(ctypes.byref(m.c), _ptr(x), ctypes.byref(e), _ptr(ws), _stream_ptr()))
+    return float(e.value)
+
+
+def macklin_mueller_neo_hookean_gradient_x(X, J, mu, lam, vol):
+    """J^T vec(vol P), (3n, 1).  simkit ``macklin_mueller_neo_hookean_gradient_x`` (:512-538)."""
+    m = _bind(J, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"])
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    g = torch.empty(3 * m.n, dtype=torch.float64, device="cuda")
+    check(_lib.load().skg_snh_gradient_x(ctypes.byref(m.c), _ptr(x), _ptr(g), _ptr(ws), _stream_ptr()))
+    return _out(g.reshape(-1, 1), X)
+
+
+def macklin_mueller_neo_hookean_hessian_x(X, J, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(psd(vol He)) J.  simkit ``macklin_mueller_neo_hookean_hessian_x`` (:541-574)."""
+    m = _bind(J, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"])
+    B = BlockMatrix(m, assemble_hessian_blocks(m, X, precision=precision, psd=psd))
+    return B if isinstance(X, torch.Tensor) else B.to_scipy()
+
+
+def macklin_mueller_neo_hookean_energy(X, T, mu, lam, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``macklin_mueller_neo_hookean_energy`` (:689-714)."""
+    return macklin_mueller_neo_hookean_energy_x(X if U is None else U, deformation_jacobian(X, T), mu, lam,
+                                                volume(X, T))
+
+
+def macklin_mueller_neo_hookean_gradient(X, T, mu, lam, U: Optional[np.ndarray] = None):
+    """simkit ``macklin_mueller_neo_hookean_gradient`` (:717-742)."""
+    return macklin_mueller_neo_hookean_gradient_x(X if U is None else U, deformation_jacobian(X, T), mu, lam,
+                                                  volume(X, T))
+
+
+def macklin_mueller_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``macklin_mueller_neo_hookean_hessian`` (:745-773)."""
+    return macklin_mueller_neo_hookean_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, lam,
+                                                 volume(X, T), psd=psd)
+
+
+# --------------------------------------------------------------------------- #
+# material dispatch: simkit/energies/elastic.py                               #
+# --------------------------------------------------------------------------- #
+def _material(material):
+    if material == "macklin-mueller-neo-hookean":
+        return "macklin_mueller_neo_hookean"
+    if material in ("linear-elasticity", "arap", "fcr"):
+        raise NotImplementedError(f"material {material!r} has no GPU kernels in this package")
+    raise ValueError("Unknown material type: " + str(material))
+
+
+def elastic_energy_element_F(F, mu, lam, material: str):
+    """simkit ``elastic_energy_element_F`` (elastic.py:86-116)."""
+    return globals()[_material(material) + "_energy_element_F"](F, mu, lam)
+
+
+def elastic_gradient_element_F(F, mu, lam, material: str):
+    """simkit ``elastic_gradient_element_F`` (elastic.py:396-426)."""
+    return globals()[_material(material) + "_gradient_element_F"](F, mu, lam)
+
+
+def elastic_hessian_element_F(F, mu, lam, material: str, psd: bool = True):
+    """simkit ``elastic_hessian_element_F`` (elastic.py:632-668): unweighted blocks, projected if psd."""
+    Q = globals()[_material(material) + "_hessian_element_F"](F, mu, lam)
+    return psd_project(Q) if psd else Q
+
+
+def elastic_energy_x(X, J, mu, lam, vol, material: str) -> float:
+    """simkit ``elastic_energy_x`` (elastic.py:119-148)."""
+    return globals()[_material(material) + "_energy_x"](X, J, mu, lam, vol)
+
+
+def elastic_gradient_x(X, J, mu, lam, vol, material: str):
+    """simkit ``elastic_gradient_x`` (elastic.py:429-459)."""
+    return globals()[_material(material) + "_gradient_x"](X, J, mu, lam, vol)
+
+
+def elastic_hessian_x(X, J, mu, lam, vol, material: str, psd: bool = True):
+    """simkit ``elastic_hessian_x`` (elastic.py:671-705)."""
+    return globals()[_material(material) + "_hessian_x"](X, J, mu, lam, vol, psd=psd)
+
+
+def elastic_energy(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``elastic_energy`` (elastic.py:360-393)."""
+    return globals()[_material(material) + "_energy"](X, T, mu, lam, U)
+
+
+def elastic_gradient(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None):
+    """simkit ``elastic_gradient`` (elastic.py:596-629)."""
+    return globals()[_material(material) + "_gradient"](X, T, mu, lam, U)
+
+
+def elastic_hessian(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``elastic_hessian`` (elastic.py:849-882)."""
+    return globals()[_material(material) + "_hessian"](X, T, mu, lam, U, psd=psd)
 
 
 # --------------------------------------------------------------------------- #

@@ -34,7 +34,7 @@ class BatchedBESolver:
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
-                 integrator="be"):
+                 integrator="be", material="stable-neo-hookean"):
         _lib.load()
         self.n_inst = len(specs)
         if self.n_inst == 0:
@@ -59,6 +59,7 @@ class BatchedBESolver:
             tets.append(tets[-1] + T.shape[0])
         mesh = TetMesh(np.concatenate(Xs), np.concatenate(Ts), np.concatenate(mus), np.concatenate(lams),
                        device=device)
+        mesh.set_energy(material)
         up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,

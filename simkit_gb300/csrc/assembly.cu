@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(128) k_tet_hessian(TetArgs<R> a, int disp, int
   }
   shape_grads(D, gN);
   const R vol = __ldg(a.vol + e), mu = __ldg(a.mu + e), lam = __ldg(a.lam + e);
-  snh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0);
+  snh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
   R* o = hbuf + (int64_t)kHStride * e;
   if constexpr (sizeof(R) == 4) {
 #pragma unroll
@@ -182,9 +182,9 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
   disp_grad(du, D, G);
   const double vol = a.vol[e], mu = a.mu[e], lam = a.lam[e];
   if (disp)
-    snh_pk1_disp<double>(G, mu, lam, P);
+    mat_pk1_disp<double>(a.material, G, mu, lam, P);
   else
-    snh_pk1<double>(G, mu, lam, P);
+    mat_pk1<double>(a.material, G, mu, lam, P);
   shape_grads(D, gN);
   double* f = fbuf + 12 * e;
 #pragma unroll
@@ -253,8 +253,8 @@ __device__ __forceinline__ double tet_energy_term(const EnergyArgs<R>& a, int64_
   load_dinv(a.tet.dinv, a.tet.t, e, D);
   disp_grad(du, D, G);
   const R vol = __ldg(a.tet.vol + e), mu = __ldg(a.tet.mu + e), lam = __ldg(a.tet.lam + e);
-  if (DIRECT) return double(vol) * double(snh_psi<R>(G, mu, lam));
-  return double(vol * snh_dpsi<R>(G, mu, lam));
+  if (DIRECT) return double(vol) * double(mat_psi<R>(a.tet.material, G, mu, lam));
+  return double(vol * mat_dpsi<R>(a.tet.material, G, mu, lam));
 }
 
 // kinetic + gravity terms of vertex v's free DOFs at u + step dx; acc[1] gets magnitudes
@@ -447,6 +447,7 @@ static TetArgs<double> tet_args64(const skg_tet_mesh* m, const double* u) {
   a.mu = m->mu;
   a.lam = m->lam;
   a.u = u;
+  a.material = m->material;
   return a;
 }
 
@@ -463,6 +464,7 @@ TetArgs<float> make_tet_args32(const skg_tet_mesh* m, const double* u, const flo
   a.u = u;
   a.uh = uh;
   a.ul = ul;
+  a.material = m->material;
   return a;
 }
 int check_mesh(const skg_tet_mesh* m, int precision) {
@@ -475,6 +477,8 @@ int check_mesh(const skg_tet_mesh* m, int precision) {
   if (precision == SKG_MIXED && (!m->dinv32 || !m->mat32))
     return fail(SKG_ERR_ARG, "mixed precision needs the FP32 mesh copies");
   if (precision != SKG_MIXED && precision != SKG_FP64) return fail(SKG_ERR_ARG, "unknown precision %d", precision);
+  if (m->material != SKG_MAT_STABLE_NEO_HOOKEAN && m->material != SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN)
+    return fail(SKG_ERR_ARG, "unknown material %d", m->material);
   return SKG_OK;
 }
 }  // namespace skg

@@ -27,6 +27,7 @@ template <typename R> struct TetArgs {
   const float* ul;
   const int32_t* tet_inst;     // optional: instance of each tet (batched solves)
   const uint8_t* inst_active;  // optional: skip tets of inactive instances
+  int material;                // kMatSNH or kMatMMNH
 };
 
 template <typename R> struct AsmArgs {

@@ -1,4 +1,4 @@
-// Element tier of the stable neo-Hookean energy over arbitrary F arrays,
+// Element tier of the stable neo-Hookean and Macklin-Mueller neo-Hookean energies over arbitrary F arrays,
 // simkit's generic psd_project, per-tet rest-shape setup, the F = J x gather
 // and the J^T P vertex gather.  Also the error plumbing of the C ABI.
 #include <stdarg.h>
@@ -25,7 +25,8 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 }
 
 // ------------------------------------------------------------ element F --
-template <typename R, int D>
+// MAT: kMatSNH (stable_neo_hookean.py) or kMatMMNH (macklin_mueller_neo_hookean.py)
+template <typename R, int D, int MAT>
 __global__ void k_elem_energy(const double* __restrict__ F, const double* __restrict__ mu,
                               const double* __restrict__ lam, double* __restrict__ psi, int64_t t) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -33,10 +34,14 @@ __global__ void k_elem_energy(const double* __restrict__ F, const double* __rest
   R f[D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  psi[e] = double(D == 3 ? snh_psi<R>(f, R(mu[e]), R(lam[e])) : snh_psi2<R>(f, R(mu[e]), R(lam[e])));
+  const R m = R(mu[e]), l = R(lam[e]);
+  R v;
+  if (MAT == kMatMMNH) v = D == 3 ? mmnh_psi<R>(f, m, l) : mmnh_psi2<R>(f, m, l);
+  else v = D == 3 ? snh_psi<R>(f, m, l) : snh_psi2<R>(f, m, l);
+  psi[e] = double(v);
 }
 
-template <typename R, int D>
+template <typename R, int D, int MAT>
 __global__ void k_elem_pk1(const double* __restrict__ F, const double* __restrict__ mu,
                            const double* __restrict__ lam, double* __restrict__ P, int64_t t) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -44,13 +49,19 @@ __global__ void k_elem_pk1(const double* __restrict__ F, const double* __restric
   R f[D * D], p[D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  if (D == 3) snh_pk1<R>(f, R(mu[e]), R(lam[e]), p);
-  else snh_pk1_2<R>(f, R(mu[e]), R(lam[e]), p);
+  const R m = R(mu[e]), l = R(lam[e]);
+  if (MAT == kMatMMNH) {
+    if (D == 3) mmnh_pk1<R>(f, m, l, p);
+    else mmnh_pk1_2<R>(f, m, l, p);
+  } else {
+    if (D == 3) snh_pk1<R>(f, m, l, p);
+    else snh_pk1_2<R>(f, m, l, p);
+  }
 #pragma unroll
   for (int k = 0; k < D * D; ++k) P[D * D * e + k] = double(p[k]);
 }
 
-template <typename R, int D>
+template <typename R, int D, int MAT>
 __global__ void k_elem_hessian(const double* __restrict__ F, const double* __restrict__ mu,
                                const double* __restrict__ lam, double* __restrict__ H, int64_t t) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -58,8 +69,14 @@ __global__ void k_elem_hessian(const double* __restrict__ F, const double* __res
   R f[D * D], h[D * D * D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  if (D == 3) snh_hessian9<R>(f, R(mu[e]), R(lam[e]), h);
-  else snh_hessian4<R>(f, R(mu[e]), R(lam[e]), h);
+  const R m = R(mu[e]), l = R(lam[e]);
+  if (MAT == kMatMMNH) {
+    if (D == 3) mmnh_hessian9<R>(f, m, l, h);
+    else mmnh_hessian4<R>(f, m, l, h);
+  } else {
+    if (D == 3) snh_hessian9<R>(f, m, l, h);
+    else snh_hessian4<R>(f, m, l, h);
+  }
   for (int k = 0; k < D * D * D * D; ++k) H[(int64_t)D * D * D * D * e + k] = double(h[k]);
 }
 
@@ -67,7 +84,7 @@ typedef void (*ElemKernel)(const double*, const double*, const double*, double*,
 
 static int launch_elem(int dim, int precision, const double* F, const double* mu, const double* lam, double* out,
                        int64_t t, void* stream, ElemKernel k33, ElemKernel k32, ElemKernel k23, ElemKernel k22) {
-  if (dim != 2 && dim != 3) return fail(SKG_ERR_ARG, "Stable Neo-Hookean supports dim=2 or dim=3");
+  if (dim != 2 && dim != 3) return fail(SKG_ERR_ARG, "the element tier supports dim=2 or dim=3");
   if (t < 0) return fail(SKG_ERR_ARG, "negative element count");
   if (t == 0) return SKG_OK;
   auto kern = dim == 3 ? (precision == SKG_FP64 ? k33 : k32) : (precision == SKG_FP64 ? k23 : k22);
@@ -225,24 +242,38 @@ int skg_last_error(char* buf, size_t len) {
   return SKG_OK;
 }
 
+#define SKG_ELEM(kern, M) kern<double, 3, M>, kern<float, 3, M>, kern<double, 2, M>, kern<float, 2, M>
+
 int skg_snh_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                              double* psi, int64_t t, void* stream) {
-  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, k_elem_energy<double, 3>,
-                                    k_elem_energy<float, 3>, k_elem_energy<double, 2>, k_elem_energy<float, 2>);
+  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, SKG_ELEM(k_elem_energy, kMatSNH));
 }
 
 int skg_snh_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                                double* P, int64_t t, void* stream) {
-  return launch_elem(dim, precision, F, mu, lam, P, t, stream, k_elem_pk1<double, 3>,
-                                 k_elem_pk1<float, 3>, k_elem_pk1<double, 2>, k_elem_pk1<float, 2>);
+  return launch_elem(dim, precision, F, mu, lam, P, t, stream, SKG_ELEM(k_elem_pk1, kMatSNH));
 }
 
 int skg_snh_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                               double* H, int64_t t, void* stream) {
-  return launch_elem(dim, precision, F, mu, lam, H, t, stream, k_elem_hessian<double, 3>,
-                                     k_elem_hessian<float, 3>, k_elem_hessian<double, 2>,
-                                     k_elem_hessian<float, 2>);
+  return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatSNH));
 }
+
+int skg_mmnh_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* psi, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, SKG_ELEM(k_elem_energy, kMatMMNH));
+}
+
+int skg_mmnh_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                                double* P, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, P, t, stream, SKG_ELEM(k_elem_pk1, kMatMMNH));
+}
+
+int skg_mmnh_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* H, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatMMNH));
+}
+#undef SKG_ELEM
 
 int skg_psd_project(const double* H, double* out, int64_t n, int d, int method, void* stream) {
   if (d < 1 || d > 12) return fail(SKG_ERR_ARG, "psd_project supports block sizes 1..12, got %d", d);

@@ -1,4 +1,5 @@
-// Stable neo-Hookean element math shared by every kernel of the FEM path.
+// Element math shared by every kernel of the FEM path: the stable neo-Hookean
+// energy and the Macklin-Mueller neo-Hookean energy (same I_C / J Hessian form).
 //
 // All routines are plain functions of registers, compiled for the device by
 // nvcc and for the host by g++ (the host build is what the CPU unit tests
@@ -183,20 +184,12 @@ template <typename R> SK_HD void snh_pk1_disp(const R* G, R mu, R lam, R* P) {
 // --------------------------------------------------------------------------
 // explicit 9x9 F-Hessian, row-major vec(F) (the element tier)
 // --------------------------------------------------------------------------
-template <typename R> SK_HD void snh_hessian9(const R* F, R mu, R lam, R* H) {
-  R IC = 0;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
-  const R J = det3(F);
-  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
-  const R den = IC + R(1);
-  const R A = mu * IC / den;
-  const R B = R(2) * mu / (den * den);
-  const R D = lam * (J - alpha);
+// A I + B f f^T + L c c^T + D d2J/dF2 for any energy of I_C and J
+template <typename R> SK_HD void hessian9_coef(const R* F, R A, R B, R L, R D, R* H) {
   R C[9];
   cof3(F, C);
   for (int p = 0; p < 9; ++p)
-    for (int q = 0; q < 9; ++q) H[9 * p + q] = B * F[p] * F[q] + lam * C[p] * C[q] + (p == q ? A : R(0));
+    for (int q = 0; q < 9; ++q) H[9 * p + q] = B * F[p] * F[q] + L * C[p] * C[q] + (p == q ? A : R(0));
   // D * d2J/dF_ij dF_kl = D * eps_ikm eps_jln F_mn: nonzero only for i != k, j != l
   for (int i = 0; i < 3; ++i)
     for (int k = 0; k < 3; ++k) {
@@ -211,6 +204,16 @@ template <typename R> SK_HD void snh_hessian9(const R* F, R mu, R lam, R* H) {
           H[9 * (3 * i + j) + (3 * k + l)] += D * sik * sjl * F[3 * m + n];
         }
     }
+}
+
+template <typename R> SK_HD void snh_hessian9(const R* F, R mu, R lam, R* H) {
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  const R J = det3(F);
+  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+  const R den = IC + R(1);
+  hessian9_coef(F, mu * IC / den, R(2) * mu / (den * den), lam, lam * (J - alpha), H);
 }
 
 // 2D element tier (simkit/energies/stable_neo_hookean.py, dim == 2 branches)
@@ -232,22 +235,116 @@ template <typename R> SK_HD void snh_pk1_2(const R* F, R mu, R lam, R* P) {
   for (int k = 0; k < 4; ++k) P[k] = A * F[k] + D * C[k];
 }
 
-template <typename R> SK_HD void snh_hessian4(const R* F, R mu, R lam, R* H) {
-  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
-  const R J = F[0] * F[3] - F[1] * F[2];
-  const R alpha = R(1) + R(2) * mu / (R(3) * lam);
-  const R den = IC + R(1);
-  const R A = mu * IC / den;
-  const R B = R(2) * mu / (den * den);
-  const R D = lam * (J - alpha);
+template <typename R> SK_HD void hessian4_coef(const R* F, R A, R B, R L, R D, R* H) {
   const R C[4] = {F[3], -F[2], -F[1], F[0]};
   for (int p = 0; p < 4; ++p)
-    for (int q = 0; q < 4; ++q) H[4 * p + q] = B * F[p] * F[q] + lam * C[p] * C[q] + (p == q ? A : R(0));
+    for (int q = 0; q < 4; ++q) H[4 * p + q] = B * F[p] * F[q] + L * C[p] * C[q] + (p == q ? A : R(0));
   // d2J: (00,11) = (11,00) = +1, (01,10) = (10,01) = -1
   H[4 * 0 + 3] += D;
   H[4 * 3 + 0] += D;
   H[4 * 1 + 2] -= D;
   H[4 * 2 + 1] -= D;
+}
+
+template <typename R> SK_HD void snh_hessian4(const R* F, R mu, R lam, R* H) {
+  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  const R J = F[0] * F[3] - F[1] * F[2];
+  const R alpha = R(1) + R(2) * mu / (R(3) * lam);
+  const R den = IC + R(1);
+  hessian4_coef(F, mu * IC / den, R(2) * mu / (den * den), lam, lam * (J - alpha), H);
+}
+
+// --------------------------------------------------------------------------
+// Macklin-Mueller neo-Hookean (simkit/energies/macklin_mueller_neo_hookean.py:66-443):
+//   psi = mu (1 - J) + lam/2 (1 - J)^2 + mu/2 (I_C - dim),
+//   P = mu F + D cof F with D = lam (J - 1) - mu,
+//   F-Hessian mu I + lam c c^T + D d2J/dF2 (the I_C/J form above with A = mu, B = 0).
+// psi(I) = 0, and the displacement forms combine the terms that cancel at rest
+// (A + D = lam (J - 1)).
+// --------------------------------------------------------------------------
+template <typename R> SK_HD R mmnh_psi(const R* F, R mu, R lam) {
+  // simkit's expression order (macklin_mueller_neo_hookean.py:108-121), d = 1 - J
+  const R d = -F[0] * F[4] * F[8] + F[0] * F[5] * F[7] + F[1] * F[3] * F[8] - F[1] * F[5] * F[6] -
+              F[2] * F[3] * F[7] + F[2] * F[4] * F[6] + R(1);
+  R IC = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
+  return mu * d + (lam * d * d) / R(2) + (mu * (IC - R(3))) / R(2);
+}
+
+// psi(I + G) = mu (|G|^2/2 - I2(G) - det G) + lam/2 y^2, y = J - 1 = tr G + I2(G) + det G
+template <typename R> SK_HD R mmnh_dpsi(const R* G, R mu, R lam) {
+  R g2 = 0;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) g2 += G[k] * G[k];
+  const R i2 = minors2(G);
+  const R dg = det3(G);
+  const R y = G[0] + G[4] + G[8] + i2 + dg;
+  return mu * (R(0.5) * g2 - i2 - dg) + R(0.5) * lam * y * y;
+}
+
+template <typename R> SK_HD void mmnh_pk1(const R* F, R mu, R lam, R* P) {
+  const R D = lam * (det3(F) - R(1)) - mu;
+  R C[9];
+  cof3(F, C);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) P[k] = mu * F[k] + D * C[k];
+}
+
+// P(I + G) = lam y I + mu G + D (tr G I - G^T + cof G)
+template <typename R> SK_HD void mmnh_pk1_disp(const R* G, R mu, R lam, R* P) {
+  const R tr = G[0] + G[4] + G[8];
+  const R y = tr + minors2(G) + det3(G);
+  const R D = lam * y - mu;
+  R C[9];
+  cof3(G, C);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int k = 3 * i + j;
+      R v = mu * G[k] + D * (C[k] - G[3 * j + i]);
+      if (i == j) v += lam * y + D * tr;
+      P[k] = v;
+    }
+}
+
+template <typename R> SK_HD void mmnh_hessian9(const R* F, R mu, R lam, R* H) {
+  hessian9_coef(F, mu, R(0), lam, lam * (det3(F) - R(1)) - mu, H);
+}
+
+template <typename R> SK_HD R mmnh_psi2(const R* F, R mu, R lam) {
+  const R d = -F[0] * F[3] + F[1] * F[2] + R(1);
+  const R IC = F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3];
+  return mu * d + (lam * d * d) / R(2) + (mu * (IC - R(2))) / R(2);
+}
+
+template <typename R> SK_HD void mmnh_pk1_2(const R* F, R mu, R lam, R* P) {
+  const R D = lam * (F[0] * F[3] - F[1] * F[2] - R(1)) - mu;
+  const R C[4] = {F[3], -F[2], -F[1], F[0]};
+  for (int k = 0; k < 4; ++k) P[k] = mu * F[k] + D * C[k];
+}
+
+template <typename R> SK_HD void mmnh_hessian4(const R* F, R mu, R lam, R* H) {
+  hessian4_coef(F, mu, R(0), lam, lam * (F[0] * F[3] - F[1] * F[2] - R(1)) - mu, H);
+}
+
+// materials of the per-tet kernels
+enum : int { kMatSNH = 0, kMatMMNH = 1 };
+
+template <typename R> SK_HD R mat_dpsi(int mat, const R* G, R mu, R lam) {
+  return mat == kMatMMNH ? mmnh_dpsi(G, mu, lam) : snh_dpsi(G, mu, lam);
+}
+template <typename R> SK_HD R mat_psi(int mat, const R* F, R mu, R lam) {
+  return mat == kMatMMNH ? mmnh_psi(F, mu, lam) : snh_psi(F, mu, lam);
+}
+template <typename R> SK_HD void mat_pk1_disp(int mat, const R* G, R mu, R lam, R* P) {
+  if (mat == kMatMMNH) mmnh_pk1_disp(G, mu, lam, P);
+  else snh_pk1_disp(G, mu, lam, P);
+}
+template <typename R> SK_HD void mat_pk1(int mat, const R* F, R mu, R lam, R* P) {
+  if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
+  else snh_pk1(F, mu, lam, P);
 }
 
 // --------------------------------------------------------------------------
@@ -430,18 +527,26 @@ SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
 // fallback_J: elements with det F below it run the SVD in FP64.
 // floor_v: eigenvalue floor (simkit's 1e-6); project = false skips the
 // projection (simkit's psd=False, snh.py:534).
+// material: kMatSNH or kMatMMNH (the coefficients A, B, D of the I_C / J form).
 template <typename R>
 SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1),
-                           bool project = true) {
+                           bool project = true, int material = kMatSNH) {
   R IC = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
   const R J = det3(F);
-  const R alpha = R(1) + R(3) * mu / (R(4) * lam);
-  const R den = IC + R(1);
-  const R A = mu * IC / den;
-  const R B = R(2) * mu / (den * den);
-  const R D = lam * (J - alpha);
+  R A, B, D;
+  if (material == kMatMMNH) {
+    A = mu;
+    B = R(0);
+    D = lam * (J - R(1)) - mu;
+  } else {
+    const R alpha = R(1) + R(3) * mu / (R(4) * lam);
+    const R den = IC + R(1);
+    A = mu * IC / den;
+    B = R(2) * mu / (den * den);
+    D = lam * (J - alpha);
+  }
   R C[9];
   cof3(F, C);
 

@@ -109,13 +109,15 @@ class TetMesh:
         return self
 
     def _set_c(self):
+        if not hasattr(self, "material"):
+            self.material = 0
         self.c = TetMeshC(
             n_verts=self.n, n_tets=self.t, n_blocks=self.nb,
             tets=self.tets.data_ptr(), dinv=self.dinv.data_ptr(), dinv32=self.dinv32.data_ptr(),
             vol=self.vol.data_ptr(), mu=self.mu.data_ptr(), lam=self.lam.data_ptr(), mat32=self.mat32.data_ptr(),
             bsr_rowptr=self.rowptr.data_ptr(), bsr_col=self.col.data_ptr(), bsr_diag=self.diag.data_ptr(),
             bsr_row=self.row.data_ptr(), hc_ptr=self.hc_ptr.data_ptr(), hc_src=self.hc_src.data_ptr(),
-            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr())
+            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr(), material=self.material)
 
     def __init__(self, X, T, mu, lam, device="cuda"):
         lib = _lib.load()
@@ -168,6 +170,14 @@ class TetMesh:
         self._scalar_perm = None
 
     # ----------------------------------------------------------------- utils
+    def set_energy(self, material):
+        """Elastic energy of every tet: 0 / 'stable-neo-hookean', 1 / 'macklin-mueller-neo-hookean'."""
+        code = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1}.get(material, material)
+        if code not in (0, 1):
+            raise ValueError(f"unknown material {material!r}")
+        self.material = code
+        self.c.material = code
+
     def set_material(self, mu, lam, vol=None):
         """Replace per-tet mu, lam (and quadrature weights vol) in place."""
         def dev(a):

@@ -77,13 +77,16 @@ class BESolver:
         cluster, 3 choose by size (cluster up to 24,576 block rows)
     integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
         (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
+    material : 'stable-neo-hookean' or 'macklin-mueller-neo-hookean' (simkit/energies/elastic.py names)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
-                 do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be"):
+                 do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
+                 material="stable-neo-hookean"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
+        self.mesh.set_energy(material)
         m = self.mesh
         dev = m.device
         X = m.X_host

@@ -18,6 +18,8 @@ Fixtures written next to this script:
 * ``rollout_small.npz``: 6x2x2 beam, 8 backward-Euler steps (positions, iterations, residuals)
 * ``rollout_beam_8x8x32.npz``: the 12,288-tet beam, 60 steps (displacements at a few steps, energies, iterations)
 * ``rollout_bdf2_small.npz``: 6x2x2 beam, 8 BDF2 steps from rest (the reference's BDF2 target and coefficient)
+* ``element_mmnh_3d.npz`` / ``element_mmnh_2d.npz``: Macklin-Mueller neo-Hookean element tier on the same F batches
+* ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
 """
 
 from __future__ import annotations
@@ -47,8 +49,10 @@ def _import_reference(path):
         from simkit.massmatrix import massmatrix
         from simkit.solvers import newton_solver
         from simkit.energies import kinetic
+        from simkit.energies import macklin_mueller_neo_hookean as ref_mmnh
     return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
-                volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic)
+                volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic,
+                mmnh=ref_mmnh)
 
 
 def element_cases(rng, d, t_each=32):
@@ -91,6 +95,17 @@ def make_element(ref, d, out):
     np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
 
 
+def make_element_mmnh(ref, d, out):
+    rng = np.random.default_rng(100 + d)
+    F, mu, lam, vol = element_cases(rng, d)
+    m = ref["mmnh"]
+    psi = m.macklin_mueller_neo_hookean_energy_element_F(F, mu, lam)
+    P = m.macklin_mueller_neo_hookean_gradient_element_F(F, mu, lam)
+    He = m.macklin_mueller_neo_hookean_hessian_element_F(F, mu, lam)
+    Hp = ref["psd_project"](He * vol.reshape(-1, 1, 1))
+    np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
+
+
 def make_beam_small(ref, out):
     from simkit_gb300.beams import make_beam
     rng = np.random.default_rng(7)
@@ -112,12 +127,19 @@ def make_beam_small(ref, out):
                         K_data=K.data, K_indices=K.indices, K_indptr=K.indptr)
 
 
-def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be"):
+def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", material="snh"):
     """The oracle harness with every FEM routine and the Newton step taken from the reference."""
     import scipy.sparse as sps
     from oracle.rollout import BeamRollout
 
-    s = ref["snh"]
+    if material == "mmnh":
+        m = ref["mmnh"]
+        s = type("MMNH", (), dict(
+            stable_neo_hookean_energy_x=staticmethod(m.macklin_mueller_neo_hookean_energy_x),
+            stable_neo_hookean_gradient_x=staticmethod(m.macklin_mueller_neo_hookean_gradient_x),
+            stable_neo_hookean_hessian_x=staticmethod(m.macklin_mueller_neo_hookean_hessian_x)))
+    else:
+        s = ref["snh"]
 
     class RefRollout(BeamRollout):
         def __init__(self):
@@ -192,6 +214,16 @@ def make_rollout_bdf2_small(ref, out):
                         ym=2e5, pr=0.45, dt=1.0 / 60.0)
 
 
+def make_rollout_mmnh_small(ref, out):
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 8, material="mmnh")
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
+                        ym=2e5, pr=0.45, dt=1.0 / 60.0)
+
+
 def make_rollout_c1(ref, out):
     from simkit_gb300.beams import beam_small_steady
     spec = beam_small_steady()
@@ -215,6 +247,9 @@ def main():
     make_beam_small(ref, os.path.join(HERE, "beam_small.npz"))
     make_rollout_small(ref, os.path.join(HERE, "rollout_small.npz"))
     make_rollout_bdf2_small(ref, os.path.join(HERE, "rollout_bdf2_small.npz"))
+    make_element_mmnh(ref, 3, os.path.join(HERE, "element_mmnh_3d.npz"))
+    make_element_mmnh(ref, 2, os.path.join(HERE, "element_mmnh_2d.npz"))
+    make_rollout_mmnh_small(ref, os.path.join(HERE, "rollout_mmnh_small.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)

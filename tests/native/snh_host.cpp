@@ -7,12 +7,12 @@ using namespace skg;
 
 template <typename R>
 static void tet_hessian_batch(int64_t t, const double* F, const double* mu, const double* lam,
-                              const double* vol, const double* gN, double* out, double fb) {
+                              const double* vol, const double* gN, double* out, double fb, int mat = kMatSNH) {
   for (int64_t e = 0; e < t; ++e) {
     R f[9], g[12], o[kTetHessVals];
     for (int k = 0; k < 9; ++k) f[k] = R(F[9 * e + k]);
     for (int k = 0; k < 12; ++k) g[k] = R(gN[12 * e + k]);
-    snh_tet_hessian<R>(f, R(mu[e]), R(lam[e]), R(vol[e]), g, o, R(fb));
+    snh_tet_hessian<R>(f, R(mu[e]), R(lam[e]), R(vol[e]), g, o, R(fb), true, mat);
     for (int k = 0; k < kTetHessVals; ++k) out[kTetHessVals * e + k] = double(o[k]);
   }
 }
@@ -46,6 +46,24 @@ static void disp_batch(int64_t t, const double* G, const double* mu, const doubl
   }
 }
 
+// Macklin-Mueller neo-Hookean: direct and displacement forms, Hessian
+template <typename R>
+static void mm_batch(int64_t t, const double* F, const double* G, const double* mu, const double* lam, double* psi,
+                     double* dpsi, double* P, double* Pd, double* H) {
+  for (int64_t e = 0; e < t; ++e) {
+    R f[9], g[9], p[9], h[81];
+    for (int k = 0; k < 9; ++k) { f[k] = R(F[9 * e + k]); g[k] = R(G[9 * e + k]); }
+    psi[e] = double(mat_psi<R>(kMatMMNH, f, R(mu[e]), R(lam[e])));
+    dpsi[e] = double(mat_dpsi<R>(kMatMMNH, g, R(mu[e]), R(lam[e])));
+    mat_pk1<R>(kMatMMNH, f, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 9; ++k) P[9 * e + k] = double(p[k]);
+    mat_pk1_disp<R>(kMatMMNH, g, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 9; ++k) Pd[9 * e + k] = double(p[k]);
+    mmnh_hessian9<R>(f, R(mu[e]), R(lam[e]), h);
+    for (int k = 0; k < 81; ++k) H[81 * e + k] = double(h[k]);
+  }
+}
+
 template <typename R>
 static void svd_batch(int64_t t, const double* F, double* U, double* s, double* V) {
   for (int64_t e = 0; e < t; ++e) {
@@ -71,6 +89,16 @@ void h_elem(int prec, int64_t t, const double* F, const double* mu, const double
 void h_disp(int prec, int64_t t, const double* G, const double* mu, const double* lam, double* dpsi, double* Pd) {
   if (prec == 64) disp_batch<double>(t, G, mu, lam, dpsi, Pd);
   else disp_batch<float>(t, G, mu, lam, dpsi, Pd);
+}
+void h_tet_hessian_mat(int prec, int mat, int64_t t, const double* F, const double* mu, const double* lam,
+                       const double* vol, const double* gN, double* out, double fallback_J) {
+  if (prec == 64) tet_hessian_batch<double>(t, F, mu, lam, vol, gN, out, fallback_J, mat);
+  else tet_hessian_batch<float>(t, F, mu, lam, vol, gN, out, fallback_J, mat);
+}
+void h_mm(int prec, int64_t t, const double* F, const double* G, const double* mu, const double* lam, double* psi,
+          double* dpsi, double* P, double* Pd, double* H) {
+  if (prec == 64) mm_batch<double>(t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+  else mm_batch<float>(t, F, G, mu, lam, psi, dpsi, P, Pd, H);
 }
 void h_svd(int prec, int64_t t, const double* F, double* U, double* s, double* V) {
   if (prec == 64) svd_batch<double>(t, F, U, s, V);

@@ -175,6 +175,53 @@ def test_tet_hessian_analytic_psd_matches_eigh_floor(hostmath, prec, tol):
     assert err.max() < tol
 
 
+@pytest.mark.parametrize("prec,tol", [(64, 1e-12), (32, 3e-6)])
+def test_mmnh_tet_hessian_analytic_psd_matches_eigh_floor(hostmath, prec, tol):
+    """The same analytic PSD floor + lift with the Macklin-Mueller coefficients (A = mu, B = 0,
+    D = lam (J - 1) - mu) == eigh floor of the oracle's vol * He, lifted."""
+    from oracle import mmnh
+    rng = np.random.default_rng(15)
+    F, mu, lam, vol, gN = _cases(rng)
+    t = F.shape[0]
+    out = np.zeros((t, 78))
+    hostmath.h_tet_hessian_mat(prec, 1, ctypes.c_int64(t), _p(F), _p(mu), _p(lam), _p(vol), _p(gN), _p(out),
+                               ctypes.c_double(0.1))
+    K = _unpack78(out)
+    H9p = psd.psd_project(mmnh.hessian_element_F(F, mu, lam) * vol[:, None, None])
+    Ko = np.einsum("taj,tbl,tijkl->taibk", gN, gN, H9p.reshape(t, 3, 3, 3, 3)).reshape(t, 12, 12)
+    err = np.abs(K - Ko).max(axis=(1, 2)) / np.abs(Ko).max(axis=(1, 2))
+    assert err.max() < tol
+
+
+def test_mmnh_element_math_matches_oracle(hostmath):
+    """Direct and displacement forms of the Macklin-Mueller energy and stress, and its F-Hessian."""
+    from oracle import mmnh
+    rng = np.random.default_rng(16)
+    t = 200
+    G = np.concatenate([1e-4 * rng.standard_normal((t // 2, 3, 3)), 0.2 * rng.standard_normal((t // 2, 3, 3))])
+    F = np.ascontiguousarray(np.eye(3)[None] + G)
+    G = np.ascontiguousarray(G)
+    mu = rng.uniform(3e4, 3e6, t)
+    lam = mu * rng.uniform(1.5, 40, t)
+    psi, dpsi, P, Pd, H = np.zeros(t), np.zeros(t), np.zeros((t, 9)), np.zeros((t, 9)), np.zeros((t, 81))
+    hostmath.h_mm(64, ctypes.c_int64(t), _p(F), _p(G), _p(mu), _p(lam), _p(psi), _p(dpsi), _p(P), _p(Pd), _p(H))
+    po = mmnh.energy_element_F(F, mu, lam).ravel()
+    Po = mmnh.gradient_element_F(F, mu, lam).reshape(t, 9)
+    Ho = mmnh.hessian_element_F(F, mu, lam).reshape(t, 81)
+    scale = mu + lam
+    assert np.all(np.abs(psi - po) <= 1e-12 * scale)
+    assert np.all(np.abs(dpsi - po) <= 1e-9 * np.abs(po) + 1e-15 * scale)     # psi(I) = 0
+    assert np.all(np.abs(P - Po).max(1) <= 1e-12 * scale)
+    assert np.all(np.abs(Pd - Po).max(1) <= 1e-9 * np.abs(Po).max(1) + 1e-15 * scale)
+    assert np.all(np.abs(H - Ho).max(1) <= 1e-12 * scale)
+    # FP32 displacement forms keep relative accuracy near rest
+    d32, P32 = np.zeros(t), np.zeros((t, 9))
+    psi32, H32, Pf = np.zeros(t), np.zeros((t, 81)), np.zeros((t, 9))
+    hostmath.h_mm(32, ctypes.c_int64(t), _p(F), _p(G), _p(mu), _p(lam), _p(psi32), _p(d32), _p(Pf), _p(P32), _p(H32))
+    assert np.max(np.abs(d32 - dpsi) / np.abs(dpsi)) < 2e-5
+    assert np.max(np.abs(P32 - Pd).max(1) / np.abs(Pd).max(1)) < 2e-5
+
+
 def test_displacement_forms_match_oracle(hostmath):
     rng = np.random.default_rng(6)
     t = 200

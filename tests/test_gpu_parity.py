@@ -213,6 +213,69 @@ def test_drop_in_bdf2_matches_oracle(api):
     assert _rel(got, ref) < 1e-9
 
 
+@pytest.mark.parametrize("d", [3, 2])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5)])
+def test_mmnh_element_tier_matches_reference(api, d, precision, tol):
+    """Macklin-Mueller element tier on the device against reference-generated values."""
+    g = _load(f"element_mmnh_{d}d.npz")
+    F, mu, lam = g["F"], g["mu"], g["lam"]
+    psi = api.macklin_mueller_neo_hookean_energy_element_F(F, mu, lam, precision=precision)
+    P = api.macklin_mueller_neo_hookean_gradient_element_F(F, mu, lam, precision=precision)
+    H = api.macklin_mueller_neo_hookean_hessian_element_F(F, mu, lam, precision=precision)
+    scale = (mu + lam).reshape(-1)
+    assert np.all(np.abs(psi - g["psi"]).reshape(len(scale), -1).max(1) <= tol * scale * 10)
+    assert np.all(np.abs(P - g["P"]).reshape(len(scale), -1).max(1) <= tol * scale * 10)
+    assert np.all(np.abs(H - g["He"]).reshape(len(scale), -1).max(1) <= tol * scale * 10)
+    via = api.elastic_hessian_element_F(F, mu, lam, "macklin-mueller-neo-hookean", psd=False)
+    assert _rel(via, g["He"]) < 1e-12
+
+
+def test_mmnh_assembled_tier_matches_oracle(api):
+    from oracle import fem, mmnh
+    from simkit_gb300.beams import make_beam
+    rng = np.random.default_rng(8)
+    spec = make_beam(4, 3, 2, ym=np.exp(rng.uniform(np.log(1e5), np.log(1e7), 6 * 24)), pr=0.42, jitter=0.1)
+    X, T = spec.X, spec.T
+    J = fem.deformation_jacobian(X, T)
+    vol = fem.tet_volumes(X, T)
+    x = X + 0.003 * rng.standard_normal(X.shape)
+    dJ = api.deformation_jacobian(X, T)
+    e = api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "macklin-mueller-neo-hookean")
+    assert abs(e - mmnh.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-10 * abs(e)
+    g = api.macklin_mueller_neo_hookean_gradient_x(x, dJ, spec.mu, spec.lam, vol)
+    assert _rel(g, mmnh.gradient_x(x, J, spec.mu, spec.lam, vol)) < 1e-10
+    K = api.macklin_mueller_neo_hookean_hessian_x(x, dJ, spec.mu, spec.lam, vol)
+    Ko = mmnh.hessian_x(x, J, spec.mu, spec.lam, vol)
+    assert abs(K - Ko).max() < 1e-9 * abs(Ko).max()
+    # the mesh returns to the stable neo-Hookean energy for the stable neo-Hookean entry points
+    from oracle import snh as osnh
+    e2 = api.stable_neo_hookean_energy_x(x, dJ, spec.mu, spec.lam, vol)
+    assert abs(e2 - osnh.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-10 * abs(e2)
+    with pytest.raises(NotImplementedError):
+        api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "arap")
+    with pytest.raises(ValueError):
+        api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "rubber")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mmnh_be_step_matches_reference_rollout(api, precision):
+    """Backward Euler with the Macklin-Mueller energy against the reference's rollout."""
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_mmnh_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    kw = dict(pcg_rtol=1e-10) if precision == "fp64" else {}
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, material="macklin-mueller-neo-hookean",
+                           **kw)
+    X = spec.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, info
+        k = list(d["steps"]).index(step)
+        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_rollout_8x8x32_matches_reference(api, precision):
     """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""

@@ -103,6 +103,31 @@ def test_rollout_bdf2_small_matches_reference():
     assert [i.iters for i in infos] == list(d["iters"])
 
 
+@pytest.mark.parametrize("d", [3, 2])
+def test_mmnh_element_tier_matches_reference(d):
+    """Macklin-Mueller neo-Hookean element tier (macklin_mueller_neo_hookean.py:66-374) against
+    reference-generated values, including inverted and nearly collapsed elements."""
+    from oracle import mmnh
+    from oracle.psd import psd_project
+    g = _load(f"element_mmnh_{d}d.npz")
+    assert _rel(mmnh.energy_element_F(g["F"], g["mu"], g["lam"]), g["psi"]) < 1e-12
+    assert _rel(mmnh.gradient_element_F(g["F"], g["mu"], g["lam"]), g["P"]) < 1e-12
+    He = mmnh.hessian_element_F(g["F"], g["mu"], g["lam"])
+    assert _rel(He, g["He"]) < 1e-12
+    assert _rel(psd_project(He * g["vol"].reshape(-1, 1, 1)), g["He_proj"]) < 1e-9
+
+
+def test_rollout_mmnh_small_matches_reference():
+    d = _load("rollout_mmnh_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    r = rollout.from_spec(spec, dt=float(d["dt"]), material="mmnh")
+    xs, infos = r.rollout(int(d["steps"].max()))
+    for k, s in enumerate(d["steps"]):
+        assert _rel(xs[s] - r.x_rest.ravel(), d["u"][k]) < 1e-8, s
+    assert [i.iters for i in infos] == list(d["iters"])
+
+
 def test_bdf2_target_is_exact_for_quadratic_motion():
     """The BDF2 velocity reconstruction is exact for quadratic motion (kinetic.py:63-101), so the
     target of x(t) = a + b t + c t^2 sampled at t = -3h..0 is x(h)."""
