@@ -85,6 +85,27 @@ int skg_mmnh_hessian_element_F(int dim, int precision, const double* F, const do
                                double* H, int64_t t, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* contact springs: simkit/energies/contact_springs_plane.py:44-200        */
+/* ---------------------------------------------------------------------- */
+/* One contact plane of simkit's contact springs (simkit/energies/contact_springs_plane.py:44-200):
+ * every vertex with (x - p) . n < 0 adds k w ((x - p) . n)^2 / 2 to the energy, w = its lumped mass
+ * (simkit's M argument) or 1. */
+typedef struct skg_contact_plane {
+  double p[3];  /* a point of the plane */
+  double n[3];  /* unit normal (the allowed side) */
+  double k;     /* spring stiffness */
+} skg_contact_plane;
+
+#define SKG_MAX_PLANES 4
+
+/* Per vertex of x (n,3) f64 against one plane, weights w = mass (n) or 1 when mass is null:
+ * energy_v (n) = k w d^2 / 2, grad (3n) = k w d n, hdiag (9n) = k w n n^T (row-major 3x3),
+ * under (n) = 1 where d = (x - p) . n < 0 (everything else 0).  Any output may be null.
+ * Replaces contact_springs_plane_energy / _gradient / _hessian (:44-200). */
+int skg_contact_plane_terms(const double* x, int64_t n, const skg_contact_plane* plane_h, const double* mass,
+                            double* energy_v, double* grad, double* hdiag, uint8_t* under, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* psd_project: simkit/psd_project.py:12-47                                */
 /* ---------------------------------------------------------------------- */
 /* Batched eigenvalue floor of symmetric d x d blocks (1 <= d <= 12) by cyclic
@@ -211,6 +232,9 @@ typedef struct skg_be_params {
                                1 BDF2 (simkit/integrators/bdf2.py:31-101): target from four
                                displacement levels (simkit/energies/kinetic.py:93-101) and
                                kinetic factor 9/4; needs u_prev2 and u_prev3 */
+  int32_t n_planes;         /* contact planes added to the potential (0..SKG_MAX_PLANES) */
+  int32_t contact_mass_weighted; /* 1: spring weight = lumped vertex mass; 0: 1 */
+  const skg_contact_plane* planes; /* host array of n_planes planes */
 } skg_be_params;
 
 typedef struct skg_be_state {
@@ -226,6 +250,7 @@ typedef struct skg_be_state {
                                ||g(x_tilde)|| */
   const double* u_prev2;    /* (3n) displacement at step k-2 (BDF2 only) */
   const double* u_prev3;    /* (3n) displacement at step k-3 (BDF2 only) */
+  const double* x_rest;     /* (3n) rest positions (needed with contact planes) */
 } skg_be_state;
 
 typedef struct skg_step_info {

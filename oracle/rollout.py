@@ -27,7 +27,7 @@ from dataclasses import dataclass
 import numpy as np
 import scipy.sparse as sps
 
-from . import fem, mmnh, snh
+from . import contact, fem, mmnh, snh
 from .solvers import BDF2_COEFF, bdf2_target, newton_solver, be_target
 
 
@@ -42,9 +42,13 @@ class StepInfo:
 class BeamRollout:
     """FP64 reference rollout of one beam instance."""
 
-    def __init__(self, X, T, mu, lam, rho, gravity, pinned, dt, tol=1e-6, max_newton=20, material="snh"):
+    def __init__(self, X, T, mu, lam, rho, gravity, pinned, dt, tol=1e-6, max_newton=20, material="snh",
+                 planes=None, contact_mass_weighted=True):
         # the elastic energy: 'snh' (stable_neo_hookean.py) or 'mmnh' (macklin_mueller_neo_hookean.py)
         self.energy = {"snh": snh, "mmnh": mmnh}[material]
+        # contact springs (contact_springs_plane.py): (k, p, n) per plane, weights = vertex masses or 1
+        self.planes = list(planes or [])
+        self.contact_mass_weighted = contact_mass_weighted
         self.X = np.asarray(X, dtype=np.float64)
         self.T = np.asarray(T)
         self.mu = np.asarray(mu, dtype=np.float64).reshape(-1, 1)
@@ -75,14 +79,29 @@ class BeamRollout:
         x[self.free] = y
         return x
 
+    def _contact_M(self):
+        return sps.diags(self.mass) if self.contact_mass_weighted else None
+
+    def contact_energy(self, x):
+        return sum(contact.energy(x, k, p, n, self._contact_M()) for k, p, n in self.planes)
+
+    def contact_gradient(self, x):
+        return sum(contact.gradient(x, k, p, n, self._contact_M()) for k, p, n in self.planes)
+
+    def contact_hessian(self, x):
+        return sum(contact.hessian(x, k, p, n, self._contact_M()) for k, p, n in self.planes)
+
     def potential(self, x) -> float:
-        return self.energy.energy_x(x, self.J, self.mu, self.lam, self.vol) - (self.f_ext.T @ x).item()
+        e = self.energy.energy_x(x, self.J, self.mu, self.lam, self.vol) - (self.f_ext.T @ x).item()
+        return e + (self.contact_energy(x) if self.planes else 0.0)
 
     def potential_gradient(self, x):
-        return self.energy.gradient_x(x, self.J, self.mu, self.lam, self.vol) - self.f_ext
+        g = self.energy.gradient_x(x, self.J, self.mu, self.lam, self.vol) - self.f_ext
+        return g + self.contact_gradient(x) if self.planes else g
 
     def potential_hessian(self, x):
-        return self.energy.hessian_x(x, self.J, self.mu, self.lam, self.vol)
+        K = self.energy.hessian_x(x, self.J, self.mu, self.lam, self.vol)
+        return (K + self.contact_hessian(x)).tocsr() if self.planes else K
 
     # inertial targets (overridable to plug in another implementation of the same formulas)
     def be_target(self, yc, yp, h):
@@ -154,6 +173,8 @@ class BeamRollout:
         return np.array(xs), infos
 
 
-def from_spec(spec, dt=1.0 / 60.0, tol=1e-6, max_newton=20, material="snh") -> BeamRollout:
+def from_spec(spec, dt=1.0 / 60.0, tol=1e-6, max_newton=20, material="snh", planes=None,
+              contact_mass_weighted=True) -> BeamRollout:
     return BeamRollout(spec.X, spec.T, spec.mu, spec.lam, spec.rho, spec.gravity, spec.pinned,
-                       dt, tol=tol, max_newton=max_newton, material=material)
+                       dt, tol=tol, max_newton=max_newton, material=material, planes=planes,
+                       contact_mass_weighted=contact_mass_weighted)

@@ -10,6 +10,8 @@ fallback.
 from __future__ import annotations
 
 import ctypes
+
+import numpy as np
 import os
 import threading
 
@@ -50,18 +52,23 @@ class TetMeshC(ctypes.Structure):
     ]
 
 
+class ContactPlaneC(ctypes.Structure):
+    _fields_ = [("p", c_dbl * 3), ("n", c_dbl * 3), ("k", c_dbl)]
+
+
 class BEParamsC(ctypes.Structure):
     _fields_ = [
         ("dt", c_dbl), ("tol", c_dbl), ("max_newton", c_i32), ("precision", c_i32), ("pcg_rtol", c_dbl),
         ("pcg_max_iter", c_i32), ("do_line_search", c_i32), ("ls_alpha", c_dbl), ("ls_beta", c_dbl),
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
         ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
+        ("n_planes", c_i32), ("contact_mass_weighted", c_i32), ("planes", ctypes.POINTER(ContactPlaneC)),
     ]
 
 
 class BEStateC(ctypes.Structure):
     _fields_ = [("u", c_vp), ("u_curr", c_vp), ("u_prev", c_vp), ("mass", c_vp), ("f_ext", c_vp), ("pinned", c_vp),
-                ("u_warm", c_vp), ("u_prev2", c_vp), ("u_prev3", c_vp)]
+                ("u_warm", c_vp), ("u_prev2", c_vp), ("u_prev3", c_vp), ("x_rest", c_vp)]
 
 
 class StepInfoC(ctypes.Structure):
@@ -89,6 +96,8 @@ _SIGNATURES = {
     "skg_mmnh_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_mmnh_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_psd_project": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
+    "skg_contact_plane_terms": (c_i32, [c_vp, c_i64, ctypes.POINTER(ContactPlaneC), c_vp, c_vp, c_vp, c_vp, c_vp,
+                                        c_vp]),
     "skg_tet_setup": (c_i32, [c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp]),
     "skg_tet_deformation_gradient": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "skg_tet_gradient_scatter": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp]),
@@ -169,3 +178,19 @@ def check(status: int):
             raise ValueError(msg)
         raise SimkitGpuError(status, msg)
     return status
+
+
+def contact_planes(planes):
+    """ctypes array of contact planes from (k, p, n) triples (n is normalised)."""
+    planes = list(planes or [])
+    if len(planes) > 4:
+        raise ValueError("at most 4 contact planes")
+    arr = (ContactPlaneC * max(len(planes), 1))()
+    for i, (k, p, n) in enumerate(planes):
+        p = np.asarray(p, dtype=np.float64).reshape(3)
+        n = np.asarray(n, dtype=np.float64).reshape(3)
+        n = n / np.linalg.norm(n)
+        arr[i].p[:] = list(p)
+        arr[i].n[:] = list(n)
+        arr[i].k = float(k)
+    return arr, len(planes)

@@ -339,6 +339,68 @@ def macklin_mueller_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] =
 
 
 # --------------------------------------------------------------------------- #
+# contact springs: simkit/energies/contact_springs_plane.py:44-200             #
+# --------------------------------------------------------------------------- #
+def _contact(X, k, p, n, M):
+    Xd = _dev(X)
+    nv = Xd.numel() // 3
+    if Xd.numel() != 3 * nv or (X.ndim == 2 and X.shape[1] != 3):
+        raise ValueError("the GPU contact springs support 3D positions")
+    arr, _ = _lib.contact_planes([(k, np.asarray(p).reshape(-1)[:3], np.asarray(n, dtype=np.float64).reshape(3))])
+    # simkit uses n as given (no normalisation)
+    arr[0].n[:] = list(np.asarray(n, dtype=np.float64).reshape(3))
+    m = None
+    if M is not None:
+        diag = M.diagonal() if sps.issparse(M) else np.diagonal(np.asarray(M))
+        m = _dev(np.asarray(diag, dtype=np.float64).reshape(-1))
+    return Xd.reshape(-1), nv, arr, m
+
+
+def _contact_inds(under):
+    idx = np.nonzero(under.cpu().numpy())[0]
+    return idx[:, None] if idx.size else None
+
+
+def contact_springs_plane_energy(X, k: float, p, n, M=None, return_contact_inds: bool = False):
+    """simkit ``contact_springs_plane_energy`` (contact_springs_plane.py:44-86): sum over vertices
+    below the plane of k m (n.(x - p))^2 / 2, m the diagonal of M (default identity)."""
+    Xd, nv, arr, m = _contact(X, k, p, n, M)
+    ev = torch.empty(nv, dtype=torch.float64, device="cuda")
+    under = torch.empty(nv, dtype=torch.uint8, device="cuda")
+    check(_lib.load().skg_contact_plane_terms(_ptr(Xd), nv, arr, _ptr(m), _ptr(ev), None, None, _ptr(under),
+                                              _stream_ptr()))
+    e = float(ev.cpu().numpy().sum())
+    return (e, _contact_inds(under)) if return_contact_inds else e
+
+
+def contact_springs_plane_gradient(X, k: float, p, n, M=None, return_contact_inds: bool = False):
+    """simkit ``contact_springs_plane_gradient`` (:87-130), (3n, 1)."""
+    Xd, nv, arr, m = _contact(X, k, p, n, M)
+    g = torch.empty(3 * nv, dtype=torch.float64, device="cuda")
+    under = torch.empty(nv, dtype=torch.uint8, device="cuda")
+    check(_lib.load().skg_contact_plane_terms(_ptr(Xd), nv, arr, _ptr(m), None, _ptr(g), None, _ptr(under),
+                                              _stream_ptr()))
+    out = _out(g.reshape(-1, 1), X)
+    return (out, _contact_inds(under)) if return_contact_inds else out
+
+
+def contact_springs_plane_hessian(X, k: float, p, n, M=None, return_contact_inds: bool = False):
+    """simkit ``contact_springs_plane_hessian`` (:131-200): block diagonal k m n n^T on the
+    vertices below the plane, scipy csc (3n x 3n)."""
+    Xd, nv, arr, m = _contact(X, k, p, n, M)
+    h = torch.empty(9 * nv, dtype=torch.float64, device="cuda")
+    under = torch.empty(nv, dtype=torch.uint8, device="cuda")
+    check(_lib.load().skg_contact_plane_terms(_ptr(Xd), nv, arr, _ptr(m), None, None, _ptr(h), _ptr(under),
+                                              _stream_ptr()))
+    hb = h.cpu().numpy().reshape(nv, 3, 3)
+    idx = np.nonzero(under.cpu().numpy())[0]
+    rows = (3 * idx[:, None, None] + np.arange(3)[None, :, None]).repeat(3, 2)
+    cols = (3 * idx[:, None, None] + np.arange(3)[None, None, :]).repeat(3, 1)
+    H = sps.csc_matrix((hb[idx].ravel(), (rows.ravel(), cols.ravel())), shape=(3 * nv, 3 * nv))
+    return (H, _contact_inds(under)) if return_contact_inds else H
+
+
+# --------------------------------------------------------------------------- #
 # material dispatch: simkit/energies/elastic.py                               #
 # --------------------------------------------------------------------------- #
 def _material(material):

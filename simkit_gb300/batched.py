@@ -34,7 +34,7 @@ class BatchedBESolver:
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
-                 integrator="be", material="stable-neo-hookean"):
+                 integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True):
         _lib.load()
         self.n_inst = len(specs)
         if self.n_inst == 0:
@@ -61,6 +61,7 @@ class BatchedBESolver:
                        device=device)
         mesh.set_energy(material)
         up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
+        self._contact_init = (contact_planes, contact_mass_weighted)
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
                     pcg_max_iter, do_line_search, ls_threshold, profile, integrator)
@@ -121,7 +122,16 @@ class BatchedBESolver:
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
             profile=int(profile), integrator=INTEGRATORS[integrator])
         self._infos = (StepInfoC * self.n_inst)()
+        init = getattr(self, "_contact_init", (None, True))
+        self.set_contact_planes(*init)
         self.steps = 0
+
+    def set_contact_planes(self, planes, mass_weighted=True):
+        """Contact springs against planes, each (k, p, n), for every instance."""
+        self._planes, n = _lib.contact_planes(planes)
+        self.params.n_planes = n
+        self.params.contact_mass_weighted = int(bool(mass_weighted))
+        self.params.planes = ctypes.cast(self._planes, ctypes.POINTER(_lib.ContactPlaneC))
 
     @property
     def n_tets(self):
@@ -142,7 +152,7 @@ class BatchedBESolver:
                       mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
                       u_warm=u_warm.data_ptr() if u_warm is not None else None,
                       u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
-                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None)
+                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
         total = StepInfoC()
         check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
                                               ctypes.byref(self.params), ctypes.byref(st),

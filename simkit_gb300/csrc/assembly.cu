@@ -131,6 +131,13 @@ __global__ void k_assemble(AsmArgs<R> a) {
     const R m = R(a.mass[v] * a.inv_h2);
     acc[0] += m; acc[4] += m; acc[8] += m;
   }
+  if (v == w && a.contact.n > 0) {
+    double x[3], hc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 3; ++i) x[i] = a.contact.X[3 * v + i] + a.u[3 * v + i];
+    contact_terms(a.contact, v, x, nullptr, hc);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) acc[k] += R(hc[k]);
+  }
   if (a.pinned) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -209,6 +216,11 @@ __global__ void __launch_bounds__(kBlock) k_vertex_gradient(GradArgs a) {
       acc[1] += f[1];
       acc[2] += f[2];
     }
+    if (a.contact.n > 0) {
+      double x[3];
+      for (int i = 0; i < 3; ++i) x[i] = a.contact.X[3 * v + i] + a.u[3 * v + i];
+      contact_terms(a.contact, v, x, acc, nullptr);
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const int64_t d = 3 * v + i;
@@ -275,6 +287,31 @@ __device__ __forceinline__ void vertex_energy_terms(const EnergyArgs<R>& a, int6
     acc[0] += kin + pot;
     acc[1] += kin + fabs(pot);
   }
+  if (a.contact.n > 0) {
+    double x[3];
+    for (int c = 0; c < 3; ++c) x[c] = a.contact.X[3 * v + c] + a.tet.u[3 * v + c] + step * dd[c];
+    const double ec = contact_terms(a.contact, v, x, nullptr, nullptr);
+    acc[0] += ec;
+    acc[1] += ec;
+  }
+}
+
+// standalone contact springs (simkit/energies/contact_springs_plane.py:44-200), one plane
+__global__ void k_contact_plane(const double* __restrict__ x, int64_t n, Contact c, double* __restrict__ ev,
+                                double* __restrict__ grad, double* __restrict__ hdiag, uint8_t* __restrict__ under) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n) return;
+  const double xv[3] = {x[3 * v], x[3 * v + 1], x[3 * v + 2]};
+  double g[3] = {0.0, 0.0, 0.0}, h[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const double e = contact_terms(c, v, xv, g, h);
+  const double d = (xv[0] - c.p[0][0]) * c.nrm[0][0] + (xv[1] - c.p[0][1]) * c.nrm[0][1] +
+                   (xv[2] - c.p[0][2]) * c.nrm[0][2];
+  if (ev) ev[v] = e;
+  if (grad)
+    for (int i = 0; i < 3; ++i) grad[3 * v + i] = g[i];
+  if (hdiag)
+    for (int k = 0; k < 9; ++k) hdiag[9 * v + k] = h[k];
+  if (under) under[v] = d < 0.0 ? 1 : 0;
 }
 
 template <typename R, bool DIRECT>
@@ -488,6 +525,23 @@ extern "C" {
 int64_t skg_assembly_workspace_size(const skg_tet_mesh* mesh, int precision) {
   if (check_mesh(mesh, precision) != SKG_OK) return -1;
   return carve_workspace(mesh, precision, nullptr).bytes;
+}
+
+int skg_contact_plane_terms(const double* x, int64_t n, const skg_contact_plane* plane_h, const double* mass,
+                            double* energy_v, double* grad, double* hdiag, uint8_t* under, void* stream) {
+  if (!x || !plane_h || n < 0) return fail(SKG_ERR_ARG, "contact_plane_terms: bad arguments");
+  if (n == 0) return SKG_OK;
+  Contact c{};
+  c.n = 1;
+  c.w = mass;
+  for (int i = 0; i < 3; ++i) {
+    c.p[0][i] = plane_h->p[i];
+    c.nrm[0][i] = plane_h->n[i];
+  }
+  c.k[0] = plane_h->k;
+  k_contact_plane<<<blocks_for(n), kBlock, 0, as_stream(stream)>>>(x, n, c, energy_v, grad, hdiag, under);
+  SKG_LAUNCHED();
+  return SKG_OK;
 }
 
 int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h, void* ws, void* stream) {

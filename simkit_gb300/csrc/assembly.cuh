@@ -30,6 +30,37 @@ template <typename R> struct TetArgs {
   int material;                // kMatSNH or kMatMMNH
 };
 
+// Contact springs against up to SKG_MAX_PLANES planes (simkit/energies/contact_springs_plane.py):
+// vertex v at x = X + u with d = (x - p) . n < 0 adds k w d^2 / 2, w = mass[v] or 1.
+struct Contact {
+  int n = 0;
+  const double* X = nullptr;      // rest positions (3n)
+  const double* w = nullptr;      // per-vertex weights (lumped masses) or null for 1
+  double p[SKG_MAX_PLANES][3];
+  double nrm[SKG_MAX_PLANES][3];
+  double k[SKG_MAX_PLANES];
+};
+
+// energy, gradient and Hessian (3x3, row-major) of the contact springs at vertex v, position x
+__device__ __forceinline__ double contact_terms(const Contact& c, int64_t v, const double* x, double* g,
+                                                double* h) {
+  double e = 0.0;
+  const double w = c.w ? c.w[v] : 1.0;
+  for (int q = 0; q < c.n; ++q) {
+    const double d = (x[0] - c.p[q][0]) * c.nrm[q][0] + (x[1] - c.p[q][1]) * c.nrm[q][1] +
+                     (x[2] - c.p[q][2]) * c.nrm[q][2];
+    if (!(d < 0.0)) continue;
+    const double kw = c.k[q] * w;
+    e += 0.5 * kw * d * d;
+    if (g)
+      for (int i = 0; i < 3; ++i) g[i] += kw * d * c.nrm[q][i];
+    if (h)
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) h[3 * i + j] += kw * c.nrm[q][i] * c.nrm[q][j];
+  }
+  return e;
+}
+
 template <typename R> struct AsmArgs {
   int64_t nb;
   const int32_t* bsr_row;
@@ -46,6 +77,8 @@ template <typename R> struct AsmArgs {
   R* jinv;               // optional: block-Jacobi inverses (9n)
   const int32_t* vert_inst;    // optional: instance of each block row (batched solves)
   const uint8_t* inst_active;  // optional: skip rows of inactive instances
+  Contact contact;             // contact springs on diagonal blocks (positions from u)
+  const double* u;             // displacement (needed with contact)
 };
 
 // Block record of the solver's SpMV: the 9 row-major entries of a 3x3 block,
@@ -72,6 +105,7 @@ struct GradArgs {
   double* partials;
   unsigned* counter;
   double* out;          // out[0] = ||g||^2
+  Contact contact;
 };
 
 template <typename R> struct EnergyArgs {
@@ -87,6 +121,7 @@ template <typename R> struct EnergyArgs {
   double* partials;
   unsigned* counter;
   double* out;          // out[0] = energy, out[1] = magnitude
+  Contact contact;
 };
 
 struct Workspace {

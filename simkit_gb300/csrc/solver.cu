@@ -607,6 +607,26 @@ __global__ void k_bdf2_init(const double* __restrict__ uc, const double* __restr
   u[i] = x;
 }
 
+// contact planes of the potential, from the parameters
+static int make_contact(const skg_be_params* prm, const skg_be_state* st, Contact* c) {
+  *c = Contact{};
+  if (prm->n_planes <= 0) return SKG_OK;
+  if (prm->n_planes > SKG_MAX_PLANES || !prm->planes)
+    return fail(SKG_ERR_ARG, "contact planes: 1..%d planes and their array", SKG_MAX_PLANES);
+  if (!st->x_rest) return fail(SKG_ERR_ARG, "contact planes need the rest positions");
+  c->n = prm->n_planes;
+  c->X = st->x_rest;
+  c->w = prm->contact_mass_weighted ? st->mass : nullptr;
+  for (int q = 0; q < c->n; ++q) {
+    for (int i = 0; i < 3; ++i) {
+      c->p[q][i] = prm->planes[q].p[i];
+      c->nrm[q][i] = prm->planes[q].n[i];
+    }
+    c->k[q] = prm->planes[q].k;
+  }
+  return SKG_OK;
+}
+
 static int check_integrator(const skg_be_params* prm, const skg_be_state* st) {
   if (prm->integrator != 0 && prm->integrator != 1) return fail(SKG_ERR_ARG, "integrator must be 0 (BE) or 1 (BDF2)");
   if (prm->integrator == 1 && (!st->u_prev2 || !st->u_prev3))
@@ -895,11 +915,15 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
   ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
   ga.partials = w.partials; ga.counter = w.counter; ga.out = w.scal + S_GG;
+  Contact contact;
+  SKG_TRY(make_contact(prm, st, &contact));
+  ga.contact = contact;
 
   EnergyArgs<R> ea{};
   if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
   else ea.tet = make_tet_args64(m, st->u);
   ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  ea.contact = contact;
   ea.partials = w.partials; ea.counter = w.counter; ea.out = w.scal + S_E;
 
   auto gradient = [&](double* gg) -> int {
@@ -978,6 +1002,8 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     aa.rec = rec;
     aa.mass = st->mass;
     aa.inv_h2 = inv_h2;
+    aa.contact = contact;
+    aa.u = st->u;
     aa.pinned = st->pinned;
     pt.begin();
     SKG_TRY(launch_assemble<R>(aa, s));
@@ -1297,10 +1323,14 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
   ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
   ga.partials = w.partials; ga.counter = w.counter; ga.out = w.scal + S_GG;
+  Contact contact;
+  SKG_TRY(make_contact(prm, st, &contact));
+  ga.contact = contact;
   EnergyArgs<R> ea{};
   if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
   else ea.tet = make_tet_args64(m, st->u);
   ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  ea.contact = contact;
   int launches = 1;
 
   auto gradient = [&]() -> int {
@@ -1419,6 +1449,8 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     aa.rec = rec;
     aa.mass = st->mass;
     aa.inv_h2 = inv_h2;
+    aa.contact = contact;
+    aa.u = st->u;
     aa.pinned = st->pinned;
     aa.vert_inst = bt->vert_inst;
     aa.inst_active = bw.active;

@@ -78,12 +78,13 @@ class BESolver:
     integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
         (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
     material : 'stable-neo-hookean' or 'macklin-mueller-neo-hookean' (simkit/energies/elastic.py names)
+    contact_planes : optional list of (k, p, n) contact-spring planes added to the potential
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
-                 material="stable-neo-hookean"):
+                 material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.set_energy(material)
@@ -117,8 +118,17 @@ class BESolver:
             ls_max_iter=100, pcg_mode=pcg_mode,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
             profile=int(profile), integrator=INTEGRATORS[integrator])
+        self.set_contact_planes(contact_planes, contact_mass_weighted)
         self.steps = 0
         self._host = None
+
+    def set_contact_planes(self, planes, mass_weighted=True):
+        """Contact springs against planes, each (k, p, n) (simkit/energies/contact_springs_plane.py);
+        mass_weighted: spring weights are the lumped vertex masses (simkit's M) instead of 1."""
+        self._planes, n = _lib.contact_planes(planes)
+        self.params.n_planes = n
+        self.params.contact_mass_weighted = int(bool(mass_weighted))
+        self.params.planes = ctypes.cast(self._planes, ctypes.POINTER(_lib.ContactPlaneC))
 
     @classmethod
     def from_spec(cls, spec, **kw):
@@ -129,7 +139,7 @@ class BESolver:
         st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
                       mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
                       u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
-                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None)
+                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
         info = StepInfoC()
         check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
                                       ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),

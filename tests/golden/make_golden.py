@@ -20,6 +20,8 @@ Fixtures written next to this script:
 * ``rollout_bdf2_small.npz``: 6x2x2 beam, 8 BDF2 steps from rest (the reference's BDF2 target and coefficient)
 * ``element_mmnh_3d.npz`` / ``element_mmnh_2d.npz``: Macklin-Mueller neo-Hookean element tier on the same F batches
 * ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
+* ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
+* ``rollout_contact_small.npz``: 6x2x2 beam falling onto a floor plane (contact springs), 14 steps
 """
 
 from __future__ import annotations
@@ -50,9 +52,10 @@ def _import_reference(path):
         from simkit.solvers import newton_solver
         from simkit.energies import kinetic
         from simkit.energies import macklin_mueller_neo_hookean as ref_mmnh
+        from simkit.energies import contact_springs_plane as ref_contact
     return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
                 volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic,
-                mmnh=ref_mmnh)
+                mmnh=ref_mmnh, contact=ref_contact)
 
 
 def element_cases(rng, d, t_each=32):
@@ -127,7 +130,28 @@ def make_beam_small(ref, out):
                         K_data=K.data, K_indices=K.indices, K_indptr=K.indptr)
 
 
-def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", material="snh"):
+def make_contact_plane(ref, out):
+    import scipy.sparse as sps
+    rng = np.random.default_rng(21)
+    X = rng.uniform(-1.0, 1.0, size=(200, 3))
+    m = rng.uniform(0.5, 2.0, size=200)
+    p = np.array([0.1, -0.2, 0.05])
+    n = np.array([0.2, 1.0, -0.3])
+    n = n / np.linalg.norm(n)
+    k = 370.0
+    c = ref["contact"]
+    out_d = {}
+    for tag, M in (("m", sps.diags(m)), ("i", None)):
+        e, inds = c.contact_springs_plane_energy(X, k, p, n, M=M, return_contact_inds=True)
+        g = c.contact_springs_plane_gradient(X, k, p, n, M=M)
+        H = c.contact_springs_plane_hessian(X, k, p, n, M=M).tocsr()
+        H.sort_indices()
+        out_d.update({f"energy_{tag}": np.array(e), f"grad_{tag}": g, f"inds_{tag}": inds,
+                      f"H_{tag}": H.toarray()})
+    np.savez_compressed(out, X=X, m=m, p=p, n=n, k=k, **out_d)
+
+
+def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", material="snh", planes=None):
     """The oracle harness with every FEM routine and the Newton step taken from the reference."""
     import scipy.sparse as sps
     from oracle.rollout import BeamRollout
@@ -154,18 +178,33 @@ def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", materia
             self.Mf = (self.S @ self.M @ self.S.T).tocsc()
 
         def potential(self, x):
-            return s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
+            e = s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
                 - (self.f_ext.T @ x).item()
+            return e + (self.contact_energy(x) if self.planes else 0.0)
 
         def potential_gradient(self, x):
-            return s.stable_neo_hookean_gradient_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
+            g = s.stable_neo_hookean_gradient_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol) \
                 - self.f_ext
+            return g + self.contact_gradient(x) if self.planes else g
 
         def potential_hessian(self, x):
-            return s.stable_neo_hookean_hessian_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
+            K = s.stable_neo_hookean_hessian_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
+            return (K + self.contact_hessian(x)).tocsr() if self.planes else K
 
         def elastic_energy(self, x):
             return s.stable_neo_hookean_energy_x(x.reshape(-1, 3), self.J, self.mu, self.lam, self.vol)
+
+        def contact_energy(self, x):
+            return sum(float(ref["contact"].contact_springs_plane_energy(x.reshape(-1, 3), k, p, n, M=self._contact_M()))
+                       for k, p, n in self.planes)
+
+        def contact_gradient(self, x):
+            return sum(ref["contact"].contact_springs_plane_gradient(x.reshape(-1, 3), k, p, n, M=self._contact_M())
+                       for k, p, n in self.planes)
+
+        def contact_hessian(self, x):
+            return sum(ref["contact"].contact_springs_plane_hessian(x.reshape(-1, 3), k, p, n, M=self._contact_M())
+                       for k, p, n in self.planes)
 
         def be_target(self, yc, yp, h):
             return ref["kinetic"].be_target(yc, yp, h)
@@ -174,6 +213,8 @@ def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", materia
             return ref["kinetic"].bdf2_target(yc, yp, yp2, yp3, h)
 
     r = RefRollout()
+    r.planes = list(planes or [])
+    r.contact_mass_weighted = True
     assert ref["kinetic"]._BDF2_COEFF == 9.0 / 4.0
     x_prev3 = r.x_rest.copy()
     x_prev2 = r.x_rest.copy()
@@ -224,6 +265,20 @@ def make_rollout_mmnh_small(ref, out):
                         ym=2e5, pr=0.45, dt=1.0 / 60.0)
 
 
+FLOOR = (1.0e4, (0.0, -0.004, 0.0), (0.0, 1.0, 0.0))   # k (mass weighted), point, normal
+
+
+def make_rollout_contact_small(ref, out):
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
+    planes = [(FLOOR[0], np.array(FLOOR[1]), np.array(FLOOR[2]))]
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 14, material="mmnh", planes=planes)
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
+                        ym=2e5, pr=0.45, dt=1.0 / 60.0, k=FLOOR[0], p=np.array(FLOOR[1]), n=np.array(FLOOR[2]))
+
+
 def make_rollout_c1(ref, out):
     from simkit_gb300.beams import beam_small_steady
     spec = beam_small_steady()
@@ -250,6 +305,8 @@ def main():
     make_element_mmnh(ref, 3, os.path.join(HERE, "element_mmnh_3d.npz"))
     make_element_mmnh(ref, 2, os.path.join(HERE, "element_mmnh_2d.npz"))
     make_rollout_mmnh_small(ref, os.path.join(HERE, "rollout_mmnh_small.npz"))
+    make_contact_plane(ref, os.path.join(HERE, "contact_plane.npz"))
+    make_rollout_contact_small(ref, os.path.join(HERE, "rollout_contact_small.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)

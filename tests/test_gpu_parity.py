@@ -276,6 +276,40 @@ def test_mmnh_be_step_matches_reference_rollout(api, precision):
         assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
 
 
+@pytest.mark.parametrize("tag", ["m", "i"])
+def test_contact_plane_drop_in_matches_reference(api, tag):
+    import scipy.sparse as sps
+    g = _load("contact_plane.npz")
+    M = sps.diags(g["m"]) if tag == "m" else None
+    k = float(g["k"])
+    e, inds = api.contact_springs_plane_energy(g["X"], k, g["p"], g["n"], M=M, return_contact_inds=True)
+    assert abs(e - float(g[f"energy_{tag}"])) < 1e-12 * abs(e)
+    assert np.array_equal(inds, g[f"inds_{tag}"])
+    assert _rel(api.contact_springs_plane_gradient(g["X"], k, g["p"], g["n"], M=M), g[f"grad_{tag}"]) < 1e-13
+    H = api.contact_springs_plane_hessian(g["X"], k, g["p"], g["n"], M=M)
+    assert _rel(H.toarray(), g[f"H_{tag}"]) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_contact_rollout_matches_reference(api, precision):
+    """Backward Euler with the Macklin-Mueller energy and a floor of contact springs on the device
+    against the reference's rollout (contact active from step 2)."""
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_contact_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    kw = dict(pcg_rtol=1e-10) if precision == "fp64" else {}
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, material="macklin-mueller-neo-hookean",
+                           contact_planes=[(float(d["k"]), d["p"], d["n"])], **kw)
+    X = spec.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, (step, info)
+        k = list(d["steps"]).index(step)
+        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5), step
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_rollout_8x8x32_matches_reference(api, precision):
     """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""

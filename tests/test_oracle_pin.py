@@ -128,6 +128,32 @@ def test_rollout_mmnh_small_matches_reference():
     assert [i.iters for i in infos] == list(d["iters"])
 
 
+@pytest.mark.parametrize("tag", ["m", "i"])
+def test_contact_plane_matches_reference(tag):
+    """Contact springs (contact_springs_plane.py:44-200) with vertex weights (M) and without."""
+    import scipy.sparse as sps
+    from oracle import contact
+    g = _load("contact_plane.npz")
+    M = sps.diags(g["m"]) if tag == "m" else None
+    k = float(g["k"])
+    assert abs(contact.energy(g["X"], k, g["p"], g["n"], M) - float(g[f"energy_{tag}"])) < 1e-12 * abs(float(g[f"energy_{tag}"]))
+    assert _rel(contact.gradient(g["X"], k, g["p"], g["n"], M), g[f"grad_{tag}"]) < 1e-13
+    assert _rel(contact.hessian(g["X"], k, g["p"], g["n"], M).toarray(), g[f"H_{tag}"]) < 1e-13
+
+
+def test_rollout_contact_small_matches_reference():
+    """A beam (Macklin-Mueller energy) falling onto a floor of contact springs."""
+    d = _load("rollout_contact_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    r = rollout.from_spec(spec, dt=float(d["dt"]), material="mmnh",
+                          planes=[(float(d["k"]), d["p"], d["n"])])
+    xs, infos = r.rollout(int(d["steps"].max()))
+    for k, s in enumerate(d["steps"]):
+        assert _rel(xs[s] - r.x_rest.ravel(), d["u"][k]) < 1e-8, s
+    assert [i.iters for i in infos] == list(d["iters"])
+
+
 def test_bdf2_target_is_exact_for_quadratic_motion():
     """The BDF2 velocity reconstruction is exact for quadratic motion (kinetic.py:63-101), so the
     target of x(t) = a + b t + c t^2 sampled at t = -3h..0 is x(h)."""
