@@ -22,6 +22,7 @@ Fixtures written next to this script:
 * ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
 * ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
 * ``rollout_contact_small.npz``: 6x2x2 beam falling onto a floor plane (contact springs), 14 steps
+* ``cache_reference.npz``: a cache file written by simkit's compute_with_cache_check (array, scalar, 1-element array)
 """
 
 from __future__ import annotations
@@ -279,6 +280,16 @@ def make_rollout_contact_small(ref, out):
                         ym=2e5, pr=0.45, dt=1.0 / 60.0, k=FLOOR[0], p=np.array(FLOOR[1]), n=np.array(FLOOR[2]))
 
 
+def make_cache_file(ref_path, out):
+    sys.path.insert(0, ref_path)
+    from simkit.filesystem.compute_with_cache_check import compute_with_cache_check
+    if os.path.exists(out):
+        os.remove(out)
+    rng = np.random.default_rng(31)
+    traj = rng.standard_normal((3, 5, 3))
+    compute_with_cache_check(lambda: (traj, 7, np.array([2.5]), np.arange(4)), out, read_cache=False)
+
+
 def make_rollout_c1(ref, out):
     from simkit_gb300.beams import beam_small_steady
     spec = beam_small_steady()
@@ -307,6 +318,7 @@ def main():
     make_rollout_mmnh_small(ref, os.path.join(HERE, "rollout_mmnh_small.npz"))
     make_contact_plane(ref, os.path.join(HERE, "contact_plane.npz"))
     make_rollout_contact_small(ref, os.path.join(HERE, "rollout_contact_small.npz"))
+    make_cache_file(a.reference, os.path.join(HERE, "cache_reference.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)
