@@ -215,7 +215,8 @@ typedef struct skg_be_params {
   int32_t ls_max_iter;      /* simkit default 100 */
   int32_t pcg_mode;         /* 0 kernel per phase, 1 grid-persistent cooperative kernel,
                                2 one thread-block cluster, 3 by size (2 up to 24,576 block
-                               rows, else 1), 4 grid-persistent Chronopoulos-Gear form */
+                               rows, else 5), 4 grid-persistent Chronopoulos-Gear form,
+                               5 grid-persistent with two barriers per iteration */
   double ls_threshold;      /* Armijo slack, simkit default 1e-12; < 0 selects a slack
                                scaled to the FP32 rounding of the energy sum */
   int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */

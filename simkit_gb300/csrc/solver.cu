@@ -579,6 +579,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) k_pcg_cg2(Bsr<R> A, PcgVecs<R> 
 }  // namespace skg
 
 #include "pcg_cluster.cuh"
+#include "pcg_grid.cuh"
 
 namespace skg {
 
@@ -792,8 +793,8 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
                      cudaStream_t s, PcgResult* res, int variant = 0) {
   const int rb = reduce_blocks(A.nbr);
-  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : 1;
-  if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 1;
+  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : 5;
+  if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 5;
   res->launches = 0;
   if (mode != 2) {
     k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal);
@@ -821,21 +822,24 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
     void* args[] = {&a2, &v2, &p2, &bar, &sc2};
     SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_cg2<R, kG>, dim3(grid), dim3(kCgThreads), args, 0, s));
     res->launches += 1;
-  } else if (mode == 1) {
-    // kernel variant: lanes per row G and rows in flight U (picked by the autotuner)
-    const void* kern = (const void*)k_pcg_persistent<R, 8, 1>;
+  } else if (mode == 1 || mode == 5) {
+    // kernel variant: lanes per row G and rows in flight U (picked by the autotuner);
+    // mode 5 is the two-barrier form (pcg_grid.cuh)
+#define SKG_PCG_KERN(G_, U_) (mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_> : (const void*)k_pcg_persistent<R, G_, U_>)
+    const void* kern = SKG_PCG_KERN(8, 1);
     int G = 8;
     switch (variant) {
-      case 1: kern = (const void*)k_pcg_persistent<R, 16, 1>; G = 16; break;
-      case 2: kern = (const void*)k_pcg_persistent<R, 8, 2>; G = 8; break;
-      case 3: kern = (const void*)k_pcg_persistent<R, 16, 2>; G = 16; break;
-      case 4: kern = (const void*)k_pcg_persistent<R, 4, 2>; G = 4; break;
-      case 5: kern = (const void*)k_pcg_persistent<R, 4, 4>; G = 4; break;
-      case 6: kern = (const void*)k_pcg_persistent<R, 2, 4>; G = 2; break;
-      case 7: kern = (const void*)k_pcg_persistent<R, 8, 4>; G = 8; break;
-      case 8: kern = (const void*)k_pcg_persistent<R, 2, 2>; G = 2; break;
+      case 1: kern = SKG_PCG_KERN(16, 1); G = 16; break;
+      case 2: kern = SKG_PCG_KERN(8, 2); G = 8; break;
+      case 3: kern = SKG_PCG_KERN(16, 2); G = 16; break;
+      case 4: kern = SKG_PCG_KERN(4, 2); G = 4; break;
+      case 5: kern = SKG_PCG_KERN(4, 4); G = 4; break;
+      case 6: kern = SKG_PCG_KERN(2, 4); G = 2; break;
+      case 7: kern = SKG_PCG_KERN(8, 4); G = 8; break;
+      case 8: kern = SKG_PCG_KERN(2, 2); G = 2; break;
       default: break;
     }
+#undef SKG_PCG_KERN
     int per_sm = 0;
     SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0));
     int64_t want = (A.nbr * G + kBlock - 1) / kBlock;

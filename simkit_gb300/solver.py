@@ -74,7 +74,8 @@ class BESolver:
     pcg_rtol : PCG relative tolerance; a negative value selects Eisenstat-Walker
         forcing capped at its magnitude
     pcg_mode : 0 kernel per phase, 1 grid-persistent, 2 one thread-block
-        cluster, 3 choose by size (cluster up to 24,576 block rows)
+        cluster, 3 choose by size (cluster up to 24,576 block rows, else 5),
+        5 grid-persistent with two barriers per iteration
     integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
         (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
     material : 'stable-neo-hookean' or 'macklin-mueller-neo-hookean' (simkit/energies/elastic.py names)

@@ -311,6 +311,24 @@ def test_contact_rollout_matches_reference(api, precision):
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_two_barrier_grid_pcg_matches_reference(api, precision):
+    """The two-barrier grid-persistent PCG (pcg_mode 5) on the 12,288-tet beam: 20 steps within the
+    same tolerances as the default path."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=5)
+    X = spec.X.reshape(-1)
+    for step in range(1, 21):
+        info = s.step()
+        assert info.converged, (step, info)
+        if step in d["steps"]:
+            k = list(d["steps"]).index(step)
+            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_rollout_8x8x32_matches_reference(api, precision):
     """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""
     from simkit_gb300.beams import beam_small_steady
