@@ -157,6 +157,48 @@ def dist_setup():
     return ws, rank, local
 
 
+class Ranks:
+    """Replica bookkeeping under torchrun: every rank steps its own independent meshes (no
+    data-path collective); the process group carries only the barriers around the timed region
+    and the max-over-ranks time.  Backend "nccl" on the GPUs, "gloo" for ranks on CPU."""
+
+    def __init__(self, backend="nccl"):
+        self.ws, self.rank, self.local = dist_setup()
+        self.dist = None
+        self.device = "cuda" if backend == "nccl" else "cpu"
+        if self.ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def whole_job_rate(self, units_per_rank: float, seconds_max: float) -> float:
+        """Units all ranks processed / the slowest rank's time."""
+        return units_per_rank * self.ws / seconds_max
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def replica_seed(rank: int) -> int:
+    """Seed of a rank's replica: rank 0 runs the published workload (seed 0), rank r its own
+    seeded draw of the same distribution."""
+    return int(rank)
+
+
 def algorithmic_bytes(spec, nb):
     n, t = spec.n_verts, spec.n_tets
     return {
@@ -229,6 +271,9 @@ def run_serving(args):
     request = completion of its 10th step - arrival.  Metric unit: instance-steps/s."""
     import torch
     from simkit_gb300.serving import BeamServer, request_stream
+    if dist_setup()[1] != 0:
+        # one server on one GPU: under torchrun the other ranks have no work
+        return 0
     torch.cuda.set_device(0)
     net, learned = (None, None)
     if args.learned:
@@ -270,8 +315,11 @@ def run_batched(args):
     from simkit_gb300.batched import BatchedBESolver
     from simkit_gb300.beams import beam_batch
     from simkit_gb300.solver import BESolver
-    torch.cuda.set_device(0)
-    specs = beam_batch(args.instances, seed=0)
+    n_ranks, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    ranks = Ranks("nccl")
+    # replicas: every rank steps its own seeded batch of the same distribution
+    specs = beam_batch(args.instances, seed=replica_seed(rank))
     b = BatchedBESolver(specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
     for _ in range(args.warmup):
         infos, total = b.step()
@@ -294,7 +342,8 @@ def run_batched(args):
         del st
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(local)
+    ranks.barrier()
     torch.cuda.synchronize()
     clocks.start()
     ev0.record(stream)
@@ -309,12 +358,13 @@ def run_batched(args):
         totals.append(total)
     ev1.record(stream)
     torch.cuda.synchronize()
+    ranks.barrier()
     clock_info = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
+    ms = ranks.max(ev0.elapsed_time(ev1))
     if any(t.status != 0 for t in totals):
         raise SystemExit(f"batched step failed: {[t.status for t in totals]}")
     inst_steps = args.instances * args.steps
-    value = inst_steps / (ms / 1000.0)
+    value = ranks.whole_job_rate(inst_steps, ms / 1000.0)
     # one extra profiled step (phase times by CUDA events; not part of the timed region)
     b.params.profile = 1
     if args.learned:
@@ -325,6 +375,9 @@ def run_batched(args):
     phase_ms = {k: getattr(prof, f"t_{k}_ms") for k in ("hessian", "assemble", "pcg", "gradient", "energy")}
     newton = sum(t.newton_iters for t in totals)
     tets = b.n_tets
+    if rank != 0:
+        ranks.close()
+        return 0
     # plain: the same beams one at a time (sample, state advanced to the same step count)
     rng = np.random.default_rng(1)
     sample = rng.choice(args.instances, size=min(args.plain_sample, args.instances), replace=False)
@@ -342,21 +395,23 @@ def run_batched(args):
         torch.cuda.synchronize()
         plain_ms.append(e0.elapsed_time(e1) / args.steps)
     plain_value = 1000.0 / float(np.mean(plain_ms))
+    ranks.close()
     line = {
-        "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": n_ranks, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": f"{args.instances} beams, nx, ny in 4..16, nz in 8..48, batched "
                                + ("+ learned warm start" if args.learned else "plain Newton"),
                    "instances": args.instances, "tets": int(tets), "verts": int(b.n_verts),
-                   "precision": args.precision, "pcg_rtol": args.pcg_rtol},
-        "tet_hessians_per_s": newton / max(args.instances, 1) * tets / (ms / 1000.0),
+                   "precision": args.precision, "pcg_rtol": args.pcg_rtol,
+                   "parallelism": f"replicas x{n_ranks}"},
+        "tet_hessians_per_s": n_ranks * newton / max(args.instances, 1) * tets / (ms / 1000.0),
         "newton_iters_per_instance_step": newton / inst_steps,
         "pcg_iters_per_instance_step": sum(t.pcg_iters for t in totals) / inst_steps,
         "batch_policy": {"vec_kb": policy[0], "min_cluster": policy[1], "step_ms_by_policy": policy_ms},
         "plain_single_instance": {"value": plain_value, "unit": "instance-steps/s",
                                   "sample": f"{len(sample)} of the beams stepped alone, {args.steps} steps each"},
-        "batched_over_plain": value / plain_value,
+        "batched_over_plain": value / n_ranks / plain_value,
         "learned": learned,
         "warm_start_kept_fraction": float(np.mean(kept)) if kept else None,
         "phase_ms_one_step": phase_ms,
@@ -404,15 +459,12 @@ def main():
     import torch
     ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    ranks = Ranks("nccl")
     from simkit_gb300.beams import beam_large_jittered, beam_small_steady
     from simkit_gb300.solver import BESolver
 
     # replicas only: every rank runs its own instance of the workload
-    spec = beam_small_steady() if args.small else beam_large_jittered(seed=rank)
+    spec = beam_small_steady() if args.small else beam_large_jittered(seed=replica_seed(rank))
     workload = "beam 8x8x32 cubes, 12,288 tets (quick check)" if args.small else WORKLOAD
     solver = BESolver.from_spec(spec, precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol,
                                 profile=False)
@@ -425,10 +477,7 @@ def main():
     from simkit_gb300.autotune import tune_pcg_variant
     variant, variant_us = tune_pcg_variant(solver, use_cache=not args.retune)
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
+    barrier = ranks.barrier
     stream = torch.cuda.current_stream()
     clocks = ClockSampler(local)
     barrier()
@@ -442,16 +491,12 @@ def main():
     barrier()
     clock_info = clocks.stop()
     ms = ev0.elapsed_time(ev1)
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = ranks.max(ms)
     for i in infos:
         if not i.converged:
             raise SystemExit(f"timed step did not converge: {i}")
     steps_total = args.steps * ws
-    value = steps_total / (ms_max / 1000.0)
+    value = ranks.whole_job_rate(args.steps, ms_max / 1000.0)
     newton = sum(i.newton_iters for i in infos)
     pcg = sum(i.pcg_iters for i in infos)
     launches = sum(i.launches for i in infos)
@@ -510,12 +555,8 @@ def main():
         x_prev, x_curr = x_curr, x_next.copy()
     torch.cuda.synchronize()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": steps_total / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 2 * 3 * spec.n_verts * 8,
+    e2e_s = ranks.max(time.perf_counter() - t0)
+    e2e = {"value": ranks.whole_job_rate(args.steps, e2e_s), "unit": "steps/s", "h2d_bytes_per_step": 2 * 3 * spec.n_verts * 8,
            "d2h_bytes_per_step": 3 * spec.n_verts * 8}
 
     cpu = None
@@ -544,8 +585,7 @@ def main():
             "clocks": clock_info,
         }
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
