@@ -431,6 +431,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--pcg-mode", type=int, default=3)
+    ap.add_argument("--coarse", default="auto",
+                    help="two-level PCG aggregates: none, auto, or a box size in mesh spacings")
+    ap.add_argument("--coarse-refresh", default="step", choices=["step", "newton"])
     ap.add_argument("--pcg-rtol", type=float, default=-0.1,
                     help="PCG tolerance; negative = Eisenstat-Walker forcing capped at its magnitude")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -466,8 +469,9 @@ def main():
     # replicas only: every rank runs its own instance of the workload
     spec = beam_small_steady() if args.small else beam_large_jittered(seed=replica_seed(rank))
     workload = "beam 8x8x32 cubes, 12,288 tets (quick check)" if args.small else WORKLOAD
+    coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
     solver = BESolver.from_spec(spec, precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol,
-                                profile=False)
+                                profile=False, coarse=coarse, coarse_refresh=args.coarse_refresh)
     nb = solver.mesh.nb
     for _ in range(args.warmup):
         info = solver.step()
@@ -574,6 +578,7 @@ def main():
             "config": {"workload": workload, "tets": spec.n_tets, "verts": spec.n_verts, "blocks": nb,
                        "precision": args.precision, "pcg_mode": args.pcg_mode, "pcg_rtol": args.pcg_rtol,
                        "pcg_variant": variant, "pcg_variant_us_per_iter": variant_us,
+                       "coarse_box": solver.coarse_box, "coarse_refresh": args.coarse_refresh,
                        "tol": 1e-6, "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2, no flush"},
             "tet_hessians_per_s": tet_hess_per_s,
             "newton_iters_per_step": newton / args.steps,

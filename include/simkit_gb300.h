@@ -156,6 +156,26 @@ typedef enum skg_material {
   SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN = 1 /* simkit/energies/macklin_mueller_neo_hookean.py */
 } skg_material;
 
+/* Two-level preconditioner data (optional; pcg_mode 7).  Vertices are grouped
+ * into aggregates; each aggregate carries 6 coarse unknowns, 3 translations and
+ * 3 rotations about its centroid, so (P e)_v = t_a + w_a x d_v on the free DOFs
+ * of v.  The PCG preconditioner becomes D^-1 + P (P^T A P)^-1 P^T with D the
+ * 3x3 block diagonal.  Built by the host from the rest positions, the pins and
+ * the block pattern (simkit_gb300/mesh.py: coarse_aggregates).  simkit solves
+ * the Newton systems with a direct solver (scipy spsolve in simkit/solvers/
+ * newton.py:52); this preconditioner is the GPU's replacement for that
+ * solver's robustness on stiff, heterogeneous meshes. */
+typedef struct skg_coarse {
+  int32_t n_agg;            /* aggregates; 6 n_agg coarse unknowns, at most 4096 */
+  int32_t n_cblocks;        /* nonzero 6x6 blocks of the coarse operator */
+  const float* mode;        /* (n, 4) per vertex: (d_x, d_y, d_z, bits) with d the offset from the
+                               aggregate centroid divided by the aggregate's RMS offset and bits
+                               (as uint32) = aggregate | free-DOF mask << 29 (bit c: DOF c free) */
+  const int32_t* cb_ptr;    /* (n_cblocks + 1) offsets into cb_slot */
+  const int32_t* cb_slot;   /* (n_blocks) fine block slots grouped by coarse block */
+  const int32_t* cb_rc;     /* (2 n_cblocks) aggregate row, aggregate column of each coarse block */
+} skg_coarse;
+
 typedef struct skg_tet_mesh {
   int64_t n_verts;
   int64_t n_tets;
@@ -176,6 +196,7 @@ typedef struct skg_tet_mesh {
   const int32_t* v2t_ptr;    /* (n+1) */
   const int32_t* v2t;        /* (4t) */
   int32_t material;          /* skg_material: the elastic energy of every tet */
+  const skg_coarse* coarse;  /* host pointer to the two-level preconditioner data, or NULL */
 } skg_tet_mesh;
 
 /* Assembled block matrix (3x3 blocks).  Values of block slot s of row v live at
@@ -216,7 +237,8 @@ typedef struct skg_be_params {
   int32_t pcg_mode;         /* 0 kernel per phase, 1 grid-persistent cooperative kernel,
                                2 one thread-block cluster, 3 by size (2 up to 24,576 block
                                rows, else 5), 4 grid-persistent Chronopoulos-Gear form,
-                               5 grid-persistent with two barriers per iteration */
+                               5 grid-persistent with two barriers per iteration,
+                               7 grid-persistent two-level (needs mesh->coarse; else 5) */
   double ls_threshold;      /* Armijo slack, simkit default 1e-12; < 0 selects a slack
                                scaled to the FP32 rounding of the energy sum */
   int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */
@@ -236,6 +258,8 @@ typedef struct skg_be_params {
   int32_t n_planes;         /* contact planes added to the potential (0..SKG_MAX_PLANES) */
   int32_t contact_mass_weighted; /* 1: spring weight = lumped vertex mass; 0: 1 */
   const skg_contact_plane* planes; /* host array of n_planes planes */
+  int32_t coarse_refresh;   /* pcg_mode 7: rebuild the coarse inverse 0 = at the first Newton
+                               iteration of each step, 1 = at every Newton iteration */
 } skg_be_params;
 
 typedef struct skg_be_state {

@@ -43,12 +43,18 @@ STATUS_NAMES = {
 }
 
 
+class CoarseC(ctypes.Structure):
+    _fields_ = [("n_agg", c_i32), ("n_cblocks", c_i32), ("mode", c_vp), ("cb_ptr", c_vp), ("cb_slot", c_vp),
+                ("cb_rc", c_vp)]
+
+
 class TetMeshC(ctypes.Structure):
     _fields_ = [
         ("n_verts", c_i64), ("n_tets", c_i64), ("n_blocks", c_i64),
         ("tets", c_vp), ("dinv", c_vp), ("dinv32", c_vp), ("vol", c_vp), ("mu", c_vp), ("lam", c_vp),
         ("mat32", c_vp), ("bsr_rowptr", c_vp), ("bsr_col", c_vp), ("bsr_diag", c_vp), ("bsr_row", c_vp),
         ("hc_ptr", c_vp), ("hc_src", c_vp), ("v2t_ptr", c_vp), ("v2t", c_vp), ("material", c_i32),
+        ("coarse", ctypes.POINTER(CoarseC)),
     ]
 
 
@@ -63,6 +69,7 @@ class BEParamsC(ctypes.Structure):
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
         ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
         ("n_planes", c_i32), ("contact_mass_weighted", c_i32), ("planes", ctypes.POINTER(ContactPlaneC)),
+        ("coarse_refresh", c_i32),
     ]
 
 

@@ -55,7 +55,9 @@ def _store(table):
 
 def _key(solver):
     bucket = 1 << max(0, int(solver.mesh.n - 1).bit_length())
-    return f"{torch.cuda.get_device_name()}|rows<={bucket}|prec={solver.precision}|mode={solver.params.pcg_mode}"
+    coarse = getattr(solver, "coarse_box", None)
+    return (f"{torch.cuda.get_device_name()}|rows<={bucket}|prec={solver.precision}|mode={solver.params.pcg_mode}"
+            f"|coarse={coarse}")
 
 
 def _history(solver):
@@ -68,7 +70,7 @@ def _history(solver):
 
 def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
     """Pick the fastest PCG kernel variant for ``solver``; returns (variant, timings_us)."""
-    if solver.params.pcg_mode not in (1, 3, 5) or (solver.params.pcg_mode == 3 and solver.mesh.n <= CLUSTER_ROWS):
+    if solver.params.pcg_mode not in (1, 3, 5, 7) or (solver.params.pcg_mode == 3 and solver.mesh.n <= CLUSTER_ROWS):
         return solver.params.pcg_variant, {}
     key = _key(solver)
     table = _load() if use_cache else {}

@@ -467,6 +467,16 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   w.partials = c.take<double>(8 * kMaxGrid);
   w.counter = c.take<unsigned>(16);
   w.scal = c.take<double>(64);
+  if (m->coarse) {
+    const int64_t np = coarse_padded(m);
+    w.cM = c.take<float>(np * np);
+    w.ccolp = c.take<float>(2 * np * 32);
+    w.crowp = c.take<float>(2 * 32 * np);
+    w.crc = c.take<unsigned long long>(np);
+    w.ce = c.take<float>(8 * (int64_t)m->coarse->n_agg);
+    w.cok = c.take<int>(4);
+    w.cbar = c.take<unsigned>(4);
+  }
   w.bytes = c.off + 256;
   return w;
 }
@@ -516,6 +526,12 @@ int check_mesh(const skg_tet_mesh* m, int precision) {
   if (precision != SKG_MIXED && precision != SKG_FP64) return fail(SKG_ERR_ARG, "unknown precision %d", precision);
   if (m->material != SKG_MAT_STABLE_NEO_HOOKEAN && m->material != SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN)
     return fail(SKG_ERR_ARG, "unknown material %d", m->material);
+  if (m->coarse) {
+    const skg_coarse* c = m->coarse;
+    if (c->n_agg <= 0 || 6 * (int64_t)c->n_agg > 4096 || c->n_cblocks < c->n_agg)
+      return fail(SKG_ERR_ARG, "coarse: %d aggregates (1..682 allowed), %d coarse blocks", c->n_agg, c->n_cblocks);
+    if (!c->mode || !c->cb_ptr || !c->cb_slot || !c->cb_rc) return fail(SKG_ERR_ARG, "coarse has a null array");
+  }
   return SKG_OK;
 }
 }  // namespace skg

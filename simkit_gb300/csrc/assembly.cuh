@@ -143,8 +143,21 @@ struct Workspace {
   double* partials;
   unsigned* counter;
   double* scal;
+  // two-level preconditioner (only with mesh->coarse)
+  float* cM;                 // np x np coarse operator / its inverse
+  float* ccolp;              // 2 x np x 32 Gauss-Jordan column panels
+  float* crowp;              // 2 x 32 x np row panels
+  unsigned long long* crc;   // np fixed-point coarse residual
+  float* ce;                 // 8 per aggregate: coarse correction
+  int* cok;                  // coarse inverse valid
+  unsigned* cbar;            // grid barrier of the inversion
   int64_t bytes;
 };
+
+// coarse unknowns padded to the Gauss-Jordan block (32)
+inline int64_t coarse_padded(const skg_tet_mesh* m) {
+  return m->coarse ? ((6 * (int64_t)m->coarse->n_agg + 31) / 32) * 32 : 0;
+}
 
 Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base);
 int check_mesh(const skg_tet_mesh* m, int precision);

@@ -1,0 +1,542 @@
+// Two-level additive preconditioner for the grid PCG:
+//
+//   M^-1 r = D^-1 r + P (P^T A P)^-1 P^T r
+//
+// D^-1 is the 3x3 block-Jacobi inverse the one-level solver uses.  P maps a
+// coarse vector (6 unknowns per aggregate of vertices: 3 translations t and 3
+// rotations w about the aggregate centroid) to the vertices,
+//   (P e)_v = m_v * (t_a + w_a x d_v),   a = aggregate of v,
+// with d_v the vertex offset from the centroid divided by the aggregate's RMS
+// offset and m_v the free-DOF mask (pinned DOFs get nothing).  Both terms are
+// symmetric positive (semi)definite, so M stays SPD and CG applies unchanged.
+//
+// Per refresh (first Newton iteration of a step, or every iteration):
+//   k_coarse_galerkin  A_c = P^T A P from the assembled blocks, one warp per
+//                      nonzero 6x6 coarse block, FP64 accumulation in a fixed
+//                      order (bitwise reproducible), small diagonal shift;
+//   k_coarse_invert    A_c^-1 in place by blocked Gauss-Jordan (SPD, no
+//                      pivoting, FP32), cooperative grid, one barrier per
+//                      32-wide pivot block.  A non-positive pivot clears the
+//                      valid flag and the PCG runs one-level.
+// Per PCG iteration (k_pcg_grid2c): the coarse residual P^T r accumulated in
+// 64-bit fixed point (order-independent, so reproducible), e = A_c^-1 P^T r by
+// a dense row-per-warp product, and P e added where the SpMV gathers form the
+// search direction.
+#pragma once
+
+namespace skg {
+
+constexpr int kCoarseMax = 4096;   // coarse unknowns the PCG stages in shared memory
+constexpr int kGjB = 32;           // Gauss-Jordan pivot block
+constexpr int kGjCols = 256;       // columns per Gauss-Jordan work unit (one per thread)
+constexpr double kCoarseShift = 1e-5;  // diagonal shift relative to the aggregate's largest diagonal
+
+struct CoarseDev {
+  int n_agg;                   // aggregates
+  int nc;                      // coarse unknowns, 6 n_agg
+  int np;                      // nc padded to a multiple of kGjB (identity in the padding)
+  int n_cb;                    // nonzero 6x6 coarse blocks
+  const float4* mode;          // (n): d_v (x, y, z); w bits: aggregate | free mask << 29
+  const int32_t* cb_ptr;       // (n_cb + 1)
+  const int32_t* cb_slot;      // fine block slots grouped by coarse block
+  const int32_t* cb_rc;        // (2 n_cb) aggregate row, column
+  const int32_t* bsr_row;      // block row of each fine slot
+  float* M;                    // np x np: A_c, inverted in place
+  float* colp;                 // 2 x np x kGjB column panels
+  float* rowp;                 // 2 x kGjB x np row panels
+  unsigned long long* rc;      // np: coarse residual in fixed point
+  float* e;                    // 8 n_agg: (t, w) per aggregate, padded to 8
+  int* ok;                     // 1 when M holds a valid inverse
+  unsigned* bar;               // 2: grid barrier of the inversion
+};
+
+__device__ __forceinline__ int mode_agg(float4 m) { return (int)(__float_as_uint(m.w) & 0x1fffffffu); }
+__device__ __forceinline__ unsigned mode_mask(float4 m) { return __float_as_uint(m.w) >> 29; }
+
+// ------------------------------------------------------------ Galerkin ----
+// C = P_v^T A'_vw P_w for one fine block, P_v = [I | -S(d_v)], S(d) = [d]x,
+// A' = diag(m_v) A diag(m_w):  C = [[A', -A' S_w], [S_v A', -S_v A' S_w]]
+__device__ __forceinline__ void skew(const float4 d, double (&S)[9]) {
+  S[0] = 0.0;          S[1] = -double(d.z); S[2] = double(d.y);
+  S[3] = double(d.z);  S[4] = 0.0;          S[5] = -double(d.x);
+  S[6] = -double(d.y); S[7] = double(d.x);  S[8] = 0.0;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev c) {
+  const int cb = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (cb >= c.n_cb) return;   // warp-uniform
+  double acc[36];
+#pragma unroll
+  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
+  const int k0 = c.cb_ptr[cb], k1 = c.cb_ptr[cb + 1];
+  for (int k = k0 + lane; k < k1; k += 32) {
+    const int s = c.cb_slot[k];
+    const Blk<R> blk = ld_rec(A.rec, s);
+    const int v = c.bsr_row[s], w = blk.col;
+    const float4 mv = c.mode[v], mw = c.mode[w];
+    const unsigned fv = mode_mask(mv), fw = mode_mask(mw);
+    double a[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) a[3 * i + j] = (((fv >> i) & 1u) && ((fw >> j) & 1u)) ? double(blk.m[3 * i + j]) : 0.0;
+    double Sv[9], Sw[9], B[9], SA[9];
+    skew(mv, Sv);
+    skew(mw, Sw);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        B[3 * i + j] = a[3 * i] * Sw[j] + a[3 * i + 1] * Sw[3 + j] + a[3 * i + 2] * Sw[6 + j];     // A' S_w
+        SA[3 * i + j] = Sv[3 * i] * a[j] + Sv[3 * i + 1] * a[3 + j] + Sv[3 * i + 2] * a[6 + j];    // S_v A'
+      }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        acc[6 * i + j] += a[3 * i + j];
+        acc[6 * i + 3 + j] -= B[3 * i + j];
+        acc[6 * (3 + i) + j] += SA[3 * i + j];
+        acc[6 * (3 + i) + 3 + j] -= Sv[3 * i] * B[j] + Sv[3 * i + 1] * B[3 + j] + Sv[3 * i + 2] * B[6 + j];
+      }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 36; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+  if (lane != 0) return;
+  const int ra = c.cb_rc[2 * cb], ca = c.cb_rc[2 * cb + 1];
+  if (ra == ca) {
+    // shift the diagonal by a small fraction of the aggregate's largest one, so
+    // rank-deficient aggregates (one vertex, collinear vertices) stay definite;
+    // an aggregate with no free DOF gets the identity
+    double dmax = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) dmax = fmax(dmax, acc[7 * i]);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) acc[7 * i] = dmax > 0.0 ? acc[7 * i] + kCoarseShift * dmax : 1.0;
+  }
+  float* out = c.M + (int64_t)(6 * ra) * c.np + 6 * ca;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) out[(int64_t)i * c.np + j] = float(acc[6 * i + j]);
+}
+
+// ------------------------------------------------------- Gauss-Jordan ----
+// Inverse of one SPD 32 x 32 block in shared memory (all threads of the
+// block take part, four elements each).  False if a pivot is not positive.
+__device__ __forceinline__ bool gj_inverse32(float (*a)[kGjB + 1]) {
+  bool good = true;
+  for (int p = 0; p < kGjB; ++p) {
+    __syncthreads();
+    const float d = a[p][p];
+    good = good && d > 0.f && isfinite(d);
+    const float inv = 1.f / d;
+    float nv[(kGjB * kGjB) / kGjCols];
+#pragma unroll
+    for (int r = 0; r < (kGjB * kGjB) / kGjCols; ++r) {
+      const int q = threadIdx.x + r * kGjCols, i = q >> 5, j = q & 31;
+      if (i == p && j == p) nv[r] = inv;
+      else if (i == p) nv[r] = a[p][j] * inv;
+      else if (j == p) nv[r] = -a[i][p] * inv;
+      else nv[r] = fmaf(-a[i][p] * inv, a[p][j], a[i][j]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < (kGjB * kGjB) / kGjCols; ++r) {
+      const int q = threadIdx.x + r * kGjCols;
+      a[q >> 5][q & 31] = nv[r];
+    }
+  }
+  __syncthreads();
+  return good;
+}
+
+// In-place inverse of the SPD np x np matrix c.M (np a multiple of 32; rows
+// nc..np-1 are padding set to the identity here).  Pivot blocks K of 32 in
+// order; with Pinv = (M_KK)^-1 and the step's old panels C = M[:, K] and
+// R = M[K, :]:
+//   M_KK <- Pinv,  M_Kj <- Pinv R_j,  M_iK <- -C_i Pinv,  M_ij <- M_ij - C_i Pinv R_j.
+// Work unit: 32 rows (one pivot-block row) x 256 columns, one column per
+// thread and the 32 rows in registers.  C and R come from double-buffered
+// panel copies written while the previous step updated those columns and
+// rows, so no unit reads what another unit of the same step writes and each
+// step ends in one grid barrier.  Every CTA inverts the pivot block itself
+// (same inputs, same order: the same Pinv everywhere).  Launched cooperatively
+// with kGjCols threads; c.ok is set to 1 only if every pivot was positive.
+__global__ void __launch_bounds__(kGjCols) k_coarse_invert(CoarseDev c, volatile double* err) {
+  __shared__ float piv[kGjB][kGjB + 1];
+  __shared__ float cs[kGjB][kGjB + 1];
+  __shared__ __align__(16) float vt[kGjB][kGjB];
+  const int np = c.np, nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols, units = nbk * ncu;
+  const int tid = threadIdx.x;
+  const int64_t gsz = (int64_t)gridDim.x * blockDim.x, g0 = blockIdx.x * (int64_t)blockDim.x + tid;
+  unsigned* count = c.bar;
+  volatile unsigned* gen = c.bar + 1;
+  bool good = true;
+  for (int64_t i = c.nc + g0; i < np; i += gsz) c.M[i * np + i] = 1.f;
+  if (!grid_barrier(count, gen, err)) return;
+  for (int64_t q = g0; q < (int64_t)np * kGjB; q += gsz) {
+    const int64_t i = q / kGjB;
+    const int k = (int)(q - i * kGjB);
+    c.colp[q] = c.M[i * np + k];
+    c.rowp[(int64_t)k * np + i] = c.M[(int64_t)k * np + i];
+  }
+  if (!grid_barrier(count, gen, err)) return;
+  for (int kb = 0; kb < nbk; ++kb) {
+    const float* C = c.colp + (int64_t)(kb & 1) * np * kGjB;
+    const float* Rw = c.rowp + (int64_t)(kb & 1) * kGjB * np;
+    float* Cn = c.colp + (int64_t)((kb + 1) & 1) * np * kGjB;
+    float* Rn = c.rowp + (int64_t)((kb + 1) & 1) * kGjB * np;
+    const int K0 = kb * kGjB, K1 = K0 + kGjB;
+    for (int q = tid; q < kGjB * kGjB; q += blockDim.x) piv[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + K0 + (q & 31)];
+    good = gj_inverse32(piv) && good;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+      const int ib = u / ncu, cu = u - ib * ncu;
+      const int I0 = ib * kGjB;
+      const bool pivrow = ib == kb;
+      __syncthreads();
+      if (!pivrow)
+        for (int q = tid; q < kGjB * kGjB; q += blockDim.x) cs[q >> 5][q & 31] = C[(int64_t)I0 * kGjB + q];
+      __syncthreads();
+      for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
+        const int k = q >> 5, i = q & 31;
+        float s;
+        if (pivrow) {
+          s = piv[i][k];
+        } else {
+          s = 0.f;
+#pragma unroll 8
+          for (int l = 0; l < kGjB; ++l) s = fmaf(cs[i][l], piv[l][k], s);
+        }
+        vt[k][i] = s;
+      }
+      __syncthreads();
+      const int j = cu * kGjCols + tid;
+      if (j >= np) continue;
+      float a[kGjB];
+      if (j >= K0 && j < K1) {
+#pragma unroll
+        for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? piv[i][j - K0] : -vt[j - K0][i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? 0.f : c.M[(int64_t)(I0 + i) * np + j];
+        const float sg = pivrow ? 1.f : -1.f;
+        for (int k = 0; k < kGjB; ++k) {
+          const float r = sg * Rw[(int64_t)k * np + j];
+          const float4* vk = reinterpret_cast<const float4*>(&vt[k][0]);
+#pragma unroll
+          for (int i4 = 0; i4 < kGjB / 4; ++i4) {
+            const float4 t = vk[i4];
+            a[4 * i4] = fmaf(t.x, r, a[4 * i4]);
+            a[4 * i4 + 1] = fmaf(t.y, r, a[4 * i4 + 1]);
+            a[4 * i4 + 2] = fmaf(t.z, r, a[4 * i4 + 2]);
+            a[4 * i4 + 3] = fmaf(t.w, r, a[4 * i4 + 3]);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kGjB; ++i) c.M[(int64_t)(I0 + i) * np + j] = a[i];
+      if (kb + 1 < nbk) {
+        if (j >= K1 && j < K1 + kGjB)
+#pragma unroll
+          for (int i = 0; i < kGjB; ++i) Cn[(int64_t)(I0 + i) * kGjB + (j - K1)] = a[i];
+        if (ib == kb + 1)
+#pragma unroll
+          for (int i = 0; i < kGjB; ++i) Rn[(int64_t)i * np + j] = a[i];
+      }
+    }
+    if (!grid_barrier(count, gen, err)) return;
+  }
+  if (blockIdx.x == 0 && tid == 0) *c.ok = good ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- PCG ----
+// (P e)_v for the coarse correction e of the current iteration (plain loads:
+// e is written earlier in the same kernel)
+__device__ __forceinline__ Vec3<float> prolong(const CoarseDev& c, int64_t v) {
+  const float4 m = __ldg(c.mode + v);
+  const int a = mode_agg(m);
+  const unsigned f = mode_mask(m);
+  const float4 e0 = reinterpret_cast<const float4*>(c.e)[2 * a];
+  const float4 e1 = reinterpret_cast<const float4*>(c.e)[2 * a + 1];
+  // t = (e0.x, e0.y, e0.z), w = (e0.w, e1.x, e1.y): t + w x d
+  const float px = e0.x + (e1.x * m.z - e1.y * m.y);
+  const float py = e0.y + (e1.y * m.x - e0.w * m.z);
+  const float pz = e0.z + (e0.w * m.y - e1.x * m.x);
+  return {(f & 1u) ? px : 0.f, (f & 2u) ? py : 0.f, (f & 4u) ? pz : 0.f};
+}
+
+// z_j = D^-1 r_j (stored) + (P e)_j, rounded the same wherever it is formed
+template <typename R> struct ZCoarse {
+  const R* z;
+  CoarseDev c;
+  bool on;
+  __device__ __forceinline__ Vec3<R> operator()(int64_t j) const {
+    Vec3<R> a = ld3c(z, j);
+    if (on) {
+      const Vec3<float> p = prolong(c, j);
+      a = {a.x + R(p.x), a.y + R(p.y), a.z + R(p.z)};
+    }
+    return a;
+  }
+};
+
+// Fixed-point scale of an iteration's coarse residual: a power of two putting
+// 64 ||r|| at 2^50 (|P^T r| of an aggregate is far below 2^12 ||r||, so sums
+// stay inside 64 bits with room for a residual that grows between iterations)
+__device__ __forceinline__ double coarse_scale(double rr) {
+  int ex;
+  frexp(64.0 * sqrt(fmax(rr, 1e-300)), &ex);
+  return ldexp(1.0, 50 - ex);
+}
+
+// c.rc += P^T r over the calling warp's rows (every lane calls; consecutive
+// rows of one aggregate are summed first by a segmented shuffle reduction, then
+// one 64-bit atomic per segment and component: integer sums do not depend on
+// the order of the atomics)
+__device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, int64_t row, float rx, float ry,
+                                                float rz, double scale) {
+  int key = -1;
+  long long q[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) q[k] = 0;
+  if (valid) {
+    const float4 m = __ldg(c.mode + row);
+    key = mode_agg(m);
+    const unsigned f = mode_mask(m);
+    const float x = (f & 1u) ? rx : 0.f, y = (f & 2u) ? ry : 0.f, z = (f & 4u) ? rz : 0.f;
+    // P_v^T r = (r, d x r)
+    const float v6[6] = {x, y, z, m.y * z - m.z * y, m.z * x - m.x * z, m.x * y - m.y * x};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) q[k] = __double2ll_rn(double(v6[k]) * scale);
+  }
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const unsigned heads = __ballot_sync(0xffffffffu, head);
+  const int seg = __popc(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int so = __shfl_down_sync(0xffffffffu, seg, o);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const long long t = __shfl_down_sync(0xffffffffu, q[k], o);
+      if (lane + o < 32 && so == seg) q[k] += t;
+    }
+  }
+  if (head && key >= 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) atomicAdd(c.rc + 6 * key + k, (unsigned long long)q[k]);
+}
+
+// e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows
+// strided over the grid), pc += (P^T r) . e over those rows.  rcf: shared
+// staging of P^T r (np floats).
+template <typename R>
+__device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, double inv_scale, Dacc<R>& pc) {
+  const int wpb = blockDim.x >> 5;
+  const int gw0 = blockIdx.x * wpb;
+  if (gw0 >= c.nc) return;   // block-uniform
+  for (int i = threadIdx.x; i < c.np; i += blockDim.x)
+    rcf[i] = i < c.nc ? float(double((long long)__ldcg(c.rc + i)) * inv_scale) : 0.f;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const float4* r4 = reinterpret_cast<const float4*>(rcf);
+  for (int row = gw0 + (threadIdx.x >> 5); row < c.nc; row += gridDim.x * wpb) {
+    const float4* Mr = reinterpret_cast<const float4*>(c.M + (int64_t)row * c.np);
+    float s = 0.f;
+    for (int j = lane; j < (c.np >> 2); j += 32) {
+      const float4 m = __ldcg(Mr + j), x = r4[j];
+      s = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, s))));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      c.e[8 * (row / 6) + row % 6] = s;
+      dacc_dot3(pc, Vec3<R>{R(rcf[row]), R(0), R(0)}, Vec3<R>{R(s), R(0), R(0)});
+    }
+  }
+}
+
+// Two-level PCG, grid-persistent.  Solve after k_pcg_init (x = 0, r, z = D^-1 r,
+// r.z in scal).  Per iteration three grid barriers:
+//   A  q = A p with p = (D^-1 r + P e) + beta p_prev formed in the gathers;
+//      p.q                                                     -> barrier 1
+//   B  x += alpha p, r -= alpha q, z = D^-1 r; r.z, r.r; P^T r -> barrier 2
+//   C  e = A_c^-1 P^T r; (P^T r).e                             -> barrier 3
+// with r.M^-1 r = r.D^-1 r + (P^T r).e.  When the coarse inverse is not valid
+// (c.ok == 0) phases C and the restriction are skipped: the one-level method.
+// partials: >= 4 gridDim + 4 accumulators of scratch.
+template <typename R, int G, int U>
+__global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v, CoarseDev c, double* partials,
+                                                       unsigned* bar, double* scal) {
+  __shared__ Dacc<R> wsum[2][kBlock / 32];
+  __shared__ __align__(16) float rcf[kCoarseMax];
+  Dacc<R>* PA = reinterpret_cast<Dacc<R>*>(partials);     // p.q per block
+  Dacc<R>* PB = PA + gridDim.x;                            // r.z, r.r per block
+  Dacc<R>* PC = PB + 2 * gridDim.x;                        // (P^T r).e per block
+  Dacc<R>* TOT = PC + gridDim.x;                           // [0] p.q, [1] r.z, [2] r.r, [3] (P^T r).e
+  unsigned* count = bar;
+  volatile unsigned* gen = bar + 1;
+  volatile double* err = scal + S_BAR_ERR;
+  const bool con = *c.ok != 0;
+  const double rz0 = scal[S_RZ];
+  Dacc<R> rz;
+  if constexpr (sizeof(R) == 4) {
+    const float h = float(rz0);
+    rz = Dacc<R>{h, float(rz0 - double(h))};
+  } else {
+    rz = Dacc<R>{R(rz0)};
+  }
+  const double tol2 = scal[S_TOL2];
+  R tol2r = R(tol2);
+  if (tol2 > 0.0 && !(tol2r > R(0))) tol2r = R(1e-45f);
+  const int max_iter = (int)scal[S_MAXIT];
+  int it = 0;
+  bool done = scal[S_DONE] != 0.0;
+  int status = 0;
+  const int lane = threadIdx.x & (G - 1);
+  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / G);
+  const int64_t row0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * (32 / G);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t wbase0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
+  Dacc<R> rr_acc;
+  dacc_zero(rr_acc);
+  double rr_final = scal[S_RR];
+  double rr_prev = scal[S_RR];
+  R beta = R(0);
+  int cur = 0;  // p_k in v.p (cur 0) or v.s (cur 1), p_{k-1} in the other
+  const ZCoarse<R> zf{v.z, c, con};
+  if (!done && con) {
+    // coarse part of z_0 = D^-1 r_0 + P e_0
+    const double sc = coarse_scale(rr_prev);
+    for (int64_t base = wbase0; base < A.nbr; base += stride) {
+      const int64_t i = base + (threadIdx.x & 31);
+      const bool ok = i < A.nbr;
+      const Vec3<R> r = ok ? ld3c(v.r, i) : Vec3<R>{R(0), R(0), R(0)};
+      coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
+    }
+    if (!grid_barrier(count, gen, err)) {
+      status = SKG_ERR_TIMEOUT;
+      done = true;
+    } else {
+      Dacc<R> pc[1];
+      dacc_zero(pc[0]);
+      coarse_product<R>(c, rcf, 1.0 / sc, pc[0]);
+      block_total<R, 1>(pc, wsum);
+      if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
+      Dacc<R> t3[1];
+      if (!grid_barrier_total<R, 1>(count, gen, err, PC, TOT + 3, t3, wsum)) {
+        status = SKG_ERR_TIMEOUT;
+        done = true;
+      } else {
+        rz = dacc_add(rz, t3[0]);
+      }
+    }
+  }
+  while (!done) {
+    const bool first = it == 0;
+    R* pk = cur ? v.s : v.p;
+    const R* pprev = cur ? v.p : v.s;
+    // the coarse residual was last read in phase C and is next written in phase B
+    if (con)
+      for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.np; i += stride) c.rc[i] = 0ull;
+    Dacc<R> pq[1];
+    dacc_zero(pq[0]);
+    for (int64_t base = row0; base < A.nbr; base += U * groups) {
+      int64_t rows[U];
+      bool val[U];
+      Vec3<R> ys[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        rows[u] = base + u * groups + ((threadIdx.x & 31) / G);
+        val[u] = rows[u] < A.nbr;
+      }
+      spmv_rows_dir<R, G, U>(A, zf, pprev, beta, first, rows, val, lane, ys);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (lane == 0 && val[u]) {
+          const Vec3<R> zi = zf(rows[u]);
+          const Vec3<R> p = first ? zi : pdir3(zi, ld3c(pprev, rows[u]), beta);
+          st3(pk, rows[u], p);
+          st3(v.q, rows[u], ys[u]);
+          dacc_dot3(pq[0], p, ys[u]);
+        }
+    }
+    block_total<R, 1>(pq, wsum);
+    if (threadIdx.x == 0) st_dacc(PA + blockIdx.x, pq[0]);
+    Dacc<R> t1[1];
+    if (!grid_barrier_total<R, 1>(count, gen, err, PA, TOT, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    const R pqr = dacc_r(t1[0]);
+    if (!(pqr > R(0)) || !isfinite(pqr)) {
+      status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
+      break;
+    }
+    const R a = dacc_r(rz) / pqr;
+    const double sc = coarse_scale(rr_prev);
+    Dacc<R> acc[2];
+    dacc_zero(acc[0]);
+    dacc_zero(acc[1]);
+    for (int64_t base = wbase0; base < A.nbr; base += stride) {
+      const int64_t i = base + (threadIdx.x & 31);
+      const bool ok = i < A.nbr;
+      Vec3<R> r{R(0), R(0), R(0)};
+      if (ok) {
+        Vec3<R> x = ld3c(v.x, i);
+        r = ld3c(v.r, i);
+        const Vec3<R> p = ld3c(pk, i), q = ld3c(v.q, i);
+        x = {x.x + a * p.x, x.y + a * p.y, x.z + a * p.z};
+        r = {r.x - a * q.x, r.y - a * q.y, r.z - a * q.z};
+        const Vec3<R> z = jacobi_apply(A.jinv, i, r);
+        st3(v.x, i, x);
+        st3(v.r, i, r);
+        st3(v.z, i, z);
+        dacc_dot3(acc[0], r, z);
+        dacc_dot3(acc[1], r, r);
+      }
+      if (con) coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
+    }
+    block_total<R, 2>(acc, wsum);
+    if (threadIdx.x == 0) {
+      st_dacc(PB + blockIdx.x, acc[0]);
+      st_dacc(PB + gridDim.x + blockIdx.x, acc[1]);
+    }
+    Dacc<R> t2[2];
+    if (!grid_barrier_total<R, 2>(count, gen, err, PB, TOT + 1, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    ++it;
+    rr_acc = t2[1];
+    rr_prev = dacc_value(t2[1]);
+    const R rrr = dacc_r(t2[1]);
+    const Dacc<R> rz_old = rz;
+    rz = t2[0];
+    if (!isfinite(rrr)) { status = SKG_ERR_NONFINITE; break; }
+    if (rrr <= tol2r || it >= max_iter) break;
+    if (con) {
+      Dacc<R> pc[1];
+      dacc_zero(pc[0]);
+      coarse_product<R>(c, rcf, 1.0 / sc, pc[0]);
+      block_total<R, 1>(pc, wsum);
+      if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
+      Dacc<R> t3[1];
+      if (!grid_barrier_total<R, 1>(count, gen, err, PC, TOT + 3, t3, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+      rz = dacc_add(rz, t3[0]);
+    }
+    beta = dacc_r(rz) / dacc_r(rz_old);
+    cur ^= 1;
+  }
+  if (it > 0) rr_final = dacc_value(rr_acc);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_ITERS] = it;
+    scal[S_RR] = rr_final;
+    scal[S_RZ] = dacc_value(rz);
+    scal[S_DONE] = 1.0;
+    if (status != 0) scal[S_STATUS] = status;
+    if (*err != 0.0) scal[S_STATUS] = *err;
+  }
+}
+
+}  // namespace skg

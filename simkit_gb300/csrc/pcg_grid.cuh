@@ -103,10 +103,16 @@ __device__ __forceinline__ bool grid_barrier_total(unsigned* count, volatile uns
   return ok != 0;
 }
 
+// preconditioned residual of a column as stored (one-level preconditioner)
+template <typename R> struct ZPlain {
+  const R* z;
+  __device__ __forceinline__ Vec3<R> operator()(int64_t j) const { return ld3c(z, j); }
+};
+
 // U block rows per lane group: y = A p_k with p_k = z + beta p_prev gathered per column
-// (p_prev skipped on the first iteration, where p_0 = z)
-template <typename R, int G, int U>
-__device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const R* __restrict__ z, const R* __restrict__ pp,
+// (p_prev skipped on the first iteration, where p_0 = z); zf(j) gives z_j
+template <typename R, int G, int U, class Zf>
+__device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const Zf& zf, const R* __restrict__ pp,
                                               R beta, bool first, const int64_t (&row)[U], const bool (&valid)[U],
                                               int lane, Vec3<R> (&y)[U]) {
   int p[U], K[U];
@@ -132,7 +138,7 @@ __device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const R* __restri
     for (int u = 0; u < U; ++u) {
       xv[u] = Vec3<R>{R(0), R(0), R(0)};
       if (k < K[u]) {
-        const Vec3<R> zc = ld3c(z, bk[u].col);
+        const Vec3<R> zc = zf(bk[u].col);
         xv[u] = first ? zc : pdir3(zc, ld3c(pp, bk[u].col), beta);
       }
     }
@@ -205,7 +211,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2(Bsr<R> A, PcgVecs<R> v,
         rows[u] = base + u * groups + ((threadIdx.x & 31) / G);
         val[u] = rows[u] < A.nbr;
       }
-      spmv_rows_dir<R, G, U>(A, v.z, pprev, beta, first, rows, val, lane, ys);
+      spmv_rows_dir<R, G, U>(A, ZPlain<R>{v.z}, pprev, beta, first, rows, val, lane, ys);
 #pragma unroll
       for (int u = 0; u < U; ++u)
         if (lane == 0 && val[u]) {

@@ -24,7 +24,7 @@ enum ScalarSlot {
   S_RZ = 0, S_PQ = 1, S_RR = 2, S_BB = 3, S_BETA = 4, S_TOL2 = 5, S_ITERS = 6, S_DONE = 7, S_STATUS = 8,
   S_MAXIT = 9, S_GG = 10, S_E = 12,      /* 12: energy, 13: magnitude */
   S_SLOPE = 14, S_TMP = 16,               /* 16..19 scratch reduction outputs */
-  S_BAR_ERR = 24
+  S_BAR_ERR = 24, S_CERR = 26
 };
 
 template <typename R> struct Bsr {
@@ -580,6 +580,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) k_pcg_cg2(Bsr<R> A, PcgVecs<R> 
 
 #include "pcg_cluster.cuh"
 #include "pcg_grid.cuh"
+#include "coarse.cuh"
 
 namespace skg {
 
@@ -744,6 +745,57 @@ constexpr int kGc = 4;  // lanes per block row in the cluster SpMV
 // systems up to this many block rows run PCG on one thread-block cluster
 constexpr int64_t kClusterAutoRows = 24576;
 
+// ------------------------------------------------- two-level coarse -----
+static CoarseDev make_coarse_dev(const skg_tet_mesh* m, const Workspace& w) {
+  CoarseDev c{};
+  const skg_coarse* h = m->coarse;
+  c.n_agg = h->n_agg;
+  c.nc = 6 * h->n_agg;
+  c.np = (int)coarse_padded(m);
+  c.n_cb = h->n_cblocks;
+  c.mode = reinterpret_cast<const float4*>(h->mode);
+  c.cb_ptr = h->cb_ptr;
+  c.cb_slot = h->cb_slot;
+  c.cb_rc = h->cb_rc;
+  c.bsr_row = m->bsr_row;
+  c.M = w.cM;
+  c.colp = w.ccolp;
+  c.rowp = w.crowp;
+  c.rc = w.crc;
+  c.e = w.ce;
+  c.ok = w.cok;
+  c.bar = w.cbar;
+  return c;
+}
+
+// A_c = P^T A P from the assembled records, then its inverse in place; on a
+// non-positive pivot (or a barrier timeout) c.ok stays 0 and the PCG runs
+// one-level.  Two launches.
+template <typename R>
+static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cudaStream_t s) {
+  SKG_CUDA(cudaMemsetAsync(c.M, 0, sizeof(float) * (size_t)c.np * c.np, s));
+  SKG_CUDA(cudaMemsetAsync(c.ok, 0, sizeof(int), s));
+  SKG_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), s));
+  SKG_CUDA(cudaMemsetAsync(scal + S_CERR, 0, sizeof(double), s));
+  const int64_t gal_threads = 32 * (int64_t)c.n_cb;
+  k_coarse_galerkin<R><<<(int)((gal_threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(A, c);
+  SKG_LAUNCHED();
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_invert, kGjCols, 0));
+    if (per_sm < 1) return fail(SKG_ERR_CUDA, "the coarse inversion kernel does not fit on an SM");
+  }
+  const int units = (c.np / kGjB) * ((c.np + kGjCols - 1) / kGjCols);
+  int grid = per_sm * num_sms();
+  if (grid > units) grid = units;
+  if (grid < 1) grid = 1;
+  CoarseDev c2 = c;
+  volatile double* err = scal + S_CERR;
+  void* args[] = {&c2, &err};
+  SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_coarse_invert, dim3(grid), dim3(kGjCols), args, 0, s));
+  return SKG_OK;
+}
+
 template <typename R>
 static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, R* xout,
                               double rtol, int max_iter, double* scal, cudaStream_t s) {
@@ -791,9 +843,10 @@ template <typename R> static int64_t cluster_rows_limit() {
 template <typename R>
 static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
-                     cudaStream_t s, PcgResult* res, int variant = 0) {
+                     cudaStream_t s, PcgResult* res, int variant = 0, const CoarseDev* cd = nullptr) {
   const int rb = reduce_blocks(A.nbr);
-  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : 5;
+  if (mode == 7 && !cd) mode = 5;
+  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : (cd ? 7 : 5);
   if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 5;
   res->launches = 0;
   if (mode != 2) {
@@ -822,10 +875,13 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
     void* args[] = {&a2, &v2, &p2, &bar, &sc2};
     SKG_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_cg2<R, kG>, dim3(grid), dim3(kCgThreads), args, 0, s));
     res->launches += 1;
-  } else if (mode == 1 || mode == 5) {
+  } else if (mode == 1 || mode == 5 || mode == 7) {
     // kernel variant: lanes per row G and rows in flight U (picked by the autotuner);
-    // mode 5 is the two-barrier form (pcg_grid.cuh)
-#define SKG_PCG_KERN(G_, U_) (mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_> : (const void*)k_pcg_persistent<R, G_, U_>)
+    // mode 5 is the two-barrier form (pcg_grid.cuh), mode 7 its two-level form (coarse.cuh)
+#define SKG_PCG_KERN(G_, U_)                                                   \
+  (mode == 7   ? (const void*)k_pcg_grid2c<R, G_, U_>                          \
+   : mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_>                           \
+               : (const void*)k_pcg_persistent<R, G_, U_>)
     const void* kern = SKG_PCG_KERN(8, 1);
     int G = 8;
     switch (variant) {
@@ -854,8 +910,15 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
     PcgVecs<R> v2 = v;
     double* p2 = partials;
     double* sc2 = scal;
-    void* args[] = {&a2, &v2, &p2, &bar, &sc2};
-    SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));
+    if (mode == 7) {
+      SKG_CUDA(cudaMemsetAsync(cd->rc, 0, sizeof(unsigned long long) * (size_t)cd->np, s));
+      CoarseDev c2 = *cd;
+      void* args[] = {&a2, &v2, &c2, &p2, &bar, &sc2};
+      SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));
+    } else {
+      void* args[] = {&a2, &v2, &p2, &bar, &sc2};
+      SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));
+    }
     res->launches += 1;
   } else {
     const int sb = (int)((A.nbr * kG + kBlock - 1) / kBlock);
@@ -955,6 +1018,10 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
 
   info->newton_iters = 0; info->pcg_iters = 0; info->ls_trials = 0; info->status = SKG_OK;
   info->min_alpha = 1.0;
+  // two-level PCG (mode 7, or mode 3 on systems above the cluster size) when the mesh has coarse data
+  const bool two_level = m->coarse && (prm->pcg_mode == 7 || (prm->pcg_mode == 3 && n > kClusterAutoRows));
+  CoarseDev cdev{};
+  if (two_level) cdev = make_coarse_dev(m, w);
   double gg;
   SKG_TRY(gradient(&gg));
   const double r0 = sqrt(gg);
@@ -1011,13 +1078,18 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     aa.pinned = st->pinned;
     pt.begin();
     SKG_TRY(launch_assemble<R>(aa, s));
-    info->t_assemble_ms += pt.end();
     info->launches += 2;
+    // coarse operator of the two-level preconditioner (timed with the assembly)
+    if (two_level && (it == 0 || prm->coarse_refresh)) {
+      SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s));
+      info->launches += 2;
+    }
+    info->t_assemble_ms += pt.end();
     // dx = -H^-1 g
     PcgResult pr{};
     pt.begin();
     SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, eta, prm->pcg_max_iter, prm->pcg_mode, w.partials,
-                         w.counter, w.scal, s, &pr, prm->pcg_variant));
+                         w.counter, w.scal, s, &pr, prm->pcg_variant, two_level ? &cdev : nullptr));
     info->t_pcg_ms += pt.end();
     info->launches += pr.launches;
     info->pcg_iters += pr.iters;

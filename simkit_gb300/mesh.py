@@ -77,6 +77,64 @@ def device_pattern(tets: torch.Tensor, n: int):
     return (rowptr.int(), col.int(), diag.int(), row.int(), hc_ptr, hc_src, v2t_ptr.int(), v2t)
 
 
+def coarse_aggregates(X, free_dof, rowptr, col, box=8, spacing=None, max_coarse=4096):
+    """Aggregates and coarse-operator pattern of the two-level preconditioner.
+
+    Vertices are grouped by the box of ``box`` x ``box`` x ``box`` mesh spacings their rest
+    position falls in (``spacing`` defaults to (bounding-box volume / n)^(1/3), the cell size of a
+    structured grid); each aggregate carries 3 translations and 3 rotations about its centroid.
+    The box grows until the 6 unknowns per aggregate fit in ``max_coarse``.
+
+    Returns a dict of host arrays: ``n_agg``; ``mode`` (n, 4) float32 whose w lane holds the uint32
+    bits aggregate | free-DOF mask << 29; ``cb_ptr``, ``cb_slot`` (fine block slots grouped by
+    coarse block, row-major over aggregate pairs), ``cb_rc`` (aggregate row, column per coarse
+    block); and ``box``, the box size used."""
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    n = X.shape[0]
+    free = np.asarray(free_dof, dtype=bool).reshape(n, 3)
+    lo = X.min(axis=0)
+    ext = np.maximum(X.max(axis=0) - lo, 1e-300)
+    if spacing is None:
+        spacing = float(np.prod(ext) / max(n, 1)) ** (1.0 / 3.0)
+        # flat or thin meshes: fall back to the largest extent per vertex
+        if not spacing > 0.0:
+            spacing = float(ext.max()) / max(n, 1)
+    while True:
+        h = box * spacing
+        ijk = np.floor((X - lo) / h + 0.5 / box).astype(np.int64)
+        keys = (ijk[:, 0] * (ijk[:, 1].max() + 1) + ijk[:, 1]) * (ijk[:, 2].max() + 1) + ijk[:, 2]
+        uk, agg = np.unique(keys, return_inverse=True)
+        n_agg = uk.size
+        if 6 * n_agg <= max_coarse:
+            break
+        box *= 2
+    agg = agg.astype(np.int64).reshape(-1)
+    cnt = np.bincount(agg, minlength=n_agg).astype(np.float64)
+    cen = np.stack([np.bincount(agg, weights=X[:, k], minlength=n_agg) for k in range(3)], 1) / cnt[:, None]
+    d = X - cen[agg]
+    rms = np.sqrt(np.bincount(agg, weights=(d * d).sum(1), minlength=n_agg) / cnt)
+    rms = np.where(rms > 0.0, rms, 1.0)
+    d = d / rms[agg][:, None]
+    mask = (free[:, 0].astype(np.uint32) | (free[:, 1].astype(np.uint32) << 1)
+            | (free[:, 2].astype(np.uint32) << 2))
+    bits = agg.astype(np.uint32) | (mask << np.uint32(29))
+    mode = np.empty((n, 4), np.float32)
+    mode[:, :3] = d
+    mode[:, 3] = bits.view(np.float32)
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    col = np.asarray(col, dtype=np.int64)
+    row = np.repeat(np.arange(n, dtype=np.int64), np.diff(rowptr))
+    ckey = agg[row] * n_agg + agg[col]
+    order = np.argsort(ckey, kind="stable")
+    ks = ckey[order]
+    starts = np.flatnonzero(np.r_[True, ks[1:] != ks[:-1]])
+    cb_keys = ks[starts]
+    cb_ptr = np.r_[starts, ks.size].astype(np.int32)
+    cb_rc = np.stack([cb_keys // n_agg, cb_keys % n_agg], 1).astype(np.int32).reshape(-1)
+    return {"n_agg": int(n_agg), "mode": mode, "cb_ptr": cb_ptr, "cb_slot": order.astype(np.int32),
+            "cb_rc": cb_rc, "box": box}
+
+
 class TetMesh:
     """Rest mesh of n vertices and t tets on one GPU.
 
@@ -170,6 +228,30 @@ class TetMesh:
         self._scalar_perm = None
 
     # ----------------------------------------------------------------- utils
+    def set_coarse(self, free_dof, box=8, spacing=None):
+        """Attach two-level preconditioner data (aggregates of ``box``^3 mesh spacings, 6 rigid
+        modes each) built from the rest positions, the free-DOF mask (3n, True = free) and the
+        block pattern.  Workspaces sized before this call are too small afterwards."""
+        if self.X_host is None:
+            self.X_host = self.X.cpu().numpy().reshape(-1, 3)
+        if self.rowptr_host is None:
+            self.rowptr_host = self.rowptr.cpu().numpy()
+            self.col_host = self.col.cpu().numpy()
+        cd = coarse_aggregates(self.X_host, free_dof, self.rowptr_host, self.col_host, box=box, spacing=spacing)
+        up = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(self.device)
+        self.coarse = {k: (up(v) if isinstance(v, np.ndarray) else v) for k, v in cd.items()}
+        self._coarse_c = _lib.CoarseC(
+            n_agg=cd["n_agg"], n_cblocks=int(cd["cb_ptr"].size - 1), mode=self.coarse["mode"].data_ptr(),
+            cb_ptr=self.coarse["cb_ptr"].data_ptr(), cb_slot=self.coarse["cb_slot"].data_ptr(),
+            cb_rc=self.coarse["cb_rc"].data_ptr())
+        self.c.coarse = ctypes.pointer(self._coarse_c)
+        return cd["n_agg"], cd["box"]
+
+    def clear_coarse(self):
+        self.c.coarse = None
+        self.coarse = None
+        self._coarse_c = None
+
     def set_energy(self, material):
         """Elastic energy of every tet: 0 / 'stable-neo-hookean', 1 / 'macklin-mueller-neo-hookean'."""
         code = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1}.get(material, material)

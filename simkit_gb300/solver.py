@@ -74,18 +74,24 @@ class BESolver:
     pcg_rtol : PCG relative tolerance; a negative value selects Eisenstat-Walker
         forcing capped at its magnitude
     pcg_mode : 0 kernel per phase, 1 grid-persistent, 2 one thread-block
-        cluster, 3 choose by size (cluster up to 24,576 block rows, else 5),
-        5 grid-persistent with two barriers per iteration
+        cluster, 3 choose by size (cluster up to 24,576 block rows, else 7 with coarse
+        data, else 5), 5 grid-persistent with two barriers per iteration, 7 its two-level form
     integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
         (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
     material : 'stable-neo-hookean' or 'macklin-mueller-neo-hookean' (simkit/energies/elastic.py names)
     contact_planes : optional list of (k, p, n) contact-spring planes added to the potential
+    coarse : two-level PCG preconditioner (block Jacobi + rigid-mode aggregates of box^3 mesh
+        spacings): None (one-level), 'auto' (box 8 on meshes above 24,576 vertices, used by
+        pcg_mode 3 there) or a box size (used by pcg_mode 3 above that size and by pcg_mode 7)
+    coarse_refresh : 'step' (coarse inverse rebuilt at the first Newton iteration of each step)
+        or 'newton' (at every Newton iteration)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
-                 material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True):
+                 material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
+                 coarse="auto", coarse_refresh="step"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.set_energy(material)
@@ -101,6 +107,11 @@ class BESolver:
         pv = np.asarray(pinned, dtype=np.int64).ravel()
         pin[(3 * pv[:, None] + np.arange(3)[None, :]).ravel()] = 1
         self.pinned = torch.from_numpy(pin).to(dev)
+        self.coarse_box = None
+        if coarse is not None and (coarse != "auto" or m.n > 24576):
+            _, self.coarse_box = m.set_coarse(pin == 0, box=8 if coarse == "auto" else int(coarse))
+        if coarse_refresh not in ("step", "newton"):
+            raise ValueError("coarse_refresh must be 'step' or 'newton'")
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
         self.u_curr = torch.zeros_like(self.u_prev)
         self.u_next = torch.zeros_like(self.u_prev)
@@ -118,7 +129,8 @@ class BESolver:
             pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
             ls_max_iter=100, pcg_mode=pcg_mode,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
-            profile=int(profile), integrator=INTEGRATORS[integrator])
+            profile=int(profile), integrator=INTEGRATORS[integrator],
+            coarse_refresh=int(coarse_refresh == "newton"))
         self.set_contact_planes(contact_planes, contact_mass_weighted)
         self.steps = 0
         self._host = None

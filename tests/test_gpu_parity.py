@@ -329,6 +329,49 @@ def test_two_barrier_grid_pcg_matches_reference(api, precision):
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("refresh", ["step", "newton"])
+def test_two_level_pcg_matches_reference(api, precision, refresh):
+    """The two-level grid PCG (pcg_mode 7: block Jacobi + rigid-mode aggregates of 4^3 cells,
+    coarse inverse by the Gauss-Jordan kernel) on the 12,288-tet beam: 20 steps within the same
+    tolerances as the default path, with fewer PCG iterations than the one-level grid form."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=7, coarse=4,
+                           coarse_refresh=refresh)
+    one = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=5)
+    assert s.coarse_box == 4
+    X = spec.X.reshape(-1)
+    pcg_two = pcg_one = 0
+    for step in range(1, 21):
+        info = s.step()
+        assert info.converged, (step, info)
+        info1 = one.step()
+        pcg_two += info.pcg_iters
+        pcg_one += info1.pcg_iters
+        if step in d["steps"]:
+            k = list(d["steps"]).index(step)
+            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+    print(f"\n{precision}/{refresh}: PCG iterations two-level {pcg_two}, one-level {pcg_one}")
+    assert 2 * pcg_two < pcg_one
+
+
+def test_two_level_repeatable(api):
+    """Two solvers with the same inputs take bitwise the same two-level steps (fixed-point
+    coarse residual, fixed-order Galerkin sums)."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    spec = beam_small_steady()
+    a = BESolver.from_spec(spec, pcg_mode=7, coarse=4)
+    b = BESolver.from_spec(spec, pcg_mode=7, coarse=4)
+    for _ in range(3):
+        ia, ib = a.step(), b.step()
+        assert ia.pcg_iters == ib.pcg_iters
+    assert torch.equal(a.u_curr, b.u_curr)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_rollout_8x8x32_matches_reference(api, precision):
     """The 12,288-tet beam, 60 steps: positions within 1e-5 relative at every stored step."""
     from simkit_gb300.beams import beam_small_steady
