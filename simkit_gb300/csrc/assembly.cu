@@ -155,8 +155,7 @@ __global__ void k_assemble(AsmArgs<R> a) {
 #pragma unroll
     for (int m = 0; m < 9; ++m) r[m] = acc[m];
     r[9] = col_bits(w, R(0));
-    r[10] = R(0);
-    r[11] = R(0);
+    rec_aux_store(r, a.cmode ? coarse_pack(__ldg(a.cmode + w)) : make_uint2(0u, 0u));
   }
   if (v == w && a.jinv) {
     R C[9];
@@ -470,7 +469,6 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   if (m->coarse) {
     const int64_t np = coarse_padded(m);
     w.cM = c.take<float>(np * np);
-    w.ccolp = c.take<float>(2 * np * 32);
     w.crowp = c.take<float>(2 * 32 * np);
     w.crc = c.take<unsigned long long>(np);
     w.ce = c.take<float>(8 * (int64_t)m->coarse->n_agg);

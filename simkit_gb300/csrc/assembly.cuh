@@ -1,6 +1,7 @@
 // Kernel argument bundles and launchers shared by the assembled tier and the
 // Newton solver.
 #pragma once
+#include <cuda_fp16.h>
 
 #include "common.cuh"
 
@@ -79,7 +80,28 @@ template <typename R> struct AsmArgs {
   const uint8_t* inst_active;  // optional: skip rows of inactive instances
   Contact contact;             // contact springs on diagonal blocks (positions from u)
   const double* u;             // displacement (needed with contact)
+  const float4* cmode;         // optional: two-level coarse data per vertex, packed into record slots 10-11
 };
+
+// A column's two-level coarse data in the two spare record slots (64 bits):
+// fp16 d_x | fp16 d_y << 16,  fp16 d_z | aggregate << 16 (13 bits) | free mask << 29.
+// The host rounds d to fp16 precision, so the packing is exact and every user
+// of d (coarse operator, restriction, prolongation) sees the same values.
+__device__ __forceinline__ uint2 coarse_pack(float4 m) {
+  const unsigned bits = __float_as_uint(m.w);
+  const unsigned hx = __half_as_ushort(__float2half_rn(m.x));
+  const unsigned hy = __half_as_ushort(__float2half_rn(m.y));
+  const unsigned hz = __half_as_ushort(__float2half_rn(m.z));
+  return make_uint2(hx | (hy << 16), hz | ((bits & 0x1fffu) << 16) | ((bits >> 29) << 29));
+}
+__device__ __forceinline__ void rec_aux_store(float* r, uint2 a) {
+  r[10] = __uint_as_float(a.x);
+  r[11] = __uint_as_float(a.y);
+}
+__device__ __forceinline__ void rec_aux_store(double* r, uint2 a) {
+  r[10] = __longlong_as_double((long long)(((unsigned long long)a.y << 32) | a.x));
+  r[11] = 0.0;
+}
 
 // Block record of the solver's SpMV: the 9 row-major entries of a 3x3 block,
 // the block column stored in the bits of entry 9, entries 10-11 zero, so one
@@ -145,7 +167,6 @@ struct Workspace {
   double* scal;
   // two-level preconditioner (only with mesh->coarse)
   float* cM;                 // np x np coarse operator / its inverse
-  float* ccolp;              // 2 x np x 32 Gauss-Jordan column panels
   float* crowp;              // 2 x 32 x np row panels
   unsigned long long* crc;   // np fixed-point coarse residual
   float* ce;                 // 8 per aggregate: coarse correction

@@ -12,7 +12,7 @@
 //
 // Per refresh (first Newton iteration of a step, or every iteration):
 //   k_coarse_galerkin  A_c = P^T A P from the assembled blocks, one warp per
-//                      nonzero 6x6 coarse block, FP64 accumulation in a fixed
+//                      nonzero 6x6 coarse block, FP32 products summed in FP64 in a fixed
 //                      order (bitwise reproducible), small diagonal shift;
 //   k_coarse_invert    A_c^-1 in place by blocked Gauss-Jordan (SPD, no
 //                      pivoting, FP32), cooperative grid, one barrier per
@@ -42,7 +42,6 @@ struct CoarseDev {
   const int32_t* cb_rc;        // (2 n_cb) aggregate row, column
   const int32_t* bsr_row;      // block row of each fine slot
   float* M;                    // np x np: A_c, inverted in place
-  float* colp;                 // 2 x np x kGjB column panels
   float* rowp;                 // 2 x kGjB x np row panels
   unsigned long long* rc;      // np: coarse residual in fixed point
   float* e;                    // 8 n_agg: (t, w) per aggregate, padded to 8
@@ -56,10 +55,10 @@ __device__ __forceinline__ unsigned mode_mask(float4 m) { return __float_as_uint
 // ------------------------------------------------------------ Galerkin ----
 // C = P_v^T A'_vw P_w for one fine block, P_v = [I | -S(d_v)], S(d) = [d]x,
 // A' = diag(m_v) A diag(m_w):  C = [[A', -A' S_w], [S_v A', -S_v A' S_w]]
-__device__ __forceinline__ void skew(const float4 d, double (&S)[9]) {
-  S[0] = 0.0;          S[1] = -double(d.z); S[2] = double(d.y);
-  S[3] = double(d.z);  S[4] = 0.0;          S[5] = -double(d.x);
-  S[6] = -double(d.y); S[7] = double(d.x);  S[8] = 0.0;
+__device__ __forceinline__ void skew(const float4 d, float (&S)[9]) {
+  S[0] = 0.f;   S[1] = -d.z; S[2] = d.y;
+  S[3] = d.z;   S[4] = 0.f;  S[5] = -d.x;
+  S[6] = -d.y;  S[7] = d.x;  S[8] = 0.f;
 }
 
 template <typename R>
@@ -77,12 +76,12 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
     const int v = c.bsr_row[s], w = blk.col;
     const float4 mv = c.mode[v], mw = c.mode[w];
     const unsigned fv = mode_mask(mv), fw = mode_mask(mw);
-    double a[9];
+    float a[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) a[3 * i + j] = (((fv >> i) & 1u) && ((fw >> j) & 1u)) ? double(blk.m[3 * i + j]) : 0.0;
-    double Sv[9], Sw[9], B[9], SA[9];
+      for (int j = 0; j < 3; ++j) a[3 * i + j] = (((fv >> i) & 1u) && ((fw >> j) & 1u)) ? float(blk.m[3 * i + j]) : 0.f;
+    float Sv[9], Sw[9], B[9], SA[9];
     skew(mv, Sv);
     skew(mw, Sw);
 #pragma unroll
@@ -96,10 +95,10 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        acc[6 * i + j] += a[3 * i + j];
-        acc[6 * i + 3 + j] -= B[3 * i + j];
-        acc[6 * (3 + i) + j] += SA[3 * i + j];
-        acc[6 * (3 + i) + 3 + j] -= Sv[3 * i] * B[j] + Sv[3 * i + 1] * B[3 + j] + Sv[3 * i + 2] * B[6 + j];
+        acc[6 * i + j] += double(a[3 * i + j]);
+        acc[6 * i + 3 + j] -= double(B[3 * i + j]);
+        acc[6 * (3 + i) + j] += double(SA[3 * i + j]);
+        acc[6 * (3 + i) + 3 + j] -= double(Sv[3 * i] * B[j] + Sv[3 * i + 1] * B[3 + j] + Sv[3 * i + 2] * B[6 + j]);
       }
   }
 #pragma unroll
@@ -156,129 +155,188 @@ __device__ __forceinline__ bool gj_inverse32(float (*a)[kGjB + 1]) {
 }
 
 // In-place inverse of the SPD np x np matrix c.M (np a multiple of 32; rows
-// nc..np-1 are padding set to the identity here).  Pivot blocks K of 32 in
-// order; with Pinv = (M_KK)^-1 and the step's old panels C = M[:, K] and
-// R = M[K, :]:
-//   M_KK <- Pinv,  M_Kj <- Pinv R_j,  M_iK <- -C_i Pinv,  M_ij <- M_ij - C_i Pinv R_j.
-// Work unit: 32 rows (one pivot-block row) x 256 columns, one column per
-// thread and the 32 rows in registers.  C and R come from double-buffered
-// panel copies written while the previous step updated those columns and
-// rows, so no unit reads what another unit of the same step writes and each
-// step ends in one grid barrier.  Every CTA inverts the pivot block itself
-// (same inputs, same order: the same Pinv everywhere).  Launched cooperatively
-// with kGjCols threads; c.ok is set to 1 only if every pivot was positive.
+// nc..np-1 are padding set to the identity here) by the symmetric sweep: pivot
+// blocks K of 32 in order, with Pinv = (M_KK)^-1, the step's old row panel
+// R = M[K, :] and C = R^T,
+//   M_KK <- -Pinv,  M_Kj <- Pinv R_j,  M_iK <- C_i Pinv,  M_ij <- M_ij - C_i Pinv R_j,
+// which keeps M symmetric, so only the upper triangle of 32-row blocks is
+// updated; after the last step M = -A^-1 there, and a mirror pass writes the
+// full A^-1.  Work unit: 32 rows (one block row) x 256 columns from the
+// diagonal block on, one column per thread and the 32 rows in registers.  R
+// comes from a double-buffered copy the previous step wrote (row K+1 from its
+// own block row, the part left of the diagonal from column block K+1 of the
+// rows above, transposed), so no unit reads what another unit of the same step
+// writes and each step ends in one grid barrier.  Every CTA inverts the pivot
+// block itself (same inputs, same order: the same Pinv everywhere).  Launched
+// cooperatively with kGjCols threads; c.ok is set to 1 only if every pivot was
+// positive.
 __global__ void __launch_bounds__(kGjCols) k_coarse_invert(CoarseDev c, volatile double* err) {
   __shared__ float piv[kGjB][kGjB + 1];
-  __shared__ float cs[kGjB][kGjB + 1];
+  __shared__ float rs[kGjB][kGjB + 1];
   __shared__ __align__(16) float vt[kGjB][kGjB];
-  const int np = c.np, nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols, units = nbk * ncu;
+  __shared__ int ustart[kCoarseMax / kGjB + 1];   // first unit of each block row (upper triangle)
+  const int np = c.np, nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols;
   const int tid = threadIdx.x;
+  if (tid == 0) {
+    int acc = 0;
+    for (int ib = 0; ib < nbk; ++ib) {
+      ustart[ib] = acc;
+      acc += ncu - (ib * kGjB) / kGjCols;
+    }
+    ustart[nbk] = acc;
+  }
+  __syncthreads();
+  const int units = ustart[nbk];
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x, g0 = blockIdx.x * (int64_t)blockDim.x + tid;
   unsigned* count = c.bar;
   volatile unsigned* gen = c.bar + 1;
   bool good = true;
   for (int64_t i = c.nc + g0; i < np; i += gsz) c.M[i * np + i] = 1.f;
   if (!grid_barrier(count, gen, err)) return;
-  for (int64_t q = g0; q < (int64_t)np * kGjB; q += gsz) {
-    const int64_t i = q / kGjB;
-    const int k = (int)(q - i * kGjB);
-    c.colp[q] = c.M[i * np + k];
-    c.rowp[(int64_t)k * np + i] = c.M[(int64_t)k * np + i];
-  }
+  for (int64_t q = g0; q < (int64_t)np * kGjB; q += gsz) c.rowp[q] = c.M[q];   // rows 0..31
   if (!grid_barrier(count, gen, err)) return;
   for (int kb = 0; kb < nbk; ++kb) {
-    const float* C = c.colp + (int64_t)(kb & 1) * np * kGjB;
     const float* Rw = c.rowp + (int64_t)(kb & 1) * kGjB * np;
-    float* Cn = c.colp + (int64_t)((kb + 1) & 1) * np * kGjB;
     float* Rn = c.rowp + (int64_t)((kb + 1) & 1) * kGjB * np;
     const int K0 = kb * kGjB, K1 = K0 + kGjB;
     for (int q = tid; q < kGjB * kGjB; q += blockDim.x) piv[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + K0 + (q & 31)];
     good = gj_inverse32(piv) && good;
+    int ib = 0;
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
-      const int ib = u / ncu, cu = u - ib * ncu;
+      while (ustart[ib + 1] <= u) ++ib;   // units are visited in increasing order
       const int I0 = ib * kGjB;
+      const int cu = I0 / kGjCols + (u - ustart[ib]);
       const bool pivrow = ib == kb;
-      __syncthreads();
-      if (!pivrow)
-        for (int q = tid; q < kGjB * kGjB; q += blockDim.x) cs[q >> 5][q & 31] = C[(int64_t)I0 * kGjB + q];
-      __syncthreads();
-      for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
-        const int k = q >> 5, i = q & 31;
-        float s;
-        if (pivrow) {
-          s = piv[i][k];
-        } else {
-          s = 0.f;
+      {
+        __syncthreads();
+        if (!pivrow)
+          for (int q = tid; q < kGjB * kGjB; q += blockDim.x) rs[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + I0 + (q & 31)];
+        __syncthreads();
+        for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
+          const int k = q >> 5, i = q & 31;
+          float sacc;
+          if (pivrow) {
+            sacc = piv[i][k];
+          } else {
+            // V = C_I Pinv with C_I[i][l] = R[l][I0 + i]
+            sacc = 0.f;
 #pragma unroll 8
-          for (int l = 0; l < kGjB; ++l) s = fmaf(cs[i][l], piv[l][k], s);
+            for (int l = 0; l < kGjB; ++l) sacc = fmaf(rs[l][i], piv[l][k], sacc);
+          }
+          vt[k][i] = sacc;
         }
-        vt[k][i] = s;
-      }
-      __syncthreads();
-      const int j = cu * kGjCols + tid;
-      if (j >= np) continue;
-      float a[kGjB];
-      if (j >= K0 && j < K1) {
+        __syncthreads();
+        const int j = cu * kGjCols + tid;
+        if (j < I0 || j >= np) continue;
+        float a[kGjB];
+        if (j >= K0 && j < K1) {
 #pragma unroll
-        for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? piv[i][j - K0] : -vt[j - K0][i];
-      } else {
+          for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? -piv[i][j - K0] : vt[j - K0][i];
+        } else {
 #pragma unroll
-        for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? 0.f : c.M[(int64_t)(I0 + i) * np + j];
-        const float sg = pivrow ? 1.f : -1.f;
-        for (int k = 0; k < kGjB; ++k) {
-          const float r = sg * Rw[(int64_t)k * np + j];
-          const float4* vk = reinterpret_cast<const float4*>(&vt[k][0]);
+          for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? 0.f : c.M[(int64_t)(I0 + i) * np + j];
+            const float sg = pivrow ? 1.f : -1.f;
+          float rv[kGjB];
 #pragma unroll
-          for (int i4 = 0; i4 < kGjB / 4; ++i4) {
-            const float4 t = vk[i4];
-            a[4 * i4] = fmaf(t.x, r, a[4 * i4]);
-            a[4 * i4 + 1] = fmaf(t.y, r, a[4 * i4 + 1]);
-            a[4 * i4 + 2] = fmaf(t.z, r, a[4 * i4 + 2]);
-            a[4 * i4 + 3] = fmaf(t.w, r, a[4 * i4 + 3]);
+          for (int k = 0; k < kGjB; ++k) rv[k] = Rw[(int64_t)k * np + j];
+#pragma unroll
+          for (int k = 0; k < kGjB; ++k) {
+            const float r = sg * rv[k];
+            const float4* vk = reinterpret_cast<const float4*>(&vt[k][0]);
+#pragma unroll
+            for (int i4 = 0; i4 < kGjB / 4; ++i4) {
+              const float4 t = vk[i4];
+              a[4 * i4] = fmaf(t.x, r, a[4 * i4]);
+              a[4 * i4 + 1] = fmaf(t.y, r, a[4 * i4 + 1]);
+              a[4 * i4 + 2] = fmaf(t.z, r, a[4 * i4 + 2]);
+              a[4 * i4 + 3] = fmaf(t.w, r, a[4 * i4 + 3]);
+            }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < kGjB; ++i) c.M[(int64_t)(I0 + i) * np + j] = a[i];
+        if (kb + 1 < nbk) {
+          if (ib == kb + 1) {
+#pragma unroll
+            for (int i = 0; i < kGjB; ++i) Rn[(int64_t)i * np + j] = a[i];
+          } else if (ib < kb + 1 && j >= K1 && j < K1 + kGjB) {
+            float4* dst = reinterpret_cast<float4*>(Rn + (int64_t)(j - K1) * np + I0);
+#pragma unroll
+            for (int i4 = 0; i4 < kGjB / 4; ++i4)
+              dst[i4] = make_float4(a[4 * i4], a[4 * i4 + 1], a[4 * i4 + 2], a[4 * i4 + 3]);
           }
         }
       }
-#pragma unroll
-      for (int i = 0; i < kGjB; ++i) c.M[(int64_t)(I0 + i) * np + j] = a[i];
-      if (kb + 1 < nbk) {
-        if (j >= K1 && j < K1 + kGjB)
-#pragma unroll
-          for (int i = 0; i < kGjB; ++i) Cn[(int64_t)(I0 + i) * kGjB + (j - K1)] = a[i];
-        if (ib == kb + 1)
-#pragma unroll
-          for (int i = 0; i < kGjB; ++i) Rn[(int64_t)i * np + j] = a[i];
-      }
     }
     if (!grid_barrier(count, gen, err)) return;
+  }
+  // mirror: A^-1 = -M on the upper block triangle, transposed below it
+  for (int t = blockIdx.x; t < nbk * nbk; t += gridDim.x) {
+    const int ib = t / nbk, jb = t - ib * nbk;
+    if (jb < ib) continue;   // block-uniform
+    __syncthreads();
+    for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
+      const int i = q >> 5, j = q & 31;
+      float* m = c.M + (int64_t)(ib * kGjB + i) * np + jb * kGjB + j;
+      const float v = -*m;
+      *m = v;
+      rs[i][j] = v;
+    }
+    __syncthreads();
+    if (jb > ib)
+      for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
+        const int i = q >> 5, j = q & 31;
+        c.M[(int64_t)(jb * kGjB + i) * np + ib * kGjB + j] = rs[j][i];
+      }
   }
   if (blockIdx.x == 0 && tid == 0) *c.ok = good ? 1 : 0;
 }
 
 // ---------------------------------------------------------------- PCG ----
-// (P e)_v for the coarse correction e of the current iteration (plain loads:
-// e is written earlier in the same kernel)
-__device__ __forceinline__ Vec3<float> prolong(const CoarseDev& c, int64_t v) {
-  const float4 m = __ldg(c.mode + v);
-  const int a = mode_agg(m);
-  const unsigned f = mode_mask(m);
-  const float4 e0 = reinterpret_cast<const float4*>(c.e)[2 * a];
-  const float4 e1 = reinterpret_cast<const float4*>(c.e)[2 * a + 1];
+// (P e) at a vertex with scaled offset d, aggregate a and free mask f, for the
+// coarse correction e of the current iteration (plain loads: e is written
+// earlier in the same kernel)
+__device__ __forceinline__ Vec3<float> prolong_at(const float* e, float dx, float dy, float dz, int a, unsigned f) {
+  const float4 e0 = reinterpret_cast<const float4*>(e)[2 * a];
+  const float4 e1 = reinterpret_cast<const float4*>(e)[2 * a + 1];
   // t = (e0.x, e0.y, e0.z), w = (e0.w, e1.x, e1.y): t + w x d
-  const float px = e0.x + (e1.x * m.z - e1.y * m.y);
-  const float py = e0.y + (e1.y * m.x - e0.w * m.z);
-  const float pz = e0.z + (e0.w * m.y - e1.x * m.x);
+  const float px = e0.x + (e1.x * dz - e1.y * dy);
+  const float py = e0.y + (e1.y * dx - e0.w * dz);
+  const float pz = e0.z + (e0.w * dy - e1.x * dx);
   return {(f & 1u) ? px : 0.f, (f & 2u) ? py : 0.f, (f & 4u) ? pz : 0.f};
 }
+// ... from the per-vertex mode array
+__device__ __forceinline__ Vec3<float> prolong(const CoarseDev& c, int64_t v) {
+  const float4 m = __ldg(c.mode + v);
+  return prolong_at(c.e, m.x, m.y, m.z, mode_agg(m), mode_mask(m));
+}
+// ... from the column data packed into a block record (same values: d is fp16-exact)
+__device__ __forceinline__ Vec3<float> prolong_rec(const float* e, unsigned a0, unsigned a1) {
+  const float dx = __half2float(__ushort_as_half((unsigned short)(a0 & 0xffffu)));
+  const float dy = __half2float(__ushort_as_half((unsigned short)(a0 >> 16)));
+  const float dz = __half2float(__ushort_as_half((unsigned short)(a1 & 0xffffu)));
+  return prolong_at(e, dx, dy, dz, (int)((a1 >> 16) & 0x1fffu), a1 >> 29);
+}
 
-// z_j = D^-1 r_j (stored) + (P e)_j, rounded the same wherever it is formed
+// z_j = D^-1 r_j (stored) + (P e)_j, rounded the same wherever it is formed: in
+// the gathers from the block record, for the own row from the mode array
 template <typename R> struct ZCoarse {
+  static constexpr bool kAux = true;
   const R* z;
   CoarseDev c;
   bool on;
-  __device__ __forceinline__ Vec3<R> operator()(int64_t j) const {
-    Vec3<R> a = ld3c(z, j);
+  __device__ __forceinline__ Vec3<R> operator()(const Blk<R>& b) const {
+    Vec3<R> a = ld3c(z, b.col);
     if (on) {
-      const Vec3<float> p = prolong(c, j);
+      const Vec3<float> p = prolong_rec(c.e, b.aux0, b.aux1);
+      a = {a.x + R(p.x), a.y + R(p.y), a.z + R(p.z)};
+    }
+    return a;
+  }
+  __device__ __forceinline__ Vec3<R> own(int64_t v) const {
+    Vec3<R> a = ld3c(z, v);
+    if (on) {
+      const Vec3<float> p = prolong(c, v);
       a = {a.x + R(p.x), a.y + R(p.y), a.z + R(p.z)};
     }
     return a;
@@ -288,10 +346,10 @@ template <typename R> struct ZCoarse {
 // Fixed-point scale of an iteration's coarse residual: a power of two putting
 // 64 ||r|| at 2^50 (|P^T r| of an aggregate is far below 2^12 ||r||, so sums
 // stay inside 64 bits with room for a residual that grows between iterations)
-__device__ __forceinline__ double coarse_scale(double rr) {
+__device__ __forceinline__ float coarse_scale(double rr) {
   int ex;
   frexp(64.0 * sqrt(fmax(rr, 1e-300)), &ex);
-  return ldexp(1.0, 50 - ex);
+  return ldexpf(1.f, max(-126, min(127, 50 - ex)));
 }
 
 // c.rc += P^T r over the calling warp's rows (every lane calls; consecutive
@@ -299,7 +357,7 @@ __device__ __forceinline__ double coarse_scale(double rr) {
 // one 64-bit atomic per segment and component: integer sums do not depend on
 // the order of the atomics)
 __device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, int64_t row, float rx, float ry,
-                                                float rz, double scale) {
+                                                float rz, float scale) {
   int key = -1;
   long long q[6];
 #pragma unroll
@@ -312,7 +370,7 @@ __device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, 
     // P_v^T r = (r, d x r)
     const float v6[6] = {x, y, z, m.y * z - m.z * y, m.z * x - m.x * z, m.x * y - m.y * x};
 #pragma unroll
-    for (int k = 0; k < 6; ++k) q[k] = __double2ll_rn(double(v6[k]) * scale);
+    for (int k = 0; k < 6; ++k) q[k] = __float2ll_rn(v6[k] * scale);   // power-of-two scale: exact
   }
   const int lane = threadIdx.x & 31;
   const int prev = __shfl_up_sync(0xffffffffu, key, 1);
@@ -337,20 +395,23 @@ __device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, 
 // strided over the grid), pc += (P^T r) . e over those rows.  rcf: shared
 // staging of P^T r (np floats).
 template <typename R>
-__device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, double inv_scale, Dacc<R>& pc) {
+__device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, float inv_scale, Dacc<R>& pc) {
   const int wpb = blockDim.x >> 5;
   const int gw0 = blockIdx.x * wpb;
   if (gw0 >= c.nc) return;   // block-uniform
+#pragma unroll 4
   for (int i = threadIdx.x; i < c.np; i += blockDim.x)
-    rcf[i] = i < c.nc ? float(double((long long)__ldcg(c.rc + i)) * inv_scale) : 0.f;
+    rcf[i] = i < c.nc ? __ll2float_rn((long long)__ldcg(c.rc + i)) * inv_scale : 0.f;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const float4* r4 = reinterpret_cast<const float4*>(rcf);
   for (int row = gw0 + (threadIdx.x >> 5); row < c.nc; row += gridDim.x * wpb) {
+    // A_c^-1 is streamed (evict-first) so that it does not push the block records out of L2
     const float4* Mr = reinterpret_cast<const float4*>(c.M + (int64_t)row * c.np);
     float s = 0.f;
+#pragma unroll 5
     for (int j = lane; j < (c.np >> 2); j += 32) {
-      const float4 m = __ldcg(Mr + j), x = r4[j];
+      const float4 m = __ldcs(Mr + j), x = r4[j];
       s = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, s))));
     }
 #pragma unroll
@@ -413,7 +474,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
   const ZCoarse<R> zf{v.z, c, con};
   if (!done && con) {
     // coarse part of z_0 = D^-1 r_0 + P e_0
-    const double sc = coarse_scale(rr_prev);
+    const float sc = coarse_scale(rr_prev);
     for (int64_t base = wbase0; base < A.nbr; base += stride) {
       const int64_t i = base + (threadIdx.x & 31);
       const bool ok = i < A.nbr;
@@ -426,7 +487,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
     } else {
       Dacc<R> pc[1];
       dacc_zero(pc[0]);
-      coarse_product<R>(c, rcf, 1.0 / sc, pc[0]);
+      coarse_product<R>(c, rcf, 1.f / sc, pc[0]);
       block_total<R, 1>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];
@@ -460,7 +521,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
 #pragma unroll
       for (int u = 0; u < U; ++u)
         if (lane == 0 && val[u]) {
-          const Vec3<R> zi = zf(rows[u]);
+          const Vec3<R> zi = zf.own(rows[u]);
           const Vec3<R> p = first ? zi : pdir3(zi, ld3c(pprev, rows[u]), beta);
           st3(pk, rows[u], p);
           st3(v.q, rows[u], ys[u]);
@@ -477,7 +538,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
       break;
     }
     const R a = dacc_r(rz) / pqr;
-    const double sc = coarse_scale(rr_prev);
+    const float sc = coarse_scale(rr_prev);
     Dacc<R> acc[2];
     dacc_zero(acc[0]);
     dacc_zero(acc[1]);
@@ -518,7 +579,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
     if (con) {
       Dacc<R> pc[1];
       dacc_zero(pc[0]);
-      coarse_product<R>(c, rcf, 1.0 / sc, pc[0]);
+      coarse_product<R>(c, rcf, 1.f / sc, pc[0]);
       block_total<R, 1>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];

@@ -105,12 +105,13 @@ __device__ __forceinline__ bool grid_barrier_total(unsigned* count, volatile uns
 
 // preconditioned residual of a column as stored (one-level preconditioner)
 template <typename R> struct ZPlain {
+  static constexpr bool kAux = false;
   const R* z;
-  __device__ __forceinline__ Vec3<R> operator()(int64_t j) const { return ld3c(z, j); }
+  __device__ __forceinline__ Vec3<R> operator()(const Blk<R>& b) const { return ld3c(z, b.col); }
 };
 
 // U block rows per lane group: y = A p_k with p_k = z + beta p_prev gathered per column
-// (p_prev skipped on the first iteration, where p_0 = z); zf(j) gives z_j
+// (p_prev skipped on the first iteration, where p_0 = z); zf(block) gives z of the block's column
 template <typename R, int G, int U, class Zf>
 __device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const Zf& zf, const R* __restrict__ pp,
                                               R beta, bool first, const int64_t (&row)[U], const bool (&valid)[U],
@@ -131,14 +132,14 @@ __device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const Zf& zf, con
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bk[u] = Blk<R>{};
-      if (k < K[u]) bk[u] = ld_rec(A.rec, p[u] + k);
+      if (k < K[u]) bk[u] = ld_rec<Zf::kAux>(A.rec, p[u] + k);
     }
     Vec3<R> xv[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       xv[u] = Vec3<R>{R(0), R(0), R(0)};
       if (k < K[u]) {
-        const Vec3<R> zc = zf(bk[u].col);
+        const Vec3<R> zc = zf(bk[u]);
         xv[u] = first ? zc : pdir3(zc, ld3c(pp, bk[u].col), beta);
       }
     }

@@ -36,18 +36,26 @@ template <typename R> struct Bsr {
   const R* rec;    // 12-wide block records (values + column), preferred
 };
 
-// one 3x3 block and its column from a record (three / six 16-byte loads)
-template <typename R> struct Blk { R m[9]; int col; };
+// one 3x3 block and its column from a record (three / five 16-byte loads);
+// aux: the two spare slots (the column's packed coarse data), loaded for FP64
+// records only when asked for (one more load)
+template <typename R> struct Blk { R m[9]; int col; unsigned aux0, aux1; };
 
+template <bool AUX = false>
 __device__ __forceinline__ Blk<float> ld_rec(const float* __restrict__ rec, int64_t s) {
   const float4* p = reinterpret_cast<const float4*>(rec) + 3 * s;
   const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.y)};
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.y), __float_as_uint(c.z),
+          __float_as_uint(c.w)};
 }
+template <bool AUX = false>
 __device__ __forceinline__ Blk<double> ld_rec(const double* __restrict__ rec, int64_t s) {
   const double2* p = reinterpret_cast<const double2*>(rec) + 6 * s;
   const double2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3), e = __ldg(p + 4);
-  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(e.y)};
+  unsigned long long x = 0;
+  if constexpr (AUX) x = (unsigned long long)__double_as_longlong(__ldg(reinterpret_cast<const double*>(p + 5)));
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(e.y), (unsigned)x,
+          (unsigned)(x >> 32)};
 }
 
 // 3-term dot in the working precision, widened once
@@ -759,7 +767,6 @@ static CoarseDev make_coarse_dev(const skg_tet_mesh* m, const Workspace& w) {
   c.cb_rc = h->cb_rc;
   c.bsr_row = m->bsr_row;
   c.M = w.cM;
-  c.colp = w.ccolp;
   c.rowp = w.crowp;
   c.rc = w.crc;
   c.e = w.ce;
@@ -785,7 +792,9 @@ static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cud
     SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_invert, kGjCols, 0));
     if (per_sm < 1) return fail(SKG_ERR_CUDA, "the coarse inversion kernel does not fit on an SM");
   }
-  const int units = (c.np / kGjB) * ((c.np + kGjCols - 1) / kGjCols);
+  // work units of the upper block triangle (as enumerated by the kernel)
+  int units = 0;
+  for (int ib = 0, ncu = (c.np + kGjCols - 1) / kGjCols; ib < c.np / kGjB; ++ib) units += ncu - (ib * kGjB) / kGjCols;
   int grid = per_sm * num_sms();
   if (grid > units) grid = units;
   if (grid < 1) grid = 1;
@@ -1076,6 +1085,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     aa.contact = contact;
     aa.u = st->u;
     aa.pinned = st->pinned;
+    aa.cmode = two_level ? cdev.mode : nullptr;
     pt.begin();
     SKG_TRY(launch_assemble<R>(aa, s));
     info->launches += 2;

@@ -114,7 +114,8 @@ def coarse_aggregates(X, free_dof, rowptr, col, box=8, spacing=None, max_coarse=
     d = X - cen[agg]
     rms = np.sqrt(np.bincount(agg, weights=(d * d).sum(1), minlength=n_agg) / cnt)
     rms = np.where(rms > 0.0, rms, 1.0)
-    d = d / rms[agg][:, None]
+    # fp16-exact offsets: the block records carry them packed as fp16 for the gathers
+    d = (d / rms[agg][:, None]).astype(np.float16).astype(np.float32)
     mask = (free[:, 0].astype(np.uint32) | (free[:, 1].astype(np.uint32) << 1)
             | (free[:, 2].astype(np.uint32) << 2))
     bits = agg.astype(np.uint32) | (mask << np.uint32(29))

@@ -109,36 +109,47 @@ def test_galerkin_formula_matches_ptap():
 
 
 def _gj_schedule(Min):
-    """The inversion kernel's schedule in numpy (FP64)."""
+    """The inversion kernel's schedule in numpy (FP64): the symmetric sweep
+    (M_KK <- -Pinv, M_KJ <- Pinv R_J, M_IK <- C_I Pinv, M_IJ <- M_IJ - C_I Pinv R_J with C = R^T)
+    over the upper triangle of 32-row blocks, row panels written by the previous step, then the
+    mirror pass that fills the lower triangle and flips the sign."""
     M = Min.copy()
     np_ = M.shape[0]
     nbk, ncu = np_ // KB, (np_ + KC - 1) // KC
-    colp = np.zeros((2, np_, KB))
+    M[np.tril_indices(np_, -KB)] = np.nan     # below the diagonal blocks: never read
+    for ib in range(nbk):
+        M[ib * KB:(ib + 1) * KB, :ib * KB] = np.nan
     rowp = np.zeros((2, KB, np_))
-    colp[0] = M[:, :KB]
-    rowp[0] = M[:KB, :]
+    rowp[0] = Min[:KB, :]
     for kb in range(nbk):
-        C, Rw = colp[kb & 1].copy(), rowp[kb & 1].copy()
+        Rw = rowp[kb & 1].copy()
         K0, K1 = kb * KB, kb * KB + KB
         piv = np.linalg.inv(Rw[:, K0:K1])
         for ib in range(nbk):
-            for cu in range(ncu):
-                I0 = ib * KB
-                vt = piv if ib == kb else C[I0:I0 + KB] @ piv          # V = C_I Pinv (or Pinv)
-                for j in range(cu * KC, min(np_, cu * KC + KC)):
+            I0 = ib * KB
+            for cu in range(I0 // KC, ncu):
+                vt = piv if ib == kb else Rw[:, I0:I0 + KB].T @ piv   # V = C_I Pinv, C_I = R[:, I]^T
+                for j in range(max(cu * KC, I0), min(np_, cu * KC + KC)):
                     if K0 <= j < K1:
-                        a = piv[:, j - K0] if ib == kb else -vt[:, j - K0]
+                        a = -piv[:, j - K0] if ib == kb else vt[:, j - K0]
                     elif ib == kb:
                         a = vt @ Rw[:, j]
                     else:
                         a = M[I0:I0 + KB, j] - vt @ Rw[:, j]
                     M[I0:I0 + KB, j] = a
                     if kb + 1 < nbk:
-                        if K1 <= j < K1 + KB:
-                            colp[(kb + 1) & 1][I0:I0 + KB, j - K1] = a
                         if ib == kb + 1:
                             rowp[(kb + 1) & 1][:, j] = a
-    return M
+                        elif K1 <= j < K1 + KB and ib < kb + 1:
+                            rowp[(kb + 1) & 1][j - K1, I0:I0 + KB] = a
+    out = np.empty_like(M)
+    for ib in range(nbk):
+        for jb in range(ib, nbk):
+            t = M[ib * KB:(ib + 1) * KB, jb * KB:(jb + 1) * KB]
+            out[ib * KB:(ib + 1) * KB, jb * KB:(jb + 1) * KB] = -t
+            if jb > ib:
+                out[jb * KB:(jb + 1) * KB, ib * KB:(ib + 1) * KB] = -t.T
+    return out
 
 
 def test_gauss_jordan_schedule_inverts():
