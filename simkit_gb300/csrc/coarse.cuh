@@ -12,7 +12,7 @@
 //
 // Per refresh (first Newton iteration of a step, or every iteration):
 //   k_coarse_galerkin  A_c = P^T A P from the assembled blocks, one warp per
-//                      nonzero 6x6 coarse block, FP32 products summed in FP64 in a fixed
+//                      nonzero 6x6 coarse block, FP32 sums in a fixed
 //                      order (bitwise reproducible), small diagonal shift;
 //   k_coarse_invert    A_c^-1 in place by blocked Gauss-Jordan (SPD, no
 //                      pivoting, FP32), cooperative grid, one barrier per
@@ -66,9 +66,9 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
   const int cb = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (cb >= c.n_cb) return;   // warp-uniform
-  double acc[36];
+  float acc[36];
 #pragma unroll
-  for (int q = 0; q < 36; ++q) acc[q] = 0.0;
+  for (int q = 0; q < 36; ++q) acc[q] = 0.f;
   const int k0 = c.cb_ptr[cb], k1 = c.cb_ptr[cb + 1];
   for (int k = k0 + lane; k < k1; k += 32) {
     const int s = c.cb_slot[k];
@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        acc[6 * i + j] += double(a[3 * i + j]);
-        acc[6 * i + 3 + j] -= double(B[3 * i + j]);
-        acc[6 * (3 + i) + j] += double(SA[3 * i + j]);
-        acc[6 * (3 + i) + 3 + j] -= double(Sv[3 * i] * B[j] + Sv[3 * i + 1] * B[3 + j] + Sv[3 * i + 2] * B[6 + j]);
+        acc[6 * i + j] += a[3 * i + j];
+        acc[6 * i + 3 + j] -= B[3 * i + j];
+        acc[6 * (3 + i) + j] += SA[3 * i + j];
+        acc[6 * (3 + i) + 3 + j] -= Sv[3 * i] * B[j] + Sv[3 * i + 1] * B[3 + j] + Sv[3 * i + 2] * B[6 + j];
       }
   }
 #pragma unroll
@@ -111,46 +111,46 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
     // shift the diagonal by a small fraction of the aggregate's largest one, so
     // rank-deficient aggregates (one vertex, collinear vertices) stay definite;
     // an aggregate with no free DOF gets the identity
-    double dmax = 0.0;
+    float dmax = 0.f;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) dmax = fmax(dmax, acc[7 * i]);
+    for (int i = 0; i < 6; ++i) dmax = fmaxf(dmax, acc[7 * i]);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) acc[7 * i] = dmax > 0.0 ? acc[7 * i] + kCoarseShift * dmax : 1.0;
+    for (int i = 0; i < 6; ++i) acc[7 * i] = dmax > 0.f ? acc[7 * i] + float(kCoarseShift) * dmax : 1.f;
   }
   float* out = c.M + (int64_t)(6 * ra) * c.np + 6 * ca;
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
-    for (int j = 0; j < 6; ++j) out[(int64_t)i * c.np + j] = float(acc[6 * i + j]);
+    for (int j = 0; j < 6; ++j) out[(int64_t)i * c.np + j] = acc[6 * i + j];
 }
 
 // ------------------------------------------------------- Gauss-Jordan ----
-// Inverse of one SPD 32 x 32 block in shared memory (all threads of the
-// block take part, four elements each).  False if a pivot is not positive.
-__device__ __forceinline__ bool gj_inverse32(float (*a)[kGjB + 1]) {
+// Inverse of one SPD 32 x 32 block (row-major at src, leading dimension ld) by
+// Gauss-Jordan in one warp: lane j keeps column j in registers, column p of
+// each pivot step is broadcast by shuffles, no block barrier.  The result goes
+// to out (shared).  False if a pivot is not positive.
+__device__ __forceinline__ bool gj_inverse32_warp(const float* src, int64_t ld, float (*out)[kGjB + 1]) {
+  const int lane = threadIdx.x & 31;
+  float a[kGjB];
+#pragma unroll
+  for (int i = 0; i < kGjB; ++i) a[i] = src[(int64_t)i * ld + lane];
   bool good = true;
+#pragma unroll
   for (int p = 0; p < kGjB; ++p) {
-    __syncthreads();
-    const float d = a[p][p];
+    const float d = __shfl_sync(0xffffffffu, a[p], p);
     good = good && d > 0.f && isfinite(d);
     const float inv = 1.f / d;
-    float nv[(kGjB * kGjB) / kGjCols];
+    const float f = a[p] * inv;   // new row-p entry of this lane's column
 #pragma unroll
-    for (int r = 0; r < (kGjB * kGjB) / kGjCols; ++r) {
-      const int q = threadIdx.x + r * kGjCols, i = q >> 5, j = q & 31;
-      if (i == p && j == p) nv[r] = inv;
-      else if (i == p) nv[r] = a[p][j] * inv;
-      else if (j == p) nv[r] = -a[i][p] * inv;
-      else nv[r] = fmaf(-a[i][p] * inv, a[p][j], a[i][j]);
+    for (int i = 0; i < kGjB; ++i) {
+      if (i == p) continue;
+      const float aip = __shfl_sync(0xffffffffu, a[i], p);   // row i of column p
+      a[i] = lane == p ? -aip * inv : fmaf(-aip, f, a[i]);
     }
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < (kGjB * kGjB) / kGjCols; ++r) {
-      const int q = threadIdx.x + r * kGjCols;
-      a[q >> 5][q & 31] = nv[r];
-    }
+    a[p] = lane == p ? inv : f;
   }
-  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kGjB; ++i) out[i][lane] = a[i];
   return good;
 }
 
@@ -170,7 +170,7 @@ __device__ __forceinline__ bool gj_inverse32(float (*a)[kGjB + 1]) {
 // block itself (same inputs, same order: the same Pinv everywhere).  Launched
 // cooperatively with kGjCols threads; c.ok is set to 1 only if every pivot was
 // positive.
-__global__ void __launch_bounds__(kGjCols) k_coarse_invert(CoarseDev c, volatile double* err) {
+__global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volatile double* err) {
   __shared__ float piv[kGjB][kGjB + 1];
   __shared__ float rs[kGjB][kGjB + 1];
   __shared__ __align__(16) float vt[kGjB][kGjB];
@@ -199,8 +199,9 @@ __global__ void __launch_bounds__(kGjCols) k_coarse_invert(CoarseDev c, volatile
     const float* Rw = c.rowp + (int64_t)(kb & 1) * kGjB * np;
     float* Rn = c.rowp + (int64_t)((kb + 1) & 1) * kGjB * np;
     const int K0 = kb * kGjB, K1 = K0 + kGjB;
-    for (int q = tid; q < kGjB * kGjB; q += blockDim.x) piv[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + K0 + (q & 31)];
-    good = gj_inverse32(piv) && good;
+    __syncthreads();   // piv of the previous step is no longer read
+    if (tid < 32) good = gj_inverse32_warp(Rw + K0, np, piv) && good;   // thread 0 keeps the flag
+    __syncthreads();
     int ib = 0;
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
       while (ustart[ib + 1] <= u) ++ib;   // units are visited in increasing order
