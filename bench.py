@@ -250,7 +250,8 @@ def train_warm_start(args):
     from simkit_gb300.beams import beam_batch
     t0 = time.perf_counter()
     train_specs = beam_batch(args.instances, seed=100)
-    tb = BatchedBESolver(train_specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
+    coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
+    tb = BatchedBESolver(train_specs, precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=coarse)
     frames, _ = ws.generate_frames(tb, train_specs, args.train_steps)
     t_gen = time.perf_counter() - t0
     net = ws.WarmStartMLP(seed=0, lr=1e-3)
@@ -320,7 +321,10 @@ def run_batched(args):
     ranks = Ranks("nccl")
     # replicas: every rank steps its own seeded batch of the same distribution
     specs = beam_batch(args.instances, seed=replica_seed(rank))
-    b = BatchedBESolver(specs, precision=args.precision, pcg_rtol=args.pcg_rtol)
+    # the same preconditioner on both sides of the comparison: two-level (per-instance
+    # aggregates) unless --coarse none
+    coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
+    b = BatchedBESolver(specs, precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=coarse)
     for _ in range(args.warmup):
         infos, total = b.step()
         if total.status != 0:
@@ -383,7 +387,7 @@ def run_batched(args):
     sample = rng.choice(args.instances, size=min(args.plain_sample, args.instances), replace=False)
     plain_ms = []
     for i in sample:
-        s1 = BESolver.from_spec(specs[i], precision=args.precision, pcg_rtol=args.pcg_rtol)
+        s1 = BESolver.from_spec(specs[i], precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=coarse)
         for _ in range(args.warmup):
             s1.step()
         torch.cuda.synchronize()
@@ -404,7 +408,7 @@ def run_batched(args):
                                + ("+ learned warm start" if args.learned else "plain Newton"),
                    "instances": args.instances, "tets": int(tets), "verts": int(b.n_verts),
                    "precision": args.precision, "pcg_rtol": args.pcg_rtol,
-                   "parallelism": f"replicas x{n_ranks}"},
+                   "coarse": args.coarse, "parallelism": f"replicas x{n_ranks}"},
         "tet_hessians_per_s": n_ranks * newton / max(args.instances, 1) * tets / (ms / 1000.0),
         "newton_iters_per_instance_step": newton / inst_steps,
         "pcg_iters_per_instance_step": sum(t.pcg_iters for t in totals) / inst_steps,

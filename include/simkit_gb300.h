@@ -166,7 +166,7 @@ typedef enum skg_material {
  * newton.py:52); this preconditioner is the GPU's replacement for that
  * solver's robustness on stiff, heterogeneous meshes. */
 typedef struct skg_coarse {
-  int32_t n_agg;            /* aggregates; 6 n_agg coarse unknowns, at most 4096 */
+  int32_t n_agg;            /* aggregates; 6 n_agg coarse unknowns, at most 4096 in the whole-mesh form */
   int32_t n_cblocks;        /* nonzero 6x6 blocks of the coarse operator */
   const float* mode;        /* (n, 4) per vertex: (d_x, d_y, d_z, bits) with d the offset from the
                                aggregate centroid divided by the aggregate's RMS offset and bits
@@ -174,6 +174,17 @@ typedef struct skg_coarse {
   const int32_t* cb_ptr;    /* (n_cblocks + 1) offsets into cb_slot */
   const int32_t* cb_slot;   /* (n_blocks) fine block slots grouped by coarse block */
   const int32_t* cb_rc;     /* (2 n_cblocks) aggregate row, aggregate column of each coarse block */
+  /* Per-instance form, for the thread-block-cluster PCG (pcg_mode 2 / 3 on small meshes, and
+   * skg_be_step_batched).  NULL inst_agg selects the whole-mesh form of pcg_mode 7.  Each
+   * instance has at most 127 aggregates (762 coarse unknowns). */
+  int32_t n_inst;           /* instances (1 for one mesh) */
+  int32_t max_np;           /* largest 6 * aggregates of an instance, rounded up to 32 */
+  int64_t m_floats;         /* sum over instances of np_i^2: dense coarse storage */
+  const int32_t* inst_agg;  /* (n_inst + 1) first aggregate of each instance */
+  const int32_t* agg_inst;  /* (n_agg) instance of each aggregate */
+  const int64_t* inst_moff; /* (n_inst + 1) offset of each instance's np_i x np_i block, in floats */
+  const uint32_t* colpack;  /* (n) per vertex: (k_x+64) | (k_y+64) << 7 | (k_z+64) << 14 | local
+                               aggregate << 21 | free mask << 28, offset = k / 64 */
 } skg_coarse;
 
 typedef struct skg_tet_mesh {

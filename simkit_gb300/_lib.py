@@ -45,7 +45,8 @@ STATUS_NAMES = {
 
 class CoarseC(ctypes.Structure):
     _fields_ = [("n_agg", c_i32), ("n_cblocks", c_i32), ("mode", c_vp), ("cb_ptr", c_vp), ("cb_slot", c_vp),
-                ("cb_rc", c_vp)]
+                ("cb_rc", c_vp), ("n_inst", c_i32), ("max_np", c_i32), ("m_floats", c_i64), ("inst_agg", c_vp),
+                ("agg_inst", c_vp), ("inst_moff", c_vp), ("colpack", c_vp)]
 
 
 class TetMeshC(ctypes.Structure):

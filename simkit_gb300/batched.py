@@ -34,7 +34,8 @@ class BatchedBESolver:
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
-                 integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True):
+                 integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
+                 coarse=None, coarse_refresh="step"):
         _lib.load()
         self.n_inst = len(specs)
         if self.n_inst == 0:
@@ -62,6 +63,12 @@ class BatchedBESolver:
         mesh.set_energy(material)
         up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
         self._contact_init = (contact_planes, contact_mass_weighted)
+        # two-level PCG: per-instance aggregates (box 4 mesh spacings by default)
+        self.coarse_boxes = None
+        if coarse is not None:
+            _, self.coarse_boxes = mesh.set_coarse_inst(np.concatenate(pins) == 0, np.array(rows),
+                                                        box=4 if coarse == "auto" else int(coarse))
+        self._coarse_refresh = coarse_refresh
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
                     pcg_max_iter, do_line_search, ls_threshold, profile, integrator)
@@ -120,7 +127,8 @@ class BatchedBESolver:
             pcg_max_iter=pcg_max_iter, do_line_search=int(do_line_search), ls_alpha=0.01, ls_beta=0.5,
             ls_max_iter=100, pcg_mode=2,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
-            profile=int(profile), integrator=INTEGRATORS[integrator])
+            profile=int(profile), integrator=INTEGRATORS[integrator],
+            coarse_refresh=int(getattr(self, "_coarse_refresh", "step") == "newton"))
         self._infos = (StepInfoC * self.n_inst)()
         init = getattr(self, "_contact_init", (None, True))
         self.set_contact_planes(*init)

@@ -156,6 +156,7 @@ __global__ void k_assemble(AsmArgs<R> a) {
     for (int m = 0; m < 9; ++m) r[m] = acc[m];
     r[9] = col_bits(w, R(0));
     rec_aux_store(r, a.cmode ? coarse_pack(__ldg(a.cmode + w)) : make_uint2(0u, 0u));
+    if (a.colpack) rec_word_store(r, __ldg(a.colpack + w));
   }
   if (v == w && a.jinv) {
     R C[9];
@@ -466,13 +467,22 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   w.partials = c.take<double>(8 * kMaxGrid);
   w.counter = c.take<unsigned>(16);
   w.scal = c.take<double>(64);
-  if (m->coarse) {
+  if (m->coarse && !m->coarse->inst_agg) {
     const int64_t np = coarse_padded(m);
     w.cM = c.take<float>(np * np);
     w.crowp = c.take<float>(2 * 32 * np);
     w.crc = c.take<unsigned long long>(np);
     w.ce = c.take<float>(8 * (int64_t)m->coarse->n_agg);
     w.cok = c.take<int>(4);
+    w.cbar = c.take<unsigned>(4);
+  } else if (m->coarse) {
+    // per-instance form: dense blocks of every instance, row panels per inversion CTA
+    const skg_coarse* h = m->coarse;
+    w.cM = c.take<float>(h->m_floats);
+    w.crowp = c.take<float>((int64_t)kCoarseInvCtas * 2 * 32 * h->max_np);
+    w.crc = c.take<unsigned long long>(6 * (int64_t)h->n_agg + 32);
+    w.ce = c.take<float>(8 * (int64_t)h->n_agg);
+    w.cok = c.take<int>(h->n_inst + 4);
     w.cbar = c.take<unsigned>(4);
   }
   w.bytes = c.off + 256;
@@ -526,9 +536,16 @@ int check_mesh(const skg_tet_mesh* m, int precision) {
     return fail(SKG_ERR_ARG, "unknown material %d", m->material);
   if (m->coarse) {
     const skg_coarse* c = m->coarse;
-    if (c->n_agg <= 0 || 6 * (int64_t)c->n_agg > 4096 || c->n_cblocks < c->n_agg)
-      return fail(SKG_ERR_ARG, "coarse: %d aggregates (1..682 allowed), %d coarse blocks", c->n_agg, c->n_cblocks);
     if (!c->mode || !c->cb_ptr || !c->cb_slot || !c->cb_rc) return fail(SKG_ERR_ARG, "coarse has a null array");
+    if (!c->inst_agg) {
+      if (c->n_agg <= 0 || 6 * (int64_t)c->n_agg > 4096 || c->n_cblocks < c->n_agg)
+        return fail(SKG_ERR_ARG, "coarse: %d aggregates (1..682 allowed), %d coarse blocks", c->n_agg, c->n_cblocks);
+    } else {
+      if (c->n_inst <= 0 || c->n_agg < c->n_inst || c->max_np <= 0 || c->max_np > 768 || c->max_np % 32 ||
+          c->m_floats <= 0 || !c->agg_inst || !c->inst_moff || !c->colpack)
+        return fail(SKG_ERR_ARG, "coarse (per instance): %d instances, %d aggregates, largest block %d", c->n_inst,
+                    c->n_agg, c->max_np);
+    }
   }
   return SKG_OK;
 }

@@ -81,6 +81,7 @@ template <typename R> struct AsmArgs {
   Contact contact;             // contact springs on diagonal blocks (positions from u)
   const double* u;             // displacement (needed with contact)
   const float4* cmode;         // optional: two-level coarse data per vertex, packed into record slots 10-11
+  const uint32_t* colpack;     // optional (cluster PCG): the column's 32-bit coarse word into record slot 11
 };
 
 // A column's two-level coarse data in the two spare record slots (64 bits):
@@ -102,6 +103,8 @@ __device__ __forceinline__ void rec_aux_store(double* r, uint2 a) {
   r[10] = __longlong_as_double((long long)(((unsigned long long)a.y << 32) | a.x));
   r[11] = 0.0;
 }
+__device__ __forceinline__ void rec_word_store(float* r, uint32_t w) { r[11] = __uint_as_float(w); }
+__device__ __forceinline__ void rec_word_store(double* r, uint32_t w) { r[11] = __longlong_as_double((long long)w); }
 
 // Block record of the solver's SpMV: the 9 row-major entries of a 3x3 block,
 // the block column stored in the bits of entry 9, entries 10-11 zero, so one
@@ -175,10 +178,13 @@ struct Workspace {
   int64_t bytes;
 };
 
-// coarse unknowns padded to the Gauss-Jordan block (32)
+// coarse unknowns padded to the Gauss-Jordan block (32); the largest instance in the per-instance form
 inline int64_t coarse_padded(const skg_tet_mesh* m) {
-  return m->coarse ? ((6 * (int64_t)m->coarse->n_agg + 31) / 32) * 32 : 0;
+  if (!m->coarse) return 0;
+  if (m->coarse->inst_agg) return m->coarse->max_np;
+  return ((6 * (int64_t)m->coarse->n_agg + 31) / 32) * 32;
 }
+constexpr int kCoarseInvCtas = 456;   // CTAs of the per-instance coarse inversion (3 per SM on 152 SMs)
 
 Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base);
 int check_mesh(const skg_tet_mesh* m, int precision);

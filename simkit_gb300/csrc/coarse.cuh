@@ -26,32 +26,6 @@
 
 namespace skg {
 
-constexpr int kCoarseMax = 4096;   // coarse unknowns the PCG stages in shared memory
-constexpr int kGjB = 32;           // Gauss-Jordan pivot block
-constexpr int kGjCols = 256;       // columns per Gauss-Jordan work unit (one per thread)
-constexpr double kCoarseShift = 1e-5;  // diagonal shift relative to the aggregate's largest diagonal
-
-struct CoarseDev {
-  int n_agg;                   // aggregates
-  int nc;                      // coarse unknowns, 6 n_agg
-  int np;                      // nc padded to a multiple of kGjB (identity in the padding)
-  int n_cb;                    // nonzero 6x6 coarse blocks
-  const float4* mode;          // (n): d_v (x, y, z); w bits: aggregate | free mask << 29
-  const int32_t* cb_ptr;       // (n_cb + 1)
-  const int32_t* cb_slot;      // fine block slots grouped by coarse block
-  const int32_t* cb_rc;        // (2 n_cb) aggregate row, column
-  const int32_t* bsr_row;      // block row of each fine slot
-  float* M;                    // np x np: A_c, inverted in place
-  float* rowp;                 // 2 x kGjB x np row panels
-  unsigned long long* rc;      // np: coarse residual in fixed point
-  float* e;                    // 8 n_agg: (t, w) per aggregate, padded to 8
-  int* ok;                     // 1 when M holds a valid inverse
-  unsigned* bar;               // 2: grid barrier of the inversion
-};
-
-__device__ __forceinline__ int mode_agg(float4 m) { return (int)(__float_as_uint(m.w) & 0x1fffffffu); }
-__device__ __forceinline__ unsigned mode_mask(float4 m) { return __float_as_uint(m.w) >> 29; }
-
 // ------------------------------------------------------------ Galerkin ----
 // C = P_v^T A'_vw P_w for one fine block, P_v = [I | -S(d_v)], S(d) = [d]x,
 // A' = diag(m_v) A diag(m_w):  C = [[A', -A' S_w], [S_v A', -S_v A' S_w]]
@@ -106,8 +80,19 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
 #pragma unroll
     for (int q = 0; q < 36; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
   if (lane != 0) return;
-  const int ra = c.cb_rc[2 * cb], ca = c.cb_rc[2 * cb + 1];
-  if (ra == ca) {
+  int ra = c.cb_rc[2 * cb], ca = c.cb_rc[2 * cb + 1];
+  const bool diag = ra == ca;
+  float* Mb = c.M;
+  int np = c.np;
+  if (c.inst_agg) {   // per-instance dense blocks
+    const int inst = c.agg_inst[ra];
+    const int a0 = c.inst_agg[inst];
+    np = ((6 * (c.inst_agg[inst + 1] - a0) + kGjB - 1) / kGjB) * kGjB;
+    Mb = c.M + c.inst_moff[inst];
+    ra -= a0;
+    ca -= a0;
+  }
+  if (diag) {
     // shift the diagonal by a small fraction of the aggregate's largest one, so
     // rank-deficient aggregates (one vertex, collinear vertices) stay definite;
     // an aggregate with no free DOF gets the identity
@@ -117,11 +102,11 @@ __global__ void __launch_bounds__(kBlock) k_coarse_galerkin(Bsr<R> A, CoarseDev 
 #pragma unroll
     for (int i = 0; i < 6; ++i) acc[7 * i] = dmax > 0.f ? acc[7 * i] + float(kCoarseShift) * dmax : 1.f;
   }
-  float* out = c.M + (int64_t)(6 * ra) * c.np + 6 * ca;
+  float* out = Mb + (int64_t)(6 * ra) * np + 6 * ca;
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
-    for (int j = 0; j < 6; ++j) out[(int64_t)i * c.np + j] = acc[6 * i + j];
+    for (int j = 0; j < 6; ++j) out[(int64_t)i * np + j] = acc[6 * i + j];
 }
 
 // ------------------------------------------------------- Gauss-Jordan ----
@@ -154,10 +139,9 @@ __device__ __forceinline__ bool gj_inverse32_warp(const float* src, int64_t ld, 
   return good;
 }
 
-// In-place inverse of the SPD np x np matrix c.M (np a multiple of 32; rows
-// nc..np-1 are padding set to the identity here) by the symmetric sweep: pivot
-// blocks K of 32 in order, with Pinv = (M_KK)^-1, the step's old row panel
-// R = M[K, :] and C = R^T,
+// Symmetric sweep inverse of an SPD np x np matrix M (np a multiple of 32;
+// rows nc..np-1 are padding set to the identity): pivot blocks K of 32 in
+// order, with Pinv = (M_KK)^-1, the step's old row panel R = M[K, :] and C = R^T,
 //   M_KK <- -Pinv,  M_Kj <- Pinv R_j,  M_iK <- C_i Pinv,  M_ij <- M_ij - C_i Pinv R_j,
 // which keeps M symmetric, so only the upper triangle of 32-row blocks is
 // updated; after the last step M = -A^-1 there, and a mirror pass writes the
@@ -166,27 +150,137 @@ __device__ __forceinline__ bool gj_inverse32_warp(const float* src, int64_t ld, 
 // comes from a double-buffered copy the previous step wrote (row K+1 from its
 // own block row, the part left of the diagonal from column block K+1 of the
 // rows above, transposed), so no unit reads what another unit of the same step
-// writes and each step ends in one grid barrier.  Every CTA inverts the pivot
-// block itself (same inputs, same order: the same Pinv everywhere).  Launched
-// cooperatively with kGjCols threads; c.ok is set to 1 only if every pivot was
-// positive.
-__global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volatile double* err) {
-  __shared__ float piv[kGjB][kGjB + 1];
-  __shared__ float rs[kGjB][kGjB + 1];
-  __shared__ __align__(16) float vt[kGjB][kGjB];
-  __shared__ int ustart[kCoarseMax / kGjB + 1];   // first unit of each block row (upper triangle)
-  const int np = c.np, nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols;
-  const int tid = threadIdx.x;
-  if (tid == 0) {
+// writes and a step needs one barrier.
+struct GjShared {
+  float piv[kGjB][kGjB + 1];
+  float rs[kGjB][kGjB + 1];
+  __align__(16) float vt[kGjB][kGjB];
+  int ustart[kCoarseMax / kGjB + 1];   // first unit of each block row (upper triangle)
+};
+
+// unit table of an np x np sweep; all threads of the block call it
+__device__ __forceinline__ int gj_units(GjShared& g, int np) {
+  const int nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols;
+  __syncthreads();
+  if (threadIdx.x == 0) {
     int acc = 0;
     for (int ib = 0; ib < nbk; ++ib) {
-      ustart[ib] = acc;
+      g.ustart[ib] = acc;
       acc += ncu - (ib * kGjB) / kGjCols;
     }
-    ustart[nbk] = acc;
+    g.ustart[nbk] = acc;
   }
   __syncthreads();
-  const int units = ustart[nbk];
+  return g.ustart[nbk];
+}
+
+// units u0, u0 + us, ... of sweep step kb (Pinv already in g.piv)
+__device__ __forceinline__ void gj_step_units(GjShared& g, float* M, int np, int kb, const float* Rw, float* Rn, int u0,
+                                              int us) {
+  const int nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols;
+  const int units = g.ustart[nbk];
+  const int K0 = kb * kGjB, K1 = K0 + kGjB;
+  const int tid = threadIdx.x;
+  int ib = 0;
+  for (int u = u0; u < units; u += us) {
+    while (g.ustart[ib + 1] <= u) ++ib;   // units are visited in increasing order
+    const int I0 = ib * kGjB;
+    const int cu = I0 / kGjCols + (u - g.ustart[ib]);
+    const bool pivrow = ib == kb;
+    __syncthreads();
+    if (!pivrow)
+      for (int q = tid; q < kGjB * kGjB; q += blockDim.x) g.rs[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + I0 + (q & 31)];
+    __syncthreads();
+    for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
+      const int k = q >> 5, i = q & 31;
+      float sacc;
+      if (pivrow) {
+        sacc = g.piv[i][k];
+      } else {
+        // V = C_I Pinv with C_I[i][l] = R[l][I0 + i]
+        sacc = 0.f;
+#pragma unroll 8
+        for (int l = 0; l < kGjB; ++l) sacc = fmaf(g.rs[l][i], g.piv[l][k], sacc);
+      }
+      g.vt[k][i] = sacc;
+    }
+    __syncthreads();
+    const int j = cu * kGjCols + tid;
+    if (j < I0 || j >= np) continue;
+    float a[kGjB];
+    if (j >= K0 && j < K1) {
+#pragma unroll
+      for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? -g.piv[i][j - K0] : g.vt[j - K0][i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? 0.f : M[(int64_t)(I0 + i) * np + j];
+      const float sg = pivrow ? 1.f : -1.f;
+      float rv[kGjB];
+#pragma unroll
+      for (int k = 0; k < kGjB; ++k) rv[k] = Rw[(int64_t)k * np + j];
+#pragma unroll
+      for (int k = 0; k < kGjB; ++k) {
+        const float r = sg * rv[k];
+        const float4* vk = reinterpret_cast<const float4*>(&g.vt[k][0]);
+#pragma unroll
+        for (int i4 = 0; i4 < kGjB / 4; ++i4) {
+          const float4 t = vk[i4];
+          a[4 * i4] = fmaf(t.x, r, a[4 * i4]);
+          a[4 * i4 + 1] = fmaf(t.y, r, a[4 * i4 + 1]);
+          a[4 * i4 + 2] = fmaf(t.z, r, a[4 * i4 + 2]);
+          a[4 * i4 + 3] = fmaf(t.w, r, a[4 * i4 + 3]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kGjB; ++i) M[(int64_t)(I0 + i) * np + j] = a[i];
+    if (kb + 1 < nbk) {
+      if (ib == kb + 1) {
+#pragma unroll
+        for (int i = 0; i < kGjB; ++i) Rn[(int64_t)i * np + j] = a[i];
+      } else if (ib < kb + 1 && j >= K1 && j < K1 + kGjB) {
+        float4* dst = reinterpret_cast<float4*>(Rn + (int64_t)(j - K1) * np + I0);
+#pragma unroll
+        for (int i4 = 0; i4 < kGjB / 4; ++i4)
+          dst[i4] = make_float4(a[4 * i4], a[4 * i4 + 1], a[4 * i4 + 2], a[4 * i4 + 3]);
+      }
+    }
+  }
+}
+
+// tiles t0, t0 + ts, ... of the mirror pass: A^-1 = -M on the upper block triangle, transposed below
+__device__ __forceinline__ void gj_mirror(GjShared& g, float* M, int np, int t0, int ts) {
+  const int nbk = np / kGjB;
+  for (int t = t0; t < nbk * nbk; t += ts) {
+    const int ib = t / nbk, jb = t - ib * nbk;
+    if (jb < ib) continue;   // block-uniform
+    __syncthreads();
+    for (int q = threadIdx.x; q < kGjB * kGjB; q += blockDim.x) {
+      const int i = q >> 5, j = q & 31;
+      float* m = M + (int64_t)(ib * kGjB + i) * np + jb * kGjB + j;
+      const float v = -*m;
+      *m = v;
+      g.rs[i][j] = v;
+    }
+    __syncthreads();
+    if (jb > ib)
+      for (int q = threadIdx.x; q < kGjB * kGjB; q += blockDim.x) {
+        const int i = q >> 5, j = q & 31;
+        M[(int64_t)(jb * kGjB + i) * np + ib * kGjB + j] = g.rs[j][i];
+      }
+  }
+}
+
+// The whole-mesh form (and a one-instance cluster form): the sweep on the
+// grid, launched cooperatively with kGjCols threads, one grid barrier per
+// step.  Every CTA inverts the pivot block itself (one warp, same inputs and
+// order: the same Pinv everywhere).  c.ok[0] is set to 1 only if every pivot
+// was positive.
+__global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volatile double* err) {
+  __shared__ GjShared g;
+  const int np = c.np, nbk = np / kGjB;
+  const int tid = threadIdx.x;
+  const int units = gj_units(g, np);
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x, g0 = blockIdx.x * (int64_t)blockDim.x + tid;
   unsigned* count = c.bar;
   volatile unsigned* gen = c.bar + 1;
@@ -198,127 +292,51 @@ __global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volat
   for (int kb = 0; kb < nbk; ++kb) {
     const float* Rw = c.rowp + (int64_t)(kb & 1) * kGjB * np;
     float* Rn = c.rowp + (int64_t)((kb + 1) & 1) * kGjB * np;
-    const int K0 = kb * kGjB, K1 = K0 + kGjB;
     __syncthreads();   // piv of the previous step is no longer read
-    if (tid < 32) good = gj_inverse32_warp(Rw + K0, np, piv) && good;   // thread 0 keeps the flag
+    if (tid < 32) good = gj_inverse32_warp(Rw + kb * kGjB, np, g.piv) && good;   // thread 0 keeps the flag
     __syncthreads();
-    int ib = 0;
-    for (int u = blockIdx.x; u < units; u += gridDim.x) {
-      while (ustart[ib + 1] <= u) ++ib;   // units are visited in increasing order
-      const int I0 = ib * kGjB;
-      const int cu = I0 / kGjCols + (u - ustart[ib]);
-      const bool pivrow = ib == kb;
-      {
-        __syncthreads();
-        if (!pivrow)
-          for (int q = tid; q < kGjB * kGjB; q += blockDim.x) rs[q >> 5][q & 31] = Rw[(int64_t)(q >> 5) * np + I0 + (q & 31)];
-        __syncthreads();
-        for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
-          const int k = q >> 5, i = q & 31;
-          float sacc;
-          if (pivrow) {
-            sacc = piv[i][k];
-          } else {
-            // V = C_I Pinv with C_I[i][l] = R[l][I0 + i]
-            sacc = 0.f;
-#pragma unroll 8
-            for (int l = 0; l < kGjB; ++l) sacc = fmaf(rs[l][i], piv[l][k], sacc);
-          }
-          vt[k][i] = sacc;
-        }
-        __syncthreads();
-        const int j = cu * kGjCols + tid;
-        if (j < I0 || j >= np) continue;
-        float a[kGjB];
-        if (j >= K0 && j < K1) {
-#pragma unroll
-          for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? -piv[i][j - K0] : vt[j - K0][i];
-        } else {
-#pragma unroll
-          for (int i = 0; i < kGjB; ++i) a[i] = pivrow ? 0.f : c.M[(int64_t)(I0 + i) * np + j];
-            const float sg = pivrow ? 1.f : -1.f;
-          float rv[kGjB];
-#pragma unroll
-          for (int k = 0; k < kGjB; ++k) rv[k] = Rw[(int64_t)k * np + j];
-#pragma unroll
-          for (int k = 0; k < kGjB; ++k) {
-            const float r = sg * rv[k];
-            const float4* vk = reinterpret_cast<const float4*>(&vt[k][0]);
-#pragma unroll
-            for (int i4 = 0; i4 < kGjB / 4; ++i4) {
-              const float4 t = vk[i4];
-              a[4 * i4] = fmaf(t.x, r, a[4 * i4]);
-              a[4 * i4 + 1] = fmaf(t.y, r, a[4 * i4 + 1]);
-              a[4 * i4 + 2] = fmaf(t.z, r, a[4 * i4 + 2]);
-              a[4 * i4 + 3] = fmaf(t.w, r, a[4 * i4 + 3]);
-            }
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < kGjB; ++i) c.M[(int64_t)(I0 + i) * np + j] = a[i];
-        if (kb + 1 < nbk) {
-          if (ib == kb + 1) {
-#pragma unroll
-            for (int i = 0; i < kGjB; ++i) Rn[(int64_t)i * np + j] = a[i];
-          } else if (ib < kb + 1 && j >= K1 && j < K1 + kGjB) {
-            float4* dst = reinterpret_cast<float4*>(Rn + (int64_t)(j - K1) * np + I0);
-#pragma unroll
-            for (int i4 = 0; i4 < kGjB / 4; ++i4)
-              dst[i4] = make_float4(a[4 * i4], a[4 * i4 + 1], a[4 * i4 + 2], a[4 * i4 + 3]);
-          }
-        }
-      }
-    }
+    gj_step_units(g, c.M, np, kb, Rw, Rn, blockIdx.x, gridDim.x);
     if (!grid_barrier(count, gen, err)) return;
   }
-  // mirror: A^-1 = -M on the upper block triangle, transposed below it
-  for (int t = blockIdx.x; t < nbk * nbk; t += gridDim.x) {
-    const int ib = t / nbk, jb = t - ib * nbk;
-    if (jb < ib) continue;   // block-uniform
-    __syncthreads();
-    for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
-      const int i = q >> 5, j = q & 31;
-      float* m = c.M + (int64_t)(ib * kGjB + i) * np + jb * kGjB + j;
-      const float v = -*m;
-      *m = v;
-      rs[i][j] = v;
-    }
-    __syncthreads();
-    if (jb > ib)
-      for (int q = tid; q < kGjB * kGjB; q += blockDim.x) {
-        const int i = q >> 5, j = q & 31;
-        c.M[(int64_t)(jb * kGjB + i) * np + ib * kGjB + j] = rs[j][i];
-      }
-  }
+  (void)units;
+  gj_mirror(g, c.M, np, blockIdx.x, gridDim.x);
   if (blockIdx.x == 0 && tid == 0) *c.ok = good ? 1 : 0;
 }
 
-// ---------------------------------------------------------------- PCG ----
-// (P e) at a vertex with scaled offset d, aggregate a and free mask f, for the
-// coarse correction e of the current iteration (plain loads: e is written
-// earlier in the same kernel)
-__device__ __forceinline__ Vec3<float> prolong_at(const float* e, float dx, float dy, float dz, int a, unsigned f) {
-  const float4 e0 = reinterpret_cast<const float4*>(e)[2 * a];
-  const float4 e1 = reinterpret_cast<const float4*>(e)[2 * a + 1];
-  // t = (e0.x, e0.y, e0.z), w = (e0.w, e1.x, e1.y): t + w x d
-  const float px = e0.x + (e1.x * dz - e1.y * dy);
-  const float py = e0.y + (e1.y * dx - e0.w * dz);
-  const float pz = e0.z + (e0.w * dy - e1.x * dx);
-  return {(f & 1u) ? px : 0.f, (f & 2u) ? py : 0.f, (f & 4u) ? pz : 0.f};
-}
-// ... from the per-vertex mode array
-__device__ __forceinline__ Vec3<float> prolong(const CoarseDev& c, int64_t v) {
-  const float4 m = __ldg(c.mode + v);
-  return prolong_at(c.e, m.x, m.y, m.z, mode_agg(m), mode_mask(m));
-}
-// ... from the column data packed into a block record (same values: d is fp16-exact)
-__device__ __forceinline__ Vec3<float> prolong_rec(const float* e, unsigned a0, unsigned a1) {
-  const float dx = __half2float(__ushort_as_half((unsigned short)(a0 & 0xffffu)));
-  const float dy = __half2float(__ushort_as_half((unsigned short)(a0 >> 16)));
-  const float dz = __half2float(__ushort_as_half((unsigned short)(a1 & 0xffffu)));
-  return prolong_at(e, dx, dy, dz, (int)((a1 >> 16) & 0x1fffu), a1 >> 29);
+// The per-instance form for batches: one CTA per instance (largest first by
+// `order`), block barriers only; row panels in a per-CTA scratch of
+// 2 x 32 x max_np floats.  c.ok[inst] = 1 only if every pivot was positive.
+__global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert_inst(CoarseDev c, const int32_t* __restrict__ order) {
+  __shared__ GjShared g;
+  const int tid = threadIdx.x;
+  float* rowp = c.rowp + (int64_t)blockIdx.x * 2 * kGjB * c.max_np;
+  for (int idx = blockIdx.x; idx < c.n_inst; idx += gridDim.x) {
+    const int inst = order ? order[idx] : idx;
+    const int nc = 6 * (c.inst_agg[inst + 1] - c.inst_agg[inst]);
+    const int np = ((nc + kGjB - 1) / kGjB) * kGjB;
+    float* M = c.M + c.inst_moff[inst];
+    const int nbk = np / kGjB;
+    gj_units(g, np);
+    for (int i = nc + tid; i < np; i += blockDim.x) M[(int64_t)i * np + i] = 1.f;
+    __syncthreads();
+    for (int q = tid; q < np * kGjB; q += blockDim.x) rowp[q] = M[q];
+    bool good = true;
+    for (int kb = 0; kb < nbk; ++kb) {
+      const float* Rw = rowp + (int64_t)(kb & 1) * kGjB * np;
+      float* Rn = rowp + (int64_t)((kb + 1) & 1) * kGjB * np;
+      __syncthreads();
+      if (tid < 32) good = gj_inverse32_warp(Rw + kb * kGjB, np, g.piv) && good;
+      __syncthreads();
+      gj_step_units(g, M, np, kb, Rw, Rn, 0, 1);
+    }
+    __syncthreads();
+    gj_mirror(g, M, np, 0, 1);
+    if (tid == 0) c.ok[inst] = good ? 1 : 0;
+    __syncthreads();
+  }
 }
 
+// ---------------------------------------------------------------- PCG ----
 // z_j = D^-1 r_j (stored) + (P e)_j, rounded the same wherever it is formed: in
 // the gathers from the block record, for the own row from the mode array
 template <typename R> struct ZCoarse {
@@ -343,54 +361,6 @@ template <typename R> struct ZCoarse {
     return a;
   }
 };
-
-// Fixed-point scale of an iteration's coarse residual: a power of two putting
-// 64 ||r|| at 2^50 (|P^T r| of an aggregate is far below 2^12 ||r||, so sums
-// stay inside 64 bits with room for a residual that grows between iterations)
-__device__ __forceinline__ float coarse_scale(double rr) {
-  int ex;
-  frexp(64.0 * sqrt(fmax(rr, 1e-300)), &ex);
-  return ldexpf(1.f, max(-126, min(127, 50 - ex)));
-}
-
-// c.rc += P^T r over the calling warp's rows (every lane calls; consecutive
-// rows of one aggregate are summed first by a segmented shuffle reduction, then
-// one 64-bit atomic per segment and component: integer sums do not depend on
-// the order of the atomics)
-__device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, int64_t row, float rx, float ry,
-                                                float rz, float scale) {
-  int key = -1;
-  long long q[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) q[k] = 0;
-  if (valid) {
-    const float4 m = __ldg(c.mode + row);
-    key = mode_agg(m);
-    const unsigned f = mode_mask(m);
-    const float x = (f & 1u) ? rx : 0.f, y = (f & 2u) ? ry : 0.f, z = (f & 4u) ? rz : 0.f;
-    // P_v^T r = (r, d x r)
-    const float v6[6] = {x, y, z, m.y * z - m.z * y, m.z * x - m.x * z, m.x * y - m.y * x};
-#pragma unroll
-    for (int k = 0; k < 6; ++k) q[k] = __float2ll_rn(v6[k] * scale);   // power-of-two scale: exact
-  }
-  const int lane = threadIdx.x & 31;
-  const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-  const bool head = lane == 0 || prev != key;
-  const unsigned heads = __ballot_sync(0xffffffffu, head);
-  const int seg = __popc(heads & (0xffffffffu >> (31 - lane)));
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int so = __shfl_down_sync(0xffffffffu, seg, o);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      const long long t = __shfl_down_sync(0xffffffffu, q[k], o);
-      if (lane + o < 32 && so == seg) q[k] += t;
-    }
-  }
-  if (head && key >= 0)
-#pragma unroll
-    for (int k = 0; k < 6; ++k) atomicAdd(c.rc + 6 * key + k, (unsigned long long)q[k]);
-}
 
 // e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows
 // strided over the grid), pc += (P^T r) . e over those rows.  rcf: shared

@@ -206,28 +206,31 @@ __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier
 
 // Record slot 10 (a pad slot the assembly leaves zero) receives, at the start of
 // each solve, the shared::cluster address of the z|p row of the block's column;
-// slot 9 (the column) is left intact.
+// slot 9 (the column) is left intact; slot 11 carries the column's two-level
+// coarse word (aux1) when the per-instance coarse data is attached.
 __device__ __forceinline__ Blk<float> ld_srec(const float* srec, int64_t i) {
   const float4* p = reinterpret_cast<const float4*>(srec) + 3 * i;
   const float4 a = p[0], b = p[1], c = p[2];
-  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z)};
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z), 0u, __float_as_uint(c.w)};
 }
 __device__ __forceinline__ Blk<double> ld_srec(const double* srec, int64_t i) {
   const double2* p = reinterpret_cast<const double2*>(srec) + 6 * i;
   const double2 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4], f = p[5];
-  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x)};
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x), 0u,
+          (unsigned)__double_as_longlong(f.y)};
 }
 // the same from global memory with plain loads (the address slot was written in this kernel,
 // so not through the read-only path)
 __device__ __forceinline__ Blk<float> ld_grec(const float* rec, int64_t i) {
   const float4* p = reinterpret_cast<const float4*>(rec) + 3 * i;
   const float4 a = p[0], b = p[1], c = p[2];
-  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z)};
+  return {{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x}, __float_as_int(c.z), 0u, __float_as_uint(c.w)};
 }
 __device__ __forceinline__ Blk<double> ld_grec(const double* rec, int64_t i) {
   const double2* p = reinterpret_cast<const double2*>(rec) + 6 * i;
   const double2 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4], f = p[5];
-  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x)};
+  return {{a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x}, (int)__double_as_longlong(f.x), 0u,
+          (unsigned)__double_as_longlong(f.y)};
 }
 
 // Shared memory the kernel needs for its vectors and local row offsets, per CTA.
@@ -244,7 +247,7 @@ struct ClusterPcgOut {
 
 // Static shared memory of a cluster PCG kernel.
 template <typename R> struct ClusterShared {
-  Dacc<R> pub[2][2];                  // CTA totals: [0] p.q, [1] r.z and r.r
+  Dacc<R> pub[3][2];                  // CTA totals: [0] p.q, [1] r.z and r.r, [2] coarse (P^T r).e
   Dacc<R> wsum[2][kClusterWarps];     // warp totals
   uint64_t mbar[kRingMax];            // record ring (slot 0 alone when the records are resident)
   uint32_t zbase[kClusterMax];        // shared::cluster address of each rank's z|p rows
@@ -304,6 +307,41 @@ __device__ __forceinline__ int cl_owner(int c, const int32_t* rowb, int csize, f
   return o;
 }
 
+// Coarse correction of one instance on the calling cluster: e = A_c^-1 P^T r
+// (the instance's dense block Mi, np x np), one row per warp over the cluster's
+// warps.  Every CTA stages P^T r (fixed point -> float) into srcf; each row of e
+// is stored into every CTA's copy sce over DSMEM (visible after the next
+// cluster barrier); pc += (P^T r).e over the rows this CTA computed.
+template <typename R>
+__device__ __forceinline__ void coarse_product_cluster(int crank, int csize, const float* Mi, int nc, int np,
+                                                       const unsigned long long* rc, float inv_scale, float* sce,
+                                                       float* srcf, Dacc<R>& pc) {
+  const int tid = threadIdx.x, lane = tid & 31, wpb = blockDim.x >> 5;
+#pragma unroll 4
+  for (int i = tid; i < np; i += blockDim.x)
+    srcf[i] = i < nc ? __ll2float_rn((long long)__ldcg(rc + i)) * inv_scale : 0.f;
+  __syncthreads();
+  const float4* r4 = reinterpret_cast<const float4*>(srcf);
+  for (int row = crank * wpb + (tid >> 5); row < nc; row += csize * wpb) {
+    const float4* Mr = reinterpret_cast<const float4*>(Mi + (int64_t)row * np);
+    float sacc = 0.f;
+#pragma unroll 4
+    for (int j = lane; j < (np >> 2); j += 32) {
+      const float4 m = __ldcg(Mr + j), x = r4[j];
+      sacc = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, sacc))));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+    if (csize == 1) {
+      if (lane == 0) sce[row] = sacc;
+    } else if (lane < csize) {
+      const uint32_t a = cluster_map(smem_addr(sce + row), lane);
+      asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(sacc) : "memory");
+    }
+    if (lane == 0) dacc_dot3(pc, Vec3<R>{R(srcf[row]), R(0), R(0)}, Vec3<R>{R(sacc), R(0), R(0)});
+  }
+}
+
 // Solve the system of block rows [gbase, gbase + nbr) (its columns lie in the
 // same range) on the calling cluster.  b: right-hand side (3n, simkit layout,
 // FP64) scaled by bsign, pinned DOFs forced to zero; x written to xout
@@ -317,11 +355,11 @@ __device__ __forceinline__ int cl_owner(int c, const int32_t* rowb, int csize, f
 // most, refilled while later chunks (and, at the end of an iteration, the
 // reductions and vector updates) are processed.  Without room for two slots
 // the records are read from global memory.
-template <typename R, int G>
+template <typename R, int G, bool CO>
 __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
     cgx::cluster_group& cl, const Bsr<R>& A, R* rec, int64_t gbase, int64_t nbr, const double* __restrict__ b,
     double bsign, const uint8_t* __restrict__ pinned, R* __restrict__ xout, double rtol, int max_iter,
-    int smem_bytes, unsigned char* smem_raw, ClusterShared<R>& sh) {
+    int smem_bytes, unsigned char* smem_raw, ClusterShared<R>& sh, const CoarseDev& cd, int inst) {
   const int crank = (int)cl.block_rank();
   const int csize = (int)cl.num_blocks();
   const int64_t r0 = gbase + nbr * crank / csize;
@@ -344,6 +382,24 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
   const uint32_t my_span = (uint32_t)(nr * kRowBytes);
   const int tid = threadIdx.x;
   const int rows_per_pass = blockDim.x / G;
+  // two-level coarse data of this instance (per-instance form); the instance's e and
+  // P^T r live past the smem_bytes the vectors and records may use
+  int cnc = 0, cnp = 0;
+  const float* cM = nullptr;
+  unsigned long long* crc = nullptr;
+  bool con = false;
+  float* sce = nullptr;
+  float* srcf = nullptr;
+  if constexpr (CO) {
+    const int ag0 = cd.inst_agg[inst];
+    cnc = 6 * (cd.inst_agg[inst + 1] - ag0);
+    cnp = ((cnc + 31) / 32) * 32;
+    cM = cd.M + cd.inst_moff[inst];
+    crc = cd.rc + 6 * (int64_t)ag0;
+    con = cd.ok[inst] != 0;
+    sce = reinterpret_cast<float*>(smem_raw + smem_bytes);
+    srcf = sce + kCoarseInstMax;
+  }
 
   if (tid < csize) sh.zbase[tid] = csize > 1 ? cluster_map(smem_addr(szp), tid) : smem_addr(szp);
   if (tid <= csize) sh.rowb[tid] = (int32_t)(nbr * tid / csize);
@@ -448,6 +504,25 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
   Dacc<R> rz = s2[0];
   double rr = dacc_value(s2[1]);
   const double bb = rr;
+  double rr_prev = rr;
+  if (CO && con && bb > 0.0) {
+    // coarse part of z_0 = D^-1 r_0 + P e_0
+    const float sc = coarse_scale(rr_prev);
+    for (int base = tid & ~31; base < nr; base += blockDim.x) {
+      const int i = base + (tid & 31);
+      const bool ok = i < nr;
+      const R* rp = sr + 4 * (ok ? i : 0);
+      coarse_restrict(cd, ok, r0 + i, float(rp[0]), float(rp[1]), float(rp[2]), sc);
+    }
+    csync(cl, csize);
+    Dacc<R> pc[1];
+    dacc_zero(pc[0]);
+    coarse_product_cluster<R>(crank, csize, cM, cnc, cnp, crc, 1.f / sc, sce, srcf, pc[0]);
+    cluster_total<R, 1>(cl, csize, pc, sh.pub[2], sh.wsum);
+    rz = dacc_add(rz, pc[0]);
+    if (crank == 0)
+      for (int i = tid; i < cnc; i += blockDim.x) crc[i] = 0ull;
+  }
   const double tol2 = rtol * rtol * bb;
   bool done = rr <= tol2 || bb == 0.0 || max_iter <= 0;
   // the per-iteration stop test in the working precision (FP64 compares cost a 64-cycle
@@ -465,7 +540,7 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
   while (!done) {
     const uint32_t po = (uint32_t)(4 * (1 + (cur ^ 1)) * sizeof(R));  // byte offset of p_{k-1} in a z|p row
     const int pn = 4 * (1 + cur);
-    auto gather = [&](uint32_t caddr) -> Vec3<R> {
+    auto gather = [&](uint32_t caddr, uint32_t cword) -> Vec3<R> {
       const uint32_t d = caddr - my_cbase;
       Vec3<R> z, pp;
       if (d < my_span) {
@@ -474,6 +549,10 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
       } else {
         z = ld_cluster3(caddr, R(0));
         pp = ld_cluster3(caddr + po, R(0));
+      }
+      if (CO && con) {
+        const Vec3<float> pe = prolong_word(sce, cword);
+        z = {z.x + R(pe.x), z.y + R(pe.y), z.z + R(pe.z)};
       }
       return pdir3(z, pp, beta);
     };
@@ -515,7 +594,7 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
         Vec3<R> v[kU];
 #pragma unroll
         for (int u = 0; u < kU; ++u)
-          if (k0 + u * G < K) v[u] = gather((uint32_t)bk[u].col);
+          if (k0 + u * G < K) v[u] = gather((uint32_t)bk[u].col, bk[u].aux1);
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
           if (k0 + u * G < K) {
@@ -534,7 +613,12 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
       if (lane == 0 && valid) {
         R* zr = szp + ZP * li;
         const int pold = 12 - pn;  // the other p buffer
-        const Vec3<R> p = pdir3(Vec3<R>{zr[0], zr[1], zr[2]}, Vec3<R>{zr[pold], zr[pold + 1], zr[pold + 2]}, beta);
+        Vec3<R> zo{zr[0], zr[1], zr[2]};
+        if (CO && con) {
+          const Vec3<float> pe = prolong_word(sce, __ldg(cd.colpack + r0 + li));
+          zo = {zo.x + R(pe.x), zo.y + R(pe.y), zo.z + R(pe.z)};
+        }
+        const Vec3<R> p = pdir3(zo, Vec3<R>{zr[pold], zr[pold + 1], zr[pold + 2]}, beta);
         zr[pn] = p.x; zr[pn + 1] = p.y; zr[pn + 2] = p.z; zr[pn + 3] = R(0);
         R* q = sq + 4 * li;
         q[0] = a0; q[1] = a1; q[2] = a2;
@@ -560,23 +644,29 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
     Dacc<R> u2[2];
     dacc_zero(u2[0]);
     dacc_zero(u2[1]);
-    for (int i = tid; i < nr; i += blockDim.x) {
-      R* x = sx + 4 * i;
-      R* r = sr + 4 * i;
-      R* zr = szp + ZP * i;
-      const R* p = zr + pn;
-      const R* q = sq + 4 * i;
-      const R* J = sj + 9 * i;
-      x[0] += a * p[0];
-      x[1] += a * p[1];
-      x[2] += a * p[2];
-      const Vec3<R> rn{r[0] - a * q[0], r[1] - a * q[1], r[2] - a * q[2]};
-      r[0] = rn.x; r[1] = rn.y; r[2] = rn.z;
-      const Vec3<R> z{J[0] * rn.x + J[1] * rn.y + J[2] * rn.z, J[3] * rn.x + J[4] * rn.y + J[5] * rn.z,
-                      J[6] * rn.x + J[7] * rn.y + J[8] * rn.z};
-      zr[0] = z.x; zr[1] = z.y; zr[2] = z.z;
-      dacc_dot3(u2[0], rn, z);
-      dacc_dot3(u2[1], rn, rn);
+    const float csc = CO ? coarse_scale(rr_prev) : 1.f;
+    for (int base = tid & ~31; base < nr; base += blockDim.x) {   // warp-uniform trip count
+      const int i = base + (tid & 31);
+      Vec3<R> rn{R(0), R(0), R(0)};
+      if (i < nr) {
+        R* x = sx + 4 * i;
+        R* r = sr + 4 * i;
+        R* zr = szp + ZP * i;
+        const R* p = zr + pn;
+        const R* q = sq + 4 * i;
+        const R* J = sj + 9 * i;
+        x[0] += a * p[0];
+        x[1] += a * p[1];
+        x[2] += a * p[2];
+        rn = Vec3<R>{r[0] - a * q[0], r[1] - a * q[1], r[2] - a * q[2]};
+        r[0] = rn.x; r[1] = rn.y; r[2] = rn.z;
+        const Vec3<R> z{J[0] * rn.x + J[1] * rn.y + J[2] * rn.z, J[3] * rn.x + J[4] * rn.y + J[5] * rn.z,
+                        J[6] * rn.x + J[7] * rn.y + J[8] * rn.z};
+        zr[0] = z.x; zr[1] = z.y; zr[2] = z.z;
+        dacc_dot3(u2[0], rn, z);
+        dacc_dot3(u2[1], rn, rn);
+      }
+      if (CO && con) coarse_restrict(cd, i < nr, r0 + i, float(rn.x), float(rn.y), float(rn.z), csc);
     }
     cluster_total<R, 2>(cl, csize, u2, sh.pub[1], sh.wsum);
     ++it;
@@ -588,9 +678,26 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
       status = SKG_ERR_NONFINITE;
       break;
     }
+    rr_prev = dacc_value(u2[1]);
     if (rrr <= tol2r || it >= max_iter) break;
+    if (CO && con) {
+      Dacc<R> pc[1];
+      dacc_zero(pc[0]);
+      coarse_product_cluster<R>(crank, csize, cM, cnc, cnp, crc, 1.f / csc, sce, srcf, pc[0]);
+      cluster_total<R, 1>(cl, csize, pc, sh.pub[2], sh.wsum);
+      rz = dacc_add(rz, pc[0]);
+      // read by every CTA before that barrier; next accumulated after the next one
+      if (crank == 0)
+        for (int i = tid; i < cnc; i += blockDim.x) crc[i] = 0ull;
+    }
     beta = dacc_r(rz) / dacc_r(rz_old);
     cur ^= 1;
+  }
+  if (CO && con) {
+    // the last restriction is never used: leave the instance's residual at zero for the next solve
+    csync(cl, csize);
+    if (crank == 0)
+      for (int i = tid; i < cnc; i += blockDim.x) crc[i] = 0ull;
   }
   // solution to global memory (padded, the layout the line search reads)
   for (int i = tid; i < nr; i += blockDim.x) {
@@ -616,16 +723,17 @@ __device__ __forceinline__ ClusterPcgOut cluster_pcg_range(
   return ClusterPcgOut{it, status, dacc_value(rr_acc), dacc_value(rz), bb};
 }
 
-// one system on one cluster (pcg_mode 2)
-template <typename R, int G>
+// one system on one cluster (pcg_mode 2); CO: two-level with the per-instance
+// coarse data of instance 0 (e and P^T r past smem_bytes in dynamic shared memory)
+template <typename R, int G, bool CO>
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_pcg_cluster(Bsr<R> A, const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
-                  R* __restrict__ xout, double rtol, int max_iter, double* scal, int smem_bytes) {
+                  R* __restrict__ xout, double rtol, int max_iter, double* scal, int smem_bytes, CoarseDev cd) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ClusterShared<R> sh;
-  const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, const_cast<R*>(A.rec), 0, A.nbr, b, bsign, pinned, xout,
-                                                  rtol, max_iter, smem_bytes, smem_raw, sh);
+  const ClusterPcgOut o = cluster_pcg_range<R, G, CO>(cl, A, const_cast<R*>(A.rec), 0, A.nbr, b, bsign, pinned,
+                                                      xout, rtol, max_iter, smem_bytes, smem_raw, sh, cd, 0);
   if (cl.block_rank() == 0 && threadIdx.x == 0) {
     scal[S_ITERS] = o.iters;
     scal[S_RR] = o.rr;
@@ -641,13 +749,13 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 // solves it to that instance's tolerance.  inst_rows (n_inst + 1) are the
 // instances' block-row offsets; order lists the n instances this launch
 // serves; inactive instances are skipped.
-template <typename R, int G>
+template <typename R, int G, bool CO>
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_pcg_cluster_queue(Bsr<R> A, const int32_t* __restrict__ inst_rows, const int32_t* __restrict__ order,
                         int n, const uint8_t* __restrict__ active, const double* __restrict__ eta,
                         const double* __restrict__ b, double bsign, const uint8_t* __restrict__ pinned,
                         R* __restrict__ xout, int max_iter, int32_t* iters_out, int32_t* status_out,
-                        unsigned* queue, int smem_bytes) {
+                        unsigned* queue, int smem_bytes, CoarseDev cd) {
   cgx::cluster_group cl = cgx::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ ClusterShared<R> sh;
@@ -675,8 +783,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
       }
       continue;
     }
-    const ClusterPcgOut o = cluster_pcg_range<R, G>(cl, A, const_cast<R*>(A.rec), gbase, nbr, b, bsign, pinned,
-                                                    xout, eta[inst], max_iter, smem_bytes, smem_raw, sh);
+    const ClusterPcgOut o = cluster_pcg_range<R, G, CO>(cl, A, const_cast<R*>(A.rec), gbase, nbr, b, bsign, pinned,
+                                                        xout, eta[inst], max_iter, smem_bytes, smem_raw, sh, cd, inst);
     if (cl.block_rank() == 0 && threadIdx.x == 0) {
       iters_out[inst] = o.iters;
       status_out[inst] = o.status;

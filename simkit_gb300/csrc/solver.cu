@@ -586,6 +586,7 @@ __global__ void __launch_bounds__(kCgThreads, 1) k_pcg_cg2(Bsr<R> A, PcgVecs<R> 
 
 }  // namespace skg
 
+#include "coarse_common.cuh"
 #include "pcg_cluster.cuh"
 #include "pcg_grid.cuh"
 #include "coarse.cuh"
@@ -772,6 +773,16 @@ static CoarseDev make_coarse_dev(const skg_tet_mesh* m, const Workspace& w) {
   c.e = w.ce;
   c.ok = w.cok;
   c.bar = w.cbar;
+  c.m_floats = (int64_t)c.np * c.np;
+  if (h->inst_agg) {
+    c.m_floats = h->m_floats;
+    c.n_inst = h->n_inst;
+    c.max_np = h->max_np;
+    c.inst_agg = h->inst_agg;
+    c.agg_inst = h->agg_inst;
+    c.inst_moff = h->inst_moff;
+    c.colpack = h->colpack;
+  }
   return c;
 }
 
@@ -779,14 +790,22 @@ static CoarseDev make_coarse_dev(const skg_tet_mesh* m, const Workspace& w) {
 // non-positive pivot (or a barrier timeout) c.ok stays 0 and the PCG runs
 // one-level.  Two launches.
 template <typename R>
-static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cudaStream_t s) {
-  SKG_CUDA(cudaMemsetAsync(c.M, 0, sizeof(float) * (size_t)c.np * c.np, s));
-  SKG_CUDA(cudaMemsetAsync(c.ok, 0, sizeof(int), s));
+static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cudaStream_t s,
+                          const int32_t* order = nullptr) {
+  SKG_CUDA(cudaMemsetAsync(c.M, 0, sizeof(float) * (size_t)c.m_floats, s));
+  SKG_CUDA(cudaMemsetAsync(c.ok, 0, sizeof(int) * (size_t)(c.inst_agg ? c.n_inst : 1), s));
   SKG_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), s));
   SKG_CUDA(cudaMemsetAsync(scal + S_CERR, 0, sizeof(double), s));
   const int64_t gal_threads = 32 * (int64_t)c.n_cb;
   k_coarse_galerkin<R><<<(int)((gal_threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(A, c);
   SKG_LAUNCHED();
+  if (c.inst_agg && c.n_inst > 1) {
+    // batches: one CTA per instance, largest first
+    const int grid = c.n_inst < kCoarseInvCtas ? c.n_inst : kCoarseInvCtas;
+    k_coarse_invert_inst<<<grid, kGjCols, 0, s>>>(c, order);
+    SKG_LAUNCHED();
+    return SKG_OK;
+  }
   static int per_sm = 0;
   if (per_sm == 0) {
     SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coarse_invert, kGjCols, 0));
@@ -805,16 +824,19 @@ static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cud
   return SKG_OK;
 }
 
+// cd (per-instance form, instance 0): the two-level kernel, which keeps the
+// instance's coarse vectors in the last kCoarseSmem bytes of dynamic shared memory
 template <typename R>
 static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, R* xout,
-                              double rtol, int max_iter, double* scal, cudaStream_t s) {
-  auto kern = k_pcg_cluster<R, kGc>;
-  static thread_local bool configured = false;
-  if (!configured) {
+                              double rtol, int max_iter, double* scal, cudaStream_t s, const CoarseDev* cd = nullptr) {
+  const void* kern = cd ? (const void*)k_pcg_cluster<R, kGc, true> : (const void*)k_pcg_cluster<R, kGc, false>;
+  static thread_local bool configured[2] = {false, false};
+  if (!configured[cd ? 1 : 0]) {
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
-    configured = true;
+    configured[cd ? 1 : 0] = true;
   }
+  const int budget = cd ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
   int csize = A.nbr >= 2048 ? kClusterMax : 8;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -836,11 +858,14 @@ static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, co
     if (csize <= 2) return fail(SKG_ERR_CUDA, "no thread-block cluster of the PCG kernel fits on this device");
     csize /= 2;
   }
-  if (cluster_vec_bytes(A.nbr, csize, (int)sizeof(R)) > kClusterSmemBudget)
+  if (cluster_vec_bytes(A.nbr, csize, (int)sizeof(R)) > budget)
     return fail(SKG_ERR_CAPACITY, "system too large for one cluster");
   Bsr<R> a2 = A;
-  int smem = kClusterSmemBudget;
-  SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, b, bsign, pinned, xout, rtol, max_iter, scal, smem));
+  int smem = budget;
+  CoarseDev c2 = cd ? *cd : CoarseDev{};
+  if (cd) SKG_CUDA(cudaMemsetAsync(cd->rc, 0, sizeof(unsigned long long) * 6 * (size_t)cd->n_agg, s));
+  void* args[] = {&a2, (void*)&b, &bsign, (void*)&pinned, &xout, &rtol, &max_iter, &scal, &smem, &c2};
+  SKG_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
   return SKG_OK;
 }
 
@@ -854,8 +879,9 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
                      cudaStream_t s, PcgResult* res, int variant = 0, const CoarseDev* cd = nullptr) {
   const int rb = reduce_blocks(A.nbr);
-  if (mode == 7 && !cd) mode = 5;
-  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : (cd ? 7 : 5);
+  const bool grid_form = cd && !cd->inst_agg;
+  if (mode == 7 && !grid_form) mode = 5;
+  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : (grid_form ? 7 : 5);
   if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 5;
   res->launches = 0;
   if (mode != 2) {
@@ -864,7 +890,8 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
     res->launches = 1;
   }
   if (mode == 2) {
-    SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s));
+    const CoarseDev* cc = cd && cd->inst_agg ? cd : nullptr;
+    SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s, cc));
     res->launches += 1;
   } else if (mode == 4) {
     int per_sm = 0;
@@ -1027,8 +1054,14 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
 
   info->newton_iters = 0; info->pcg_iters = 0; info->ls_trials = 0; info->status = SKG_OK;
   info->min_alpha = 1.0;
-  // two-level PCG (mode 7, or mode 3 on systems above the cluster size) when the mesh has coarse data
-  const bool two_level = m->coarse && (prm->pcg_mode == 7 || (prm->pcg_mode == 3 && n > kClusterAutoRows));
+  // two-level PCG when the mesh has coarse data: the whole-mesh form with the grid kernel (mode 7, or
+  // mode 3 above the cluster size), the per-instance form with the cluster kernel (mode 2, or mode 3
+  // up to the cluster size)
+  const bool inst_form = m->coarse && m->coarse->inst_agg;
+  const bool small = n <= kClusterAutoRows && n <= cluster_rows_limit<R>();
+  const bool two_level =
+      m->coarse && (inst_form ? (prm->pcg_mode == 2 || prm->pcg_mode == 3) && small && m->coarse->n_inst == 1
+                              : prm->pcg_mode == 7 || (prm->pcg_mode == 3 && n > kClusterAutoRows));
   CoarseDev cdev{};
   if (two_level) cdev = make_coarse_dev(m, w);
   double gg;
@@ -1085,7 +1118,8 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     aa.contact = contact;
     aa.u = st->u;
     aa.pinned = st->pinned;
-    aa.cmode = two_level ? cdev.mode : nullptr;
+    aa.cmode = two_level && !inst_form ? cdev.mode : nullptr;
+    aa.colpack = two_level && inst_form ? cdev.colpack : nullptr;
     pt.begin();
     SKG_TRY(launch_assemble<R>(aa, s));
     info->launches += 2;
@@ -1270,15 +1304,18 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
                             const uint8_t* active_h, int min_cluster, int vec_kb, const uint8_t* active,
                             const double* eta,
                             const double* b, const uint8_t* pinned, R* xout, int max_iter, int32_t* it_out,
-                            int32_t* st_out, unsigned* queue, cudaStream_t s, int* launches) {
-  auto kern = k_pcg_cluster_queue<R, kGc>;
-  static thread_local bool configured = false;
+                            int32_t* st_out, unsigned* queue, cudaStream_t s, int* launches,
+                            const CoarseDev* cd = nullptr) {
+  const void* kern = cd ? (const void*)k_pcg_cluster_queue<R, kGc, true> : (const void*)k_pcg_cluster_queue<R, kGc, false>;
+  static thread_local bool configured[2] = {false, false};
   static thread_local ClassStreams cs;
-  if (!configured) {
+  if (!configured[cd ? 1 : 0]) {
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
-    configured = true;
+    configured[cd ? 1 : 0] = true;
   }
+  // with the two-level data the instance's coarse vectors take the last kCoarseSmem bytes
+  const int64_t budget = cd ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
   if (!cs.ready) {
     for (int c = 0; c < 5; ++c) {
       SKG_CUDA(cudaStreamCreateWithFlags(&cs.s[c], cudaStreamNonBlocking));
@@ -1293,14 +1330,15 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
   while (cmin < min_cluster && cmin < kClusterMax) cmin *= 2;
   // smallest cluster of at least cmin CTAs whose per-CTA vectors take at most `target`
   // bytes (the rest holds block records), else the smallest that holds the vectors at all
-  const int64_t target = vec_kb > 0 ? (int64_t)vec_kb * 1024 : (int64_t)kClusterVecTarget;
+  int64_t target = vec_kb > 0 ? (int64_t)vec_kb * 1024 : (int64_t)kClusterVecTarget;
+  if (target > budget) target = budget;
   auto need = [&](int inst) {
     const int64_t rows = rows_h[inst + 1] - rows_h[inst];
     int c = cmin;
     while (c < kClusterMax && cluster_vec_bytes(rows, c, (int)sizeof(R)) > target) c *= 2;
     if (cluster_vec_bytes(rows, c, (int)sizeof(R)) > target) {
       c = cmin;
-      while (c < kClusterMax && cluster_vec_bytes(rows, c, (int)sizeof(R)) > kClusterSmemBudget) c *= 2;
+      while (c < kClusterMax && cluster_vec_bytes(rows, c, (int)sizeof(R)) > budget) c *= 2;
     }
     return c;
   };
@@ -1333,6 +1371,8 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
   }
   if (total_rows <= 0.0) return SKG_OK;
   SKG_CUDA(cudaMemsetAsync(queue, 0, 8 * sizeof(unsigned), s));
+  if (cd) SKG_CUDA(cudaMemsetAsync(cd->rc, 0, sizeof(unsigned long long) * 6 * (size_t)cd->n_agg, s));
+  CoarseDev c2 = cd ? *cd : CoarseDev{};
   SKG_CUDA(cudaEventRecord(cs.fork, s));
   const int sms = num_sms();
   for (int c = 0; c < ncls; ++c) {
@@ -1360,9 +1400,14 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
     cfg.gridDim = dim3(csize * nclusters, 1, 1);
     SKG_CUDA(cudaStreamWaitEvent(cs.s[c], cs.fork, 0));
     Bsr<R> a2 = A;
-    SKG_CUDA(cudaLaunchKernelEx(&cfg, kern, a2, bt->inst_rows, bt->order + cls_begin[c],
-                                cls_end[c] - cls_begin[c], active, eta, b, -1.0, pinned, xout, max_iter, it_out,
-                                st_out, queue + c, (int)kClusterSmemBudget));
+    const int32_t* ord = bt->order + cls_begin[c];
+    int ncls_inst = cls_end[c] - cls_begin[c];
+    double bs = -1.0;
+    unsigned* qc = queue + c;
+    int smem = (int)budget;
+    void* args[] = {&a2, (void*)&bt->inst_rows, (void*)&ord, &ncls_inst, (void*)&active, (void*)&eta, (void*)&b, &bs,
+                    (void*)&pinned, &xout, &max_iter, &it_out, &st_out, &qc, &smem, &c2};
+    SKG_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
     SKG_CUDA(cudaEventRecord(cs.join[c], cs.s[c]));
     SKG_CUDA(cudaStreamWaitEvent(s, cs.join[c], 0));
     ++*launches;
@@ -1484,6 +1529,10 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     SKG_TRY(gradient());
   }
   const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  // two-level PCG with the per-instance coarse data, when attached (one instance per mesh of the batch)
+  const bool two_level = m->coarse && m->coarse->inst_agg && m->coarse->n_inst == bt->n_inst;
+  CoarseDev cdev{};
+  if (two_level) cdev = make_coarse_dev(m, w);
   for (int it = 0; it < prm->max_newton; ++it) {
     n_active = 0;
     for (int i = 0; i < ni; ++i) {
@@ -1540,14 +1589,21 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     aa.pinned = st->pinned;
     aa.vert_inst = bt->vert_inst;
     aa.inst_active = bw.active;
+    aa.colpack = two_level ? cdev.colpack : nullptr;
     pt.begin();
     SKG_TRY(launch_assemble<R>(aa, s));
+    // per-instance coarse operators of the two-level PCG (every instance is active at the first
+    // Newton iteration of the step)
+    if (two_level && (it == 0 || prm->coarse_refresh)) {
+      SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s, bt->order));
+      launches += 2;
+    }
     total->t_assemble_ms += pt.end();
     // all active instances' PCG solves, one cluster per instance at a time
     pt.begin();
     SKG_TRY(launch_pcg_queue<R>(A, bt, rows_h.data(), order_h.data(), active.data(), prm->batch_min_cluster,
                                 prm->batch_vec_kb, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it, bw.pcg_st,
-                                bw.queue, s, &launches));
+                                bw.queue, s, &launches, two_level ? &cdev : nullptr));
     total->t_pcg_ms += pt.end();
     launches += 2;
     SKG_CUDA(cudaMemcpyAsync(pit.data(), bw.pcg_it, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));

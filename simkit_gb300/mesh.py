@@ -122,6 +122,11 @@ def coarse_aggregates(X, free_dof, rowptr, col, box=8, spacing=None, max_coarse=
     mode = np.empty((n, 4), np.float32)
     mode[:, :3] = d
     mode[:, 3] = bits.view(np.float32)
+    cb_ptr, cb_slot, cb_rc = _coarse_pattern(agg, n_agg, rowptr, col, n)
+    return {"n_agg": int(n_agg), "mode": mode, "cb_ptr": cb_ptr, "cb_slot": cb_slot, "cb_rc": cb_rc, "box": box}
+
+
+def _coarse_pattern(agg, n_agg, rowptr, col, n):
     rowptr = np.asarray(rowptr, dtype=np.int64)
     col = np.asarray(col, dtype=np.int64)
     row = np.repeat(np.arange(n, dtype=np.int64), np.diff(rowptr))
@@ -132,8 +137,78 @@ def coarse_aggregates(X, free_dof, rowptr, col, box=8, spacing=None, max_coarse=
     cb_keys = ks[starts]
     cb_ptr = np.r_[starts, ks.size].astype(np.int32)
     cb_rc = np.stack([cb_keys // n_agg, cb_keys % n_agg], 1).astype(np.int32).reshape(-1)
-    return {"n_agg": int(n_agg), "mode": mode, "cb_ptr": cb_ptr, "cb_slot": order.astype(np.int32),
-            "cb_rc": cb_rc, "box": box}
+    return cb_ptr, order.astype(np.int32), cb_rc
+
+
+def coarse_aggregates_inst(X, free_dof, rowptr, col, inst_rows, box=4, max_agg=127, spacing=None):
+    """Per-instance aggregates of the two-level preconditioner for the thread-block-cluster PCG
+    (one mesh is one instance; a batch has one per mesh).
+
+    Each instance's vertices are grouped by boxes of ``box`` mesh spacings (grown until the instance
+    has at most ``max_agg`` aggregates, so a local aggregate index fits 7 bits).  Offsets from the
+    aggregate centroid are divided by the aggregate's largest |component| and quantised to k/64,
+    k in [-64, 63]; those exact values are what every user of P sees.  Returns host arrays:
+    ``n_agg``; ``mode`` (n, 4) float32 (offset, uint32 bits global aggregate | free mask << 29);
+    ``colpack`` (n) uint32 = (k_x+64) | (k_y+64) << 7 | (k_z+64) << 14 | local aggregate << 21 |
+    free mask << 28, the word the block records carry for their column; the coarse block
+    pattern ``cb_ptr``, ``cb_slot``, ``cb_rc``; per instance ``inst_agg`` (n_inst + 1),
+    ``agg_inst`` (n_agg), ``inst_moff`` (n_inst + 1, offsets of the padded dense blocks in
+    floats), ``m_floats``, ``max_np``, ``boxes``."""
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    n = X.shape[0]
+    free = np.asarray(free_dof, dtype=bool).reshape(n, 3)
+    inst_rows = np.asarray(inst_rows, dtype=np.int64)
+    ni = inst_rows.size - 1
+    agg = np.empty(n, np.int64)
+    local = np.empty(n, np.int64)
+    d = np.empty((n, 3), np.float64)
+    inst_agg = [0]
+    boxes = []
+    for i in range(ni):
+        a, b = int(inst_rows[i]), int(inst_rows[i + 1])
+        Xi = X[a:b]
+        lo = Xi.min(axis=0)
+        ext = np.maximum(Xi.max(axis=0) - lo, 1e-300)
+        sp = spacing if spacing is not None else float(np.prod(ext) / max(b - a, 1)) ** (1.0 / 3.0)
+        bx = box
+        while True:
+            h = bx * sp
+            ijk = np.floor((Xi - lo) / h + 0.5 / bx).astype(np.int64)
+            keys = (ijk[:, 0] * (ijk[:, 1].max() + 1) + ijk[:, 1]) * (ijk[:, 2].max() + 1) + ijk[:, 2]
+            uk, la = np.unique(keys, return_inverse=True)
+            if uk.size <= max_agg:
+                break
+            bx *= 2
+        la = la.reshape(-1)
+        na = uk.size
+        cnt = np.bincount(la, minlength=na).astype(np.float64)
+        cen = np.stack([np.bincount(la, weights=Xi[:, k], minlength=na) for k in range(3)], 1) / cnt[:, None]
+        di = Xi - cen[la]
+        mx = np.zeros(na)
+        np.maximum.at(mx, la, np.abs(di).max(axis=1))
+        di = di / np.where(mx > 0.0, mx, 1.0)[la][:, None]
+        agg[a:b] = inst_agg[-1] + la
+        local[a:b] = la
+        d[a:b] = di
+        inst_agg.append(inst_agg[-1] + na)
+        boxes.append(bx)
+    n_agg = inst_agg[-1]
+    q = np.clip(np.rint(d * 64.0), -64, 63).astype(np.int64)
+    mask = (free[:, 0].astype(np.uint32) | (free[:, 1].astype(np.uint32) << 1)
+            | (free[:, 2].astype(np.uint32) << 2))
+    mode = np.empty((n, 4), np.float32)
+    mode[:, :3] = q / 64.0
+    mode[:, 3] = (agg.astype(np.uint32) | (mask << np.uint32(29))).view(np.float32)
+    colpack = ((q[:, 0] + 64) | ((q[:, 1] + 64) << 7) | ((q[:, 2] + 64) << 14) | (local << 21)
+               | (mask.astype(np.int64) << 28)).astype(np.uint32)
+    cb_ptr, cb_slot, cb_rc = _coarse_pattern(agg, n_agg, rowptr, col, n)
+    inst_agg = np.asarray(inst_agg, np.int64)
+    nps = ((6 * np.diff(inst_agg) + 31) // 32) * 32
+    inst_moff = np.r_[0, np.cumsum(nps * nps)].astype(np.int64)
+    agg_inst = np.repeat(np.arange(ni, dtype=np.int32), np.diff(inst_agg))
+    return {"n_agg": int(n_agg), "mode": mode, "colpack": colpack, "cb_ptr": cb_ptr, "cb_slot": cb_slot,
+            "cb_rc": cb_rc, "inst_agg": inst_agg.astype(np.int32), "agg_inst": agg_inst, "inst_moff": inst_moff,
+            "m_floats": int(inst_moff[-1]), "max_np": int(nps.max()), "boxes": np.asarray(boxes)}
 
 
 class TetMesh:
@@ -247,6 +322,28 @@ class TetMesh:
             cb_rc=self.coarse["cb_rc"].data_ptr())
         self.c.coarse = ctypes.pointer(self._coarse_c)
         return cd["n_agg"], cd["box"]
+
+    def set_coarse_inst(self, free_dof, inst_rows=None, box=4):
+        """Attach per-instance two-level data for the cluster PCG (``inst_rows``: instance vertex
+        offsets, default one instance).  Workspaces sized before this call are too small afterwards."""
+        if self.X_host is None:
+            self.X_host = self.X.cpu().numpy().reshape(-1, 3)
+        if self.rowptr_host is None:
+            self.rowptr_host = self.rowptr.cpu().numpy()
+            self.col_host = self.col.cpu().numpy()
+        if inst_rows is None:
+            inst_rows = np.array([0, self.n])
+        cd = coarse_aggregates_inst(self.X_host, free_dof, self.rowptr_host, self.col_host, inst_rows, box=box)
+        up = lambda x: torch.from_numpy(np.ascontiguousarray(x)).to(self.device)
+        self.coarse = {k: (up(v) if isinstance(v, np.ndarray) and k != "boxes" else v) for k, v in cd.items()}
+        ptr = lambda k: self.coarse[k].data_ptr()
+        self._coarse_c = _lib.CoarseC(
+            n_agg=cd["n_agg"], n_cblocks=int(cd["cb_ptr"].size - 1), mode=ptr("mode"), cb_ptr=ptr("cb_ptr"),
+            cb_slot=ptr("cb_slot"), cb_rc=ptr("cb_rc"), n_inst=int(cd["inst_agg"].size - 1), max_np=cd["max_np"],
+            m_floats=cd["m_floats"], inst_agg=ptr("inst_agg"), agg_inst=ptr("agg_inst"), inst_moff=ptr("inst_moff"),
+            colpack=ptr("colpack"))
+        self.c.coarse = ctypes.pointer(self._coarse_c)
+        return cd["n_agg"], cd["boxes"]
 
     def clear_coarse(self):
         self.c.coarse = None

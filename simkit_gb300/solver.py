@@ -81,8 +81,10 @@ class BESolver:
     material : 'stable-neo-hookean' or 'macklin-mueller-neo-hookean' (simkit/energies/elastic.py names)
     contact_planes : optional list of (k, p, n) contact-spring planes added to the potential
     coarse : two-level PCG preconditioner (block Jacobi + rigid-mode aggregates of box^3 mesh
-        spacings): None (one-level), 'auto' (box 8 on meshes above 24,576 vertices, used by
-        pcg_mode 3 there) or a box size (used by pcg_mode 3 above that size and by pcg_mode 7)
+        spacings): None (one-level), 'auto' or a box size.  Meshes above 24,576 vertices get the
+        whole-mesh form (box 8 by default; the grid PCG, pcg_mode 3 or 7), smaller ones the
+        per-instance form (box 4; the thread-block-cluster PCG, pcg_mode 2 or 3)
+    coarse_form : 'auto' (by size, as above), 'grid' or 'cluster'
     coarse_refresh : 'step' (coarse inverse rebuilt at the first Newton iteration of each step)
         or 'newton' (at every Newton iteration)
     """
@@ -91,7 +93,7 @@ class BESolver:
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
                  material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh="step"):
+                 coarse="auto", coarse_refresh="step", coarse_form="auto"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.set_energy(material)
@@ -108,8 +110,17 @@ class BESolver:
         pin[(3 * pv[:, None] + np.arange(3)[None, :]).ravel()] = 1
         self.pinned = torch.from_numpy(pin).to(dev)
         self.coarse_box = None
-        if coarse is not None and (coarse != "auto" or m.n > 24576):
-            _, self.coarse_box = m.set_coarse(pin == 0, box=8 if coarse == "auto" else int(coarse))
+        self.coarse_form = None
+        if coarse is not None:
+            form = coarse_form if coarse_form != "auto" else ("grid" if m.n > 24576 else "cluster")
+            if form not in ("grid", "cluster"):
+                raise ValueError("coarse_form must be 'auto', 'grid' or 'cluster'")
+            self.coarse_form = form
+            if form == "grid":
+                _, self.coarse_box = m.set_coarse(pin == 0, box=8 if coarse == "auto" else int(coarse))
+            else:
+                _, boxes = m.set_coarse_inst(pin == 0, box=4 if coarse == "auto" else int(coarse))
+                self.coarse_box = int(boxes[0])
         if coarse_refresh not in ("step", "newton"):
             raise ValueError("coarse_refresh must be 'step' or 'newton'")
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)

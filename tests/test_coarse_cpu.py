@@ -206,3 +206,44 @@ def test_two_level_cuts_iterations():
     it_two, x2 = _pcg(H, b, two, 1e-6)
     assert it_two * 2 < it_bj, (it_bj, it_two)
     assert np.linalg.norm(H @ x2 - b) <= 1e-5 * np.linalg.norm(b)
+
+
+def _decode_colpack(w):
+    w = w.astype(np.int64)
+    d = np.stack([((w >> s) & 127) - 64 for s in (0, 7, 14)], 1) / 64.0
+    return d, (w >> 21) & 127, (w >> 28) & 7
+
+
+def test_per_instance_form_two_beams():
+    """Per-instance aggregates over a two-mesh batch: local/global aggregate ids, the packed
+    column word, dense-block offsets, and each instance's Galerkin block = its own P^T A P."""
+    from simkit_gb300.mesh import coarse_aggregates_inst
+    parts = [_system(nx=10, ny=4, nz=4, seed=1), _system(nx=6, ny=5, nz=3, ym=3e6, seed=2)]
+    Xs = [p[0].X for p in parts]
+    Hs = [p[1] for p in parts]
+    pins = [p[2] for p in parts]
+    rows = np.r_[0, np.cumsum([x.shape[0] for x in Xs])]
+    H = sps.block_diag(Hs).tocsr()
+    X = np.concatenate(Xs)
+    pin = np.concatenate(pins)
+    n = X.shape[0]
+    rowptr, col, blocks = _bsr_pattern(H, n)
+    cd = coarse_aggregates_inst(X, ~pin, rowptr, col, rows, box=4)
+    ia = cd["inst_agg"]
+    assert ia[0] == 0 and ia[-1] == cd["n_agg"] and np.all(np.diff(ia) <= 127)
+    bits = cd["mode"][:, 3].view(np.uint32)
+    agg = (bits & 0x1FFFFFFF).astype(np.int64)
+    d, local, mask = _decode_colpack(cd["colpack"])
+    inst_of = np.repeat(np.arange(len(Xs)), np.diff(rows))
+    assert np.array_equal(local, agg - ia[inst_of])
+    assert np.array_equal(mask, bits >> 29)
+    assert np.array_equal(d.astype(np.float32), cd["mode"][:, :3])        # the same offsets everywhere
+    assert np.all(np.abs(cd["mode"][:, :3]) <= 1.0)
+    # coarse blocks never couple two instances
+    assert np.array_equal(cd["agg_inst"][cd["cb_rc"][0::2]], cd["agg_inst"][cd["cb_rc"][1::2]])
+    Ac = _galerkin_blocks(cd, rowptr, col, blocks, n)
+    P = _explicit_P(cd["mode"], n, cd["n_agg"])
+    ref = P.T @ H.toarray() @ P
+    assert np.abs(Ac - ref).max() <= 1e-9 * np.abs(ref).max()
+    nps = ((6 * np.diff(ia) + 31) // 32) * 32
+    assert np.array_equal(np.diff(cd["inst_moff"]), nps * nps) and cd["max_np"] == nps.max()

@@ -339,8 +339,8 @@ def test_two_level_pcg_matches_reference(api, precision, refresh):
     d = _load("rollout_beam_8x8x32.npz")
     spec = beam_small_steady()
     s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=7, coarse=4,
-                           coarse_refresh=refresh)
-    one = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=5)
+                           coarse_refresh=refresh, coarse_form="grid")
+    one = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=5, coarse=None)
     assert s.coarse_box == 4
     X = spec.X.reshape(-1)
     pcg_two = pcg_one = 0
@@ -363,8 +363,8 @@ def test_two_level_repeatable(api):
     from simkit_gb300.beams import beam_small_steady
     from simkit_gb300.solver import BESolver
     spec = beam_small_steady()
-    a = BESolver.from_spec(spec, pcg_mode=7, coarse=4)
-    b = BESolver.from_spec(spec, pcg_mode=7, coarse=4)
+    a = BESolver.from_spec(spec, pcg_mode=7, coarse=4, coarse_form="grid")
+    b = BESolver.from_spec(spec, pcg_mode=7, coarse=4, coarse_form="grid")
     for _ in range(3):
         ia, ib = a.step(), b.step()
         assert ia.pcg_iters == ib.pcg_iters
@@ -410,6 +410,64 @@ def test_nonfinite_input_is_reported(api):
     assert info.status == -5
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_cluster_two_level_small_beam(api, precision):
+    """The per-instance two-level form on the thread-block-cluster PCG (aggregates of 4^3 cells,
+    coarse vectors in shared memory, e broadcast over DSMEM) on the 12,288-tet beam: 20 steps
+    within the tolerances of the default path, fewer PCG iterations than one-level."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=2, coarse=4,
+                           coarse_form="cluster")
+    one = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, pcg_mode=2, coarse=None)
+    assert s.coarse_form == "cluster" and s.coarse_box == 4
+    X = spec.X.reshape(-1)
+    two_it = one_it = 0
+    for step in range(1, 21):
+        info = s.step()
+        assert info.converged, (step, info)
+        info1 = one.step()
+        two_it += info.pcg_iters
+        one_it += info1.pcg_iters
+        if step in d["steps"]:
+            k = list(d["steps"]).index(step)
+            assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+    print(f"\n{precision}: PCG iterations cluster two-level {two_it}, one-level {one_it}")
+    assert 2 * two_it < one_it
+
+
+def test_batched_two_level(api):
+    """A batch with per-instance coarse data: every instance equals the same beam stepped alone with
+    the same two-level cluster PCG (1e-7), stays within 1e-5 of the one-level batch, and needs fewer
+    PCG iterations.  Beam sizes up to 17 x 17 x 49 vertices, so clusters of several CTAs share e."""
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    from simkit_gb300.solver import BESolver
+    specs = beam_batch(8, seed=5)
+    b = BatchedBESolver(specs, coarse="auto")
+    b1 = BatchedBESolver(specs)
+    singles = [BESolver.from_spec(sp, coarse="auto", coarse_form="cluster", pcg_mode=2) for sp in specs]
+    it2 = it1 = 0
+    for step in range(3):
+        infos, total = b.step()
+        infos1, total1 = b1.step()
+        assert total.status == 0 and total1.status == 0, (total, total1)
+        it2 += total.pcg_iters
+        it1 += total1.pcg_iters
+        for i, sp in enumerate(specs):
+            assert infos[i].converged, (i, infos[i])
+            si = singles[i].step()
+            assert si.converged
+            X = sp.X.reshape(-1)
+            ub = b.displacement(i)
+            assert _rel(X + ub, X + singles[i].displacement()) < 1e-7, i
+            assert _rel(X + ub, X + b1.displacement(i)) < 1e-5, i
+    print(f"\nbatched PCG iterations two-level {it2}, one-level {it1}")
+    assert 2 * it2 < it1
+
+
 def test_batched_step_matches_single_instance_and_oracle(api):
     """A batch of uneven beams (own material, gravity direction, pins) stepped together
     equals each beam stepped alone, and the FP64 oracle: positions within 1e-5."""
@@ -419,7 +477,7 @@ def test_batched_step_matches_single_instance_and_oracle(api):
     from oracle import rollout
     specs = beam_batch(6, seed=3, nx_range=(2, 5), ny_range=(2, 4), nz_range=(3, 8))
     b = BatchedBESolver(specs)
-    singles = [BESolver.from_spec(sp) for sp in specs]
+    singles = [BESolver.from_spec(sp, coarse=None) for sp in specs]
     refs = [rollout.from_spec(sp) for sp in specs]
     states = [(r.x_rest.copy(), r.x_rest.copy()) for r in refs]
     for step in range(3):
