@@ -345,6 +345,21 @@ class TetMesh:
         self.c.coarse = ctypes.pointer(self._coarse_c)
         return cd["n_agg"], cd["boxes"]
 
+    def set_coarse_device(self, t):
+        """Attach per-instance two-level data already on the device: ``t`` holds ``mode`` (n, 4)
+        float32, ``colpack`` (n) int32/uint32, ``cb_ptr``, ``cb_slot``, ``cb_rc``, ``inst_agg``,
+        ``agg_inst`` (int32) and ``inst_moff`` (int64), as ``coarse_aggregates_inst`` lays them out."""
+        ia = t["inst_agg"].cpu().numpy()
+        nps = ((6 * np.diff(ia) + 31) // 32) * 32
+        self.coarse = dict(t)
+        ptr = lambda k: self.coarse[k].data_ptr()
+        self._coarse_c = _lib.CoarseC(
+            n_agg=int(ia[-1]), n_cblocks=int(t["cb_ptr"].numel() - 1), mode=ptr("mode"), cb_ptr=ptr("cb_ptr"),
+            cb_slot=ptr("cb_slot"), cb_rc=ptr("cb_rc"), n_inst=int(ia.size - 1), max_np=int(nps.max()),
+            m_floats=int((nps.astype(np.int64) ** 2).sum()), inst_agg=ptr("inst_agg"), agg_inst=ptr("agg_inst"),
+            inst_moff=ptr("inst_moff"), colpack=ptr("colpack"))
+        self.c.coarse = ctypes.pointer(self._coarse_c)
+
     def clear_coarse(self):
         self.c.coarse = None
         self.coarse = None

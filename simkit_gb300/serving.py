@@ -35,7 +35,7 @@ import torch
 from . import _lib
 from .batched import BatchedBESolver
 from .beams import _lame, beam_meshes
-from .mesh import TetMesh, _ptr, _stream_ptr, device_pattern
+from .mesh import coarse_aggregates_inst, TetMesh, _ptr, _stream_ptr, device_pattern
 from .solver import lumped_mass
 
 
@@ -76,7 +76,7 @@ class ShapeTemplate:
     are the shape's first vertex, tet and block within its chunk."""
 
     __slots__ = ("dims", "n", "t", "nb", "X", "tets", "dinv", "vol", "mass", "pinned", "pattern", "vbase", "tbase",
-                 "bbase")
+                 "bbase", "coarse", "abase", "n_agg")
 
 
 class TemplateCache:
@@ -86,7 +86,8 @@ class TemplateCache:
     matrices and volumes by one ``skg_tet_setup`` launch, and the block pattern with its
     gather maps by one pair of device sorts (``device_pattern``)."""
 
-    def __init__(self, device="cuda", chunk_tets=4_000_000, cell=0.025, rho=1000.0):
+    def __init__(self, device="cuda", chunk_tets=4_000_000, cell=0.025, rho=1000.0, coarse=True):
+        self.coarse = coarse      # per-shape two-level aggregates (box 4) for the cluster PCG
         self.device = torch.device(device)
         self.chunk_tets = chunk_tets
         self.cell, self.rho = cell, rho
@@ -151,6 +152,17 @@ class TemplateCache:
         dinv2 = dinv.view(9, t)
         rowptr, col, diag, row, hc_ptr, hc_src, v2t_ptr, v2t = pattern
         self.bytes += sum(x.numel() * x.element_size() for x in (Xd, Td, dinv, vol, massd, pind, *pattern))
+        cz = None
+        if self.coarse:
+            # per-shape aggregates over the chunk (chunk-wide aggregate and block indices, like the pattern)
+            cd = coarse_aggregates_inst(X, pin.reshape(-1) == 0, rowptr.cpu().numpy(), col.cpu().numpy(), v_off,
+                                        box=4)
+            up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+            cz = {"d": up(cd["mode"][:, :3]), "bits": up(cd["mode"][:, 3].view(np.int32)),
+                  "colpack": up(cd["colpack"].view(np.int32)), "cb_ptr": up(cd["cb_ptr"]), "cb_slot": up(cd["cb_slot"]),
+                  "cb_rc": up(cd["cb_rc"]), "inst_agg": cd["inst_agg"], "cb_ptr_h": cd["cb_ptr"],
+                  "cb_first": np.searchsorted(cd["cb_rc"][0::2], cd["inst_agg"])}
+            self.bytes += sum(v.numel() * v.element_size() for v in cz.values() if isinstance(v, torch.Tensor))
         for s, d in enumerate(dims):
             v0, v1, t0, t1, b0, b1 = (int(v_off[s]), int(v_off[s + 1]), int(t_off[s]), int(t_off[s + 1]),
                                       int(b_off[s]), int(b_off[s + 1]))
@@ -165,6 +177,13 @@ class TemplateCache:
             tp.pinned = pind[3 * v0: 3 * v1]
             tp.pattern = (rowptr[v0: v1 + 1], col[b0:b1], diag[v0:v1], row[b0:b1], hc_ptr[b0: b1 + 1],
                           hc_src[16 * t0: 16 * t1], v2t_ptr[v0: v1 + 1], v2t[4 * t0: 4 * t1])
+            tp.coarse = None
+            if cz is not None:
+                a0, a1 = int(cz["inst_agg"][s]), int(cz["inst_agg"][s + 1])
+                c0, c1 = int(cz["cb_first"][s]), int(cz["cb_first"][s + 1])
+                tp.abase, tp.n_agg = a0, a1 - a0
+                tp.coarse = (cz["d"][v0:v1], cz["bits"][v0:v1], cz["colpack"][v0:v1], cz["cb_ptr"][c0: c1 + 1],
+                             cz["cb_slot"][int(cz["cb_ptr_h"][c0]): int(cz["cb_ptr_h"][c1])], cz["cb_rc"][2 * c0: 2 * c1])
             self.shapes[d] = tp
 
 
@@ -185,6 +204,31 @@ def concat_patterns(parts, n_shift, t_shift, b_shift, nb_total, nt_total):
     v2t_ptr = torch.cat([p[6][:-1] + 4 * t for p, t in zip(parts, t_shift)] + [i32(4 * nt_total)])
     v2t = torch.cat([p[7] + 4 * t for p, t in zip(parts, t_shift)])
     return rowptr, col, diag, row, hc_ptr, hc_src, v2t_ptr, v2t
+
+
+def concat_coarse(tps, b_shift):
+    """Per-instance two-level data of a cohort from the templates' pieces: aggregate indices
+    shifted to the cohort's numbering, fine block slots by the pattern's block shifts, the coarse
+    block pointers rebased; the packed column words hold instance-local aggregates and need none."""
+    dev = tps[0].X.device
+    na = np.array([tp.n_agg for tp in tps], np.int64)
+    a_off = np.concatenate([[0], np.cumsum(na)])
+    a_shift = [int(a_off[i] - tp.abase) for i, tp in enumerate(tps)]
+    d = torch.cat([tp.coarse[0] for tp in tps])
+    bits = torch.cat([tp.coarse[1] + a for tp, a in zip(tps, a_shift)])
+    mode = torch.cat([d, bits.view(torch.float32)[:, None]], dim=1).contiguous()
+    colpack = torch.cat([tp.coarse[2] for tp in tps])
+    ns = np.array([tp.coarse[4].numel() for tp in tps], np.int64)
+    s_off = np.concatenate([[0], np.cumsum(ns)])
+    cb_ptr = torch.cat([tp.coarse[3][:-1] - tp.coarse[3][0] + int(o) for tp, o in zip(tps, s_off[:-1])]
+                       + [torch.tensor([int(s_off[-1])], dtype=torch.int32, device=dev)])
+    cb_slot = torch.cat([tp.coarse[4] + b for tp, b in zip(tps, b_shift)])
+    cb_rc = torch.cat([tp.coarse[5] + a for tp, a in zip(tps, a_shift)])
+    nps = ((6 * na + 31) // 32) * 32
+    up = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a).astype(dt)).to(dev)
+    return {"mode": mode, "colpack": colpack, "cb_ptr": cb_ptr.to(torch.int32), "cb_slot": cb_slot, "cb_rc": cb_rc,
+            "inst_agg": up(a_off, np.int32), "agg_inst": up(np.repeat(np.arange(len(tps)), na), np.int32),
+            "inst_moff": up(np.concatenate([[0], np.cumsum(nps * nps)]), np.int64)}
 
 
 def build_cohort(cache, reqs, **solver_kw):
@@ -214,6 +258,8 @@ def build_cohort(cache, reqs, **solver_kw):
     lam = torch.repeat_interleave(torch.from_numpy(lam_i).to(dev), tcount)
     pattern = concat_patterns([tp.pattern for tp in tps], n_shift, t_shift, b_shift, int(b_off[-1]), int(t_off[-1]))
     mesh = TetMesh.from_device(X, tets, dinv, vol, mu, lam, pattern)
+    if all(tp.coarse is not None for tp in tps):
+        mesh.set_coarse_device(concat_coarse(tps, b_shift))
     mass = torch.cat([tp.mass for tp in tps])
     grav = torch.from_numpy(np.stack([r.gravity for r in reqs])).to(dev)
     f_ext = (mass[:, None] * torch.repeat_interleave(grav, torch.from_numpy(ns).to(dev), dim=0)).reshape(-1)
@@ -274,11 +320,12 @@ class BeamServer:
 
     max_cohort: requests per cohort; max_live: requests in flight; hbm_reserve_gb: HBM
     left free; net: a trained ``WarmStartMLP`` (the learned warm start with its
-    energy-judged fallback) or None for plain Newton starts."""
+    energy-judged fallback) or None for plain Newton starts; coarse: two-level PCG with
+    per-shape aggregates (built with the templates)."""
 
     def __init__(self, max_cohort=512, max_live=2048, hbm_reserve_gb=16.0, net=None, device="cuda",
-                 **solver_kw):
-        self.cache = TemplateCache(device)
+                 coarse=True, **solver_kw):
+        self.cache = TemplateCache(device, coarse=coarse)
         self.prewarm_s = 0.0
         self.max_cohort = max_cohort
         self.max_live = max_live

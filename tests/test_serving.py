@@ -92,9 +92,12 @@ def test_request_stream_is_a_seeded_poisson_stream():
 
 
 @pytest.mark.gpu
-def test_cohort_steps_equal_batched_solver_from_specs():
+@pytest.mark.parametrize("coarse", [False, True])
+def test_cohort_steps_equal_batched_solver_from_specs(coarse):
     """A cohort assembled on the device from shape templates takes bitwise the same
-    steps as the batched solver built from the equivalent beam specs on the host."""
+    steps as the batched solver built from the equivalent beam specs on the host, with
+    and without the per-instance two-level data (template pieces concatenated with shifts
+    on the device vs aggregates built for the batch on the host)."""
     from simkit_gb300.batched import BatchedBESolver
     from simkit_gb300.beams import make_beam
     from simkit_gb300.serving import BeamRequest, TemplateCache, build_cohort
@@ -105,11 +108,12 @@ def test_cohort_steps_equal_batched_solver_from_specs():
         g = 9.8 * g / np.linalg.norm(g)
         reqs.append(BeamRequest(i, d, float(np.exp(rng.uniform(np.log(1e5), np.log(1e7)))),
                                 float(rng.uniform(0.3, 0.49)), g, 3, 0.0))
-    cache = TemplateCache("cuda")   # both shapes in one chunk: one of them has nonzero bases
+    cache = TemplateCache("cuda", coarse=coarse)   # both shapes in one chunk: one has nonzero bases
     a, _ = build_cohort(cache, reqs)
     assert len(cache.shapes) == 2 and max(tp.tbase for tp in cache.shapes.values()) > 0
     b = BatchedBESolver([make_beam(*r.dims, cell=0.025, ym=r.ym, pr=r.pr, rho=1000.0, gravity=r.gravity)
-                         for r in reqs])
+                         for r in reqs], coarse="auto" if coarse else None)
+    assert (a.mesh.c.coarse is not None and bool(a.mesh.c.coarse)) == coarse
     for _ in range(3):
         ia, ta = a.step()
         ib, tb = b.step()
