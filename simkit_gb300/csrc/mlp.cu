@@ -158,7 +158,7 @@ struct GemmArgs {
 };
 
 // dynamic shared memory: A blocks (kb x 16 KB) then B blocks (kb x Nc x 128 B), 1024-aligned
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(256, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_dyn[];
   __shared__ __align__(8) uint64_t bar_load;
@@ -230,43 +230,96 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_after();
   __syncthreads();
 
-  // epilogue: warp w holds rows 32w .. 32w + 31 of the tile
-  const int r = row0 + warp * 32 + lane;
+  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of the tile; the lane quarter a
+  // warp may access) and every other 32-column chunk starting at chunk w / 4
+  const int quarter = warp & 3;
+  const int r = row0 + quarter * 32 + lane;
   const bool live = ok_load && ok_mma;
-  for (int c0 = 0; c0 < g.Nc; c0 += 32) {
+  for (int c0 = (warp >> 2) * 32; c0 < g.Nc; c0 += 64) {
     float v[32];
     if (nkb > 0 && live) {
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
     } else {
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] = 0.f;
     }
     if (r >= g.R) continue;
+    // each thread writes its own row: 16-byte vector stores where the whole 32-column chunk is
+    // stored and the row stride keeps them aligned, scalar stores otherwise
+    const bool vec16 = c0 + 32 <= g.Nstore;
     if (g.epi == EPI_F32) {
       float* o = g.out_f32 + ((size_t)split * g.R + r) * g.ld_out;
+      if (vec16 && (g.ld_out % 4) == 0) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int c = c0 + i;
-        if (c < g.Nstore) o[c] = v[i] + (g.bias ? g.bias[c] : 0.f);
+        for (int q = 0; q < 8; ++q) {
+          float4 t;
+          t.x = v[4 * q] + (g.bias ? g.bias[c0 + 4 * q] : 0.f);
+          t.y = v[4 * q + 1] + (g.bias ? g.bias[c0 + 4 * q + 1] : 0.f);
+          t.z = v[4 * q + 2] + (g.bias ? g.bias[c0 + 4 * q + 2] : 0.f);
+          t.w = v[4 * q + 3] + (g.bias ? g.bias[c0 + 4 * q + 3] : 0.f);
+          reinterpret_cast<float4*>(o + c0)[q] = t;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = c0 + i;
+          if (c < g.Nstore) o[c] = v[i] + (g.bias ? g.bias[c] : 0.f);
+        }
       }
     } else if (g.epi == EPI_BIAS_GELU) {
       __nv_bfloat16* oz = g.out_z + (size_t)r * g.ld_out;
       __nv_bfloat16* oh = g.out_h + (size_t)r * g.ld_out;
+      if (vec16 && (g.ld_out % 8) == 0) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int c = c0 + i;
-        if (c < g.Nstore) {
-          const float z = v[i] + g.bias[c];
-          oz[c] = __float2bfloat16(z);
-          oh[c] = __float2bfloat16(gelu_tanh(z));
+        for (int q = 0; q < 4; ++q) {
+          uint4 zz, hh;
+          uint32_t* zw = reinterpret_cast<uint32_t*>(&zz);
+          uint32_t* hw = reinterpret_cast<uint32_t*>(&hh);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int c = 8 * q + 2 * i;
+            const float z0 = v[c] + g.bias[c0 + c], z1 = v[c + 1] + g.bias[c0 + c + 1];
+            const __nv_bfloat162 zb = __floats2bfloat162_rn(z0, z1);
+            const __nv_bfloat162 hb = __floats2bfloat162_rn(gelu_tanh(z0), gelu_tanh(z1));
+            zw[i] = *reinterpret_cast<const uint32_t*>(&zb);
+            hw[i] = *reinterpret_cast<const uint32_t*>(&hb);
+          }
+          reinterpret_cast<uint4*>(oz + c0)[q] = zz;
+          reinterpret_cast<uint4*>(oh + c0)[q] = hh;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = c0 + i;
+          if (c < g.Nstore) {
+            const float z = v[i] + g.bias[c];
+            oz[c] = __float2bfloat16(z);
+            oh[c] = __float2bfloat16(gelu_tanh(z));
+          }
         }
       }
     } else {
       __nv_bfloat16* oh = g.out_h + (size_t)r * g.ld_out;
+      if (vec16 && (g.ld_out % 8) == 0) {
 #pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int c = c0 + i;
-        if (c < g.Nstore) oh[c] = __float2bfloat16(v[i] + (g.bias ? g.bias[c] : 0.f));
+        for (int q = 0; q < 4; ++q) {
+          uint4 hh;
+          uint32_t* hw = reinterpret_cast<uint32_t*>(&hh);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int c = 8 * q + 2 * i;
+            const __nv_bfloat162 hb = __floats2bfloat162_rn(v[c] + (g.bias ? g.bias[c0 + c] : 0.f),
+                                                            v[c + 1] + (g.bias ? g.bias[c0 + c + 1] : 0.f));
+            hw[i] = *reinterpret_cast<const uint32_t*>(&hb);
+          }
+          reinterpret_cast<uint4*>(oh + c0)[q] = hh;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = c0 + i;
+          if (c < g.Nstore) oh[c] = __float2bfloat16(v[i] + (g.bias ? g.bias[c] : 0.f));
+        }
       }
     }
   }
@@ -419,7 +472,7 @@ int skg_mlp_gemm(const void* A, int64_t R, int64_t lda, const void* B, int Nc, i
   g.bias = bias; g.out_f32 = out_f32; g.out_z = (__nv_bfloat16*)out_z; g.out_h = (__nv_bfloat16*)out_h;
   g.ld_out = ld_out; g.err = err;
   dim3 grid((unsigned)((R + kTileM - 1) / kTileM), (unsigned)splits);
-  k_gemm_tc<<<grid, 128, smem, as_stream(stream)>>>(mA, mB, g);
+  k_gemm_tc<<<grid, 256, smem, as_stream(stream)>>>(mA, mB, g);
   SKG_LAUNCHED();
   return SKG_OK;
 }
