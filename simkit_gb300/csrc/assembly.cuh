@@ -185,6 +185,7 @@ inline int64_t coarse_padded(const skg_tet_mesh* m) {
   return ((6 * (int64_t)m->coarse->n_agg + 31) / 32) * 32;
 }
 constexpr int kCoarseInvCtas = 456;   // CTAs of the per-instance coarse inversion (3 per SM on 152 SMs)
+// (its row-panel scratch is sized per CTA, which covers one panel pair per cluster of CTAs)
 
 Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base);
 int check_mesh(const skg_tet_mesh* m, int precision);

@@ -14,9 +14,10 @@
 //   k_coarse_galerkin  A_c = P^T A P from the assembled blocks, one warp per
 //                      nonzero 6x6 coarse block, FP32 sums in a fixed
 //                      order (bitwise reproducible), small diagonal shift;
-//   k_coarse_invert    A_c^-1 in place by blocked Gauss-Jordan (SPD, no
+//   k_coarse_invert    A_c^-1 in place by a blocked symmetric sweep (SPD, no
 //                      pivoting, FP32), cooperative grid, one barrier per
-//                      32-wide pivot block.  A non-positive pivot clears the
+//                      32-wide pivot block (k_coarse_invert_inst: one CTA per
+//                      instance of a batch).  A non-positive pivot clears the
 //                      valid flag and the PCG runs one-level.
 // Per PCG iteration (k_pcg_grid2c): the coarse residual P^T r accumulated in
 // 64-bit fixed point (order-independent, so reproducible), e = A_c^-1 P^T r by
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volat
   __shared__ GjShared g;
   const int np = c.np, nbk = np / kGjB;
   const int tid = threadIdx.x;
-  const int units = gj_units(g, np);
+  gj_units(g, np);
   const int64_t gsz = (int64_t)gridDim.x * blockDim.x, g0 = blockIdx.x * (int64_t)blockDim.x + tid;
   unsigned* count = c.bar;
   volatile unsigned* gen = c.bar + 1;
@@ -298,28 +299,35 @@ __global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert(CoarseDev c, volat
     gj_step_units(g, c.M, np, kb, Rw, Rn, blockIdx.x, gridDim.x);
     if (!grid_barrier(count, gen, err)) return;
   }
-  (void)units;
   gj_mirror(g, c.M, np, blockIdx.x, gridDim.x);
   if (blockIdx.x == 0 && tid == 0) *c.ok = good ? 1 : 0;
 }
 
-// The per-instance form for batches: one CTA per instance (largest first by
-// `order`), block barriers only; row panels in a per-CTA scratch of
+// The per-instance form for batches: one thread-block cluster of kGjCluster
+// CTAs per instance (instances largest first by `order`, clusters striding
+// over them), the units of a sweep step spread over the cluster's CTAs and a
+// cluster barrier per step; row panels in a per-cluster scratch of
 // 2 x 32 x max_np floats.  c.ok[inst] = 1 only if every pivot was positive.
+constexpr int kGjCluster = 4;
 __global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert_inst(CoarseDev c, const int32_t* __restrict__ order) {
   __shared__ GjShared g;
+  cgx::cluster_group cl = cgx::this_cluster();
+  const int crank = (int)cl.block_rank(), csize = (int)cl.num_blocks();
+  const int cid = blockIdx.x / csize, ncl = gridDim.x / csize;
   const int tid = threadIdx.x;
-  float* rowp = c.rowp + (int64_t)blockIdx.x * 2 * kGjB * c.max_np;
-  for (int idx = blockIdx.x; idx < c.n_inst; idx += gridDim.x) {
+  const int ct = crank * blockDim.x + tid, cstride = csize * blockDim.x;
+  float* rowp = c.rowp + (int64_t)cid * 2 * kGjB * c.max_np;
+  for (int idx = cid; idx < c.n_inst; idx += ncl) {
     const int inst = order ? order[idx] : idx;
     const int nc = 6 * (c.inst_agg[inst + 1] - c.inst_agg[inst]);
     const int np = ((nc + kGjB - 1) / kGjB) * kGjB;
     float* M = c.M + c.inst_moff[inst];
     const int nbk = np / kGjB;
     gj_units(g, np);
-    for (int i = nc + tid; i < np; i += blockDim.x) M[(int64_t)i * np + i] = 1.f;
-    __syncthreads();
-    for (int q = tid; q < np * kGjB; q += blockDim.x) rowp[q] = M[q];
+    for (int i = nc + ct; i < np; i += cstride) M[(int64_t)i * np + i] = 1.f;
+    cl.sync();
+    for (int q = ct; q < np * kGjB; q += cstride) rowp[q] = M[q];
+    cl.sync();
     bool good = true;
     for (int kb = 0; kb < nbk; ++kb) {
       const float* Rw = rowp + (int64_t)(kb & 1) * kGjB * np;
@@ -327,12 +335,12 @@ __global__ void __launch_bounds__(kGjCols, 3) k_coarse_invert_inst(CoarseDev c, 
       __syncthreads();
       if (tid < 32) good = gj_inverse32_warp(Rw + kb * kGjB, np, g.piv) && good;
       __syncthreads();
-      gj_step_units(g, M, np, kb, Rw, Rn, 0, 1);
+      gj_step_units(g, M, np, kb, Rw, Rn, crank, csize);
+      cl.sync();
     }
-    __syncthreads();
-    gj_mirror(g, M, np, 0, 1);
-    if (tid == 0) c.ok[inst] = good ? 1 : 0;
-    __syncthreads();
+    gj_mirror(g, M, np, crank, csize);
+    if (crank == 0 && tid == 0) c.ok[inst] = good ? 1 : 0;
+    cl.sync();   // the scratch and the table are reused by the next instance
   }
 }
 

@@ -800,10 +800,22 @@ static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cud
   k_coarse_galerkin<R><<<(int)((gal_threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(A, c);
   SKG_LAUNCHED();
   if (c.inst_agg && c.n_inst > 1) {
-    // batches: one CTA per instance, largest first
-    const int grid = c.n_inst < kCoarseInvCtas ? c.n_inst : kCoarseInvCtas;
-    k_coarse_invert_inst<<<grid, kGjCols, 0, s>>>(c, order);
-    SKG_LAUNCHED();
+    // batches: one cluster of kGjCluster CTAs per instance, largest first
+    int nclu = kCoarseInvCtas / kGjCluster;
+    if (nclu > c.n_inst) nclu = c.n_inst;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kGjCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(nclu * kGjCluster, 1, 1);
+    cfg.blockDim = dim3(kGjCols, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SKG_CUDA(cudaLaunchKernelEx(&cfg, k_coarse_invert_inst, c, order));
     return SKG_OK;
   }
   static int per_sm = 0;
