@@ -334,7 +334,7 @@ def run_batched(args):
         if total.status != 0:
             raise SystemExit(f"batched warm-up step failed: {total}")
     # cluster-size policy of the batched PCG (untimed; cached per device and batch)
-    from simkit_gb300.autotune import tune_batch_policy
+    from simkit_gb300.autotune import tune_batch_policy, tune_pcg_variant
     policy, policy_ms = tune_batch_policy(b, use_cache=not args.retune)
     learned = None
     fb = None
@@ -396,6 +396,7 @@ def run_batched(args):
             s1 = BESolver.from_spec(specs[i], precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=cs)
             for _ in range(args.warmup):
                 s1.step()
+            tune_pcg_variant(s1, use_cache=not args.retune)   # the single-instance solver at its best cluster size
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)

@@ -254,8 +254,9 @@ typedef struct skg_be_params {
                                scaled to the FP32 rounding of the energy sum */
   int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */
   int32_t pcg_variant;      /* grid-persistent PCG kernel variant 0-8 (lanes per row x rows in
-                               flight: 8x1, 16x1, 8x2, 16x2, 4x2, 4x4, 2x4, 8x4, 2x2), chosen
-                               by the autotuner */
+                               flight: 8x1, 16x1, 8x2, 16x2, 4x2, 4x4, 2x4, 8x4, 2x2); for the
+                               one-cluster PCG (mode 2) the cluster size: 0 by system size,
+                               1-4 = 16, 8, 4, 2 CTAs; chosen by the autotuner */
   int32_t batch_min_cluster; /* batched PCG: smallest thread-block cluster an instance gets (1, 2,
                                4, 8 or 16; 0 = 4); each instance gets the smallest power of two
                                at least this large whose CTAs hold its vectors */

@@ -1,7 +1,6 @@
 """Autotuners for the PCG kernels.
 
-Single systems: the grid-persistent PCG kernel
-The PCG kernel comes in variants that trade lanes per block row (G) against
+Single systems: the grid-persistent PCG kernel comes in variants that trade lanes per block row (G) against
 block rows in flight per lane group (U): (8,1), (16,1), (8,2), (16,2),
 (4,2), (4,4), (2,4), (8,4), (2,2).  Which one keeps the most loads in flight without idling lanes
 depends on the row lengths of the mesh and on the device, so the variant is
@@ -9,7 +8,9 @@ picked by timing: each candidate runs one backward-Euler step from the same
 saved state with per-phase CUDA-event timing, and the variant with the
 lowest time per PCG iteration wins.  Results are cached in a JSON file keyed
 by device, system size and precision (``$SIMKIT_GB300_CACHE`` or
-``~/.cache/simkit_gb300/autotune.json``).
+``~/.cache/simkit_gb300/autotune.json``).  Systems small enough for one
+thread-block cluster have one knob instead, the cluster size (16, 8, 4 or 2
+CTAs: fewer CTAs make the cluster barriers cheaper and give each CTA more rows).
 
 Batches: the cluster-size policy of the batched PCG (the per-CTA shared-memory
 cap for vectors and the smallest cluster an instance gets) decides how many
@@ -68,10 +69,19 @@ def _history(solver):
     return levels
 
 
-def tune_pcg_variant(solver, variants=tuple(VARIANTS), use_cache=True):
-    """Pick the fastest PCG kernel variant for ``solver``; returns (variant, timings_us)."""
-    if solver.params.pcg_mode not in (1, 3, 5, 7) or (solver.params.pcg_mode == 3 and solver.mesh.n <= CLUSTER_ROWS):
+CLUSTER_VARIANTS = {1: 16, 2: 8, 3: 4, 4: 2}   # thread-block cluster sizes of the one-cluster PCG
+
+
+def tune_pcg_variant(solver, variants=None, use_cache=True):
+    """Pick the fastest PCG kernel variant for ``solver``: the (lanes per row, rows in flight)
+    variant of the grid kernel, or the cluster size of the one-cluster kernel; returns
+    (variant, timings_us per PCG iteration)."""
+    mode = solver.params.pcg_mode
+    cluster = mode == 2 or (mode == 3 and solver.mesh.n <= CLUSTER_ROWS)
+    if mode not in (1, 2, 3, 5, 7):
         return solver.params.pcg_variant, {}
+    if variants is None:
+        variants = tuple(CLUSTER_VARIANTS) if cluster else tuple(VARIANTS)
     key = _key(solver)
     table = _load() if use_cache else {}
     if key in table:

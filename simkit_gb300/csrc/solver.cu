@@ -840,7 +840,8 @@ static int coarse_refresh(const Bsr<R>& A, const CoarseDev& c, double* scal, cud
 // instance's coarse vectors in the last kCoarseSmem bytes of dynamic shared memory
 template <typename R>
 static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, R* xout,
-                              double rtol, int max_iter, double* scal, cudaStream_t s, const CoarseDev* cd = nullptr) {
+                              double rtol, int max_iter, double* scal, cudaStream_t s, const CoarseDev* cd = nullptr,
+                              int variant = 0) {
   const void* kern = cd ? (const void*)k_pcg_cluster<R, kGc, true> : (const void*)k_pcg_cluster<R, kGc, false>;
   static thread_local bool configured[2] = {false, false};
   if (!configured[cd ? 1 : 0]) {
@@ -849,7 +850,11 @@ static int launch_pcg_cluster(const Bsr<R>& A, const double* b, double bsign, co
     configured[cd ? 1 : 0] = true;
   }
   const int budget = cd ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
+  // cluster size: variant 0 by size, 1..4 = 16, 8, 4, 2 CTAs (picked by the autotuner), never
+  // smaller than what holds the vectors
   int csize = A.nbr >= 2048 ? kClusterMax : 8;
+  if (variant >= 1 && variant <= 4) csize = kClusterMax >> (variant - 1);
+  while (csize < kClusterMax && cluster_vec_bytes(A.nbr, csize, (int)sizeof(R)) > budget) csize *= 2;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -903,7 +908,7 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
   }
   if (mode == 2) {
     const CoarseDev* cc = cd && cd->inst_agg ? cd : nullptr;
-    SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s, cc));
+    SKG_TRY(launch_pcg_cluster<R>(A, b, bsign, pinned, v.x, rtol, max_iter, scal, s, cc, variant));
     res->launches += 1;
   } else if (mode == 4) {
     int per_sm = 0;
