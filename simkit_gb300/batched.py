@@ -29,13 +29,15 @@ class BatchedBESolver:
 
     ``specs`` is a list of objects with ``X, T, mu, lam, rho, gravity,
     pinned`` (e.g. ``simkit_gb300.beams.BeamSpec``); each keeps its own
-    material, gravity direction and pins.
+    material, gravity direction and pins.  ``coarse``: two-level PCG with
+    per-instance aggregates ('auto': 4^3 mesh spacings, or a box size), None for
+    the one-level block-Jacobi PCG; ``coarse_refresh`` as in ``BESolver``.
     """
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
                  integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse=None, coarse_refresh="step"):
+                 coarse="auto", coarse_refresh="step"):
         _lib.load()
         self.n_inst = len(specs)
         if self.n_inst == 0:

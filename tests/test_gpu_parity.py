@@ -447,7 +447,7 @@ def test_batched_two_level(api):
     from simkit_gb300.solver import BESolver
     specs = beam_batch(8, seed=5)
     b = BatchedBESolver(specs, coarse="auto")
-    b1 = BatchedBESolver(specs)
+    b1 = BatchedBESolver(specs, coarse=None)
     singles = [BESolver.from_spec(sp, coarse="auto", coarse_form="cluster", pcg_mode=2) for sp in specs]
     it2 = it1 = 0
     for step in range(3):
@@ -476,7 +476,7 @@ def test_batched_step_matches_single_instance_and_oracle(api):
     from simkit_gb300.solver import BESolver
     from oracle import rollout
     specs = beam_batch(6, seed=3, nx_range=(2, 5), ny_range=(2, 4), nz_range=(3, 8))
-    b = BatchedBESolver(specs)
+    b = BatchedBESolver(specs, coarse=None)
     singles = [BESolver.from_spec(sp, coarse=None) for sp in specs]
     refs = [rollout.from_spec(sp) for sp in specs]
     states = [(r.x_rest.copy(), r.x_rest.copy()) for r in refs]
