@@ -81,7 +81,9 @@ def tune_pcg_variant(solver, variants=None, use_cache=True):
     if mode not in (1, 2, 3, 5, 7):
         return solver.params.pcg_variant, {}
     if variants is None:
-        variants = tuple(CLUSTER_VARIANTS) if cluster else tuple(VARIANTS)
+        two_level_grid = getattr(solver, "coarse_form", None) == "grid" and not cluster
+        variants = (tuple(CLUSTER_VARIANTS) if cluster
+                    else tuple(VARIANTS) + tuple(v + 9 for v in VARIANTS) if two_level_grid else tuple(VARIANTS))
     key = _key(solver)
     table = _load() if use_cache else {}
     if key in table:

@@ -411,10 +411,12 @@ __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, f
 // with r.M^-1 r = r.D^-1 r + (P^T r).e.  When the coarse inverse is not valid
 // (c.ok == 0) phases C and the restriction are skipped: the one-level method.
 // partials: >= 4 gridDim + 4 accumulators of scratch.
-template <typename R, int G, int U>
-__global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v, CoarseDev c, double* partials,
-                                                       unsigned* bar, double* scal) {
-  __shared__ Dacc<R> wsum[2][kBlock / 32];
+// NT threads per block: 256 (three blocks per SM) or 768 (one per SM: a third of the
+// barrier arrivals and block partials, the same threads in flight)
+template <typename R, int G, int U, int NT = kBlock>
+__global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v, CoarseDev c,
+                                                                      double* partials, unsigned* bar, double* scal) {
+  __shared__ Dacc<R> wsum[2][NT / 32];
   __shared__ __align__(16) float rcf[kCoarseMax];
   Dacc<R>* PA = reinterpret_cast<Dacc<R>*>(partials);     // p.q per block
   Dacc<R>* PB = PA + gridDim.x;                            // r.z, r.r per block
@@ -467,10 +469,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
       Dacc<R> pc[1];
       dacc_zero(pc[0]);
       coarse_product<R>(c, rcf, 1.f / sc, pc[0]);
-      block_total<R, 1>(pc, wsum);
+      block_total<R, 1, NT>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];
-      if (!grid_barrier_total<R, 1>(count, gen, err, PC, TOT + 3, t3, wsum)) {
+      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, TOT + 3, t3, wsum)) {
         status = SKG_ERR_TIMEOUT;
         done = true;
       } else {
@@ -507,10 +509,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
           dacc_dot3(pq[0], p, ys[u]);
         }
     }
-    block_total<R, 1>(pq, wsum);
+    block_total<R, 1, NT>(pq, wsum);
     if (threadIdx.x == 0) st_dacc(PA + blockIdx.x, pq[0]);
     Dacc<R> t1[1];
-    if (!grid_barrier_total<R, 1>(count, gen, err, PA, TOT, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 1, NT>(count, gen, err, PA, TOT, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     const R pqr = dacc_r(t1[0]);
     if (!(pqr > R(0)) || !isfinite(pqr)) {
       status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
@@ -540,13 +542,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
       }
       if (con) coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
     }
-    block_total<R, 2>(acc, wsum);
+    block_total<R, 2, NT>(acc, wsum);
     if (threadIdx.x == 0) {
       st_dacc(PB + blockIdx.x, acc[0]);
       st_dacc(PB + gridDim.x + blockIdx.x, acc[1]);
     }
     Dacc<R> t2[2];
-    if (!grid_barrier_total<R, 2>(count, gen, err, PB, TOT + 1, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 2, NT>(count, gen, err, PB, TOT + 1, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     ++it;
     rr_acc = t2[1];
     rr_prev = dacc_value(t2[1]);
@@ -559,10 +561,10 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v
       Dacc<R> pc[1];
       dacc_zero(pc[0]);
       coarse_product<R>(c, rcf, 1.f / sc, pc[0]);
-      block_total<R, 1>(pc, wsum);
+      block_total<R, 1, NT>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];
-      if (!grid_barrier_total<R, 1>(count, gen, err, PC, TOT + 3, t3, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, TOT + 3, t3, wsum)) { status = SKG_ERR_TIMEOUT; break; }
       rz = dacc_add(rz, t3[0]);
     }
     beta = dacc_r(rz) / dacc_r(rz_old);

@@ -19,8 +19,8 @@
 namespace skg {
 
 // block total of NV accumulators by a fixed tree; valid in thread 0
-template <typename R, int NV>
-__device__ __forceinline__ void block_total(Dacc<R> (&v)[NV], Dacc<R> (*wsum)[kBlock / 32]) {
+template <typename R, int NV, int NT = kBlock>
+__device__ __forceinline__ void block_total(Dacc<R> (&v)[NV], Dacc<R> (*wsum)[NT / 32]) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
@@ -33,7 +33,7 @@ __device__ __forceinline__ void block_total(Dacc<R> (&v)[NV], Dacc<R> (*wsum)[kB
     for (int k = 0; k < NV; ++k) {
       Dacc<R> x;
       dacc_zero(x);
-      if (lane < kBlock / 32) x = wsum[k][lane];
+      if (lane < NT / 32) x = wsum[k][lane];
       v[k] = dacc_tree<R, 32>(x);
     }
   }
@@ -52,10 +52,10 @@ __device__ __forceinline__ Dacc<double> ld_dacc(const Dacc<double>* p) { return 
 // Grid barrier whose last arriving block first sums the NV x gridDim partials
 // (part[k * gridDim + b]) in index order into tot[0..NV); every thread returns
 // the totals.  Bounded spin: on timeout err is set and false returned.
-template <typename R, int NV>
+template <typename R, int NV, int NT = kBlock>
 __device__ __forceinline__ bool grid_barrier_total(unsigned* count, volatile unsigned* gen, volatile double* err,
                                                    const Dacc<R>* part, Dacc<R>* tot, Dacc<R> (&out)[NV],
-                                                   Dacc<R> (*wsum)[kBlock / 32]) {
+                                                   Dacc<R> (*wsum)[NT / 32]) {
   __shared__ int last;
   __shared__ int ok;
   __shared__ unsigned g0;
@@ -75,7 +75,7 @@ __device__ __forceinline__ bool grid_barrier_total(unsigned* count, volatile uns
       dacc_zero(s[k]);
       for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s[k] = dacc_add(s[k], ld_dacc(part + k * gridDim.x + i));
     }
-    block_total<R, NV>(s, wsum);
+    block_total<R, NV, NT>(s, wsum);
     if (threadIdx.x == 0) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) st_dacc(tot + k, s[k]);

@@ -931,9 +931,12 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
   } else if (mode == 1 || mode == 5 || mode == 7) {
     // kernel variant: lanes per row G and rows in flight U (picked by the autotuner);
     // mode 5 is the two-barrier form (pcg_grid.cuh), mode 7 its two-level form (coarse.cuh)
-#define SKG_PCG_KERN(G_, U_)                                                   \
-  (mode == 7   ? (const void*)k_pcg_grid2c<R, G_, U_>                          \
-   : mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_>                           \
+    // mode 7 variants 9..17: the shapes of 0..8 with 768-thread blocks (one per SM)
+    const bool wide = mode == 7 && variant >= 9;
+    if (wide) variant -= 9;
+#define SKG_PCG_KERN(G_, U_)                                                                              \
+  (mode == 7   ? (wide ? (const void*)k_pcg_grid2c<R, G_, U_, 768> : (const void*)k_pcg_grid2c<R, G_, U_>) \
+   : mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_>                                                      \
                : (const void*)k_pcg_persistent<R, G_, U_>)
     const void* kern = SKG_PCG_KERN(8, 1);
     int G = 8;
@@ -949,9 +952,10 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
       default: break;
     }
 #undef SKG_PCG_KERN
+    const int nt = wide ? 768 : kBlock;
     int per_sm = 0;
-    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0));
-    int64_t want = (A.nbr * G + kBlock - 1) / kBlock;
+    SKG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, 0));
+    int64_t want = (A.nbr * G + nt - 1) / nt;
     int64_t cap = (int64_t)per_sm * num_sms();
     if (cap > kMaxGrid / 2) cap = kMaxGrid / 2;
     int grid = (int)(want < cap ? want : cap);
@@ -967,7 +971,7 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
       SKG_CUDA(cudaMemsetAsync(cd->rc, 0, sizeof(unsigned long long) * (size_t)cd->np, s));
       CoarseDev c2 = *cd;
       void* args[] = {&a2, &v2, &c2, &p2, &bar, &sc2};
-      SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));
+      SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(nt), args, 0, s));
     } else {
       void* args[] = {&a2, &v2, &p2, &bar, &sc2};
       SKG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kBlock), args, 0, s));

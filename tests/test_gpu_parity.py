@@ -357,6 +357,26 @@ def test_two_level_pcg_matches_reference(api, precision, refresh):
     assert 2 * pcg_two < pcg_one
 
 
+@pytest.mark.parametrize("variant", [4, 13])
+def test_two_level_grid_block_shapes(api, variant):
+    """The two-level grid PCG with 256-thread blocks (variant 4: 4 lanes per row, 2 rows in flight)
+    and the same shape with 768-thread blocks (variant 13): 20 steps within the tolerances of the
+    default path on the 12,288-tet beam."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    d = _load("rollout_beam_8x8x32.npz")
+    spec = beam_small_steady()
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), pcg_mode=7, coarse=4, coarse_form="grid")
+    s.params.pcg_variant = variant
+    X = spec.X.reshape(-1)
+    for step in range(1, 21):
+        info = s.step()
+        assert info.converged, (step, info)
+        if step in d["steps"]:
+            k = list(d["steps"]).index(step)
+            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+
+
 def test_two_level_repeatable(api):
     """Two solvers with the same inputs take bitwise the same two-level steps (fixed-point
     coarse residual, fixed-order Galerkin sums)."""
