@@ -246,10 +246,12 @@ typedef struct skg_be_params {
   double ls_beta;           /* step factor, simkit default 0.5 */
   int32_t ls_max_iter;      /* simkit default 100 */
   int32_t pcg_mode;         /* 0 kernel per phase, 1 grid-persistent cooperative kernel,
-                               2 one thread-block cluster, 3 by size (2 up to 24,576 block
-                               rows, else 5), 4 grid-persistent Chronopoulos-Gear form,
-                               5 grid-persistent with two barriers per iteration,
-                               7 grid-persistent two-level (needs mesh->coarse; else 5) */
+                               2 one thread-block cluster (two-level with the per-instance
+                               coarse form), 3 by size (2 up to 24,576 block rows, else 7 with
+                               the whole-mesh coarse form, else 5), 4 grid-persistent
+                               Chronopoulos-Gear form, 5 grid-persistent with two barriers per
+                               iteration, 7 grid-persistent two-level (needs the whole-mesh
+                               coarse form; else 5) */
   double ls_threshold;      /* Armijo slack, simkit default 1e-12; < 0 selects a slack
                                scaled to the FP32 rounding of the energy sum */
   int32_t profile;          /* 1: time each phase with CUDA events (adds syncs) */
@@ -311,9 +313,10 @@ typedef struct skg_step_info {
 } skg_step_info;
 
 int64_t skg_be_workspace_size(const skg_tet_mesh* mesh, int precision);
-/* One backward-Euler step: Newton on the free DOFs from x_tilde = 2 x_k - x_{k-1}
- * with a block-Jacobi PCG solve per iteration and Armijo backtracking, until the
- * relative residual is below tol.  Host-synchronizes for its decisions. */
+/* One backward-Euler (or BDF2) step: Newton on the free DOFs from x_tilde = 2 x_k - x_{k-1}
+ * with a PCG solve per iteration (block Jacobi, plus the coarse level when mesh->coarse
+ * is attached) and Armijo backtracking, until the relative residual is below tol.
+ * Host-synchronizes for its decisions. */
 int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state,
                 void* workspace, skg_step_info* info_h, void* stream);
 
