@@ -536,7 +536,7 @@ def main():
     p_newton = sum(i.newton_iters for i in pinfos)
     p_pcg = sum(i.pcg_iters for i in pinfos)
     hbm, peak_kind = peaks()
-    n_coarse = 6 * solver._coarse_n_agg() if solver.coarse_form == "grid" else 0
+    n_coarse = 6 * solver._coarse_n_agg() if solver.coarse_form is not None else 0
     ab = algorithmic_bytes(spec, nb, n_coarse)
     pcg_ms_per_iter = tp["pcg"] / max(p_pcg, 1)
     pcg_gbs = ab["pcg_iter"] / (pcg_ms_per_iter * 1e-3) / 1e9
@@ -546,21 +546,24 @@ def main():
     share = {k: v / total_p for k, v in tp.items()} if total_p > 0 else {}
     dominant = max(share, key=share.get) if share else "pcg"
     traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f)
-    except Exception:
-        traffic = None
+    if not args.small:   # the ncu figures are for the 32 x 32 x 128 beam
+        try:
+            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+                traffic = json.load(f)
+        except Exception:
+            traffic = None
     if dominant in ("hessian", "assemble"):
         roof = {"bound": "hbm", "kernel": "k_tet_hessian + k_assemble", "achieved": hess_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": hess_gbs / hbm,
                 "traffic": (traffic or {}).get("tet_hessian_bytes_per_launch"),
                 "algorithmic_bytes": ab["tet_hessian"] * spec.n_tets, "ms_per_launch": hess_ms_per_launch}
     else:
-        roof = {"bound": "hbm", "kernel": ("k_pcg_grid2c (two-level grid PCG)" if n_coarse else "k_pcg_grid2 / k_pcg_cluster")
-                + ", per PCG iteration", "achieved": pcg_gbs, "peak": hbm,
+        kname = {"grid": "k_pcg_grid2c (two-level grid PCG)", "cluster": "k_pcg_cluster (two-level, one cluster)"}.get(
+            solver.coarse_form, "k_pcg_grid2 / k_pcg_cluster")
+        roof = {"bound": "hbm", "kernel": kname + ", per PCG iteration", "achieved": pcg_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": pcg_gbs / hbm,
-                "traffic": (traffic or {}).get("pcg2c_bytes_per_iter" if n_coarse else "pcg_bytes_per_iter"),
+                "traffic": (traffic or {}).get("pcg2c_bytes_per_iter" if solver.coarse_form == "grid"
+                                               else "pcg_bytes_per_iter" if solver.coarse_form is None else "none"),
                 "algorithmic_bytes": ab["pcg_iter"], "ms_per_launch": pcg_ms_per_iter}
     roof["peak_kind"] = peak_kind
     roof["phase_share"] = share
