@@ -85,6 +85,30 @@ int skg_mmnh_hessian_element_F(int dim, int precision, const double* F, const do
                                double* H, int64_t t, void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* element tier: simkit/energies/arap.py and simkit/energies/fcr.py         */
+/* ---------------------------------------------------------------------- */
+/* Same arguments as the stable neo-Hookean element tier (lam is read by the
+ * fixed-corotated entries only; the ARAP entries accept lam = NULL).  R is the
+ * rotation of the rotation-variant SVD (simkit/polar_svd.py:59-90), dR/dF the
+ * closed form of simkit/rotation_gradient.py:12-70.  Replace
+ * arap_energy_element_F (arap.py:71-91), arap_gradient_element_F (:94-114),
+ * arap_hessian_element_F (:117-145, not projected), fcr_energy_element_F
+ * (fcr.py:41-62), fcr_gradient_element_F (:65-125) and fcr_hessian_element_F
+ * (:128-302, not projected). */
+int skg_arap_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* psi, int64_t t, void* stream);
+int skg_arap_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                                double* P, int64_t t, void* stream);
+int skg_arap_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* H, int64_t t, void* stream);
+int skg_fcr_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                             double* psi, int64_t t, void* stream);
+int skg_fcr_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* P, int64_t t, void* stream);
+int skg_fcr_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* H, int64_t t, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* contact springs: simkit/energies/contact_springs_plane.py:44-200        */
 /* ---------------------------------------------------------------------- */
 /* One contact plane of simkit's contact springs (simkit/energies/contact_springs_plane.py:44-200):
@@ -152,8 +176,10 @@ int skg_pattern_build(const int32_t* T_h, int64_t n, int64_t t, int64_t* n_block
 /* Elastic energies of the per-tet kernels (simkit/energies/elastic.py:75 dispatches the same set
  * by name). */
 typedef enum skg_material {
-  SKG_MAT_STABLE_NEO_HOOKEAN = 0,        /* simkit/energies/stable_neo_hookean.py */
-  SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN = 1 /* simkit/energies/macklin_mueller_neo_hookean.py */
+  SKG_MAT_STABLE_NEO_HOOKEAN = 0,          /* simkit/energies/stable_neo_hookean.py */
+  SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN = 1, /* simkit/energies/macklin_mueller_neo_hookean.py */
+  SKG_MAT_ARAP = 2,                        /* simkit/energies/arap.py (lam unused) */
+  SKG_MAT_FIXED_COROTATED = 3              /* simkit/energies/fcr.py */
 } skg_material;
 
 /* Two-level preconditioner data (optional; pcg_mode 7).  Vertices are grouped

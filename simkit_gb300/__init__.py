@@ -20,7 +20,11 @@ _API = {
     "macklin_mueller_neo_hookean_hessian_element_F", "macklin_mueller_neo_hookean_energy_x",
     "macklin_mueller_neo_hookean_gradient_x", "macklin_mueller_neo_hookean_hessian_x",
     "macklin_mueller_neo_hookean_energy", "macklin_mueller_neo_hookean_gradient",
-    "macklin_mueller_neo_hookean_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
+    "macklin_mueller_neo_hookean_hessian", "arap_energy_element_F", "arap_gradient_element_F",
+    "arap_hessian_element_F", "arap_energy_x", "arap_gradient_x", "arap_hessian_x", "arap_energy",
+    "arap_gradient", "arap_hessian", "fcr_energy_element_F", "fcr_gradient_element_F",
+    "fcr_hessian_element_F", "fcr_energy_x", "fcr_gradient_x", "fcr_hessian_x", "fcr_energy",
+    "fcr_gradient", "fcr_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
     "elastic_hessian_element_F", "elastic_energy_x", "elastic_gradient_x", "elastic_hessian_x",
     "elastic_energy", "elastic_gradient", "elastic_hessian", "contact_springs_plane_energy",
     "contact_springs_plane_gradient", "contact_springs_plane_hessian",

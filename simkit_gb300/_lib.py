@@ -103,6 +103,12 @@ _SIGNATURES = {
     "skg_mmnh_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_mmnh_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_mmnh_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_arap_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_arap_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_arap_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_fcr_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_fcr_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_fcr_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_psd_project": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "skg_contact_plane_terms": (c_i32, [c_vp, c_i64, ctypes.POINTER(ContactPlaneC), c_vp, c_vp, c_vp, c_vp, c_vp,
                                         c_vp]),

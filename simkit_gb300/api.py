@@ -275,7 +275,7 @@ def stable_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, ps
 # Macklin-Mueller neo-Hookean: simkit/energies/macklin_mueller_neo_hookean.py  #
 # --------------------------------------------------------------------------- #
 _MM = "Macklin-Mueller Neo-Hookean"
-MATERIALS = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1}
+MATERIALS = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1, "arap": 2, "fcr": 3}
 
 
 def macklin_mueller_neo_hookean_energy_element_F(F, mu, lam, precision: str = "fp64"):
@@ -336,6 +336,128 @@ def macklin_mueller_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] =
     """simkit ``macklin_mueller_neo_hookean_hessian`` (:745-773)."""
     return macklin_mueller_neo_hookean_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, lam,
                                                  volume(X, T), psd=psd)
+
+
+# --------------------------------------------------------------------------- #
+# corotational energies: simkit/energies/arap.py, simkit/energies/fcr.py       #
+# --------------------------------------------------------------------------- #
+def _energy_x(X, J, mu, lam, vol, material) -> float:
+    m = _bind(J, mu, lam, vol, material)
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    e = ctypes.c_double()
+    check(_lib.load().skg_snh_energy_x(ctypes.byref(m.c), _ptr(x), ctypes.byref(e), _ptr(ws), _stream_ptr()))
+    return float(e.value)
+
+
+def _gradient_x(X, J, mu, lam, vol, material):
+    m = _bind(J, mu, lam, vol, material)
+    x = _dev(X).reshape(-1)
+    ws = m.workspace(SKG_FP64)
+    g = torch.empty(3 * m.n, dtype=torch.float64, device="cuda")
+    check(_lib.load().skg_snh_gradient_x(ctypes.byref(m.c), _ptr(x), _ptr(g), _ptr(ws), _stream_ptr()))
+    return _out(g.reshape(-1, 1), X)
+
+
+def _hessian_x(X, J, mu, lam, vol, material, psd, precision):
+    m = _bind(J, mu, lam, vol, material)
+    B = BlockMatrix(m, assemble_hessian_blocks(m, X, precision=precision, psd=psd))
+    return B if isinstance(X, torch.Tensor) else B.to_scipy()
+
+
+def _no_lam(mu):
+    """ARAP has no volume term; the kernels take a lam array and ignore it."""
+    return mu
+
+
+def arap_energy_element_F(F, mu, precision: str = "fp64"):
+    """psi = mu/2 |F - R|^2 per element, (t, 1).  simkit ``arap_energy_element_F`` (arap.py:71-91)."""
+    return _elem("skg_arap_energy_element_F", F, mu, _no_lam(mu), lambda t, d: (t, 1), precision, "ARAP")
+
+
+def arap_gradient_element_F(F, mu, precision: str = "fp64"):
+    """P = mu (F - R), (t, d, d).  simkit ``arap_gradient_element_F`` (arap.py:94-114)."""
+    return _elem("skg_arap_gradient_element_F", F, mu, _no_lam(mu), lambda t, d: (t, d, d), precision, "ARAP")
+
+
+def arap_hessian_element_F(F, mu, precision: str = "fp64"):
+    """mu (I - dR/dF), (t, d*d, d*d), not projected.  simkit ``arap_hessian_element_F`` (arap.py:117-145)."""
+    return _elem("skg_arap_hessian_element_F", F, mu, _no_lam(mu), lambda t, d: (t, d * d, d * d), precision, "ARAP")
+
+
+def arap_energy_x(X, J, mu, vol) -> float:
+    """sum vol psi(J x).  simkit ``arap_energy_x`` (arap.py:242-265)."""
+    return _energy_x(X, J, mu, _no_lam(mu), vol, MATERIALS["arap"])
+
+
+def arap_gradient_x(X, J, mu, vol):
+    """J^T vec(vol P), (3n, 1).  simkit ``arap_gradient_x`` (arap.py:268-292)."""
+    return _gradient_x(X, J, mu, _no_lam(mu), vol, MATERIALS["arap"])
+
+
+def arap_hessian_x(X, J, mu, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(psd(vol He)) J.  simkit ``arap_hessian_x`` (arap.py:295-325)."""
+    return _hessian_x(X, J, mu, _no_lam(mu), vol, MATERIALS["arap"], psd, precision)
+
+
+def arap_energy(X, T, mu, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``arap_energy`` (arap.py:505-529)."""
+    return arap_energy_x(X if U is None else U, deformation_jacobian(X, T), mu, volume(X, T))
+
+
+def arap_gradient(X, T, mu, U: Optional[np.ndarray] = None):
+    """simkit ``arap_gradient`` (arap.py:532-555)."""
+    return arap_gradient_x(X if U is None else U, deformation_jacobian(X, T), mu, volume(X, T))
+
+
+def arap_hessian(X, T, mu, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``arap_hessian`` (arap.py:558-583)."""
+    return arap_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, volume(X, T), psd=psd)
+
+
+def fcr_energy_element_F(F, mu, lam, precision: str = "fp64"):
+    """psi = mu |F - R|^2 + lam/2 (J - 1)^2 per element, (t, 1).  simkit ``fcr_energy_element_F`` (fcr.py:41-62)."""
+    return _elem("skg_fcr_energy_element_F", F, mu, lam, lambda t, d: (t, 1), precision, "FCR")
+
+
+def fcr_gradient_element_F(F, mu, lam, precision: str = "fp64"):
+    """P = 2 mu (F - R) + lam (J - 1) cof F, (t, d, d).  simkit ``fcr_gradient_element_F`` (fcr.py:65-125)."""
+    return _elem("skg_fcr_gradient_element_F", F, mu, lam, lambda t, d: (t, d, d), precision, "FCR")
+
+
+def fcr_hessian_element_F(F, mu, lam, precision: str = "fp64"):
+    """(t, d*d, d*d), not projected.  simkit ``fcr_hessian_element_F`` (fcr.py:128-302)."""
+    return _elem("skg_fcr_hessian_element_F", F, mu, lam, lambda t, d: (t, d * d, d * d), precision, "FCR")
+
+
+def fcr_energy_x(X, J, mu, lam, vol) -> float:
+    """sum vol psi(J x).  simkit ``fcr_energy_x`` (fcr.py:308-333)."""
+    return _energy_x(X, J, mu, lam, vol, MATERIALS["fcr"])
+
+
+def fcr_gradient_x(X, J, mu, lam, vol):
+    """J^T vec(vol P), (3n, 1).  simkit ``fcr_gradient_x`` (fcr.py:336-362)."""
+    return _gradient_x(X, J, mu, lam, vol, MATERIALS["fcr"])
+
+
+def fcr_hessian_x(X, J, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(psd(vol He)) J.  simkit ``fcr_hessian_x`` (fcr.py:365-397)."""
+    return _hessian_x(X, J, mu, lam, vol, MATERIALS["fcr"], psd, precision)
+
+
+def fcr_energy(X, T, mu, lam, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``fcr_energy`` (fcr.py:508-533)."""
+    return fcr_energy_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T))
+
+
+def fcr_gradient(X, T, mu, lam, U: Optional[np.ndarray] = None):
+    """simkit ``fcr_gradient`` (fcr.py:536-561)."""
+    return fcr_gradient_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T))
+
+
+def fcr_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``fcr_hessian`` (fcr.py:564-591)."""
+    return fcr_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T), psd=psd)
 
 
 # --------------------------------------------------------------------------- #
@@ -403,58 +525,72 @@ def contact_springs_plane_hessian(X, k: float, p, n, M=None, return_contact_inds
 # --------------------------------------------------------------------------- #
 # material dispatch: simkit/energies/elastic.py                               #
 # --------------------------------------------------------------------------- #
-def _material(material):
-    if material == "macklin-mueller-neo-hookean":
-        return "macklin_mueller_neo_hookean"
-    if material in ("linear-elasticity", "arap", "fcr"):
+_PREFIX = {"macklin-mueller-neo-hookean": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr"}
+
+
+def _material(material, lam_args):
+    """(function-name prefix, lam-carrying positional args) of ``material``; ARAP's functions
+    take no lam (simkit/energies/elastic.py passes lam to every material but ARAP)."""
+    if material in _PREFIX:
+        return _PREFIX[material], (() if material == "arap" else lam_args)
+    if material == "linear-elasticity":
         raise NotImplementedError(f"material {material!r} has no GPU kernels in this package")
     raise ValueError("Unknown material type: " + str(material))
 
 
 def elastic_energy_element_F(F, mu, lam, material: str):
     """simkit ``elastic_energy_element_F`` (elastic.py:86-116)."""
-    return globals()[_material(material) + "_energy_element_F"](F, mu, lam)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_energy_element_F"](F, mu, *la)
 
 
 def elastic_gradient_element_F(F, mu, lam, material: str):
     """simkit ``elastic_gradient_element_F`` (elastic.py:396-426)."""
-    return globals()[_material(material) + "_gradient_element_F"](F, mu, lam)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_gradient_element_F"](F, mu, *la)
 
 
 def elastic_hessian_element_F(F, mu, lam, material: str, psd: bool = True):
     """simkit ``elastic_hessian_element_F`` (elastic.py:632-668): unweighted blocks, projected if psd."""
-    Q = globals()[_material(material) + "_hessian_element_F"](F, mu, lam)
+    pre, la = _material(material, (lam,))
+    Q = globals()[pre + "_hessian_element_F"](F, mu, *la)
     return psd_project(Q) if psd else Q
 
 
 def elastic_energy_x(X, J, mu, lam, vol, material: str) -> float:
     """simkit ``elastic_energy_x`` (elastic.py:119-148)."""
-    return globals()[_material(material) + "_energy_x"](X, J, mu, lam, vol)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_energy_x"](X, J, mu, *la, vol)
 
 
 def elastic_gradient_x(X, J, mu, lam, vol, material: str):
     """simkit ``elastic_gradient_x`` (elastic.py:429-459)."""
-    return globals()[_material(material) + "_gradient_x"](X, J, mu, lam, vol)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_gradient_x"](X, J, mu, *la, vol)
 
 
 def elastic_hessian_x(X, J, mu, lam, vol, material: str, psd: bool = True):
     """simkit ``elastic_hessian_x`` (elastic.py:671-705)."""
-    return globals()[_material(material) + "_hessian_x"](X, J, mu, lam, vol, psd=psd)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_hessian_x"](X, J, mu, *la, vol, psd=psd)
 
 
 def elastic_energy(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None) -> float:
     """simkit ``elastic_energy`` (elastic.py:360-393)."""
-    return globals()[_material(material) + "_energy"](X, T, mu, lam, U)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_energy"](X, T, mu, *la, U)
 
 
 def elastic_gradient(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None):
     """simkit ``elastic_gradient`` (elastic.py:596-629)."""
-    return globals()[_material(material) + "_gradient"](X, T, mu, lam, U)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_gradient"](X, T, mu, *la, U)
 
 
 def elastic_hessian(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None, psd: bool = True):
     """simkit ``elastic_hessian`` (elastic.py:849-882)."""
-    return globals()[_material(material) + "_hessian"](X, T, mu, lam, U, psd=psd)
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_hessian"](X, T, mu, *la, U, psd=psd)
 
 
 # --------------------------------------------------------------------------- #

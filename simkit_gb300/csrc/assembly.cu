@@ -179,6 +179,9 @@ __global__ void k_assemble(AsmArgs<R> a) {
 // --------------------------------------------------------- FP64 forces ---
 // f_a = vol P(F) grad N_a per tet, in FP64 (the Newton residual is formed
 // from these; FP32 cannot resolve 1e-6 relative residuals of stiff beams).
+// COROT: the instantiation for ARAP / fixed-corotated meshes (its SVD would cost the
+// neo-Hookean instantiation registers and occupancy).
+template <bool COROT>
 __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp, double* __restrict__ fbuf) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= a.t) return;
@@ -188,10 +191,20 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
   load_dinv(a.dinv, a.t, e, D);
   disp_grad(du, D, G);
   const double vol = a.vol[e], mu = a.mu[e], lam = a.lam[e];
-  if (disp)
-    mat_pk1_disp<double>(a.material, G, mu, lam, P);
-  else
-    mat_pk1<double>(a.material, G, mu, lam, P);
+  const int mat = COROT ? a.material : (a.material == kMatMMNH ? kMatMMNH : kMatSNH);
+  if (COROT ? mat == kMatARAP : false) {
+    if (disp) arap_pk1_disp<double>(G, mu, P);
+    else arap_pk1<double>(G, mu, P);
+  } else if (COROT) {
+    if (disp) fcr_pk1_disp<double>(G, mu, lam, P);
+    else fcr_pk1<double>(G, mu, lam, P);
+  } else if (mat == kMatMMNH) {
+    if (disp) mmnh_pk1_disp<double>(G, mu, lam, P);
+    else mmnh_pk1<double>(G, mu, lam, P);
+  } else {
+    if (disp) snh_pk1_disp<double>(G, mu, lam, P);
+    else snh_pk1<double>(G, mu, lam, P);
+  }
   shape_grads(D, gN);
   double* f = fbuf + 12 * e;
 #pragma unroll
@@ -393,7 +406,10 @@ int launch_assemble(const AsmArgs<R>& a, cudaStream_t s) {
 
 int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t s) {
   if (a.t == 0) return SKG_OK;
-  k_tet_forces<<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, fbuf);
+  if (a.material == kMatARAP || a.material == kMatFCR)
+    k_tet_forces<true><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, fbuf);
+  else
+    k_tet_forces<false><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, fbuf);
   SKG_LAUNCHED();
   return SKG_OK;
 }
@@ -532,7 +548,7 @@ int check_mesh(const skg_tet_mesh* m, int precision) {
   if (precision == SKG_MIXED && (!m->dinv32 || !m->mat32))
     return fail(SKG_ERR_ARG, "mixed precision needs the FP32 mesh copies");
   if (precision != SKG_MIXED && precision != SKG_FP64) return fail(SKG_ERR_ARG, "unknown precision %d", precision);
-  if (m->material != SKG_MAT_STABLE_NEO_HOOKEAN && m->material != SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN)
+  if (m->material < SKG_MAT_STABLE_NEO_HOOKEAN || m->material > SKG_MAT_FIXED_COROTATED)
     return fail(SKG_ERR_ARG, "unknown material %d", m->material);
   if (m->coarse) {
     const skg_coarse* c = m->coarse;

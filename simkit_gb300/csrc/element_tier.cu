@@ -25,7 +25,8 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 }
 
 // ------------------------------------------------------------ element F --
-// MAT: kMatSNH (stable_neo_hookean.py) or kMatMMNH (macklin_mueller_neo_hookean.py)
+// MAT: kMatSNH (stable_neo_hookean.py), kMatMMNH (macklin_mueller_neo_hookean.py),
+// kMatARAP (arap.py) or kMatFCR (fcr.py)
 template <typename R, int D, int MAT>
 __global__ void k_elem_energy(const double* __restrict__ F, const double* __restrict__ mu,
                               const double* __restrict__ lam, double* __restrict__ psi, int64_t t) {
@@ -34,11 +35,7 @@ __global__ void k_elem_energy(const double* __restrict__ F, const double* __rest
   R f[D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  const R m = R(mu[e]), l = R(lam[e]);
-  R v;
-  if (MAT == kMatMMNH) v = D == 3 ? mmnh_psi<R>(f, m, l) : mmnh_psi2<R>(f, m, l);
-  else v = D == 3 ? snh_psi<R>(f, m, l) : snh_psi2<R>(f, m, l);
-  psi[e] = double(v);
+  psi[e] = double(elem_psi<R, D>(MAT, f, R(mu[e]), R(lam[e])));
 }
 
 template <typename R, int D, int MAT>
@@ -49,14 +46,7 @@ __global__ void k_elem_pk1(const double* __restrict__ F, const double* __restric
   R f[D * D], p[D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  const R m = R(mu[e]), l = R(lam[e]);
-  if (MAT == kMatMMNH) {
-    if (D == 3) mmnh_pk1<R>(f, m, l, p);
-    else mmnh_pk1_2<R>(f, m, l, p);
-  } else {
-    if (D == 3) snh_pk1<R>(f, m, l, p);
-    else snh_pk1_2<R>(f, m, l, p);
-  }
+  elem_pk1<R, D>(MAT, f, R(mu[e]), R(lam[e]), p);
 #pragma unroll
   for (int k = 0; k < D * D; ++k) P[D * D * e + k] = double(p[k]);
 }
@@ -69,14 +59,7 @@ __global__ void k_elem_hessian(const double* __restrict__ F, const double* __res
   R f[D * D], h[D * D * D * D];
 #pragma unroll
   for (int k = 0; k < D * D; ++k) f[k] = R(F[D * D * e + k]);
-  const R m = R(mu[e]), l = R(lam[e]);
-  if (MAT == kMatMMNH) {
-    if (D == 3) mmnh_hessian9<R>(f, m, l, h);
-    else mmnh_hessian4<R>(f, m, l, h);
-  } else {
-    if (D == 3) snh_hessian9<R>(f, m, l, h);
-    else snh_hessian4<R>(f, m, l, h);
-  }
+  elem_hessian<R, D>(MAT, f, R(mu[e]), R(lam[e]), h);
   for (int k = 0; k < D * D * D * D; ++k) H[(int64_t)D * D * D * D * e + k] = double(h[k]);
 }
 
@@ -272,6 +255,36 @@ int skg_mmnh_gradient_element_F(int dim, int precision, const double* F, const d
 int skg_mmnh_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                                double* H, int64_t t, void* stream) {
   return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatMMNH));
+}
+
+int skg_arap_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* psi, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, SKG_ELEM(k_elem_energy, kMatARAP));
+}
+
+int skg_arap_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                                double* P, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, P, t, stream, SKG_ELEM(k_elem_pk1, kMatARAP));
+}
+
+int skg_arap_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* H, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatARAP));
+}
+
+int skg_fcr_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                             double* psi, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, SKG_ELEM(k_elem_energy, kMatFCR));
+}
+
+int skg_fcr_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                               double* P, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, P, t, stream, SKG_ELEM(k_elem_pk1, kMatFCR));
+}
+
+int skg_fcr_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* H, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatFCR));
 }
 #undef SKG_ELEM
 

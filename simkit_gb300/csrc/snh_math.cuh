@@ -330,22 +330,7 @@ template <typename R> SK_HD void mmnh_hessian4(const R* F, R mu, R lam, R* H) {
 }
 
 // materials of the per-tet kernels
-enum : int { kMatSNH = 0, kMatMMNH = 1 };
-
-template <typename R> SK_HD R mat_dpsi(int mat, const R* G, R mu, R lam) {
-  return mat == kMatMMNH ? mmnh_dpsi(G, mu, lam) : snh_dpsi(G, mu, lam);
-}
-template <typename R> SK_HD R mat_psi(int mat, const R* F, R mu, R lam) {
-  return mat == kMatMMNH ? mmnh_psi(F, mu, lam) : snh_psi(F, mu, lam);
-}
-template <typename R> SK_HD void mat_pk1_disp(int mat, const R* G, R mu, R lam, R* P) {
-  if (mat == kMatMMNH) mmnh_pk1_disp(G, mu, lam, P);
-  else snh_pk1_disp(G, mu, lam, P);
-}
-template <typename R> SK_HD void mat_pk1(int mat, const R* F, R mu, R lam, R* P) {
-  if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
-  else snh_pk1(F, mu, lam, P);
-}
+enum : int { kMatSNH = 0, kMatMMNH = 1, kMatARAP = 2, kMatFCR = 3 };
 
 // --------------------------------------------------------------------------
 // symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations
@@ -465,6 +450,232 @@ template <typename R> SK_HD void svd3_rv(const R* F, R* U, R* s, R* V) {
 }
 
 // --------------------------------------------------------------------------
+// Corotational energies (simkit/energies/arap.py:71-145, fcr.py:40-190):
+//   ARAP: psi = mu/2 |F - R|^2,                  P = mu (F - R),
+//         H = mu (I - dR/dF)
+//   FCR:  psi = mu |F - R|^2 + lam/2 (J - 1)^2,   P = 2 mu (F - R) + lam (J - 1) cof F,
+//         H = 2 mu (I - dR/dF) + lam c c^T + lam (J - 1) d2J/dF2
+// with R = U V^T of the rotation-variant SVD and, as simkit/rotation_gradient.py
+// forms it,
+//   dR/dF = sum over the pairs (i,j) of 2 / max(s_i + s_j, 1e-8) t t^T,
+//   t = vec(U (e_i e_j^T - e_j e_i^T) V^T) / sqrt2
+// (one pair and 1e-12 in 2D).  In 2D the polar factor is closed form:
+// R = [[c, -s], [s, c]] with (c, s) the unit vector along (F00 + F11, F10 - F01),
+// s_0 + s_1 = |(F00 + F11, F10 - F01)| and t = vec(J R) / sqrt2, J the quarter turn.
+// --------------------------------------------------------------------------
+template <typename R> SK_HD void polar3(const R* F, R* Rm) {
+  R U[9], s[3], V[9];
+  svd3_rv(F, U, s, V);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Rm[3 * i + j] = U[3 * i] * V[3 * j] + U[3 * i + 1] * V[3 * j + 1] + U[3 * i + 2] * V[3 * j + 2];
+}
+template <typename R> SK_HD R corot_shear3(const R* F) {   // |F - R|^2
+  R Rm[9];
+  polar3(F, Rm);
+  R a = 0;
+  for (int k = 0; k < 9; ++k) a += (F[k] - Rm[k]) * (F[k] - Rm[k]);
+  return a;
+}
+// H -= coef dR/dF (9x9, row-major vec(F))
+template <typename R> SK_HD void corot_twist9(const R* F, R coef, R* H) {
+  R U[9], s[3], V[9];
+  svd3_rv(F, U, s, V);
+  const R rs2 = R(0.70710678118654752440);
+  const int pi[3] = {0, 1, 0}, pj[3] = {1, 2, 2};
+  for (int p = 0; p < 3; ++p) {
+    const int i = pi[p], j = pj[p];
+    const R w = coef * R(2) / sk_max(s[i] + s[j], R(1e-8));
+    R t[9];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) t[3 * a + b] = rs2 * (U[3 * a + i] * V[3 * b + j] - U[3 * a + j] * V[3 * b + i]);
+    for (int q = 0; q < 9; ++q)
+      for (int r = 0; r < 9; ++r) H[9 * q + r] -= w * t[q] * t[r];
+  }
+}
+template <typename R> SK_HD R arap_psi(const R* F, R mu) { return R(0.5) * mu * corot_shear3(F); }
+template <typename R> SK_HD R fcr_psi(const R* F, R mu, R lam) {
+  const R y = det3(F) - R(1);
+  return mu * corot_shear3(F) + R(0.5) * lam * y * y;
+}
+// Displacement forms psi(I + G), accurate relative to psi near rest.
+// |F - R|^2 = sum_k (s_k - 1)^2 with s_k^2 = 1 + l_k, l_k the eigenvalues of
+// E = F^T F - I = G + G^T + G^T G, so s_k - 1 = l_k / (sqrt(1 + l_k) + 1) has no
+// cancellation; for det F < 0 the smallest singular value is negative
+// (s - 1 = -(sqrt(1 + l) + 1)).  J - 1 = tr G + I2(G) + det G likewise.
+template <typename R> SK_HD R corot_dshear3(const R* G, R Jm1) {
+  R E[6];
+  E[0] = R(2) * G[0] + G[0] * G[0] + G[3] * G[3] + G[6] * G[6];
+  E[1] = G[1] + G[3] + G[0] * G[1] + G[3] * G[4] + G[6] * G[7];
+  E[2] = G[2] + G[6] + G[0] * G[2] + G[3] * G[5] + G[6] * G[8];
+  E[3] = R(2) * G[4] + G[1] * G[1] + G[4] * G[4] + G[7] * G[7];
+  E[4] = G[5] + G[7] + G[1] * G[2] + G[4] * G[5] + G[7] * G[8];
+  E[5] = R(2) * G[8] + G[2] * G[2] + G[5] * G[5] + G[8] * G[8];
+  R l[3], W[9];
+  sym3_eig(E, l, W);
+  const int kmin = l[0] <= l[1] ? (l[0] <= l[2] ? 0 : 2) : (l[1] <= l[2] ? 1 : 2);
+  R a = R(0);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const R r = sk_sqrt(sk_max(R(1) + l[k], R(0)));
+    const R d = (Jm1 < R(-1) && k == kmin) ? -(r + R(1)) : l[k] / (r + R(1));
+    a += d * d;
+  }
+  return a;
+}
+template <typename R> SK_HD R arap_dpsi(const R* G, R mu) {
+  const R Jm1 = G[0] + G[4] + G[8] + minors2(G) + det3(G);
+  return R(0.5) * mu * corot_dshear3(G, Jm1);
+}
+template <typename R> SK_HD R fcr_dpsi(const R* G, R mu, R lam) {
+  const R y = G[0] + G[4] + G[8] + minors2(G) + det3(G);
+  return mu * corot_dshear3(G, y) + R(0.5) * lam * y * y;
+}
+template <typename R> SK_HD void corot_pk1(const R* F, R two_mu_or_mu, R vol_coef, R* P) {
+  // P = a (F - R) + vol_coef cof F
+  R Rm[9], C[9];
+  polar3(F, Rm);
+  cof3(F, C);
+  for (int k = 0; k < 9; ++k) P[k] = two_mu_or_mu * (F[k] - Rm[k]) + vol_coef * C[k];
+}
+template <typename R> SK_HD void arap_pk1(const R* F, R mu, R* P) { corot_pk1(F, mu, R(0), P); }
+template <typename R> SK_HD void fcr_pk1(const R* F, R mu, R lam, R* P) {
+  corot_pk1(F, R(2) * mu, lam * (det3(F) - R(1)), P);
+}
+template <typename R> SK_HD void arap_pk1_disp(const R* G, R mu, R* P) {
+  R F[9];
+  for (int k = 0; k < 9; ++k) F[k] = G[k] + ((k % 4 == 0) ? R(1) : R(0));
+  corot_pk1(F, mu, R(0), P);
+}
+template <typename R> SK_HD void fcr_pk1_disp(const R* G, R mu, R lam, R* P) {
+  R F[9];
+  for (int k = 0; k < 9; ++k) F[k] = G[k] + ((k % 4 == 0) ? R(1) : R(0));
+  const R y = G[0] + G[4] + G[8] + minors2(G) + det3(G);
+  corot_pk1(F, R(2) * mu, lam * y, P);
+}
+template <typename R> SK_HD void arap_hessian9(const R* F, R mu, R* H) {
+  hessian9_coef(F, mu, R(0), R(0), R(0), H);
+  corot_twist9(F, mu, H);
+}
+template <typename R> SK_HD void fcr_hessian9(const R* F, R mu, R lam, R* H) {
+  hessian9_coef(F, R(2) * mu, R(0), lam, lam * (det3(F) - R(1)), H);
+  corot_twist9(F, R(2) * mu, H);
+}
+// 2D (row-major F = [F00, F01, F10, F11])
+template <typename R> SK_HD R polar2(const R* F, R* Rm) {   // returns s_0 + s_1
+  const R a = F[0] + F[3], b = F[2] - F[1];
+  const R n = sk_sqrt(a * a + b * b);
+  R c = R(1), sn = R(0);
+  if (n > R(0)) {
+    c = a / n;
+    sn = b / n;
+  }
+  Rm[0] = c; Rm[1] = -sn; Rm[2] = sn; Rm[3] = c;
+  return n;
+}
+template <typename R> SK_HD R corot_shear2(const R* F) {
+  R Rm[4];
+  polar2(F, Rm);
+  R a = 0;
+  for (int k = 0; k < 4; ++k) a += (F[k] - Rm[k]) * (F[k] - Rm[k]);
+  return a;
+}
+template <typename R> SK_HD R arap_psi2(const R* F, R mu) { return R(0.5) * mu * corot_shear2(F); }
+template <typename R> SK_HD R fcr_psi2(const R* F, R mu, R lam) {
+  const R y = F[0] * F[3] - F[1] * F[2] - R(1);
+  return mu * corot_shear2(F) + R(0.5) * lam * y * y;
+}
+template <typename R> SK_HD void corot_pk1_2(const R* F, R a, R vol_coef, R* P) {
+  R Rm[4];
+  polar2(F, Rm);
+  const R C[4] = {F[3], -F[2], -F[1], F[0]};
+  for (int k = 0; k < 4; ++k) P[k] = a * (F[k] - Rm[k]) + vol_coef * C[k];
+}
+template <typename R> SK_HD void arap_pk1_2(const R* F, R mu, R* P) { corot_pk1_2(F, mu, R(0), P); }
+template <typename R> SK_HD void fcr_pk1_2(const R* F, R mu, R lam, R* P) {
+  corot_pk1_2(F, R(2) * mu, lam * (F[0] * F[3] - F[1] * F[2] - R(1)), P);
+}
+template <typename R> SK_HD void corot_twist4(const R* F, R coef, R* H) {
+  R Rm[4];
+  const R n = polar2(F, Rm);
+  const R c = Rm[0], sn = Rm[2];
+  const R rs2 = R(0.70710678118654752440);
+  const R t[4] = {-rs2 * sn, -rs2 * c, rs2 * c, -rs2 * sn};
+  const R w = coef * R(2) / sk_max(n, R(1e-12));
+  for (int q = 0; q < 4; ++q)
+    for (int r = 0; r < 4; ++r) H[4 * q + r] -= w * t[q] * t[r];
+}
+template <typename R> SK_HD void arap_hessian4(const R* F, R mu, R* H) {
+  hessian4_coef(F, mu, R(0), R(0), R(0), H);
+  corot_twist4(F, mu, H);
+}
+template <typename R> SK_HD void fcr_hessian4(const R* F, R mu, R lam, R* H) {
+  hessian4_coef(F, R(2) * mu, R(0), lam, lam * (F[0] * F[3] - F[1] * F[2] - R(1)), H);
+  corot_twist4(F, R(2) * mu, H);
+}
+
+// element-tier dispatch over material and dimension (F is row-major D x D)
+template <typename R, int D> SK_HD R elem_psi(int mat, const R* F, R mu, R lam) {
+  if (D == 3) return mat == kMatMMNH ? mmnh_psi(F, mu, lam)
+                   : mat == kMatARAP ? arap_psi(F, mu)
+                   : mat == kMatFCR  ? fcr_psi(F, mu, lam) : snh_psi(F, mu, lam);
+  return mat == kMatMMNH ? mmnh_psi2(F, mu, lam)
+       : mat == kMatARAP ? arap_psi2(F, mu)
+       : mat == kMatFCR  ? fcr_psi2(F, mu, lam) : snh_psi2(F, mu, lam);
+}
+template <typename R, int D> SK_HD void elem_pk1(int mat, const R* F, R mu, R lam, R* P) {
+  if (D == 3) {
+    if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
+    else if (mat == kMatARAP) arap_pk1(F, mu, P);
+    else if (mat == kMatFCR) fcr_pk1(F, mu, lam, P);
+    else snh_pk1(F, mu, lam, P);
+  } else {
+    if (mat == kMatMMNH) mmnh_pk1_2(F, mu, lam, P);
+    else if (mat == kMatARAP) arap_pk1_2(F, mu, P);
+    else if (mat == kMatFCR) fcr_pk1_2(F, mu, lam, P);
+    else snh_pk1_2(F, mu, lam, P);
+  }
+}
+template <typename R, int D> SK_HD void elem_hessian(int mat, const R* F, R mu, R lam, R* H) {
+  if (D == 3) {
+    if (mat == kMatMMNH) mmnh_hessian9(F, mu, lam, H);
+    else if (mat == kMatARAP) arap_hessian9(F, mu, H);
+    else if (mat == kMatFCR) fcr_hessian9(F, mu, lam, H);
+    else snh_hessian9(F, mu, lam, H);
+  } else {
+    if (mat == kMatMMNH) mmnh_hessian4(F, mu, lam, H);
+    else if (mat == kMatARAP) arap_hessian4(F, mu, H);
+    else if (mat == kMatFCR) fcr_hessian4(F, mu, lam, H);
+    else snh_hessian4(F, mu, lam, H);
+  }
+}
+
+// material dispatch of the per-tet kernels (3D)
+template <typename R> SK_HD R mat_dpsi(int mat, const R* G, R mu, R lam) {
+  if (mat == kMatMMNH) return mmnh_dpsi(G, mu, lam);
+  if (mat == kMatARAP) return arap_dpsi(G, mu);
+  if (mat == kMatFCR) return fcr_dpsi(G, mu, lam);
+  return snh_dpsi(G, mu, lam);
+}
+template <typename R> SK_HD R mat_psi(int mat, const R* F, R mu, R lam) {
+  if (mat == kMatMMNH) return mmnh_psi(F, mu, lam);
+  if (mat == kMatARAP) return arap_psi(F, mu);
+  if (mat == kMatFCR) return fcr_psi(F, mu, lam);
+  return snh_psi(F, mu, lam);
+}
+template <typename R> SK_HD void mat_pk1_disp(int mat, const R* G, R mu, R lam, R* P) {
+  if (mat == kMatMMNH) mmnh_pk1_disp(G, mu, lam, P);
+  else if (mat == kMatARAP) arap_pk1_disp(G, mu, P);
+  else if (mat == kMatFCR) fcr_pk1_disp(G, mu, lam, P);
+  else snh_pk1_disp(G, mu, lam, P);
+}
+template <typename R> SK_HD void mat_pk1(int mat, const R* F, R mu, R lam, R* P) {
+  if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
+  else if (mat == kMatARAP) arap_pk1(F, mu, P);
+  else if (mat == kMatFCR) fcr_pk1(F, mu, lam, P);
+  else snh_pk1(F, mu, lam, P);
+}
+
+// --------------------------------------------------------------------------
 // Per-tet Hessian w.r.t. the 12 vertex coordinates:
 //   K = L^T psd(vol * H_F) L, L the lift dF/dx,
 // with psd() the eigenvalue floor of simkit's psd_project applied to the
@@ -494,9 +705,11 @@ SK_HD int offdiag_index(int a, int b) {  // a < b
   return a == 0 ? (b - 1) : (a == 1 ? (b + 1) : 5);
 }
 
+// Tw: coefficient of the corotational term -Tw dR/dF (0 for the neo-Hookean
+// materials); it lowers each twist eigenvalue by Tw 2 / max(s_i + s_j, 1e-8).
 template <typename R, typename RS>
 SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
-                           R* U, R* s, R* V, R* W, R* lam9) {
+                           R* U, R* s, R* V, R* W, R* lam9, R Tw = R(0)) {
   // SVD in precision RS (double for nearly inverted elements)
   RS Fs[9], Us[9], ss[3], Vs[9];
   for (int k = 0; k < 9; ++k) Fs[k] = RS(F[k]);
@@ -507,6 +720,11 @@ SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
   lam9[0] = A + D * s[2]; lam9[1] = A - D * s[2];
   lam9[2] = A + D * s[1]; lam9[3] = A - D * s[1];
   lam9[4] = A + D * s[0]; lam9[5] = A - D * s[0];
+  if (Tw != R(0)) {
+    lam9[0] -= Tw * R(2) / sk_max(s[0] + s[1], R(1e-8));
+    lam9[2] -= Tw * R(2) / sk_max(s[0] + s[2], R(1e-8));
+    lam9[4] -= Tw * R(2) / sk_max(s[1] + s[2], R(1e-8));
+  }
   // scaling block
   const R c0 = s[1] * s[2], c1 = s[0] * s[2], c2 = s[0] * s[1];
   RS S3[6];
@@ -527,7 +745,10 @@ SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
 // fallback_J: elements with det F below it run the SVD in FP64.
 // floor_v: eigenvalue floor (simkit's 1e-6); project = false skips the
 // projection (simkit's psd=False, snh.py:534).
-// material: kMatSNH or kMatMMNH (the coefficients A, B, D of the I_C / J form).
+// material: kMatSNH, kMatMMNH, kMatARAP or kMatFCR.  Every material's F-space
+// Hessian has the form A I + B f f^T + Lc c c^T + D d2J/dF2 - Tw dR/dF
+// (f = vec F, c = vec cof F); the first four terms are lifted analytically, the
+// corotational term as its three rank-1 twist directions.
 template <typename R>
 SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1),
                            bool project = true, int material = kMatSNH) {
@@ -535,11 +756,15 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
 #pragma unroll
   for (int k = 0; k < 9; ++k) IC += F[k] * F[k];
   const R J = det3(F);
-  R A, B, D;
+  R A, B, D, Lc = lam, Tw = R(0);
   if (material == kMatMMNH) {
     A = mu;
     B = R(0);
     D = lam * (J - R(1)) - mu;
+  } else if (material == kMatARAP) {
+    A = mu; B = R(0); Lc = R(0); D = R(0); Tw = mu;
+  } else if (material == kMatFCR) {
+    A = R(2) * mu; B = R(0); D = lam * (J - R(1)); Tw = R(2) * mu;
   } else {
     const R alpha = R(1) + R(3) * mu / (R(4) * lam);
     const R den = IC + R(1);
@@ -559,7 +784,7 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
       p[3 * a + i] = F[3 * i] * gN[3 * a] + F[3 * i + 1] * gN[3 * a + 1] + F[3 * i + 2] * gN[3 * a + 2];
       c[3 * a + i] = C[3 * i] * gN[3 * a] + C[3 * i + 1] * gN[3 * a + 1] + C[3 * i + 2] * gN[3 * a + 2];
     }
-  const R vA = vol * A, vB = vol * B, vL = vol * lam, vD = vol * D;
+  const R vA = vol * A, vB = vol * B, vL = vol * Lc, vD = vol * D;
 
   // analytic terms
 #pragma unroll
@@ -596,13 +821,13 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
       o[6] += w[1]; o[7] -= w[0];
     }
 
-  if (!project) return;
+  if (!project && Tw == R(0)) return;
   // eigenvalue floor
   R U[9], s[3], V[9], W[9], lam9[9];
   if (J < fallback_J)
-    snh_eigensystem<R, double>(F, mu, lam, vol, A, D, B, U, s, V, W, lam9);
+    snh_eigensystem<R, double>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
   else
-    snh_eigensystem<R, R>(F, mu, lam, vol, A, D, B, U, s, V, W, lam9);
+    snh_eigensystem<R, R>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
   const R floor_v = R(kPsdFloor);
   R beta[12];  // beta[3a + n] = v_n . gN_a
 #pragma unroll
@@ -613,8 +838,19 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
   const R rs2 = R(0.70710678118654752440);
 #pragma unroll
   for (int m = 0; m < 9; ++m) {
-    const R kappa = floor_v - vol * lam9[m];
-    if (!(kappa > R(0))) continue;
+    // Correction along eigenvector m on top of the analytic terms.  Twist
+    // directions (even m < 6) of a corotational material carry -Tw dR/dF; when
+    // the full eigenvalue falls below the floor the correction is taken from the
+    // analytic eigenvalue A + D s_k, so the floor is met without cancelling two
+    // large terms (s_i + s_j -> 0).
+    const bool floored = project && floor_v - vol * lam9[m] > R(0);
+    R kappa = floored ? floor_v - vol * lam9[m] : R(0);
+    if (Tw != R(0) && m < 6 && !(m & 1)) {
+      const int pr = m >> 1;
+      const R ssum = pr == 0 ? s[0] + s[1] : (pr == 1 ? s[0] + s[2] : s[1] + s[2]);
+      kappa = floored ? floor_v - vol * (A + D * s[2 - pr]) : -vol * Tw * R(2) / sk_max(ssum, R(1e-8));
+    }
+    if (kappa == R(0)) continue;
     R r[12];
     if (m < 6) {
       const int pr = m >> 1;

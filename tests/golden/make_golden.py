@@ -20,6 +20,8 @@ Fixtures written next to this script:
 * ``rollout_bdf2_small.npz``: 6x2x2 beam, 8 BDF2 steps from rest (the reference's BDF2 target and coefficient)
 * ``element_mmnh_3d.npz`` / ``element_mmnh_2d.npz``: Macklin-Mueller neo-Hookean element tier on the same F batches
 * ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
+* ``element_arap_{3d,2d}.npz`` / ``element_fcr_{3d,2d}.npz``: ARAP and fixed-corotated element tiers on the same F batches
+* ``rollout_arap_small.npz`` / ``rollout_fcr_small.npz``: 6x2x2 beam, 8 backward-Euler steps with those energies
 * ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
 * ``rollout_contact_small.npz``: 6x2x2 beam falling onto a floor plane (contact springs), 14 steps
 * ``cache_reference.npz``: a cache file written by simkit's compute_with_cache_check (array, scalar, 1-element array)
@@ -54,9 +56,11 @@ def _import_reference(path):
         from simkit.energies import kinetic
         from simkit.energies import macklin_mueller_neo_hookean as ref_mmnh
         from simkit.energies import contact_springs_plane as ref_contact
+        from simkit.energies import arap as ref_arap
+        from simkit.energies import fcr as ref_fcr
     return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
                 volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic,
-                mmnh=ref_mmnh, contact=ref_contact)
+                mmnh=ref_mmnh, contact=ref_contact, arap=ref_arap, fcr=ref_fcr)
 
 
 def element_cases(rng, d, t_each=32):
@@ -106,6 +110,24 @@ def make_element_mmnh(ref, d, out):
     psi = m.macklin_mueller_neo_hookean_energy_element_F(F, mu, lam)
     P = m.macklin_mueller_neo_hookean_gradient_element_F(F, mu, lam)
     He = m.macklin_mueller_neo_hookean_hessian_element_F(F, mu, lam)
+    Hp = ref["psd_project"](He * vol.reshape(-1, 1, 1))
+    np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
+
+
+def make_element_corot(ref, d, out, material):
+    """ARAP (lam stored but unused) or fixed-corotated element tier."""
+    rng = np.random.default_rng(100 + d)
+    F, mu, lam, vol = element_cases(rng, d)
+    if material == "arap":
+        a = ref["arap"]
+        psi = a.arap_energy_element_F(F, mu)
+        P = a.arap_gradient_element_F(F, mu)
+        He = a.arap_hessian_element_F(F, mu)
+    else:
+        f = ref["fcr"]
+        psi = f.fcr_energy_element_F(F, mu, lam)
+        P = f.fcr_gradient_element_F(F, mu, lam)
+        He = f.fcr_hessian_element_F(F, mu, lam)
     Hp = ref["psd_project"](He * vol.reshape(-1, 1, 1))
     np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
 
@@ -163,6 +185,18 @@ def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", materia
             stable_neo_hookean_energy_x=staticmethod(m.macklin_mueller_neo_hookean_energy_x),
             stable_neo_hookean_gradient_x=staticmethod(m.macklin_mueller_neo_hookean_gradient_x),
             stable_neo_hookean_hessian_x=staticmethod(m.macklin_mueller_neo_hookean_hessian_x)))
+    elif material == "arap":
+        a = ref["arap"]   # arap_*_x take no lam
+        s = type("ARAP", (), dict(
+            stable_neo_hookean_energy_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_energy_x(x, J, mu, vol)),
+            stable_neo_hookean_gradient_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_gradient_x(x, J, mu, vol)),
+            stable_neo_hookean_hessian_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_hessian_x(x, J, mu, vol))))
+    elif material == "fcr":
+        f = ref["fcr"]
+        s = type("FCR", (), dict(
+            stable_neo_hookean_energy_x=staticmethod(f.fcr_energy_x),
+            stable_neo_hookean_gradient_x=staticmethod(f.fcr_gradient_x),
+            stable_neo_hookean_hessian_x=staticmethod(f.fcr_hessian_x)))
     else:
         s = ref["snh"]
 
@@ -266,6 +300,16 @@ def make_rollout_mmnh_small(ref, out):
                         ym=2e5, pr=0.45, dt=1.0 / 60.0)
 
 
+def make_rollout_corot_small(ref, out, material):
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 2, 2, ym=2e5, pr=0.45)
+    us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, 8, material=material)
+    keys = sorted(us)
+    np.savez_compressed(out, steps=np.array(keys), u=np.stack([us[k] for k in keys]),
+                        energy=en, iters=it, residual=rl, dims=np.array(spec.dims),
+                        ym=2e5, pr=0.45, dt=1.0 / 60.0)
+
+
 FLOOR = (1.0e4, (0.0, -0.004, 0.0), (0.0, 1.0, 0.0))   # k (mass weighted), point, normal
 
 
@@ -302,12 +346,25 @@ def make_rollout_c1(ref, out):
                         energy=en, iters=it, residual=rl, dt=1.0 / 60.0)
 
 
+def _write_corot(ref):
+    for mat in ("arap", "fcr"):
+        make_element_corot(ref, 3, os.path.join(HERE, f"element_{mat}_3d.npz"), mat)
+        make_element_corot(ref, 2, os.path.join(HERE, f"element_{mat}_2d.npz"), mat)
+        make_rollout_corot_small(ref, os.path.join(HERE, f"rollout_{mat}_small.npz"), mat)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE", "/root/reference"))
     ap.add_argument("--skip-c1", action="store_true")
+    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot")
     a = ap.parse_args()
     ref = _import_reference(a.reference)
+    if a.only:
+        if "corot" in a.only.split(","):
+            _write_corot(ref)
+        print("fixtures written to", HERE)
+        return
     make_element(ref, 3, os.path.join(HERE, "element_3d.npz"))
     make_element(ref, 2, os.path.join(HERE, "element_2d.npz"))
     make_beam_small(ref, os.path.join(HERE, "beam_small.npz"))
@@ -319,6 +376,7 @@ def main():
     make_contact_plane(ref, os.path.join(HERE, "contact_plane.npz"))
     make_rollout_contact_small(ref, os.path.join(HERE, "rollout_contact_small.npz"))
     make_cache_file(a.reference, os.path.join(HERE, "cache_reference.npz"))
+    _write_corot(ref)
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)

@@ -46,21 +46,36 @@ static void disp_batch(int64_t t, const double* G, const double* mu, const doubl
   }
 }
 
-// Macklin-Mueller neo-Hookean: direct and displacement forms, Hessian
+// any material: direct and displacement forms (3D), Hessian
 template <typename R>
-static void mm_batch(int64_t t, const double* F, const double* G, const double* mu, const double* lam, double* psi,
-                     double* dpsi, double* P, double* Pd, double* H) {
+static void mat_batch(int mat, int64_t t, const double* F, const double* G, const double* mu, const double* lam,
+                      double* psi, double* dpsi, double* P, double* Pd, double* H) {
   for (int64_t e = 0; e < t; ++e) {
     R f[9], g[9], p[9], h[81];
     for (int k = 0; k < 9; ++k) { f[k] = R(F[9 * e + k]); g[k] = R(G[9 * e + k]); }
-    psi[e] = double(mat_psi<R>(kMatMMNH, f, R(mu[e]), R(lam[e])));
-    dpsi[e] = double(mat_dpsi<R>(kMatMMNH, g, R(mu[e]), R(lam[e])));
-    mat_pk1<R>(kMatMMNH, f, R(mu[e]), R(lam[e]), p);
+    psi[e] = double(mat_psi<R>(mat, f, R(mu[e]), R(lam[e])));
+    dpsi[e] = double(mat_dpsi<R>(mat, g, R(mu[e]), R(lam[e])));
+    mat_pk1<R>(mat, f, R(mu[e]), R(lam[e]), p);
     for (int k = 0; k < 9; ++k) P[9 * e + k] = double(p[k]);
-    mat_pk1_disp<R>(kMatMMNH, g, R(mu[e]), R(lam[e]), p);
+    mat_pk1_disp<R>(mat, g, R(mu[e]), R(lam[e]), p);
     for (int k = 0; k < 9; ++k) Pd[9 * e + k] = double(p[k]);
-    mmnh_hessian9<R>(f, R(mu[e]), R(lam[e]), h);
+    elem_hessian<R, 3>(mat, f, R(mu[e]), R(lam[e]), h);
     for (int k = 0; k < 81; ++k) H[81 * e + k] = double(h[k]);
+  }
+}
+
+// any material, 2D element tier
+template <typename R>
+static void mat_batch2(int mat, int64_t t, const double* F, const double* mu, const double* lam, double* psi,
+                       double* P, double* H) {
+  for (int64_t e = 0; e < t; ++e) {
+    R f[4], p[4], h[16];
+    for (int k = 0; k < 4; ++k) f[k] = R(F[4 * e + k]);
+    psi[e] = double(elem_psi<R, 2>(mat, f, R(mu[e]), R(lam[e])));
+    elem_pk1<R, 2>(mat, f, R(mu[e]), R(lam[e]), p);
+    for (int k = 0; k < 4; ++k) P[4 * e + k] = double(p[k]);
+    elem_hessian<R, 2>(mat, f, R(mu[e]), R(lam[e]), h);
+    for (int k = 0; k < 16; ++k) H[16 * e + k] = double(h[k]);
   }
 }
 
@@ -97,8 +112,18 @@ void h_tet_hessian_mat(int prec, int mat, int64_t t, const double* F, const doub
 }
 void h_mm(int prec, int64_t t, const double* F, const double* G, const double* mu, const double* lam, double* psi,
           double* dpsi, double* P, double* Pd, double* H) {
-  if (prec == 64) mm_batch<double>(t, F, G, mu, lam, psi, dpsi, P, Pd, H);
-  else mm_batch<float>(t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+  if (prec == 64) mat_batch<double>(kMatMMNH, t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+  else mat_batch<float>(kMatMMNH, t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+}
+void h_mat(int prec, int mat, int64_t t, const double* F, const double* G, const double* mu, const double* lam,
+           double* psi, double* dpsi, double* P, double* Pd, double* H) {
+  if (prec == 64) mat_batch<double>(mat, t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+  else mat_batch<float>(mat, t, F, G, mu, lam, psi, dpsi, P, Pd, H);
+}
+void h_mat2(int prec, int mat, int64_t t, const double* F, const double* mu, const double* lam, double* psi,
+            double* P, double* H) {
+  if (prec == 64) mat_batch2<double>(mat, t, F, mu, lam, psi, P, H);
+  else mat_batch2<float>(mat, t, F, mu, lam, psi, P, H);
 }
 void h_svd(int prec, int64_t t, const double* F, double* U, double* s, double* V) {
   if (prec == 64) svd_batch<double>(t, F, U, s, V);

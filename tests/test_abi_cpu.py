@@ -222,6 +222,81 @@ def test_mmnh_element_math_matches_oracle(hostmath):
     assert np.max(np.abs(P32 - Pd).max(1) / np.abs(Pd).max(1)) < 2e-5
 
 
+@pytest.mark.parametrize("mat,name", [(2, "arap"), (3, "fcr")])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-12), (32, 3e-6)])
+def test_corot_tet_hessian_analytic_psd_matches_eigh_floor(hostmath, mat, name, prec, tol):
+    """ARAP / fixed-corotated per-tet Hessian: the analytic terms plus the three rank-1 twist
+    terms of dR/dF, with the eigenvalue floor on the twist eigenvalues, == eigh floor of the
+    oracle's vol * He (including inverted elements), lifted to 12 x 12."""
+    from oracle import corot
+    rng = np.random.default_rng(25 + mat)
+    F, mu, lam, vol, gN = _cases(rng)
+    t = F.shape[0]
+    out = np.zeros((t, 78))
+    hostmath.h_tet_hessian_mat(prec, mat, ctypes.c_int64(t), _p(F), _p(mu), _p(lam), _p(vol), _p(gN), _p(out),
+                               ctypes.c_double(0.1))
+    K = _unpack78(out)
+    He = corot.arap_hessian_element_F(F, mu) if name == "arap" else corot.fcr_hessian_element_F(F, mu, lam)
+    H9p = psd.psd_project(He * vol[:, None, None])
+    Ko = np.einsum("taj,tbl,tijkl->taibk", gN, gN, H9p.reshape(t, 3, 3, 3, 3)).reshape(t, 12, 12)
+    err = np.abs(K - Ko).max(axis=(1, 2)) / np.abs(Ko).max(axis=(1, 2))
+    assert err.max() < tol
+
+
+@pytest.mark.parametrize("mat,name", [(2, "arap"), (3, "fcr")])
+def test_corot_element_math_matches_oracle(hostmath, mat, name):
+    """Direct and displacement forms of the ARAP / fixed-corotated energy and stress, the
+    F-Hessian, and the 2D element tier; the FP32 displacement-form energy keeps relative
+    accuracy from rest (|G| = 1e-5) to inverted elements."""
+    from oracle import corot
+    rng = np.random.default_rng(30 + mat)
+    t = 400
+    G = np.concatenate([1e-5 * rng.standard_normal((t // 4, 3, 3)), 1e-3 * rng.standard_normal((t // 4, 3, 3)),
+                        0.2 * rng.standard_normal((t // 4, 3, 3)), 0.3 * rng.standard_normal((t // 4, 3, 3))])
+    G[3 * t // 4:, :, 0] -= 2.0 * (np.eye(3)[None] + G[3 * t // 4:])[:, :, 0]   # inverted: F[:, :, 0] negated
+    G = np.ascontiguousarray(G)
+    F = np.ascontiguousarray(np.eye(3)[None] + G)
+    assert (np.linalg.det(F[3 * t // 4:]) < 0).mean() > 0.9
+    mu = rng.uniform(3e4, 3e6, t)
+    lam = mu * rng.uniform(1.5, 40, t)
+    res = {}
+    for prec in (64, 32):
+        r = np.zeros(t), np.zeros(t), np.zeros((t, 9)), np.zeros((t, 9)), np.zeros((t, 81))
+        hostmath.h_mat(prec, mat, ctypes.c_int64(t), _p(F), _p(G), _p(mu), _p(lam), *map(_p, r))
+        res[prec] = r
+    psi, dpsi, P, Pd, H = res[64]
+    if name == "arap":
+        po, Po, Ho = (corot.arap_energy_element_F(F, mu).ravel(), corot.arap_gradient_element_F(F, mu).reshape(t, 9),
+                      corot.arap_hessian_element_F(F, mu).reshape(t, 81))
+    else:
+        po, Po, Ho = (corot.fcr_energy_element_F(F, mu, lam).ravel(),
+                      corot.fcr_gradient_element_F(F, mu, lam).reshape(t, 9),
+                      corot.fcr_hessian_element_F(F, mu, lam).reshape(t, 81))
+    scale = mu + lam
+    assert np.all(np.abs(psi - po) <= 1e-12 * scale)
+    # the oracle's |F - R|^2 from absolute F carries ~1e-16 absolute error: near rest the
+    # displacement form is the more accurate of the two
+    assert np.all(np.abs(dpsi - po) <= 1e-9 * np.abs(po) + 1e-14 * scale)
+    assert np.all(np.abs(P - Po).max(1) <= 1e-12 * scale)
+    assert np.all(np.abs(Pd - Po).max(1) <= 1e-9 * np.abs(Po).max(1) + 1e-14 * scale)
+    assert np.all(np.abs(H - Ho).max(1) <= 1e-11 * scale)
+    d32 = res[32][1]
+    assert np.max(np.abs(d32 - dpsi) / np.abs(dpsi)) < 1e-5
+    # 2D element tier
+    F2 = np.ascontiguousarray(np.eye(2)[None] + 0.4 * rng.standard_normal((t, 2, 2)))
+    psi2, P2, H2 = np.zeros(t), np.zeros((t, 4)), np.zeros((t, 16))
+    hostmath.h_mat2(64, mat, ctypes.c_int64(t), _p(F2), _p(mu), _p(lam), _p(psi2), _p(P2), _p(H2))
+    if name == "arap":
+        po, Po, Ho = corot.arap_energy_element_F(F2, mu), corot.arap_gradient_element_F(F2, mu), \
+            corot.arap_hessian_element_F(F2, mu)
+    else:
+        po, Po, Ho = corot.fcr_energy_element_F(F2, mu, lam), corot.fcr_gradient_element_F(F2, mu, lam), \
+            corot.fcr_hessian_element_F(F2, mu, lam)
+    assert np.all(np.abs(psi2 - po.ravel()) <= 1e-12 * scale)
+    assert np.all(np.abs(P2 - Po.reshape(t, 4)).max(1) <= 1e-12 * scale)
+    assert np.all(np.abs(H2 - Ho.reshape(t, 16)).max(1) <= 1e-11 * scale)
+
+
 def test_displacement_forms_match_oracle(hostmath):
     rng = np.random.default_rng(6)
     t = 200

@@ -252,7 +252,7 @@ def test_mmnh_assembled_tier_matches_oracle(api):
     e2 = api.stable_neo_hookean_energy_x(x, dJ, spec.mu, spec.lam, vol)
     assert abs(e2 - osnh.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-10 * abs(e2)
     with pytest.raises(NotImplementedError):
-        api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "arap")
+        api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "linear-elasticity")
     with pytest.raises(ValueError):
         api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "rubber")
 
@@ -274,6 +274,108 @@ def test_mmnh_be_step_matches_reference_rollout(api, precision):
         assert info.converged, info
         k = list(d["steps"]).index(step)
         assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+
+
+def _corot_entry(api, material, kind):
+    pre = "arap" if material == "arap" else "fcr"
+    return getattr(api, f"{pre}_{kind}")
+
+
+@pytest.mark.parametrize("material", ["arap", "fcr"])
+@pytest.mark.parametrize("d", [3, 2])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5)])
+def test_corot_element_tier_matches_reference(api, material, d, precision, tol):
+    """ARAP / fixed-corotated element tier on the device against reference-generated values
+    (arap.py:71-145, fcr.py:41-302), through the drop-in names and the elastic dispatch."""
+    from oracle import corot
+    g = _load(f"element_{material}_{d}d.npz")
+    F, mu, lam = g["F"], g["mu"], g["lam"]
+    la = () if material == "arap" else (lam,)
+    psi = _corot_entry(api, material, "energy_element_F")(F, mu, *la, precision=precision)
+    P = _corot_entry(api, material, "gradient_element_F")(F, mu, *la, precision=precision)
+    H = _corot_entry(api, material, "hessian_element_F")(F, mu, *la, precision=precision)
+    t = len(mu)
+    scale = (mu + lam).reshape(-1)
+    assert np.all(np.abs(psi - g["psi"]).reshape(t, -1).max(1) <= tol * scale * 10)
+    assert np.all(np.abs(P - g["P"]).reshape(t, -1).max(1) <= tol * scale * 10)
+    # dR/dF carries 2 / (s_i + s_j): where a pair sum of the signed singular values is near 0
+    # (inverted elements) FP32 keeps only eps / |s_i + s_j| of it
+    _, sv, _ = corot.svd_rv(F)
+    pair = np.min(np.abs(sv[:, :, None] + sv[:, None, :]) + 1e30 * np.eye(d)[None], axis=(1, 2))
+    ok = pair > (0.0 if precision == "fp64" else 0.05)
+    assert ok.sum() > 0.8 * t
+    assert np.all((np.abs(H - g["He"]).reshape(t, -1).max(1) <= tol * scale * 10)[ok])
+    via = api.elastic_hessian_element_F(F, mu, lam, material, psd=False)
+    assert _rel(via, g["He"]) < 1e-11
+    via_e = api.elastic_energy_element_F(F, mu, lam, material)
+    assert _rel(via_e, g["psi"]) < 1e-12
+    proj = api.elastic_hessian_element_F(F, mu, lam, material, psd=True)
+    assert _rel(proj, np.asarray(api.psd_project(g["He"]))) < 1e-10
+
+
+@pytest.mark.parametrize("material", ["arap", "fcr"])
+def test_corot_assembled_tier_matches_oracle(api, material):
+    """energy_x / gradient_x / hessian_x (psd and not) of the corotational materials on a jittered
+    beam against the oracle (arap.py:242-325, fcr.py:308-397)."""
+    from oracle import corot, fem
+    from simkit_gb300.beams import make_beam
+    rng = np.random.default_rng(9)
+    spec = make_beam(4, 3, 2, ym=np.exp(rng.uniform(np.log(1e5), np.log(1e7), 6 * 24)), pr=0.42, jitter=0.1)
+    X, T = spec.X, spec.T
+    J = fem.deformation_jacobian(X, T)
+    vol = fem.tet_volumes(X, T)
+    x = X + 0.003 * rng.standard_normal(X.shape)
+    dJ = api.deformation_jacobian(X, T)
+    o = getattr(corot, material)
+    la = () if material == "arap" else (spec.lam,)
+    e = _corot_entry(api, material, "energy_x")(x, dJ, spec.mu, *la, vol)
+    assert abs(e - o.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-10 * abs(e)
+    assert abs(api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, material) - e) < 1e-12 * abs(e)
+    g = _corot_entry(api, material, "gradient_x")(x, dJ, spec.mu, *la, vol)
+    assert _rel(g, o.gradient_x(x, J, spec.mu, spec.lam, vol)) < 1e-10
+    for psd in (True, False):
+        K = _corot_entry(api, material, "hessian_x")(x, dJ, spec.mu, *la, vol, psd=psd)
+        Ko = o.hessian_x(x, J, spec.mu, spec.lam, vol, psd=psd)
+        assert abs(K - Ko).max() < 1e-9 * abs(Ko).max(), psd
+    # the X, T entry points build J and vol themselves
+    e2 = _corot_entry(api, material, "energy")(X, T, spec.mu, *la, U=x)
+    assert abs(e2 - e) < 1e-10 * abs(e)
+
+
+@pytest.mark.parametrize("material", ["arap", "fcr"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_corot_be_step_matches_reference_rollout(api, material, precision):
+    """Backward Euler with the ARAP / fixed-corotated energy against the reference's rollout."""
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    d = _load(f"rollout_{material}_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    kw = dict(pcg_rtol=1e-10) if precision == "fp64" else {}
+    s = BESolver.from_spec(spec, dt=float(d["dt"]), precision=precision, material=material, **kw)
+    X = spec.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, info
+        k = list(d["steps"]).index(step)
+        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+
+
+def test_corot_batched_equals_single(api):
+    """A batch of fixed-corotated beams steps like the single-instance solver."""
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    specs = [make_beam(6, 2, 2, ym=2e5 * (1 + 0.3 * i), pr=0.45) for i in range(3)]
+    b = BatchedBESolver(specs, dt=1.0 / 60.0, material="fcr", coarse=None)
+    singles = [BESolver.from_spec(sp, dt=1.0 / 60.0, material="fcr", coarse=None) for sp in specs]
+    for _ in range(4):
+        b.step()
+        for s in singles:
+            assert s.step().converged
+    for i, s in enumerate(singles):
+        X = specs[i].X.reshape(-1)
+        assert _rel(X + b.displacement(i), X + s.displacement()) < 1e-6
 
 
 @pytest.mark.parametrize("tag", ["m", "i"])

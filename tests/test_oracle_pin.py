@@ -128,6 +128,41 @@ def test_rollout_mmnh_small_matches_reference():
     assert [i.iters for i in infos] == list(d["iters"])
 
 
+@pytest.mark.parametrize("material", ["arap", "fcr"])
+@pytest.mark.parametrize("d", [3, 2])
+def test_corot_element_tier_matches_reference(material, d):
+    """ARAP (arap.py:71-145) and fixed-corotated (fcr.py:41-302) element tiers against
+    reference-generated values, including inverted and nearly collapsed elements (where
+    the rotation-variant SVD flips a singular pair)."""
+    from oracle import corot
+    from oracle.psd import psd_project
+    g = _load(f"element_{material}_{d}d.npz")
+    if material == "arap":
+        psi = corot.arap_energy_element_F(g["F"], g["mu"])
+        P = corot.arap_gradient_element_F(g["F"], g["mu"])
+        He = corot.arap_hessian_element_F(g["F"], g["mu"])
+    else:
+        psi = corot.fcr_energy_element_F(g["F"], g["mu"], g["lam"])
+        P = corot.fcr_gradient_element_F(g["F"], g["mu"], g["lam"])
+        He = corot.fcr_hessian_element_F(g["F"], g["mu"], g["lam"])
+    assert _rel(psi, g["psi"]) < 1e-12
+    assert _rel(P, g["P"]) < 1e-12
+    assert _rel(He, g["He"]) < 1e-11
+    assert _rel(psd_project(He * g["vol"].reshape(-1, 1, 1)), g["He_proj"]) < 1e-9
+
+
+@pytest.mark.parametrize("material", ["arap", "fcr"])
+def test_rollout_corot_small_matches_reference(material):
+    d = _load(f"rollout_{material}_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    spec = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    r = rollout.from_spec(spec, dt=float(d["dt"]), material=material)
+    xs, infos = r.rollout(int(d["steps"].max()))
+    for k, s in enumerate(d["steps"]):
+        assert _rel(xs[s] - r.x_rest.ravel(), d["u"][k]) < 1e-8, s
+    assert [i.iters for i in infos] == list(d["iters"])
+
+
 @pytest.mark.parametrize("tag", ["m", "i"])
 def test_contact_plane_matches_reference(tag):
     """Contact springs (contact_springs_plane.py:44-200) with vertex weights (M) and without."""
