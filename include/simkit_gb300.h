@@ -257,6 +257,18 @@ int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, voi
 int skg_snh_hessian_x(const skg_tet_mesh* mesh, const double* x, int precision, int psd, double* val64,
                       float* val32, void* workspace, void* stream);
 
+/* The displacement (_u) tier: F_e = (J u)_e + Jx_bar_e, where Jx_bar (9 t f64, row 9e + 3i + j =
+ * F_ij, the layout of J's rows) is the caller's precomputed J x_bar for an arbitrary reference
+ * x_bar.  Same outputs and workspace as the _x calls.  Replace stable_neo_hookean_energy_u
+ * (snh.py:544-576), _gradient_u (:579-611) and _hessian_u (:614-648); with mesh->material they
+ * also replace the _u functions of macklin_mueller_neo_hookean.py, arap.py and fcr.py. */
+int skg_snh_energy_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, double* energy_h,
+                     void* workspace, void* stream);
+int skg_snh_gradient_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, double* g,
+                       void* workspace, void* stream);
+int skg_snh_hessian_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, int precision, int psd,
+                      double* val64, float* val32, void* workspace, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* Newton / backward Euler: solvers/newton.py:7-75, integrators/backward_euler.py:27-91 */
 /* ---------------------------------------------------------------------- */

@@ -24,7 +24,11 @@ _API = {
     "arap_hessian_element_F", "arap_energy_x", "arap_gradient_x", "arap_hessian_x", "arap_energy",
     "arap_gradient", "arap_hessian", "fcr_energy_element_F", "fcr_gradient_element_F",
     "fcr_hessian_element_F", "fcr_energy_x", "fcr_gradient_x", "fcr_hessian_x", "fcr_energy",
-    "fcr_gradient", "fcr_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
+    "fcr_gradient", "fcr_hessian", "stable_neo_hookean_energy_u", "stable_neo_hookean_gradient_u",
+    "stable_neo_hookean_hessian_u", "macklin_mueller_neo_hookean_energy_u", "macklin_mueller_neo_hookean_gradient_u",
+    "macklin_mueller_neo_hookean_hessian_u", "arap_energy_u", "arap_gradient_u", "arap_hessian_u", "fcr_energy_u",
+    "fcr_gradient_u", "fcr_hessian_u", "elastic_energy_u", "elastic_gradient_u", "elastic_hessian_u",
+    "elastic_energy_element_F", "elastic_gradient_element_F",
     "elastic_hessian_element_F", "elastic_energy_x", "elastic_gradient_x", "elastic_hessian_x",
     "elastic_energy", "elastic_gradient", "elastic_hessian", "contact_springs_plane_energy",
     "contact_springs_plane_gradient", "contact_springs_plane_hessian",

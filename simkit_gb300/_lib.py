@@ -120,6 +120,9 @@ _SIGNATURES = {
     "skg_snh_energy_x": (c_i32, [P(TetMeshC), c_vp, P(c_dbl), c_vp, c_vp]),
     "skg_snh_gradient_x": (c_i32, [P(TetMeshC), c_vp, c_vp, c_vp, c_vp]),
     "skg_snh_hessian_x": (c_i32, [P(TetMeshC), c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "skg_snh_energy_u": (c_i32, [P(TetMeshC), c_vp, c_vp, P(c_dbl), c_vp, c_vp]),
+    "skg_snh_gradient_u": (c_i32, [P(TetMeshC), c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "skg_snh_hessian_u": (c_i32, [P(TetMeshC), c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "skg_be_workspace_size": (c_i64, [P(TetMeshC), c_i32]),
     "skg_be_step": (c_i32, [P(TetMeshC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC), c_vp]),
     "skg_batch_workspace_size": (c_i64, [P(TetMeshC), P(BatchC), c_i32]),

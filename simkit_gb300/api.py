@@ -365,6 +365,81 @@ def _hessian_x(X, J, mu, lam, vol, material, psd, precision):
     return B if isinstance(X, torch.Tensor) else B.to_scipy()
 
 
+# displacement tier: F = J u + Jx_bar (simkit's *_u functions)
+def _jx_bar(Jx_bar, m: TetMesh):
+    f = _dev(Jx_bar).reshape(-1)
+    if f.numel() != 9 * m.t:
+        raise ValueError(f"Jx_bar needs 9 values per tet ({9 * m.t}), got {f.numel()}")
+    return f
+
+
+def _energy_u(u, J, Jx_bar, mu, lam, vol, material) -> float:
+    m = _bind(J, mu, lam, vol, material)
+    ud = _dev(u).reshape(-1)
+    f = _jx_bar(Jx_bar, m)
+    ws = m.workspace(SKG_FP64)
+    e = ctypes.c_double()
+    check(_lib.load().skg_snh_energy_u(ctypes.byref(m.c), _ptr(ud), _ptr(f), ctypes.byref(e), _ptr(ws),
+                                       _stream_ptr()))
+    return float(e.value)
+
+
+def _gradient_u(u, J, Jx_bar, mu, lam, vol, material):
+    m = _bind(J, mu, lam, vol, material)
+    ud = _dev(u).reshape(-1)
+    f = _jx_bar(Jx_bar, m)
+    ws = m.workspace(SKG_FP64)
+    g = torch.empty(3 * m.n, dtype=torch.float64, device="cuda")
+    check(_lib.load().skg_snh_gradient_u(ctypes.byref(m.c), _ptr(ud), _ptr(f), _ptr(g), _ptr(ws), _stream_ptr()))
+    return _out(g.reshape(-1, 1), u)
+
+
+def _hessian_u(u, J, Jx_bar, mu, lam, vol, material, psd, precision):
+    m = _bind(J, mu, lam, vol, material)
+    ud = _dev(u).reshape(-1)
+    f = _jx_bar(Jx_bar, m)
+    prec = _PREC[precision]
+    ws = m.workspace(prec)
+    dt = torch.float64 if prec == SKG_FP64 else torch.float32
+    val = torch.empty(9 * m.nb, dtype=dt, device="cuda")
+    v64, v32 = (val, None) if prec == SKG_FP64 else (None, val)
+    check(_lib.load().skg_snh_hessian_u(ctypes.byref(m.c), _ptr(ud), _ptr(f), prec, int(psd), _ptr(v64), _ptr(v32),
+                                        _ptr(ws), _stream_ptr()))
+    B = BlockMatrix(m, val)
+    return B if isinstance(u, torch.Tensor) else B.to_scipy()
+
+
+def stable_neo_hookean_energy_u(u, J, Jx_bar, mu, lam, vol) -> float:
+    """sum vol psi(J u + Jx_bar).  simkit ``stable_neo_hookean_energy_u`` (snh.py:544-576)."""
+    return _energy_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["stable-neo-hookean"])
+
+
+def stable_neo_hookean_gradient_u(u, J, Jx_bar, mu, lam, vol):
+    """J^T vec(vol P(J u + Jx_bar)), (3n, 1).  simkit ``stable_neo_hookean_gradient_u`` (snh.py:579-611)."""
+    return _gradient_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["stable-neo-hookean"])
+
+
+def stable_neo_hookean_hessian_u(u, J, Jx_bar, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(psd(vol He)) J at F = J u + Jx_bar.  simkit ``stable_neo_hookean_hessian_u``
+    (snh.py:614-648)."""
+    return _hessian_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["stable-neo-hookean"], psd, precision)
+
+
+def macklin_mueller_neo_hookean_energy_u(u, J, Jx_bar, mu, lam, vol) -> float:
+    """simkit ``macklin_mueller_neo_hookean_energy_u`` (:579-611)."""
+    return _energy_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"])
+
+
+def macklin_mueller_neo_hookean_gradient_u(u, J, Jx_bar, mu, lam, vol):
+    """simkit ``macklin_mueller_neo_hookean_gradient_u`` (:614-646)."""
+    return _gradient_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"])
+
+
+def macklin_mueller_neo_hookean_hessian_u(u, J, Jx_bar, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """simkit ``macklin_mueller_neo_hookean_hessian_u`` (:649-683)."""
+    return _hessian_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["macklin-mueller-neo-hookean"], psd, precision)
+
+
 def _no_lam(mu):
     """ARAP has no volume term; the kernels take a lam array and ignore it."""
     return mu
@@ -415,6 +490,21 @@ def arap_hessian(X, T, mu, U: Optional[np.ndarray] = None, psd: bool = True):
     return arap_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, volume(X, T), psd=psd)
 
 
+def arap_energy_u(u, J, Jx_bar, mu, vol) -> float:
+    """simkit ``arap_energy_u`` (arap.py:331-360)."""
+    return _energy_u(u, J, Jx_bar, mu, _no_lam(mu), vol, MATERIALS["arap"])
+
+
+def arap_gradient_u(u, J, Jx_bar, mu, vol):
+    """simkit ``arap_gradient_u`` (arap.py:363-389)."""
+    return _gradient_u(u, J, Jx_bar, mu, _no_lam(mu), vol, MATERIALS["arap"])
+
+
+def arap_hessian_u(u, J, Jx_bar, mu, vol, psd: bool = True, precision: str = "fp64"):
+    """simkit ``arap_hessian_u`` (arap.py:392-424)."""
+    return _hessian_u(u, J, Jx_bar, mu, _no_lam(mu), vol, MATERIALS["arap"], psd, precision)
+
+
 def fcr_energy_element_F(F, mu, lam, precision: str = "fp64"):
     """psi = mu |F - R|^2 + lam/2 (J - 1)^2 per element, (t, 1).  simkit ``fcr_energy_element_F`` (fcr.py:41-62)."""
     return _elem("skg_fcr_energy_element_F", F, mu, lam, lambda t, d: (t, 1), precision, "FCR")
@@ -443,6 +533,21 @@ def fcr_gradient_x(X, J, mu, lam, vol):
 def fcr_hessian_x(X, J, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
     """J^T blockdiag(psd(vol He)) J.  simkit ``fcr_hessian_x`` (fcr.py:365-397)."""
     return _hessian_x(X, J, mu, lam, vol, MATERIALS["fcr"], psd, precision)
+
+
+def fcr_energy_u(u, J, Jx_bar, mu, lam, vol) -> float:
+    """simkit ``fcr_energy_u`` (fcr.py:403-434)."""
+    return _energy_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["fcr"])
+
+
+def fcr_gradient_u(u, J, Jx_bar, mu, lam, vol):
+    """simkit ``fcr_gradient_u`` (fcr.py:437-465)."""
+    return _gradient_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["fcr"])
+
+
+def fcr_hessian_u(u, J, Jx_bar, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """simkit ``fcr_hessian_u`` (fcr.py:468-502)."""
+    return _hessian_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["fcr"], psd, precision)
 
 
 def fcr_energy(X, T, mu, lam, U: Optional[np.ndarray] = None) -> float:
@@ -573,6 +678,24 @@ def elastic_hessian_x(X, J, mu, lam, vol, material: str, psd: bool = True):
     """simkit ``elastic_hessian_x`` (elastic.py:671-705)."""
     pre, la = _material(material, (lam,))
     return globals()[pre + "_hessian_x"](X, J, mu, *la, vol, psd=psd)
+
+
+def elastic_energy_u(u, J, Jx_bar, mu, lam, vol, material: str) -> float:
+    """simkit ``elastic_energy_u`` (elastic.py:151-188)."""
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_energy_u"](u, J, Jx_bar, mu, *la, vol)
+
+
+def elastic_gradient_u(u, J, Jx_bar, mu, lam, vol, material: str):
+    """simkit ``elastic_gradient_u`` (elastic.py:462-497)."""
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_gradient_u"](u, J, Jx_bar, mu, *la, vol)
+
+
+def elastic_hessian_u(u, J, Jx_bar, mu, lam, vol, material: str, psd: bool = True):
+    """simkit ``elastic_hessian_u`` (elastic.py:708-746)."""
+    pre, la = _material(material, (lam,))
+    return globals()[pre + "_hessian_u"](u, J, Jx_bar, mu, *la, vol, psd=psd)
 
 
 def elastic_energy(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None) -> float:

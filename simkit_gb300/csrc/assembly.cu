@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(128) k_tet_hessian(TetArgs<R> a, int disp, int
     G[4] += R(1);
     G[8] += R(1);
   }
+  add_fbar(a, e, G);
   shape_grads(D, gN);
   const R vol = __ldg(a.vol + e), mu = __ldg(a.mu + e), lam = __ldg(a.lam + e);
   snh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
@@ -190,6 +191,7 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
   tet_du(a.u, v, du);
   load_dinv(a.dinv, a.t, e, D);
   disp_grad(du, D, G);
+  add_fbar(a, e, G);
   const double vol = a.vol[e], mu = a.mu[e], lam = a.lam[e];
   const int mat = COROT ? a.material : (a.material == kMatMMNH ? kMatMMNH : kMatSNH);
   if (COROT ? mat == kMatARAP : false) {
@@ -277,6 +279,7 @@ __device__ __forceinline__ double tet_energy_term(const EnergyArgs<R>& a, int64_
   }
   load_dinv(a.tet.dinv, a.tet.t, e, D);
   disp_grad(du, D, G);
+  if (DIRECT) add_fbar(a.tet, e, G);
   const R vol = __ldg(a.tet.vol + e), mu = __ldg(a.tet.mu + e), lam = __ldg(a.tet.lam + e);
   if (DIRECT) return double(vol) * double(mat_psi<R>(a.tet.material, G, mu, lam));
   return double(vol * mat_dpsi<R>(a.tet.material, G, mu, lam));
@@ -591,14 +594,20 @@ int skg_contact_plane_terms(const double* x, int64_t n, const skg_contact_plane*
   return SKG_OK;
 }
 
-int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h, void* ws, void* stream) {
+}  // extern "C"
+
+// The _x tier (fbar = null: x are positions) and the _u tier (x are displacements u,
+// F = J u + fbar) share these bodies.
+static int energy_xu(const skg_tet_mesh* mesh, const double* x, const double* fbar, double* energy_h, void* ws,
+                     void* stream) {
   SKG_TRY(check_mesh(mesh, SKG_FP64));
-  if (!x || !ws || !energy_h) return fail(SKG_ERR_ARG, "energy_x: null pointer");
+  if (!x || !ws || !energy_h) return fail(SKG_ERR_ARG, "energy: null pointer");
   cudaStream_t s = as_stream(stream);
   Workspace w = carve_workspace(mesh, SKG_FP64, ws);
   SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
   EnergyArgs<double> a{};
   a.tet = tet_args64(mesh, x);
+  a.tet.fbar = fbar;
   a.n = mesh->n_verts;
   a.partials = w.partials;
   a.counter = w.counter;
@@ -609,13 +618,16 @@ int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h
   return SKG_OK;
 }
 
-int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, void* ws, void* stream) {
+static int gradient_xu(const skg_tet_mesh* mesh, const double* x, const double* fbar, double* g, void* ws,
+                       void* stream) {
   SKG_TRY(check_mesh(mesh, SKG_FP64));
-  if (!x || !g || !ws) return fail(SKG_ERR_ARG, "gradient_x: null pointer");
+  if (!x || !g || !ws) return fail(SKG_ERR_ARG, "gradient: null pointer");
   cudaStream_t s = as_stream(stream);
   Workspace w = carve_workspace(mesh, SKG_FP64, ws);
   SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
-  SKG_TRY(launch_forces(tet_args64(mesh, x), 0, w.fbuf, s));
+  TetArgs<double> ta = tet_args64(mesh, x);
+  ta.fbar = fbar;
+  SKG_TRY(launch_forces(ta, 0, w.fbuf, s));
   GradArgs ga{};
   ga.n = mesh->n_verts;
   ga.v2t_ptr = mesh->v2t_ptr;
@@ -628,23 +640,60 @@ int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, voi
   return launch_vertex_gradient(ga, s);
 }
 
-int skg_snh_hessian_x(const skg_tet_mesh* mesh, const double* x, int precision, int psd, double* val64,
-                      float* val32, void* ws, void* stream) {
+static int hessian_xu(const skg_tet_mesh* mesh, const double* x, const double* fbar, int precision, int psd,
+                      double* val64, float* val32, void* ws, void* stream) {
   SKG_TRY(check_mesh(mesh, precision));
-  if (!x || !ws) return fail(SKG_ERR_ARG, "hessian_x: null pointer");
+  if (!x || !ws) return fail(SKG_ERR_ARG, "hessian: null pointer");
   cudaStream_t s = as_stream(stream);
   Workspace w = carve_workspace(mesh, precision, ws);
   if (precision == SKG_FP64) {
-    if (!val64) return fail(SKG_ERR_ARG, "hessian_x: FP64 needs val64");
-    SKG_TRY(launch_tet_hessian<double>(tet_args64(mesh, x), 0, psd, w.hbuf64, s));
+    if (!val64) return fail(SKG_ERR_ARG, "hessian: FP64 needs val64");
+    TetArgs<double> ta = tet_args64(mesh, x);
+    ta.fbar = fbar;
+    SKG_TRY(launch_tet_hessian<double>(ta, 0, psd, w.hbuf64, s));
     AsmArgs<double> aa = make_asm_args<double>(mesh, w.hbuf64, val64, nullptr);
     return launch_assemble<double>(aa, s);
   }
-  if (!val32) return fail(SKG_ERR_ARG, "hessian_x: mixed precision needs val32");
+  if (!val32) return fail(SKG_ERR_ARG, "hessian: mixed precision needs val32");
   SKG_TRY(launch_split(x, mesh->n_verts, w.uh, w.ul, s));
-  SKG_TRY(launch_tet_hessian<float>(make_tet_args32(mesh, x, w.uh, w.ul), 0, psd, w.hbuf32, s));
+  TetArgs<float> ta = make_tet_args32(mesh, x, w.uh, w.ul);
+  ta.fbar = fbar;
+  SKG_TRY(launch_tet_hessian<float>(ta, 0, psd, w.hbuf32, s));
   AsmArgs<float> aa = make_asm_args<float>(mesh, w.hbuf32, val32, nullptr);
   return launch_assemble<float>(aa, s);
+}
+
+extern "C" {
+
+int skg_snh_energy_x(const skg_tet_mesh* mesh, const double* x, double* energy_h, void* ws, void* stream) {
+  return energy_xu(mesh, x, nullptr, energy_h, ws, stream);
+}
+
+int skg_snh_gradient_x(const skg_tet_mesh* mesh, const double* x, double* g, void* ws, void* stream) {
+  return gradient_xu(mesh, x, nullptr, g, ws, stream);
+}
+
+int skg_snh_hessian_x(const skg_tet_mesh* mesh, const double* x, int precision, int psd, double* val64,
+                      float* val32, void* ws, void* stream) {
+  return hessian_xu(mesh, x, nullptr, precision, psd, val64, val32, ws, stream);
+}
+
+int skg_snh_energy_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, double* energy_h, void* ws,
+                     void* stream) {
+  if (!Jx_bar) return fail(SKG_ERR_ARG, "energy_u: Jx_bar is null");
+  return energy_xu(mesh, u, Jx_bar, energy_h, ws, stream);
+}
+
+int skg_snh_gradient_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, double* g, void* ws,
+                       void* stream) {
+  if (!Jx_bar) return fail(SKG_ERR_ARG, "gradient_u: Jx_bar is null");
+  return gradient_xu(mesh, u, Jx_bar, g, ws, stream);
+}
+
+int skg_snh_hessian_u(const skg_tet_mesh* mesh, const double* u, const double* Jx_bar, int precision, int psd,
+                      double* val64, float* val32, void* ws, void* stream) {
+  if (!Jx_bar) return fail(SKG_ERR_ARG, "hessian_u: Jx_bar is null");
+  return hessian_xu(mesh, u, Jx_bar, precision, psd, val64, val32, ws, stream);
 }
 
 }  // extern "C"

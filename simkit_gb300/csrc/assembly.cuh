@@ -28,8 +28,18 @@ template <typename R> struct TetArgs {
   const float* ul;
   const int32_t* tet_inst;     // optional: instance of each tet (batched solves)
   const uint8_t* inst_active;  // optional: skip tets of inactive instances
-  int material;                // kMatSNH or kMatMMNH
+  const double* fbar;          // optional: per-tet F offset, 9 row-major values per tet:
+                               // F = (J u) + fbar, simkit's _u tier with fbar = J x_bar
+  int material;                // kMatSNH, kMatMMNH, kMatARAP or kMatFCR
 };
+
+template <typename R>
+__device__ __forceinline__ void add_fbar(const TetArgs<R>& a, int64_t e, R* G) {
+  if (a.fbar) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) G[k] += R(a.fbar[9 * e + k]);
+  }
+}
 
 // Contact springs against up to SKG_MAX_PLANES planes (simkit/energies/contact_springs_plane.py):
 // vertex v at x = X + u with d = (x - p) . n < 0 adds k w d^2 / 2, w = mass[v] or 1.

@@ -22,6 +22,8 @@ Fixtures written next to this script:
 * ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
 * ``element_arap_{3d,2d}.npz`` / ``element_fcr_{3d,2d}.npz``: ARAP and fixed-corotated element tiers on the same F batches
 * ``rollout_arap_small.npz`` / ``rollout_fcr_small.npz``: 6x2x2 beam, 8 backward-Euler steps with those energies
+* ``beam_u_tier.npz``: 3x2x2 jittered beam: the displacement (_u) tier of all four energies (F = J u + J x_bar
+  with x_bar a perturbed pose): energies, gradients and projected / unprojected Hessians
 * ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
 * ``rollout_contact_small.npz``: 6x2x2 beam falling onto a floor plane (contact springs), 14 steps
 * ``cache_reference.npz``: a cache file written by simkit's compute_with_cache_check (array, scalar, 1-element array)
@@ -151,6 +153,35 @@ def make_beam_small(ref, out):
                         J_data=J.data, J_indices=J.indices, J_indptr=J.indptr, J_shape=np.array(J.shape),
                         vol=vol, mass=M.diagonal(), energy=np.array(E), gradient=g,
                         K_data=K.data, K_indices=K.indices, K_indptr=K.indptr)
+
+
+def make_beam_u_tier(ref, out):
+    """simkit's *_u functions: stable_neo_hookean (snh.py:544-648) and the elastic dispatch
+    (elastic.py:151-746) for the three other materials."""
+    from simkit.energies import elastic as ref_elastic
+    from simkit_gb300.beams import make_beam
+    rng = np.random.default_rng(19)
+    t = 6 * 3 * 2 * 2
+    ym = np.exp(rng.uniform(np.log(1e5), np.log(1e7), size=t))
+    b = make_beam(3, 2, 2, ym=ym, pr=0.42, jitter=0.1, seed=13)
+    J = ref["deformation_jacobian"](b.X, b.T)
+    vol = ref["volume"](b.X, b.T)
+    x_bar = b.X + 0.01 * rng.standard_normal(b.X.shape)
+    Jx_bar = J @ x_bar.reshape(-1, 1)
+    u = 0.003 * rng.standard_normal(b.X.shape)
+    s = ref["snh"]
+    res = dict(X=b.X, T=b.T, mu=b.mu, lam=b.lam, vol=vol, u=u, Jx_bar=Jx_bar)
+    res["snh_energy"] = np.array(s.stable_neo_hookean_energy_u(u, J, Jx_bar, b.mu, b.lam, vol))
+    res["snh_gradient"] = s.stable_neo_hookean_gradient_u(u, J, Jx_bar, b.mu, b.lam, vol)
+    res["snh_hessian"] = s.stable_neo_hookean_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol).toarray()
+    res["snh_hessian_raw"] = s.stable_neo_hookean_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol, psd=False).toarray()
+    for tag, mat in (("mmnh", "macklin-mueller-neo-hookean"), ("arap", "arap"), ("fcr", "fcr")):
+        res[f"{tag}_energy"] = np.array(ref_elastic.elastic_energy_u(u, J, Jx_bar, b.mu, b.lam, vol, mat))
+        res[f"{tag}_gradient"] = ref_elastic.elastic_gradient_u(u, J, Jx_bar, b.mu, b.lam, vol, mat)
+        res[f"{tag}_hessian"] = ref_elastic.elastic_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol, mat).toarray()
+        res[f"{tag}_hessian_raw"] = ref_elastic.elastic_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol, mat,
+                                                                  psd=False).toarray()
+    np.savez_compressed(out, **res)
 
 
 def make_contact_plane(ref, out):
@@ -357,12 +388,14 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE", "/root/reference"))
     ap.add_argument("--skip-c1", action="store_true")
-    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot")
+    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot, u")
     a = ap.parse_args()
     ref = _import_reference(a.reference)
     if a.only:
         if "corot" in a.only.split(","):
             _write_corot(ref)
+        if "u" in a.only.split(","):
+            make_beam_u_tier(ref, os.path.join(HERE, "beam_u_tier.npz"))
         print("fixtures written to", HERE)
         return
     make_element(ref, 3, os.path.join(HERE, "element_3d.npz"))
@@ -377,6 +410,7 @@ def main():
     make_rollout_contact_small(ref, os.path.join(HERE, "rollout_contact_small.npz"))
     make_cache_file(a.reference, os.path.join(HERE, "cache_reference.npz"))
     _write_corot(ref)
+    make_beam_u_tier(ref, os.path.join(HERE, "beam_u_tier.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
     print("fixtures written to", HERE)

@@ -378,6 +378,42 @@ def test_corot_batched_equals_single(api):
         assert _rel(X + b.displacement(i), X + s.displacement()) < 1e-6
 
 
+_U_NAMES = {"snh": "stable_neo_hookean", "mmnh": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr"}
+_U_MATERIAL = {"mmnh": "macklin-mueller-neo-hookean", "arap": "arap", "fcr": "fcr"}
+
+
+@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr"])
+def test_u_tier_matches_reference(api, material):
+    """The displacement tier F = J u + Jx_bar (snh.py:544-648 and the *_u functions of the other
+    energies, elastic.py:151-746) on the device against simkit-generated values."""
+    g = _load("beam_u_tier.npz")
+    J = api.deformation_jacobian(g["X"], g["T"])
+    pre = _U_NAMES[material]
+    la = () if material == "arap" else (g["lam"],)
+    u, Jx, mu, vol = g["u"], g["Jx_bar"], g["mu"], g["vol"]
+    e = getattr(api, f"{pre}_energy_u")(u, J, Jx, mu, *la, vol)
+    assert abs(e - float(g[f"{material}_energy"])) < 1e-12 * abs(e)
+    gr = getattr(api, f"{pre}_gradient_u")(u, J, Jx, mu, *la, vol)
+    assert _rel(gr, g[f"{material}_gradient"]) < 1e-10
+    K = getattr(api, f"{pre}_hessian_u")(u, J, Jx, mu, *la, vol)
+    assert _rel(K.toarray(), g[f"{material}_hessian"]) < 1e-9
+    K = getattr(api, f"{pre}_hessian_u")(u, J, Jx, mu, *la, vol, psd=False)
+    assert _rel(K.toarray(), g[f"{material}_hessian_raw"]) < 1e-10
+    K32 = getattr(api, f"{pre}_hessian_u")(u, J, Jx, mu, *la, vol, precision="mixed")
+    assert _rel(K32.toarray(), g[f"{material}_hessian"]) < 3e-6
+    # device tensors in, device results out
+    import torch
+    gd = getattr(api, f"{pre}_gradient_u")(torch.from_numpy(u).cuda(), J, torch.from_numpy(Jx).cuda(), mu, *la, vol)
+    assert isinstance(gd, torch.Tensor) and _rel(gd.cpu().numpy(), g[f"{material}_gradient"]) < 1e-10
+    if material in _U_MATERIAL:
+        m = _U_MATERIAL[material]
+        assert abs(api.elastic_energy_u(u, J, Jx, mu, g["lam"], vol, m) - e) < 1e-13 * abs(e)
+        assert _rel(api.elastic_gradient_u(u, J, Jx, mu, g["lam"], vol, m), g[f"{material}_gradient"]) < 1e-10
+        assert _rel(api.elastic_hessian_u(u, J, Jx, mu, g["lam"], vol, m).toarray(), g[f"{material}_hessian"]) < 1e-9
+    with pytest.raises(ValueError):
+        getattr(api, f"{pre}_energy_u")(u, J, Jx[:-9], mu, *la, vol)
+
+
 @pytest.mark.parametrize("tag", ["m", "i"])
 def test_contact_plane_drop_in_matches_reference(api, tag):
     import scipy.sparse as sps

@@ -163,6 +163,21 @@ def test_rollout_corot_small_matches_reference(material):
     assert [i.iters for i in infos] == list(d["iters"])
 
 
+@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr"])
+def test_u_tier_matches_reference(material):
+    """The displacement tier (F = J u + Jx_bar) of all four energies against simkit's *_u
+    functions on a jittered beam with an arbitrary reference pose."""
+    from oracle import fem, utier
+    g = _load("beam_u_tier.npz")
+    J = fem.deformation_jacobian(g["X"], g["T"])
+    args = (g["u"], J, g["Jx_bar"], g["mu"], g["lam"], g["vol"])
+    e = utier.energy_u(material, *args)
+    assert abs(e - float(g[f"{material}_energy"])) < 1e-12 * abs(e)
+    assert _rel(utier.gradient_u(material, *args), g[f"{material}_gradient"]) < 1e-11
+    assert _rel(utier.hessian_u(material, *args).toarray(), g[f"{material}_hessian"]) < 1e-9
+    assert _rel(utier.hessian_u(material, *args, psd=False).toarray(), g[f"{material}_hessian_raw"]) < 1e-11
+
+
 @pytest.mark.parametrize("tag", ["m", "i"])
 def test_contact_plane_matches_reference(tag):
     """Contact springs (contact_springs_plane.py:44-200) with vertex weights (M) and without."""
