@@ -371,20 +371,19 @@ template <typename R> struct ZCoarse {
 };
 
 // e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows
-// strided over the grid), pc += (P^T r) . e over those rows.  rcf: shared
+// dealt to the blocks in turn so that every block gets nc / gridDim of them), pc += (P^T r) . e over those rows.  rcf: shared
 // staging of P^T r (np floats).
 template <typename R>
 __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, float inv_scale, Dacc<R>& pc) {
   const int wpb = blockDim.x >> 5;
-  const int gw0 = blockIdx.x * wpb;
-  if (gw0 >= c.nc) return;   // block-uniform
+  if ((int)blockIdx.x >= c.nc) return;   // block-uniform
 #pragma unroll 4
   for (int i = threadIdx.x; i < c.np; i += blockDim.x)
     rcf[i] = i < c.nc ? __ll2float_rn((long long)__ldcg(c.rc + i)) * inv_scale : 0.f;
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const float4* r4 = reinterpret_cast<const float4*>(rcf);
-  for (int row = gw0 + (threadIdx.x >> 5); row < c.nc; row += gridDim.x * wpb) {
+  for (int row = blockIdx.x + (threadIdx.x >> 5) * gridDim.x; row < c.nc; row += gridDim.x * wpb) {
     // A_c^-1 is streamed (evict-first) so that it does not push the block records out of L2
     const float4* Mr = reinterpret_cast<const float4*>(c.M + (int64_t)row * c.np);
     float s = 0.f;
@@ -410,7 +409,9 @@ __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, f
 //   C  e = A_c^-1 P^T r; (P^T r).e                             -> barrier 3
 // with r.M^-1 r = r.D^-1 r + (P^T r).e.  When the coarse inverse is not valid
 // (c.ok == 0) phases C and the restriction are skipped: the one-level method.
-// partials: >= 4 gridDim + 4 accumulators of scratch.
+// partials: >= 4 gridDim accumulators of scratch.  Each block owns an equal
+// contiguous range of block rows (the SpMV lane groups and the per-row update
+// both work inside it), so the phases end at about the same time in every block.
 // NT threads per block: 256 (three blocks per SM) or 768 (one per SM: a third of the
 // barrier arrivals and block partials, the same threads in flight)
 template <typename R, int G, int U, int NT = kBlock>
@@ -421,7 +422,6 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
   Dacc<R>* PA = reinterpret_cast<Dacc<R>*>(partials);     // p.q per block
   Dacc<R>* PB = PA + gridDim.x;                            // r.z, r.r per block
   Dacc<R>* PC = PB + 2 * gridDim.x;                        // (P^T r).e per block
-  Dacc<R>* TOT = PC + gridDim.x;                           // [0] p.q, [1] r.z, [2] r.r, [3] (P^T r).e
   unsigned* count = bar;
   volatile unsigned* gen = bar + 1;
   volatile double* err = scal + S_BAR_ERR;
@@ -442,10 +442,12 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
   bool done = scal[S_DONE] != 0.0;
   int status = 0;
   const int lane = threadIdx.x & (G - 1);
-  const int64_t groups = (int64_t)gridDim.x * (blockDim.x / G);
-  const int64_t row0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * (32 / G);
+  const int64_t chunk = (A.nbr + gridDim.x - 1) / gridDim.x;
+  const int64_t rbeg = min((int64_t)blockIdx.x * chunk, A.nbr), rend = min(rbeg + chunk, A.nbr);
+  const int64_t groups = NT / G;                                  // lane groups per block
+  const int64_t row0 = rbeg + (threadIdx.x >> 5) * (32 / G);      // warp-uniform loop bounds
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t wbase0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31);
+  const int64_t wbase0 = rbeg + (threadIdx.x & ~31);
   Dacc<R> rr_acc;
   dacc_zero(rr_acc);
   double rr_final = scal[S_RR];
@@ -456,9 +458,9 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
   if (!done && con) {
     // coarse part of z_0 = D^-1 r_0 + P e_0
     const float sc = coarse_scale(rr_prev);
-    for (int64_t base = wbase0; base < A.nbr; base += stride) {
+    for (int64_t base = wbase0; base < rend; base += NT) {
       const int64_t i = base + (threadIdx.x & 31);
-      const bool ok = i < A.nbr;
+      const bool ok = i < rend;
       const Vec3<R> r = ok ? ld3c(v.r, i) : Vec3<R>{R(0), R(0), R(0)};
       coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
     }
@@ -472,7 +474,7 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
       block_total<R, 1, NT>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];
-      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, TOT + 3, t3, wsum)) {
+      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, t3, wsum)) {
         status = SKG_ERR_TIMEOUT;
         done = true;
       } else {
@@ -489,14 +491,14 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
       for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.np; i += stride) c.rc[i] = 0ull;
     Dacc<R> pq[1];
     dacc_zero(pq[0]);
-    for (int64_t base = row0; base < A.nbr; base += U * groups) {
+    for (int64_t base = row0; base < rend; base += U * groups) {
       int64_t rows[U];
       bool val[U];
       Vec3<R> ys[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         rows[u] = base + u * groups + ((threadIdx.x & 31) / G);
-        val[u] = rows[u] < A.nbr;
+        val[u] = rows[u] < rend;
       }
       spmv_rows_dir<R, G, U>(A, zf, pprev, beta, first, rows, val, lane, ys);
 #pragma unroll
@@ -512,7 +514,7 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
     block_total<R, 1, NT>(pq, wsum);
     if (threadIdx.x == 0) st_dacc(PA + blockIdx.x, pq[0]);
     Dacc<R> t1[1];
-    if (!grid_barrier_total<R, 1, NT>(count, gen, err, PA, TOT, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 1, NT>(count, gen, err, PA, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     const R pqr = dacc_r(t1[0]);
     if (!(pqr > R(0)) || !isfinite(pqr)) {
       status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
@@ -523,9 +525,9 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
     Dacc<R> acc[2];
     dacc_zero(acc[0]);
     dacc_zero(acc[1]);
-    for (int64_t base = wbase0; base < A.nbr; base += stride) {
+    for (int64_t base = wbase0; base < rend; base += NT) {
       const int64_t i = base + (threadIdx.x & 31);
-      const bool ok = i < A.nbr;
+      const bool ok = i < rend;
       Vec3<R> r{R(0), R(0), R(0)};
       if (ok) {
         Vec3<R> x = ld3c(v.x, i);
@@ -548,7 +550,7 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
       st_dacc(PB + gridDim.x + blockIdx.x, acc[1]);
     }
     Dacc<R> t2[2];
-    if (!grid_barrier_total<R, 2, NT>(count, gen, err, PB, TOT + 1, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 2, NT>(count, gen, err, PB, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     ++it;
     rr_acc = t2[1];
     rr_prev = dacc_value(t2[1]);
@@ -564,7 +566,7 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
       block_total<R, 1, NT>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];
-      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, TOT + 3, t3, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+      if (!grid_barrier_total<R, 1, NT>(count, gen, err, PC, t3, wsum)) { status = SKG_ERR_TIMEOUT; break; }
       rz = dacc_add(rz, t3[0]);
     }
     beta = dacc_r(rz) / dacc_r(rz_old);

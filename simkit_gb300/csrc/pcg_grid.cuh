@@ -9,11 +9,10 @@
 // dependent reduction (p.q, then r.z and r.r) and no separate direction pass.
 //
 // Reductions: each block reduces its double-float (FP32 systems) or FP64
-// partials with a fixed tree and stores them; at the barrier the last block to
-// arrive sums every block's partial in index order and publishes the totals
-// before releasing the others, who read the totals (one L2 load) instead of
-// each summing all partials.  The order of the sums does not depend on which
-// block arrives last, so the scalars are the same on every run.
+// partials with a fixed tree and stores them; after the barrier every block
+// sums all partials in index order with the same tree.  The order of the sums
+// does not depend on which block arrives last, so the scalars are the same in
+// every block and on every run.
 #pragma once
 
 namespace skg {
@@ -49,58 +48,31 @@ __device__ __forceinline__ Dacc<float> ld_dacc(const Dacc<float>* p) {
 }
 __device__ __forceinline__ Dacc<double> ld_dacc(const Dacc<double>* p) { return {__ldcg(&p->v)}; }
 
-// Grid barrier whose last arriving block first sums the NV x gridDim partials
-// (part[k * gridDim + b]) in index order into tot[0..NV); every thread returns
-// the totals.  Bounded spin: on timeout err is set and false returned.
+// Grid barrier followed by the totals of the NV x gridDim partials
+// (part[k * gridDim + b]): every block sums them itself in index order with the
+// same tree, so all blocks hold bitwise the same totals and no block works
+// between the last arrival and the release.  Returns false on a barrier timeout.
 template <typename R, int NV, int NT = kBlock>
 __device__ __forceinline__ bool grid_barrier_total(unsigned* count, volatile unsigned* gen, volatile double* err,
-                                                   const Dacc<R>* part, Dacc<R>* tot, Dacc<R> (&out)[NV],
+                                                   const Dacc<R>* part, Dacc<R> (&out)[NV],
                                                    Dacc<R> (*wsum)[NT / 32]) {
-  __shared__ int last;
-  __shared__ int ok;
-  __shared__ unsigned g0;
-  __syncthreads();
+  __shared__ Dacc<R> bc[NV];
+  const bool ok = grid_barrier(count, gen, err);
+  Dacc<R> s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    dacc_zero(s[k]);
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s[k] = dacc_add(s[k], ld_dacc(part + k * gridDim.x + i));
+  }
+  block_total<R, NV, NT>(s, wsum);
   if (threadIdx.x == 0) {
-    ok = 1;
-    g0 = *gen;
-    __threadfence();
-    last = atomicAdd(count, 1u) == gridDim.x - 1;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) bc[k] = s[k];
   }
   __syncthreads();
-  if (last) {
-    __threadfence();
-    Dacc<R> s[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      dacc_zero(s[k]);
-      for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s[k] = dacc_add(s[k], ld_dacc(part + k * gridDim.x + i));
-    }
-    block_total<R, NV, NT>(s, wsum);
-    if (threadIdx.x == 0) {
-#pragma unroll
-      for (int k = 0; k < NV; ++k) st_dacc(tot + k, s[k]);
-      __threadfence();
-      *count = 0u;
-      __threadfence();
-      atomicAdd((unsigned*)gen, 1u);
-    }
-  } else if (threadIdx.x == 0) {
-    long long spins = 0;
-    while (*gen == g0) {
-      if (++spins > kSpinLimit) {
-        *err = (double)SKG_ERR_TIMEOUT;
-        ok = 0;
-        break;
-      }
-      if (spins > 256) __nanosleep(32);
-    }
-    __threadfence();
-  }
-  if (threadIdx.x == 0 && *err != 0.0) ok = 0;
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) out[k] = ld_dacc(tot + k);
-  return ok != 0;
+  for (int k = 0; k < NV; ++k) out[k] = bc[k];
+  return ok;
 }
 
 // preconditioned residual of a column as stored (one-level preconditioner)
@@ -161,14 +133,13 @@ __device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const Zf& zf, con
 }
 
 // Solve after k_pcg_init (x = 0, r, z, p = z, rz, rr, bb, tol2 in scal).  Direction
-// buffers: v.p and v.s alternate.  partials: >= 3 gridDim + 3 accumulators of scratch.
+// buffers: v.p and v.s alternate.  partials: >= 3 gridDim accumulators of scratch.
 template <typename R, int G, int U>
 __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2(Bsr<R> A, PcgVecs<R> v, double* partials, unsigned* bar,
                                                       double* scal) {
   __shared__ Dacc<R> wsum[2][kBlock / 32];
   Dacc<R>* PA = reinterpret_cast<Dacc<R>*>(partials);     // p.q per block
   Dacc<R>* PB = PA + gridDim.x;                            // r.z, r.r per block
-  Dacc<R>* TOT = PB + 2 * gridDim.x;                       // totals: [0] p.q, [1] r.z, [2] r.r
   unsigned* count = bar;
   volatile unsigned* gen = bar + 1;
   volatile double* err = scal + S_BAR_ERR;
@@ -226,7 +197,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2(Bsr<R> A, PcgVecs<R> v,
     block_total<R, 1>(pq, wsum);
     if (threadIdx.x == 0) st_dacc(PA + blockIdx.x, pq[0]);
     Dacc<R> t1[1];
-    if (!grid_barrier_total<R, 1>(count, gen, err, PA, TOT, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 1>(count, gen, err, PA, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     const R pqr = dacc_r(t1[0]);
     if (!(pqr > R(0)) || !isfinite(pqr)) {
       status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
@@ -254,7 +225,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_pcg_grid2(Bsr<R> A, PcgVecs<R> v,
       st_dacc(PB + gridDim.x + blockIdx.x, acc[1]);
     }
     Dacc<R> t2[2];
-    if (!grid_barrier_total<R, 2>(count, gen, err, PB, TOT + 1, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if (!grid_barrier_total<R, 2>(count, gen, err, PB, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     ++it;
     rr_acc = t2[1];
     const R rrr = dacc_r(t2[1]);

@@ -289,21 +289,23 @@ __global__ void __launch_bounds__(kBlock) k_pcg_direction(int64_t nbr, PcgVecs<R
 // are resident and the barrier completes in normal operation.
 constexpr long long kSpinLimit = 1ll << 24;
 
+// Arrive-and-wait grid barrier.  Thread 0 of each block arrives with an acq_rel
+// atomic (releasing the block's writes, ordered before it by __syncthreads); the
+// last arrival resets the count and publishes the next generation with a
+// release store; the others poll the generation with acquire loads.  Bounded
+// spin: on timeout err is set and false returned.
 __device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned* gen, volatile double* err) {
   __syncthreads();
-  __shared__ int ok;
+  __shared__ int ok_s;
   if (threadIdx.x == 0) {
-    ok = 1;
+    int ok = 1;
     const unsigned g = *gen;
-    __threadfence();
-    const unsigned arrived = atomicAdd(count, 1u);
-    if (arrived == gridDim.x - 1) {
-      *count = 0u;
-      __threadfence();
-      atomicAdd((unsigned*)gen, 1u);
+    if (atom_add_acqrel_gpu(count, 1u) == gridDim.x - 1) {
+      st_relaxed_gpu(count, 0u);
+      st_release_gpu((unsigned*)gen, g + 1u);
     } else {
       long long spins = 0;
-      while (*gen == g) {
+      while (ld_acquire_gpu((const unsigned*)gen) == g) {
         if (++spins > kSpinLimit) {
           *err = (double)SKG_ERR_TIMEOUT;
           ok = 0;
@@ -312,11 +314,11 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned*
         if (spins > 256) __nanosleep(32);
       }
     }
-    __threadfence();
     if (*err != 0.0) ok = 0;
+    ok_s = ok;
   }
   __syncthreads();
-  return ok != 0;
+  return ok_s != 0;
 }
 
 // sum of NV per-block partials in index order, computed redundantly by
