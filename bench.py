@@ -199,6 +199,15 @@ def replica_seed(rank: int) -> int:
     return int(rank)
 
 
+def _refresh_arg(v):
+    if v in ("step", "newton"):
+        return v
+    k = int(v)
+    if k < 1:
+        raise ValueError("refresh interval must be >= 1")
+    return k
+
+
 def algorithmic_bytes(spec, nb, n_coarse=0):
     n, t = spec.n_verts, spec.n_tets
     return {
@@ -450,7 +459,8 @@ def main():
     ap.add_argument("--pcg-mode", type=int, default=3)
     ap.add_argument("--coarse", default="auto",
                     help="two-level PCG aggregates: none, auto, or a box size in mesh spacings")
-    ap.add_argument("--coarse-refresh", default="step", choices=["step", "newton"])
+    ap.add_argument("--coarse-refresh", default=4, type=_refresh_arg,
+                    help="'step', 'newton' or k: rebuild the coarse inverse every k steps")
     ap.add_argument("--pcg-rtol", type=float, default=-0.1,
                     help="PCG tolerance; negative = Eisenstat-Walker forcing capped at its magnitude")
     ap.add_argument("--no-cpu-baseline", action="store_true")

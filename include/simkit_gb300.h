@@ -312,8 +312,10 @@ typedef struct skg_be_params {
   int32_t n_planes;         /* contact planes added to the potential (0..SKG_MAX_PLANES) */
   int32_t contact_mass_weighted; /* 1: spring weight = lumped vertex mass; 0: 1 */
   const skg_contact_plane* planes; /* host array of n_planes planes */
-  int32_t coarse_refresh;   /* pcg_mode 7: rebuild the coarse inverse 0 = at the first Newton
-                               iteration of each step, 1 = at every Newton iteration */
+  int32_t coarse_refresh;   /* two-level PCG: rebuild the coarse inverse 0 = at the first Newton
+                               iteration of this step, 1 = at every Newton iteration, -1 = not
+                               at all: reuse the inverse an earlier call built in the same
+                               workspace for the same mesh (the caller guarantees one exists) */
 } skg_be_params;
 
 typedef struct skg_be_state {

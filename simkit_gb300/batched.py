@@ -31,7 +31,8 @@ class BatchedBESolver:
     pinned`` (e.g. ``simkit_gb300.beams.BeamSpec``); each keeps its own
     material, gravity direction and pins.  ``coarse``: two-level PCG with
     per-instance aggregates ('auto': 4^3 mesh spacings, or a box size), None for
-    the one-level block-Jacobi PCG; ``coarse_refresh`` as in ``BESolver``.
+    the one-level block-Jacobi PCG; ``coarse_refresh``: 'step' (per-instance coarse inverses
+    rebuilt at the first Newton iteration of each step) or 'newton' (at every iteration).
     """
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
@@ -70,6 +71,8 @@ class BatchedBESolver:
         if coarse is not None:
             _, self.coarse_boxes = mesh.set_coarse_inst(np.concatenate(pins) == 0, np.array(rows),
                                                         box=4 if coarse == "auto" else int(coarse))
+        if coarse_refresh not in ("step", "newton"):
+            raise ValueError("coarse_refresh must be 'step' or 'newton'")
         self._coarse_refresh = coarse_refresh
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,

@@ -12,6 +12,7 @@
 //   u           f64[3n]   displacement from rest (or absolute positions)
 //   uh, ul      f32[n][4] hi/lo split of u for FP32 kernels
 #include "assembly.cuh"
+#include "dfloat.cuh"
 #include "snh_math.cuh"
 
 namespace skg {
@@ -216,20 +217,88 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
       f[3 * b + i] = vol * (P[3 * i] * gN[3 * b] + P[3 * i + 1] * gN[3 * b + 1] + P[3 * i + 2] * gN[3 * b + 2]);
 }
 
+// Double-float forces of the mixed-precision stepper (neo-Hookean materials,
+// displacement form): the f_a of k_tet_forces evaluated in double-float
+// arithmetic (dfloat.cuh) from the FP32 hi/lo splits of u (uh, ul) and of Dinv
+// (dinv_hi = dinv32, dinv_lo), so that only the three material loads touch the
+// FP64 units.  Written as (hi, lo) pairs for k_vertex_gradient<true>.
+__global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const float* __restrict__ dinv_hi,
+                                                       const float* __restrict__ dinv_lo,
+                                                       const float* __restrict__ uh, const float* __restrict__ ul,
+                                                       float2* __restrict__ fbuf) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= a.t) return;
+  const int4 v = __ldg(a.tets + e);
+  DF du[9], D[9], G[9], P[9], gN[12];
+  {
+    const Vec3<float> h0 = ld3(uh, v.x), l0 = ld3(ul, v.x);
+    const DF x0 = DF(h0.x, l0.x), y0 = DF(h0.y, l0.y), z0 = DF(h0.z, l0.z);
+    const int vv[3] = {v.y, v.z, v.w};
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const Vec3<float> h = ld3(uh, vv[b]), l = ld3(ul, vv[b]);
+      du[3 * b + 0] = DF(h.x, l.x) - x0;
+      du[3 * b + 1] = DF(h.y, l.y) - y0;
+      du[3 * b + 2] = DF(h.z, l.z) - z0;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) D[k] = DF(__ldg(dinv_hi + k * a.t + e), __ldg(dinv_lo + k * a.t + e));
+  disp_grad(du, D, G);
+  const DF vol(a.vol[e]), mu(a.mu[e]), lam(a.lam[e]);
+  if (a.material == kMatMMNH)
+    mmnh_pk1_disp<DF>(G, mu, lam, P);
+  else
+    snh_pk1_disp<DF>(G, mu, lam, P);
+  shape_grads(D, gN);
+  float2* f = fbuf + 12 * e;
+#pragma unroll
+  for (int b = 0; b < 4; ++b)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const DF s = vol * (P[3 * i] * gN[3 * b] + P[3 * i + 1] * gN[3 * b + 1] + P[3 * i + 2] * gN[3 * b + 2]);
+      f[3 * b + i] = make_float2(s.hi, s.lo);
+    }
+}
+
+// low parts of Dinv for the double-float forces: dinv = dinv32 + dinv_lo to ~48 bits
+__global__ void k_dinv_lo(const double* __restrict__ dinv, const float* __restrict__ dinv32, int64_t n,
+                          float* __restrict__ lo) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) lo[i] = float(dinv[i] - double(dinv32[i]));
+}
+
 // Vertex gather of the forces in list (tet) order, plus the backward-Euler
 // terms M/h^2 (u - u_tilde) - f_ext when `mass` is set; pinned DOFs are
 // zeroed.  Grid-stride over a fixed grid; ||g||^2 reduced deterministically.
+// DFB: the forces are double-float pairs (k_tet_forces_df), summed in double-float.
+template <bool DFB>
 __global__ void __launch_bounds__(kBlock) k_vertex_gradient(GradArgs a) {
   double gg[1] = {0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < a.n; v += stride) {
     double acc[3] = {0.0, 0.0, 0.0};
-    for (int k = __ldg(a.v2t_ptr + v); k < __ldg(a.v2t_ptr + v + 1); ++k) {
-      const int code = __ldg(a.v2t + k);
-      const double* f = a.fbuf + 12 * (int64_t)(code >> 2) + 3 * (code & 3);
-      acc[0] += f[0];
-      acc[1] += f[1];
-      acc[2] += f[2];
+    if constexpr (DFB) {
+      DF s[3] = {DF(0.f, 0.f), DF(0.f, 0.f), DF(0.f, 0.f)};
+      for (int k = __ldg(a.v2t_ptr + v); k < __ldg(a.v2t_ptr + v + 1); ++k) {
+        const int code = __ldg(a.v2t + k);
+        const float2* f = reinterpret_cast<const float2*>(a.fbuf) + 12 * (int64_t)(code >> 2) + 3 * (code & 3);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float2 x = f[c];
+          s[c] += DF(x.x, x.y);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] = s[c].to_double();
+    } else {
+      for (int k = __ldg(a.v2t_ptr + v); k < __ldg(a.v2t_ptr + v + 1); ++k) {
+        const int code = __ldg(a.v2t + k);
+        const double* f = a.fbuf + 12 * (int64_t)(code >> 2) + 3 * (code & 3);
+        acc[0] += f[0];
+        acc[1] += f[1];
+        acc[2] += f[2];
+      }
     }
     if (a.contact.n > 0) {
       double x[3];
@@ -417,8 +486,27 @@ int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t
   return SKG_OK;
 }
 
-int launch_vertex_gradient(const GradArgs& a, cudaStream_t s) {
-  k_vertex_gradient<<<reduce_blocks(a.n), kBlock, 0, s>>>(a);
+int launch_vertex_gradient(const GradArgs& a, cudaStream_t s, bool df) {
+  if (df)
+    k_vertex_gradient<true><<<reduce_blocks(a.n), kBlock, 0, s>>>(a);
+  else
+    k_vertex_gradient<false><<<reduce_blocks(a.n), kBlock, 0, s>>>(a);
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+int launch_forces_df(const TetArgs<double>& a, const float* dinv32, const float* dinv_lo, const float* uh,
+                     const float* ul, double* fbuf, cudaStream_t s) {
+  if (a.t == 0) return SKG_OK;
+  k_tet_forces_df<<<blocks_for(a.t, 128), 128, 0, s>>>(a, dinv32, dinv_lo, uh, ul, reinterpret_cast<float2*>(fbuf));
+  SKG_LAUNCHED();
+  return SKG_OK;
+}
+
+int launch_dinv_lo(const skg_tet_mesh* m, float* lo, cudaStream_t s) {
+  const int64_t n = 9 * m->n_tets;
+  if (n == 0) return SKG_OK;
+  k_dinv_lo<<<blocks_for(n), kBlock, 0, s>>>(m->dinv, m->dinv32, n, lo);
   SKG_LAUNCHED();
   return SKG_OK;
 }
@@ -479,6 +567,7 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   w.ut = c.take<double>(3 * n);
   w.uh = c.take<float>(4 * n);
   w.ul = c.take<float>(4 * n);
+  w.dinv_lo = mixed ? c.take<float>(9 * t) : nullptr;
   for (int k = 0; k < 6; ++k) {
     w.vec32[k] = mixed ? c.take<float>(4 * n) : nullptr;
     w.vec64[k] = mixed ? nullptr : c.take<double>(4 * n);

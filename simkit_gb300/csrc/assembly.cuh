@@ -173,6 +173,7 @@ struct Workspace {
   double* ut;
   float* uh;
   float* ul;
+  float* dinv_lo;    // mixed: low parts of Dinv for the double-float forces (9 t)
   float* vec32[6];   // PCG x, r, z, p, q, s (padded)
   double* vec64[6];
   double* partials;
@@ -220,7 +221,12 @@ inline AsmArgs<R> make_asm_args(const skg_tet_mesh* m, const R* hbuf, R* val, R*
 template <typename R> int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s);
 template <typename R> int launch_assemble(const AsmArgs<R>& a, cudaStream_t s);
 int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t s);
-int launch_vertex_gradient(const GradArgs& a, cudaStream_t s);
+// double-float forces (mixed precision, neo-Hookean materials, displacement form); fbuf holds
+// 12 (hi, lo) float pairs per tet, summed by launch_vertex_gradient(..., df = true)
+int launch_forces_df(const TetArgs<double>& a, const float* dinv32, const float* dinv_lo, const float* uh,
+                     const float* ul, double* fbuf, cudaStream_t s);
+int launch_dinv_lo(const skg_tet_mesh* m, float* lo, cudaStream_t s);
+int launch_vertex_gradient(const GradArgs& a, cudaStream_t s, bool df = false);
 template <typename R> int launch_energy(const EnergyArgs<R>& a, bool direct, cudaStream_t s);
 int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t s);
 template <typename R>

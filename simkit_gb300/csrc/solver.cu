@@ -1052,10 +1052,23 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   ea.contact = contact;
   ea.partials = w.partials; ea.counter = w.counter; ea.out = w.scal + S_E;
 
+  // mixed precision, neo-Hookean materials: forces in double-float from the hi/lo split
+  // (the FP64 units of GB300 are the bottleneck of the FP64 force kernel)
+  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH);
+  if (dff) {
+    SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s));
+    info->launches++;
+  }
   auto gradient = [&](double* gg) -> int {
     pt.begin();
-    SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
-    SKG_TRY(launch_vertex_gradient(ga, s));
+    if (dff) {
+      SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
+      SKG_TRY(launch_forces_df(make_tet_args64(m, st->u), m->dinv32, w.dinv_lo, w.uh, w.ul, w.fbuf, s));
+      info->launches++;
+    } else {
+      SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    }
+    SKG_TRY(launch_vertex_gradient(ga, s, dff));
     info->launches += 2;
     info->t_gradient_ms += pt.end();
     return read_scalars(w.scal + S_GG, gg, 1, s);
@@ -1147,7 +1160,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     SKG_TRY(launch_assemble<R>(aa, s));
     info->launches += 2;
     // coarse operator of the two-level preconditioner (timed with the assembly)
-    if (two_level && (it == 0 || prm->coarse_refresh)) {
+    if (two_level && ((it == 0 && prm->coarse_refresh >= 0) || prm->coarse_refresh > 0)) {
       SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s));
       info->launches += 2;
     }
@@ -1487,10 +1500,21 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   ea.contact = contact;
   int launches = 1;
 
+  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH);
+  if (dff) {
+    SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s));
+    launches++;
+  }
   auto gradient = [&]() -> int {
     pt.begin();
-    SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
-    SKG_TRY(launch_vertex_gradient(ga, s));
+    if (dff) {
+      SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
+      SKG_TRY(launch_forces_df(make_tet_args64(m, st->u), m->dinv32, w.dinv_lo, w.uh, w.ul, w.fbuf, s));
+      launches++;
+    } else {
+      SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    }
+    SKG_TRY(launch_vertex_gradient(ga, s, dff));
     k_inst_sumsq<<<ni, kBlock, 0, s>>>(w.g, bt->inst_rows, bw.gg);
     SKG_LAUNCHED();
     launches += 3;
@@ -1617,7 +1641,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     SKG_TRY(launch_assemble<R>(aa, s));
     // per-instance coarse operators of the two-level PCG (every instance is active at the first
     // Newton iteration of the step)
-    if (two_level && (it == 0 || prm->coarse_refresh)) {
+    if (two_level && ((it == 0 && prm->coarse_refresh >= 0) || prm->coarse_refresh > 0)) {
       SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s, bt->order));
       launches += 2;
     }

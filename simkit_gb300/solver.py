@@ -86,15 +86,17 @@ class BESolver:
         whole-mesh form (box 8 by default; the grid PCG, pcg_mode 3 or 7), smaller ones the
         per-instance form (box 4; the thread-block-cluster PCG, pcg_mode 2 or 3)
     coarse_form : 'auto' (by size, as above), 'grid' or 'cluster'
-    coarse_refresh : 'step' (coarse inverse rebuilt at the first Newton iteration of each step)
-        or 'newton' (at every Newton iteration)
+    coarse_refresh : 'step' (coarse inverse rebuilt at the first Newton iteration of each step),
+        'newton' (at every Newton iteration) or an int k (default 4: at the first Newton iteration
+        of every k-th step; the steps between reuse it: the preconditioner stays SPD, only less
+        fresh, and on the 786,432-tet beam the PCG iteration count did not change)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
                  material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh="step", coarse_form="auto"):
+                 coarse="auto", coarse_refresh=4, coarse_form="auto"):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.set_energy(material)
@@ -122,8 +124,10 @@ class BESolver:
             else:
                 _, boxes = m.set_coarse_inst(pin == 0, box=4 if coarse == "auto" else int(coarse))
                 self.coarse_box = int(boxes[0])
-        if coarse_refresh not in ("step", "newton"):
-            raise ValueError("coarse_refresh must be 'step' or 'newton'")
+        if not (coarse_refresh in ("step", "newton") or (isinstance(coarse_refresh, int) and coarse_refresh >= 1)):
+            raise ValueError("coarse_refresh must be 'step', 'newton' or an int >= 1")
+        self.coarse_refresh = coarse_refresh
+        self._coarse_age = None   # steps since the coarse inverse was built (None: not built)
         self.u_prev = torch.zeros(3 * m.n, dtype=torch.float64, device=dev)
         self.u_curr = torch.zeros_like(self.u_prev)
         self.u_next = torch.zeros_like(self.u_prev)
@@ -169,6 +173,10 @@ class BESolver:
                       u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
                       u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
         info = StepInfoC()
+        if isinstance(self.coarse_refresh, int):
+            rebuild = self._coarse_age is None or self._coarse_age + 1 >= self.coarse_refresh
+            self.params.coarse_refresh = 0 if rebuild else -1
+            self._coarse_age = 0 if rebuild else self._coarse_age + 1
         check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
                                       ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),
                                       _stream_ptr(stream)))

@@ -132,3 +132,15 @@ void h_svd(int prec, int64_t t, const double* F, double* U, double* s, double* V
 double h_phi(double z) { return phi_log1p<double>(z); }
 float h_phi_f(float z) { return phi_log1p<float>(z); }
 }
+
+// double-float stress of the mixed-precision force kernel (simkit_gb300/csrc/dfloat.cuh)
+#include "../../simkit_gb300/csrc/dfloat.cuh"
+extern "C" void h_pk1_disp_df(int mat, int64_t t, const double* G, const double* mu, const double* lam, double* P) {
+  for (int64_t e = 0; e < t; ++e) {
+    DF g[9], p[9];
+    for (int k = 0; k < 9; ++k) g[k] = DF(G[9 * e + k]);
+    if (mat == kMatMMNH) mmnh_pk1_disp<DF>(g, DF(mu[e]), DF(lam[e]), p);
+    else snh_pk1_disp<DF>(g, DF(mu[e]), DF(lam[e]), p);
+    for (int k = 0; k < 9; ++k) P[9 * e + k] = p[k].to_double();
+  }
+}

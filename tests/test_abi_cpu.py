@@ -297,6 +297,27 @@ def test_corot_element_math_matches_oracle(hostmath, mat, name):
     assert np.all(np.abs(H2 - Ho.reshape(t, 16)).max(1) <= 1e-11 * scale)
 
 
+@pytest.mark.parametrize("mat", [0, 1])
+def test_double_float_stress_matches_fp64(hostmath, mat):
+    """The double-float displacement-form stress (dfloat.cuh) of the mixed-precision force kernel
+    agrees with the FP64 evaluation to ~1e-13 of the element's stress, from |G| = 1e-6 to 0.4."""
+    rng = np.random.default_rng(40 + mat)
+    t = 800
+    G = np.concatenate([s * rng.standard_normal((t // 4, 9)) for s in (1e-6, 1e-3, 0.1, 0.4)])
+    G = np.ascontiguousarray(G)
+    F = np.ascontiguousarray(G + np.eye(3).reshape(1, 9))
+    mu = rng.uniform(3e4, 3e6, t)
+    lam = mu * rng.uniform(1.5, 40, t)
+    r = np.zeros(t), np.zeros(t), np.zeros((t, 9)), np.zeros((t, 9)), np.zeros((t, 81))
+    hostmath.h_mat(64, mat, ctypes.c_int64(t), _p(F), _p(G), _p(mu), _p(lam), *map(_p, r))
+    Pd = r[3]
+    Pf = np.zeros((t, 9))
+    hostmath.h_pk1_disp_df(mat, ctypes.c_int64(t), _p(G), _p(mu), _p(lam), _p(Pf))
+    rel = np.abs(Pf - Pd).max(1) / np.abs(Pd).max(1)
+    assert rel[: 3 * t // 4].max() < 1e-13
+    assert rel.max() < 3e-12
+
+
 def test_displacement_forms_match_oracle(hostmath):
     rng = np.random.default_rng(6)
     t = 200

@@ -467,7 +467,7 @@ def test_two_barrier_grid_pcg_matches_reference(api, precision):
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
-@pytest.mark.parametrize("refresh", ["step", "newton"])
+@pytest.mark.parametrize("refresh", ["step", "newton", 4])
 def test_two_level_pcg_matches_reference(api, precision, refresh):
     """The two-level grid PCG (pcg_mode 7: block Jacobi + rigid-mode aggregates of 4^3 cells,
     coarse inverse by the Gauss-Jordan kernel) on the 12,288-tet beam: 20 steps within the same
@@ -527,6 +527,26 @@ def test_two_level_repeatable(api):
         ia, ib = a.step(), b.step()
         assert ia.pcg_iters == ib.pcg_iters
     assert torch.equal(a.u_curr, b.u_curr)
+
+
+@pytest.mark.parametrize("material", ["stable-neo-hookean", "macklin-mueller-neo-hookean"])
+def test_double_float_forces_match_fp64(api, material):
+    """The mixed-precision stepper's double-float force kernel gives the same Newton residual as
+    the FP64 force kernel at the same state (the initial residual of a step, ||g(x_tilde)||)."""
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    spec = beam_small_steady()
+    a = BESolver.from_spec(spec, precision="fp64", material=material, coarse=None)
+    b = BESolver.from_spec(spec, precision="mixed", material=material, coarse=None)
+    for _ in range(3):
+        assert a.step().converged
+    b.u_curr.copy_(a.u_curr)
+    b.u_prev.copy_(a.u_prev)
+    ia, ib = a.step(), b.step()
+    assert ib.converged
+    assert abs(ia.residual0 - ib.residual0) < 1e-11 * ia.residual0
+    X = spec.X.reshape(-1)
+    assert _rel(X + a.displacement(), X + b.displacement()) < 1e-6
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
