@@ -104,7 +104,7 @@ __device__ __forceinline__ void spmv_rows_dir(const Bsr<R>& A, const Zf& zf, con
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       bk[u] = Blk<R>{};
-      if (k < K[u]) bk[u] = ld_rec<Zf::kAux>(A.rec, p[u] + k);
+      if (k < K[u]) bk[u] = ld_rec<Zf::kAux>(A.rec, p[u] + k, p[u] + k >= A.keep);
     }
     Vec3<R> xv[U];
 #pragma unroll
