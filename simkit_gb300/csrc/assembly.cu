@@ -106,7 +106,41 @@ __global__ void k_assemble(AsmArgs<R> a) {
 #pragma unroll
   for (int m = 0; m < 9; ++m) acc[m] = R(0);
   const int c0 = __ldg(a.hc_ptr + s), c1 = __ldg(a.hc_ptr + s + 1);
-  for (int c = c0; c < c1; ++c) {
+  int c = c0;
+  // four contributions at a time: their loads are all issued before any is summed (a diagonal
+  // slot has one contribution per incident tet, ~24 on a Kuhn-split grid).  Every contribution
+  // is read as 9 values from its offset (a diagonal block's 6 plus 3 that are not used; they
+  // stay inside the tet's kHStride record); the sums keep the list order.
+  for (; c + 4 <= c1; c += 4) {
+    int cd[4];
+    R b[4][9];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int code = __ldg(a.hc_src + c + j);
+      cd[j] = code & 15;
+      const int off = cd[j] < 4 ? 6 * cd[j] : 24 + 9 * (cd[j] < 10 ? cd[j] - 4 : cd[j] - 10);
+      const R* h = a.hbuf + (int64_t)kHStride * (code >> 4) + off;
+#pragma unroll
+      for (int m = 0; m < 9; ++m) b[j][m] = h[m];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (cd[j] < 4) {
+        acc[0] += b[j][0]; acc[1] += b[j][1]; acc[2] += b[j][2];
+        acc[3] += b[j][1]; acc[4] += b[j][3]; acc[5] += b[j][4];
+        acc[6] += b[j][2]; acc[7] += b[j][4]; acc[8] += b[j][5];
+      } else if (cd[j] < 10) {
+#pragma unroll
+        for (int m = 0; m < 9; ++m) acc[m] += b[j][m];
+      } else {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int k2 = 0; k2 < 3; ++k2) acc[3 * i + k2] += b[j][3 * k2 + i];
+      }
+    }
+  }
+  for (; c < c1; ++c) {
     const int code = __ldg(a.hc_src + c);
     const int64_t e = code >> 4;
     const int cd = code & 15;
