@@ -384,12 +384,13 @@ __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, f
   const int lane = threadIdx.x & 31;
   const float4* r4 = reinterpret_cast<const float4*>(rcf);
   for (int row = blockIdx.x + (threadIdx.x >> 5) * gridDim.x; row < c.nc; row += gridDim.x * wpb) {
-    // A_c^-1 is streamed (evict-first) so that it does not push the block records out of L2
+    // A_c^-1 is read with normal L2 priority: with the block records past 20% read evict-first
+    // it stays in L2 beside the kept records and the vectors
     const float4* Mr = reinterpret_cast<const float4*>(c.M + (int64_t)row * c.np);
     float s = 0.f;
 #pragma unroll 5
     for (int j = lane; j < (c.np >> 2); j += 32) {
-      const float4 m = __ldcs(Mr + j), x = r4[j];
+      const float4 m = __ldcg(Mr + j), x = r4[j];
       s = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, s))));
     }
 #pragma unroll

@@ -27,7 +27,7 @@ enum ScalarSlot {
   S_BAR_ERR = 24, S_CERR = 26
 };
 
-constexpr double kKeepFrac = 0.4;   // fraction of the grid PCG's block records read with normal L2 priority
+constexpr double kKeepFrac = 0.2;   // fraction of the grid PCG's block records read with normal L2 priority
 
 template <typename R> struct Bsr {
   int64_t nbr;
@@ -1039,9 +1039,9 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
   pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4]; pv.s = vv[5];
   Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
-  // the first 40% of the block records stay in L2 across PCG iterations, the rest is read
-  // evict-first (measured on the 786,432-tet beam: 55.9 -> 52.0 us per two-level iteration;
-  // any kept fraction in 0.3..0.6 was within 0.3 us)
+  // the first 20% of the block records stay in L2 across PCG iterations, the rest is read
+  // evict-first (measured on the 786,432-tet beam: 55.9 -> 52.0 us per two-level iteration with
+  // 40% kept; 49.7 us with 20% kept and the dense coarse inverse read with normal priority)
   A.keep = (int64_t)(kKeepFrac * (double)m->n_blocks);
 
   PhaseTimer pt;
