@@ -193,27 +193,30 @@ class BESolver:
 
     def step_host(self, x_curr: np.ndarray, x_prev: np.ndarray, out: np.ndarray = None, stream=None):
         """One step with host positions in and out (simkit's backward_euler contract:
-        x_curr, x_prev (3n, 1) float64 -> x_next).  Copies host->device, steps, copies back."""
+        x_curr, x_prev (3n, 1) float64 -> x_next).  Copies the caller's arrays straight to the
+        device and the result straight into ``out`` (no intermediate host copy: a DMA when the
+        arrays live in pinned memory, the driver's pageable path otherwise)."""
         m = self.mesh
         if self._host is None:
-            self._host = [torch.empty(3 * m.n, dtype=torch.float64, pin_memory=True) for _ in range(3)]
+            self._host = True
             self._X = torch.from_numpy(m.X_host.reshape(-1).copy()).to(m.device)
-        hc, hp, hn = self._host
-        hc.numpy()[:] = np.asarray(x_curr, dtype=np.float64).reshape(-1)
-        hp.numpy()[:] = np.asarray(x_prev, dtype=np.float64).reshape(-1)
-        self.u_curr.copy_(hc, non_blocking=True)
-        self.u_prev.copy_(hp, non_blocking=True)
+        xc = torch.from_numpy(np.ascontiguousarray(x_curr, dtype=np.float64).reshape(-1))
+        xp = torch.from_numpy(np.ascontiguousarray(x_prev, dtype=np.float64).reshape(-1))
+        self.u_curr.copy_(xc, non_blocking=xc.is_pinned())
+        self.u_prev.copy_(xp, non_blocking=xp.is_pinned())
         self.u_curr.sub_(self._X)
         self.u_prev.sub_(self._X)
         info = self.step(stream)
         self.u_next.copy_(self.u_curr).add_(self._X)      # u_next is scratch after the rotation
-        hn.copy_(self.u_next, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        res = hn.numpy().reshape(-1, 1)
+        if out is not None and out.dtype == np.float64 and out.flags["C_CONTIGUOUS"] and out.size == 3 * m.n:
+            torch.from_numpy(out.reshape(-1)).copy_(self.u_next)   # synchronous device->host
+            return out, info
+        res = np.empty((3 * m.n, 1), dtype=np.float64)
+        torch.from_numpy(res.reshape(-1)).copy_(self.u_next)
         if out is not None:
             out[...] = res
             return out, info
-        return res.copy(), info
+        return res, info
 
     def displacement(self) -> np.ndarray:
         return self.u_curr.cpu().numpy().copy()

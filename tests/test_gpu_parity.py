@@ -529,6 +529,37 @@ def test_two_level_repeatable(api):
     assert torch.equal(a.u_curr, b.u_curr)
 
 
+def test_step_host_matches_device_steps(api):
+    """The host-buffer entry point (simkit's backward_euler contract) takes the same steps as the
+    device-resident stepper, with pageable or pinned host arrays and with or without ``out``."""
+    import torch
+    from simkit_gb300.beams import beam_small_steady
+    from simkit_gb300.solver import BESolver
+    spec = beam_small_steady()
+    a = BESolver.from_spec(spec, coarse=None)
+    b = BESolver.from_spec(spec, coarse=None)
+    X = spec.X.reshape(-1, 1).astype(np.float64)
+    x_prev, x_curr = X.copy(), X.copy()
+    pinned = torch.empty(X.shape, dtype=torch.float64, pin_memory=True).numpy()
+    for k in range(4):
+        assert a.step().converged
+        if k == 0:
+            x_next, info = b.step_host(x_curr, x_prev)                  # pageable in, new array out
+        elif k == 1:
+            x_next, info = b.step_host(x_curr, x_prev, out=pinned)      # pinned out
+            assert x_next is pinned
+            x_next = x_next.copy()
+        else:
+            pc = torch.empty(X.shape, dtype=torch.float64, pin_memory=True).numpy()
+            pp = torch.empty(X.shape, dtype=torch.float64, pin_memory=True).numpy()
+            pc[...] = x_curr
+            pp[...] = x_prev
+            x_next, info = b.step_host(pc, pp)                           # pinned in
+        assert info.converged
+        assert _rel(x_next.ravel(), X.ravel() + a.displacement()) < 1e-12
+        x_prev, x_curr = x_curr, x_next
+
+
 @pytest.mark.parametrize("material", ["stable-neo-hookean", "macklin-mueller-neo-hookean"])
 def test_double_float_forces_match_fp64(api, material):
     """The mixed-precision stepper's double-float force kernel gives the same Newton residual as
