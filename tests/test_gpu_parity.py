@@ -556,7 +556,10 @@ def test_step_host_matches_device_steps(api):
             pp[...] = x_prev
             x_next, info = b.step_host(pc, pp)                           # pinned in
         assert info.converged
-        assert _rel(x_next.ravel(), X.ravel() + a.displacement()) < 1e-12
+        # step 0 starts from identical state; later steps start from (X + u) - X, which differs from
+        # u by rounding, so the two Newton solves agree to their convergence tolerance (as the
+        # batched and single-instance solvers do)
+        assert _rel(x_next.ravel(), X.ravel() + a.displacement()) < (1e-12 if k == 0 else 1e-7)
         x_prev, x_curr = x_curr, x_next
 
 
