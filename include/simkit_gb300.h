@@ -108,6 +108,16 @@ int skg_fcr_gradient_element_F(int dim, int precision, const double* F, const do
 int skg_fcr_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                               double* H, int64_t t, void* stream);
 
+/* element tier: simkit/energies/linear_elasticity.py.  Same arguments; replace
+ * linear_elasticity_energy_element_F (:43-70), _gradient_element_F (:73-100) and
+ * _hessian_element_F (:103-136, constant in F). */
+int skg_le_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                            double* psi, int64_t t, void* stream);
+int skg_le_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* P, int64_t t, void* stream);
+int skg_le_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                             double* H, int64_t t, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* contact springs: simkit/energies/contact_springs_plane.py:44-200        */
 /* ---------------------------------------------------------------------- */
@@ -179,7 +189,9 @@ typedef enum skg_material {
   SKG_MAT_STABLE_NEO_HOOKEAN = 0,          /* simkit/energies/stable_neo_hookean.py */
   SKG_MAT_MACKLIN_MUELLER_NEO_HOOKEAN = 1, /* simkit/energies/macklin_mueller_neo_hookean.py */
   SKG_MAT_ARAP = 2,                        /* simkit/energies/arap.py (lam unused) */
-  SKG_MAT_FIXED_COROTATED = 3              /* simkit/energies/fcr.py */
+  SKG_MAT_FIXED_COROTATED = 3,             /* simkit/energies/fcr.py */
+  SKG_MAT_LINEAR_ELASTICITY = 4            /* simkit/energies/linear_elasticity.py (Hessian never
+                                              projected, as simkit's) */
 } skg_material;
 
 /* Two-level preconditioner data (optional; pcg_mode 7).  Vertices are grouped

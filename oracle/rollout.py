@@ -27,7 +27,7 @@ from dataclasses import dataclass
 import numpy as np
 import scipy.sparse as sps
 
-from . import contact, corot, fem, mmnh, snh
+from . import contact, corot, fem, linel, mmnh, snh
 from .solvers import BDF2_COEFF, bdf2_target, newton_solver, be_target
 
 
@@ -45,8 +45,8 @@ class BeamRollout:
     def __init__(self, X, T, mu, lam, rho, gravity, pinned, dt, tol=1e-6, max_newton=20, material="snh",
                  planes=None, contact_mass_weighted=True):
         # the elastic energy: 'snh' (stable_neo_hookean.py), 'mmnh' (macklin_mueller_neo_hookean.py),
-        # 'arap' (arap.py) or 'fcr' (fcr.py)
-        self.energy = {"snh": snh, "mmnh": mmnh, "arap": corot.arap, "fcr": corot.fcr}[material]
+        # 'arap' (arap.py), 'fcr' (fcr.py) or 'le' (linear_elasticity.py)
+        self.energy = {"snh": snh, "mmnh": mmnh, "arap": corot.arap, "fcr": corot.fcr, "le": linel}[material]
         # contact springs (contact_springs_plane.py): (k, p, n) per plane, weights = vertex masses or 1
         self.planes = list(planes or [])
         self.contact_mass_weighted = contact_mass_weighted

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import corot, mmnh, snh
+from . import corot, linel, mmnh, snh
 from .psd import psd_project
 from .snh import _block_diag
 
@@ -24,7 +24,9 @@ ELEMENT = {
     "mmnh": (mmnh.energy_element_F, mmnh.gradient_element_F, mmnh.hessian_element_F),
     "arap": (corot.arap._psi, corot.arap._pk1, corot.arap._hess),
     "fcr": (corot.fcr._psi, corot.fcr._pk1, corot.fcr._hess),
+    "le": (linel.energy_element_F, linel.gradient_element_F, linel.hessian_element_F),
 }
+NEVER_PROJECTED = {"le"}   # linear_elasticity_hessian_u ignores psd (linear_elasticity.py:301-333)
 
 
 def _F(u, J, Jx_bar):
@@ -47,6 +49,6 @@ def gradient_u(material, u, J, Jx_bar, mu, lam, vol) -> np.ndarray:
 def hessian_u(material, u, J, Jx_bar, mu, lam, vol, psd: bool = True):
     F = _F(u, J, Jx_bar)
     He = ELEMENT[material][2](F, mu, lam) * np.asarray(vol).reshape(-1, 1, 1)
-    if psd:
+    if psd and material not in NEVER_PROJECTED:
         He = psd_project(He)
     return (J.T @ _block_diag(He) @ J).tocsr()

@@ -28,7 +28,11 @@ _API = {
     "stable_neo_hookean_hessian_u", "macklin_mueller_neo_hookean_energy_u", "macklin_mueller_neo_hookean_gradient_u",
     "macklin_mueller_neo_hookean_hessian_u", "arap_energy_u", "arap_gradient_u", "arap_hessian_u", "fcr_energy_u",
     "fcr_gradient_u", "fcr_hessian_u", "elastic_energy_u", "elastic_gradient_u", "elastic_hessian_u",
-    "elastic_energy_element_F", "elastic_gradient_element_F",
+    "linear_elasticity_energy_element_F", "linear_elasticity_gradient_element_F",
+    "linear_elasticity_hessian_element_F", "linear_elasticity_energy_x", "linear_elasticity_gradient_x",
+    "linear_elasticity_hessian_x", "linear_elasticity_energy_u", "linear_elasticity_gradient_u",
+    "linear_elasticity_hessian_u", "linear_elasticity_energy", "linear_elasticity_gradient",
+    "linear_elasticity_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
     "elastic_hessian_element_F", "elastic_energy_x", "elastic_gradient_x", "elastic_hessian_x",
     "elastic_energy", "elastic_gradient", "elastic_hessian", "contact_springs_plane_energy",
     "contact_springs_plane_gradient", "contact_springs_plane_hessian",

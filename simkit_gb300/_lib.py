@@ -109,6 +109,9 @@ _SIGNATURES = {
     "skg_fcr_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_fcr_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_fcr_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_le_energy_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_le_gradient_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "skg_le_hessian_element_F": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "skg_psd_project": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "skg_contact_plane_terms": (c_i32, [c_vp, c_i64, ctypes.POINTER(ContactPlaneC), c_vp, c_vp, c_vp, c_vp, c_vp,
                                         c_vp]),

@@ -275,7 +275,7 @@ def stable_neo_hookean_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, ps
 # Macklin-Mueller neo-Hookean: simkit/energies/macklin_mueller_neo_hookean.py  #
 # --------------------------------------------------------------------------- #
 _MM = "Macklin-Mueller Neo-Hookean"
-MATERIALS = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1, "arap": 2, "fcr": 3}
+MATERIALS = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1, "arap": 2, "fcr": 3, "linear-elasticity": 4}
 
 
 def macklin_mueller_neo_hookean_energy_element_F(F, mu, lam, precision: str = "fp64"):
@@ -566,6 +566,75 @@ def fcr_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, psd: bool = True)
 
 
 # --------------------------------------------------------------------------- #
+# linear elasticity: simkit/energies/linear_elasticity.py                      #
+# --------------------------------------------------------------------------- #
+_LE = "Linear elasticity"
+
+
+def linear_elasticity_energy_element_F(F, mu, lam, precision: str = "fp64"):
+    """psi = mu |eps|^2 + lam/2 tr(eps)^2, eps = sym(F) - I, (t, 1).  simkit
+    ``linear_elasticity_energy_element_F`` (linear_elasticity.py:43-70)."""
+    return _elem("skg_le_energy_element_F", F, mu, lam, lambda t, d: (t, 1), precision, _LE)
+
+
+def linear_elasticity_gradient_element_F(F, mu, lam, precision: str = "fp64"):
+    """P = mu (F + F^T - 2 I) + lam tr(F - I) I, (t, d, d).  simkit ``linear_elasticity_gradient_element_F`` (:73-100)."""
+    return _elem("skg_le_gradient_element_F", F, mu, lam, lambda t, d: (t, d, d), precision, _LE)
+
+
+def linear_elasticity_hessian_element_F(F, mu, lam, precision: str = "fp64"):
+    """mu (I + T) + lam vec(I) vec(I)^T, (t, d*d, d*d).  simkit ``linear_elasticity_hessian_element_F`` (:103-136)."""
+    return _elem("skg_le_hessian_element_F", F, mu, lam, lambda t, d: (t, d * d, d * d), precision, _LE)
+
+
+def linear_elasticity_energy_x(X, J, mu, lam, vol) -> float:
+    """simkit ``linear_elasticity_energy_x`` (:142-167)."""
+    return _energy_x(X, J, mu, lam, vol, MATERIALS["linear-elasticity"])
+
+
+def linear_elasticity_gradient_x(X, J, mu, lam, vol):
+    """simkit ``linear_elasticity_gradient_x`` (:170-196)."""
+    return _gradient_x(X, J, mu, lam, vol, MATERIALS["linear-elasticity"])
+
+
+def linear_elasticity_hessian_x(X, J, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """J^T blockdiag(vol He) J; ``psd`` is accepted and has no effect, as in simkit
+    ``linear_elasticity_hessian_x`` (:199-230): the Hessian is constant and PSD."""
+    return _hessian_x(X, J, mu, lam, vol, MATERIALS["linear-elasticity"], psd, precision)
+
+
+def linear_elasticity_energy_u(u, J, Jx_bar, mu, lam, vol) -> float:
+    """simkit ``linear_elasticity_energy_u`` (:236-267)."""
+    return _energy_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["linear-elasticity"])
+
+
+def linear_elasticity_gradient_u(u, J, Jx_bar, mu, lam, vol):
+    """simkit ``linear_elasticity_gradient_u`` (:270-298)."""
+    return _gradient_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["linear-elasticity"])
+
+
+def linear_elasticity_hessian_u(u, J, Jx_bar, mu, lam, vol, psd: bool = True, precision: str = "fp64"):
+    """simkit ``linear_elasticity_hessian_u`` (:301-333); ``psd`` has no effect."""
+    return _hessian_u(u, J, Jx_bar, mu, lam, vol, MATERIALS["linear-elasticity"], psd, precision)
+
+
+def linear_elasticity_energy(X, T, mu, lam, U: Optional[np.ndarray] = None) -> float:
+    """simkit ``linear_elasticity_energy`` (:339-364)."""
+    return linear_elasticity_energy_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T))
+
+
+def linear_elasticity_gradient(X, T, mu, lam, U: Optional[np.ndarray] = None):
+    """simkit ``linear_elasticity_gradient`` (:367-392)."""
+    return linear_elasticity_gradient_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T))
+
+
+def linear_elasticity_hessian(X, T, mu, lam, U: Optional[np.ndarray] = None, psd: bool = True):
+    """simkit ``linear_elasticity_hessian`` (:395-423)."""
+    return linear_elasticity_hessian_x(X if U is None else U, deformation_jacobian(X, T), mu, lam, volume(X, T),
+                                       psd=psd)
+
+
+# --------------------------------------------------------------------------- #
 # contact springs: simkit/energies/contact_springs_plane.py:44-200             #
 # --------------------------------------------------------------------------- #
 def _contact(X, k, p, n, M):
@@ -630,7 +699,8 @@ def contact_springs_plane_hessian(X, k: float, p, n, M=None, return_contact_inds
 # --------------------------------------------------------------------------- #
 # material dispatch: simkit/energies/elastic.py                               #
 # --------------------------------------------------------------------------- #
-_PREFIX = {"macklin-mueller-neo-hookean": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr"}
+_PREFIX = {"macklin-mueller-neo-hookean": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr",
+           "linear-elasticity": "linear_elasticity"}
 
 
 def _material(material, lam_args):
@@ -638,8 +708,6 @@ def _material(material, lam_args):
     take no lam (simkit/energies/elastic.py passes lam to every material but ARAP)."""
     if material in _PREFIX:
         return _PREFIX[material], (() if material == "arap" else lam_args)
-    if material == "linear-elasticity":
-        raise NotImplementedError(f"material {material!r} has no GPU kernels in this package")
     raise ValueError("Unknown material type: " + str(material))
 
 

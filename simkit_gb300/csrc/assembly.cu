@@ -52,19 +52,20 @@ __device__ __forceinline__ void load_dinv(const R* __restrict__ dinv, int64_t t,
 }
 
 // -------------------------------------------------------- tet Hessians ---
-template <typename R>
+template <typename R, bool LE>
 __device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e, int disp, int project,
                                                  R* __restrict__ hbuf);
 // FP32: at most 168 registers so that 3 blocks fit an SM (measured 1.60 -> 1.32 ms of Hessian
 // evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills); FP64 unbounded.
-template <typename R>
+// LE: the instantiation for linear-elasticity meshes (constant stiffness, no eigensystem)
+template <typename R, bool LE = false>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 3 : 1) k_tet_hessian(TetArgs<R> a, int disp, int project,
                                                                             R* __restrict__ hbuf) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= a.t) return;
-  tet_hessian_body(a, e, disp, project, hbuf);
+  tet_hessian_body<R, LE>(a, e, disp, project, hbuf);
 }
-template <typename R>
+template <typename R, bool LE>
 __device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e, int disp, int project,
                                                  R* __restrict__ hbuf) {
   if (a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]) return;
@@ -85,7 +86,10 @@ __device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e,
   add_fbar(a, e, G);
   shape_grads(D, gN);
   const R vol = __ldg(a.vol + e), mu = __ldg(a.mu + e), lam = __ldg(a.lam + e);
-  snh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
+  if constexpr (LE)
+    le_tet_hessian<R>(mu, lam, vol, gN, out);
+  else
+    nh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
   R* o = hbuf + (int64_t)kHStride * e;
   if constexpr (sizeof(R) == 4) {
 #pragma unroll
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
   disp_grad(du, D, G);
   add_fbar(a, e, G);
   const double vol = a.vol[e], mu = a.mu[e], lam = a.lam[e];
-  const int mat = COROT ? a.material : (a.material == kMatMMNH ? kMatMMNH : kMatSNH);
+  const int mat = COROT ? a.material : (a.material == kMatMMNH || a.material == kMatLE ? a.material : kMatSNH);
   if (COROT ? mat == kMatARAP : false) {
     if (disp) arap_pk1_disp<double>(G, mu, P);
     else arap_pk1<double>(G, mu, P);
@@ -257,6 +261,9 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
   } else if (mat == kMatMMNH) {
     if (disp) mmnh_pk1_disp<double>(G, mu, lam, P);
     else mmnh_pk1<double>(G, mu, lam, P);
+  } else if (mat == kMatLE) {
+    if (disp) le_pk1_disp_d<double, 3>(G, mu, lam, P);
+    else le_pk1_d<double, 3>(G, mu, lam, P);
   } else {
     if (disp) snh_pk1_disp<double>(G, mu, lam, P);
     else snh_pk1<double>(G, mu, lam, P);
@@ -270,7 +277,7 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
       f[3 * b + i] = vol * (P[3 * i] * gN[3 * b] + P[3 * i + 1] * gN[3 * b + 1] + P[3 * i + 2] * gN[3 * b + 2]);
 }
 
-// Double-float forces of the mixed-precision stepper (neo-Hookean materials,
+// Double-float forces of the mixed-precision stepper (neo-Hookean and linear materials,
 // displacement form): the f_a of k_tet_forces evaluated in double-float
 // arithmetic (dfloat.cuh) from the FP32 hi/lo splits of u (uh, ul) and of Dinv
 // (dinv_hi = dinv32, dinv_lo), so that only the three material loads touch the
@@ -301,6 +308,8 @@ __global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const 
   const DF vol(a.vol[e]), mu(a.mu[e]), lam(a.lam[e]);
   if (a.material == kMatMMNH)
     mmnh_pk1_disp<DF>(G, mu, lam, P);
+  else if (a.material == kMatLE)
+    le_pk1_disp_d<DF, 3>(G, mu, lam, P);
   else
     snh_pk1_disp<DF>(G, mu, lam, P);
   shape_grads(D, gN);
@@ -516,7 +525,10 @@ __global__ void k_split(const double* __restrict__ u, int64_t n, float* __restri
 template <typename R>
 int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s) {
   if (a.t == 0) return SKG_OK;
-  k_tet_hessian<R><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
+  if (a.material == kMatLE)
+    k_tet_hessian<R, true><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
+  else
+    k_tet_hessian<R, false><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
   SKG_LAUNCHED();
   return SKG_OK;
 }
@@ -693,7 +705,7 @@ int check_mesh(const skg_tet_mesh* m, int precision) {
   if (precision == SKG_MIXED && (!m->dinv32 || !m->mat32))
     return fail(SKG_ERR_ARG, "mixed precision needs the FP32 mesh copies");
   if (precision != SKG_MIXED && precision != SKG_FP64) return fail(SKG_ERR_ARG, "unknown precision %d", precision);
-  if (m->material < SKG_MAT_STABLE_NEO_HOOKEAN || m->material > SKG_MAT_FIXED_COROTATED)
+  if (m->material < SKG_MAT_STABLE_NEO_HOOKEAN || m->material > SKG_MAT_LINEAR_ELASTICITY)
     return fail(SKG_ERR_ARG, "unknown material %d", m->material);
   if (m->coarse) {
     const skg_coarse* c = m->coarse;

@@ -26,7 +26,7 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
 
 // ------------------------------------------------------------ element F --
 // MAT: kMatSNH (stable_neo_hookean.py), kMatMMNH (macklin_mueller_neo_hookean.py),
-// kMatARAP (arap.py) or kMatFCR (fcr.py)
+// kMatARAP (arap.py), kMatFCR (fcr.py) or kMatLE (linear_elasticity.py)
 template <typename R, int D, int MAT>
 __global__ void k_elem_energy(const double* __restrict__ F, const double* __restrict__ mu,
                               const double* __restrict__ lam, double* __restrict__ psi, int64_t t) {
@@ -285,6 +285,21 @@ int skg_fcr_gradient_element_F(int dim, int precision, const double* F, const do
 int skg_fcr_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
                               double* H, int64_t t, void* stream) {
   return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatFCR));
+}
+
+int skg_le_energy_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                            double* psi, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, psi, t, stream, SKG_ELEM(k_elem_energy, kMatLE));
+}
+
+int skg_le_gradient_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                              double* P, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, P, t, stream, SKG_ELEM(k_elem_pk1, kMatLE));
+}
+
+int skg_le_hessian_element_F(int dim, int precision, const double* F, const double* mu, const double* lam,
+                             double* H, int64_t t, void* stream) {
+  return launch_elem(dim, precision, F, mu, lam, H, t, stream, SKG_ELEM(k_elem_hessian, kMatLE));
 }
 #undef SKG_ELEM
 

@@ -330,7 +330,7 @@ template <typename R> SK_HD void mmnh_hessian4(const R* F, R mu, R lam, R* H) {
 }
 
 // materials of the per-tet kernels
-enum : int { kMatSNH = 0, kMatMMNH = 1, kMatARAP = 2, kMatFCR = 3 };
+enum : int { kMatSNH = 0, kMatMMNH = 1, kMatARAP = 2, kMatFCR = 3, kMatLE = 4 };
 
 // --------------------------------------------------------------------------
 // symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations
@@ -613,8 +613,63 @@ template <typename R> SK_HD void fcr_hessian4(const R* F, R mu, R lam, R* H) {
   corot_twist4(F, R(2) * mu, H);
 }
 
+// --------------------------------------------------------------------------
+// Linear (small-strain) elasticity (simkit/energies/linear_elasticity.py:43-136):
+//   psi = mu |eps|^2 + lam/2 tr(eps)^2,  eps = (F + F^T)/2 - I
+//   P   = mu (F + F^T - 2 I) + lam tr(F - I) I
+//   H   = mu (I + T) + lam vec(I) vec(I)^T   (T: vec(X) -> vec(X^T)), constant and PSD;
+// simkit applies no PSD projection to it.  In displacement form eps = sym(G) exactly.
+// --------------------------------------------------------------------------
+template <typename R, int D> SK_HD R le_dpsi_d(const R* G, R mu, R lam) {
+  R e2 = 0, tr = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    tr += G[(D + 1) * i];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const R e = R(0.5) * (G[D * i + j] + G[D * j + i]);
+      e2 += e * e;
+    }
+  }
+  return mu * e2 + R(0.5) * lam * tr * tr;
+}
+template <typename R, int D> SK_HD void le_pk1_disp_d(const R* G, R mu, R lam, R* P) {
+  R tr = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) tr += G[(D + 1) * i];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) P[D * i + j] = mu * (G[D * i + j] + G[D * j + i]) + (i == j ? lam * tr : R(0));
+}
+template <typename R, int D> SK_HD void le_grad_of(const R* F, R* G) {
+#pragma unroll
+  for (int k = 0; k < D * D; ++k) G[k] = F[k] - ((k % (D + 1) == 0) ? R(1) : R(0));
+}
+template <typename R, int D> SK_HD R le_psi_d(const R* F, R mu, R lam) {
+  R G[D * D];
+  le_grad_of<R, D>(F, G);
+  return le_dpsi_d<R, D>(G, mu, lam);
+}
+template <typename R, int D> SK_HD void le_pk1_d(const R* F, R mu, R lam, R* P) {
+  R G[D * D];
+  le_grad_of<R, D>(F, G);
+  le_pk1_disp_d<R, D>(G, mu, lam, P);
+}
+template <typename R, int D> SK_HD void le_hessian_d(R mu, R lam, R* H) {
+  constexpr int N = D * D;
+#pragma unroll
+  for (int p = 0; p < N; ++p)
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      const int i = p / D, j = p % D, k = q / D, l = q % D;
+      H[N * p + q] = mu * (R(i == k && j == l) + R(i == l && j == k)) + lam * R(i == j && k == l);
+    }
+}
+
 // element-tier dispatch over material and dimension (F is row-major D x D)
 template <typename R, int D> SK_HD R elem_psi(int mat, const R* F, R mu, R lam) {
+  if (mat == kMatLE) return le_psi_d<R, D>(F, mu, lam);
   if (D == 3) return mat == kMatMMNH ? mmnh_psi(F, mu, lam)
                    : mat == kMatARAP ? arap_psi(F, mu)
                    : mat == kMatFCR  ? fcr_psi(F, mu, lam) : snh_psi(F, mu, lam);
@@ -623,7 +678,9 @@ template <typename R, int D> SK_HD R elem_psi(int mat, const R* F, R mu, R lam) 
        : mat == kMatFCR  ? fcr_psi2(F, mu, lam) : snh_psi2(F, mu, lam);
 }
 template <typename R, int D> SK_HD void elem_pk1(int mat, const R* F, R mu, R lam, R* P) {
-  if (D == 3) {
+  if (mat == kMatLE) {
+    le_pk1_d<R, D>(F, mu, lam, P);
+  } else if (D == 3) {
     if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
     else if (mat == kMatARAP) arap_pk1(F, mu, P);
     else if (mat == kMatFCR) fcr_pk1(F, mu, lam, P);
@@ -636,7 +693,9 @@ template <typename R, int D> SK_HD void elem_pk1(int mat, const R* F, R mu, R la
   }
 }
 template <typename R, int D> SK_HD void elem_hessian(int mat, const R* F, R mu, R lam, R* H) {
-  if (D == 3) {
+  if (mat == kMatLE) {
+    le_hessian_d<R, D>(mu, lam, H);
+  } else if (D == 3) {
     if (mat == kMatMMNH) mmnh_hessian9(F, mu, lam, H);
     else if (mat == kMatARAP) arap_hessian9(F, mu, H);
     else if (mat == kMatFCR) fcr_hessian9(F, mu, lam, H);
@@ -651,25 +710,29 @@ template <typename R, int D> SK_HD void elem_hessian(int mat, const R* F, R mu, 
 
 // material dispatch of the per-tet kernels (3D)
 template <typename R> SK_HD R mat_dpsi(int mat, const R* G, R mu, R lam) {
+  if (mat == kMatLE) return le_dpsi_d<R, 3>(G, mu, lam);
   if (mat == kMatMMNH) return mmnh_dpsi(G, mu, lam);
   if (mat == kMatARAP) return arap_dpsi(G, mu);
   if (mat == kMatFCR) return fcr_dpsi(G, mu, lam);
   return snh_dpsi(G, mu, lam);
 }
 template <typename R> SK_HD R mat_psi(int mat, const R* F, R mu, R lam) {
+  if (mat == kMatLE) return le_psi_d<R, 3>(F, mu, lam);
   if (mat == kMatMMNH) return mmnh_psi(F, mu, lam);
   if (mat == kMatARAP) return arap_psi(F, mu);
   if (mat == kMatFCR) return fcr_psi(F, mu, lam);
   return snh_psi(F, mu, lam);
 }
 template <typename R> SK_HD void mat_pk1_disp(int mat, const R* G, R mu, R lam, R* P) {
-  if (mat == kMatMMNH) mmnh_pk1_disp(G, mu, lam, P);
+  if (mat == kMatLE) le_pk1_disp_d<R, 3>(G, mu, lam, P);
+  else if (mat == kMatMMNH) mmnh_pk1_disp(G, mu, lam, P);
   else if (mat == kMatARAP) arap_pk1_disp(G, mu, P);
   else if (mat == kMatFCR) fcr_pk1_disp(G, mu, lam, P);
   else snh_pk1_disp(G, mu, lam, P);
 }
 template <typename R> SK_HD void mat_pk1(int mat, const R* F, R mu, R lam, R* P) {
-  if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
+  if (mat == kMatLE) le_pk1_d<R, 3>(F, mu, lam, P);
+  else if (mat == kMatMMNH) mmnh_pk1(F, mu, lam, P);
   else if (mat == kMatARAP) arap_pk1(F, mu, P);
   else if (mat == kMatFCR) fcr_pk1(F, mu, lam, P);
   else snh_pk1(F, mu, lam, P);
@@ -749,9 +812,55 @@ SK_HD void snh_eigensystem(const R* F, R mu, R lam, R vol, R A, R D, R B,
 // Hessian has the form A I + B f f^T + Lc c c^T + D d2J/dF2 - Tw dR/dF
 // (f = vec F, c = vec cof F); the first four terms are lifted analytically, the
 // corotational term as its three rank-1 twist directions.
+// linear elasticity: K_ab = vol (mu (g_a . g_b) I + mu g_b g_a^T + lam g_a g_b^T), constant in F
+// and never projected (simkit/energies/linear_elasticity.py:199-230)
+template <typename R> SK_HD void le_tet_hessian(R mu, R lam, R vol, const R* gN, R* out) {
+  const R vm = vol * mu, vl = vol * lam;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const R* g = gN + 3 * a;
+    const R gg = vm * (g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    R* o = out + 6 * a;
+    o[0] = gg + (vm + vl) * g[0] * g[0];
+    o[1] = (vm + vl) * g[0] * g[1];
+    o[2] = (vm + vl) * g[0] * g[2];
+    o[3] = gg + (vm + vl) * g[1] * g[1];
+    o[4] = (vm + vl) * g[1] * g[2];
+    o[5] = gg + (vm + vl) * g[2] * g[2];
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a + 1; b < 4; ++b) {
+      R* o = out + 24 + 9 * offdiag_index(a, b);
+      const R* ga = gN + 3 * a;
+      const R* gb = gN + 3 * b;
+      const R gg = vm * (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) o[3 * i + k] = (i == k ? gg : R(0)) + vm * ga[k] * gb[i] + vl * ga[i] * gb[k];
+    }
+}
+
+template <typename R>
+SK_HD void nh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J, bool project,
+                          int material);
+
+// any material (the kernels call le_tet_hessian / nh_tet_hessian from separate instantiations)
 template <typename R>
 SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J = R(0.1),
                            bool project = true, int material = kMatSNH) {
+  if (material == kMatLE)
+    le_tet_hessian(mu, lam, vol, gN, out);
+  else
+    nh_tet_hessian(F, mu, lam, vol, gN, out, fallback_J, project, material);
+}
+
+// the neo-Hookean and corotational materials
+template <typename R>
+SK_HD void nh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J, bool project,
+                          int material) {
   R IC = 0;
 #pragma unroll
   for (int k = 0; k < 9; ++k) IC += F[k] * F[k];

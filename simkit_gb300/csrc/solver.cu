@@ -1069,7 +1069,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
 
   // mixed precision, neo-Hookean materials: forces in double-float from the hi/lo split
   // (the FP64 units of GB300 are the bottleneck of the FP64 force kernel)
-  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH);
+  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH || m->material == kMatLE);
   if (dff) {
     SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s));
     info->launches++;
@@ -1515,7 +1515,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   ea.contact = contact;
   int launches = 1;
 
-  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH);
+  const bool dff = sizeof(R) == 4 && (m->material == kMatSNH || m->material == kMatMMNH || m->material == kMatLE);
   if (dff) {
     SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s));
     launches++;

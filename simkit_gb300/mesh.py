@@ -367,9 +367,10 @@ class TetMesh:
 
     def set_energy(self, material):
         """Elastic energy of every tet: 0 / 'stable-neo-hookean', 1 / 'macklin-mueller-neo-hookean',
-        2 / 'arap', 3 / 'fcr'."""
-        code = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1, "arap": 2, "fcr": 3}.get(material, material)
-        if code not in (0, 1, 2, 3):
+        2 / 'arap', 3 / 'fcr', 4 / 'linear-elasticity'."""
+        code = {"stable-neo-hookean": 0, "macklin-mueller-neo-hookean": 1, "arap": 2, "fcr": 3,
+                "linear-elasticity": 4}.get(material, material)
+        if code not in (0, 1, 2, 3, 4):
             raise ValueError(f"unknown material {material!r}")
         self.material = code
         self.c.material = code

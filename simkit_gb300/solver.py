@@ -78,8 +78,8 @@ class BESolver:
         data, else 5), 5 grid-persistent with two barriers per iteration, 7 its two-level form
     integrator : 'be' (simkit/integrators/backward_euler.py) or 'bdf2'
         (simkit/integrators/bdf2.py: four displacement levels, all at rest initially)
-    material : 'stable-neo-hookean', 'macklin-mueller-neo-hookean', 'arap' or 'fcr'
-        (simkit/energies/elastic.py names; 'arap' ignores lam)
+    material : 'stable-neo-hookean', 'macklin-mueller-neo-hookean', 'arap', 'fcr' or
+        'linear-elasticity' (simkit/energies/elastic.py names; 'arap' ignores lam)
     contact_planes : optional list of (k, p, n) contact-spring planes added to the potential
     coarse : two-level PCG preconditioner (block Jacobi + rigid-mode aggregates of box^3 mesh
         spacings): None (one-level), 'auto' or a box size.  Meshes above 24,576 vertices get the

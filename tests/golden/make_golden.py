@@ -22,6 +22,7 @@ Fixtures written next to this script:
 * ``rollout_mmnh_small.npz``: 6x2x2 beam, 8 backward-Euler steps with the Macklin-Mueller energy
 * ``element_arap_{3d,2d}.npz`` / ``element_fcr_{3d,2d}.npz``: ARAP and fixed-corotated element tiers on the same F batches
 * ``rollout_arap_small.npz`` / ``rollout_fcr_small.npz``: 6x2x2 beam, 8 backward-Euler steps with those energies
+* ``element_le_{3d,2d}.npz`` / ``rollout_le_small.npz``: the same for linear elasticity
 * ``beam_u_tier.npz``: 3x2x2 jittered beam: the displacement (_u) tier of all four energies (F = J u + J x_bar
   with x_bar a perturbed pose): energies, gradients and projected / unprojected Hessians
 * ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
@@ -60,7 +61,8 @@ def _import_reference(path):
         from simkit.energies import contact_springs_plane as ref_contact
         from simkit.energies import arap as ref_arap
         from simkit.energies import fcr as ref_fcr
-    return dict(snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
+        from simkit.energies import linear_elasticity as ref_le
+    return dict(le=ref_le, snh=ref_snh, psd_project=psd_project, deformation_jacobian=deformation_jacobian,
                 volume=volume, massmatrix=massmatrix, newton_solver=newton_solver, kinetic=kinetic,
                 mmnh=ref_mmnh, contact=ref_contact, arap=ref_arap, fcr=ref_fcr)
 
@@ -134,6 +136,16 @@ def make_element_corot(ref, d, out, material):
     np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He, He_proj=Hp)
 
 
+def make_element_le(ref, d, out):
+    rng = np.random.default_rng(100 + d)
+    F, mu, lam, vol = element_cases(rng, d)
+    m = ref["le"]
+    psi = m.linear_elasticity_energy_element_F(F, mu, lam)
+    P = m.linear_elasticity_gradient_element_F(F, mu, lam)
+    He = m.linear_elasticity_hessian_element_F(F, mu, lam)
+    np.savez_compressed(out, F=F, mu=mu, lam=lam, vol=vol, psi=psi, P=P, He=He)
+
+
 def make_beam_small(ref, out):
     from simkit_gb300.beams import make_beam
     rng = np.random.default_rng(7)
@@ -175,7 +187,8 @@ def make_beam_u_tier(ref, out):
     res["snh_gradient"] = s.stable_neo_hookean_gradient_u(u, J, Jx_bar, b.mu, b.lam, vol)
     res["snh_hessian"] = s.stable_neo_hookean_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol).toarray()
     res["snh_hessian_raw"] = s.stable_neo_hookean_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol, psd=False).toarray()
-    for tag, mat in (("mmnh", "macklin-mueller-neo-hookean"), ("arap", "arap"), ("fcr", "fcr")):
+    for tag, mat in (("mmnh", "macklin-mueller-neo-hookean"), ("arap", "arap"), ("fcr", "fcr"),
+                     ("le", "linear-elasticity")):
         res[f"{tag}_energy"] = np.array(ref_elastic.elastic_energy_u(u, J, Jx_bar, b.mu, b.lam, vol, mat))
         res[f"{tag}_gradient"] = ref_elastic.elastic_gradient_u(u, J, Jx_bar, b.mu, b.lam, vol, mat)
         res[f"{tag}_hessian"] = ref_elastic.elastic_hessian_u(u, J, Jx_bar, b.mu, b.lam, vol, mat).toarray()
@@ -222,6 +235,12 @@ def _reference_rollout(ref, spec, dt, steps, keep=None, integrator="be", materia
             stable_neo_hookean_energy_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_energy_x(x, J, mu, vol)),
             stable_neo_hookean_gradient_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_gradient_x(x, J, mu, vol)),
             stable_neo_hookean_hessian_x=staticmethod(lambda x, J, mu, lam, vol: a.arap_hessian_x(x, J, mu, vol))))
+    elif material == "le":
+        m = ref["le"]
+        s = type("LE", (), dict(
+            stable_neo_hookean_energy_x=staticmethod(m.linear_elasticity_energy_x),
+            stable_neo_hookean_gradient_x=staticmethod(m.linear_elasticity_gradient_x),
+            stable_neo_hookean_hessian_x=staticmethod(m.linear_elasticity_hessian_x)))
     elif material == "fcr":
         f = ref["fcr"]
         s = type("FCR", (), dict(
@@ -384,16 +403,24 @@ def _write_corot(ref):
         make_rollout_corot_small(ref, os.path.join(HERE, f"rollout_{mat}_small.npz"), mat)
 
 
+def _write_le(ref):
+    make_element_le(ref, 3, os.path.join(HERE, "element_le_3d.npz"))
+    make_element_le(ref, 2, os.path.join(HERE, "element_le_2d.npz"))
+    make_rollout_corot_small(ref, os.path.join(HERE, "rollout_le_small.npz"), "le")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE", "/root/reference"))
     ap.add_argument("--skip-c1", action="store_true")
-    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot, u")
+    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot, le, u")
     a = ap.parse_args()
     ref = _import_reference(a.reference)
     if a.only:
         if "corot" in a.only.split(","):
             _write_corot(ref)
+        if "le" in a.only.split(","):
+            _write_le(ref)
         if "u" in a.only.split(","):
             make_beam_u_tier(ref, os.path.join(HERE, "beam_u_tier.npz"))
         print("fixtures written to", HERE)
@@ -410,6 +437,7 @@ def main():
     make_rollout_contact_small(ref, os.path.join(HERE, "rollout_contact_small.npz"))
     make_cache_file(a.reference, os.path.join(HERE, "cache_reference.npz"))
     _write_corot(ref)
+    _write_le(ref)
     make_beam_u_tier(ref, os.path.join(HERE, "beam_u_tier.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))

@@ -318,6 +318,39 @@ def test_double_float_stress_matches_fp64(hostmath, mat):
     assert rel.max() < 3e-12
 
 
+def test_le_element_math_and_tet_stiffness_match_oracle(hostmath):
+    """Linear elasticity: element math (direct, displacement and 2D forms) and the per-tet
+    stiffness J^T (vol H) J, never projected (linear_elasticity.py:43-230)."""
+    from oracle import linel
+    rng = np.random.default_rng(50)
+    F, mu, lam, vol, gN = _cases(rng)
+    t = F.shape[0]
+    G = np.ascontiguousarray(F - np.eye(3)[None])
+    r = np.zeros(t), np.zeros(t), np.zeros((t, 9)), np.zeros((t, 9)), np.zeros((t, 81))
+    hostmath.h_mat(64, 4, ctypes.c_int64(t), _p(F), _p(G), _p(mu), _p(lam), *map(_p, r))
+    po = linel.energy_element_F(F, mu, lam).ravel()
+    Po = linel.gradient_element_F(F, mu, lam).reshape(t, 9)
+    Ho = linel.hessian_element_F(F, mu, lam)
+    scale = mu + lam
+    assert np.all(np.abs(r[0] - po) <= 1e-13 * scale) and np.all(np.abs(r[1] - po) <= 1e-13 * scale)
+    assert np.all(np.abs(r[2] - Po).max(1) <= 1e-13 * scale) and np.all(np.abs(r[3] - Po).max(1) <= 1e-13 * scale)
+    assert np.array_equal(r[4], Ho.reshape(t, 81))
+    F2 = np.ascontiguousarray(F[:, :2, :2])
+    p2, P2, H2 = np.zeros(t), np.zeros((t, 4)), np.zeros((t, 16))
+    hostmath.h_mat2(64, 4, ctypes.c_int64(t), _p(F2), _p(mu), _p(lam), _p(p2), _p(P2), _p(H2))
+    assert np.all(np.abs(p2 - linel.energy_element_F(F2, mu, lam).ravel()) <= 1e-13 * scale)
+    assert np.all(np.abs(P2 - linel.gradient_element_F(F2, mu, lam).reshape(t, 4)).max(1) <= 1e-13 * scale)
+    for prec, tol in ((64, 1e-14), (32, 1e-6)):
+        out = np.zeros((t, 78))
+        hostmath.h_tet_hessian_mat(prec, 4, ctypes.c_int64(t), _p(F), _p(mu), _p(lam), _p(vol), _p(gN), _p(out),
+                                   ctypes.c_double(0.1))
+        K = _unpack78(out)
+        Ko = np.einsum("taj,tbl,tijkl->taibk", gN, gN,
+                       (Ho * vol[:, None, None]).reshape(t, 3, 3, 3, 3)).reshape(t, 12, 12)
+        err = np.abs(K - Ko).max(axis=(1, 2)) / np.abs(Ko).max(axis=(1, 2))
+        assert err.max() < tol
+
+
 def test_displacement_forms_match_oracle(hostmath):
     rng = np.random.default_rng(6)
     t = 200

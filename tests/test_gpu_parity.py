@@ -251,8 +251,6 @@ def test_mmnh_assembled_tier_matches_oracle(api):
     from oracle import snh as osnh
     e2 = api.stable_neo_hookean_energy_x(x, dJ, spec.mu, spec.lam, vol)
     assert abs(e2 - osnh.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-10 * abs(e2)
-    with pytest.raises(NotImplementedError):
-        api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "linear-elasticity")
     with pytest.raises(ValueError):
         api.elastic_energy_x(x, dJ, spec.mu, spec.lam, vol, "rubber")
 
@@ -361,6 +359,58 @@ def test_corot_be_step_matches_reference_rollout(api, material, precision):
         assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
 
 
+@pytest.mark.parametrize("d", [3, 2])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 2e-6)])
+def test_le_element_tier_matches_reference(api, d, precision, tol):
+    """Linear elasticity element tier (linear_elasticity.py:43-136) against simkit-generated values,
+    directly and through the elastic dispatch (whose psd flag projects the element blocks)."""
+    g = _load(f"element_le_{d}d.npz")
+    F, mu, lam = g["F"], g["mu"], g["lam"]
+    t = len(mu)
+    scale = (mu + lam).reshape(-1)
+    for fn, key in (("energy", "psi"), ("gradient", "P"), ("hessian", "He")):
+        got = getattr(api, f"linear_elasticity_{fn}_element_F")(F, mu, lam, precision=precision)
+        assert np.all(np.abs(got - g[key]).reshape(t, -1).max(1) <= tol * scale * 10), fn
+    assert _rel(api.elastic_hessian_element_F(F, mu, lam, "linear-elasticity", psd=False), g["He"]) < 1e-14
+    proj = api.elastic_hessian_element_F(F, mu, lam, "linear-elasticity", psd=True)
+    assert _rel(proj, np.asarray(api.psd_project(g["He"]))) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_le_assembled_and_rollout_match_reference(api, precision):
+    """Linear elasticity: the _x tier against the oracle (the Hessian is never projected, with or
+    without psd, as simkit's linear_elasticity_hessian_x) and backward Euler against simkit's rollout."""
+    from oracle import fem, linel
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import BESolver
+    rng = np.random.default_rng(10)
+    spec = make_beam(4, 3, 2, ym=np.exp(rng.uniform(np.log(1e5), np.log(1e7), 6 * 24)), pr=0.42, jitter=0.1)
+    X, T = spec.X, spec.T
+    J = fem.deformation_jacobian(X, T)
+    vol = fem.tet_volumes(X, T)
+    x = X + 0.003 * rng.standard_normal(X.shape)
+    dJ = api.deformation_jacobian(X, T)
+    e = api.linear_elasticity_energy_x(x, dJ, spec.mu, spec.lam, vol)
+    assert abs(e - linel.energy_x(x, J, spec.mu, spec.lam, vol)) < 1e-11 * abs(e)
+    assert _rel(api.linear_elasticity_gradient_x(x, dJ, spec.mu, spec.lam, vol),
+                linel.gradient_x(x, J, spec.mu, spec.lam, vol)) < 1e-11
+    Ko = linel.hessian_x(x, J, spec.mu, spec.lam, vol)
+    for psd in (True, False):
+        K = api.linear_elasticity_hessian_x(x, dJ, spec.mu, spec.lam, vol, psd=psd)
+        assert abs(K - Ko).max() < 1e-11 * abs(Ko).max()
+    d = _load("rollout_le_small.npz")
+    nx, ny, nz = (int(v) for v in d["dims"])
+    beam = make_beam(nx, ny, nz, ym=float(d["ym"]), pr=float(d["pr"]))
+    kw = dict(pcg_rtol=1e-10) if precision == "fp64" else {}
+    s = BESolver.from_spec(beam, dt=float(d["dt"]), precision=precision, material="linear-elasticity", **kw)
+    Xb = beam.X.reshape(-1)
+    for step in range(1, int(d["steps"].max()) + 1):
+        info = s.step()
+        assert info.converged, info
+        k = list(d["steps"]).index(step)
+        assert _rel(Xb + s.displacement(), Xb + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+
+
 def test_corot_batched_equals_single(api):
     """A batch of fixed-corotated beams steps like the single-instance solver."""
     from simkit_gb300.batched import BatchedBESolver
@@ -378,11 +428,12 @@ def test_corot_batched_equals_single(api):
         assert _rel(X + b.displacement(i), X + s.displacement()) < 1e-6
 
 
-_U_NAMES = {"snh": "stable_neo_hookean", "mmnh": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr"}
-_U_MATERIAL = {"mmnh": "macklin-mueller-neo-hookean", "arap": "arap", "fcr": "fcr"}
+_U_NAMES = {"snh": "stable_neo_hookean", "mmnh": "macklin_mueller_neo_hookean", "arap": "arap", "fcr": "fcr",
+            "le": "linear_elasticity"}
+_U_MATERIAL = {"mmnh": "macklin-mueller-neo-hookean", "arap": "arap", "fcr": "fcr", "le": "linear-elasticity"}
 
 
-@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr"])
+@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr", "le"])
 def test_u_tier_matches_reference(api, material):
     """The displacement tier F = J u + Jx_bar (snh.py:544-648 and the *_u functions of the other
     energies, elastic.py:151-746) on the device against simkit-generated values."""

@@ -151,7 +151,17 @@ def test_corot_element_tier_matches_reference(material, d):
     assert _rel(psd_project(He * g["vol"].reshape(-1, 1, 1)), g["He_proj"]) < 1e-9
 
 
-@pytest.mark.parametrize("material", ["arap", "fcr"])
+@pytest.mark.parametrize("d", [3, 2])
+def test_le_element_tier_matches_reference(d):
+    """Linear elasticity element tier (linear_elasticity.py:43-136) against reference values."""
+    from oracle import linel
+    g = _load(f"element_le_{d}d.npz")
+    assert _rel(linel.energy_element_F(g["F"], g["mu"], g["lam"]), g["psi"]) < 1e-13
+    assert _rel(linel.gradient_element_F(g["F"], g["mu"], g["lam"]), g["P"]) < 1e-13
+    assert _rel(linel.hessian_element_F(g["F"], g["mu"], g["lam"]), g["He"]) < 1e-14
+
+
+@pytest.mark.parametrize("material", ["arap", "fcr", "le"])
 def test_rollout_corot_small_matches_reference(material):
     d = _load(f"rollout_{material}_small.npz")
     nx, ny, nz = (int(v) for v in d["dims"])
@@ -163,7 +173,7 @@ def test_rollout_corot_small_matches_reference(material):
     assert [i.iters for i in infos] == list(d["iters"])
 
 
-@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr"])
+@pytest.mark.parametrize("material", ["snh", "mmnh", "arap", "fcr", "le"])
 def test_u_tier_matches_reference(material):
     """The displacement tier (F = J u + Jx_bar) of all four energies against simkit's *_u
     functions on a jittered beam with an arbitrary reference pose."""
