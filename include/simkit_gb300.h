@@ -328,6 +328,10 @@ typedef struct skg_be_params {
                                iteration of this step, 1 = at every Newton iteration, -1 = not
                                at all: reuse the inverse an earlier call built in the same
                                workspace for the same mesh (the caller guarantees one exists) */
+  int32_t stop_rule;        /* skg_be_step: 0 = relative residual ||g|| / ||g(x_tilde)|| < tol
+                               (SKG_ERR_NOT_CONVERGED after max_newton); 1 = simkit's newton_solver
+                               (solvers/newton.py:43-75): at least one iteration, stop once
+                               ||alpha dx|| < tol, at most max_newton iterations, no status */
 } skg_be_params;
 
 typedef struct skg_be_state {

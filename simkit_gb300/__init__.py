@@ -35,7 +35,7 @@ _API = {
     "linear_elasticity_hessian", "elastic_energy_element_F", "elastic_gradient_element_F",
     "elastic_hessian_element_F", "elastic_energy_x", "elastic_gradient_x", "elastic_hessian_x",
     "elastic_energy", "elastic_gradient", "elastic_hessian", "contact_springs_plane_energy",
-    "contact_springs_plane_gradient", "contact_springs_plane_hessian",
+    "contact_springs_plane_gradient", "contact_springs_plane_hessian", "ElasticPotential",
 }
 
 

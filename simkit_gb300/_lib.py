@@ -70,7 +70,7 @@ class BEParamsC(ctypes.Structure):
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
         ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
         ("n_planes", c_i32), ("contact_mass_weighted", c_i32), ("planes", ctypes.POINTER(ContactPlaneC)),
-        ("coarse_refresh", c_i32),
+        ("coarse_refresh", c_i32), ("stop_rule", c_i32),
     ]
 
 

@@ -896,10 +896,105 @@ def newton_solver(x0, energy_func, gradient_func, hessian_func, tolerance=1e-6, 
     return x
 
 
+class ElasticPotential:
+    """V(x) = sum_e vol_e psi(F_e(x)) - f_ext . x for one tet mesh, with simkit's closure signatures:
+    ``energy(x) -> float``, ``gradient(x) -> (3n, 1)``, ``hessian(x) -> sparse (3n, 3n)`` (PSD-projected
+    element blocks, as simkit's ``*_hessian_x`` default), x the (3n, 1) positions.
+
+    Handed to ``backward_euler`` as ``(pot.energy, pot.gradient, pot.hessian)`` with a lumped
+    (diagonal) mass matrix, the whole Newton solve runs on the device (``BESolver`` with simkit's
+    stop rule ``||alpha dx|| < tolerance``, at most ``max_iter`` iterations, FP64 with the linear
+    solves to 1e-12); any other closures take the closure path, as in simkit.
+    """
+
+    def __init__(self, X, T, mu, lam, material: str = "stable-neo-hookean", f_ext=None):
+        self.X = np.asarray(X, dtype=np.float64)
+        self.T = np.asarray(T)
+        self.mu = np.asarray(mu, dtype=np.float64).reshape(-1)
+        self.lam = np.asarray(lam, dtype=np.float64).reshape(-1)
+        if material not in MATERIALS:
+            raise ValueError("Unknown material type: " + str(material))
+        self.material = material
+        self.J = deformation_jacobian(self.X, self.T)
+        self.vol = volume(self.X, self.T)
+        n3 = self.X.size
+        self.f_ext = np.zeros((n3, 1)) if f_ext is None else np.asarray(f_ext, dtype=np.float64).reshape(n3, 1)
+        self._steppers = {}
+
+    def _args(self):
+        return self.J, self.mu, self.lam, self.vol, MATERIALS[self.material]
+
+    def energy(self, x) -> float:
+        J, mu, lam, vol, code = self._args()
+        return _energy_x(x, J, mu, lam, vol, code) - float((self.f_ext.T @ np.asarray(x).reshape(-1, 1)).item())
+
+    def gradient(self, x):
+        J, mu, lam, vol, code = self._args()
+        return _gradient_x(x, J, mu, lam, vol, code) - self.f_ext
+
+    def hessian(self, x):
+        J, mu, lam, vol, code = self._args()
+        return _hessian_x(x, J, mu, lam, vol, code, True, "fp64")
+
+    def stepper(self, h: float, mass):
+        """The device stepper for step h and per-vertex masses (cached)."""
+        from .solver import BESolver
+        key = (float(h), np.asarray(mass).tobytes())
+        if key not in self._steppers:
+            self._steppers[key] = BESolver(self.X, self.T, self.mu, self.lam, dt=float(h), precision="fp64",
+                                           pcg_rtol=1e-12, pcg_max_iter=20000, material=self.material,
+                                           mass=mass, f_ext=self.f_ext)
+        return self._steppers[key]
+
+
+def _potential_of(*funcs):
+    """The ElasticPotential whose energy, gradient and hessian methods these are, else None."""
+    owners = [getattr(f, "__self__", None) for f in funcs]
+    names = [getattr(getattr(f, "__func__", None), "__name__", None) for f in funcs]
+    if (isinstance(owners[0], ElasticPotential) and all(o is owners[0] for o in owners)
+            and names == ["energy", "gradient", "hessian"]):
+        return owners[0]
+    return None
+
+
+def _vertex_masses(M, n: int):
+    """Per-vertex masses of a diagonal (3n, 3n) mass matrix with equal entries per vertex, else None."""
+    if sps.issparse(M):
+        d = np.asarray(M.diagonal(), dtype=np.float64)
+        if M.shape != (3 * n, 3 * n) or abs(M - sps.diags(d)).max() != 0.0:
+            return None
+    else:
+        A = np.asarray(M, dtype=np.float64)
+        if A.shape != (3 * n, 3 * n):
+            return None
+        d = np.diagonal(A).copy()
+        if np.count_nonzero(A - np.diag(d)):
+            return None
+    dv = d.reshape(n, 3)
+    if not np.all(dv == dv[:, :1]):
+        return None
+    return dv[:, 0].copy()
+
+
 def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, h, tolerance: float = 1e-6,
                    max_iter: int = 1, do_line_search: bool = True, return_info: bool = False):
     """simkit ``backward_euler`` (integrators/backward_euler.py:27-91): minimise
-    V(x) + 1/(2h^2) (x - x~)^T M (x - x~), x~ = 2 x_curr - x_prev, by ``newton_solver``."""
+    V(x) + 1/(2h^2) (x - x~)^T M (x - x~), x~ = 2 x_curr - x_prev, by ``newton_solver``.
+
+    With the closures of an ``ElasticPotential`` and a lumped M (host arrays, no ``return_info``)
+    the step runs on the device with the same Newton contract; otherwise the closures are called.
+    """
+    pot = _potential_of(energy_func, gradient_func, hessian_func)
+    if pot is not None and not return_info and isinstance(x_curr, np.ndarray) and isinstance(x_prev, np.ndarray):
+        mass = _vertex_masses(M, pot.X.shape[0])
+        if mass is not None:
+            solver = pot.stepper(h, mass)
+            solver.params.tol = float(tolerance)
+            solver.params.max_newton = int(max_iter)
+            solver.params.do_line_search = int(do_line_search)
+            solver.params.stop_rule = 1
+            x_next, _ = solver.step_host(x_curr, x_prev)
+            return x_next
     x_tilde = x_curr + h * ((x_curr - x_prev) / h)
 
     def energy(x):

@@ -687,17 +687,19 @@ __global__ void k_apply_step(double* __restrict__ u, const R* __restrict__ dx, d
     if (!(pinned && pinned[3 * v + c])) u[3 * v + c] += step * dd[c];
 }
 
-// g . dx (FP64)
+// g . dx and dx . dx (FP64): the Armijo slope and the step norm of simkit's stop rule
 template <typename R>
 __global__ void __launch_bounds__(kBlock) k_dot_g(const double* __restrict__ g, const R* __restrict__ dx, int64_t n,
                                                   double* partials, unsigned* counter, double* out) {
-  double acc[1] = {0.0};
+  double acc[2] = {0.0, 0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += stride) {
     const Vec3<R> d = ld3c(dx, v);
-    acc[0] += g[3 * v] * double(d.x) + g[3 * v + 1] * double(d.y) + g[3 * v + 2] * double(d.z);
+    const double x = double(d.x), y = double(d.y), z = double(d.z);
+    acc[0] += g[3 * v] * x + g[3 * v + 1] * y + g[3 * v + 2] * z;
+    acc[1] += x * x + y * y + z * z;
   }
-  grid_sum<1, kBlock>(acc, partials, counter, out);
+  grid_sum<2, kBlock>(acc, partials, counter, out);
 }
 
 // padded vector -> simkit layout (3n), FP64
@@ -1129,10 +1131,13 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   SKG_TRY(energy(nullptr, 0.0, ecur));
   const double eps_r = mixed ? 5.96e-8 : 1.11e-16;
   double res_prev = 1.0, eta_prev = 0.0;
-  for (int it = 0; it < prm->max_newton && r0 > 0.0; ++it) {
-    const double res = sqrt(gg) / r0;
+  // stop_rule 1 is simkit's newton_solver (solvers/newton.py:43-75): at least one iteration, then
+  // stop once ||alpha dx|| < tol, at most max_newton iterations, no convergence status
+  const bool simkit_stop = prm->stop_rule == 1;
+  for (int it = 0; it < prm->max_newton && (r0 > 0.0 || simkit_stop); ++it) {
+    const double res = r0 > 0.0 ? sqrt(gg) / r0 : 0.0;
     info->residual = res;
-    if (res < prm->tol) break;
+    if (!simkit_stop && res < prm->tol) break;
     // PCG forcing term: fixed (pcg_rtol > 0) or Eisenstat-Walker choice 2
     // (gamma 0.9, exponent 2, safeguarded) capped at |pcg_rtol|, never
     // tighter than what brings the residual to a quarter of tol
@@ -1193,11 +1198,12 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
       break;
     }
     // Armijo backtracking (simkit/backtracking_line_search.py:56-67)
-    double slope;
+    double slope_dd[2];
     k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s>>>(w.g, pv.x, n, w.partials, w.counter, w.scal + S_SLOPE);
     SKG_LAUNCHED();
     info->launches++;
-    SKG_TRY(read_scalars(w.scal + S_SLOPE, &slope, 1, s));
+    SKG_TRY(read_scalars(w.scal + S_SLOPE, slope_dd, 2, s));
+    const double slope = slope_dd[0];
     double step = 1.0, enew[2] = {ecur[0], ecur[1]};
     bool accepted = !prm->do_line_search;
     if (prm->do_line_search) {
@@ -1235,9 +1241,11 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
       info->status = SKG_ERR_NONFINITE;
       break;
     }
-    info->residual = sqrt(gg) / r0;
+    info->residual = r0 > 0.0 ? sqrt(gg) / r0 : 0.0;
+    if (simkit_stop && step * sqrt(slope_dd[1]) < prm->tol) break;
   }
-  if (info->status == SKG_OK && info->residual >= prm->tol && r0 > 0.0) info->status = SKG_ERR_NOT_CONVERGED;
+  if (!simkit_stop && info->status == SKG_OK && info->residual >= prm->tol && r0 > 0.0)
+    info->status = SKG_ERR_NOT_CONVERGED;
   info->energy = ecur[0];
   return SKG_OK;
 }

@@ -86,6 +86,8 @@ class BESolver:
         whole-mesh form (box 8 by default; the grid PCG, pcg_mode 3 or 7), smaller ones the
         per-instance form (box 4; the thread-block-cluster PCG, pcg_mode 2 or 3)
     coarse_form : 'auto' (by size, as above), 'grid' or 'cluster'
+    mass, f_ext : per-vertex lumped masses (n) and external forces (3n) instead of the ones
+        ``rho`` and ``gravity`` give
     coarse_refresh : 'step' (coarse inverse rebuilt at the first Newton iteration of each step),
         'newton' (at every Newton iteration) or an int k (default 4: at the first Newton iteration
         of every k-th step; the steps between reuse it: the preconditioner stays SPD, only less
@@ -96,7 +98,7 @@ class BESolver:
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
                  material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh=4, coarse_form="auto"):
+                 coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.set_energy(material)
@@ -104,10 +106,17 @@ class BESolver:
         dev = m.device
         X = m.X_host
         self.precision = PRECISIONS[precision]
-        mass = lumped_mass(X, m.T_host, rho)
+        mass = lumped_mass(X, m.T_host, rho) if mass is None else np.asarray(mass, dtype=np.float64).reshape(-1)
+        if mass.size != m.n:
+            raise ValueError("mass needs one lumped value per vertex")
         self.mass = torch.from_numpy(mass).to(dev)
-        g = np.asarray(gravity, dtype=np.float64)
-        self.f_ext = torch.from_numpy((mass[:, None] * g[None, :]).reshape(-1)).to(dev)
+        if f_ext is None:
+            g = np.asarray(gravity, dtype=np.float64)
+            f_ext = (mass[:, None] * g[None, :]).reshape(-1)
+        f_ext = np.asarray(f_ext, dtype=np.float64).reshape(-1)
+        if f_ext.size != 3 * m.n:
+            raise ValueError("f_ext needs 3 values per vertex")
+        self.f_ext = torch.from_numpy(f_ext.copy()).to(dev)
         pin = np.zeros(3 * m.n, np.uint8)
         pv = np.asarray(pinned, dtype=np.int64).ravel()
         pin[(3 * pv[:, None] + np.arange(3)[None, :]).ravel()] = 1

@@ -580,6 +580,35 @@ def test_two_level_repeatable(api):
     assert torch.equal(a.u_curr, b.u_curr)
 
 
+@pytest.mark.parametrize("max_iter,tol", [(1, 1e-6), (20, 1e-9)])
+def test_backward_euler_fast_path_matches_closure_path(api, max_iter, tol):
+    """simkit's backward_euler with an ElasticPotential's closures and a lumped M runs the whole Newton
+    solve on the device (stop once ||alpha dx|| < tol, at most max_iter iterations); the same closures
+    wrapped in lambdas take the closure path.  Both give the same positions."""
+    import scipy.sparse as sps
+    from oracle import fem
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 3, 3, ym=2e5, pr=0.45)
+    X, T = spec.X, spec.T
+    m = fem.lumped_mass(X, T, 1000.0)
+    M = sps.diags(np.repeat(m, 3)).tocsc()
+    f = (m[:, None] * np.array([0.0, -9.8, 0.0])[None, :]).reshape(-1, 1)
+    pot = api.ElasticPotential(X, T, spec.mu, spec.lam, f_ext=f)
+    rng = np.random.default_rng(3)
+    x_prev = X.reshape(-1, 1).copy()
+    x_curr = x_prev + 1e-3 * rng.standard_normal(x_prev.shape)
+    h = 1.0 / 60.0
+    for _ in range(3):
+        fast = api.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h,
+                                  tolerance=tol, max_iter=max_iter)
+        slow = api.backward_euler(x_curr, x_prev, lambda x: pot.energy(x), lambda x: pot.gradient(x),
+                                  lambda x: pot.hessian(x), M, h, tolerance=tol, max_iter=max_iter)
+        assert fast.shape == slow.shape == x_curr.shape
+        assert _rel(fast - x_curr, slow - x_curr) < 1e-6
+        x_prev, x_curr = x_curr, fast
+    assert len(pot._steppers) == 1   # the device path ran (and its stepper was reused)
+
+
 def test_step_host_matches_device_steps(api):
     """The host-buffer entry point (simkit's backward_euler contract) takes the same steps as the
     device-resident stepper, with pageable or pinned host arrays and with or without ``out``."""
