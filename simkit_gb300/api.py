@@ -936,15 +936,31 @@ class ElasticPotential:
         J, mu, lam, vol, code = self._args()
         return _hessian_x(x, J, mu, lam, vol, code, True, "fp64")
 
-    def stepper(self, h: float, mass):
-        """The device stepper for step h and per-vertex masses (cached)."""
+    def stepper(self, h: float, mass, integrator: str = "be"):
+        """The device stepper for step h, per-vertex masses and integrator ('be' or 'bdf2'), cached."""
         from .solver import BESolver
-        key = (float(h), np.asarray(mass).tobytes())
+        key = (float(h), np.asarray(mass).tobytes(), integrator)
         if key not in self._steppers:
             self._steppers[key] = BESolver(self.X, self.T, self.mu, self.lam, dt=float(h), precision="fp64",
                                            pcg_rtol=1e-12, pcg_max_iter=20000, material=self.material,
-                                           mass=mass, f_ext=self.f_ext)
+                                           mass=mass, f_ext=self.f_ext, integrator=integrator)
         return self._steppers[key]
+
+    def _device_step(self, integrator, M, h, tolerance, max_iter, do_line_search, xs):
+        """simkit's Newton contract on the device, or None when M is not lumped."""
+        mass = _vertex_masses(M, self.X.shape[0])
+        if mass is None:
+            return None
+        solver = self.stepper(h, mass, integrator)
+        solver.params.tol = float(tolerance)
+        solver.params.max_newton = int(max_iter)
+        solver.params.do_line_search = int(do_line_search)
+        solver.params.stop_rule = 1
+        if integrator == "bdf2":
+            x_next, _ = solver.step_host(xs[0], xs[1], x_prev2=xs[2], x_prev3=xs[3])
+        else:
+            x_next, _ = solver.step_host(xs[0], xs[1])
+        return x_next
 
 
 def _potential_of(*funcs):
@@ -985,15 +1001,9 @@ def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, 
     the step runs on the device with the same Newton contract; otherwise the closures are called.
     """
     pot = _potential_of(energy_func, gradient_func, hessian_func)
-    if pot is not None and not return_info and isinstance(x_curr, np.ndarray) and isinstance(x_prev, np.ndarray):
-        mass = _vertex_masses(M, pot.X.shape[0])
-        if mass is not None:
-            solver = pot.stepper(h, mass)
-            solver.params.tol = float(tolerance)
-            solver.params.max_newton = int(max_iter)
-            solver.params.do_line_search = int(do_line_search)
-            solver.params.stop_rule = 1
-            x_next, _ = solver.step_host(x_curr, x_prev)
+    if pot is not None and not return_info and all(isinstance(a, np.ndarray) for a in (x_curr, x_prev)):
+        x_next = pot._device_step("be", M, h, tolerance, max_iter, do_line_search, (x_curr, x_prev))
+        if x_next is not None:
             return x_next
     x_tilde = x_curr + h * ((x_curr - x_prev) / h)
 
@@ -1018,7 +1028,14 @@ def bdf2(x_curr, x_prev, x_prev2, x_prev3, energy_func, gradient_func, hessian_f
          max_iter: int = 1, do_line_search: bool = True, return_info: bool = False):
     """simkit ``bdf2`` (integrators/bdf2.py:31-101): minimise V(x) + (9/4)/(2h^2) (x - x~)^T M (x - x~)
     with the BDF2 target x~ = (4/3) x_curr - (1/3) x_prev + (8h/9) v_curr - (2h/9) v_prev, velocities
-    by the second-order backward difference (energies/kinetic.py:63-101), by ``newton_solver``."""
+    by the second-order backward difference (energies/kinetic.py:63-101), by ``newton_solver``.
+    An ``ElasticPotential``'s closures with a lumped M take the device path, as in ``backward_euler``."""
+    pot = _potential_of(energy_func, gradient_func, hessian_func)
+    xs = (x_curr, x_prev, x_prev2, x_prev3)
+    if pot is not None and not return_info and all(isinstance(a, np.ndarray) for a in xs):
+        x_next = pot._device_step("bdf2", M, h, tolerance, max_iter, do_line_search, xs)
+        if x_next is not None:
+            return x_next
     v_curr = (3.0 * x_curr - 4.0 * x_prev + x_prev2) / (2.0 * h)
     v_prev = (3.0 * x_prev - 4.0 * x_prev2 + x_prev3) / (2.0 * h)
     x_tilde = (4.0 / 3.0) * x_curr - (1.0 / 3.0) * x_prev + (8.0 * h / 9.0) * v_curr - (2.0 * h / 9.0) * v_prev

@@ -200,11 +200,13 @@ class BESolver:
                         info.residual, info.min_alpha, info.energy, info.launches, info.t_hessian_ms,
                         info.t_assemble_ms, info.t_pcg_ms, info.t_gradient_ms, info.t_energy_ms)
 
-    def step_host(self, x_curr: np.ndarray, x_prev: np.ndarray, out: np.ndarray = None, stream=None):
+    def step_host(self, x_curr: np.ndarray, x_prev: np.ndarray, out: np.ndarray = None, stream=None,
+                  x_prev2: np.ndarray = None, x_prev3: np.ndarray = None):
         """One step with host positions in and out (simkit's backward_euler contract:
         x_curr, x_prev (3n, 1) float64 -> x_next).  Copies the caller's arrays straight to the
         device and the result straight into ``out`` (no intermediate host copy: a DMA when the
-        arrays live in pinned memory, the driver's pageable path otherwise)."""
+        arrays live in pinned memory, the driver's pageable path otherwise).  A BDF2 solver also
+        takes the positions two and three steps back (simkit's bdf2 contract)."""
         m = self.mesh
         if self._host is None:
             self._host = True
@@ -215,6 +217,13 @@ class BESolver:
         self.u_prev.copy_(xp, non_blocking=xp.is_pinned())
         self.u_curr.sub_(self._X)
         self.u_prev.sub_(self._X)
+        if self.integrator == "bdf2":
+            if x_prev2 is None or x_prev3 is None:
+                raise ValueError("a BDF2 step needs x_prev2 and x_prev3")
+            for dst, src in ((self.u_prev2, x_prev2), (self.u_prev3, x_prev3)):
+                t = torch.from_numpy(np.ascontiguousarray(src, dtype=np.float64).reshape(-1))
+                dst.copy_(t, non_blocking=t.is_pinned())
+                dst.sub_(self._X)
         info = self.step(stream)
         self.u_next.copy_(self.u_curr).add_(self._X)      # u_next is scratch after the rotation
         if out is not None and out.dtype == np.float64 and out.flags["C_CONTIGUOUS"] and out.size == 3 * m.n:

@@ -607,6 +607,16 @@ def test_backward_euler_fast_path_matches_closure_path(api, max_iter, tol):
         assert _rel(fast - x_curr, slow - x_curr) < 1e-6
         x_prev, x_curr = x_curr, fast
     assert len(pot._steppers) == 1   # the device path ran (and its stepper was reused)
+    # BDF2 (integrators/bdf2.py:31-101) through the same two paths
+    xs = [x_prev.copy(), x_prev.copy(), x_prev.copy(), x_curr.copy()]   # x_prev3, x_prev2, x_prev, x_curr
+    for _ in range(2):
+        fast = api.bdf2(xs[3], xs[2], xs[1], xs[0], pot.energy, pot.gradient, pot.hessian, M, h,
+                        tolerance=tol, max_iter=max_iter)
+        slow = api.bdf2(xs[3], xs[2], xs[1], xs[0], lambda x: pot.energy(x), lambda x: pot.gradient(x),
+                        lambda x: pot.hessian(x), M, h, tolerance=tol, max_iter=max_iter)
+        assert _rel(fast - xs[3], slow - xs[3]) < 1e-6
+        xs = xs[1:] + [fast]
+    assert len(pot._steppers) == 2
 
 
 def test_step_host_matches_device_steps(api):
