@@ -238,6 +238,8 @@ __device__ __forceinline__ void assemble_slot(const AsmArgs<R>& a, int64_t s) {
 // --------------------------------------------------------- FP64 forces ---
 // f_a = vol P(F) grad N_a per tet, in FP64 (the Newton residual is formed
 // from these; FP32 cannot resolve 1e-6 relative residuals of stiff beams).
+// The mixed-precision stepper uses the double-float kernel below for the
+// neo-Hookean and linear materials.
 // COROT: the instantiation for ARAP / fixed-corotated meshes (its SVD would cost the
 // neo-Hookean instantiation registers and occupancy).
 template <bool COROT>
