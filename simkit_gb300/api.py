@@ -976,8 +976,10 @@ def _potential_of(*funcs):
 def _vertex_masses(M, n: int):
     """Per-vertex masses of a diagonal (3n, 3n) mass matrix with equal entries per vertex, else None."""
     if sps.issparse(M):
+        if M.shape != (3 * n, 3 * n):
+            return None
         d = np.asarray(M.diagonal(), dtype=np.float64)
-        if M.shape != (3 * n, 3 * n) or abs(M - sps.diags(d)).max() != 0.0:
+        if (sps.csr_matrix(M) - sps.diags(d)).tocsr().count_nonzero():
             return None
     else:
         A = np.asarray(M, dtype=np.float64)
