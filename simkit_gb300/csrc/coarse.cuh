@@ -178,7 +178,7 @@ __device__ __forceinline__ int gj_units(GjShared& g, int np) {
 // units u0, u0 + us, ... of sweep step kb (Pinv already in g.piv)
 __device__ __forceinline__ void gj_step_units(GjShared& g, float* M, int np, int kb, const float* Rw, float* Rn, int u0,
                                               int us) {
-  const int nbk = np / kGjB, ncu = (np + kGjCols - 1) / kGjCols;
+  const int nbk = np / kGjB;
   const int units = g.ustart[nbk];
   const int K0 = kb * kGjB, K1 = K0 + kGjB;
   const int tid = threadIdx.x;

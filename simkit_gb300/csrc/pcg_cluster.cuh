@@ -58,13 +58,15 @@ __device__ __forceinline__ uint32_t cluster_map(uint32_t addr, uint32_t rank) {
   return r;
 }
 __device__ __forceinline__ Vec3<float> ld_cluster3(uint32_t addr, float) {
-  float a, b, c, d;
+  float a, b, c;
+  [[maybe_unused]] float d;   // the record's fourth lane: padding
   asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
                : "=f"(a), "=f"(b), "=f"(c), "=f"(d) : "r"(addr) : "memory");
   return {a, b, c};
 }
 __device__ __forceinline__ Vec3<double> ld_cluster3(uint32_t addr, double) {
-  double a, b, c, d;
+  double a, b, c;
+  [[maybe_unused]] double d;   // padding
   asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(a), "=d"(b) : "r"(addr) : "memory");
   asm volatile("ld.shared::cluster.v2.f64 {%0, %1}, [%2];" : "=d"(c), "=d"(d) : "r"(addr + 16) : "memory");
   return {a, b, c};
