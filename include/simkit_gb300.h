@@ -154,7 +154,9 @@ int skg_psd_project(const double* H, double* out, int64_t n, int d, int method, 
  * Replaces the per-element D of deformation_jacobian (deformation_jacobian.py:43-61)
  * and volume/tetrahedron_volumes (volume.py:14-41, tetrahedron_volumes.py:26-27).
  * X (n,3) f64, T (t,4) i32 -> dinv (9,t) f64 SoA, vol (t) f64.  A degenerate rest
- * tet gives non-finite Dinv entries (simkit's np.linalg.inv raises instead). */
+ * tet gives non-finite Dinv entries (simkit's np.linalg.inv raises instead); a tet
+ * with a vertex index outside [0, n) is not read and gets NaN vol and Dinv.  The
+ * Python layer rejects both (ValueError) before any solve. */
 int skg_tet_setup(const double* X, const int32_t* T, int64_t n, int64_t t, double* dinv, double* vol,
                   void* stream);
 
@@ -420,14 +422,27 @@ int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const 
  * only inputs and outputs.  Its scratch is one fixed device array inside the
  * library (about 1 MB, held by every GPU that loads the library until exit),
  * enough for at most skg_pcg_noalloc_max_rows() block rows (4096, i.e. 12,288
- * unknowns); larger systems return SKG_ERR_CAPACITY.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress) and should
- * come before any stream capture.  All calls share that array, so calls that
- * overlap on the GPU race; serialise them.  Allocates no device memory. */
+ * unknowns); larger systems return SKG_ERR_CAPACITY.  Every call looks up the
+ * array's device address on the current device (cudaGetSymbolAddress); the first
+ * call on a device also loads the library there and should come before any
+ * stream capture.  Each call synchronizes `stream` to read the solve's status.
+ * All calls share that array, so calls that overlap on the GPU race; serialise
+ * them.  Allocates no device memory. */
 int64_t skg_pcg_noalloc_max_rows(void);
 int skg_pcg_bsr64_noalloc(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val,
                           const double* b, double* x, double rtol, int32_t max_iter, int32_t* iters_h,
                           void* stream);
+
+/* Self-test of the bounded device waits (no counterpart in the reference, which
+ * has no device code).  kind 0 runs the grid barrier of the grid-persistent PCG
+ * forms with one of its two blocks never arriving; kind 1 runs the mbarrier wait
+ * of the cluster PCG's bulk-copy pipeline on a phase that never completes.  The
+ * wait gives up after `limit` polls (1..2^24; the solvers use 2^24 for the grid
+ * barrier and 2^20 for the mbarrier) and *status_h receives SKG_ERR_TIMEOUT, the
+ * status the solvers return when a wait gives up; the context stays usable.
+ * Workspace: skg_wait_selftest_workspace_size() bytes.  Synchronizes `stream`. */
+int64_t skg_wait_selftest_workspace_size(void);
+int skg_wait_selftest(int kind, int64_t limit, int32_t* status_h, void* workspace, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* learned warm start: BF16 tensor-core MLP pieces (no simkit counterpart)  */

@@ -304,8 +304,9 @@ constexpr long long kSpinLimit = 1ll << 24;
 // atomic (releasing the block's writes, ordered before it by __syncthreads); the
 // last arrival resets the count and publishes the next generation with a
 // release store; the others poll the generation with acquire loads.  Bounded
-// spin: on timeout err is set and false returned.
-__device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned* gen, volatile double* err) {
+// spin (at most `limit` polls): on timeout err is set and false returned.
+__device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned* gen, volatile double* err,
+                                             long long limit = kSpinLimit) {
   __syncthreads();
   __shared__ int ok_s;
   if (threadIdx.x == 0) {
@@ -317,7 +318,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, volatile unsigned*
     } else {
       long long spins = 0;
       while (ld_acquire_gpu((const unsigned*)gen) == g) {
-        if (++spins > kSpinLimit) {
+        if (++spins > limit) {
           *err = (double)SKG_ERR_TIMEOUT;
           ok = 0;
           break;
@@ -1803,14 +1804,33 @@ int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const 
   return be_step_batched<double>(mesh, batch, params, state, workspace, infos_h, total_h, s);
 }
 
-int64_t skg_pcg_workspace_size(int64_t nbr) {
-  Carve c(nullptr);
-  for (int k = 0; k < 5; ++k) c.take<double>(4 * nbr);
-  c.take<double>(9 * nbr);
-  c.take<double>(8 * kMaxGrid);
-  c.take<unsigned>(16);
-  c.take<double>(64);
-  return c.off + 256;
+}  // extern "C"
+
+namespace skg {
+
+// Scratch of the generic block-Jacobi PCG for nbr block rows, carved from base (sizes only
+// when base is null): five padded vectors, the 3x3 inverses, reduction partials, counters and
+// scalars.  Shared by skg_pcg_bsr64 (caller workspace) and skg_pcg_bsr64_noalloc (fixed array).
+struct PcgScratch {
+  PcgVecs<double> v;
+  double* jinv;
+  double* partials;
+  unsigned* counter;
+  double* scal;
+  int64_t bytes;
+};
+
+static PcgScratch carve_pcg_scratch(void* base, int64_t nbr) {
+  Carve c(base);
+  PcgScratch w{};
+  w.v.x = c.take<double>(4 * nbr); w.v.r = c.take<double>(4 * nbr); w.v.z = c.take<double>(4 * nbr);
+  w.v.p = c.take<double>(4 * nbr); w.v.q = c.take<double>(4 * nbr);
+  w.jinv = c.take<double>(9 * nbr);
+  w.partials = c.take<double>(8 * kMaxGrid);
+  w.counter = c.take<unsigned>(16);
+  w.scal = c.take<double>(64);
+  w.bytes = c.off;
+  return w;
 }
 
 // Generic symmetric solve for newton_solver's spsolve (newton.py:52): FP64
@@ -1836,25 +1856,19 @@ __global__ void k_diag_inverse(int64_t nbr, const int32_t* rowptr, const int32_t
   }
 }
 
-int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
-                  double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* workspace, void* stream) {
-  if (nbr <= 0 || !rowptr || !col || !val || !b || !x || !workspace) return fail(SKG_ERR_ARG, "pcg: bad arguments");
-  cudaStream_t s = as_stream(stream);
-  Carve c(workspace);
-  PcgVecs<double> v;
-  v.x = c.take<double>(4 * nbr); v.r = c.take<double>(4 * nbr); v.z = c.take<double>(4 * nbr);
-  v.p = c.take<double>(4 * nbr); v.q = c.take<double>(4 * nbr);
-  double* jinv = c.take<double>(9 * nbr);
-  double* partials = c.take<double>(8 * kMaxGrid);
-  unsigned* counter = c.take<unsigned>(16);
-  double* scal = c.take<double>(64);
-  SKG_CUDA(cudaMemsetAsync(counter, 0, 16 * sizeof(unsigned), s));
-  k_diag_inverse<<<blocks_for(nbr), kBlock, 0, s>>>(nbr, rowptr, col, val, jinv);
+// The solve: block-Jacobi inverses, the grid-persistent PCG, x unpadded, then a stream
+// synchronize to read the status and the convergence test.
+static int pcg_bsr64_run(const PcgScratch& w, int64_t nbr, const int32_t* rowptr, const int32_t* col,
+                         const double* val, const double* b, double* x, double rtol, int32_t max_iter,
+                         int32_t* iters_h, cudaStream_t s) {
+  // the scratch may hold an earlier call's contents: the reduction counters start at zero
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s));
+  k_diag_inverse<<<blocks_for(nbr), kBlock, 0, s>>>(nbr, rowptr, col, val, w.jinv);
   SKG_LAUNCHED();
-  Bsr<double> A{nbr, rowptr, col, val, jinv};
+  Bsr<double> A{nbr, rowptr, col, val, w.jinv};
   PcgResult pr{};
-  SKG_TRY(pcg_solve<double>(A, b, 1.0, nullptr, v, rtol, max_iter, 1, partials, counter, scal, s, &pr));
-  k_unpad<double><<<blocks_for(nbr), kBlock, 0, s>>>(v.x, nbr, x);
+  SKG_TRY(pcg_solve<double>(A, b, 1.0, nullptr, w.v, rtol, max_iter, 1, w.partials, w.counter, w.scal, s, &pr));
+  k_unpad<double><<<blocks_for(nbr), kBlock, 0, s>>>(w.v.x, nbr, x);
   SKG_LAUNCHED();
   SKG_CUDA(cudaStreamSynchronize(s));
   if (iters_h) *iters_h = pr.iters;
@@ -1863,6 +1877,19 @@ int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const 
     return fail(SKG_ERR_NOT_CONVERGED, "pcg reached %d iterations at relative residual %.3e", pr.iters,
                 sqrt(pr.rr / pr.bb));
   return SKG_OK;
+}
+
+}  // namespace skg
+
+extern "C" {
+
+int64_t skg_pcg_workspace_size(int64_t nbr) { return carve_pcg_scratch(nullptr, nbr).bytes + 256; }
+
+int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const double* val, const double* b,
+                  double* x, double rtol, int32_t max_iter, int32_t* iters_h, void* workspace, void* stream) {
+  if (nbr <= 0 || !rowptr || !col || !val || !b || !x || !workspace) return fail(SKG_ERR_ARG, "pcg: bad arguments");
+  return pcg_bsr64_run(carve_pcg_scratch(workspace, nbr), nbr, rowptr, col, val, b, x, rtol, max_iter, iters_h,
+                       as_stream(stream));
 }
 
 }  // extern "C"
@@ -1880,14 +1907,13 @@ int skg_pcg_bsr64(int64_t nbr, const int32_t* rowptr, const int32_t* col, const 
 // 1 MB that every GPU which loads the library holds until the process exits.
 //
 // Host code cannot pass the array's name to a kernel (on the host it is only
-// a stand-in for the device symbol), so the first call on each device looks
-// the address up with cudaGetSymbolAddress while that device is current and
-// caches it; make that first call before any stream capture.  All calls share
-// the one array: two calls that overlap on the GPU (other streams, other host
-// threads) race on it and must be serialised by the caller.
+// a stand-in for the device symbol), so every call looks the address up with
+// cudaGetSymbolAddress on the current device; the first call on a device also
+// loads the library's module there, so make it before any stream capture.
+// Each call synchronizes its stream to read the solve's status.  All calls
+// share the one array: two calls that overlap on the GPU (other streams, other
+// host threads) race on it and must be serialised by the caller.
 // ---------------------------------------------------------------------------
-#include <mutex>
-
 namespace skg {
 
 constexpr int64_t kNoAllocMaxRows = 4096;
@@ -1899,22 +1925,12 @@ constexpr int64_t kNoAllocBytes = 5 * al256(4 * kNoAllocMaxRows * (int64_t)sizeo
 
 static __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// device address of the scratch array on the current device (looked up once)
+// device address of the scratch array on the current device, looked up on every call (a host-side
+// lookup; a cached address would go stale if the device's context were torn down and re-created)
 static int noalloc_scratch(void** out) {
-  int dev = 0;
-  SKG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SKG_ERR_CAPACITY, "device ordinal %d not supported", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    SKG_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  SKG_CUDA(cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch));
+  *out = p;
   return SKG_OK;
 }
 
@@ -1934,30 +1950,72 @@ int skg_pcg_bsr64_noalloc(int64_t nbr, const int32_t* rowptr, const int32_t* col
                 (long long)nbr, (long long)kNoAllocMaxRows);
   void* scratch = nullptr;
   SKG_TRY(noalloc_scratch(&scratch));
+  const PcgScratch w = carve_pcg_scratch(scratch, nbr);
+  if (w.bytes > kNoAllocBytes)
+    return fail(SKG_ERR_CAPACITY, "pcg_noalloc: %lld scratch bytes exceed the fixed array of %lld", (long long)w.bytes,
+                (long long)kNoAllocBytes);
+  return pcg_bsr64_run(w, nbr, rowptr, col, val, b, x, rtol, max_iter, iters_h, as_stream(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Self-test of the bounded waits.  Each kernel below runs one production wait
+// helper (grid_barrier of the grid-persistent PCG forms, mbar_wait of the
+// cluster PCG's bulk-copy pipeline) on a condition that nothing ever meets: a
+// grid barrier whose second block never arrives, an mbarrier phase that waits
+// for a second arrival that never comes.  The wait gives up after `limit`
+// polls and the kernel returns SKG_ERR_TIMEOUT through device memory, so a
+// caller can check that a stuck wait ends with a status and leaves the CUDA
+// context usable.  No copy is ever in flight and no other block waits.
+// ---------------------------------------------------------------------------
+namespace skg {
+
+__global__ void k_wait_selftest_grid(unsigned* count, unsigned* gen, double* err, int* status, long long limit) {
+  if (blockIdx.x != 0) return;  // the second block never arrives at the barrier
+  const bool ok = grid_barrier(count, gen, err, limit);
+  if (threadIdx.x == 0) *status = ok ? SKG_OK : SKG_ERR_TIMEOUT;
+}
+
+__global__ void k_wait_selftest_mbar(int* status, int tries) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 2);
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+    const bool ok = mbar_wait(&bar, 0, tries);  // the phase needs a second arrival
+    // complete the phase and retire the barrier before the block exits
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+    mbar_inval(&bar);
+    *status = ok ? SKG_OK : SKG_ERR_TIMEOUT;
+  }
+}
+
+}  // namespace skg
+
+extern "C" {
+
+int64_t skg_wait_selftest_workspace_size(void) { return 256; }
+
+int skg_wait_selftest(int kind, int64_t limit, int32_t* status_h, void* workspace, void* stream) {
+  if (!status_h || !workspace || limit < 1 || limit > (int64_t)kSpinLimit || (kind != 0 && kind != 1))
+    return fail(SKG_ERR_ARG, "wait_selftest: kind 0 or 1, 1 <= limit <= %lld, status and workspace needed",
+                (long long)kSpinLimit);
   cudaStream_t s = as_stream(stream);
-  Carve c(scratch);
-  PcgVecs<double> v;
-  v.x = c.take<double>(4 * nbr); v.r = c.take<double>(4 * nbr); v.z = c.take<double>(4 * nbr);
-  v.p = c.take<double>(4 * nbr); v.q = c.take<double>(4 * nbr);
-  double* jinv = c.take<double>(9 * nbr);
-  double* partials = c.take<double>(8 * kMaxGrid);
-  unsigned* counter = c.take<unsigned>(16);
-  double* scal = c.take<double>(64);
-  // the array keeps the previous call's contents: the reduction counters must start at zero
-  SKG_CUDA(cudaMemsetAsync(counter, 0, 16 * sizeof(unsigned), s));
-  k_diag_inverse<<<blocks_for(nbr), kBlock, 0, s>>>(nbr, rowptr, col, val, jinv);
+  Carve c(workspace);
+  unsigned* bar = c.take<unsigned>(2);
+  double* err = c.take<double>(1);
+  int* st = c.take<int>(1);
+  SKG_CUDA(cudaMemsetAsync(workspace, 0, 256, s));
+  if (kind == 0) {
+    k_wait_selftest_grid<<<2, 32, 0, s>>>(bar, bar + 1, err, st, (long long)limit);
+  } else {
+    k_wait_selftest_mbar<<<1, 32, 0, s>>>(st, (int)(limit < (1 << 30) ? limit : (1 << 30)));
+  }
   SKG_LAUNCHED();
-  Bsr<double> A{nbr, rowptr, col, val, jinv};
-  PcgResult pr{};
-  SKG_TRY(pcg_solve<double>(A, b, 1.0, nullptr, v, rtol, max_iter, 1, partials, counter, scal, s, &pr));
-  k_unpad<double><<<blocks_for(nbr), kBlock, 0, s>>>(v.x, nbr, x);
-  SKG_LAUNCHED();
+  int h = 0;
+  SKG_CUDA(cudaMemcpyAsync(&h, st, sizeof(int), cudaMemcpyDeviceToHost, s));
   SKG_CUDA(cudaStreamSynchronize(s));
-  if (iters_h) *iters_h = pr.iters;
-  if (pr.status != 0) return fail(pr.status, "pcg failed with status %d", pr.status);
-  if (!(pr.rr <= rtol * rtol * pr.bb) && pr.bb > 0.0)
-    return fail(SKG_ERR_NOT_CONVERGED, "pcg reached %d iterations at relative residual %.3e", pr.iters,
-                sqrt(pr.rr / pr.bb));
+  *status_h = h;
   return SKG_OK;
 }
 

@@ -30,9 +30,9 @@ def compute_with_cache_check(func, cache_path, read_cache: bool = True):
                     out += (value,)
             return out
         except Exception:
-            print("Could not read from cache. Recomputing from scratch...")
+            print(f"rollout cache {cache_path} unreadable; computing the result")
     else:
-        print("Will not read from cache. Recomputing from scratch...")
+        print(f"rollout cache reading off; computing the result into {cache_path}")
     output = func()
     if not isinstance(output, tuple):
         output = (output,)

@@ -2,7 +2,8 @@
 
 Usage::
 
-    python tests/golden/make_golden.py [--reference /path/to/simkit/checkout] [--skip-c1]
+    SIMKIT_REFERENCE=/path/to/simkit/checkout python tests/golden/make_golden.py [--skip-c1] [--skip-c2]
+    python tests/golden/make_golden.py --reference /path/to/simkit/checkout --only c2
 
 Every number stored here comes out of the reference's own functions
 (``simkit.energies.stable_neo_hookean``, ``simkit.psd_project``,
@@ -28,6 +29,8 @@ Fixtures written next to this script:
 * ``contact_plane.npz``: contact springs energy / gradient / Hessian of seeded points against a plane
 * ``rollout_contact_small.npz``: 6x2x2 beam falling onto a floor plane (contact springs), 14 steps
 * ``cache_reference.npz``: a cache file written by simkit's compute_with_cache_check (array, scalar, 1-element array)
+* ``rollout_beam_32x32x128_first_steps.npz``: the 786,432-tet jittered beam with E log-uniform [1e5, 1e7], the first
+  two steps from rest (sampled vertices), with simkit's spsolve replaced by a 1e-10 PCG (labelled in the file)
 """
 
 from __future__ import annotations
@@ -396,6 +399,122 @@ def make_rollout_c1(ref, out):
                         energy=en, iters=it, residual=rl, dt=1.0 / 60.0)
 
 
+class _TightPCG:
+    """A stand-in for ``scipy.sparse.linalg.spsolve`` on the free-DOF Hessians of one beam: CG to a
+    1e-10 relative residual, preconditioned by 3x3 block Jacobi plus a rigid-mode coarse space (six
+    modes per box of 8^3 cells, Cholesky of P^T A P).  On the 786,432-tet beam simkit's own call
+    (SuperLU) did not finish in 25 minutes; this solve agrees with an exact one to the 1e-10
+    residual, far below the 1e-6 Newton tolerance the rollout stops at."""
+
+    def __init__(self, X_free_verts, cell, box=8, rtol=1e-10, max_iter=20000):
+        import scipy.sparse as sps
+        Xv = np.asarray(X_free_verts, dtype=np.float64)
+        nv = Xv.shape[0]
+        key = np.floor(Xv / (box * cell) + 1e-9).astype(np.int64)
+        _, agg = np.unique(key, axis=0, return_inverse=True)
+        agg = agg.ravel()
+        na = int(agg.max()) + 1
+        cnt = np.bincount(agg, minlength=na).astype(np.float64)
+        cen = np.stack([np.bincount(agg, weights=Xv[:, k], minlength=na) for k in range(3)], 1) / cnt[:, None]
+        d = Xv - cen[agg]
+        rms = np.sqrt(np.bincount(agg, weights=(d * d).sum(1), minlength=na) / cnt) + 1e-30
+        d = d / rms[agg][:, None]
+        rows, cols, vals = [], [], []
+        v = np.arange(nv)
+        for c in range(3):                                # translations
+            rows.append(3 * v + c); cols.append(6 * agg + c); vals.append(np.ones(nv))
+        # rotations w x d: row x gets (w_y d_z - w_z d_y), y gets (w_z d_x - w_x d_z), z (w_x d_y - w_y d_x)
+        for r, (ca, sa), (cb, sb) in ((0, (4, 2), (5, 1)), (1, (5, 0), (3, 2)), (2, (3, 1), (4, 0))):
+            rows.append(3 * v + r); cols.append(6 * agg + ca); vals.append(d[:, sa])
+            rows.append(3 * v + r); cols.append(6 * agg + cb); vals.append(-d[:, sb])
+        P = sps.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                           shape=(3 * nv, 6 * na))
+        # aggregates of one vertex (or of collinear vertices) give zero rotation columns: drop them
+        norms = np.sqrt(np.asarray(P.multiply(P).sum(axis=0)).ravel())
+        self.P = P[:, norms > 1e-9 * norms.max()].tocsr()
+        self.nv, self.rtol, self.max_iter = nv, rtol, max_iter
+        self.worst = 0.0
+        self.iters = []
+
+    def __call__(self, A, b):
+        import scipy.linalg as sla
+        A = A.tocsr()
+        n = A.shape[0]
+        assert n == 3 * self.nv
+        b = np.asarray(b, dtype=np.float64).reshape(-1)
+        # 3x3 diagonal blocks
+        D = np.zeros((self.nv, 3, 3))
+        Ac = A.tocoo()
+        on = (Ac.row // 3) == (Ac.col // 3)
+        np.add.at(D, (Ac.row[on] // 3, Ac.row[on] % 3, Ac.col[on] % 3), Ac.data[on])
+        Dinv = np.linalg.inv(D)
+        Acoarse = (self.P.T @ (A @ self.P)).toarray()
+        Acoarse[np.diag_indices_from(Acoarse)] *= 1.0 + 1e-10    # linearly dependent modes stay invertible
+        cf = sla.cho_factor(Acoarse)
+        P = self.P
+
+        def prec(r):
+            z = np.einsum("vij,vj->vi", Dinv, r.reshape(-1, 3)).reshape(-1)
+            return z + P @ sla.cho_solve(cf, P.T @ r)
+
+        x = np.zeros(n)
+        r = b.copy()
+        bn = np.linalg.norm(b)
+        z = prec(r)
+        p = z.copy()
+        rz = r @ z
+        it = 0
+        while np.linalg.norm(r) > self.rtol * bn and it < self.max_iter:
+            q = A @ p
+            a = rz / (p @ q)
+            x += a * p
+            r -= a * q
+            z = prec(r)
+            rz_new = r @ z
+            p = z + (rz_new / rz) * p
+            rz = rz_new
+            it += 1
+        rel = float(np.linalg.norm(b - A @ x) / bn)
+        assert rel < 10 * self.rtol, f"PCG stalled at {rel:.2e}"
+        self.worst = max(self.worst, rel)
+        self.iters.append(it)
+        return x
+
+
+def make_rollout_c2_first_steps(ref, out, steps=2, stride=8):
+    """The benchmarked 786,432-tet beam (32x32x128 cubes, rest shape jittered by U(-0.1, 0.1) cells,
+    E log-uniform [1e5, 1e7] per tet, seed 0): the first ``steps`` backward-Euler steps from rest with
+    simkit's energies, Hessians (incl. psd_project), line search and newton_solver, under the harness
+    rules of oracle/rollout.py.  The one substitution: simkit's ``spsolve`` is replaced by a PCG to a
+    1e-10 relative residual (_TightPCG) because SuperLU does not finish on this mesh.  Stored: the
+    displacement of every ``stride``-th vertex and of every vertex on the free end face, per step."""
+    import scipy.sparse.linalg as spla
+    from simkit_gb300.beams import beam_large_jittered
+    spec = beam_large_jittered(seed=0)
+    n = spec.n_verts
+    pin = np.zeros(n, bool)
+    pin[spec.pinned] = True
+    solver = _TightPCG(spec.X[~pin], cell=0.025)
+    tip = np.nonzero(np.isclose(spec.X[:, 0], spec.X[:, 0].max()))[0]
+    sample = np.union1d(np.arange(0, n, stride), tip)
+    orig = spla.spsolve
+    spla.spsolve = solver
+    t0 = time.time()
+    try:
+        us, en, it, rl = _reference_rollout(ref, spec, 1.0 / 60.0, steps)
+    finally:
+        spla.spsolve = orig
+    print(f"  reference 32x32x128 first {steps} steps: {time.time() - t0:.1f} s, Newton iterations {list(it)}, "
+          f"PCG iterations {solver.iters}, worst solve residual {solver.worst:.2e}")
+    keys = sorted(us)
+    U = np.stack([us[k].reshape(-1, 3)[sample] for k in keys])
+    np.savez_compressed(out, steps=np.array(keys), sample=sample, u=U, energy=en, iters=it, residual=rl,
+                        dims=np.array(spec.dims), seed=0, dt=1.0 / 60.0, solve_rtol=solver.rtol,
+                        solve_worst=solver.worst, solve_iters=np.array(solver.iters),
+                        solve="PCG (3x3 block Jacobi + rigid-mode aggregates of 8^3 cells) to 1e-10 relative "
+                              "residual in place of scipy spsolve")
+
+
 def _write_corot(ref):
     for mat in ("arap", "fcr"):
         make_element_corot(ref, 3, os.path.join(HERE, f"element_{mat}_3d.npz"), mat)
@@ -411,12 +530,18 @@ def _write_le(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("SIMKIT_REFERENCE"),
+                    help="path of a simkit checkout (or set SIMKIT_REFERENCE)")
     ap.add_argument("--skip-c1", action="store_true")
-    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot, le, u")
+    ap.add_argument("--skip-c2", action="store_true")
+    ap.add_argument("--only", default="", help="comma-separated groups to (re)write: corot, le, u, c2")
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("give --reference or set SIMKIT_REFERENCE to a simkit checkout")
     ref = _import_reference(a.reference)
     if a.only:
+        if "c2" in a.only.split(","):
+            make_rollout_c2_first_steps(ref, os.path.join(HERE, "rollout_beam_32x32x128_first_steps.npz"))
         if "corot" in a.only.split(","):
             _write_corot(ref)
         if "le" in a.only.split(","):
@@ -441,6 +566,8 @@ def main():
     make_beam_u_tier(ref, os.path.join(HERE, "beam_u_tier.npz"))
     if not a.skip_c1:
         make_rollout_c1(ref, os.path.join(HERE, "rollout_beam_8x8x32.npz"))
+    if not a.skip_c2:
+        make_rollout_c2_first_steps(ref, os.path.join(HERE, "rollout_beam_32x32x128_first_steps.npz"))
     print("fixtures written to", HERE)
 
 

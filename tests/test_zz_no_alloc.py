@@ -95,3 +95,44 @@ def test_noalloc_pcg_rejects_systems_beyond_its_capacity():
     st = lib.skg_pcg_bsr64_noalloc(cap + 1, p, p, p, p, p, 1e-8, 10, None, None)
     assert st == _lib.SKG_ERR_CAPACITY
     assert "capacity" in _lib.last_error()
+
+
+def _block_tridiagonal(nbr, seed):
+    """A symmetric positive definite block-tridiagonal system with nbr 3x3 block rows (diagonally
+    dominant blocks), to fill the fixed scratch to its capacity."""
+    rng = np.random.default_rng(seed)
+    n = 3 * nbr
+    # the coupling of block row i to block row i + 1: every scalar offset 1..5 that lands there
+    rows, cols, vals = [], [], []
+    for d in range(1, 6):
+        i = np.arange(n - d)
+        keep = (i + d) // 3 == i // 3 + 1
+        rows.append(i[keep]); cols.append(i[keep] + d); vals.append(rng.uniform(-1.0, 1.0, keep.sum()))
+    band = sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+    A = band + band.T
+    # a dense symmetric 3x3 diagonal block per row, dominant over the row's off-diagonal sum
+    Dd = rng.uniform(-0.5, 0.5, size=(nbr, 3, 3))
+    Dd = Dd + Dd.transpose(0, 2, 1)
+    rows = np.repeat(np.arange(nbr) * 3, 9) + np.tile(np.repeat(np.arange(3), 3), nbr)
+    cols = np.repeat(np.arange(nbr) * 3, 9) + np.tile(np.tile(np.arange(3), 3), nbr)
+    A = A + sps.csr_matrix((Dd.reshape(-1), (rows, cols)), shape=(n, n))
+    rowsum = np.asarray(abs(A).sum(axis=1)).ravel()
+    return (A + sps.diags(rowsum + 1.0)).tocsr()
+
+
+def test_noalloc_pcg_at_full_capacity_matches_allocating_entry_point():
+    """A system of exactly skg_pcg_noalloc_max_rows() block rows fits the fixed scratch and gives the
+    allocating entry point's answer (twice, so the second call starts from the first one's scratch)."""
+    from simkit_gb300 import _lib
+    lib = _lib.load()
+    cap = int(lib.skg_pcg_noalloc_max_rows())
+    A = _block_tridiagonal(cap, 5)
+    assert A.shape[0] // 3 == cap
+    rng = np.random.default_rng(1)
+    for call in range(2):
+        b = rng.standard_normal(A.shape[0])
+        x_ref, x_na, it_ref, it_na = _solve_both(lib, A, b)
+        err = np.linalg.norm(x_na - x_ref) / np.linalg.norm(x_ref)
+        assert err <= RTOL_COMPARE, (call, err)
+        assert it_na == it_ref
+        assert np.linalg.norm(A @ x_na - b) <= 1e-9 * np.linalg.norm(b)
