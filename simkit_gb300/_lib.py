@@ -148,6 +148,8 @@ _SIGNATURES = {
     "skg_warmstart_targets": (c_i32, [c_vp, c_vp, c_vp, c_dbl, c_i64, c_vp, c_vp]),
     "skg_pcg_noalloc_max_rows": (c_i64, []),
     "skg_pcg_bsr64_noalloc": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp]),
+    "skg_wait_selftest_workspace_size": (c_i64, []),
+    "skg_wait_selftest": (c_i32, [c_i32, c_i64, P(c_i32), c_vp, c_vp]),
 }
 
 _lock = threading.Lock()

@@ -63,6 +63,7 @@ class BatchedBESolver:
             tets.append(tets[-1] + T.shape[0])
         mesh = TetMesh(np.concatenate(Xs), np.concatenate(Ts), np.concatenate(mus), np.concatenate(lams),
                        device=device)
+        mesh.check_orientation()
         mesh.set_energy(material)
         up = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(mesh.device)
         self._contact_init = (contact_planes, contact_mass_weighted)

@@ -141,11 +141,19 @@ __global__ void k_psd_project(const double* __restrict__ H, double* __restrict__
 }
 
 // ------------------------------------------------------------- tet setup --
-__global__ void k_tet_setup(const double* __restrict__ X, const int4* __restrict__ T, int64_t t,
+__global__ void k_tet_setup(const double* __restrict__ X, const int4* __restrict__ T, int64_t n, int64_t t,
                             double* __restrict__ dinv, double* __restrict__ vol) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (e >= t) return;
   const int4 v = T[e];
+  // a vertex index outside [0, n) is not read: the tet gets NaN volume and shape operator
+  const auto out = [n](int i) { return i < 0 || (int64_t)i >= n; };
+  if (out(v.x) || out(v.y) || out(v.z) || out(v.w)) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dinv[k * t + e] = nan("");
+    vol[e] = nan("");
+    return;
+  }
   const double* x0 = X + 3 * (int64_t)v.x;
   double E[9];  // columns: X1 - X0, X2 - X0, X3 - X0
   const int vv[3] = {v.y, v.z, v.w};
@@ -320,7 +328,7 @@ int skg_psd_project(const double* H, double* out, int64_t n, int d, int method, 
 int skg_tet_setup(const double* X, const int32_t* T, int64_t n, int64_t t, double* dinv, double* vol, void* stream) {
   if (n <= 0 || t < 0) return fail(SKG_ERR_ARG, "bad mesh sizes n=%lld t=%lld", (long long)n, (long long)t);
   if (t == 0) return SKG_OK;
-  k_tet_setup<<<blocks_for(t), kBlock, 0, as_stream(stream)>>>(X, reinterpret_cast<const int4*>(T), t, dinv, vol);
+  k_tet_setup<<<blocks_for(t), kBlock, 0, as_stream(stream)>>>(X, reinterpret_cast<const int4*>(T), n, t, dinv, vol);
   SKG_LAUNCHED();
   return SKG_OK;
 }

@@ -272,6 +272,12 @@ class TetMesh:
         self.dinv = torch.empty(9 * t, dtype=torch.float64, device=dev)
         self.vol = torch.empty(t, dtype=torch.float64, device=dev)
         check(lib.skg_tet_setup(_ptr(self.X), _ptr(self.tets), n, t, _ptr(self.dinv), _ptr(self.vol), _stream_ptr()))
+        # simkit's deformation_jacobian raises on a singular rest edge matrix (np.linalg.inv); the
+        # device setup leaves a zero or non-finite volume and shape operator there instead
+        bad = (self.vol == 0) | ~torch.isfinite(self.vol) | ~torch.isfinite(self.dinv.view(9, t)).all(dim=0)
+        if bool(bad.any()):
+            e = int(torch.nonzero(bad)[0, 0])
+            raise ValueError(f"tet {e} is degenerate at rest (signed volume {float(self.vol[e]):.3e})")
         self.mu = torch.as_tensor(np.asarray(mu, dtype=np.float64).reshape(-1), device=dev).contiguous()
         self.lam = torch.as_tensor(np.asarray(lam, dtype=np.float64).reshape(-1), device=dev).contiguous()
         if self.mu.numel() != t or self.lam.numel() != t:
@@ -302,6 +308,15 @@ class TetMesh:
         self.hc_ptr, self.hc_src, self.v2t_ptr, self.v2t = up(hc_ptr), up(hc_src), up(v2t_ptr), up(v2t)
         self._set_c()
         self._scalar_perm = None
+
+    def check_orientation(self):
+        """Raise ValueError if a tet is inverted at rest (negative signed volume): its energy would
+        enter the potential with a negative weight and Newton would maximise it."""
+        neg = self.vol < 0
+        if bool(neg.any()):
+            e = int(torch.nonzero(neg)[0, 0])
+            raise ValueError(f"tet {e} is inverted at rest (signed volume {float(self.vol[e]):.3e}); "
+                             "swap two of its vertices")
 
     # ----------------------------------------------------------------- utils
     def set_coarse(self, free_dof, box=8, spacing=None):

@@ -101,6 +101,7 @@ class BESolver:
                  coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
+        self.mesh.check_orientation()
         self.mesh.set_energy(material)
         m = self.mesh
         dev = m.device

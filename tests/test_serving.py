@@ -133,3 +133,41 @@ def test_short_stream_is_served():
     assert st.failed_steps == 0 and st.backlog == 0
     assert all(r.t_done >= r.t_admit >= r.t_arrival for r in reqs)
     assert s["latency_ms_p99"] >= s["latency_ms_p50"] > 0
+
+
+def test_admission_refuses_requests_beyond_free_hbm(monkeypatch):
+    """Admission takes requests, oldest first, while the free HBM less the reserve covers their
+    estimated footprint; with the reserve above the free memory nothing is admitted and the
+    requests stay queued (CPU: the free-memory query is replaced by a fake)."""
+    import collections
+    from simkit_gb300.serving import BeamRequest, BeamServer
+    free = {"bytes": 8 * 2 ** 30}
+    monkeypatch.setattr(torch.cuda, "mem_get_info", lambda *a: (free["bytes"], 16 * 2 ** 30))
+    reqs = [BeamRequest(i, (4, 4, 8), 1e6, 0.4, np.array([0.0, -9.8, 0.0]), 10, 0.0) for i in range(5)]
+    srv = BeamServer(max_cohort=64, max_live=256, hbm_reserve_gb=1.0, device="cpu")
+    srv.bytes_per_tet = 2 ** 20                     # 768 MiB per 768-tet request
+    pending = collections.deque(reqs)
+    take = srv._admit(pending, 0)                   # 7 GiB usable: nine would fit, five are queued
+    assert [r.rid for r in take] == [0, 1, 2, 3, 4] and not pending
+    pending = collections.deque(reqs)
+    free["bytes"] = int(2.6 * 2 ** 30)              # 1.6 GiB usable: two requests
+    take = srv._admit(pending, 0)
+    assert [r.rid for r in take] == [0, 1] and [r.rid for r in pending] == [2, 3, 4]
+    srv.reserve = 64 * 2 ** 30                      # reserve above the free memory: refuse all
+    pending = collections.deque(reqs)
+    assert srv._admit(pending, 0) == [] and len(pending) == 5
+    srv.reserve = 0
+    free["bytes"] = 8 * 2 ** 30
+    assert len(srv._admit(collections.deque(reqs), 252)) == 4       # max_live caps the cohort too
+
+
+@pytest.mark.gpu
+def test_server_with_no_free_hbm_queues_every_request():
+    """With a reserve larger than the GPU's memory the server admits nothing: every request is
+    reported as backlog, none fails, and no cohort is built."""
+    from simkit_gb300.serving import BeamServer, request_stream
+    reqs = request_stream(40.0, 0.5, steps=2, seed=2, nx_range=(4, 5), ny_range=(4, 5), nz_range=(8, 9))
+    srv = BeamServer(max_cohort=64, max_live=256, hbm_reserve_gb=1.0e6)
+    st = srv.run(reqs, 0.5)
+    assert st.admitted == 0 and st.completed == 0 and st.cohorts == 0
+    assert st.backlog == st.arrived == len(reqs) and st.failed_steps == 0
