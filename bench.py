@@ -98,55 +98,79 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_reference_sample(spec, newton_iters_per_step, ls_trials_per_iter, slab_cubes=6, reps=1):
-    """Time simkit's FP64 numpy/scipy algorithm (the oracle restatement) on the host.
+def host_cpu():
+    """CPU model (lscpu), logical cores and the BLAS/OpenMP thread setting of this process."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model"):
+                model = ln.split(":", 1)[1].strip()
+                if ln.startswith("Model name"):
+                    break
+    except Exception:
+        pass
+    return {"model": model, "logical_cores": os.cpu_count(),
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS", "default")}
 
-    Sample: the first `slab_cubes` layers of cubes along x of the workload beam
-    (slab_cubes * 32 * 32 * 6 tets).  Timed per Newton iteration: Hessian
-    (element Hessians, eigen floor, block_diag, J^T H J), gradient, and one
-    energy per line-search trial, scaled to the full mesh by tet count.  The
-    sparse direct solve (scipy spsolve) is NOT included - on the full mesh it
-    did not finish in 25 minutes - so the resulting steps/s is an upper bound
-    on the reference's speed.
-    """
-    from oracle import fem, snh
+
+def slab_of(spec, layers):
+    """The first ``layers`` cube layers (along x, from the pinned face) of a beam: a complete,
+    smaller beam with the same jitter, materials and pins (vertices and tets are numbered x-major)."""
     nx, ny, nz = spec.dims
-    keep_t = 6 * slab_cubes * ny * nz
-    T = spec.T[:keep_t]
-    used = np.unique(T)
-    remap = -np.ones(spec.X.shape[0], np.int64)
-    remap[used] = np.arange(used.size)
-    Ts = remap[T]
-    Xs = spec.X[used]
-    mu, lam = spec.mu[:keep_t], spec.lam[:keep_t]
-    J = fem.deformation_jacobian(Xs, Ts)
-    vol = fem.tet_volumes(Xs, Ts)
-    x = (Xs + 1e-3 * np.random.default_rng(0).standard_normal(Xs.shape)).reshape(-1, 1)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        snh.hessian_x(x, J, mu, lam, vol)
-    th = (time.perf_counter() - t0) / reps
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        snh.gradient_x(x, J, mu, lam, vol)
-    tg = (time.perf_counter() - t0) / reps
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        snh.energy_x(x, J, mu, lam, vol)
-    te = (time.perf_counter() - t0) / reps
-    scale = spec.n_tets / keep_t
-    per_iter = scale * (th + tg + te * max(ls_trials_per_iter, 1.0))
-    per_step = per_iter * newton_iters_per_step
-    return {
-        "steps_per_s": 1.0 / per_step,
-        "tet_hessians_per_s": keep_t / th,
-        "s_per_newton_iter_no_solve": per_iter,
-        "sample": (f"{keep_t} tets ({slab_cubes}x{ny}x{nz} cube slab) of the workload beam: Hessian "
-                   f"{th:.3f} s, gradient {tg:.3f} s, energy {te:.3f} s per call, scaled by tet count to "
-                   f"{spec.n_tets} tets and to {newton_iters_per_step:.2f} Newton iterations/step; "
-                   "spsolve excluded (did not finish on the full mesh), so steps/s is an upper bound"),
-        "cores": os.cpu_count(),
-    }
+    nv = (layers + 1) * (ny + 1) * (nz + 1)
+    nt = 6 * layers * ny * nz
+    return nv, nt
+
+
+class CpuReferenceSteps:
+    """simkit's FP64 numpy/scipy step (the oracle restatement: its energies, Hessians with the
+    eigenvalue floor, block_diag / J^T H J assembly, scipy spsolve, Armijo line search, Newton to
+    the 1e-6 relative residual) run for real on a slab of the workload beam, one backward-Euler
+    step per call, continuing a rollout from rest.  Every call is a measured full step (the direct
+    solve included).  ``extrapolate`` scales the measured step time to the whole mesh by tet count:
+    the sparse direct solve grows faster than linearly with the mesh (a slab twice as long takes
+    3x as long per step), so the linear figure is an upper bound on the reference's steps/s."""
+
+    def __init__(self, spec, layers=2):
+        from oracle import rollout
+        nv, nt = slab_of(spec, layers)
+        self.layers, self.nt, self.full_tets = layers, nt, spec.n_tets
+        self.r = rollout.BeamRollout(spec.X[:nv], spec.T[:nt], spec.mu[:nt], spec.lam[:nt], spec.rho,
+                                     spec.gravity, spec.pinned, 1.0 / 60.0)
+        self.x_prev = self.r.x_rest.copy()
+        self.x_curr = self.r.x_rest.copy()
+        self.times, self.iters = [], []
+
+    def step(self):
+        t0 = time.perf_counter()
+        x_next, info = self.r.step(self.x_curr, self.x_prev)
+        dt = time.perf_counter() - t0
+        if not info.converged:
+            raise SystemExit(f"reference slab step did not converge: {info}")
+        self.x_prev, self.x_curr = self.x_curr, x_next
+        self.times.append(dt)
+        self.iters.append(info.iters)
+        return dt
+
+    def summary(self, skip=0):
+        t = np.array(self.times[skip:])
+        ms = 1e3 * float(t.mean())
+        per_full_step_s = float(t.mean()) * self.full_tets / self.nt
+        nx = self.full_tets // (6 * self.layers)
+        return {
+            "measured_ms_per_step": ms,
+            "measured_steps_per_s": 1e3 / ms,
+            "measured_tet_hessians_per_s": self.nt * float(np.mean(self.iters[skip:])) / float(t.mean()),
+            "newton_iters_per_step": float(np.mean(self.iters[skip:])),
+            "extrapolated_steps_per_s": 1.0 / per_full_step_s,
+            "sample": (f"{len(t)} measured backward-Euler steps (Newton to 1e-6 with scipy spsolve and Armijo "
+                       f"search, FP64) of the first {self.layers} cube layers of the workload beam "
+                       f"({self.nt} tets, same jitter, materials and pinned face), continuing a rollout from "
+                       f"rest; steps/s for the {self.full_tets}-tet mesh = measured step time x "
+                       f"{self.full_tets / self.nt:.0f} (tet ratio): an upper bound, the direct solve "
+                       "grows faster than linearly"),
+        }
 
 
 # --------------------------------------------------------------- helpers
@@ -225,29 +249,74 @@ def algorithmic_bytes(spec, nb, n_coarse=0):
     }
 
 
+def parity_report(spec, solver_kw, steps_fp64=30):
+    """Errors of the timed configuration on the workload beam (seed 0), outside the timed region:
+    (1) the first two steps from rest against simkit's own steps stored in
+    tests/golden/rollout_beam_32x32x128_first_steps.npz (simkit's spsolve replaced there by a 1e-10
+    PCG; sampled vertices); (2) ``steps_fp64`` steps against the package's FP64 mode (FP64 kernels,
+    PCG forcing 1e-3).  Positions relative to the largest rest coordinate, displacements relative
+    to the largest displacement."""
+    from simkit_gb300.solver import BESolver
+    out = {}
+    scale = float(np.abs(spec.X).max())
+    path = os.path.join(ROOT, "tests", "golden", "rollout_beam_32x32x128_first_steps.npz")
+    if os.path.exists(path):
+        d = np.load(path)
+        s = BESolver.from_spec(spec, **solver_kw)
+        pos = disp = 0.0
+        for k, step in enumerate(d["steps"]):
+            while s.steps < int(step):
+                if not s.step().converged:
+                    raise SystemExit("parity step did not converge")
+            u = s.displacement().reshape(-1, 3)[d["sample"]]
+            pos = max(pos, float(np.abs(u - d["u"][k]).max()) / scale)
+            disp = max(disp, float(np.abs(u - d["u"][k]).max() / np.abs(d["u"][k]).max()))
+        out["vs_simkit"] = {"steps": int(d["steps"].max()), "positions_rel": pos, "displacement_rel": disp,
+                            "vertices": int(d["sample"].size),
+                            "reference": "simkit's energies, Hessians, line search and Newton; " + str(d["solve"])}
+        del s
+    a = BESolver.from_spec(spec, **solver_kw)
+    kw64 = dict(solver_kw, precision="fp64", pcg_rtol=1e-3)
+    b = BESolver.from_spec(spec, **kw64)
+    pos = disp = 0.0
+    for _ in range(steps_fp64):
+        if not (a.step().converged and b.step().converged):
+            raise SystemExit("parity step did not converge")
+        ua, ub = a.displacement(), b.displacement()
+        pos = max(pos, float(np.abs(ua - ub).max()) / scale)
+        disp = max(disp, float(np.abs(ua - ub).max() / np.abs(ub).max()))
+    out["vs_fp64_mode"] = {"steps": steps_fp64, "positions_rel": pos, "displacement_rel": disp}
+    return out
+
+
 def run_reference(args):
+    """The reference's CPU path (the oracle restatement of simkit's algorithm) on the machine's host:
+    each bench step is one measured backward-Euler step of a slab of the workload beam, the direct
+    solve included (CpuReferenceSteps).  ms_per_step is that measured time; value is the whole-mesh
+    steps/s extrapolated from it (labelled, an upper bound)."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
     from simkit_gb300.beams import beam_large_jittered
     spec = beam_large_jittered()
-    # per-step Newton iteration and line-search counts measured by the GPU arm on this workload
-    iters = args.ref_newton_iters
-    vals = []
-    info = None
-    for k in range(args.warmup + args.steps):
-        info = cpu_reference_sample(spec, iters, 1.0)
-        if k >= args.warmup:
-            vals.append(info["steps_per_s"])
-    v = float(np.mean(vals))
+    ref = CpuReferenceSteps(spec, layers=args.ref_layers)
+    t0 = time.perf_counter()
+    for _ in range(args.warmup + args.steps):
+        ref.step()
+    wall = time.perf_counter() - t0
+    sm = ref.summary(skip=args.warmup)
+    v = sm["extrapolated_steps_per_s"]
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sm["measured_ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "precision": "fp64 numpy/scipy", "l2": "inputs larger than L2"},
-        "tet_hessians_per_s": info["tet_hessians_per_s"],
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": info["cores"], "kind": "port",
-                         "sample": info["sample"]},
+        "value_kind": "extrapolated from the measured slab steps (linear in tets, an upper bound)",
+        "ms_per_step_kind": "measured: one full backward-Euler step of the slab sample",
+        "measured": sm, "wall_s": wall, "host": host_cpu(),
+        "tet_hessians_per_s": sm["measured_tet_hessians_per_s"],
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port", "sample": sm["sample"],
+                         "threads": "numpy/scipy as simkit runs them: element math and SuperLU single-threaded"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -467,9 +536,12 @@ def main():
                     help="--pcg-rtol of the single-mesh headline solver (the batched and serving "
                          "modes use --pcg-rtol); -0.3 measured fastest on the 786,432-tet beam")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-newton-iters", type=float, default=4.0,
-                    help="Newton iterations per step used to scale the CPU reference sample (both arms): "
-                         "the reference's exact-solve Newton needs about 4 on the 786,432-tet beam")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity report of the headline line")
+    ap.add_argument("--ref-layers", type=int, default=2,
+                    help="cube layers of the workload beam in the CPU reference sample (2: 12,288 tets, "
+                         "about 1 s per measured step)")
+    ap.add_argument("--cpu-baseline-steps", type=int, default=4,
+                    help="measured CPU reference steps in the GPU arm's cpu_baseline")
     ap.add_argument("--small", action="store_true", help="use the 8x8x32 beam (quick check)")
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "serving"])
@@ -501,8 +573,9 @@ def main():
     spec = beam_small_steady() if args.small else beam_large_jittered(seed=replica_seed(rank))
     workload = "beam 8x8x32 cubes, 12,288 tets (quick check)" if args.small else WORKLOAD
     coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
-    solver = BESolver.from_spec(spec, precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol_single,
-                                profile=False, coarse=coarse, coarse_refresh=args.coarse_refresh)
+    solver_kw = dict(precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol_single,
+                     coarse=coarse, coarse_refresh=args.coarse_refresh)
+    solver = BESolver.from_spec(spec, **solver_kw)
     nb = solver.mesh.nb
     for _ in range(args.warmup):
         info = solver.step()
@@ -580,6 +653,8 @@ def main():
                                                else "pcg_bytes_per_iter" if solver.coarse_form is None else "none"),
                 "algorithmic_bytes": ab["pcg_iter"], "ms_per_launch": pcg_ms_per_iter}
     roof["peak_kind"] = peak_kind
+    roof["traffic_source"] = (("ncu capture committed with the repository, not measured in this run: "
+                               + traffic.get("source", "profiles/")) if traffic and roof.get("traffic") else None)
     roof["phase_share"] = share
     roof["secondary"] = {"tet_hessian_assembly_gbs": hess_gbs, "tet_hessian_frac": hess_gbs / hbm,
                          "pcg_gbs": pcg_gbs, "pcg_frac": pcg_gbs / hbm}
@@ -607,11 +682,18 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        # scaled by the Newton count of the reference's own algorithm (exact sparse solves), not by
-        # this solver's (inexact Newton takes more, cheaper iterations): the same count the reference arm uses
-        cpu_info = cpu_reference_sample(spec, args.ref_newton_iters, 1.0)
-        cpu = {"value": cpu_info["steps_per_s"], "unit": "steps/s", "cores": cpu_info["cores"], "kind": "port",
-               "sample": cpu_info["sample"], "tet_hessians_per_s": cpu_info["tet_hessians_per_s"]}
+        # the same measurement the reference arm makes (real slab steps), over a few steps
+        ref = CpuReferenceSteps(spec, layers=args.ref_layers)
+        for _ in range(args.cpu_baseline_steps):
+            ref.step()
+        sm = ref.summary(skip=1)
+        cpu = {"value": sm["extrapolated_steps_per_s"], "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": sm["sample"], "value_kind": "extrapolated from the measured slab steps (upper bound)",
+               "measured": sm, "host": host_cpu()}
+
+    parity = None
+    if rank == 0 and not args.small and not args.no_parity:
+        parity = parity_report(spec, solver_kw)
 
     if rank == 0:
         line = {
@@ -632,6 +714,7 @@ def main():
             "e2e": e2e,
             "roofline": roof,
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clock_info,
         }
         print(json.dumps(line))

@@ -286,6 +286,18 @@ int skg_snh_hessian_u(const skg_tet_mesh* mesh, const double* u, const double* J
 /* ---------------------------------------------------------------------- */
 /* Newton / backward Euler: solvers/newton.py:7-75, integrators/backward_euler.py:27-91 */
 /* ---------------------------------------------------------------------- */
+/* Per-iteration record of one skg_be_step call, for simkit's newton_solver info dict
+ * (solvers/newton.py:43-67: 'g', 'dx', 'alphas', 'iters'), plus the relative residual and the
+ * PCG iterations of each Newton iteration.  Rows past newton_iters are left untouched. */
+typedef struct skg_newton_record {
+  int32_t capacity;         /* Newton iterations the arrays hold (>= max_newton to record all) */
+  double* g;                /* device (capacity, 3n): gradient at the start of each iteration */
+  double* dx;               /* device (capacity, 3n): Newton direction (solution of H dx = -g) */
+  double* alpha_h;          /* host (capacity): accepted step length (0 when the search failed) */
+  double* residual_h;       /* host (capacity): ||g|| / ||g(x_tilde)|| at the start of the iteration */
+  int32_t* pcg_iters_h;     /* host (capacity): PCG iterations of the iteration's solve */
+} skg_newton_record;
+
 typedef struct skg_be_params {
   double dt;                /* time step h */
   double tol;               /* relative residual ||g(x)|| / ||g(x_tilde)|| */
@@ -334,6 +346,7 @@ typedef struct skg_be_params {
                                (SKG_ERR_NOT_CONVERGED after max_newton); 1 = simkit's newton_solver
                                (solvers/newton.py:43-75): at least one iteration, stop once
                                ||alpha dx|| < tol, at most max_newton iterations, no status */
+  skg_newton_record* record; /* host pointer, or NULL: skg_be_step fills it per Newton iteration */
 } skg_be_params;
 
 typedef struct skg_be_state {

@@ -63,6 +63,11 @@ class ContactPlaneC(ctypes.Structure):
     _fields_ = [("p", c_dbl * 3), ("n", c_dbl * 3), ("k", c_dbl)]
 
 
+class NewtonRecordC(ctypes.Structure):
+    _fields_ = [("capacity", c_i32), ("g", c_vp), ("dx", c_vp), ("alpha_h", c_vp), ("residual_h", c_vp),
+                ("pcg_iters_h", c_vp)]
+
+
 class BEParamsC(ctypes.Structure):
     _fields_ = [
         ("dt", c_dbl), ("tol", c_dbl), ("max_newton", c_i32), ("precision", c_i32), ("pcg_rtol", c_dbl),
@@ -70,7 +75,7 @@ class BEParamsC(ctypes.Structure):
         ("ls_max_iter", c_i32), ("pcg_mode", c_i32), ("ls_threshold", c_dbl), ("profile", c_i32),
         ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
         ("n_planes", c_i32), ("contact_mass_weighted", c_i32), ("planes", ctypes.POINTER(ContactPlaneC)),
-        ("coarse_refresh", c_i32), ("stop_rule", c_i32),
+        ("coarse_refresh", c_i32), ("stop_rule", c_i32), ("record", ctypes.POINTER(NewtonRecordC)),
     ]
 
 

@@ -946,8 +946,12 @@ class ElasticPotential:
                                            mass=mass, f_ext=self.f_ext, integrator=integrator)
         return self._steppers[key]
 
-    def _device_step(self, integrator, M, h, tolerance, max_iter, do_line_search, xs):
-        """simkit's Newton contract on the device, or None when M is not lumped."""
+    def _device_step(self, integrator, M, h, tolerance, max_iter, do_line_search, xs, return_info=False):
+        """simkit's Newton contract on the device, or None when M is not lumped.  With return_info,
+        (x_next, info): simkit's newton_solver info (newton.py:43-67: per-iteration gradient 'g' and
+        direction 'dx' as (3n, 1) arrays, 'alphas', 'iters' = index of the last iteration) plus
+        'residuals' (||g|| / ||g(x_tilde)|| at the start of each iteration), 'pcg_iters' per
+        iteration and the step's 'status' (0, or the skg_status of a failed solve or search)."""
         mass = _vertex_masses(M, self.X.shape[0])
         if mass is None:
             return None
@@ -956,11 +960,35 @@ class ElasticPotential:
         solver.params.max_newton = int(max_iter)
         solver.params.do_line_search = int(do_line_search)
         solver.params.stop_rule = 1
-        if integrator == "bdf2":
-            x_next, _ = solver.step_host(xs[0], xs[1], x_prev2=xs[2], x_prev3=xs[3])
-        else:
-            x_next, _ = solver.step_host(xs[0], xs[1])
-        return x_next
+        rec = None
+        if return_info:
+            cap = max(int(max_iter), 1)
+            n3 = self.X.size
+            rec = {"g": torch.empty((cap, n3), dtype=torch.float64, device=solver.mesh.device),
+                   "dx": torch.empty((cap, n3), dtype=torch.float64, device=solver.mesh.device),
+                   "alpha": np.zeros(cap), "res": np.zeros(cap), "pcg": np.zeros(cap, np.int32)}
+            host = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+            rec["c"] = _lib.NewtonRecordC(capacity=cap, g=rec["g"].data_ptr(), dx=rec["dx"].data_ptr(),
+                                          alpha_h=host(rec["alpha"]), residual_h=host(rec["res"]),
+                                          pcg_iters_h=host(rec["pcg"]))
+            solver.params.record = ctypes.pointer(rec["c"])
+        try:
+            if integrator == "bdf2":
+                x_next, st = solver.step_host(xs[0], xs[1], x_prev2=xs[2], x_prev3=xs[3])
+            else:
+                x_next, st = solver.step_host(xs[0], xs[1])
+        finally:
+            solver.params.record = None
+        if rec is None:
+            return x_next
+        k = int(st.newton_iters)
+        g = rec["g"][:k].cpu().numpy()
+        dx = rec["dx"][:k].cpu().numpy()
+        info = {"g": [g[i].reshape(-1, 1) for i in range(k)], "dx": [dx[i].reshape(-1, 1) for i in range(k)],
+                "alphas": [float(a) for a in rec["alpha"][:k]], "iters": k - 1,
+                "residuals": [float(r) for r in rec["res"][:k]], "pcg_iters": [int(c) for c in rec["pcg"][:k]],
+                "status": int(st.status)}
+        return x_next, info
 
 
 def _potential_of(*funcs):
@@ -999,14 +1027,15 @@ def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, 
     """simkit ``backward_euler`` (integrators/backward_euler.py:27-91): minimise
     V(x) + 1/(2h^2) (x - x~)^T M (x - x~), x~ = 2 x_curr - x_prev, by ``newton_solver``.
 
-    With the closures of an ``ElasticPotential`` and a lumped M (host arrays, no ``return_info``)
-    the step runs on the device with the same Newton contract; otherwise the closures are called.
+    With the closures of an ``ElasticPotential`` and a lumped M (host arrays) the step runs on the
+    device with the same Newton contract (``return_info`` gives simkit's info dict plus per-iteration
+    residuals, PCG iterations and a status); otherwise the closures are called.
     """
     pot = _potential_of(energy_func, gradient_func, hessian_func)
-    if pot is not None and not return_info and all(isinstance(a, np.ndarray) for a in (x_curr, x_prev)):
-        x_next = pot._device_step("be", M, h, tolerance, max_iter, do_line_search, (x_curr, x_prev))
-        if x_next is not None:
-            return x_next
+    if pot is not None and all(isinstance(a, np.ndarray) for a in (x_curr, x_prev)):
+        out = pot._device_step("be", M, h, tolerance, max_iter, do_line_search, (x_curr, x_prev), return_info)
+        if out is not None:
+            return out
     x_tilde = x_curr + h * ((x_curr - x_prev) / h)
 
     def energy(x):
@@ -1034,10 +1063,10 @@ def bdf2(x_curr, x_prev, x_prev2, x_prev3, energy_func, gradient_func, hessian_f
     An ``ElasticPotential``'s closures with a lumped M take the device path, as in ``backward_euler``."""
     pot = _potential_of(energy_func, gradient_func, hessian_func)
     xs = (x_curr, x_prev, x_prev2, x_prev3)
-    if pot is not None and not return_info and all(isinstance(a, np.ndarray) for a in xs):
-        x_next = pot._device_step("bdf2", M, h, tolerance, max_iter, do_line_search, xs)
-        if x_next is not None:
-            return x_next
+    if pot is not None and all(isinstance(a, np.ndarray) for a in xs):
+        out = pot._device_step("bdf2", M, h, tolerance, max_iter, do_line_search, xs, return_info)
+        if out is not None:
+            return out
     v_curr = (3.0 * x_curr - 4.0 * x_prev + x_prev2) / (2.0 * h)
     v_prev = (3.0 * x_prev - 4.0 * x_prev2 + x_prev3) / (2.0 * h)
     x_tilde = (4.0 / 3.0) * x_curr - (1.0 / 3.0) * x_prev + (8.0 * h / 9.0) * v_curr - (2.0 * h / 9.0) * v_prev

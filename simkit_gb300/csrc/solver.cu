@@ -1135,10 +1135,18 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
   // stop_rule 1 is simkit's newton_solver (solvers/newton.py:43-75): at least one iteration, then
   // stop once ||alpha dx|| < tol, at most max_newton iterations, no convergence status
   const bool simkit_stop = prm->stop_rule == 1;
+  skg_newton_record* nrec = prm->record;
   for (int it = 0; it < prm->max_newton && (r0 > 0.0 || simkit_stop); ++it) {
     const double res = r0 > 0.0 ? sqrt(gg) / r0 : 0.0;
     info->residual = res;
     if (!simkit_stop && res < prm->tol) break;
+    const bool record = nrec && it < nrec->capacity;
+    if (record) {
+      SKG_CUDA(cudaMemcpyAsync(nrec->g + (int64_t)it * nd, w.g, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      nrec->residual_h[it] = res;
+      nrec->alpha_h[it] = 0.0;
+      nrec->pcg_iters_h[it] = 0;
+    }
     // PCG forcing term: fixed (pcg_rtol > 0) or Eisenstat-Walker choice 2
     // (gamma 0.9, exponent 2, safeguarded) capped at |pcg_rtol|, never
     // tighter than what brings the residual to a quarter of tol
@@ -1194,6 +1202,12 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     info->t_pcg_ms += pt.end();
     info->launches += pr.launches;
     info->pcg_iters += pr.iters;
+    if (record) {
+      k_unpad<R><<<blocks_for(n), kBlock, 0, s>>>(pv.x, n, nrec->dx + (int64_t)it * nd);
+      SKG_LAUNCHED();
+      info->launches++;
+      nrec->pcg_iters_h[it] = pr.iters;
+    }
     if (pr.status != 0) {
       info->status = pr.status;
       break;
@@ -1220,6 +1234,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
       }
     }
     info->newton_iters = it + 1;
+    if (record) nrec->alpha_h[it] = accepted ? step : 0.0;
     if (!accepted) {
       // simkit returns t = 0 (backtracking_line_search.py:66-67) and Newton
       // stops because ||0 * dx|| < tol (newton.py:69)
@@ -1774,6 +1789,10 @@ int skg_be_step(const skg_tet_mesh* mesh, const skg_be_params* params, const skg
     return fail(SKG_ERR_ARG, "line search alpha must lie in (0, 0.5]");
   if (params->do_line_search && !(params->ls_beta > 0.0 && params->ls_beta < 1.0))
     return fail(SKG_ERR_ARG, "line search beta must lie in (0, 1)");
+  const skg_newton_record* rec = params->record;
+  if (rec && (rec->capacity < 0 || (rec->capacity > 0 && (!rec->g || !rec->dx || !rec->alpha_h || !rec->residual_h ||
+                                                          !rec->pcg_iters_h))))
+    return fail(SKG_ERR_ARG, "be_step: a Newton record needs capacity >= 0 and all five arrays");
   cudaStream_t s = as_stream(stream);
   Workspace w = carve_workspace(mesh, params->precision, workspace);
   if (params->precision == SKG_MIXED) return be_step<float>(mesh, params, state, w, info_h, s);
@@ -1990,22 +2009,39 @@ __global__ void k_wait_selftest_mbar(int* status, int tries) {
   }
 }
 
+// barrier words, error flag and status of the self-test, carved as the solvers carve theirs
+struct WaitSelftestWs {
+  unsigned* bar;
+  double* err;
+  int* status;
+  int64_t bytes;
+};
+static WaitSelftestWs carve_wait_selftest(void* base) {
+  Carve c(base);
+  WaitSelftestWs w{};
+  w.bar = c.take<unsigned>(2);
+  w.err = c.take<double>(1);
+  w.status = c.take<int>(1);
+  w.bytes = c.off;
+  return w;
+}
+
 }  // namespace skg
 
 extern "C" {
 
-int64_t skg_wait_selftest_workspace_size(void) { return 256; }
+int64_t skg_wait_selftest_workspace_size(void) { return carve_wait_selftest(nullptr).bytes; }
 
 int skg_wait_selftest(int kind, int64_t limit, int32_t* status_h, void* workspace, void* stream) {
   if (!status_h || !workspace || limit < 1 || limit > (int64_t)kSpinLimit || (kind != 0 && kind != 1))
     return fail(SKG_ERR_ARG, "wait_selftest: kind 0 or 1, 1 <= limit <= %lld, status and workspace needed",
                 (long long)kSpinLimit);
   cudaStream_t s = as_stream(stream);
-  Carve c(workspace);
-  unsigned* bar = c.take<unsigned>(2);
-  double* err = c.take<double>(1);
-  int* st = c.take<int>(1);
-  SKG_CUDA(cudaMemsetAsync(workspace, 0, 256, s));
+  const WaitSelftestWs w = carve_wait_selftest(workspace);
+  unsigned* bar = w.bar;
+  double* err = w.err;
+  int* st = w.status;
+  SKG_CUDA(cudaMemsetAsync(workspace, 0, (size_t)w.bytes, s));
   if (kind == 0) {
     k_wait_selftest_grid<<<2, 32, 0, s>>>(bar, bar + 1, err, st, (long long)limit);
   } else {

@@ -796,3 +796,61 @@ def test_batched_step_matches_single_instance_and_oracle(api):
             ub = b.displacement(i)
             assert _rel(X + ub, X + singles[i].displacement()) < 1e-7
             assert _rel(X + ub, xn.ravel()) < 1e-5
+
+
+def test_self_contained_tier_matches_reference(api):
+    """stable_neo_hookean_{energy,gradient,hessian}(X, T, mu, lam, U) (snh.py:654-737: J and vol rebuilt
+    from X, T, then the _x tier at U) against simkit's values in beam_small.npz."""
+    import scipy.sparse as sps
+    d = _load("beam_small.npz")
+    X, T, mu, lam, U = d["X"], d["T"], d["mu"], d["lam"], d["x"]
+    E = api.stable_neo_hookean_energy(X, T, mu, lam, U)
+    assert abs(E - float(d["energy"])) <= 1e-12 * abs(float(d["energy"]))
+    g = api.stable_neo_hookean_gradient(X, T, mu, lam, U)
+    assert g.shape == d["gradient"].shape and _rel(g, d["gradient"]) < 1e-10
+    K = api.stable_neo_hookean_hessian(X, T, mu, lam, U).tocsr()
+    K_ref = sps.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=K.shape)
+    assert abs(K - K_ref).max() <= 1e-10 * abs(K_ref).max()
+    # U omitted: evaluated at the rest positions, where the elastic force vanishes
+    g0 = api.stable_neo_hookean_gradient(X, T, mu, lam)
+    assert np.abs(g0).max() <= 1e-12 * np.abs(d["gradient"]).max()
+
+
+@pytest.mark.parametrize("max_iter,tol", [(1, 1e-6), (20, 1e-9)])
+def test_backward_euler_fast_path_matches_oracle_with_info(api, max_iter, tol):
+    """The drop-in backward_euler on the device fast path (ElasticPotential closures, lumped M) against
+    the oracle's backward_euler (simkit's integrators/backward_euler.py:27-91 and newton.py:7-75 with
+    spsolve) on the same closures' math: same positions, Newton iteration count and step lengths, and
+    return_info gives simkit's info dict (g, dx, alphas, iters) plus residuals, pcg_iters, status."""
+    import scipy.sparse as sps
+    from oracle import fem, snh as osnh, solvers as osol
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 3, 3, ym=2e5, pr=0.45)
+    X, T = spec.X, spec.T
+    m = fem.lumped_mass(X, T, 1000.0)
+    M = sps.diags(np.repeat(m, 3)).tocsc()
+    f = (m[:, None] * np.array([0.0, -9.8, 0.0])[None, :]).reshape(-1, 1)
+    pot = api.ElasticPotential(X, T, spec.mu, spec.lam, f_ext=f)
+    J, vol = fem.deformation_jacobian(X, T), fem.tet_volumes(X, T)
+    Eo = lambda x: osnh.energy_x(x, J, spec.mu, spec.lam, vol) - float((f.T @ x).item())
+    Go = lambda x: osnh.gradient_x(x, J, spec.mu, spec.lam, vol) - f
+    Ho = lambda x: osnh.hessian_x(x, J, spec.mu, spec.lam, vol)
+    rng = np.random.default_rng(5)
+    x_prev = X.reshape(-1, 1).copy()
+    x_curr = x_prev + 1e-3 * rng.standard_normal(x_prev.shape)
+    h = 1.0 / 60.0
+    for _ in range(3):
+        got, info = api.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h,
+                                       tolerance=tol, max_iter=max_iter, return_info=True)
+        ref, rinfo = osol.backward_euler(x_curr, x_prev, Eo, Go, Ho, M, h, tolerance=tol, max_iter=max_iter,
+                                         return_info=True)
+        assert len(pot._steppers) == 1                     # the device path ran
+        assert _rel(got - x_curr, ref - x_curr) < 1e-9
+        assert info["iters"] == rinfo["iters"] and info["alphas"] == rinfo["alphas"]
+        assert info["status"] == 0 and len(info["pcg_iters"]) == len(info["residuals"]) == info["iters"] + 1
+        assert info["residuals"][0] == 1.0 and all(c > 0 for c in info["pcg_iters"])
+        for k in range(info["iters"] + 1):
+            assert info["g"][k].shape == rinfo["g"][k].shape == x_curr.shape
+            assert _rel(info["g"][k], rinfo["g"][k]) < 1e-9 * max(1.0, 1.0 / max(info["residuals"][k], 1e-3))
+            assert _rel(info["dx"][k], rinfo["dx"][k]) < 1e-7
+        x_prev, x_curr = x_curr, got
