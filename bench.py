@@ -127,27 +127,31 @@ class CpuReferenceSteps:
     """simkit's FP64 numpy/scipy step (the oracle restatement: its energies, Hessians with the
     eigenvalue floor, block_diag / J^T H J assembly, scipy spsolve, Armijo line search, Newton to
     the 1e-6 relative residual) run for real on a slab of the workload beam, one backward-Euler
-    step per call, continuing a rollout from rest.  Every call is a measured full step (the direct
-    solve included).  ``extrapolate`` scales the measured step time to the whole mesh by tet count:
-    the sparse direct solve grows faster than linearly with the mesh (a slab twice as long takes
-    3x as long per step), so the linear figure is an upper bound on the reference's steps/s."""
+    step per call, on a rollout from rest that restarts every ``restart`` steps (the stiff slab
+    comes to rest within a few steps, after which the relative residual measures FP64 noise; the
+    headline beam is still swinging).  Every call is a measured full step (the direct solve
+    included).  The whole-mesh figure scales the measured step time by tet count: the sparse direct
+    solve grows faster than linearly with the mesh (a slab twice as long takes 3x as long per
+    step), so the linear figure is an upper bound on the reference's steps/s."""
 
-    def __init__(self, spec, layers=2):
+    def __init__(self, spec, layers=2, restart=4):
         from oracle import rollout
         nv, nt = slab_of(spec, layers)
         self.layers, self.nt, self.full_tets = layers, nt, spec.n_tets
+        self.restart = restart
         self.r = rollout.BeamRollout(spec.X[:nv], spec.T[:nt], spec.mu[:nt], spec.lam[:nt], spec.rho,
                                      spec.gravity, spec.pinned, 1.0 / 60.0)
-        self.x_prev = self.r.x_rest.copy()
-        self.x_curr = self.r.x_rest.copy()
         self.times, self.iters = [], []
+        self.not_converged = 0
 
     def step(self):
+        if len(self.times) % self.restart == 0:
+            self.x_prev = self.r.x_rest.copy()
+            self.x_curr = self.r.x_rest.copy()
         t0 = time.perf_counter()
         x_next, info = self.r.step(self.x_curr, self.x_prev)
         dt = time.perf_counter() - t0
-        if not info.converged:
-            raise SystemExit(f"reference slab step did not converge: {info}")
+        self.not_converged += int(not info.converged)
         self.x_prev, self.x_curr = self.x_curr, x_next
         self.times.append(dt)
         self.iters.append(info.iters)
@@ -157,17 +161,17 @@ class CpuReferenceSteps:
         t = np.array(self.times[skip:])
         ms = 1e3 * float(t.mean())
         per_full_step_s = float(t.mean()) * self.full_tets / self.nt
-        nx = self.full_tets // (6 * self.layers)
         return {
             "measured_ms_per_step": ms,
             "measured_steps_per_s": 1e3 / ms,
             "measured_tet_hessians_per_s": self.nt * float(np.mean(self.iters[skip:])) / float(t.mean()),
             "newton_iters_per_step": float(np.mean(self.iters[skip:])),
+            "steps_not_converged": self.not_converged,
             "extrapolated_steps_per_s": 1.0 / per_full_step_s,
             "sample": (f"{len(t)} measured backward-Euler steps (Newton to 1e-6 with scipy spsolve and Armijo "
                        f"search, FP64) of the first {self.layers} cube layers of the workload beam "
-                       f"({self.nt} tets, same jitter, materials and pinned face), continuing a rollout from "
-                       f"rest; steps/s for the {self.full_tets}-tet mesh = measured step time x "
+                       f"({self.nt} tets, same jitter, materials and pinned face), rollouts from rest of "
+                       f"{self.restart} steps; steps/s for the {self.full_tets}-tet mesh = measured step time x "
                        f"{self.full_tets / self.nt:.0f} (tet ratio): an upper bound, the direct solve "
                        "grows faster than linearly"),
         }
@@ -205,6 +209,14 @@ class Ranks:
         import torch
         t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
         self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.dist is None:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
         return float(t.item())
 
     def whole_job_rate(self, units_per_rank: float, seconds_max: float) -> float:
@@ -398,11 +410,14 @@ def run_batched(args):
     from simkit_gb300.batched import BatchedBESolver
     from simkit_gb300.beams import beam_batch
     from simkit_gb300.solver import BESolver
+    from simkit_gb300.sharding import gather_to_rank0, shard
     n_ranks, rank, local = dist_setup()
     torch.cuda.set_device(local)
     ranks = Ranks("nccl")
-    # replicas: every rank steps its own seeded batch of the same distribution
-    specs = beam_batch(args.instances, seed=replica_seed(rank))
+    # one batch of args.instances beams split across the ranks by LPT on tet count (instances are
+    # independent: no exchange in the solve); per-instance results are gathered on rank 0 at the end
+    specs_all = beam_batch(args.instances, seed=0)
+    shard_idx, specs = shard(specs_all, rank, n_ranks)
     # the same preconditioner on both sides of the comparison: two-level (per-instance
     # aggregates) unless --coarse none
     coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
@@ -449,8 +464,12 @@ def run_batched(args):
     ms = ranks.max(ev0.elapsed_time(ev1))
     if any(t.status != 0 for t in totals):
         raise SystemExit(f"batched step failed: {[t.status for t in totals]}")
-    inst_steps = args.instances * args.steps
-    value = ranks.whole_job_rate(inst_steps, ms / 1000.0)
+    inst_steps = args.instances * args.steps          # the whole batch, over all ranks
+    value = inst_steps / (ms / 1000.0)
+    # host gather of per-instance results (Newton iterations of the last step, final displacement)
+    local = [{"newton": int(i.newton_iters), "status": int(i.status),
+              "u_max": float(np.abs(b.displacement(k)).max())} for k, i in enumerate(infos)]
+    gathered = gather_to_rank0(ranks.dist, shard_idx, local, args.instances)
     # one extra profiled step (phase times by CUDA events; not part of the timed region)
     b.params.profile = 1
     if args.learned:
@@ -459,8 +478,11 @@ def run_batched(args):
         _, prof = b.step()
     b.params.profile = 0
     phase_ms = {k: getattr(prof, f"t_{k}_ms") for k in ("hessian", "assemble", "pcg", "gradient", "energy")}
-    newton = sum(t.newton_iters for t in totals)
-    tets = b.n_tets
+    newton = ranks.sum(sum(t.newton_iters for t in totals))     # Newton iterations of the whole batch
+    pcg = ranks.sum(sum(t.pcg_iters for t in totals))
+    launches = ranks.sum(sum(t.launches for t in totals))
+    tets = sum(sp.n_tets for sp in specs_all)
+    verts = sum(sp.n_verts for sp in specs_all)
     if rank != 0:
         ranks.close()
         return 0
@@ -471,7 +493,7 @@ def run_batched(args):
         """the sampled beams stepped one at a time through the single-instance solver"""
         ms = []
         for i in sample:
-            s1 = BESolver.from_spec(specs[i], precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=cs)
+            s1 = BESolver.from_spec(specs_all[i], precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=cs)
             for _ in range(args.warmup):
                 s1.step()
             tune_pcg_variant(s1, use_cache=not args.retune)   # the single-instance solver at its best cluster size
@@ -490,16 +512,19 @@ def run_batched(args):
     ranks.close()
     line = {
         "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": n_ranks, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": f"{args.instances} beams, nx, ny in 4..16, nz in 8..48, batched "
                                + ("+ learned warm start" if args.learned else "plain Newton"),
-                   "instances": args.instances, "tets": int(tets), "verts": int(b.n_verts),
-                   "precision": args.precision, "pcg_rtol": args.pcg_rtol,
-                   "coarse": args.coarse, "parallelism": f"replicas x{n_ranks}"},
-        "tet_hessians_per_s": n_ranks * newton / max(args.instances, 1) * tets / (ms / 1000.0),
+                   "instances": args.instances, "tets": int(tets), "verts": int(verts),
+                   "precision": args.precision, "pcg_rtol": args.pcg_rtol, "coarse": args.coarse,
+                   "parallelism": f"instances sharded x{n_ranks} (LPT on tet count)"},
+        "tet_hessians_per_s": newton / max(args.instances, 1) * tets / (ms / 1000.0),
         "newton_iters_per_instance_step": newton / inst_steps,
-        "pcg_iters_per_instance_step": sum(t.pcg_iters for t in totals) / inst_steps,
+        "pcg_iters_per_instance_step": pcg / inst_steps,
+        "gathered": {"instances": len(gathered), "failed": sum(1 for g in gathered if g["status"] != 0),
+                     "newton_last_step_mean": float(np.mean([g["newton"] for g in gathered])),
+                     "u_max": max(g["u_max"] for g in gathered)},
         "batch_policy": {"vec_kb": policy[0], "min_cluster": policy[1], "step_ms_by_policy": policy_ms},
         "plain_single_instance": {"value": plain_value, "unit": "instance-steps/s",
                                   "sample": f"{len(sample)} of the beams stepped alone, {args.steps} steps each"},
@@ -511,7 +536,7 @@ def run_batched(args):
         "warm_start_kept_fraction": float(np.mean(kept)) if kept else None,
         "phase_ms_one_step": phase_ms,
         "newton_iters_profiled_step": prof.newton_iters,
-        "gpu_launches": sum(t.launches for t in totals),
+        "gpu_launches": int(launches),
         "clocks": clock_info,
     }
     print(json.dumps(line))

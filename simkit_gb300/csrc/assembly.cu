@@ -103,89 +103,10 @@ __device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e,
 }
 
 // ------------------------------------------------------------ assembly ---
-// One thread per block slot: sum the slot's per-tet blocks in list order,
-// add the lumped mass / h^2 on diagonal blocks, apply pinned rows/columns
-// (identity on the diagonal, zero elsewhere) and, for diagonal slots, write
-// the inverse of the 3x3 block for the block-Jacobi preconditioner.
+// Terms every slot gets after its per-tet blocks are summed: lumped mass / h^2 and contact
+// springs on diagonal blocks, then pinned rows / columns (identity on the diagonal).
 template <typename R>
-__device__ __forceinline__ void assemble_slot(const AsmArgs<R>& a, int64_t s);
-
-template <typename R>
-__global__ void k_assemble(AsmArgs<R> a) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= a.nb) return;
-  assemble_slot(a, s);
-}
-
-template <typename R>
-__device__ __forceinline__ void assemble_slot(const AsmArgs<R>& a, int64_t s) {
-  const int v = __ldg(a.bsr_row + s);
-  if (a.inst_active && !a.inst_active[__ldg(a.vert_inst + v)]) return;
-  const int w = __ldg(a.bsr_col + s);
-  const int rp = __ldg(a.rowptr + v);
-  const int K = __ldg(a.rowptr + v + 1) - rp;
-  const int k = (int)(s - rp);
-  R acc[9];
-#pragma unroll
-  for (int m = 0; m < 9; ++m) acc[m] = R(0);
-  const int c0 = __ldg(a.hc_ptr + s), c1 = __ldg(a.hc_ptr + s + 1);
-  int c = c0;
-  // four contributions at a time: their loads are all issued before any is summed (a diagonal
-  // slot has one contribution per incident tet, ~24 on a Kuhn-split grid).  Every contribution
-  // is read as 9 values from its offset (a diagonal block's 6 plus 3 that are not used; they
-  // stay inside the tet's kHStride record); the sums keep the list order.
-  for (; c + 4 <= c1; c += 4) {
-    int cd[4];
-    R b[4][9];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int code = __ldg(a.hc_src + c + j);
-      cd[j] = code & 15;
-      const int off = cd[j] < 4 ? 6 * cd[j] : 24 + 9 * (cd[j] < 10 ? cd[j] - 4 : cd[j] - 10);
-      const R* h = a.hbuf + (int64_t)kHStride * (code >> 4) + off;
-#pragma unroll
-      for (int m = 0; m < 9; ++m) b[j][m] = h[m];
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (cd[j] < 4) {
-        acc[0] += b[j][0]; acc[1] += b[j][1]; acc[2] += b[j][2];
-        acc[3] += b[j][1]; acc[4] += b[j][3]; acc[5] += b[j][4];
-        acc[6] += b[j][2]; acc[7] += b[j][4]; acc[8] += b[j][5];
-      } else if (cd[j] < 10) {
-#pragma unroll
-        for (int m = 0; m < 9; ++m) acc[m] += b[j][m];
-      } else {
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int k2 = 0; k2 < 3; ++k2) acc[3 * i + k2] += b[j][3 * k2 + i];
-      }
-    }
-  }
-  for (; c < c1; ++c) {
-    const int code = __ldg(a.hc_src + c);
-    const int64_t e = code >> 4;
-    const int cd = code & 15;
-    const R* h = a.hbuf + (int64_t)kHStride * e;
-    if (cd < 4) {
-      const R* d = h + 6 * cd;
-      const R d0 = d[0], d1 = d[1], d2 = d[2], d3 = d[3], d4 = d[4], d5 = d[5];
-      acc[0] += d0; acc[1] += d1; acc[2] += d2;
-      acc[3] += d1; acc[4] += d3; acc[5] += d4;
-      acc[6] += d2; acc[7] += d4; acc[8] += d5;
-    } else if (cd < 10) {
-      const R* b = h + 24 + 9 * (cd - 4);
-#pragma unroll
-      for (int m = 0; m < 9; ++m) acc[m] += b[m];
-    } else {
-      const R* b = h + 24 + 9 * (cd - 10);
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) acc[3 * i + j] += b[3 * j + i];
-    }
-  }
+__device__ __forceinline__ void finish_slot(const AsmArgs<R>& a, int v, int w, R (&acc)[9]) {
   if (v == w && a.mass) {
     const R m = R(a.mass[v] * a.inv_h2);
     acc[0] += m; acc[4] += m; acc[8] += m;
@@ -204,34 +125,151 @@ __device__ __forceinline__ void assemble_slot(const AsmArgs<R>& a, int64_t s) {
       for (int j = 0; j < 3; ++j)
         if (a.pinned[3 * v + i] | a.pinned[3 * w + j]) acc[3 * i + j] = (v == w && i == j) ? R(1) : R(0);
   }
-  if (a.val) {
-    R* dst = a.val + 9 * (int64_t)rp + k;
+}
+
+// the 3x3 inverse of a diagonal block for the block-Jacobi preconditioner
+template <typename R>
+__device__ __forceinline__ void write_jinv(const AsmArgs<R>& a, int v, const R (&acc)[9]) {
+  R C[9];
+  cof3(acc, C);
+  const R det = acc[0] * C[0] + acc[1] * C[1] + acc[2] * C[2];
+  R* ji = a.jinv + 9 * (int64_t)v;
+  if (det != R(0)) {
+    const R id = R(1) / det;
 #pragma unroll
-    for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) ji[3 * i + j] = C[3 * j + i] * id;
+  } else {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) ji[m] = (m % 4 == 0 && acc[m] != R(0)) ? R(1) / acc[m] : R(0);
   }
-  if (a.rec) {
-    R* r = a.rec + kRec * s;
+}
+
+// the solver's block record of slot s (column w) at r
+template <typename R>
+__device__ __forceinline__ void fill_record(const AsmArgs<R>& a, int w, const R (&acc)[9], R* r) {
 #pragma unroll
-    for (int m = 0; m < 9; ++m) r[m] = acc[m];
-    r[9] = col_bits(w, R(0));
-    rec_aux_store(r, a.cmode ? coarse_pack(__ldg(a.cmode + w)) : make_uint2(0u, 0u));
-    if (a.colpack) rec_word_store(r, __ldg(a.colpack + w));
+  for (int m = 0; m < 9; ++m) r[m] = acc[m];
+  r[9] = col_bits(w, R(0));
+  rec_aux_store(r, a.cmode ? coarse_pack(__ldg(a.cmode + w)) : make_uint2(0u, 0u));
+  if (a.colpack) rec_word_store(r, __ldg(a.colpack + w));
+}
+
+// add contribution `code` (tet << 4 | pair) whose 9 stored values are b, in place
+template <typename R>
+__device__ __forceinline__ void add_contribution(int cd, const R* b, R (&acc)[9]) {
+  if (cd < 4) {
+    const R d0 = b[0], d1 = b[1], d2 = b[2], d3 = b[3], d4 = b[4], d5 = b[5];
+    acc[0] += d0; acc[1] += d1; acc[2] += d2;
+    acc[3] += d1; acc[4] += d3; acc[5] += d4;
+    acc[6] += d2; acc[7] += d4; acc[8] += d5;
+  } else if (cd < 10) {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) acc[m] += b[m];
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) acc[3 * i + j] += b[3 * j + i];
   }
-  if (v == w && a.jinv) {
-    R C[9];
-    cof3(acc, C);
-    const R det = acc[0] * C[0] + acc[1] * C[1] + acc[2] * C[2];
-    R* ji = a.jinv + 9 * (int64_t)v;
-    if (det != R(0)) {
-      const R id = R(1) / det;
+}
+
+// offset of a contribution's 9 values inside its tet's kHStride record: diagonal block cd < 4
+// (6 stored values, read as 9: the 3 after them are not used and stay inside the record),
+// off-diagonal pair cd - 4 (cd < 10) or its transpose (cd - 10)
+__device__ __forceinline__ int contribution_offset(int cd) {
+  return cd < 4 ? 6 * cd : 24 + 9 * (cd < 10 ? cd - 4 : cd - 10);
+}
+
+// Deterministic gather assembly.  Every block slot is the sum of its per-tet blocks (the
+// hc_src list of the slot, in tet order) plus the lumped mass / h^2 and contact terms on
+// diagonal blocks; pinned rows / columns become identity / zero; diagonal slots also give the
+// 3x3 inverse for the block-Jacobi preconditioner.  Output: the solver's block records (rec)
+// and / or the entry-major block values of the assembled tier (val).
+//
+// A warp owns 32 consecutive slots, whose contributions are one contiguous range of hc_src.
+// The range is staged through shared memory kAsmChunk contributions at a time: the warp loads
+// each contribution's 9 values with 9 consecutive lanes (one or two sectors per contribution,
+// all nine loads of a lane in flight) - one lane per slot issuing 9 scalar loads would touch
+// 32 different tet records per instruction.  Each lane then sums its own slot's contributions
+// from shared memory in list order (a fixed order: bitwise repeatable), and the warp writes its
+// 32 records with 16-byte stores.
+constexpr int kAsmWarps = 8;
+constexpr int kAsmChunk = 32;
+
+template <typename R>
+__global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
+  __shared__ __align__(16) R stage[kAsmWarps][9 * kAsmChunk];
+  __shared__ int scode[kAsmWarps][kAsmChunk];
+  __shared__ __align__(16) R srec[kAsmWarps][kRec * 32];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t s0 = ((int64_t)blockIdx.x * kAsmWarps + wid) * 32;
+  if (s0 >= a.nb) return;  // warp-uniform
+  const int64_t s = s0 + lane;
+  const bool has = s < a.nb;
+  int v = 0, w = 0, cb = 0, ce = 0;
+  bool active = has;
+  if (has) {
+    v = __ldg(a.bsr_row + s);
+    w = __ldg(a.bsr_col + s);
+    cb = __ldg(a.hc_ptr + s);
+    ce = __ldg(a.hc_ptr + s + 1);
+    if (a.inst_active && !a.inst_active[__ldg(a.vert_inst + v)]) active = false;
+  }
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  if (act == 0u) return;  // every slot of the warp belongs to an instance that is not stepping
+  const int last = (int)min((int64_t)31, a.nb - 1 - s0);
+  const int wb = __shfl_sync(0xffffffffu, cb, 0);
+  const int we = __shfl_sync(0xffffffffu, ce, last);
+  R acc[9];
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+  for (int m = 0; m < 9; ++m) acc[m] = R(0);
+  R* st = stage[wid];
+  int* sc = scode[wid];
+  for (int k0 = wb; k0 < we; k0 += kAsmChunk) {
+    const int nk = min(kAsmChunk, we - k0);
+    const int code = lane < nk ? __ldg(a.hc_src + k0 + lane) : 0;
+    sc[lane] = code;
+    R vals[9];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) ji[3 * i + j] = C[3 * j + i] * id;
-    } else {
-#pragma unroll
-      for (int m = 0; m < 9; ++m) ji[m] = (m % 4 == 0 && acc[m] != R(0)) ? R(1) / acc[m] : R(0);
+    for (int t = 0; t < 9; ++t) {
+      const int j = lane + 32 * t;  // element j of the chunk: contribution j / 9, entry j % 9
+      const int cj = j / 9;
+      const int cc = __shfl_sync(0xffffffffu, code, cj);
+      vals[t] = R(0);
+      if (cj < nk) vals[t] = __ldg(a.hbuf + (int64_t)kHStride * (cc >> 4) + contribution_offset(cc & 15) + (j - 9 * cj));
     }
+#pragma unroll
+    for (int t = 0; t < 9; ++t) st[lane + 32 * t] = vals[t];
+    __syncwarp();
+    const int lo = max(cb, k0), hi = min(ce, k0 + nk);
+    for (int c = lo; c < hi; ++c) add_contribution<R>(sc[c - k0] & 15, st + 9 * (c - k0), acc);
+    __syncwarp();
+  }
+  R* my = srec[wid] + kRec * lane;
+  if (active) {
+    finish_slot(a, v, w, acc);
+    if (a.rec) fill_record(a, w, acc, my);
+    if (a.val) {
+      const int rp = __ldg(a.rowptr + v);
+      const int K = __ldg(a.rowptr + v + 1) - rp;
+      R* dst = a.val + 9 * (int64_t)rp + (s - rp);
+#pragma unroll
+      for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+    }
+    if (v == w && a.jinv) write_jinv(a, v, acc);
+  }
+  if (!a.rec) return;  // warp-uniform
+  __syncwarp();
+  // 32 records of kRec values: 16-byte pieces, each inside one record
+  constexpr int kPer = kRec * (int)sizeof(R) / 16;  // pieces per record
+  const int4* src = reinterpret_cast<const int4*>(srec[wid]);
+  int4* dst = reinterpret_cast<int4*>(a.rec + kRec * s0);
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) {
+    const int q = lane + 32 * t;
+    if ((act >> (q / kPer)) & 1u) dst[q] = src[q];
   }
 }
 
@@ -538,7 +576,8 @@ int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cuda
 template <typename R>
 int launch_assemble(const AsmArgs<R>& a, cudaStream_t s) {
   if (a.nb == 0) return SKG_OK;
-  k_assemble<R><<<blocks_for(a.nb), kBlock, 0, s>>>(a);
+  const int64_t warps = (a.nb + 31) / 32;
+  k_assemble<R><<<(int)((warps + kAsmWarps - 1) / kAsmWarps), 32 * kAsmWarps, 0, s>>>(a);
   SKG_LAUNCHED();
   return SKG_OK;
 }

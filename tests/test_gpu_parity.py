@@ -28,6 +28,30 @@ def _rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
+_WORST = {}
+
+
+@pytest.fixture(autouse=True)
+def _report_rollout_errors(request):
+    """Print the worst rollout errors each test measured (run with -s to see them)."""
+    _WORST.clear()
+    yield
+    if _WORST:
+        print(f"\n{request.node.name}: positions rel err {_WORST['pos']:.2e}, "
+              f"displacement rel err {_WORST['disp']:.2e}")
+
+
+def _rollout_check(X, u, u_ref, pos_tol, disp_tol):
+    """Positions relative to the largest rest coordinate (the stated bar) and displacements relative
+    to the largest reference displacement (displacements are mm to cm against |X| ~ 1 m)."""
+    pos = _rel(X + u, X + u_ref)
+    disp = _rel(u, u_ref)
+    _WORST["pos"] = max(_WORST.get("pos", 0.0), pos)
+    _WORST["disp"] = max(_WORST.get("disp", 0.0), disp)
+    assert pos < pos_tol, pos
+    assert disp < disp_tol, disp
+
+
 @pytest.fixture(scope="module")
 def api():
     import simkit_gb300 as sk
@@ -148,8 +172,7 @@ def test_be_step_fp64_matches_reference_rollout(api):
         assert info.converged, info
         k = list(d["steps"]).index(step)
         u = s.displacement()
-        assert _rel(X + u, X + d["u"][k]) < 1e-7
-        assert _rel(u, d["u"][k]) < 1e-4
+        _rollout_check(X, u, d["u"][k], 1e-7, 1e-4)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -168,7 +191,7 @@ def test_bdf2_step_matches_reference_rollout(api, precision):
         assert info.converged, info
         k = list(d["steps"]).index(step)
         u = s.displacement()
-        assert _rel(X + u, X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+        _rollout_check(X, u, d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
 
 
 def test_bdf2_batched_equals_single(api):
@@ -271,7 +294,7 @@ def test_mmnh_be_step_matches_reference_rollout(api, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
 
 
 def _corot_entry(api, material, kind):
@@ -356,7 +379,7 @@ def test_corot_be_step_matches_reference_rollout(api, material, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
 
 
 @pytest.mark.parametrize("d", [3, 2])
@@ -408,7 +431,8 @@ def test_le_assembled_and_rollout_match_reference(api, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        assert _rel(Xb + s.displacement(), Xb + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+        _rollout_check(Xb, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5,
+                       1e-4 if precision == "fp64" else 1e-3)
 
 
 def test_corot_batched_equals_single(api):
@@ -496,7 +520,7 @@ def test_contact_rollout_matches_reference(api, precision):
         info = s.step()
         assert info.converged, (step, info)
         k = list(d["steps"]).index(step)
-        assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5), step
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -514,7 +538,7 @@ def test_two_barrier_grid_pcg_matches_reference(api, precision):
         assert info.converged, (step, info)
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -541,7 +565,7 @@ def test_two_level_pcg_matches_reference(api, precision, refresh):
         pcg_one += info1.pcg_iters
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
     print(f"\n{precision}/{refresh}: PCG iterations two-level {pcg_two}, one-level {pcg_one}")
     assert 2 * pcg_two < pcg_one
 
@@ -563,7 +587,7 @@ def test_two_level_grid_block_shapes(api, variant):
         assert info.converged, (step, info)
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            assert _rel(X + s.displacement(), X + d["u"][k]) < 1e-5
+            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
 
 
 def test_two_level_repeatable(api):
@@ -693,6 +717,7 @@ def test_rollout_8x8x32_matches_reference(api, precision):
             u = s.displacement()
             worst_pos = max(worst_pos, _rel(X + u, X + d["u"][k]))
             worst_u = max(worst_u, _rel(u, d["u"][k]))
+            _rollout_check(X, u, d["u"][k], 1e-5, 1e-3)
     print(f"\n{precision}: positions rel err {worst_pos:.2e}, displacement rel err {worst_u:.2e}, "
           f"newton iters {sum(iters)} (reference {int(d['iters'].sum())})")
     assert worst_pos < 1e-5
@@ -735,7 +760,7 @@ def test_cluster_two_level_small_beam(api, precision):
         one_it += info1.pcg_iters
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            assert _rel(X + s.displacement(), X + d["u"][k]) < (1e-7 if precision == "fp64" else 1e-5)
+            _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
     print(f"\n{precision}: PCG iterations cluster two-level {two_it}, one-level {one_it}")
     assert 2 * two_it < one_it
 
@@ -795,7 +820,7 @@ def test_batched_step_matches_single_instance_and_oracle(api):
             X = sp.X.reshape(-1)
             ub = b.displacement(i)
             assert _rel(X + ub, X + singles[i].displacement()) < 1e-7
-            assert _rel(X + ub, xn.ravel()) < 1e-5
+            _rollout_check(X, ub, xn.ravel() - X, 1e-5, 1e-3)
 
 
 def test_self_contained_tier_matches_reference(api):
@@ -849,8 +874,11 @@ def test_backward_euler_fast_path_matches_oracle_with_info(api, max_iter, tol):
         assert info["iters"] == rinfo["iters"] and info["alphas"] == rinfo["alphas"]
         assert info["status"] == 0 and len(info["pcg_iters"]) == len(info["residuals"]) == info["iters"] + 1
         assert info["residuals"][0] == 1.0 and all(c > 0 for c in info["pcg_iters"])
+        # every iteration's gradient and direction against the first iteration's scale (late ones are
+        # tiny: relative to themselves they would measure FP64 noise)
+        g0, dx0 = np.abs(rinfo["g"][0]).max(), np.abs(rinfo["dx"][0]).max()
         for k in range(info["iters"] + 1):
             assert info["g"][k].shape == rinfo["g"][k].shape == x_curr.shape
-            assert _rel(info["g"][k], rinfo["g"][k]) < 1e-9 * max(1.0, 1.0 / max(info["residuals"][k], 1e-3))
-            assert _rel(info["dx"][k], rinfo["dx"][k]) < 1e-7
+            assert np.abs(info["g"][k] - rinfo["g"][k]).max() <= 1e-9 * g0, k
+            assert np.abs(info["dx"][k] - rinfo["dx"][k]).max() <= 1e-8 * dx0, k
         x_prev, x_curr = x_curr, got
