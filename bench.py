@@ -33,6 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Newton-converged steps/s & tet-Hessians/s, plain vs batched+learned @1e-6 resid"
 WORKLOAD = "beam 32x32x128 cubes, 786,432 tets, jittered, E log-uniform [1e5,1e7], 1 instance, plain Newton"
+SMALL_WORKLOAD = "beam 8x8x32 cubes, 12,288 tets, E 1e6, nu 0.45 (quick check)"
 
 
 def peaks():
@@ -309,9 +310,14 @@ def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    from simkit_gb300.beams import beam_large_jittered
-    spec = beam_large_jittered()
-    ref = CpuReferenceSteps(spec, layers=args.ref_layers)
+    from simkit_gb300.beams import beam_large_jittered, beam_small_steady
+    if args.small:
+        # the 12,288-tet beam is small enough to time whole: a plain rollout from rest, nothing scaled
+        spec = beam_small_steady()
+        ref = CpuReferenceSteps(spec, layers=spec.dims[0], restart=10 ** 9)
+    else:
+        spec = beam_large_jittered()
+        ref = CpuReferenceSteps(spec, layers=args.ref_layers)
     t0 = time.perf_counter()
     for _ in range(args.warmup + args.steps):
         ref.step()
@@ -322,8 +328,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sm["measured_ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "fp64 numpy/scipy", "l2": "inputs larger than L2"},
-        "value_kind": "extrapolated from the measured slab steps (linear in tets, an upper bound)",
+        "config": {"workload": SMALL_WORKLOAD if args.small else WORKLOAD, "precision": "fp64 numpy/scipy",
+                   "l2": "inputs larger than L2"},
+        "value_kind": ("measured: the whole beam, a rollout from rest" if args.small else
+                       "extrapolated from the measured slab steps (linear in tets, an upper bound)"),
         "ms_per_step_kind": "measured: one full backward-Euler step of the slab sample",
         "measured": sm, "wall_s": wall, "host": host_cpu(),
         "tet_hessians_per_s": sm["measured_tet_hessians_per_s"],
@@ -510,6 +518,28 @@ def run_batched(args):
     # the plain form as first specified: single instance, block-Jacobi PCG
     plain_bj = plain_rate(None) if coarse is not None else plain_value
     ranks.close()
+    cpu = None
+    if not args.no_cpu_baseline:
+        # simkit's algorithm (the oracle: spsolve, Armijo, Newton to 1e-6) on a seeded subset of
+        # the beams, each stepped from rest; whole-batch rate by tet count (labelled)
+        from oracle import rollout
+        pick = np.random.default_rng(2).choice(args.instances, size=min(4, args.instances), replace=False)
+        t_sum, tet_steps = 0.0, 0
+        for i in pick:
+            r = rollout.from_spec(specs_all[i])
+            xc = xp = r.x_rest.copy()
+            for _ in range(2):
+                t0 = time.perf_counter()
+                xn, _ = r.step(xc, xp)
+                t_sum += time.perf_counter() - t0
+                xp, xc = xc, xn
+                tet_steps += specs_all[i].n_tets
+        cpu = {"value": args.instances / (t_sum / tet_steps * tets), "unit": "instance-steps/s", "cores": 1,
+               "kind": "port", "host": host_cpu(),
+               "value_kind": "extrapolated by tet count from the measured subset",
+               "sample": f"beams {sorted(int(i) for i in pick)} of the batch, 2 measured steps each from rest "
+                         f"({tet_steps // 2} tets in all, {t_sum:.2f} s); whole-batch instance-steps/s = "
+                         f"{args.instances} / (measured seconds per tet-step x {tets} tets)"}
     line = {
         "metric": METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": n_ranks, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "strong",
@@ -534,6 +564,7 @@ def run_batched(args):
         "batched_over_plain_block_jacobi": value / n_ranks / plain_bj,
         "learned": learned,
         "warm_start_kept_fraction": float(np.mean(kept)) if kept else None,
+        "cpu_baseline": cpu,
         "phase_ms_one_step": phase_ms,
         "newton_iters_profiled_step": prof.newton_iters,
         "gpu_launches": int(launches),
@@ -596,7 +627,7 @@ def main():
 
     # replicas only: every rank runs its own instance of the workload
     spec = beam_small_steady() if args.small else beam_large_jittered(seed=replica_seed(rank))
-    workload = "beam 8x8x32 cubes, 12,288 tets (quick check)" if args.small else WORKLOAD
+    workload = SMALL_WORKLOAD if args.small else WORKLOAD
     coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
     solver_kw = dict(precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol_single,
                      coarse=coarse, coarse_refresh=args.coarse_refresh)
@@ -708,7 +739,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         # the same measurement the reference arm makes (real slab steps), over a few steps
-        ref = CpuReferenceSteps(spec, layers=args.ref_layers)
+        ref = (CpuReferenceSteps(spec, layers=spec.dims[0], restart=10 ** 9) if args.small
+               else CpuReferenceSteps(spec, layers=args.ref_layers))
         for _ in range(args.cpu_baseline_steps):
             ref.step()
         sm = ref.summary(skip=1)

@@ -418,6 +418,24 @@ int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const 
                         const skg_be_state* state, void* workspace, skg_step_info* infos_h, skg_step_info* total_h,
                         void* stream);
 
+/* The same batched step with the Newton loop on the device, as a reusable plan.
+ * skg_be_batch_plan_create records one call of skg_be_step_batched for these buffers into an
+ * executable CUDA graph: every per-instance decision (relative-residual test, Eisenstat-Walker
+ * forcing, Armijo trials, stop) is made by control kernels between the solver's kernels, and
+ * the Newton iterations and line-search trials are conditional WHILE nodes those kernels drive
+ * (the coarse refresh of the first iteration is a conditional IF node).  skg_be_batch_plan_step
+ * launches the graph on `stream` and synchronizes once to return infos_h / total_h, the records
+ * skg_be_step_batched returns.  The plan reads and writes through the pointers it was created
+ * with (mesh and batch arrays, state buffers, workspace, the contents of *params and of the
+ * contact planes): they must stay valid and their sizes unchanged until
+ * skg_be_batch_plan_destroy; their contents may change between steps.  Uses no profiling
+ * (params->profile is ignored) and allocates no device memory beyond the graph itself. */
+typedef struct skg_batch_plan skg_batch_plan;
+int skg_be_batch_plan_create(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
+                             const skg_be_state* state, void* workspace, skg_batch_plan** plan_h);
+int skg_be_batch_plan_step(skg_batch_plan* plan, skg_step_info* infos_h, skg_step_info* total_h, void* stream);
+int skg_be_batch_plan_destroy(skg_batch_plan* plan);
+
 /* ---------------------------------------------------------------------- */
 /* generic sparse solve: replaces spsolve in newton_solver (newton.py:52)   */
 /* ---------------------------------------------------------------------- */

@@ -136,6 +136,9 @@ _SIGNATURES = {
     "skg_batch_workspace_size": (c_i64, [P(TetMeshC), P(BatchC), c_i32]),
     "skg_be_step_batched": (c_i32, [P(TetMeshC), P(BatchC), P(BEParamsC), P(BEStateC), c_vp, P(StepInfoC),
                                     P(StepInfoC), c_vp]),
+    "skg_be_batch_plan_create": (c_i32, [P(TetMeshC), P(BatchC), P(BEParamsC), P(BEStateC), c_vp, P(c_vp)]),
+    "skg_be_batch_plan_step": (c_i32, [c_vp, P(StepInfoC), P(StepInfoC), c_vp]),
+    "skg_be_batch_plan_destroy": (c_i32, [c_vp]),
     "skg_pcg_workspace_size": (c_i64, [c_i64]),
     "skg_pcg_bsr64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp, c_vp]),
     "skg_mlp_gemm": (c_i32, [c_vp, c_i64, c_i64, c_vp, c_i32, c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,

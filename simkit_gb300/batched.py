@@ -4,11 +4,16 @@ simkit steps one mesh per ``backward_euler`` call
 (``simkit/integrators/backward_euler.py:27-91``).  ``BatchedBESolver`` takes a
 list of meshes of uneven sizes, concatenates them into one device mesh with
 disjoint vertex and tet ranges, and advances all of them by one
-backward-Euler step per call through ``skg_be_step_batched``: the element,
-assembly and gradient kernels run once over the concatenation, and every
-instance gets its own Newton iteration, forcing term, Armijo search and
-convergence test, with its linear system solved on a thread-block cluster
-taken from a largest-first queue.
+backward-Euler step per call: the element, assembly and gradient kernels run
+once over the concatenation, and every instance gets its own Newton
+iteration, forcing term, Armijo search and convergence test, with its linear
+system solved on a thread-block cluster taken from a largest-first queue.
+
+By default a step is one launch of a CUDA graph with the Newton loop on the
+device (``skg_be_batch_plan_*``: per-instance decisions in control kernels,
+the Newton iterations and line-search trials as conditional graph nodes), one
+plan per rotation of the state buffers; profiled steps and ``graph=False``
+take ``skg_be_step_batched``, which makes the same decisions on the host.
 """
 
 from __future__ import annotations
@@ -38,8 +43,9 @@ class BatchedBESolver:
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
                  integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh="step"):
+                 coarse="auto", coarse_refresh="step", graph=True):
         _lib.load()
+        self.graph = graph
         self.n_inst = len(specs)
         if self.n_inst == 0:
             raise ValueError("empty batch")
@@ -82,11 +88,12 @@ class BatchedBESolver:
     @classmethod
     def from_device(cls, mesh, inst_rows, inst_tets, mass, f_ext, pinned, dt=1.0 / 60.0, tol=1e-6, max_newton=20,
                     precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, do_line_search=True, ls_threshold=None,
-                    profile=False, integrator="be"):
+                    profile=False, integrator="be", graph=True):
         """A batch over an already concatenated device mesh: ``inst_rows`` / ``inst_tets`` (host
         int arrays, n_inst + 1) delimit the instances; mass (n), f_ext (3n) f64 and pinned (3n) u8
         are device tensors."""
         self = cls.__new__(cls)
+        self.graph = graph
         self.n_inst = len(inst_rows) - 1
         if self.n_inst <= 0:
             raise ValueError("empty batch")
@@ -136,6 +143,9 @@ class BatchedBESolver:
             profile=int(profile), integrator=INTEGRATORS[integrator],
             coarse_refresh=int(getattr(self, "_coarse_refresh", "step") == "newton"))
         self._infos = (StepInfoC * self.n_inst)()
+        self._plans = {}          # device-loop graphs, one per rotation of the state buffers
+        self._plan_key = None     # parameters and contact planes the plans were recorded with
+        self._u_warm = None       # fixed buffer the warm start is copied into for the graphs
         init = getattr(self, "_contact_init", (None, True))
         self.set_contact_planes(*init)
         self.steps = 0
@@ -168,10 +178,21 @@ class BatchedBESolver:
                       u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
                       u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
         total = StepInfoC()
-        check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
-                                              ctypes.byref(self.params), ctypes.byref(st),
-                                              ctypes.c_void_p(self.workspace.data_ptr()), self._infos,
-                                              ctypes.byref(total), _stream_ptr(stream)))
+        # a one-instance batch with coarse data inverts its coarse operator with a cooperative grid
+        # launch, which stays on the host-driven path
+        if self.graph and not self.params.profile and not (self.n_inst == 1 and bool(self.mesh.c.coarse)):
+            if u_warm is not None:
+                if self._u_warm is None:
+                    self._u_warm = torch.empty_like(self.u_curr)
+                self._u_warm.copy_(u_warm)
+                st.u_warm = self._u_warm.data_ptr()
+            plan = self._plan(st)
+            check(_lib.load().skg_be_batch_plan_step(plan, self._infos, ctypes.byref(total), _stream_ptr(stream)))
+        else:
+            check(_lib.load().skg_be_step_batched(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
+                                                  ctypes.byref(self.params), ctypes.byref(st),
+                                                  ctypes.c_void_p(self.workspace.data_ptr()), self._infos,
+                                                  ctypes.byref(total), _stream_ptr(stream)))
         if bdf2:
             self.u_prev3, self.u_prev2, self.u_prev, self.u_curr, self.u_next = (
                 self.u_prev2, self.u_prev, self.u_curr, self.u_next, self.u_prev3)
@@ -182,6 +203,39 @@ class BatchedBESolver:
                                   c.min_alpha, c.energy, c.launches, c.t_hessian_ms, c.t_assemble_ms, c.t_pcg_ms,
                                   c.t_gradient_ms, c.t_energy_ms, c.warm_used)
         return [conv(c) for c in self._infos], conv(total)
+
+    def _params_key(self):
+        raw = ctypes.string_at(ctypes.addressof(self.params), ctypes.sizeof(self.params))
+        planes = ctypes.string_at(ctypes.addressof(self._planes), ctypes.sizeof(self._planes)) if self._planes else b""
+        return raw + planes
+
+    def _plan(self, st):
+        """The graph for this state binding (recorded on first use; all of them again after a
+        change of parameters or contact planes)."""
+        key = self._params_key()
+        if key != self._plan_key:
+            self.release_plans()
+            self._plan_key = key
+        bind = (st.u, st.u_curr, st.u_prev, st.u_prev2, st.u_prev3, st.u_warm)
+        plan = self._plans.get(bind)
+        if plan is None:
+            h = ctypes.c_void_p()
+            check(_lib.load().skg_be_batch_plan_create(ctypes.byref(self.mesh.c), ctypes.byref(self.batch),
+                                                       ctypes.byref(self.params), ctypes.byref(st),
+                                                       ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(h)))
+            plan = self._plans[bind] = h
+        return plan
+
+    def release_plans(self):
+        for h in getattr(self, "_plans", {}).values():
+            _lib.load().skg_be_batch_plan_destroy(h)
+        self._plans = {}
+
+    def __del__(self):
+        try:
+            self.release_plans()
+        except Exception:
+            pass
 
     def state(self):
         """Clones of the displacement levels (current first; four with BDF2)."""

@@ -52,25 +52,12 @@ __device__ __forceinline__ void load_dinv(const R* __restrict__ dinv, int64_t t,
 }
 
 // -------------------------------------------------------- tet Hessians ---
+// the 78 packed values of tet e's lifted Hessian
 template <typename R, bool LE>
-__device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e, int disp, int project,
-                                                 R* __restrict__ hbuf);
-// FP32: at most 168 registers so that 3 blocks fit an SM (measured 1.60 -> 1.32 ms of Hessian
-// evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills); FP64 unbounded.
-// LE: the instantiation for linear-elasticity meshes (constant stiffness, no eigensystem)
-template <typename R, bool LE = false>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 3 : 1) k_tet_hessian(TetArgs<R> a, int disp, int project,
-                                                                            R* __restrict__ hbuf) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= a.t) return;
-  tet_hessian_body<R, LE>(a, e, disp, project, hbuf);
-}
-template <typename R, bool LE>
-__device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e, int disp, int project,
-                                                 R* __restrict__ hbuf) {
-  if (a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]) return;
+__device__ __forceinline__ void tet_hessian_values(const TetArgs<R>& a, int64_t e, int disp, int project,
+                                                   R (&out)[kTetHessVals]) {
   const int4 v = __ldg(a.tets + e);
-  R du[9], D[9], G[9], gN[12], out[kTetHessVals];
+  R du[9], D[9], G[9], gN[12];
   if constexpr (sizeof(R) == 8) {
     tet_du(a.u, v, du);
   } else {
@@ -90,15 +77,51 @@ __device__ __forceinline__ void tet_hessian_body(const TetArgs<R>& a, int64_t e,
     le_tet_hessian<R>(mu, lam, vol, gN, out);
   else
     nh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
-  R* o = hbuf + (int64_t)kHStride * e;
-  if constexpr (sizeof(R) == 4) {
+}
+
+// One thread per tet.  FP32: at most 168 registers so that 3 blocks fit an SM (measured 1.60 ->
+// 1.32 ms of Hessian evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills),
+// and the block's records leave through shared memory: every thread stores its 78 values as pairs
+// at a conflict-free stride, then the block writes its tets' contiguous kHStride records with
+// consecutive lanes on consecutive words - one thread storing its own record would touch 32
+// different records with every warp store (ncu: LSU-throttle stalls).  FP64 stores directly.
+// LE: the instantiation for linear-elasticity meshes (constant stiffness, no eigensystem).
+constexpr int kHessThreads = 128;
+constexpr int kHessStage = kTetHessVals + 4;  // staging row stride (82 words: 41 pairs, odd, so the
+                                              // 8-byte stores of a half-warp hit distinct bank pairs)
+
+template <typename R, bool LE = false>
+__global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? 3 : 1) k_tet_hessian(TetArgs<R> a, int disp,
+                                                                                     int project,
+                                                                                     R* __restrict__ hbuf) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = e < a.t && !(a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]);
+  if constexpr (sizeof(R) == 8) {
+    if (!valid) return;
+    R out[kTetHessVals];
+    tet_hessian_values<R, LE>(a, e, disp, project, out);
+    R* o = hbuf + (int64_t)kHStride * e;
 #pragma unroll
-    for (int k = 0; k < kTetHessVals / 2; ++k)
-      reinterpret_cast<float2*>(o)[k] = make_float2(out[2 * k], out[2 * k + 1]);
+    for (int k = 0; k < kTetHessVals / 2; ++k) reinterpret_cast<double2*>(o)[k] = make_double2(out[2 * k], out[2 * k + 1]);
   } else {
+    __shared__ __align__(16) float stage[kHessThreads * kHessStage];
+    __shared__ unsigned char keep[kHessThreads];
+    keep[threadIdx.x] = valid ? 1 : 0;
+    if (valid) {
+      float out[kTetHessVals];
+      tet_hessian_values<float, LE>(a, e, disp, project, out);
+      float2* row = reinterpret_cast<float2*>(stage + threadIdx.x * kHessStage);
 #pragma unroll
-    for (int k = 0; k < kTetHessVals / 2; ++k)
-      reinterpret_cast<double2*>(o)[k] = make_double2(out[2 * k], out[2 * k + 1]);
+      for (int k = 0; k < kTetHessVals / 2; ++k) row[k] = make_float2(out[2 * k], out[2 * k + 1]);
+    }
+    __syncthreads();
+    const int64_t e0 = (int64_t)blockIdx.x * blockDim.x;
+    const int nt = (int)min((int64_t)blockDim.x, a.t - e0);
+    float* dst = hbuf + (int64_t)kHStride * e0;
+    for (int q = threadIdx.x; q < nt * kHStride; q += blockDim.x) {
+      const int tt = q / kHStride, k = q - kHStride * tt;
+      if (k < kTetHessVals && keep[tt]) dst[q] = stage[tt * kHessStage + k];
+    }
   }
 }
 
@@ -156,25 +179,6 @@ __device__ __forceinline__ void fill_record(const AsmArgs<R>& a, int w, const R 
   if (a.colpack) rec_word_store(r, __ldg(a.colpack + w));
 }
 
-// add contribution `code` (tet << 4 | pair) whose 9 stored values are b, in place
-template <typename R>
-__device__ __forceinline__ void add_contribution(int cd, const R* b, R (&acc)[9]) {
-  if (cd < 4) {
-    const R d0 = b[0], d1 = b[1], d2 = b[2], d3 = b[3], d4 = b[4], d5 = b[5];
-    acc[0] += d0; acc[1] += d1; acc[2] += d2;
-    acc[3] += d1; acc[4] += d3; acc[5] += d4;
-    acc[6] += d2; acc[7] += d4; acc[8] += d5;
-  } else if (cd < 10) {
-#pragma unroll
-    for (int m = 0; m < 9; ++m) acc[m] += b[m];
-  } else {
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) acc[3 * i + j] += b[3 * j + i];
-  }
-}
-
 // offset of a contribution's 9 values inside its tet's kHStride record: diagonal block cd < 4
 // (6 stored values, read as 9: the 3 after them are not used and stay inside the record),
 // off-diagonal pair cd - 4 (cd < 10) or its transpose (cd - 10)
@@ -189,20 +193,34 @@ __device__ __forceinline__ int contribution_offset(int cd) {
 // and / or the entry-major block values of the assembled tier (val).
 //
 // A warp owns 32 consecutive slots, whose contributions are one contiguous range of hc_src.
-// The range is staged through shared memory kAsmChunk contributions at a time: the warp loads
-// each contribution's 9 values with 9 consecutive lanes (one or two sectors per contribution,
-// all nine loads of a lane in flight) - one lane per slot issuing 9 scalar loads would touch
-// 32 different tet records per instruction.  Each lane then sums its own slot's contributions
-// from shared memory in list order (a fixed order: bitwise repeatable), and the warp writes its
-// 32 records with 16-byte stores.
+// The range goes through shared memory kAsmChunk contributions at a time: the warp loads each
+// contribution's 9 values with 9 consecutive lanes (one or two sectors per contribution, all
+// nine loads of a lane in flight) - one lane per slot issuing 9 scalar loads would touch 32
+// different tet records per instruction - and stores them already in the slot's orientation
+// (diagonal blocks expanded from their 6 packed values, transposed pairs transposed).  Lane p
+// then takes contribution p of the chunk; a segmented warp scan (segments = slots, whose
+// contributions are contiguous) forms each slot's chunk sum, and the segment's last lane adds
+// it to the slot's accumulator in shared memory.  Every sum's order is fixed by the mesh (chunk
+// boundaries, scan tree), so the records are bitwise repeatable.  The warp writes its 32
+// records with 16-byte stores.
 constexpr int kAsmWarps = 8;
 constexpr int kAsmChunk = 32;
+
+// index, among a contribution's stored values, of entry m (row-major 3x3) of the slot's block
+__device__ __forceinline__ int contribution_entry(int cd, int m) {
+  const int i = m / 3, k = m - 3 * i;
+  if (cd < 4) {  // symmetric diagonal block packed (xx, xy, xz, yy, yz, zz)
+    const int lo = i < k ? i : k, hi = i < k ? k : i;
+    return 3 * lo - (lo * (lo - 1)) / 2 + (hi - lo);
+  }
+  return cd < 10 ? m : 3 * k + i;
+}
 
 template <typename R>
 __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   __shared__ __align__(16) R stage[kAsmWarps][9 * kAsmChunk];
-  __shared__ int scode[kAsmWarps][kAsmChunk];
-  __shared__ __align__(16) R srec[kAsmWarps][kRec * 32];
+  __shared__ __align__(16) R srec[kAsmWarps][kRec * 32];  // the slots' accumulators, then their records
+  __shared__ unsigned char sown[kAsmWarps][kAsmChunk];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t s0 = ((int64_t)blockIdx.x * kAsmWarps + wid) * 32;
   if (s0 >= a.nb) return;  // warp-uniform
@@ -222,15 +240,20 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   const int last = (int)min((int64_t)31, a.nb - 1 - s0);
   const int wb = __shfl_sync(0xffffffffu, cb, 0);
   const int we = __shfl_sync(0xffffffffu, ce, last);
-  R acc[9];
-#pragma unroll
-  for (int m = 0; m < 9; ++m) acc[m] = R(0);
   R* st = stage[wid];
-  int* sc = scode[wid];
+  R* accs = srec[wid];  // 9 per slot while summing
+  unsigned char* own = sown[wid];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) accs[9 * lane + m] = R(0);
   for (int k0 = wb; k0 < we; k0 += kAsmChunk) {
     const int nk = min(kAsmChunk, we - k0);
     const int code = lane < nk ? __ldg(a.hc_src + k0 + lane) : 0;
-    sc[lane] = code;
+    // segment heads and their owner slots: a slot's contributions start at cb - k0, and the slot
+    // whose range holds k0 owns position 0 (exactly one lane meets each condition per position)
+    const bool starts = has && cb > k0 && cb < k0 + nk;
+    if (starts) own[cb - k0] = (unsigned char)lane;
+    if (has && cb <= k0 && k0 < ce) own[0] = (unsigned char)lane;
+    const unsigned heads = __reduce_or_sync(0xffffffffu, starts ? 1u << (cb - k0) : 0u) | 1u;
     R vals[9];
 #pragma unroll
     for (int t = 0; t < 9; ++t) {
@@ -238,15 +261,40 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
       const int cj = j / 9;
       const int cc = __shfl_sync(0xffffffffu, code, cj);
       vals[t] = R(0);
-      if (cj < nk) vals[t] = __ldg(a.hbuf + (int64_t)kHStride * (cc >> 4) + contribution_offset(cc & 15) + (j - 9 * cj));
+      if (cj < nk) {
+        const int cd = cc & 15;
+        vals[t] = __ldg(a.hbuf + (int64_t)kHStride * (cc >> 4) + contribution_offset(cd) +
+                        contribution_entry(cd, j - 9 * cj));
+      }
     }
 #pragma unroll
     for (int t = 0; t < 9; ++t) st[lane + 32 * t] = vals[t];
     __syncwarp();
-    const int lo = max(cb, k0), hi = min(ce, k0 + nk);
-    for (int c = lo; c < hi; ++c) add_contribution<R>(sc[c - k0] & 15, st + 9 * (c - k0), acc);
+    // lane = position p: inclusive segmented scan over [head(p), p]
+    const int hp = lane < nk ? 31 - __clz(heads & (0xffffffffu >> (31 - lane))) : lane;
+    R x[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) x[m] = lane < nk ? st[9 * lane + m] : R(0);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+      for (int m = 0; m < 9; ++m) {
+        const R y = __shfl_up_sync(0xffffffffu, x[m], d);
+        if (lane - d >= hp) x[m] += y;
+      }
+    }
+    const bool tail = lane < nk && (lane == nk - 1 || ((heads >> (lane + 1)) & 1u));
+    if (tail) {
+      R* acc = accs + 9 * own[hp];
+#pragma unroll
+      for (int m = 0; m < 9; ++m) acc[m] += x[m];
+    }
     __syncwarp();
   }
+  R acc[9];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) acc[m] = accs[9 * lane + m];
+  __syncwarp();  // every accumulator is read before the records overwrite the area
   R* my = srec[wid] + kRec * lane;
   if (active) {
     finish_slot(a, v, w, acc);
@@ -566,9 +614,9 @@ template <typename R>
 int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s) {
   if (a.t == 0) return SKG_OK;
   if (a.material == kMatLE)
-    k_tet_hessian<R, true><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
+    k_tet_hessian<R, true><<<blocks_for(a.t, kHessThreads), kHessThreads, 0, s>>>(a, disp, project, hbuf);
   else
-    k_tet_hessian<R, false><<<blocks_for(a.t, 128), 128, 0, s>>>(a, disp, project, hbuf);
+    k_tet_hessian<R, false><<<blocks_for(a.t, kHessThreads), kHessThreads, 0, s>>>(a, disp, project, hbuf);
   SKG_LAUNCHED();
   return SKG_OK;
 }

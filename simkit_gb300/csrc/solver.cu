@@ -1337,6 +1337,15 @@ struct BatchWs {
   int32_t* pcg_it;
   int32_t* pcg_st;
   unsigned* queue;
+  // device-resident Newton loop (batch plans): per-instance control state
+  uint8_t* accept;
+  double* g0;
+  double* fnorm;
+  double* res_prev;
+  double* eta_prev;
+  double* ecur;           // 2 per instance: incremental potential and its magnitude
+  skg_step_info* info;    // n_inst per-instance records, then the total
+  int32_t* ctr;           // loop counters (see BatchCtl)
   int64_t bytes;
 };
 
@@ -1355,6 +1364,14 @@ static BatchWs carve_batch(const skg_tet_mesh* m, const skg_batch* b, int precis
   w.pcg_it = c.take<int32_t>(ni);
   w.pcg_st = c.take<int32_t>(ni);
   w.queue = c.take<unsigned>(8);
+  w.accept = c.take<uint8_t>(ni);
+  w.g0 = c.take<double>(ni);
+  w.fnorm = c.take<double>(ni);
+  w.res_prev = c.take<double>(ni);
+  w.eta_prev = c.take<double>(ni);
+  w.ecur = c.take<double>(2 * ni);
+  w.info = c.take<skg_step_info>(ni + 1);
+  w.ctr = c.take<int32_t>(8);
   w.bytes = w0.bytes + c.off + 256;
   return w;
 }
@@ -1373,24 +1390,36 @@ struct ClassStreams {
 // queue kernel.  The launches run concurrently on their own streams, each with
 // a number of clusters proportional to the block rows of its active instances,
 // so the classes finish together; within a launch, clusters take instances
-// from the range largest first.
+// from the range largest first.  plan_pcg_classes does the host-side part (class
+// ranges, cluster counts, kernel attributes, the class streams); launch_pcg_classes
+// only enqueues, so a graph capture can record it.
+struct PcgClassPlan {
+  int n = 0;
+  int begin[5], end[5], size[5], nclusters[5];
+  bool two_level = false;
+};
+
 template <typename R>
-static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t* rows_h, const int32_t* order_h,
-                            const uint8_t* active_h, int min_cluster, int vec_kb, const uint8_t* active,
-                            const double* eta,
-                            const double* b, const uint8_t* pinned, R* xout, int max_iter, int32_t* it_out,
-                            int32_t* st_out, unsigned* queue, cudaStream_t s, int* launches,
-                            const CoarseDev* cd = nullptr) {
-  const void* kern = cd ? (const void*)k_pcg_cluster_queue<R, kGc, true> : (const void*)k_pcg_cluster_queue<R, kGc, false>;
-  static thread_local bool configured[2] = {false, false};
+static const void* pcg_queue_kernel(bool two_level) {
+  return two_level ? (const void*)k_pcg_cluster_queue<R, kGc, true> : (const void*)k_pcg_cluster_queue<R, kGc, false>;
+}
+
+static ClassStreams& class_streams() {
   static thread_local ClassStreams cs;
-  if (!configured[cd ? 1 : 0]) {
+  return cs;
+}
+
+template <typename R>
+static int plan_pcg_classes(const skg_batch* bt, const int32_t* rows_h, const int32_t* order_h,
+                            const uint8_t* active_h, int min_cluster, int vec_kb, bool two_level, PcgClassPlan* p) {
+  const void* kern = pcg_queue_kernel<R>(two_level);
+  static thread_local bool configured[2] = {false, false};
+  if (!configured[two_level ? 1 : 0]) {
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     SKG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kClusterSmemBudget));
-    configured[cd ? 1 : 0] = true;
+    configured[two_level ? 1 : 0] = true;
   }
-  // with the two-level data the instance's coarse vectors take the last kCoarseSmem bytes
-  const int64_t budget = cd ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
+  ClassStreams& cs = class_streams();
   if (!cs.ready) {
     for (int c = 0; c < 5; ++c) {
       SKG_CUDA(cudaStreamCreateWithFlags(&cs.s[c], cudaStreamNonBlocking));
@@ -1399,6 +1428,8 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
     SKG_CUDA(cudaEventCreateWithFlags(&cs.fork, cudaEventDisableTiming));
     cs.ready = true;
   }
+  // with the two-level data the instance's coarse vectors take the last kCoarseSmem bytes
+  const int64_t budget = two_level ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
   const int ni = bt->n_inst;
   if (min_cluster <= 0) min_cluster = kClusterMinDefault;
   int cmin = 1;
@@ -1417,15 +1448,14 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
     }
     return c;
   };
-  // class ranges along the order, with their active block rows
-  int cls_begin[5], cls_end[5], cls_size[5];
-  double cls_rows[5];
-  int ncls = 0;
-  double total_rows = 0.0;
   // the cluster size never grows along the order (a smaller instance fits wherever a larger
   // one does), so the classes are at most five contiguous ranges
+  double cls_rows[5];
+  double total_rows = 0.0;
   std::vector<int> csz(ni);
   for (int k = 0; k < ni; ++k) csz[k] = k == 0 ? need(order_h[0]) : std::min(need(order_h[k]), csz[k - 1]);
+  p->n = 0;
+  p->two_level = two_level;
   for (int k = 0; k < ni;) {
     const int c = csz[k];
     int e = k;
@@ -1435,24 +1465,61 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
       if (active_h[inst]) w += rows_h[inst + 1] - rows_h[inst];
       ++e;
     }
-    if (ncls == 5) return fail(SKG_ERR_ARG, "batched PCG: more than five cluster sizes");
-    cls_begin[ncls] = k;
-    cls_end[ncls] = e;
-    cls_size[ncls] = c;
-    cls_rows[ncls] = w;
+    if (p->n == 5) return fail(SKG_ERR_ARG, "batched PCG: more than five cluster sizes");
+    p->begin[p->n] = k;
+    p->end[p->n] = e;
+    p->size[p->n] = c;
+    cls_rows[p->n] = w;
     total_rows += w;
-    ++ncls;
+    ++p->n;
     k = e;
   }
-  if (total_rows <= 0.0) return SKG_OK;
+  const int sms = num_sms();
+  for (int c = 0; c < p->n; ++c) {
+    p->nclusters[c] = 0;
+    if (cls_rows[c] <= 0.0) continue;
+    const int csize = p->size[c];
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kClusterThreads, 1, 1);
+    cfg.dynamicSmemBytes = kClusterSmemBudget;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(csize, 1, 1);
+    int fit = 0;
+    SKG_CUDA(cudaOccupancyMaxActiveClusters(&fit, kern, &cfg));
+    if (fit < 1) return fail(SKG_ERR_CUDA, "batched PCG: no cluster of %d CTAs fits", csize);
+    int nclusters = (int)(sms * cls_rows[c] / total_rows / csize + 0.5);
+    if (nclusters < 1) nclusters = 1;
+    if (nclusters > fit) nclusters = fit;
+    if (nclusters > p->end[c] - p->begin[c]) nclusters = p->end[c] - p->begin[c];
+    p->nclusters[c] = nclusters;
+  }
+  return SKG_OK;
+}
+
+template <typename R>
+static int launch_pcg_classes(const PcgClassPlan& p, const Bsr<R>& A, const skg_batch* bt, const uint8_t* active,
+                              const double* eta, const double* b, const uint8_t* pinned, R* xout, int max_iter,
+                              int32_t* it_out, int32_t* st_out, unsigned* queue, cudaStream_t s, int* launches,
+                              const CoarseDev* cd = nullptr) {
+  int any = 0;
+  for (int c = 0; c < p.n; ++c) any += p.nclusters[c];
+  if (any == 0) return SKG_OK;
+  const void* kern = pcg_queue_kernel<R>(p.two_level);
+  const int64_t budget = p.two_level ? kClusterSmemBudget - kCoarseSmem : kClusterSmemBudget;
+  ClassStreams& cs = class_streams();
   SKG_CUDA(cudaMemsetAsync(queue, 0, 8 * sizeof(unsigned), s));
   if (cd) SKG_CUDA(cudaMemsetAsync(cd->rc, 0, sizeof(unsigned long long) * 6 * (size_t)cd->n_agg, s));
   CoarseDev c2 = cd ? *cd : CoarseDev{};
   SKG_CUDA(cudaEventRecord(cs.fork, s));
-  const int sms = num_sms();
-  for (int c = 0; c < ncls; ++c) {
-    if (cls_rows[c] <= 0.0) continue;
-    const int csize = cls_size[c];
+  for (int c = 0; c < p.n; ++c) {
+    if (p.nclusters[c] <= 0) continue;
+    const int csize = p.size[c];
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1464,19 +1531,11 @@ static int launch_pcg_queue(const Bsr<R>& A, const skg_batch* bt, const int32_t*
     cfg.stream = cs.s[c];
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cfg.gridDim = dim3(csize, 1, 1);
-    int fit = 0;
-    SKG_CUDA(cudaOccupancyMaxActiveClusters(&fit, kern, &cfg));
-    if (fit < 1) return fail(SKG_ERR_CUDA, "batched PCG: no cluster of %d CTAs fits", csize);
-    int nclusters = (int)(sms * cls_rows[c] / total_rows / csize + 0.5);
-    if (nclusters < 1) nclusters = 1;
-    if (nclusters > fit) nclusters = fit;
-    if (nclusters > cls_end[c] - cls_begin[c]) nclusters = cls_end[c] - cls_begin[c];
-    cfg.gridDim = dim3(csize * nclusters, 1, 1);
+    cfg.gridDim = dim3(csize * p.nclusters[c], 1, 1);
     SKG_CUDA(cudaStreamWaitEvent(cs.s[c], cs.fork, 0));
     Bsr<R> a2 = A;
-    const int32_t* ord = bt->order + cls_begin[c];
-    int ncls_inst = cls_end[c] - cls_begin[c];
+    const int32_t* ord = bt->order + p.begin[c];
+    int ncls_inst = p.end[c] - p.begin[c];
     double bs = -1.0;
     unsigned* qc = queue + c;
     int smem = (int)budget;
@@ -1687,9 +1746,11 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
     total->t_assemble_ms += pt.end();
     // all active instances' PCG solves, one cluster per instance at a time
     pt.begin();
-    SKG_TRY(launch_pcg_queue<R>(A, bt, rows_h.data(), order_h.data(), active.data(), prm->batch_min_cluster,
-                                prm->batch_vec_kb, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it, bw.pcg_st,
-                                bw.queue, s, &launches, two_level ? &cdev : nullptr));
+    PcgClassPlan cp;
+    SKG_TRY(plan_pcg_classes<R>(bt, rows_h.data(), order_h.data(), active.data(), prm->batch_min_cluster,
+                                prm->batch_vec_kb, two_level, &cp));
+    SKG_TRY(launch_pcg_classes<R>(cp, A, bt, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it,
+                                  bw.pcg_st, bw.queue, s, &launches, two_level ? &cdev : nullptr));
     total->t_pcg_ms += pt.end();
     launches += 2;
     SKG_CUDA(cudaMemcpyAsync(pit.data(), bw.pcg_it, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -1768,6 +1829,512 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   return SKG_OK;
 }
 
+// ------------------------------------------- device-resident batched loop --
+// The batched step of be_step_batched with every per-instance decision made on the device and
+// the whole step recorded once into a CUDA graph (skg_batch_plan).  Newton's relative-residual
+// test, the Eisenstat-Walker forcing, the Armijo search and the stop are small control kernels
+// between the solver's kernels; the Newton iterations and the line-search trials are
+// conditional WHILE nodes whose conditions those kernels set (cudaGraphSetConditional), and the
+// coarse refresh of the first iteration is a conditional IF node.  One graph launch runs the
+// step; the host reads the per-instance records once at the end.  Every decision uses the
+// arithmetic of be_step_batched's host loop, in the same order.
+
+constexpr int kCtlThreads = 512;
+enum { kCtrIter = 0, kCtrTrial = 1, kCtrTrials = 2, kCtrRefresh = 3 };
+
+struct CtlParams {
+  double tol, pcg_rtol, ls_alpha, ls_beta, ls_threshold, eps_r;
+  int max_newton, ls_max_iter, do_line_search, coarse_refresh, has_fext, two_level;
+};
+
+struct BatchCtl {
+  int ni;
+  uint8_t *active, *mask, *accept;
+  double *eta, *steps, *gg, *slope, *e2, *g0, *fnorm, *res_prev, *eta_prev, *ecur;
+  int32_t *pit, *pst, *ctr;
+  skg_step_info* info;
+};
+
+static BatchCtl make_ctl(const BatchWs& bw, int ni) {
+  BatchCtl c{};
+  c.ni = ni;
+  c.active = bw.active; c.mask = bw.mask; c.accept = bw.accept;
+  c.eta = bw.eta; c.steps = bw.steps; c.gg = bw.gg; c.slope = bw.slope; c.e2 = bw.e2; c.g0 = bw.g0;
+  c.fnorm = bw.fnorm; c.res_prev = bw.res_prev; c.eta_prev = bw.eta_prev; c.ecur = bw.ecur;
+  c.pit = bw.pcg_it; c.pst = bw.pcg_st; c.ctr = bw.ctr; c.info = bw.info;
+  return c;
+}
+
+// sum of v over the block (one control block of kCtlThreads)
+__device__ __forceinline__ int ctl_block_sum(int v) {
+  __shared__ int tot;
+  if (threadIdx.x == 0) tot = 0;
+  __syncthreads();
+  if (v) atomicAdd(&tot, v);
+  __syncthreads();
+  const int r = tot;
+  __syncthreads();
+  return r;
+}
+
+// after the first gradient (gg at x_tilde, f_ext's squared norm in fnorm) and energy (e2)
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_begin(BatchCtl c, CtlParams p) {
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    skg_step_info f{};
+    f.min_alpha = 1.0;
+    c.g0[i] = sqrt(c.gg[i]);
+    c.fnorm[i] = p.has_fext ? sqrt(c.fnorm[i]) : 0.0;
+    f.residual0 = c.g0[i];
+    f.residual = c.g0[i] > 0.0 ? 1.0 : 0.0;
+    if (!isfinite(c.g0[i])) f.status = SKG_ERR_NONFINITE;
+    c.info[i] = f;
+    c.res_prev[i] = 1.0;
+    c.eta_prev[i] = 0.0;
+    c.ecur[2 * i] = c.e2[2 * i];
+    c.ecur[2 * i + 1] = c.e2[2 * i + 1];
+  }
+  if (threadIdx.x < 8) c.ctr[threadIdx.x] = 0;
+}
+
+// energy-judged warm start: keep it where the incremental potential is below its value at x_tilde
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_warm(BatchCtl c) {
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    const bool keep = isfinite(c.e2[2 * i]) && c.e2[2 * i] < c.ecur[2 * i];
+    c.mask[i] = keep ? 1 : 0;
+    c.info[i].warm_used = keep ? 1 : 0;
+  }
+}
+
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_take_energy(BatchCtl c) {
+  for (int i = threadIdx.x; i < 2 * c.ni; i += blockDim.x) c.ecur[i] = c.e2[i];
+}
+
+// top of a Newton iteration: convergence test and forcing term per instance; the loop goes on
+// while an instance is active and fewer than max_newton iterations ran
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_newton(BatchCtl c, CtlParams p,
+                                                             cudaGraphConditionalHandle loop) {
+  const int it = c.ctr[kCtrIter];
+  int na = 0;
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    c.active[i] = 0;
+    skg_step_info& f = c.info[i];
+    if (it >= p.max_newton || f.status != SKG_OK || !(c.g0[i] > 0.0)) continue;
+    const double res = sqrt(c.gg[i]) / c.g0[i];
+    f.residual = res;
+    if (res < p.tol || sqrt(c.gg[i]) < 1e-10 * c.fnorm[i]) continue;
+    double e = p.pcg_rtol;
+    if (p.pcg_rtol < 0.0) {
+      const double emax = -p.pcg_rtol;
+      if (it == 0) {
+        e = emax;
+      } else {
+        const double q = res / c.res_prev[i];
+        e = 0.9 * q * q;
+        const double safe = 0.9 * c.eta_prev[i] * c.eta_prev[i];
+        if (safe > 0.1 && safe > e) e = safe;
+      }
+      const double reach = 0.25 * p.tol / res;
+      if (e < reach) e = reach;
+      if (e > emax) e = emax;
+      if (e < 1e-8) e = 1e-8;
+    }
+    c.res_prev[i] = res;
+    c.eta_prev[i] = e;
+    c.eta[i] = e;
+    c.active[i] = 1;
+    ++na;
+  }
+  const int tot = ctl_block_sum(na);
+  if (threadIdx.x == 0) cudaGraphSetConditional(loop, tot > 0 ? 1u : 0u);
+}
+
+// whether this iteration rebuilds the per-instance coarse operators
+__global__ void k_bctl_refresh(BatchCtl c, CtlParams p, cudaGraphConditionalHandle refresh) {
+  const int it = c.ctr[kCtrIter];
+  const bool r = p.two_level && ((it == 0 && p.coarse_refresh >= 0) || p.coarse_refresh > 0);
+  if (r) c.ctr[kCtrRefresh] += 1;
+  cudaGraphSetConditional(refresh, r ? 1u : 0u);
+}
+
+// after the solves: per-instance PCG results, search start (step 1) for the instances that solved
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_search(BatchCtl c, CtlParams p, cudaGraphConditionalHandle ls) {
+  const int it = c.ctr[kCtrIter];
+  int ns = 0;
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    c.mask[i] = 0;
+    c.accept[i] = 0;
+    if (!c.active[i]) continue;
+    skg_step_info& f = c.info[i];
+    f.pcg_iters += c.pit[i];
+    f.newton_iters = it + 1;
+    if (c.pst[i] != 0) {
+      f.status = c.pst[i];
+      c.active[i] = 0;
+      continue;
+    }
+    c.steps[i] = 1.0;
+    c.mask[i] = 1;
+    ++ns;
+  }
+  const int tot = ctl_block_sum(ns);
+  if (threadIdx.x == 0) {
+    c.ctr[kCtrTrial] = 0;
+    cudaGraphSetConditional(ls, tot > 0 && p.ls_max_iter > 0 ? 1u : 0u);
+  }
+}
+
+// one Armijo trial (simkit/backtracking_line_search.py:56-67) for the instances still searching
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_trial(BatchCtl c, CtlParams p, cudaGraphConditionalHandle ls) {
+  int ns = 0;
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    if (!c.mask[i]) continue;
+    skg_step_info& f = c.info[i];
+    f.ls_trials++;
+    const double thr = p.ls_threshold >= 0.0 ? p.ls_threshold : 1e-12 + 16.0 * p.eps_r * c.ecur[2 * i + 1];
+    if (!p.do_line_search || c.e2[2 * i] <= c.ecur[2 * i] + p.ls_alpha * c.steps[i] * c.slope[i] + thr) {
+      c.accept[i] = 1;
+      c.mask[i] = 0;
+      c.ecur[2 * i] = c.e2[2 * i];
+      c.ecur[2 * i + 1] = c.e2[2 * i + 1];
+      if (c.steps[i] < f.min_alpha) f.min_alpha = c.steps[i];
+    } else {
+      c.steps[i] *= p.ls_beta;
+      ++ns;
+    }
+  }
+  const int tot = ctl_block_sum(ns);
+  if (threadIdx.x == 0) {
+    const int k = ++c.ctr[kCtrTrial];
+    c.ctr[kCtrTrials] += 1;
+    cudaGraphSetConditional(ls, tot > 0 && k < p.ls_max_iter ? 1u : 0u);
+  }
+}
+
+// exhausted searches: simkit returns t = 0 and its Newton loop stops
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_searched(BatchCtl c) {
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x)
+    if (c.mask[i]) {
+      c.info[i].status = SKG_ERR_LINESEARCH;
+      c.active[i] = 0;
+    }
+  if (threadIdx.x == 0) c.ctr[kCtrIter] += 1;
+}
+
+// final residuals, statuses and energies; the total record after the instances
+__global__ void __launch_bounds__(kCtlThreads) k_bctl_final(BatchCtl c, CtlParams p) {
+  __shared__ int sn, sp, sl, sfirst;
+  if (threadIdx.x == 0) {
+    sn = sp = sl = 0;
+    sfirst = c.ni;
+  }
+  __syncthreads();
+  int n = 0, pc = 0, l = 0, first = c.ni;
+  for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
+    skg_step_info& f = c.info[i];
+    if (f.status == SKG_OK && c.g0[i] > 0.0) {
+      f.residual = sqrt(c.gg[i]) / c.g0[i];
+      if (!(f.residual < p.tol) && !(sqrt(c.gg[i]) < 1e-10 * c.fnorm[i])) f.status = SKG_ERR_NOT_CONVERGED;
+    }
+    f.energy = c.ecur[2 * i];
+    n += f.newton_iters;
+    pc += f.pcg_iters;
+    l += f.ls_trials;
+    if (f.status != SKG_OK && i < first) first = i;
+  }
+  atomicAdd(&sn, n);
+  atomicAdd(&sp, pc);
+  atomicAdd(&sl, l);
+  atomicMin(&sfirst, first);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    skg_step_info t{};
+    t.newton_iters = sn;
+    t.pcg_iters = sp;
+    t.ls_trials = sl;
+    t.status = sfirst < c.ni ? c.info[sfirst].status : SKG_OK;
+    c.info[c.ni] = t;
+  }
+}
+
+}  // namespace skg
+
+// One batched step recorded as an executable CUDA graph for fixed buffers.
+struct skg_batch_plan {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap[3] = {nullptr, nullptr, nullptr};
+  skg_step_info* info = nullptr;  // device: n_inst records, then the total
+  int32_t* ctr = nullptr;         // device loop counters
+  int ni = 0;
+  // kernel launches: before the loop, per Newton iteration, per search trial, per coarse refresh, after
+  int l_pre = 0, l_iter = 0, l_trial = 0, l_refresh = 0, l_post = 0;
+};
+
+namespace skg {
+
+// a conditional node of `type` at the capture position of `s`, its body graph returned; the
+// capture of `s` continues after the node
+static int add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                           cudaGraph_t* body) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  SKG_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+  if (st != cudaStreamCaptureStatusActive) return fail(SKG_ERR_CUDA, "batch plan: stream is not capturing");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = type;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  SKG_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+  *body = np.conditional.phGraph_out[0];
+  SKG_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return SKG_OK;
+}
+
+// a condition handle of the graph `s` is capturing into
+static int capture_handle(cudaStream_t s, cudaGraphConditionalHandle* h) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  SKG_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr));
+  if (st != cudaStreamCaptureStatusActive) return fail(SKG_ERR_CUDA, "batch plan: stream is not capturing");
+  SKG_CUDA(cudaGraphConditionalHandleCreate(h, g, 0, cudaGraphCondAssignDefault));
+  return SKG_OK;
+}
+
+// Records the batched step into plan->graph with the plan's three capture streams.
+template <typename R>
+static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const skg_be_params* prm,
+                              const skg_be_state* st, void* wsbase, skg_batch_plan* plan) {
+  const int64_t n = m->n_verts, nd = 3 * n;
+  const int ni = bt->n_inst;
+  const bool mixed = sizeof(R) == 4;
+  Workspace w = carve_workspace(m, prm->precision, wsbase);
+  BatchWs bw = carve_batch(m, bt, prm->precision, wsbase);
+  R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
+  R* rec = mixed ? (R*)w.rec32 : (R*)w.rec64;
+  R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
+  R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
+  R* dx = vv[0];
+  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
+  const BatchCtl ctl = make_ctl(bw, ni);
+  plan->info = bw.info;
+  plan->ctr = bw.ctr;
+  plan->ni = ni;
+  const bool two_level = m->coarse && m->coarse->inst_agg && m->coarse->n_inst == bt->n_inst;
+  CoarseDev cdev{};
+  if (two_level) cdev = make_coarse_dev(m, w);
+
+  // host-side preparation: instance offsets and order, the PCG size classes (every instance
+  // counted: the queue kernel skips the inactive ones), the contact planes
+  std::vector<int32_t> rows_h(ni + 1), order_h(ni);
+  SKG_CUDA(cudaMemcpy(rows_h.data(), bt->inst_rows, (ni + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  SKG_CUDA(cudaMemcpy(order_h.data(), bt->order, ni * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> all(ni, 1);
+  PcgClassPlan cp;
+  SKG_TRY(plan_pcg_classes<R>(bt, rows_h.data(), order_h.data(), all.data(), prm->batch_min_cluster,
+                              prm->batch_vec_kb, two_level, &cp));
+  Contact contact;
+  SKG_TRY(make_contact(prm, st, &contact));
+  CtlParams cpar{};
+  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
+  cpar.ls_threshold = prm->ls_threshold; cpar.eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  cpar.max_newton = prm->max_newton; cpar.ls_max_iter = prm->ls_max_iter; cpar.do_line_search = prm->do_line_search;
+  cpar.coarse_refresh = prm->coarse_refresh; cpar.has_fext = st->f_ext != nullptr; cpar.two_level = two_level;
+
+  cudaStream_t s0 = plan->cap[0], s1 = plan->cap[1], s2 = plan->cap[2];
+  double inv_h2 = 0.0;
+  int launches = 0;
+  SKG_CUDA(cudaGraphCreate(&plan->graph, 0));
+  SKG_CUDA(cudaStreamBeginCaptureToGraph(s0, plan->graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+
+  // ---- before the loop: target, first gradient and energy, optional warm start
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s0));
+  SKG_TRY(launch_target(prm, st, nd, w.ut, s0, &inv_h2));
+  launches++;
+  GradArgs ga{};
+  ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
+  ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
+  ga.partials = w.partials; ga.counter = w.counter; ga.out = w.scal + S_GG;
+  ga.contact = contact;
+  EnergyArgs<R> ea{};
+  if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
+  else ea.tet = make_tet_args64(m, st->u);
+  ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  ea.contact = contact;
+  const bool dff = mixed && (m->material == kMatSNH || m->material == kMatMMNH || m->material == kMatLE);
+  if (dff) {
+    SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s0));
+    launches++;
+  }
+  auto gradient = [&](cudaStream_t s) -> int {
+    if (dff) {
+      SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
+      SKG_TRY(launch_forces_df(make_tet_args64(m, st->u), m->dinv32, w.dinv_lo, w.uh, w.ul, w.fbuf, s));
+      launches++;
+    } else {
+      SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    }
+    SKG_TRY(launch_vertex_gradient(ga, s, dff));
+    k_inst_sumsq<<<ni, kBlock, 0, s>>>(w.g, bt->inst_rows, bw.gg);
+    SKG_LAUNCHED();
+    launches += 3;
+    return SKG_OK;
+  };
+  auto energy = [&](const R* d, const double* steps_dev, const uint8_t* mask_dev, cudaStream_t s) -> int {
+    ea.dx = d;
+    SKG_TRY(launch_inst_energy<R>(ea, ni, bt->inst_rows, bt->inst_tets, mask_dev, steps_dev, bw.e2, s));
+    launches++;
+    return SKG_OK;
+  };
+  auto split = [&](cudaStream_t s) -> int {
+    if (!mixed) return SKG_OK;
+    launches++;
+    return launch_split(st->u, n, w.uh, w.ul, s);
+  };
+  if (st->f_ext) {
+    k_inst_sumsq<<<ni, kBlock, 0, s0>>>(st->f_ext, bt->inst_rows, bw.fnorm);
+    SKG_LAUNCHED();
+    launches++;
+  }
+  SKG_TRY(gradient(s0));
+  SKG_TRY(split(s0));
+  SKG_TRY(energy(nullptr, nullptr, nullptr, s0));
+  k_bctl_begin<<<1, kCtlThreads, 0, s0>>>(ctl, cpar);
+  SKG_LAUNCHED();
+  launches++;
+  if (st->u_warm) {
+    SKG_CUDA(cudaMemcpyAsync(st->u, st->u_warm, nd * sizeof(double), cudaMemcpyDeviceToDevice, s0));
+    SKG_TRY(split(s0));
+    SKG_TRY(energy(nullptr, nullptr, nullptr, s0));
+    k_bctl_warm<<<1, kCtlThreads, 0, s0>>>(ctl);
+    SKG_LAUNCHED();
+    k_choose_start<<<blocks_for(n), kBlock, 0, s0>>>(st->u, st->u_warm, w.ut, bw.mask, bt->vert_inst, n);
+    SKG_LAUNCHED();
+    launches += 2;
+    SKG_TRY(split(s0));
+    SKG_TRY(energy(nullptr, nullptr, nullptr, s0));
+    k_bctl_take_energy<<<1, kCtlThreads, 0, s0>>>(ctl);
+    SKG_LAUNCHED();
+    launches++;
+    SKG_TRY(gradient(s0));
+  }
+  cudaGraphConditionalHandle h_loop;
+  SKG_TRY(capture_handle(s0, &h_loop));
+  k_bctl_newton<<<1, kCtlThreads, 0, s0>>>(ctl, cpar, h_loop);
+  SKG_LAUNCHED();
+  launches++;
+  plan->l_pre = launches;
+
+  // ---- the Newton loop
+  cudaGraph_t body = nullptr;
+  SKG_TRY(add_conditional(s0, h_loop, cudaGraphCondTypeWhile, &body));
+  SKG_CUDA(cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  launches = 0;
+  if constexpr (sizeof(R) == 4) {
+    TetArgs<float> ta = make_tet_args32(m, st->u, w.uh, w.ul);
+    ta.tet_inst = bt->tet_inst;
+    ta.inst_active = bw.active;
+    SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s1));
+  } else {
+    TetArgs<double> ta = make_tet_args64(m, st->u);
+    ta.tet_inst = bt->tet_inst;
+    ta.inst_active = bw.active;
+    SKG_TRY(launch_tet_hessian<double>(ta, 1, 1, (double*)hbuf, s1));
+  }
+  AsmArgs<R> aa = make_asm_args<R>(m, hbuf, nullptr, jinv);
+  aa.rec = rec;
+  aa.mass = st->mass;
+  aa.inv_h2 = inv_h2;
+  aa.contact = contact;
+  aa.u = st->u;
+  aa.pinned = st->pinned;
+  aa.vert_inst = bt->vert_inst;
+  aa.inst_active = bw.active;
+  aa.colpack = two_level ? cdev.colpack : nullptr;
+  SKG_TRY(launch_assemble<R>(aa, s1));
+  launches += 2;
+  if (two_level) {
+    cudaGraphConditionalHandle h_ref;
+    SKG_TRY(capture_handle(s1, &h_ref));
+    k_bctl_refresh<<<1, 1, 0, s1>>>(ctl, cpar, h_ref);
+    SKG_LAUNCHED();
+    launches++;
+    cudaGraph_t rbody = nullptr;
+    SKG_TRY(add_conditional(s1, h_ref, cudaGraphCondTypeIf, &rbody));
+    SKG_CUDA(cudaStreamBeginCaptureToGraph(s2, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s2, bt->order));
+    SKG_CUDA(cudaStreamEndCapture(s2, &rbody));
+    plan->l_refresh = 2;
+  }
+  SKG_TRY(launch_pcg_classes<R>(cp, A, bt, bw.active, bw.eta, w.g, st->pinned, dx, prm->pcg_max_iter, bw.pcg_it,
+                                bw.pcg_st, bw.queue, s1, &launches, two_level ? &cdev : nullptr));
+  k_inst_dot<R><<<ni, kBlock, 0, s1>>>(w.g, dx, bt->inst_rows, bw.active, bw.slope);
+  SKG_LAUNCHED();
+  cudaGraphConditionalHandle h_ls;
+  SKG_TRY(capture_handle(s1, &h_ls));
+  k_bctl_search<<<1, kCtlThreads, 0, s1>>>(ctl, cpar, h_ls);
+  SKG_LAUNCHED();
+  launches += 2;
+  {
+    cudaGraph_t lbody = nullptr;
+    SKG_TRY(add_conditional(s1, h_ls, cudaGraphCondTypeWhile, &lbody));
+    SKG_CUDA(cudaStreamBeginCaptureToGraph(s2, lbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    const int before = launches;
+    SKG_TRY(energy(dx, bw.steps, bw.mask, s2));
+    k_bctl_trial<<<1, kCtlThreads, 0, s2>>>(ctl, cpar, h_ls);
+    SKG_LAUNCHED();
+    launches++;
+    plan->l_trial = launches - before;
+    launches = before;
+    SKG_CUDA(cudaStreamEndCapture(s2, &lbody));
+  }
+  k_bctl_searched<<<1, kCtlThreads, 0, s1>>>(ctl);
+  SKG_LAUNCHED();
+  k_apply_step_batched<R><<<blocks_for(n), kBlock, 0, s1>>>(st->u, dx, bw.steps, bw.accept, bt->vert_inst, n,
+                                                            st->pinned);
+  SKG_LAUNCHED();
+  launches += 2;
+  SKG_TRY(split(s1));
+  SKG_TRY(gradient(s1));
+  k_bctl_newton<<<1, kCtlThreads, 0, s1>>>(ctl, cpar, h_loop);
+  SKG_LAUNCHED();
+  launches++;
+  SKG_CUDA(cudaStreamEndCapture(s1, &body));
+  plan->l_iter = launches;
+
+  // ---- after the loop
+  k_bctl_final<<<1, kCtlThreads, 0, s0>>>(ctl, cpar);
+  SKG_LAUNCHED();
+  plan->l_post = 1;
+  SKG_CUDA(cudaStreamEndCapture(s0, &plan->graph));
+  SKG_CUDA(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
+  return SKG_OK;
+}
+
+// ends any capture still open on the plan's streams (after a failure part-way through)
+static void abandon_capture(skg_batch_plan* plan) {
+  for (int k = 2; k >= 0; --k) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (plan->cap[k] && cudaStreamIsCapturing(plan->cap[k], &st) == cudaSuccess && st != cudaStreamCaptureStatusNone) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(plan->cap[k], &g);
+    }
+  }
+  (void)cudaGetLastError();
+}
+
+static void release_plan(skg_batch_plan* plan) {
+  if (!plan) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  for (int k = 0; k < 3; ++k)
+    if (plan->cap[k]) cudaStreamDestroy(plan->cap[k]);
+  delete plan;
+}
+
 }  // namespace skg
 
 using namespace skg;
@@ -1821,6 +2388,62 @@ int skg_be_step_batched(const skg_tet_mesh* mesh, const skg_batch* batch, const 
   if (params->precision == SKG_MIXED)
     return be_step_batched<float>(mesh, batch, params, state, workspace, infos_h, total_h, s);
   return be_step_batched<double>(mesh, batch, params, state, workspace, infos_h, total_h, s);
+}
+
+static int check_batch_args(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
+                            const skg_be_state* state, const void* workspace) {
+  if (!batch || !params || !state || !workspace) return fail(SKG_ERR_ARG, "batch plan: null argument");
+  SKG_TRY(check_mesh(mesh, params->precision));
+  if (batch->n_inst <= 0 || !batch->inst_rows || !batch->inst_tets || !batch->vert_inst || !batch->tet_inst ||
+      !batch->order)
+    return fail(SKG_ERR_ARG, "batch plan: incomplete batch description");
+  if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "batch plan: dt must be positive");
+  if (!state->u || !state->u_curr || !state->u_prev || !state->mass) return fail(SKG_ERR_ARG, "batch plan: null state");
+  SKG_TRY(check_integrator(params, state));
+  return SKG_OK;
+}
+
+int skg_be_batch_plan_create(const skg_tet_mesh* mesh, const skg_batch* batch, const skg_be_params* params,
+                             const skg_be_state* state, void* workspace, skg_batch_plan** plan_h) {
+  if (!plan_h) return fail(SKG_ERR_ARG, "batch plan: null plan pointer");
+  *plan_h = nullptr;
+  SKG_TRY(check_batch_args(mesh, batch, params, state, workspace));
+  skg_batch_plan* plan = new skg_batch_plan();
+  for (int k = 0; k < 3; ++k) {
+    if (cudaStreamCreateWithFlags(&plan->cap[k], cudaStreamNonBlocking) != cudaSuccess) {
+      release_plan(plan);
+      return fail(SKG_ERR_CUDA, "batch plan: stream creation failed");
+    }
+  }
+  const int r = params->precision == SKG_MIXED
+                    ? capture_batch_step<float>(mesh, batch, params, state, workspace, plan)
+                    : capture_batch_step<double>(mesh, batch, params, state, workspace, plan);
+  if (r != SKG_OK) {
+    abandon_capture(plan);
+    release_plan(plan);
+    return r;
+  }
+  *plan_h = plan;
+  return SKG_OK;
+}
+
+int skg_be_batch_plan_step(skg_batch_plan* plan, skg_step_info* infos_h, skg_step_info* total_h, void* stream) {
+  if (!plan || !plan->exec || !infos_h || !total_h) return fail(SKG_ERR_ARG, "batch plan step: null argument");
+  cudaStream_t s = as_stream(stream);
+  SKG_CUDA(cudaGraphLaunch(plan->exec, s));
+  int32_t ctr[8];
+  SKG_CUDA(cudaMemcpyAsync(infos_h, plan->info, plan->ni * sizeof(skg_step_info), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaMemcpyAsync(total_h, plan->info + plan->ni, sizeof(skg_step_info), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaMemcpyAsync(ctr, plan->ctr, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+  SKG_CUDA(cudaStreamSynchronize(s));
+  total_h->launches = plan->l_pre + ctr[kCtrIter] * plan->l_iter + ctr[kCtrTrials] * plan->l_trial +
+                      ctr[kCtrRefresh] * plan->l_refresh + plan->l_post;
+  return SKG_OK;
+}
+
+int skg_be_batch_plan_destroy(skg_batch_plan* plan) {
+  release_plan(plan);
+  return SKG_OK;
 }
 
 }  // extern "C"

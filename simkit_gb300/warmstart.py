@@ -73,6 +73,14 @@ class WarmStartMLP:
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.scratch = torch.zeros(2056, dtype=torch.float64, device=device)
 
+    def refresh_bf16(self):
+        """Rebuild the BF16 copies the GEMMs read (W and W^T, padded) from the FP32 masters - after
+        the masters were loaded from a checkpoint (the Adam kernel keeps them in step otherwise)."""
+        for li, (k, n) in enumerate(DIMS):
+            self.W16[li].copy_(self.W[li].bfloat16())
+            self.WT16[li].zero_()
+            self.WT16[li][:, :n] = self.W[li].T.bfloat16()
+
     # -------------------------------------------------------------- GEMM
     def _gemm(self, A, B, Nc, epi, bias=None, out_f=None, out_z=None, out_h=None, Nstore=None, ld_out=None,
               splits=1):

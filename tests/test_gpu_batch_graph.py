@@ -1,0 +1,83 @@
+"""The batched step with the Newton loop on the device (one CUDA graph launch per step: per-instance
+decisions in control kernels, Newton iterations and line-search trials as conditional graph nodes)
+against the host-driven batched step, which makes the same decisions with the same arithmetic on the
+host: bitwise the same positions and the same per-instance records, for backward Euler and BDF2, with
+the learned warm start's energy-judged choice, with contact planes, and when the PCG is starved."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(specs, **kw):
+    from simkit_gb300.batched import BatchedBESolver
+    g = BatchedBESolver(specs, graph=True, **kw)
+    h = BatchedBESolver(specs, graph=False, **kw)
+    return g, h
+
+
+def _same_records(ig, tg, ih, th):
+    for a, b in zip(ig, ih):
+        assert (a.newton_iters, a.pcg_iters, a.ls_trials, a.status, a.warm_used) == \
+               (b.newton_iters, b.pcg_iters, b.ls_trials, b.status, b.warm_used)
+        assert a.residual0 == b.residual0 and a.residual == b.residual
+        assert a.min_alpha == b.min_alpha and a.energy == b.energy
+    assert (tg.newton_iters, tg.pcg_iters, tg.ls_trials, tg.status) == \
+           (th.newton_iters, th.pcg_iters, th.ls_trials, th.status)
+
+
+@pytest.mark.parametrize("coarse", ["auto", None])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_step_equals_host_driven_step(coarse, precision):
+    from simkit_gb300.beams import beam_batch
+    specs = beam_batch(12, seed=7, nx_range=(4, 10), ny_range=(4, 8), nz_range=(8, 24))
+    g, h = _pair(specs, coarse=coarse, precision=precision)
+    for _ in range(4):
+        ig, tg = g.step()
+        ih, th = h.step()
+        assert tg.status == 0 and th.status == 0
+        _same_records(ig, tg, ih, th)
+        assert torch.equal(g.u_curr, h.u_curr)
+    assert len(g._plans) == 3          # one graph per rotation of the three state buffers
+    assert tg.launches > 0
+
+
+def test_graph_step_bdf2_with_contact_and_warm_start():
+    from simkit_gb300.beams import beam_batch
+    specs = beam_batch(6, seed=9, nx_range=(4, 8), ny_range=(4, 6), nz_range=(8, 16))
+    floor = [(1.0e4, (0.0, -0.01, 0.0), (0.0, 1.0, 0.0))]
+    g, h = _pair(specs, integrator="bdf2", contact_planes=floor)
+    rng = np.random.default_rng(0)
+    for k in range(5):
+        warm = None
+        if k >= 2:   # a perturbed prediction: the energy test keeps it for some instances only
+            warm = g.u_curr + 1e-4 * torch.from_numpy(rng.standard_normal(g.u_curr.numel())).cuda()
+        ig, tg = g.step(u_warm=warm)
+        ih, th = h.step(u_warm=warm)
+        _same_records(ig, tg, ih, th)
+        assert torch.equal(g.u_curr, h.u_curr)
+    assert len(g._plans) == 5          # BDF2 rotates five buffers (steps 0-1 plain, 2-4 with the warm start)
+
+
+def test_graph_reports_failures_like_the_host_loop():
+    """A one-iteration PCG cap: every instance ends not converged after max_newton iterations, with
+    the same records on both paths; parameters changed afterwards re-record the graphs."""
+    from simkit_gb300 import _lib
+    from simkit_gb300.beams import beam_batch
+    specs = beam_batch(5, seed=4, nx_range=(4, 6), ny_range=(4, 5), nz_range=(8, 12))
+    g, h = _pair(specs, pcg_max_iter=1, max_newton=3, coarse=None)
+    ig, tg = g.step()
+    ih, th = h.step()
+    _same_records(ig, tg, ih, th)
+    assert all(i.status == _lib.SKG_ERR_NOT_CONVERGED and i.newton_iters == 3 for i in ig)
+    assert tg.status == _lib.SKG_ERR_NOT_CONVERGED
+    for s in (g, h):
+        s.params.pcg_max_iter = 4000
+        s.params.max_newton = 20
+    ig, tg = g.step()
+    ih, th = h.step()
+    _same_records(ig, tg, ih, th)
+    assert tg.status == 0
+    assert torch.equal(g.u_curr, h.u_curr)

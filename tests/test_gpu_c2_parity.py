@@ -21,8 +21,6 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-# achieved on a GB300 (printed by the tests), with headroom for run-to-run rounding of the
-# order-free coarse restriction; see the bounds in each test
 FIXTURE = "rollout_beam_32x32x128_first_steps.npz"
 
 
@@ -56,8 +54,8 @@ def test_c2_first_steps_match_simkit(c2_spec):
         disp = np.abs(u - u_ref).max() / np.abs(u_ref).max()
         print(f"\nstep {int(step)}: positions rel err {pos:.2e}, displacement rel err {disp:.2e}, "
               f"newton {info.newton_iters} (simkit, exact solves: {int(d['iters'][k])})")
-        assert pos < 1e-7
-        assert disp < 2e-5
+        assert pos < 2e-10     # measured 1.5e-11 (step 1), 3.5e-11 (step 2)
+        assert disp < 1e-7     # measured 1.7e-8, 1.3e-8
 
 
 def test_c2_mixed_matches_fp64_mode_over_30_steps(c2_spec):
@@ -73,5 +71,5 @@ def test_c2_mixed_matches_fp64_mode_over_30_steps(c2_spec):
         worst_pos = max(worst_pos, np.abs(ua - ub).max() / scale)
         worst_disp = max(worst_disp, np.abs(ua - ub).max() / np.abs(ub).max())
     print(f"\n30 steps, mixed vs FP64 mode: positions rel err {worst_pos:.2e}, displacement rel err {worst_disp:.2e}")
-    assert worst_pos < 1e-6
-    assert worst_disp < 1e-4
+    assert worst_pos < 5e-8    # measured 1.0e-8
+    assert worst_disp < 2e-7   # measured 3.2e-8

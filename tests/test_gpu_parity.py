@@ -3,8 +3,11 @@
 Tolerances (stated per check):
 * FP64 kernels vs the reference: 1e-12 relative (element tier), 1e-10 (assembled).
 * FP32 ("mixed") element Hessians: 3e-6 relative to the block's largest entry.
-* Rollouts: positions within 1e-5 relative to the reference after every
-  stored step (the stated parity bar), displacements within 1e-3.
+* Rollouts: positions relative to the largest rest coordinate and displacements relative to the
+  largest reference displacement, at every stored step; each bound sits about 5x above the error
+  measured on a GB300 (written beside it).  Rollouts stop Newton at a 1e-6 relative residual, so
+  where this solver's inexact Newton and the reference's exact one take different paths the
+  displacements agree to ~1e-7 in either precision; with tight PCG tolerances FP64 agrees to ~1e-14.
 """
 
 import os
@@ -172,7 +175,7 @@ def test_be_step_fp64_matches_reference_rollout(api):
         assert info.converged, info
         k = list(d["steps"]).index(step)
         u = s.displacement()
-        _rollout_check(X, u, d["u"][k], 1e-7, 1e-4)
+        _rollout_check(X, u, d["u"][k], 1e-13, 1e-12)   # measured 1.9e-16 / 1.4e-14
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -191,7 +194,9 @@ def test_bdf2_step_matches_reference_rollout(api, precision):
         assert info.converged, info
         k = list(d["steps"]).index(step)
         u = s.displacement()
-        _rollout_check(X, u, d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
+        # measured FP64 2.7e-16 / 2.1e-14, mixed 2.9e-9 / 6.8e-8
+        _rollout_check(X, u, d["u"][k], 1e-13 if precision == "fp64" else 2e-8,
+                       1e-12 if precision == "fp64" else 4e-7)
 
 
 def test_bdf2_batched_equals_single(api):
@@ -294,7 +299,9 @@ def test_mmnh_be_step_matches_reference_rollout(api, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
+        # measured FP64 1.9e-16 / 1.0e-14, mixed 1.6e-8 / 2.9e-7
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-13 if precision == "fp64" else 1e-7,
+                       1e-12 if precision == "fp64" else 1.5e-6)
 
 
 def _corot_entry(api, material, kind):
@@ -379,7 +386,9 @@ def test_corot_be_step_matches_reference_rollout(api, material, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
+        # measured FP64 <= 3.9e-15 / 1.0e-13, mixed <= 1.1e-8 / 1.7e-7
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-13 if precision == "fp64" else 6e-8,
+                       1e-12 if precision == "fp64" else 1e-6)
 
 
 @pytest.mark.parametrize("d", [3, 2])
@@ -431,8 +440,9 @@ def test_le_assembled_and_rollout_match_reference(api, precision):
         info = s.step()
         assert info.converged, info
         k = list(d["steps"]).index(step)
-        _rollout_check(Xb, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5,
-                       1e-4 if precision == "fp64" else 1e-3)
+        # measured FP64 1.7e-14 / 1.2e-12, mixed 5.4e-11 / 3.4e-9
+        _rollout_check(Xb, s.displacement(), d["u"][k], 1e-13 if precision == "fp64" else 3e-10,
+                       1e-11 if precision == "fp64" else 2e-8)
 
 
 def test_corot_batched_equals_single(api):
@@ -520,7 +530,9 @@ def test_contact_rollout_matches_reference(api, precision):
         info = s.step()
         assert info.converged, (step, info)
         k = list(d["steps"]).index(step)
-        _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
+        # measured FP64 1.9e-16 / 1.0e-14, mixed 4.1e-9 / 1.2e-7
+        _rollout_check(X, s.displacement(), d["u"][k], 1e-13 if precision == "fp64" else 2e-8,
+                       1e-12 if precision == "fp64" else 7e-7)
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -538,7 +550,7 @@ def test_two_barrier_grid_pcg_matches_reference(api, precision):
         assert info.converged, (step, info)
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
+            _rollout_check(X, s.displacement(), d["u"][k], 1e-7, 5e-7)   # measured 2.0e-8 / 9.8e-8
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
@@ -565,7 +577,7 @@ def test_two_level_pcg_matches_reference(api, precision, refresh):
         pcg_one += info1.pcg_iters
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
+            _rollout_check(X, s.displacement(), d["u"][k], 5e-7, 1.5e-6)   # measured <= 9.8e-8 / 2.6e-7
     print(f"\n{precision}/{refresh}: PCG iterations two-level {pcg_two}, one-level {pcg_one}")
     assert 2 * pcg_two < pcg_one
 
@@ -587,7 +599,7 @@ def test_two_level_grid_block_shapes(api, variant):
         assert info.converged, (step, info)
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            _rollout_check(X, s.displacement(), d["u"][k], 1e-5, 1e-3)
+            _rollout_check(X, s.displacement(), d["u"][k], 5e-7, 1.5e-6)   # measured 7.3e-8 / 2.5e-7
 
 
 def test_two_level_repeatable(api):
@@ -717,11 +729,11 @@ def test_rollout_8x8x32_matches_reference(api, precision):
             u = s.displacement()
             worst_pos = max(worst_pos, _rel(X + u, X + d["u"][k]))
             worst_u = max(worst_u, _rel(u, d["u"][k]))
-            _rollout_check(X, u, d["u"][k], 1e-5, 1e-3)
+            _rollout_check(X, u, d["u"][k], 5e-7, 1.5e-6)   # measured 7.3e-8 / 2.5e-7 in both precisions
     print(f"\n{precision}: positions rel err {worst_pos:.2e}, displacement rel err {worst_u:.2e}, "
           f"newton iters {sum(iters)} (reference {int(d['iters'].sum())})")
-    assert worst_pos < 1e-5
-    assert worst_u < 1e-3
+    assert worst_pos < 5e-7
+    assert worst_u < 1.5e-6
 
 
 def test_nonfinite_input_is_reported(api):
@@ -760,7 +772,7 @@ def test_cluster_two_level_small_beam(api, precision):
         one_it += info1.pcg_iters
         if step in d["steps"]:
             k = list(d["steps"]).index(step)
-            _rollout_check(X, s.displacement(), d["u"][k], 1e-7 if precision == "fp64" else 1e-5, 1e-4 if precision == "fp64" else 1e-3)
+            _rollout_check(X, s.displacement(), d["u"][k], 5e-7, 1.5e-6)   # measured 7.3e-8 / 2.5e-7
     print(f"\n{precision}: PCG iterations cluster two-level {two_it}, one-level {one_it}")
     assert 2 * two_it < one_it
 
@@ -820,7 +832,7 @@ def test_batched_step_matches_single_instance_and_oracle(api):
             X = sp.X.reshape(-1)
             ub = b.displacement(i)
             assert _rel(X + ub, X + singles[i].displacement()) < 1e-7
-            _rollout_check(X, ub, xn.ravel() - X, 1e-5, 1e-3)
+            _rollout_check(X, ub, xn.ravel() - X, 1e-8, 2e-6)   # measured 1.1e-9 / 3.4e-7
 
 
 def test_self_contained_tier_matches_reference(api):
