@@ -302,6 +302,82 @@ def parity_report(spec, solver_kw, steps_fp64=30):
     return out
 
 
+def batched_summary(instances=128, steps=4, warmup=3, plain_sample=4, train_steps=12, seed=0):
+    """Reduced 512-beam workload for the headline line: ``instances`` beams of the same seeded
+    distribution (nx, ny in 4..16, nz in 8..48, own E, nu and gravity direction) stepped together
+    (the device-resident Newton loop: one graph launch per step), against a sample of the same beams
+    stepped one at a time by the single-instance solver (two-level cluster PCG and the one-level
+    block-Jacobi form first specified), and the batch with the learned warm start (a network
+    trained here on frames of a separately seeded batch).  Times by CUDA events; not part of the
+    headline's timed region."""
+    import torch
+    from simkit_gb300 import warmstart as wsm
+    from simkit_gb300.autotune import tune_pcg_variant
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    from simkit_gb300.solver import BESolver
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = [fn() for _ in range(k)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    specs = beam_batch(instances, seed=seed)
+    b = BatchedBESolver(specs)
+    for _ in range(warmup):
+        b.step()
+    ms, outs = timed(b.step, steps)
+    if any(t.status != 0 for _, t in outs):
+        raise SystemExit("batched summary: a step failed")
+    batched = instances * steps / (ms / 1000.0)
+    newton = sum(t.newton_iters for _, t in outs) / (instances * steps)
+    pick = np.random.default_rng(1).choice(instances, size=plain_sample, replace=False)
+
+    def plain(coarse):
+        per = []
+        for i in pick:
+            s1 = BESolver.from_spec(specs[i], coarse=coarse)
+            for _ in range(warmup):
+                s1.step()
+            tune_pcg_variant(s1)
+            m1, _ = timed(s1.step, steps)
+            per.append(m1 / steps)
+        return 1000.0 / float(np.mean(per))
+    plain_2l, plain_bj = plain("auto"), plain(None)
+    # learned warm start: trained on a separate seeded batch of the same distribution
+    tspecs = beam_batch(instances, seed=100 + seed)
+    tb = BatchedBESolver(tspecs)
+    frames, _ = wsm.generate_frames(tb, tspecs, train_steps)
+    net = wsm.WarmStartMLP(seed=0, lr=1e-3)
+    wsm.train(net, tb, frames, epochs=2, batch_frames=64)
+    del frames, tb
+    bl = BatchedBESolver(specs)
+    fb = wsm.FeatureBuilder(bl, specs)
+    for _ in range(warmup):
+        ut = fb.u_tilde()
+        bl.step()
+        fb.record_correction(ut)
+    ml, louts = timed(lambda: wsm.warm_step(bl, fb, net), steps)
+    learned = instances * steps / (ml / 1000.0)
+    return {
+        "workload": f"{instances} beams of the 512-beam distribution, {steps} timed steps after {warmup}",
+        "batched_instance_steps_per_s": batched, "newton_iters_per_instance_step": newton,
+        "plain_single_instance": plain_2l, "plain_single_instance_block_jacobi": plain_bj,
+        "plain_sample": f"{plain_sample} of the beams stepped alone, {steps} steps each after {warmup}",
+        "batched_over_plain": batched / plain_2l, "batched_over_plain_block_jacobi": batched / plain_bj,
+        "learned_instance_steps_per_s": learned,
+        "learned_newton_iters_per_instance_step": sum(t.newton_iters for _, t in louts) / (instances * steps),
+        "learned_kept_fraction": float(np.mean([sum(i.warm_used for i in inf) / len(inf) for inf, _ in louts])),
+        "learned_over_plain_block_jacobi": learned / plain_bj,
+        "learned_training": f"{instances} beams x {train_steps} steps of frames, 2 epochs, Adam lr 1e-3",
+    }
+
+
 def run_reference(args):
     """The reference's CPU path (the oracle restatement of simkit's algorithm) on the machine's host:
     each bench step is one measured backward-Euler step of a slab of the workload beam, the direct
@@ -593,6 +669,7 @@ def main():
                          "modes use --pcg-rtol); -0.3 measured fastest on the 786,432-tet beam")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity report of the headline line")
+    ap.add_argument("--no-batched", action="store_true", help="skip the reduced batched workload of the headline line")
     ap.add_argument("--ref-layers", type=int, default=2,
                     help="cube layers of the workload beam in the CPU reference sample (2: 12,288 tets, "
                          "about 1 s per measured step)")
@@ -751,6 +828,9 @@ def main():
     parity = None
     if rank == 0 and not args.small and not args.no_parity:
         parity = parity_report(spec, solver_kw)
+    batched = None
+    if rank == 0 and not args.small and not args.no_batched:
+        batched = batched_summary()
 
     if rank == 0:
         line = {
@@ -772,6 +852,7 @@ def main():
             "roofline": roof,
             "cpu_baseline": cpu,
             "parity": parity,
+            "batched": batched,
             "clocks": clock_info,
         }
         print(json.dumps(line))

@@ -221,6 +221,10 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   __shared__ __align__(16) R stage[kAsmWarps][9 * kAsmChunk];
   __shared__ __align__(16) R srec[kAsmWarps][kRec * 32];  // the slots' accumulators, then their records
   __shared__ unsigned char sown[kAsmWarps][kAsmChunk];
+  __shared__ int sentry[16 * 9];  // [pair code][entry]: offset in the tet record, in the slot's orientation
+  for (int i = threadIdx.x; i < 16 * 9; i += blockDim.x)
+    sentry[i] = contribution_offset(i / 9) + contribution_entry(i / 9, i - 9 * (i / 9));
+  __syncthreads();
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t s0 = ((int64_t)blockIdx.x * kAsmWarps + wid) * 32;
   if (s0 >= a.nb) return;  // warp-uniform
@@ -261,11 +265,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
       const int cj = j / 9;
       const int cc = __shfl_sync(0xffffffffu, code, cj);
       vals[t] = R(0);
-      if (cj < nk) {
-        const int cd = cc & 15;
-        vals[t] = __ldg(a.hbuf + (int64_t)kHStride * (cc >> 4) + contribution_offset(cd) +
-                        contribution_entry(cd, j - 9 * cj));
-      }
+      if (cj < nk) vals[t] = __ldg(a.hbuf + (int64_t)kHStride * (cc >> 4) + sentry[9 * (cc & 15) + (j - 9 * cj)]);
     }
 #pragma unroll
     for (int t = 0; t < 9; ++t) st[lane + 32 * t] = vals[t];

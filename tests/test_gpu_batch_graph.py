@@ -81,3 +81,36 @@ def test_graph_reports_failures_like_the_host_loop():
     _same_records(ig, tg, ih, th)
     assert tg.status == 0
     assert torch.equal(g.u_curr, h.u_curr)
+
+
+def test_real_distribution_beams_match_oracle():
+    """Beams drawn from the benchmarked 512-beam batch itself (seed 0: the smallest, the median and the
+    90th-percentile instance, 1,200 to 36,288 tets, each with its own E, nu and gravity direction),
+    stepped in one batch with the default settings (mixed precision, two-level cluster PCG, device
+    Newton loop), against the FP64 oracle's first two steps."""
+    from oracle import rollout
+    from simkit_gb300.batched import BatchedBESolver
+    from simkit_gb300.beams import beam_batch
+    every = beam_batch(512, seed=0)
+    sizes = np.array([s.n_tets for s in every])
+    order = np.argsort(sizes, kind="stable")
+    specs = [every[int(order[0])], every[int(order[len(order) // 2])], every[int(order[int(0.9 * len(order))])]]
+    b = BatchedBESolver(specs)
+    refs = [rollout.from_spec(sp) for sp in specs]
+    states = [(r.x_rest.copy(), r.x_rest.copy()) for r in refs]
+    worst_pos = worst_disp = 0.0
+    for _ in range(2):
+        infos, total = b.step()
+        assert total.status == 0, total
+        for i, sp in enumerate(specs):
+            xc, xp = states[i]
+            xn, info = refs[i].step(xc, xp)
+            assert info.converged
+            states[i] = (xn, xc)
+            X = sp.X.reshape(-1)
+            u, u_ref = b.displacement(i), xn.ravel() - X
+            worst_pos = max(worst_pos, np.abs(u - u_ref).max() / np.abs(X).max())
+            worst_disp = max(worst_disp, np.abs(u - u_ref).max() / np.abs(u_ref).max())
+    print(f"\nreal-distribution beams vs oracle: positions rel err {worst_pos:.2e}, displacement rel err {worst_disp:.2e}")
+    assert worst_pos < 1e-7
+    assert worst_disp < 5e-6
