@@ -459,7 +459,7 @@ def run_serving(args):
         net, learned = train_warm_start(args)
     reqs = request_stream(args.rate, args.duration, steps=10, seed=0)
     srv = BeamServer(max_cohort=args.max_cohort, max_live=args.max_live, net=net, precision=args.precision,
-                     pcg_rtol=args.pcg_rtol, coarse=args.coarse != "none")
+                     pcg_rtol=args.pcg_rtol, coarse=args.coarse != "none", graph=not args.no_graph)
     # the shape catalog (every nx, ny in 4..16, nz in 8..48) is built before traffic starts
     catalog = [(a, b, c) for a in range(4, 17) for b in range(4, 17) for c in range(8, 49)]
     srv.prewarm(catalog)
@@ -477,7 +477,8 @@ def run_serving(args):
                                "(nx, ny in 4..16, nz in 8..48) asking for 10 backward-Euler steps"
                                + (", learned warm start" if args.learned else ", plain Newton"),
                    "rate": args.rate, "duration_s": args.duration, "max_cohort": args.max_cohort,
-                   "max_live": args.max_live, "precision": args.precision},
+                   "max_live": args.max_live, "precision": args.precision,
+                   "newton_loop": "host" if args.no_graph else "device (CUDA graph)"},
         "serving": sm, "learned": learned, "clocks": clock_info,
         "catalog": {"shapes": len(srv.cache.shapes), "build_s": srv.prewarm_s,
                     "device_bytes": srv.cache.bytes},
@@ -505,7 +506,8 @@ def run_batched(args):
     # the same preconditioner on both sides of the comparison: two-level (per-instance
     # aggregates) unless --coarse none
     coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
-    b = BatchedBESolver(specs, precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=coarse)
+    b = BatchedBESolver(specs, precision=args.precision, pcg_rtol=args.pcg_rtol, coarse=coarse,
+                        graph=not args.no_graph)
     for _ in range(args.warmup):
         infos, total = b.step()
         if total.status != 0:
@@ -624,7 +626,8 @@ def run_batched(args):
                                + ("+ learned warm start" if args.learned else "plain Newton"),
                    "instances": args.instances, "tets": int(tets), "verts": int(verts),
                    "precision": args.precision, "pcg_rtol": args.pcg_rtol, "coarse": args.coarse,
-                   "parallelism": f"instances sharded x{n_ranks} (LPT on tet count)"},
+                   "parallelism": f"instances sharded x{n_ranks} (LPT on tet count)",
+                   "newton_loop": "host" if args.no_graph else "device (CUDA graph)"},
         "tet_hessians_per_s": newton / max(args.instances, 1) * tets / (ms / 1000.0),
         "newton_iters_per_instance_step": newton / inst_steps,
         "pcg_iters_per_instance_step": pcg / inst_steps,
@@ -660,8 +663,9 @@ def main():
     ap.add_argument("--pcg-mode", type=int, default=3)
     ap.add_argument("--coarse", default="auto",
                     help="two-level PCG aggregates: none, auto, or a box size in mesh spacings")
-    ap.add_argument("--coarse-refresh", default=4, type=_refresh_arg,
-                    help="'step', 'newton' or k: rebuild the coarse inverse every k steps")
+    ap.add_argument("--coarse-refresh", default=8, type=_refresh_arg,
+                    help="'step', 'newton' or k: rebuild the coarse inverse every k steps (8 measured "
+                         "fastest on the 786,432-tet beam, with the same PCG iteration counts as 4)")
     ap.add_argument("--pcg-rtol", type=float, default=-0.1,
                     help="PCG tolerance; negative = Eisenstat-Walker forcing capped at its magnitude")
     ap.add_argument("--pcg-rtol-single", type=float, default=-0.3,
@@ -670,6 +674,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity report of the headline line")
     ap.add_argument("--no-batched", action="store_true", help="skip the reduced batched workload of the headline line")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="batched and serving workloads: the host-driven Newton loop instead of the device loop")
     ap.add_argument("--ref-layers", type=int, default=2,
                     help="cube layers of the workload beam in the CPU reference sample (2: 12,288 tets, "
                          "about 1 s per measured step)")

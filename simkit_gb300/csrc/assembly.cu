@@ -115,12 +115,16 @@ __global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? 3 : 1) k_tet_he
       for (int k = 0; k < kTetHessVals / 2; ++k) row[k] = make_float2(out[2 * k], out[2 * k + 1]);
     }
     __syncthreads();
+    // each warp writes whole records: 39 pairs per tet (the 78 values), lanes on consecutive pairs
     const int64_t e0 = (int64_t)blockIdx.x * blockDim.x;
     const int nt = (int)min((int64_t)blockDim.x, a.t - e0);
-    float* dst = hbuf + (int64_t)kHStride * e0;
-    for (int q = threadIdx.x; q < nt * kHStride; q += blockDim.x) {
-      const int tt = q / kHStride, k = q - kHStride * tt;
-      if (k < kTetHessVals && keep[tt]) dst[q] = stage[tt * kHessStage + k];
+    const int lane = threadIdx.x & 31;
+    for (int tt = threadIdx.x >> 5; tt < nt; tt += blockDim.x >> 5) {
+      if (!keep[tt]) continue;  // warp-uniform
+      const float2* src = reinterpret_cast<const float2*>(stage + tt * kHessStage);
+      float2* dst = reinterpret_cast<float2*>(hbuf + (int64_t)kHStride * (e0 + tt));
+      dst[lane] = src[lane];
+      if (lane < kTetHessVals / 2 - 32) dst[32 + lane] = src[32 + lane];
     }
   }
 }

@@ -83,7 +83,8 @@ class BESolver:
     contact_planes : optional list of (k, p, n) contact-spring planes added to the potential
     coarse : two-level PCG preconditioner (block Jacobi + rigid-mode aggregates of box^3 mesh
         spacings): None (one-level), 'auto' or a box size.  Meshes above 24,576 vertices get the
-        whole-mesh form (box 8 by default; the grid PCG, pcg_mode 3 or 7), smaller ones the
+        whole-mesh form (the grid PCG, pcg_mode 3 or 7; 'auto': the finest box from 6 spacings up
+        whose coarse space fits 3,072 unknowns, box 7 on the 32 x 32 x 128 beam), smaller ones the
         per-instance form (box 4; the thread-block-cluster PCG, pcg_mode 2 or 3)
     coarse_form : 'auto' (by size, as above), 'grid' or 'cluster'
     mass, f_ext : per-vertex lumped masses (n) and external forces (3n) instead of the ones
@@ -130,7 +131,7 @@ class BESolver:
                 raise ValueError("coarse_form must be 'auto', 'grid' or 'cluster'")
             self.coarse_form = form
             if form == "grid":
-                _, self.coarse_box = m.set_coarse(pin == 0, box=8 if coarse == "auto" else int(coarse))
+                _, self.coarse_box = m.set_coarse(pin == 0, box=None if coarse == "auto" else int(coarse))
             else:
                 _, boxes = m.set_coarse_inst(pin == 0, box=4 if coarse == "auto" else int(coarse))
                 self.coarse_box = int(boxes[0])
