@@ -894,3 +894,35 @@ def test_backward_euler_fast_path_matches_oracle_with_info(api, max_iter, tol):
             assert np.abs(info["g"][k] - rinfo["g"][k]).max() <= 1e-9 * g0, k
             assert np.abs(info["dx"][k] - rinfo["dx"][k]).max() <= 1e-8 * dx0, k
         x_prev, x_curr = x_curr, got
+
+
+def test_bdf2_fast_path_matches_oracle_with_info(api):
+    """The drop-in bdf2 on the device fast path against the oracle's bdf2 (simkit's
+    integrators/bdf2.py:31-101 with newton.py's spsolve) on the same closures' math: positions,
+    Newton iteration count and step lengths; return_info gives simkit's keys."""
+    import scipy.sparse as sps
+    from oracle import fem, snh as osnh, solvers as osol
+    from simkit_gb300.beams import make_beam
+    spec = make_beam(6, 3, 3, ym=2e5, pr=0.45)
+    X, T = spec.X, spec.T
+    m = fem.lumped_mass(X, T, 1000.0)
+    M = sps.diags(np.repeat(m, 3)).tocsc()
+    f = (m[:, None] * np.array([0.0, -9.8, 0.0])[None, :]).reshape(-1, 1)
+    pot = api.ElasticPotential(X, T, spec.mu, spec.lam, f_ext=f)
+    J, vol = fem.deformation_jacobian(X, T), fem.tet_volumes(X, T)
+    Eo = lambda x: osnh.energy_x(x, J, spec.mu, spec.lam, vol) - float((f.T @ x).item())
+    Go = lambda x: osnh.gradient_x(x, J, spec.mu, spec.lam, vol) - f
+    Ho = lambda x: osnh.hessian_x(x, J, spec.mu, spec.lam, vol)
+    rng = np.random.default_rng(8)
+    x0 = X.reshape(-1, 1).copy()
+    xs = [x0 + 1e-3 * k * rng.standard_normal(x0.shape) for k in range(4)]   # x_prev3 .. x_curr
+    h = 1.0 / 60.0
+    for _ in range(2):
+        got, info = api.bdf2(xs[3], xs[2], xs[1], xs[0], pot.energy, pot.gradient, pot.hessian, M, h,
+                             tolerance=1e-9, max_iter=20, return_info=True)
+        ref, rinfo = osol.bdf2(xs[3], xs[2], xs[1], xs[0], Eo, Go, Ho, M, h, tolerance=1e-9, max_iter=20,
+                               return_info=True)
+        assert _rel(got - xs[3], ref - xs[3]) < 1e-9
+        assert info["iters"] == rinfo["iters"] and info["alphas"] == rinfo["alphas"] and info["status"] == 0
+        assert set(rinfo) <= set(info)
+        xs = xs[1:] + [got]
