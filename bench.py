@@ -683,6 +683,8 @@ def main():
                     help="measured CPU reference steps in the GPU arm's cpu_baseline")
     ap.add_argument("--small", action="store_true", help="use the 8x8x32 beam (quick check)")
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner cache")
+    ap.add_argument("--pcg-variant", type=int, default=None,
+                    help="single mesh: this PCG kernel variant instead of the autotuner's choice")
     ap.add_argument("--workload", default="single", choices=["single", "batched", "serving"])
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of traffic")
@@ -722,7 +724,11 @@ def main():
             raise SystemExit(f"warm-up step did not converge: {info}")
     # pick the PCG kernel variant on this system (untimed; cached per device and size)
     from simkit_gb300.autotune import tune_pcg_variant
-    variant, variant_us = tune_pcg_variant(solver, use_cache=not args.retune)
+    if args.pcg_variant is None:
+        variant, variant_us = tune_pcg_variant(solver, use_cache=not args.retune)
+    else:
+        variant, variant_us = args.pcg_variant, {}
+        solver.params.pcg_variant = variant
 
     barrier = ranks.barrier
     stream = torch.cuda.current_stream()

@@ -323,7 +323,9 @@ typedef struct skg_be_params {
                                flight: 8x1, 16x1, 8x2, 16x2, 4x2, 4x4, 2x4, 8x4, 2x2); for the
                                one-cluster PCG (mode 2) the cluster size: 0 by system size,
                                1-4 = 16, 8, 4, 2 CTAs; for the two-level grid PCG (mode 7) also
-                               9-17 = the shapes of 0-8 with 768-thread blocks; chosen by the
+                               9-17 = the shapes of 0-8 with 768-thread blocks, and 18-20 = two
+                               grid barriers per iteration instead of three (coarse residual by
+                               recurrence), 768-thread blocks, shapes 4x2, 8x2, 2x2; chosen by the
                                autotuner */
   int32_t batch_min_cluster; /* batched PCG: smallest thread-block cluster an instance gets (1, 2,
                                4, 8 or 16; 0 = 4); each instance gets the smallest power of two

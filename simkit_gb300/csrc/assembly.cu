@@ -738,6 +738,8 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
     w.cM = c.take<float>(np * np);
     w.crowp = c.take<float>(2 * 32 * np);
     w.crc = c.take<unsigned long long>(np);
+    w.crq = c.take<unsigned long long>(2 * np);
+    w.crcg = c.take<double>(2 * np);
     w.ce = c.take<float>(8 * (int64_t)m->coarse->n_agg);
     w.cok = c.take<int>(4);
     w.cbar = c.take<unsigned>(4);

@@ -183,6 +183,8 @@ struct Workspace {
   float* cM;                 // np x np coarse operator / its inverse
   float* crowp;              // 2 x 32 x np row panels
   unsigned long long* crc;   // np fixed-point coarse residual
+  unsigned long long* crq;   // 2 np fixed-point P^T q (two-barrier PCG), by iteration parity
+  double* crcg;              // 2 np coarse residual kept between iterations (two-barrier PCG)
   float* ce;                 // 8 per aggregate: coarse correction
   int* cok;                  // coarse inverse valid
   unsigned* cbar;            // grid barrier of the inversion

@@ -370,17 +370,12 @@ template <typename R> struct ZCoarse {
   }
 };
 
-// e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows
-// dealt to the blocks in turn so that every block gets nc / gridDim of them), pc += (P^T r) . e over those rows.  rcf: shared
-// staging of P^T r (np floats).
+// e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows dealt to the blocks
+// in turn so that every block gets nc / gridDim of them), pc += (P^T r) . e over those rows, from
+// P^T r staged in shared memory (rcf: np floats)
 template <typename R>
-__device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, float inv_scale, Dacc<R>& pc) {
+__device__ __forceinline__ void coarse_rows_product(const CoarseDev& c, const float* rcf, Dacc<R>& pc) {
   const int wpb = blockDim.x >> 5;
-  if ((int)blockIdx.x >= c.nc) return;   // block-uniform
-#pragma unroll 4
-  for (int i = threadIdx.x; i < c.np; i += blockDim.x)
-    rcf[i] = i < c.nc ? __ll2float_rn((long long)__ldcg(c.rc + i)) * inv_scale : 0.f;
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const float4* r4 = reinterpret_cast<const float4*>(rcf);
   for (int row = blockIdx.x + (threadIdx.x >> 5) * gridDim.x; row < c.nc; row += gridDim.x * wpb) {
@@ -402,6 +397,50 @@ __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, f
   }
 }
 
+// The coarse product from the fixed-point restriction c.rc (scaled back by inv_scale).  keep: the
+// two-barrier form also stores P^T r in double there, entry i by block i mod gridDim.
+template <typename R>
+__device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, float inv_scale, Dacc<R>& pc,
+                                               double* keep = nullptr) {
+  if ((int)blockIdx.x >= c.nc) return;   // block-uniform
+#pragma unroll 4
+  for (int i = threadIdx.x; i < c.np; i += blockDim.x) {
+    const long long q = i < c.nc ? (long long)__ldcg(c.rc + i) : 0ll;
+    rcf[i] = i < c.nc ? __ll2float_rn(q) * inv_scale : 0.f;
+    if (keep && i < c.nc && i % (int)gridDim.x == (int)blockIdx.x) keep[i] = (double)q * (double)inv_scale;
+  }
+  __syncthreads();
+  coarse_rows_product<R>(c, rcf, pc);
+}
+
+// Two-barrier form: P^T r_{k+1} = P^T r_k - alpha_k P^T q_k, with P^T r_k carried in double (cur)
+// and P^T q_k in fixed point (rq, scale 1 / a_inv_sq times alpha_k).  Every block forms all entries
+// with the same operations (so all hold the same bits) into rcf, and block i mod gridDim stores entry
+// i for the next iteration (next); then the coarse product.
+template <typename R>
+__device__ __forceinline__ void coarse_product_recur(const CoarseDev& c, float* rcf, const double* cur,
+                                                     const unsigned long long* rq, double a_inv_sq, double* next,
+                                                     Dacc<R>& pc) {
+  if ((int)blockIdx.x >= c.nc) return;   // block-uniform
+#pragma unroll 4
+  for (int i = threadIdx.x; i < c.np; i += blockDim.x) {
+    double x = 0.0;
+    if (i < c.nc) {
+      x = __ldcg(cur + i) - a_inv_sq * (double)(long long)__ldcg(rq + i);
+      if (i % (int)gridDim.x == (int)blockIdx.x) next[i] = x;
+    }
+    rcf[i] = (float)x;
+  }
+  __syncthreads();
+  coarse_rows_product<R>(c, rcf, pc);
+}
+
+// iterations of the two-barrier form that restrict r itself (the recurrence restarts from the exact
+// restriction; the first iteration has no alpha_{k-1} for the scale of P^T q)
+constexpr int kRecurExact = 8;
+// block rows whose q the two-barrier form stages in shared memory (larger ranges: three barriers)
+constexpr int kStageRows = 2048;
+
 // Two-level PCG, grid-persistent.  Solve after k_pcg_init (x = 0, r, z = D^-1 r,
 // r.z in scal).  Per iteration three grid barriers:
 //   A  q = A p with p = (D^-1 r + P e) + beta p_prev formed in the gathers;
@@ -410,19 +449,27 @@ __device__ __forceinline__ void coarse_product(const CoarseDev& c, float* rcf, f
 //   C  e = A_c^-1 P^T r; (P^T r).e                             -> barrier 3
 // with r.M^-1 r = r.D^-1 r + (P^T r).e.  When the coarse inverse is not valid
 // (c.ok == 0) phases C and the restriction are skipped: the one-level method.
-// partials: >= 4 gridDim accumulators of scratch.  Each block owns an equal
+// TB (two barriers): phase A also restricts q (staged in shared memory; P^T q in fixed point, scaled
+// by the previous iteration's alpha), and phase B forms P^T r_{k+1} = P^T r_k - alpha P^T q and runs the coarse
+// product beside the update, so barrier 3 goes.  Every kRecurExact-th iteration (and one whose
+// scaled P^T q leaves the exact range, counted in the p.q reduction) takes the three-barrier path
+// with the restriction of r itself, which restarts the recurrence.
+// partials: >= 6 gridDim accumulators of scratch.  Each block owns an equal
 // contiguous range of block rows (the SpMV lane groups and the per-row update
 // both work inside it), so the phases end at about the same time in every block.
 // NT threads per block: 256 (three blocks per SM) or 768 (one per SM: a third of the
 // barrier arrivals and block partials, the same threads in flight)
-template <typename R, int G, int U, int NT = kBlock>
+template <typename R, int G, int U, int NT = kBlock, bool TB = false>
 __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> A, PcgVecs<R> v, CoarseDev c,
                                                                       double* partials, unsigned* bar, double* scal) {
-  __shared__ Dacc<R> wsum[2][NT / 32];
+  constexpr int NA = TB ? 2 : 1;   // phase A totals: p.q (and the out-of-range count)
+  constexpr int NB = TB ? 3 : 2;   // phase B totals: r.z, r.r (and (P^T r).e)
+  __shared__ Dacc<R> wsum[3][NT / 32];
   __shared__ __align__(16) float rcf[kCoarseMax];
+  __shared__ float qs[TB ? 3 * kStageRows : 1];   // q of the block's rows (two-barrier form)
   Dacc<R>* PA = reinterpret_cast<Dacc<R>*>(partials);     // p.q per block
-  Dacc<R>* PB = PA + gridDim.x;                            // r.z, r.r per block
-  Dacc<R>* PC = PB + 2 * gridDim.x;                        // (P^T r).e per block
+  Dacc<R>* PB = PA + NA * gridDim.x;                       // r.z, r.r per block
+  Dacc<R>* PC = PB + NB * gridDim.x;                       // (P^T r).e per block
   unsigned* count = bar;
   volatile unsigned* gen = bar + 1;
   volatile double* err = scal + S_BAR_ERR;
@@ -454,6 +501,7 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
   double rr_final = scal[S_RR];
   double rr_prev = scal[S_RR];
   R beta = R(0);
+  R a_prev = R(0);
   int cur = 0;  // p_k in v.p (cur 0) or v.s (cur 1), p_{k-1} in the other
   const ZCoarse<R> zf{v.z, c, con};
   if (!done && con) {
@@ -487,11 +535,24 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
     const bool first = it == 0;
     R* pk = cur ? v.s : v.p;
     const R* pprev = cur ? v.p : v.s;
+    // two-barrier iterations restrict q here, at a power-of-two scale from |r_k| and alpha_{k-1}
+    // (alpha_k P^T q_k is about the change of P^T r), 2^8 below the scale of r's restriction: room for
+    // alpha_{k-1} |q| up to ~2^16 |r| per row, at a resolution of ~1e-8 |r|
+    const bool rec = TB && con && !first && (it % kRecurExact) != 0 && chunk <= kStageRows;
+    unsigned long long* rqk = TB && con ? c.rq + (int64_t)(it & 1) * c.np : nullptr;
+    float sq = 0.f;
+    if (rec) {
+      int ea = 0;
+      frexpf(float(a_prev), &ea);
+      sq = ldexpf(coarse_scale(rr_prev), -ea - 8);
+    }
     // the coarse residual was last read in phase C and is next written in phase B
     if (con)
       for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.np; i += stride) c.rc[i] = 0ull;
-    Dacc<R> pq[1];
-    dacc_zero(pq[0]);
+    Dacc<R> pq[NA];
+#pragma unroll
+    for (int k = 0; k < NA; ++k) dacc_zero(pq[k]);
+    bool out_of_range = rec && !(sq > 0.f && sq < INFINITY);
     for (int64_t base = row0; base < rend; base += U * groups) {
       int64_t rows[U];
       bool val[U];
@@ -510,22 +571,58 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
           st3(pk, rows[u], p);
           st3(v.q, rows[u], ys[u]);
           dacc_dot3(pq[0], p, ys[u]);
+          if (TB && rec) {
+            float* qq = qs + 3 * (rows[u] - rbeg);
+            qq[0] = float(ys[u].x);
+            qq[1] = float(ys[u].y);
+            qq[2] = float(ys[u].z);
+          }
         }
     }
-    block_total<R, 1, NT>(pq, wsum);
-    if (threadIdx.x == 0) st_dacc(PA + blockIdx.x, pq[0]);
-    Dacc<R> t1[1];
-    if (!grid_barrier_total<R, 1, NT>(count, gen, err, PA, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    if constexpr (TB) {
+      if (rec) {   // block-uniform: P^T q over the block's rows, 32 consecutive rows per warp pass
+        __syncthreads();
+#pragma unroll 2
+        for (int64_t base = wbase0; base < rend; base += NT) {
+          const int64_t i = base + (threadIdx.x & 31);
+          const bool ok = i < rend;
+          const float* qq = qs + 3 * (ok ? i - rbeg : 0);
+          out_of_range |= coarse_restrict_groups<1>(c, rqk, ok, i, ok ? qq[0] : 0.f, ok ? qq[1] : 0.f,
+                                                    ok ? qq[2] : 0.f, sq);
+        }
+      }
+    }
+    if constexpr (TB) {
+      if (out_of_range) pq[NA - 1] = dacc_add(pq[NA - 1], Dacc<R>{R(1)});
+    }
+    block_total<R, NA, NT>(pq, wsum);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NA; ++k) st_dacc(PA + k * gridDim.x + blockIdx.x, pq[k]);
+    Dacc<R> t1[NA];
+    if (!grid_barrier_total<R, NA, NT>(count, gen, err, PA, t1, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     const R pqr = dacc_r(t1[0]);
     if (!(pqr > R(0)) || !isfinite(pqr)) {
       status = isfinite(pqr) ? 0 : SKG_ERR_NONFINITE;
       break;
     }
     const R a = dacc_r(rz) / pqr;
+    bool use_rec = false;
+    if constexpr (TB) use_rec = rec && dacc_value(t1[NA - 1]) == 0.0;
     const float sc = coarse_scale(rr_prev);
-    Dacc<R> acc[2];
-    dacc_zero(acc[0]);
-    dacc_zero(acc[1]);
+    Dacc<R> acc[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) dacc_zero(acc[k]);
+    if constexpr (TB) {
+      if (con) {
+        // the P^T q buffer of the next iteration was last read in the previous iteration's phase B
+        unsigned long long* rqn = c.rq + (int64_t)((it + 1) & 1) * c.np;
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < c.np; i += stride) rqn[i] = 0ull;
+      }
+      if (use_rec)
+        coarse_product_recur<R>(c, rcf, c.rcg + (int64_t)(it & 1) * c.np, rqk, double(a) / double(sq),
+                                c.rcg + (int64_t)((it + 1) & 1) * c.np, acc[2]);
+    }
     for (int64_t base = wbase0; base < rend; base += NT) {
       const int64_t i = base + (threadIdx.x & 31);
       const bool ok = i < rend;
@@ -543,27 +640,30 @@ __global__ void __launch_bounds__(NT, NT == kBlock ? 3 : 1) k_pcg_grid2c(Bsr<R> 
         dacc_dot3(acc[0], r, z);
         dacc_dot3(acc[1], r, r);
       }
-      if (con) coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
+      if (con && !use_rec) coarse_restrict(c, ok, i, float(r.x), float(r.y), float(r.z), sc);
     }
-    block_total<R, 2, NT>(acc, wsum);
-    if (threadIdx.x == 0) {
-      st_dacc(PB + blockIdx.x, acc[0]);
-      st_dacc(PB + gridDim.x + blockIdx.x, acc[1]);
-    }
-    Dacc<R> t2[2];
-    if (!grid_barrier_total<R, 2, NT>(count, gen, err, PB, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
+    block_total<R, NB, NT>(acc, wsum);
+    if (threadIdx.x == 0)
+#pragma unroll
+      for (int k = 0; k < NB; ++k) st_dacc(PB + k * gridDim.x + blockIdx.x, acc[k]);
+    Dacc<R> t2[NB];
+    if (!grid_barrier_total<R, NB, NT>(count, gen, err, PB, t2, wsum)) { status = SKG_ERR_TIMEOUT; break; }
     ++it;
+    a_prev = a;
     rr_acc = t2[1];
     rr_prev = dacc_value(t2[1]);
     const R rrr = dacc_r(t2[1]);
     const Dacc<R> rz_old = rz;
     rz = t2[0];
+    if constexpr (TB) {
+      if (use_rec) rz = dacc_add(rz, t2[2]);
+    }
     if (!isfinite(rrr)) { status = SKG_ERR_NONFINITE; break; }
     if (rrr <= tol2r || it >= max_iter) break;
-    if (con) {
+    if (con && !use_rec) {
       Dacc<R> pc[1];
       dacc_zero(pc[0]);
-      coarse_product<R>(c, rcf, 1.f / sc, pc[0]);
+      coarse_product<R>(c, rcf, 1.f / sc, pc[0], TB ? c.rcg + (int64_t)(it & 1) * c.np : nullptr);
       block_total<R, 1, NT>(pc, wsum);
       if (threadIdx.x == 0) st_dacc(PC + blockIdx.x, pc[0]);
       Dacc<R> t3[1];

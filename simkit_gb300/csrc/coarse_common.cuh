@@ -24,6 +24,8 @@ struct CoarseDev {
   float* M;                    // np x np: A_c, inverted in place
   float* rowp;                 // 2 x kGjB x np row panels
   unsigned long long* rc;      // np: coarse residual in fixed point
+  unsigned long long* rq;      // 2 np: P^T q in fixed point by iteration parity (two-barrier whole-mesh PCG)
+  double* rcg;                 // 2 np: the coarse residual carried between iterations (two-barrier PCG)
   float* e;                    // 8 n_agg: (t, w) per aggregate, padded to 8
   int* ok;                     // 1 when M holds a valid inverse (per instance in the per-instance form)
   unsigned* bar;               // 2: grid barrier of the inversion
@@ -125,6 +127,56 @@ __device__ __forceinline__ void coarse_restrict(const CoarseDev& c, bool valid, 
   if (head && key >= 0)
 #pragma unroll
     for (int k = 0; k < 6; ++k) atomicAdd(c.rc + 6 * key + k, (unsigned long long)q[k]);
+}
+
+// dst += P^T y over the rows of the calling warp's lane groups (G lanes per block row, every lane
+// of a group holding its row's y, as the SpMV leaves it): the first lane of each group contributes
+// its row, runs of rows of one aggregate are summed by a segmented shuffle reduction over those
+// lanes, then one 64-bit atomic per run and component.  The scaled values must stay within 2^52
+// so that the sums of up to 2^10 rows of an aggregate cannot overflow; a value outside that range
+// (or not finite) is left out and the return value is true, and the caller then does not use dst.
+template <int G>
+__device__ __forceinline__ bool coarse_restrict_groups(const CoarseDev& c, unsigned long long* dst, bool valid,
+                                                      int64_t row, float yx, float yy, float yz, float scale) {
+  const int lane = threadIdx.x & 31;
+  const bool leader = (lane & (G - 1)) == 0;
+  int key = -1;
+  bool bad = false;
+  long long q[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) q[k] = 0;
+  if (valid) {
+    const float4 m = __ldg(c.mode + row);
+    key = mode_agg(m);
+    if (leader) {
+      const unsigned f = mode_mask(m);
+      const float x = (f & 1u) ? yx : 0.f, y = (f & 2u) ? yy : 0.f, z = (f & 4u) ? yz : 0.f;
+      const float v6[6] = {x, y, z, m.y * z - m.z * y, m.z * x - m.x * z, m.x * y - m.y * x};
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float t = v6[k] * scale;   // power-of-two scale: exact
+        if (fabsf(t) <= 0x1p52f) q[k] = __float2ll_rn(t);
+        else bad = true;
+      }
+    }
+  }
+  const int prev = __shfl_up_sync(0xffffffffu, key, G);
+  const bool head = leader && (lane == 0 || prev != key);
+  const unsigned heads = __ballot_sync(0xffffffffu, head);
+  const int seg = __popc(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1) {
+    const int so = __shfl_down_sync(0xffffffffu, seg, o);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const long long t = __shfl_down_sync(0xffffffffu, q[k], o);
+      if (lane + o < 32 && so == seg) q[k] += t;
+    }
+  }
+  if (head && key >= 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) atomicAdd(dst + 6 * key + k, (unsigned long long)q[k]);
+  return bad;
 }
 
 }  // namespace skg

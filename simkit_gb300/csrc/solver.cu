@@ -786,6 +786,8 @@ static CoarseDev make_coarse_dev(const skg_tet_mesh* m, const Workspace& w) {
   c.M = w.cM;
   c.rowp = w.crowp;
   c.rc = w.crc;
+  c.rq = w.crq;
+  c.rcg = w.crcg;
   c.e = w.ce;
   c.ok = w.cok;
   c.bar = w.cbar;
@@ -947,15 +949,26 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
   } else if (mode == 1 || mode == 5 || mode == 7) {
     // kernel variant: lanes per row G and rows in flight U (picked by the autotuner);
     // mode 5 is the two-barrier form (pcg_grid.cuh), mode 7 its two-level form (coarse.cuh)
-    // mode 7 variants 9..17: the shapes of 0..8 with 768-thread blocks (one per SM)
-    const bool wide = mode == 7 && variant >= 9;
-    if (wide) variant -= 9;
+    // mode 7 variants 9..17: the shapes of 0..8 with 768-thread blocks (one per SM); 18..20: the
+    // two-barrier form (coarse residual by recurrence) with 768-thread blocks, shapes (4, 2), (8, 2), (2, 2)
+    const bool two_barrier = mode == 7 && variant >= 18 && variant <= 20;
+    const bool wide = mode == 7 && (variant >= 9 || two_barrier);
 #define SKG_PCG_KERN(G_, U_)                                                                              \
   (mode == 7   ? (wide ? (const void*)k_pcg_grid2c<R, G_, U_, 768> : (const void*)k_pcg_grid2c<R, G_, U_>) \
    : mode == 5 ? (const void*)k_pcg_grid2<R, G_, U_>                                                      \
                : (const void*)k_pcg_persistent<R, G_, U_>)
     const void* kern = SKG_PCG_KERN(8, 1);
     int G = 8;
+    if (two_barrier) {
+      switch (variant) {
+        case 18: kern = (const void*)k_pcg_grid2c<R, 4, 2, 768, true>; G = 4; break;
+        case 19: kern = (const void*)k_pcg_grid2c<R, 8, 2, 768, true>; G = 8; break;
+        default: kern = (const void*)k_pcg_grid2c<R, 2, 2, 768, true>; G = 2; break;
+      }
+      variant = -1;
+    } else if (wide) {
+      variant -= 9;
+    }
     switch (variant) {
       case 1: kern = SKG_PCG_KERN(16, 1); G = 16; break;
       case 2: kern = SKG_PCG_KERN(8, 2); G = 8; break;

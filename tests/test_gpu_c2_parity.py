@@ -24,10 +24,13 @@ pytestmark = pytest.mark.gpu
 FIXTURE = "rollout_beam_32x32x128_first_steps.npz"
 
 
-def _bench_solver(spec, precision="mixed"):
+def _bench_solver(spec, precision="mixed", variant=None):
     from simkit_gb300.solver import BESolver
     kw = dict(pcg_rtol=-0.3) if precision == "mixed" else dict(pcg_rtol=1e-3)
-    return BESolver.from_spec(spec, precision=precision, pcg_mode=3, coarse="auto", coarse_refresh=8, **kw)
+    s = BESolver.from_spec(spec, precision=precision, pcg_mode=3, coarse="auto", coarse_refresh=8, **kw)
+    if variant is not None:
+        s.params.pcg_variant = variant
+    return s
 
 
 @pytest.fixture(scope="module")
@@ -36,12 +39,14 @@ def c2_spec():
     return beam_large_jittered(seed=0)
 
 
-def test_c2_first_steps_match_simkit(c2_spec):
+# variant 13: the three-barrier two-level kernel the autotuner picked on a GB300; 18: its two-barrier form
+@pytest.mark.parametrize("variant", [13, 18])
+def test_c2_first_steps_match_simkit(c2_spec, variant):
     d = np.load(os.path.join(GOLDEN, FIXTURE))
     spec = c2_spec
     assert tuple(int(v) for v in d["dims"]) == spec.dims
     sample = d["sample"]
-    s = _bench_solver(spec)
+    s = _bench_solver(spec, variant=variant)
     X = spec.X[sample]
     scale = np.abs(spec.X).max()
     for k, step in enumerate(d["steps"]):

@@ -1,0 +1,60 @@
+"""The two-level grid PCG with two grid barriers per iteration (pcg_variant 18-20: the coarse residual
+carried by the recurrence P^T r_{k+1} = P^T r_k - alpha_k P^T q_k, restarted from the exact restriction
+every 8th iteration) against the three-barrier form (variant 13, the same (4, 2) shape with 768-thread
+blocks) on a jittered beam with E spread over two decades: both take Newton to the same 1e-6 relative
+residual, so the steps agree to the Newton tolerance; the PCG iteration counts stay within a few
+percent; and the two-barrier form repeats bitwise."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def spec():
+    from simkit_gb300.beams import beam_large_jittered
+    return beam_large_jittered(nx=48, ny=12, nz=12, seed=3)   # 41,472 tets, 8,281 vertices
+
+
+def _solver(spec, variant, precision):
+    from simkit_gb300.solver import BESolver
+    kw = dict(pcg_rtol=-0.3) if precision == "mixed" else dict(pcg_rtol=1e-6)
+    s = BESolver.from_spec(spec, precision=precision, pcg_mode=7, coarse="auto", coarse_form="grid",
+                           coarse_refresh=4, **kw)
+    s.params.pcg_variant = variant
+    return s
+
+
+def _run(s, steps):
+    pcg = newton = 0
+    for _ in range(steps):
+        info = s.step()
+        assert info.converged, info
+        pcg += info.pcg_iters
+        newton += info.newton_iters
+    return s.displacement(), pcg, newton
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("variant", [18, 19, 20])
+def test_two_barrier_steps_match_three_barrier(spec, variant, precision):
+    u3, pcg3, n3 = _run(_solver(spec, 13, precision), 6)
+    u2, pcg2, n2 = _run(_solver(spec, variant, precision), 6)
+    err = np.abs(u2 - u3).max() / np.abs(u3).max()
+    print(f"\nvariant {variant} {precision}: displacement rel diff {err:.2e}, PCG {pcg2} vs {pcg3}, "
+          f"Newton {n2} vs {n3}")
+    # both stop at a 1e-6 relative Newton residual from different PCG iterates
+    assert err < (1e-4 if precision == "mixed" else 1e-6)
+    assert abs(pcg2 - pcg3) <= 0.1 * pcg3 + 4
+    assert abs(n2 - n3) <= 2
+
+
+def test_two_barrier_repeats_bitwise(spec):
+    a = _solver(spec, 18, "mixed")
+    b = _solver(spec, 18, "mixed")
+    for _ in range(3):
+        ia, ib = a.step(), b.step()
+        assert (ia.newton_iters, ia.pcg_iters) == (ib.newton_iters, ib.pcg_iters)
+        assert torch.equal(a.u_curr, b.u_curr)
