@@ -225,7 +225,9 @@ def assemble_hessian_blocks(mesh: TetMesh, X, precision="fp64", psd=True) -> tor
 
 
 class BlockMatrix:
-    """Assembled 3x3-block symmetric matrix resident on the GPU."""
+    """Assembled 3x3-block symmetric matrix resident on the GPU.  ``+`` a diagonal matrix (scipy or
+    dense, e.g. a lumped M / h^2) or a BlockMatrix of the same mesh, ``*`` or ``/`` a scalar stay on the
+    device; ``+`` any other matrix gives the host sum."""
 
     def __init__(self, mesh: TetMesh, val: torch.Tensor):
         self.mesh = mesh
@@ -234,6 +236,32 @@ class BlockMatrix:
 
     def to_scipy(self) -> sps.csr_matrix:
         return self.mesh.block_values_to_csr(self.val)
+
+    def __add__(self, other):
+        if isinstance(other, BlockMatrix):
+            if other.mesh is not self.mesh:
+                raise ValueError("BlockMatrix sum needs both matrices on the same mesh")
+            return BlockMatrix(self.mesh, self.val + other.val.to(self.val.dtype))
+        d = _diagonal_of(other, self.shape[0])
+        if d is None:
+            return self.to_scipy() + other
+        val = self.val.clone()
+        val[self.mesh.diag_value_index()] += torch.from_numpy(d).to(device=val.device, dtype=val.dtype)
+        return BlockMatrix(self.mesh, val)
+
+    __radd__ = __add__
+
+    def __mul__(self, s):
+        if not np.isscalar(s):
+            return NotImplemented
+        return BlockMatrix(self.mesh, self.val * float(s))
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, s):
+        if not np.isscalar(s):
+            return NotImplemented
+        return BlockMatrix(self.mesh, self.val / float(s))
 
     tocsr = to_scipy
 
@@ -787,59 +815,135 @@ def elastic_hessian(X, T, mu, lam, material: str, U: Optional[np.ndarray] = None
 # --------------------------------------------------------------------------- #
 # linear solve standing in for spsolve (simkit/solvers/newton.py:52)           #
 # --------------------------------------------------------------------------- #
-def solve_sparse(A, b, rtol: float = 1e-12, max_iter: int = 20000):
-    """x = A^{-1} b for symmetric positive definite A by FP64 block-Jacobi PCG on the GPU.
+def _diagonal_of(M, N: int):
+    """The diagonal (N,) of a diagonal matrix M (scipy sparse or dense, N x N), else None."""
+    if sps.issparse(M):
+        if M.shape != (N, N):
+            return None
+        d = np.asarray(M.diagonal(), dtype=np.float64)
+        C = sps.coo_matrix(M)
+        if np.any((C.row != C.col) & (C.data != 0)):
+            return None
+        return d
+    if isinstance(M, torch.Tensor):
+        M = M.detach().cpu().numpy()
+    A = np.asarray(M, dtype=np.float64)
+    if A.shape != (N, N):
+        return None
+    d = np.diagonal(A).copy()
+    if np.count_nonzero(A - np.diag(d)):
+        return None
+    return d
 
-    A may be a scipy sparse matrix, a dense array or a ``BlockMatrix``.
+
+class _BlockPlan:
+    """The 3x3-block CSR pattern (every diagonal block present, rows padded to a multiple of 3 with
+    the identity) of a scalar CSR pattern, and the scatter of the scalar values into the solver's
+    entry-major block values: val[dst] = data (padding diagonal entries at pad_dst get 1)."""
+
+    def __init__(self, indptr, indices, n):
+        self.indptr, self.indices, self.n = indptr.copy(), indices.copy(), n
+        N = n + (-n) % 3
+        nbr = N // 3
+        rows = np.repeat(np.arange(n, dtype=np.int64), np.diff(indptr))
+        cols = indices.astype(np.int64)
+        br, bc = rows // 3, cols // 3
+        keys = np.unique(np.concatenate([br * nbr + bc, np.arange(nbr, dtype=np.int64) * (nbr + 1)]))
+        krow = keys // nbr
+        rowptr = np.zeros(nbr + 1, np.int64)
+        rowptr[1:] = np.cumsum(np.bincount(krow, minlength=nbr))
+        K = np.diff(rowptr)
+
+        def dst_of(r, c):
+            slot = np.searchsorted(keys, (r // 3) * nbr + c // 3)
+            v = r // 3
+            return 9 * rowptr[v] + (3 * (r % 3) + c % 3) * K[v] + (slot - rowptr[v])
+
+        self.dst = dst_of(rows, cols)
+        pad = np.arange(n, N, dtype=np.int64)
+        self.pad_dst = dst_of(pad, pad)
+        self.nbr, self.N, self.nvals = nbr, N, 9 * keys.size
+        self.rowptr = rowptr.astype(np.int32)
+        self.col = (keys % nbr).astype(np.int32)
+
+    def matches(self, A) -> bool:
+        return (A.shape[0] == self.n and A.indptr.size == self.indptr.size and A.indices.size == self.indices.size
+                and np.array_equal(A.indptr, self.indptr) and np.array_equal(A.indices, self.indices))
+
+    def values(self, data) -> np.ndarray:
+        val = np.zeros(self.nvals)
+        if self.has_duplicates:   # a CSR matrix not in canonical form: repeated entries add
+            np.add.at(val, self.dst, data)
+        else:
+            val[self.dst] = data
+        val[self.pad_dst] = 1.0
+        return val
+
+    @property
+    def has_duplicates(self) -> bool:
+        """Whether a row repeats a column (or lists its columns unsorted: then summed the slow way)."""
+        if not hasattr(self, "_dup"):
+            d = np.diff(self.indices.astype(np.int64)) > 0
+            starts = self.indptr[1:-1].astype(np.int64)
+            d[starts[(starts > 0) & (starts < self.indices.size)] - 1] = True   # steps into the next row
+            self._dup = not bool(d.all())
+        return self._dup
+
+
+_PLANS: dict = {}   # block plans by scalar pattern size (a Newton loop reuses one pattern)
+
+
+def _block_plan(A) -> _BlockPlan:
+    key = (A.shape[0], A.nnz)
+    plan = _PLANS.get(key)
+    if plan is None or not plan.matches(A):
+        plan = _BlockPlan(A.indptr, A.indices, A.shape[0])
+        if len(_PLANS) >= 8:
+            _PLANS.pop(next(iter(_PLANS)))
+        _PLANS[key] = plan
+    if not hasattr(plan, "rowptr_d"):
+        plan.rowptr_d = torch.from_numpy(plan.rowptr).cuda()
+        plan.col_d = torch.from_numpy(plan.col).cuda()
+    return plan
+
+
+def _pcg64(nbr, rowptr_d, col_d, val_d, b_d, rtol, max_iter):
+    lib = _lib.load()
+    x_d = torch.empty(3 * nbr, dtype=torch.float64, device=val_d.device)
+    ws = torch.empty(int(lib.skg_pcg_workspace_size(nbr)), dtype=torch.uint8, device=val_d.device)
+    iters = ctypes.c_int32()
+    check(lib.skg_pcg_bsr64(nbr, _ptr(rowptr_d), _ptr(col_d), _ptr(val_d), _ptr(b_d), _ptr(x_d), rtol, max_iter,
+                            ctypes.byref(iters), _ptr(ws), _stream_ptr()))
+    return x_d
+
+
+def solve_sparse(A, b, rtol: float = 1e-12, max_iter: int = 20000):
+    """x = A^{-1} b for symmetric positive definite A by FP64 block-Jacobi PCG on the GPU (the
+    replacement of simkit's ``spsolve`` in solvers/newton.py:52).
+
+    A may be a scipy sparse matrix, a dense array or a ``BlockMatrix``.  A ``BlockMatrix`` is solved
+    where it lives (the mesh's block pattern and the device values).  A scipy matrix goes through a
+    block plan cached by its sparsity pattern, so the repeated solves of a Newton loop copy only the
+    values (one scatter on the host, one host-to-device copy).
     """
+    torch_b = isinstance(b, torch.Tensor)
     if isinstance(A, BlockMatrix):
-        A = A.to_scipy()
+        m = A.mesh
+        b_d = (b.detach().to(m.device, torch.float64) if torch_b
+               else torch.from_numpy(np.asarray(b, dtype=np.float64)).to(m.device)).reshape(-1).contiguous()
+        x = _pcg64(m.n, m.rowptr, m.col, A.val.double().contiguous(), b_d, rtol, max_iter).reshape(-1, 1)
+        return x if torch_b else x.cpu().numpy()
     if not sps.issparse(A):
         A = sps.csr_matrix(np.asarray(A, dtype=np.float64))
-    n = A.shape[0]
-    npad = (-n) % 3
     A = sps.csr_matrix(A, dtype=np.float64)
-    if npad:
-        A = sps.block_diag([A, sps.identity(npad)], format="csr")
-    N = A.shape[0]
-    nbr = N // 3
-    Ab = sps.bsr_matrix(A, blocksize=(3, 3))
-    Ab.sort_indices()
-    # every block row needs its diagonal block
-    rowptr = Ab.indptr.astype(np.int64)
-    cols = Ab.indices.astype(np.int64)
-    data = Ab.data
-    has_diag = np.zeros(nbr, bool)
-    rows_of = np.repeat(np.arange(nbr), np.diff(rowptr))
-    has_diag[rows_of[cols == rows_of]] = True
-    if not has_diag.all():
-        Ab = sps.bsr_matrix(Ab + sps.bsr_matrix((np.zeros((nbr, 3, 3)), np.arange(nbr), np.arange(nbr + 1)),
-                                                shape=Ab.shape), blocksize=(3, 3))
-        Ab.sort_indices()
-        rowptr = Ab.indptr.astype(np.int64)
-        cols = Ab.indices.astype(np.int64)
-        data = Ab.data
-        rows_of = np.repeat(np.arange(nbr), np.diff(rowptr))
-    K = np.diff(rowptr)
-    kloc = np.arange(cols.size) - rowptr[rows_of]
-    val = np.empty(9 * cols.size)
-    for m_ in range(9):
-        val[9 * rowptr[rows_of] + m_ * K[rows_of] + kloc] = data[:, m_ // 3, m_ % 3]
-    bb = np.zeros(N)
-    bv = b.reshape(-1) if not isinstance(b, torch.Tensor) else b.detach().cpu().numpy().reshape(-1)
-    bb[:n] = bv
-    lib = _lib.load()
-    rp_d = torch.from_numpy(rowptr.astype(np.int32)).cuda()
-    col_d = torch.from_numpy(cols.astype(np.int32)).cuda()
-    val_d = torch.from_numpy(val).cuda()
-    b_d = torch.from_numpy(bb).cuda()
-    x_d = torch.empty(N, dtype=torch.float64, device="cuda")
-    ws = torch.empty(int(lib.skg_pcg_workspace_size(nbr)), dtype=torch.uint8, device="cuda")
-    iters = ctypes.c_int32()
-    check(lib.skg_pcg_bsr64(nbr, _ptr(rp_d), _ptr(col_d), _ptr(val_d), _ptr(b_d), _ptr(x_d), rtol, max_iter,
-                            ctypes.byref(iters), _ptr(ws), _stream_ptr()))
-    x = x_d[:n].reshape(-1, 1)
-    return x if isinstance(b, torch.Tensor) else x.cpu().numpy()
+    n = A.shape[0]
+    plan = _block_plan(A)
+    bb = np.zeros(plan.N)
+    bb[:n] = b.detach().cpu().numpy().reshape(-1) if torch_b else np.asarray(b, dtype=np.float64).reshape(-1)
+    val_d = torch.from_numpy(plan.values(A.data)).cuda()
+    x = _pcg64(plan.nbr, plan.rowptr_d, plan.col_d, val_d, torch.from_numpy(bb).cuda(), rtol, max_iter)
+    x = x[:n].reshape(-1, 1)
+    return x if torch_b else x.cpu().numpy()
 
 
 # --------------------------------------------------------------------------- #
@@ -1046,10 +1150,7 @@ def backward_euler(x_curr, x_prev, energy_func, gradient_func, hessian_func, M, 
         return gradient_func(x) + (M @ (x - x_tilde)) / h ** 2
 
     def hessian(x):
-        H = hessian_func(x)
-        if isinstance(H, BlockMatrix):
-            H = H.to_scipy()
-        return H + M / h ** 2
+        return hessian_func(x) + M / h ** 2   # a device BlockMatrix stays on the device
 
     return newton_solver(x_tilde, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
                          do_line_search=do_line_search, return_info=return_info)
@@ -1080,10 +1181,7 @@ def bdf2(x_curr, x_prev, x_prev2, x_prev3, energy_func, gradient_func, hessian_f
         return gradient_func(x) + c * (M @ (x - x_tilde)) / h ** 2
 
     def hessian(x):
-        H = hessian_func(x)
-        if isinstance(H, BlockMatrix):
-            H = H.to_scipy()
-        return H + c * M / h ** 2
+        return hessian_func(x) + c * M / h ** 2   # a device BlockMatrix stays on the device
 
     return newton_solver(x_tilde, energy, gradient, hessian, tolerance=tolerance, max_iter=max_iter,
                          do_line_search=do_line_search, return_info=return_info)

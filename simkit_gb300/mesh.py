@@ -446,6 +446,16 @@ class TetMesh:
             self._scalar_perm = (indptr, indices, perm)
         return self._scalar_perm
 
+    def diag_value_index(self) -> torch.Tensor:
+        """(3n,) device positions, in the entry-major block values, of the scalar diagonal entries
+        (3v + i, 3v + i)."""
+        if getattr(self, "_diag_idx", None) is None:
+            rp = self.rowptr.long()
+            K = rp[1:] - rp[:-1]
+            base = 9 * rp[:-1] + (self.diag.long() - rp[:-1])
+            self._diag_idx = torch.stack([base + 4 * i * K for i in range(3)], dim=1).reshape(-1).contiguous()
+        return self._diag_idx
+
     def block_values_to_csr(self, val: torch.Tensor):
         """scipy CSR (3n x 3n) from device block values."""
         import scipy.sparse as sps

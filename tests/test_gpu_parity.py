@@ -162,6 +162,36 @@ def test_pcg_solves_spd_block_system(api):
     assert np.allclose(A @ x, b, atol=1e-8)
 
 
+def test_solve_sparse_block_matrix_stays_on_device(api):
+    """A device BlockMatrix plus a lumped M / h^2 stays a BlockMatrix equal to the host sum, solve_sparse
+    solves it in place and agrees with the solve of its scipy copy, and the scipy path reuses its block
+    plan for another matrix of the same pattern."""
+    import scipy.sparse as sps
+    from simkit_gb300 import api as A_
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.mesh import TetMesh
+    spec = make_beam(6, 3, 3)
+    rng = np.random.default_rng(5)
+    m = TetMesh(spec.X, spec.T, spec.mu, spec.lam)
+    x = spec.X + 1e-3 * rng.standard_normal(spec.X.shape)
+    H = A_.BlockMatrix(m, A_.assemble_hessian_blocks(m, x, precision="fp64"))
+    M = sps.diags(np.repeat(rng.uniform(0.5, 2.0, m.n), 3))
+    h = 1.0 / 60.0
+    Ad = H + M / h ** 2
+    assert isinstance(Ad, A_.BlockMatrix)
+    As = H.to_scipy() + M / h ** 2
+    assert abs(Ad.to_scipy() - As).max() <= 1e-12 * abs(As).max()
+    b = rng.standard_normal((3 * m.n, 1))
+    xd = A_.solve_sparse(Ad, b)
+    xs = A_.solve_sparse(As, b)
+    assert np.linalg.norm(As @ xd - b) <= 1e-10 * np.linalg.norm(b)
+    assert np.abs(xd - xs).max() <= 1e-9 * np.abs(xs).max()
+    plans = len(A_._PLANS)
+    x2 = A_.solve_sparse(As * 2.0, b)
+    assert len(A_._PLANS) == plans
+    assert np.abs(2.0 * x2 - xs).max() <= 1e-9 * np.abs(xs).max()
+
+
 def test_be_step_fp64_matches_reference_rollout(api):
     from simkit_gb300.beams import make_beam
     from simkit_gb300.solver import BESolver
