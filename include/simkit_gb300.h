@@ -248,6 +248,15 @@ typedef struct skg_tet_mesh {
   const int32_t* v2t;        /* (4t) */
   int32_t material;          /* skg_material: the elastic energy of every tet */
   const skg_coarse* coarse;  /* host pointer to the two-level preconditioner data, or NULL */
+  /* Optional upper-triangle lists (up_slot NULL: every slot is summed from hc_ptr / hc_src).  With
+   * them the assembly sums each block (v, w), w >= v, once and writes its transpose into the slot
+   * (w, v), so the assembled matrix is exactly symmetric and 10 instead of 16 per-tet blocks are
+   * gathered per tet. */
+  int64_t n_upper;           /* slots with column >= row */
+  const int32_t* up_slot;    /* (n_upper) those slots, ascending */
+  const int32_t* up_mirror;  /* (n_upper) slot of the transposed block (the slot itself on the diagonal) */
+  const int32_t* hcu_ptr;    /* (n_upper+1) offsets into hcu_src */
+  const int32_t* hcu_src;    /* contributions of the upper slots, encoded and ordered as hc_src */
 } skg_tet_mesh;
 
 /* Assembled block matrix (3x3 blocks).  Values of block slot s of row v live at

@@ -56,6 +56,7 @@ class TetMeshC(ctypes.Structure):
         ("mat32", c_vp), ("bsr_rowptr", c_vp), ("bsr_col", c_vp), ("bsr_diag", c_vp), ("bsr_row", c_vp),
         ("hc_ptr", c_vp), ("hc_src", c_vp), ("v2t_ptr", c_vp), ("v2t", c_vp), ("material", c_i32),
         ("coarse", ctypes.POINTER(CoarseC)),
+        ("n_upper", c_i64), ("up_slot", c_vp), ("up_mirror", c_vp), ("hcu_ptr", c_vp), ("hcu_src", c_vp),
     ]
 
 

@@ -195,6 +195,9 @@ __device__ __forceinline__ int contribution_offset(int cd) {
 // diagonal blocks; pinned rows / columns become identity / zero; diagonal slots also give the
 // 3x3 inverse for the block-Jacobi preconditioner.  Output: the solver's block records (rec)
 // and / or the entry-major block values of the assembled tier (val).
+// SYM: the work items are the upper-triangle slots (up_slot, with the lists hcu_ptr / hcu_src);
+// each lane writes its block's record and the transposed block's record in the mirror slot, so the
+// matrix is exactly symmetric and the lower triangle's contributions are not gathered again.
 //
 // A warp owns 32 consecutive slots, whose contributions are one contiguous range of hc_src.
 // The range goes through shared memory kAsmChunk contributions at a time: the warp loads each
@@ -220,7 +223,17 @@ __device__ __forceinline__ int contribution_entry(int cd, int m) {
   return cd < 10 ? m : 3 * k + i;
 }
 
+// a lane's record (staged in shared memory at r) to slot s, in 16-byte pieces
 template <typename R>
+__device__ __forceinline__ void store_record(const AsmArgs<R>& a, const R* r, int64_t s) {
+  constexpr int kPer = kRec * (int)sizeof(R) / 16;
+  const int4* src = reinterpret_cast<const int4*>(r);
+  int4* dst = reinterpret_cast<int4*>(a.rec + kRec * s);
+#pragma unroll
+  for (int t = 0; t < kPer; ++t) dst[t] = src[t];
+}
+
+template <typename R, bool SYM>
 __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   __shared__ __align__(16) R stage[kAsmWarps][9 * kAsmChunk];
   __shared__ __align__(16) R srec[kAsmWarps][kRec * 32];  // the slots' accumulators, then their records
@@ -230,22 +243,30 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
     sentry[i] = contribution_offset(i / 9) + contribution_entry(i / 9, i - 9 * (i / 9));
   __syncthreads();
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t items = SYM ? a.n_up : a.nb;              // slots, or upper-triangle slots
+  const int32_t* hcp = SYM ? a.hcu_ptr : a.hc_ptr;
+  const int32_t* hcs = SYM ? a.hcu_src : a.hc_src;
   const int64_t s0 = ((int64_t)blockIdx.x * kAsmWarps + wid) * 32;
-  if (s0 >= a.nb) return;  // warp-uniform
-  const int64_t s = s0 + lane;
-  const bool has = s < a.nb;
+  if (s0 >= items) return;  // warp-uniform
+  const int64_t j = s0 + lane;
+  const bool has = j < items;
+  int64_t s = j, mir = j;
   int v = 0, w = 0, cb = 0, ce = 0;
   bool active = has;
   if (has) {
+    if constexpr (SYM) {
+      s = __ldg(a.up_slot + j);
+      mir = __ldg(a.up_mirror + j);
+    }
     v = __ldg(a.bsr_row + s);
     w = __ldg(a.bsr_col + s);
-    cb = __ldg(a.hc_ptr + s);
-    ce = __ldg(a.hc_ptr + s + 1);
+    cb = __ldg(hcp + j);
+    ce = __ldg(hcp + j + 1);
     if (a.inst_active && !a.inst_active[__ldg(a.vert_inst + v)]) active = false;
   }
   const unsigned act = __ballot_sync(0xffffffffu, active);
   if (act == 0u) return;  // every slot of the warp belongs to an instance that is not stepping
-  const int last = (int)min((int64_t)31, a.nb - 1 - s0);
+  const int last = (int)min((int64_t)31, items - 1 - s0);
   const int wb = __shfl_sync(0xffffffffu, cb, 0);
   const int we = __shfl_sync(0xffffffffu, ce, last);
   R* st = stage[wid];
@@ -255,7 +276,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   for (int m = 0; m < 9; ++m) accs[9 * lane + m] = R(0);
   for (int k0 = wb; k0 < we; k0 += kAsmChunk) {
     const int nk = min(kAsmChunk, we - k0);
-    const int code = lane < nk ? __ldg(a.hc_src + k0 + lane) : 0;
+    const int code = lane < nk ? __ldg(hcs + k0 + lane) : 0;
     // segment heads and their owner slots: a slot's contributions start at cb - k0, and the slot
     // whose range holds k0 owns position 0 (exactly one lane meets each condition per position)
     const bool starts = has && cb > k0 && cb < k0 + nk;
@@ -302,17 +323,36 @@ __global__ void __launch_bounds__(32 * kAsmWarps) k_assemble(AsmArgs<R> a) {
   R* my = srec[wid] + kRec * lane;
   if (active) {
     finish_slot(a, v, w, acc);
-    if (a.rec) fill_record(a, w, acc, my);
+    if (a.rec) {
+      fill_record(a, w, acc, my);
+      if constexpr (SYM) {   // this lane's record, then the transposed block's (own staging area only)
+        store_record(a, my, s);
+        if (mir != s) {
+          R t[9];
+#pragma unroll
+          for (int m = 0; m < 9; ++m) t[m] = acc[3 * (m % 3) + m / 3];
+          fill_record(a, v, t, my);
+          store_record(a, my, mir);
+        }
+      }
+    }
     if (a.val) {
       const int rp = __ldg(a.rowptr + v);
       const int K = __ldg(a.rowptr + v + 1) - rp;
       R* dst = a.val + 9 * (int64_t)rp + (s - rp);
 #pragma unroll
       for (int m = 0; m < 9; ++m) dst[(int64_t)m * K] = acc[m];
+      if (SYM && mir != s) {
+        const int rq = __ldg(a.rowptr + w);
+        const int Kq = __ldg(a.rowptr + w + 1) - rq;
+        R* dq = a.val + 9 * (int64_t)rq + (mir - rq);
+#pragma unroll
+        for (int m = 0; m < 9; ++m) dq[(int64_t)m * Kq] = acc[3 * (m % 3) + m / 3];
+      }
     }
     if (v == w && a.jinv) write_jinv(a, v, acc);
   }
-  if (!a.rec) return;  // warp-uniform
+  if (SYM || !a.rec) return;  // warp-uniform
   __syncwarp();
   // 32 records of kRec values: 16-byte pieces, each inside one record
   constexpr int kPer = kRec * (int)sizeof(R) / 16;  // pieces per record
@@ -628,8 +668,13 @@ int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cuda
 template <typename R>
 int launch_assemble(const AsmArgs<R>& a, cudaStream_t s) {
   if (a.nb == 0) return SKG_OK;
-  const int64_t warps = (a.nb + 31) / 32;
-  k_assemble<R><<<(int)((warps + kAsmWarps - 1) / kAsmWarps), 32 * kAsmWarps, 0, s>>>(a);
+  const bool sym = a.up_slot != nullptr;
+  const int64_t warps = ((sym ? a.n_up : a.nb) + 31) / 32;
+  const int blocks = (int)((warps + kAsmWarps - 1) / kAsmWarps);
+  if (sym)
+    k_assemble<R, true><<<blocks, 32 * kAsmWarps, 0, s>>>(a);
+  else
+    k_assemble<R, false><<<blocks, 32 * kAsmWarps, 0, s>>>(a);
   SKG_LAUNCHED();
   return SKG_OK;
 }

@@ -92,6 +92,13 @@ template <typename R> struct AsmArgs {
   const double* u;             // displacement (needed with contact)
   const float4* cmode;         // optional: two-level coarse data per vertex, packed into record slots 10-11
   const uint32_t* colpack;     // optional (cluster PCG): the column's 32-bit coarse word into record slot 11
+  // optional: the upper-triangle lists (symmetric assembly: each block summed once, its transpose
+  // written into the mirror slot)
+  int64_t n_up;
+  const int32_t* up_slot;
+  const int32_t* up_mirror;
+  const int32_t* hcu_ptr;
+  const int32_t* hcu_src;
 };
 
 // A column's two-level coarse data in the two spare record slots (64 bits):
@@ -214,6 +221,13 @@ inline AsmArgs<R> make_asm_args(const skg_tet_mesh* m, const R* hbuf, R* val, R*
   a.rowptr = m->bsr_rowptr;
   a.hc_ptr = m->hc_ptr;
   a.hc_src = m->hc_src;
+  if (m->up_slot && m->up_mirror && m->hcu_ptr && m->hcu_src) {
+    a.n_up = m->n_upper;
+    a.up_slot = m->up_slot;
+    a.up_mirror = m->up_mirror;
+    a.hcu_ptr = m->hcu_ptr;
+    a.hcu_src = m->hcu_src;
+  }
   a.hbuf = hbuf;
   a.val = val;
   a.jinv = jinv;

@@ -250,16 +250,38 @@ class TetMesh:
         self._scalar_perm = None
         return self
 
+    def _set_upper(self):
+        """Upper-triangle slot lists for the symmetric assembly (device, from the pattern): the slots
+        (v, w) with w >= v, the slot of each one's transpose, and their contribution lists."""
+        row, col = self.row.long(), self.col.long()
+        up = col >= row
+        slot = torch.nonzero(up).reshape(-1)
+        keys = row * self.n + col                      # ascending: rows in order, columns sorted
+        mirror = torch.searchsorted(keys, col[slot] * self.n + row[slot])
+        hp = self.hc_ptr.long()
+        cnt = (hp[1:] - hp[:-1])[slot]
+        ptr = torch.zeros(slot.numel() + 1, dtype=torch.int64, device=row.device)
+        ptr[1:] = torch.cumsum(cnt, 0)
+        total = int(ptr[-1])
+        idx = torch.repeat_interleave(hp[:-1][slot] - ptr[:-1], cnt, output_size=total)
+        idx += torch.arange(total, device=row.device)
+        self.up_slot, self.up_mirror = slot.int(), mirror.int()
+        self.hcu_ptr, self.hcu_src = ptr.int(), self.hc_src[idx].contiguous()
+
     def _set_c(self):
         if not hasattr(self, "material"):
             self.material = 0
+        if getattr(self, "up_slot", None) is None:
+            self._set_upper()
         self.c = TetMeshC(
             n_verts=self.n, n_tets=self.t, n_blocks=self.nb,
             tets=self.tets.data_ptr(), dinv=self.dinv.data_ptr(), dinv32=self.dinv32.data_ptr(),
             vol=self.vol.data_ptr(), mu=self.mu.data_ptr(), lam=self.lam.data_ptr(), mat32=self.mat32.data_ptr(),
             bsr_rowptr=self.rowptr.data_ptr(), bsr_col=self.col.data_ptr(), bsr_diag=self.diag.data_ptr(),
             bsr_row=self.row.data_ptr(), hc_ptr=self.hc_ptr.data_ptr(), hc_src=self.hc_src.data_ptr(),
-            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr(), material=self.material)
+            v2t_ptr=self.v2t_ptr.data_ptr(), v2t=self.v2t.data_ptr(), material=self.material,
+            n_upper=self.up_slot.numel(), up_slot=self.up_slot.data_ptr(), up_mirror=self.up_mirror.data_ptr(),
+            hcu_ptr=self.hcu_ptr.data_ptr(), hcu_src=self.hcu_src.data_ptr())
 
     def __init__(self, X, T, mu, lam, device="cuda"):
         lib = _lib.load()

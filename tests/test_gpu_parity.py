@@ -133,7 +133,8 @@ def test_assembled_tier_matches_reference(api):
 
 
 def test_mixed_precision_hessian_and_determinism(api):
-    """FP32 Hessian assembly within 3e-6 of the FP64 one; two assemblies are bitwise equal."""
+    """FP32 Hessian assembly within 3e-6 of the FP64 one; two assemblies are bitwise equal; both are
+    exactly symmetric (each block is summed once and its transpose written to the mirror slot)."""
     from simkit_gb300.mesh import TetMesh
     from simkit_gb300.beams import make_beam
     b = make_beam(6, 3, 3, ym=np.exp(np.random.default_rng(1).uniform(np.log(1e5), np.log(1e7), 6 * 54)),
@@ -148,6 +149,7 @@ def test_mixed_precision_hessian_and_determinism(api):
     K64 = m.block_values_to_csr(v64)
     K32 = m.block_values_to_csr(v32a)
     assert abs(K64 - K32).max() <= 3e-6 * abs(K64).max()
+    assert (K64 - K64.T).count_nonzero() == 0 and (K32 - K32.T).count_nonzero() == 0
 
 
 def test_pcg_solves_spd_block_system(api):
