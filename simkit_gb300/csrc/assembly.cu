@@ -52,12 +52,13 @@ __device__ __forceinline__ void load_dinv(const R* __restrict__ dinv, int64_t t,
 }
 
 // -------------------------------------------------------- tet Hessians ---
-// the 78 packed values of tet e's lifted Hessian
-template <typename R, bool LE>
-__device__ __forceinline__ void tet_hessian_values(const TetArgs<R>& a, int64_t e, int disp, int project,
-                                                   R (&out)[kTetHessVals]) {
+constexpr float kFallbackJ = 0.1f;   // det F below which the eigensystem's SVD runs in FP64
+
+// F of tet e (G) and its shape operator (D)
+template <typename R>
+__device__ __forceinline__ void tet_F(const TetArgs<R>& a, int64_t e, int disp, R (&D)[9], R (&G)[9]) {
   const int4 v = __ldg(a.tets + e);
-  R du[9], D[9], G[9], gN[12];
+  R du[9];
   if constexpr (sizeof(R) == 8) {
     tet_du(a.u, v, du);
   } else {
@@ -71,17 +72,39 @@ __device__ __forceinline__ void tet_hessian_values(const TetArgs<R>& a, int64_t 
     G[8] += R(1);
   }
   add_fbar(a, e, G);
+}
+
+// the 78 packed values of tet e's lifted Hessian from its F
+template <typename R, bool LE, bool FP64_SVD = true>
+__device__ __forceinline__ void tet_hessian_from_F(const TetArgs<R>& a, int64_t e, int project, const R (&D)[9],
+                                                   const R (&G)[9], R (&out)[kTetHessVals]) {
+  R gN[12];
   shape_grads(D, gN);
   const R vol = __ldg(a.vol + e), mu = __ldg(a.mu + e), lam = __ldg(a.lam + e);
   if constexpr (LE)
     le_tet_hessian<R>(mu, lam, vol, gN, out);
   else
-    nh_tet_hessian<R>(G, mu, lam, vol, gN, out, R(0.1), project != 0, a.material);
+    nh_tet_hessian<R, FP64_SVD>(G, mu, lam, vol, gN, out, R(kFallbackJ), project != 0, a.material);
+}
+
+template <typename R, bool LE>
+__device__ __forceinline__ void tet_hessian_values(const TetArgs<R>& a, int64_t e, int disp, int project,
+                                                   R (&out)[kTetHessVals]) {
+  R D[9], G[9];
+  tet_F(a, e, disp, D, G);
+  tet_hessian_from_F<R, LE>(a, e, project, D, G, out);
+}
+
+// float pairs of a record (78 values)
+__device__ __forceinline__ void store_hess_record(float* dst, const float (&out)[kTetHessVals]) {
+#pragma unroll
+  for (int k = 0; k < kTetHessVals / 2; ++k)
+    reinterpret_cast<float2*>(dst)[k] = make_float2(out[2 * k], out[2 * k + 1]);
 }
 
 // One thread per tet.  FP32: at most 168 registers so that 3 blocks fit an SM (measured 1.60 ->
-// 1.32 ms of Hessian evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills),
-// and the block's records leave through shared memory: every thread stores its 78 values as pairs
+// 1.32 ms of Hessian evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills; the
+// split form below, 128 registers at 4 blocks), and the block's records leave through shared memory: every thread stores its 78 values as pairs
 // at a conflict-free stride, then the block writes its tets' contiguous kHStride records with
 // consecutive lanes on consecutive words - one thread storing its own record would touch 32
 // different records with every warp store (ncu: LSU-throttle stalls).  FP64 stores directly.
@@ -90,12 +113,18 @@ constexpr int kHessThreads = 128;
 constexpr int kHessStage = kTetHessVals + 4;  // staging row stride (82 words: 41 pairs, odd, so the
                                               // 8-byte stores of a half-warp hit distinct bank pairs)
 
-template <typename R, bool LE = false>
-__global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? 3 : 1) k_tet_hessian(TetArgs<R> a, int disp,
+// SPLIT (FP32, non-linear materials): tets with det F < kFallbackJ are appended to late / late_n
+// instead (their record is written by k_tet_hessian_late, with the eigensystem's SVD in FP64); without
+// the FP64 path the kernel has no spills at 3 blocks per SM and fits 4 (measured on the 786,432-tet
+// beam: 163 us with the FP64 path at 3 blocks, 155 us split at 3, ~144 us split at 4).
+template <typename R, bool LE = false, bool SPLIT = false>
+__global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? (SPLIT ? 4 : 3) : 1) k_tet_hessian(TetArgs<R> a, int disp,
                                                                                      int project,
-                                                                                     R* __restrict__ hbuf) {
+                                                                                     R* __restrict__ hbuf,
+                                                                                     int32_t* late,
+                                                                                     unsigned* late_n) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool valid = e < a.t && !(a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]);
+  bool valid = e < a.t && !(a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]);
   if constexpr (sizeof(R) == 8) {
     if (!valid) return;
     R out[kTetHessVals];
@@ -108,11 +137,16 @@ __global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? 3 : 1) k_tet_he
     __shared__ unsigned char keep[kHessThreads];
     keep[threadIdx.x] = valid ? 1 : 0;
     if (valid) {
-      float out[kTetHessVals];
-      tet_hessian_values<float, LE>(a, e, disp, project, out);
-      float2* row = reinterpret_cast<float2*>(stage + threadIdx.x * kHessStage);
-#pragma unroll
-      for (int k = 0; k < kTetHessVals / 2; ++k) row[k] = make_float2(out[2 * k], out[2 * k + 1]);
+      float D[9], G[9];
+      tet_F(a, e, disp, D, G);
+      if (SPLIT && det3(G) < kFallbackJ) {   // nearly inverted: the FP64-SVD kernel takes it
+        late[atomicAdd(late_n, 1u)] = (int32_t)e;
+        keep[threadIdx.x] = 0;
+      } else {
+        float out[kTetHessVals];
+        tet_hessian_from_F<float, LE, !SPLIT>(a, e, project, D, G, out);
+        store_hess_record(stage + threadIdx.x * kHessStage, out);
+      }
     }
     __syncthreads();
     // each warp writes whole records: 39 pairs per tet (the 78 values), lanes on consecutive pairs
@@ -126,6 +160,22 @@ __global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? 3 : 1) k_tet_he
       dst[lane] = src[lane];
       if (lane < kTetHessVals / 2 - 32) dst[32 + lane] = src[32 + lane];
     }
+  }
+}
+
+// The tets k_tet_hessian set aside (det F < kFallbackJ), with the FP64 SVD; grid-stride over the list
+// (usually empty or a few tets: a small fixed grid).
+constexpr int kLateBlocks = 256;
+template <typename R, bool LE = false>
+__global__ void __launch_bounds__(kHessThreads) k_tet_hessian_late(TetArgs<R> a, int disp, int project,
+                                                                   R* __restrict__ hbuf, const int32_t* late,
+                                                                   const unsigned* late_n) {
+  const unsigned n = *late_n;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int64_t e = late[i];
+    float out[kTetHessVals];
+    tet_hessian_values<float, LE>(a, e, disp, project, out);
+    store_hess_record(hbuf + (int64_t)kHStride * e, out);
   }
 }
 
@@ -655,12 +705,26 @@ __global__ void k_split(const double* __restrict__ u, int64_t n, float* __restri
 
 // ------------------------------------------------------------ launchers --
 template <typename R>
-int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s) {
+int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s, HessLate late) {
+  if (late.launches) *late.launches = 1;
   if (a.t == 0) return SKG_OK;
-  if (a.material == kMatLE)
-    k_tet_hessian<R, true><<<blocks_for(a.t, kHessThreads), kHessThreads, 0, s>>>(a, disp, project, hbuf);
-  else
-    k_tet_hessian<R, false><<<blocks_for(a.t, kHessThreads), kHessThreads, 0, s>>>(a, disp, project, hbuf);
+  const int blocks = blocks_for(a.t, kHessThreads);
+  bool launched = false;
+  if (a.material == kMatLE) {
+    k_tet_hessian<R, true><<<blocks, kHessThreads, 0, s>>>(a, disp, project, hbuf, nullptr, nullptr);
+    launched = true;
+  }
+  if constexpr (sizeof(R) == 4) {
+    if (!launched && late.list && late.n) {
+      SKG_CUDA(cudaMemsetAsync(late.n, 0, sizeof(unsigned), s));
+      k_tet_hessian<R, false, true><<<blocks, kHessThreads, 0, s>>>(a, disp, project, hbuf, late.list, late.n);
+      SKG_LAUNCHED();
+      k_tet_hessian_late<R, false><<<kLateBlocks, kHessThreads, 0, s>>>(a, disp, project, hbuf, late.list, late.n);
+      if (late.launches) *late.launches = 2;
+      launched = true;
+    }
+  }
+  if (!launched) k_tet_hessian<R, false><<<blocks, kHessThreads, 0, s>>>(a, disp, project, hbuf, nullptr, nullptr);
   SKG_LAUNCHED();
   return SKG_OK;
 }
@@ -744,8 +808,8 @@ int launch_split(const double* u, int64_t n, float* uh, float* ul, cudaStream_t 
   return SKG_OK;
 }
 
-template int launch_tet_hessian<float>(const TetArgs<float>&, int, int, float*, cudaStream_t);
-template int launch_tet_hessian<double>(const TetArgs<double>&, int, int, double*, cudaStream_t);
+template int launch_tet_hessian<float>(const TetArgs<float>&, int, int, float*, cudaStream_t, HessLate);
+template int launch_tet_hessian<double>(const TetArgs<double>&, int, int, double*, cudaStream_t, HessLate);
 template int launch_assemble<float>(const AsmArgs<float>&, cudaStream_t);
 template int launch_assemble<double>(const AsmArgs<double>&, cudaStream_t);
 template int launch_energy<float>(const EnergyArgs<float>&, bool, cudaStream_t);
@@ -758,6 +822,8 @@ Workspace carve_workspace(const skg_tet_mesh* m, int precision, void* base) {
   const int64_t t = m->n_tets, n = m->n_verts, nb = m->n_blocks;
   const bool mixed = precision == SKG_MIXED;
   w.hbuf32 = mixed ? c.take<float>(kHStride * t) : nullptr;
+  w.hlate = mixed ? c.take<int32_t>(t) : nullptr;
+  w.hlate_n = mixed ? c.take<unsigned>(4) : nullptr;
   w.hbuf64 = mixed ? nullptr : c.take<double>(kHStride * t);
   w.fbuf = c.take<double>(12 * t);
   w.val32 = mixed ? c.take<float>(9 * nb) : nullptr;
@@ -952,7 +1018,7 @@ static int hessian_xu(const skg_tet_mesh* mesh, const double* x, const double* f
   SKG_TRY(launch_split(x, mesh->n_verts, w.uh, w.ul, s));
   TetArgs<float> ta = make_tet_args32(mesh, x, w.uh, w.ul);
   ta.fbar = fbar;
-  SKG_TRY(launch_tet_hessian<float>(ta, 0, psd, w.hbuf32, s));
+  SKG_TRY(launch_tet_hessian<float>(ta, 0, psd, w.hbuf32, s, HessLate{w.hlate, w.hlate_n, nullptr}));
   AsmArgs<float> aa = make_asm_args<float>(mesh, w.hbuf32, val32, nullptr);
   return launch_assemble<float>(aa, s);
 }

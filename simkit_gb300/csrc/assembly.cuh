@@ -181,6 +181,8 @@ struct Workspace {
   float* uh;
   float* ul;
   float* dinv_lo;    // mixed: low parts of Dinv for the double-float forces (9 t)
+  int32_t* hlate;    // mixed: tets whose Hessian takes the FP64-SVD kernel (t)
+  unsigned* hlate_n; // their count
   float* vec32[6];   // PCG x, r, z, p, q, s (padded)
   double* vec64[6];
   double* partials;
@@ -234,7 +236,15 @@ inline AsmArgs<R> make_asm_args(const skg_tet_mesh* m, const R* hbuf, R* val, R*
   return a;
 }
 
-template <typename R> int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s);
+// optional FP32 split of the Hessian kernel: the list (t entries) and counter for the nearly inverted
+// tets, and where to return the number of kernels launched (1 or 2)
+struct HessLate {
+  int32_t* list = nullptr;
+  unsigned* n = nullptr;
+  int* launches = nullptr;
+};
+template <typename R>
+int launch_tet_hessian(const TetArgs<R>& a, int disp, int project, R* hbuf, cudaStream_t s, HessLate late = {});
 template <typename R> int launch_assemble(const AsmArgs<R>& a, cudaStream_t s);
 int launch_forces(const TetArgs<double>& a, int disp, double* fbuf, cudaStream_t s);
 // double-float forces (mixed precision, neo-Hookean materials, displacement form); fbuf holds

@@ -843,7 +843,10 @@ template <typename R> SK_HD void le_tet_hessian(R mu, R lam, R vol, const R* gN,
     }
 }
 
-template <typename R>
+// FP64_SVD: nearly inverted elements (J < fallback_J) take the SVD in FP64; without it the caller has
+// set those elements aside (the FP32 Hessian kernel hands them to a second kernel, so that the FP64
+// path's registers do not limit the occupancy of the common one)
+template <typename R, bool FP64_SVD = true>
 SK_HD void nh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J, bool project,
                           int material);
 
@@ -858,7 +861,7 @@ SK_HD void snh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, 
 }
 
 // the neo-Hookean and corotational materials
-template <typename R>
+template <typename R, bool FP64_SVD>
 SK_HD void nh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R fallback_J, bool project,
                           int material) {
   R IC = 0;
@@ -933,10 +936,14 @@ SK_HD void nh_tet_hessian(const R* F, R mu, R lam, R vol, const R* gN, R* out, R
   if (!project && Tw == R(0)) return;
   // eigenvalue floor
   R U[9], s[3], V[9], W[9], lam9[9];
-  if (J < fallback_J)
-    snh_eigensystem<R, double>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
-  else
+  if constexpr (FP64_SVD) {
+    if (J < fallback_J)
+      snh_eigensystem<R, double>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
+    else
+      snh_eigensystem<R, R>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
+  } else {
     snh_eigensystem<R, R>(F, mu, Lc, vol, A, D, B, U, s, V, W, lam9, Tw);
+  }
   const R floor_v = R(kPsdFloor);
   R beta[12];  // beta[3a + n] = v_n . gN_a
 #pragma unroll

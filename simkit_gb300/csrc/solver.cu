@@ -1184,7 +1184,10 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     // H(u) + M/h^2 with pinned rows/columns, block-Jacobi inverses
     pt.begin();
     if constexpr (sizeof(R) == 4) {
-      SKG_TRY(launch_tet_hessian<float>(make_tet_args32(m, st->u, w.uh, w.ul), 1, 1, (float*)hbuf, s));
+      int hl = 1;
+      SKG_TRY(launch_tet_hessian<float>(make_tet_args32(m, st->u, w.uh, w.ul), 1, 1, (float*)hbuf, s,
+                                        HessLate{w.hlate, w.hlate_n, &hl}));
+      info->launches += hl - 1;
     } else {
       SKG_TRY(launch_tet_hessian<double>(make_tet_args64(m, st->u), 1, 1, (double*)hbuf, s));
     }
@@ -1730,7 +1733,9 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
       TetArgs<float> ta = make_tet_args32(m, st->u, w.uh, w.ul);
       ta.tet_inst = bt->tet_inst;
       ta.inst_active = bw.active;
-      SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s));
+      int hl = 1;
+      SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s, HessLate{w.hlate, w.hlate_n, &hl}));
+      launches += hl - 1;
     } else {
       TetArgs<double> ta = make_tet_args64(m, st->u);
       ta.tet_inst = bt->tet_inst;
@@ -2250,7 +2255,9 @@ static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const 
     TetArgs<float> ta = make_tet_args32(m, st->u, w.uh, w.ul);
     ta.tet_inst = bt->tet_inst;
     ta.inst_active = bw.active;
-    SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s1));
+    int hl = 1;
+    SKG_TRY(launch_tet_hessian<float>(ta, 1, 1, (float*)hbuf, s1, HessLate{w.hlate, w.hlate_n, &hl}));
+    launches += hl - 1;
   } else {
     TetArgs<double> ta = make_tet_args64(m, st->u);
     ta.tet_inst = bt->tet_inst;
