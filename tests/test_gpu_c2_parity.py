@@ -1,7 +1,7 @@
 """Parity on the benchmarked workload: the 786,432-tet beam (32 x 32 x 128 cubes, rest shape jittered by
 U(-0.1, 0.1) cells, Young's modulus log-uniform [1e5, 1e7] per tet, seed 0), stepped by the
 mixed-precision solver with the settings ``bench.py`` times (two-level grid PCG, Eisenstat-Walker forcing
-capped at 0.3, coarse inverse rebuilt every 8 steps, Newton to a 1e-6 relative residual).
+capped at 0.3, coarse inverse rebuilt every 16 steps, Newton to a 1e-6 relative residual).
 
 * Against simkit: the first two backward-Euler steps from rest, compared with
   ``golden/rollout_beam_32x32x128_first_steps.npz`` (simkit's energies, Hessians, line search and Newton;
@@ -27,7 +27,7 @@ FIXTURE = "rollout_beam_32x32x128_first_steps.npz"
 def _bench_solver(spec, precision="mixed", variant=None):
     from simkit_gb300.solver import BESolver
     kw = dict(pcg_rtol=-0.3) if precision == "mixed" else dict(pcg_rtol=1e-3)
-    s = BESolver.from_spec(spec, precision=precision, pcg_mode=3, coarse="auto", coarse_refresh=8, **kw)
+    s = BESolver.from_spec(spec, precision=precision, pcg_mode=3, coarse="auto", coarse_refresh=16, **kw)
     if variant is not None:
         s.params.pcg_variant = variant
     return s
