@@ -909,10 +909,13 @@ template <typename R> static int64_t cluster_rows_limit() {
   return (int64_t)kClusterMax * (kClusterSmemBudget / (kClusterVals * (int64_t)sizeof(R)));
 }
 
+// read = false: the solve is enqueued and its scalars (iterations, status, residual) are left in scal
+// for the caller to read with its next host round trip
 template <typename R>
 static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
-                     cudaStream_t s, PcgResult* res, int variant = 0, const CoarseDev* cd = nullptr) {
+                     cudaStream_t s, PcgResult* res, int variant = 0, const CoarseDev* cd = nullptr,
+                     bool read = true) {
   const int rb = reduce_blocks(A.nbr);
   const bool grid_form = cd && !cd->inst_agg;
   if (mode == 7 && !grid_form) mode = 5;
@@ -1025,6 +1028,7 @@ static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8
       if (hs[1] != 0.0) break;
     }
   }
+  if (!read) return SKG_OK;
   double h[10];
   SKG_CUDA(cudaMemcpyAsync(h, scal, 10 * sizeof(double), cudaMemcpyDeviceToHost, s));
   SKG_CUDA(cudaStreamSynchronize(s));
@@ -1104,13 +1108,17 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     info->t_gradient_ms += pt.end();
     return read_scalars(w.scal + S_GG, gg, 1, s);
   };
-  auto energy = [&](const R* dx, double step, double* e2) -> int {
+  auto energy_launch = [&](const R* dx, double step) -> int {
     ea.dx = dx;
     ea.step = step;
     pt.begin();
     SKG_TRY(launch_energy<R>(ea, false, s));
     info->launches++;
     info->t_energy_ms += pt.end();
+    return SKG_OK;
+  };
+  auto energy = [&](const R* dx, double step, double* e2) -> int {
+    SKG_TRY(energy_launch(dx, step));
     return read_scalars(w.scal + S_E, e2, 2, s);
   };
   auto split = [&]() -> int {
@@ -1214,33 +1222,44 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     PcgResult pr{};
     pt.begin();
     SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, eta, prm->pcg_max_iter, prm->pcg_mode, w.partials,
-                         w.counter, w.scal, s, &pr, prm->pcg_variant, two_level ? &cdev : nullptr));
+                         w.counter, w.scal, s, &pr, prm->pcg_variant, two_level ? &cdev : nullptr, false));
     info->t_pcg_ms += pt.end();
     info->launches += pr.launches;
-    info->pcg_iters += pr.iters;
     if (record) {
       k_unpad<R><<<blocks_for(n), kBlock, 0, s>>>(pv.x, n, nrec->dx + (int64_t)it * nd);
       SKG_LAUNCHED();
       info->launches++;
-      nrec->pcg_iters_h[it] = pr.iters;
     }
+    // Armijo backtracking (simkit/backtracking_line_search.py:56-67).  The slope g.dx and the first
+    // trial (step 1) are enqueued behind the PCG, and one host round trip reads the PCG's scalars,
+    // the slope and that trial's energy (a failed solve discards the two)
+    k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s>>>(w.g, pv.x, n, w.partials, w.counter, w.scal + S_SLOPE);
+    SKG_LAUNCHED();
+    info->launches++;
+    if (prm->do_line_search && prm->ls_max_iter > 0) SKG_TRY(energy_launch(pv.x, 1.0));
+    double hs[S_SLOPE + 2];
+    SKG_TRY(read_scalars(w.scal, hs, S_SLOPE + 2, s));
+    pr.iters = (int)hs[S_ITERS];
+    pr.status = (int)hs[S_STATUS];
+    info->pcg_iters += pr.iters;
+    if (record) nrec->pcg_iters_h[it] = pr.iters;
     if (pr.status != 0) {
       info->status = pr.status;
       break;
     }
-    // Armijo backtracking (simkit/backtracking_line_search.py:56-67)
-    double slope_dd[2];
-    k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s>>>(w.g, pv.x, n, w.partials, w.counter, w.scal + S_SLOPE);
-    SKG_LAUNCHED();
-    info->launches++;
-    SKG_TRY(read_scalars(w.scal + S_SLOPE, slope_dd, 2, s));
+    const double slope_dd[2] = {hs[S_SLOPE], hs[S_SLOPE + 1]};
     const double slope = slope_dd[0];
     double step = 1.0, enew[2] = {ecur[0], ecur[1]};
     bool accepted = !prm->do_line_search;
     if (prm->do_line_search) {
       const double thr = prm->ls_threshold >= 0.0 ? prm->ls_threshold : 1e-12 + 16.0 * eps_r * ecur[1];
       for (int k = 0; k < prm->ls_max_iter; ++k) {
-        SKG_TRY(energy(pv.x, step, enew));
+        if (k == 0) {
+          enew[0] = hs[S_E];
+          enew[1] = hs[S_E + 1];
+        } else {
+          SKG_TRY(energy(pv.x, step, enew));
+        }
         info->ls_trials++;
         if (enew[0] <= ecur[0] + prm->ls_alpha * step * slope + thr) {
           accepted = true;
