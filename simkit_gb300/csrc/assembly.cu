@@ -104,10 +104,11 @@ __device__ __forceinline__ void store_hess_record(float* dst, const float (&out)
 
 // One thread per tet.  FP32: at most 168 registers so that 3 blocks fit an SM (measured 1.60 ->
 // 1.32 ms of Hessian evaluation per step on the 786,432-tet beam, despite ~140 bytes of spills; the
-// split form below, 128 registers at 4 blocks), and the block's records leave through shared memory: every thread stores its 78 values as pairs
-// at a conflict-free stride, then the block writes its tets' contiguous kHStride records with
-// consecutive lanes on consecutive words - one thread storing its own record would touch 32
-// different records with every warp store (ncu: LSU-throttle stalls).  FP64 stores directly.
+// split form below: 128 registers at 4 blocks), and the block's records leave through shared
+// memory: every thread stores its 78 values as pairs at a conflict-free stride, then the block
+// writes its tets' contiguous kHStride records with consecutive lanes on consecutive words - one
+// thread storing its own record would touch 32 different records with every warp store (ncu:
+// LSU-throttle stalls).  FP64 stores directly.
 // LE: the instantiation for linear-elasticity meshes (constant stiffness, no eigensystem).
 constexpr int kHessThreads = 128;
 constexpr int kHessStage = kTetHessVals + 4;  // staging row stride (82 words: 41 pairs, odd, so the
@@ -118,11 +119,8 @@ constexpr int kHessStage = kTetHessVals + 4;  // staging row stride (82 words: 4
 // the FP64 path the kernel has no spills at 3 blocks per SM and fits 4 (measured on the 786,432-tet
 // beam: 163 us with the FP64 path at 3 blocks, 155 us split at 3, ~144 us split at 4).
 template <typename R, bool LE = false, bool SPLIT = false>
-__global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? (SPLIT ? 4 : 3) : 1) k_tet_hessian(TetArgs<R> a, int disp,
-                                                                                     int project,
-                                                                                     R* __restrict__ hbuf,
-                                                                                     int32_t* late,
-                                                                                     unsigned* late_n) {
+__global__ void __launch_bounds__(kHessThreads, sizeof(R) == 4 ? (SPLIT ? 4 : 3) : 1)
+    k_tet_hessian(TetArgs<R> a, int disp, int project, R* __restrict__ hbuf, int32_t* late, unsigned* late_n) {
   const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   bool valid = e < a.t && !(a.inst_active && !a.inst_active[__ldg(a.tet_inst + e)]);
   if constexpr (sizeof(R) == 8) {
