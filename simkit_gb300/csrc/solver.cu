@@ -1170,12 +1170,13 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     }
     // PCG forcing term: fixed (pcg_rtol > 0) or Eisenstat-Walker choice 2
     // (gamma 0.9, exponent 2, safeguarded) capped at |pcg_rtol|, never
-    // tighter than what brings the residual to a quarter of tol
+    // tighter than what brings the residual to a quarter of tol; the first
+    // one is |pcg_rtol| times the start's relative residual (1 here)
     double eta = prm->pcg_rtol;
     if (prm->pcg_rtol < 0.0) {
       const double eta_max = -prm->pcg_rtol;
       if (it == 0) {
-        eta = eta_max;
+        eta = eta_max * (res < 1.0 ? res : 1.0);   // 1 from x_tilde; a closer start gets a tighter first solve
       } else {
         const double q = res / res_prev;
         eta = 0.9 * q * q;
@@ -1725,7 +1726,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
       if (prm->pcg_rtol < 0.0) {
         const double emax = -prm->pcg_rtol;
         if (it == 0) {
-          e = emax;
+          e = emax * (res < 1.0 ? res : 1.0);   // a start closer than x_tilde gets a tighter first solve
         } else {
           const double q = res / res_prev[i];
           e = 0.9 * q * q;
@@ -1963,7 +1964,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_bctl_newton(BatchCtl c, CtlPara
     if (p.pcg_rtol < 0.0) {
       const double emax = -p.pcg_rtol;
       if (it == 0) {
-        e = emax;
+        e = emax * (res < 1.0 ? res : 1.0);   // as the host loop: the first forcing scales with the start's residual
       } else {
         const double q = res / c.res_prev[i];
         e = 0.9 * q * q;
