@@ -302,6 +302,42 @@ def parity_report(spec, solver_kw, steps_fp64=30):
     return out
 
 
+def dropin_summary(steps=10, warmup=2):
+    """simkit's own call on the device fast path: ``backward_euler`` handed an ElasticPotential's
+    closures and a lumped M (FP64, the linear solves to 1e-12, simkit's stop rule ||alpha dx|| < 1e-6
+    with up to 20 Newton iterations, the step's positions in and out as host arrays) on the
+    12,288-tet 8 x 8 x 32 beam (E 1e6, nu 0.45, gravity, no pins: simkit's integrator takes none),
+    timed on the host clock over ``steps`` steps after ``warmup``."""
+    import scipy.sparse as sps
+    import torch
+    from simkit_gb300 import api
+    from simkit_gb300.beams import make_beam
+    from simkit_gb300.solver import lumped_mass
+    spec = make_beam(8, 8, 32, ym=1e6, pr=0.45)
+    m = lumped_mass(spec.X, spec.T, spec.rho)
+    M = sps.diags(np.repeat(m, 3)).tocsc()
+    f = (m[:, None] * spec.gravity[None, :]).reshape(-1, 1)
+    pot = api.ElasticPotential(spec.X, spec.T, spec.mu, spec.lam, f_ext=f)
+    h = 1.0 / 60.0
+    x_prev = spec.X.reshape(-1, 1).copy()
+    x_curr = x_prev.copy()
+    t0 = None
+    for k in range(warmup + steps):
+        if k == warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        x_next = api.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h,
+                                    tolerance=1e-6, max_iter=20)
+        x_prev, x_curr = x_curr, x_next
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"workload": "simkit.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h, "
+                        "tolerance=1e-6, max_iter=20) on the 8 x 8 x 32 beam (12,288 tets), ElasticPotential "
+                        "closures, lumped M, FP64, host arrays in and out",
+            "steps": steps, "steps_per_s": steps / dt, "ms_per_step": 1e3 * dt / steps,
+            "stepper": "device fast path (one BESolver per (h, M))" if len(pot._steppers) == 1 else "closure path"}
+
+
 def batched_summary(instances=128, steps=4, warmup=3, plain_sample=4, train_steps=12, seed=0):
     """Reduced 512-beam workload for the headline line: ``instances`` beams of the same seeded
     distribution (nx, ny in 4..16, nz in 8..48, own E, nu and gravity direction) stepped together
@@ -675,6 +711,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity report of the headline line")
     ap.add_argument("--no-batched", action="store_true", help="skip the reduced batched workload of the headline line")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the timing of the drop-in backward_euler call in the headline line")
     ap.add_argument("--no-graph", action="store_true",
                     help="batched and serving workloads: the host-driven Newton loop instead of the device loop")
     ap.add_argument("--ref-layers", type=int, default=2,
@@ -848,6 +886,9 @@ def main():
     batched = None
     if rank == 0 and not args.small and not args.no_batched:
         batched = batched_summary()
+    dropin = None
+    if rank == 0 and not args.small and not args.no_dropin:
+        dropin = dropin_summary()
 
     if rank == 0:
         line = {
@@ -870,6 +911,7 @@ def main():
             "cpu_baseline": cpu,
             "parity": parity,
             "batched": batched,
+            "dropin": dropin,
             "clocks": clock_info,
         }
         print(json.dumps(line))
