@@ -302,7 +302,7 @@ def parity_report(spec, solver_kw, steps_fp64=30):
     return out
 
 
-def dropin_summary(steps=10, warmup=2):
+def dropin_summary(steps=10, warmup=2, cpu_steps=2):
     """simkit's own call on the device fast path: ``backward_euler`` handed an ElasticPotential's
     closures and a lumped M (FP64, the linear solves to 1e-12, simkit's stop rule ||alpha dx|| < 1e-6
     with up to 20 Newton iterations, the step's positions in and out as host arrays) on the
@@ -331,11 +331,29 @@ def dropin_summary(steps=10, warmup=2):
         x_prev, x_curr = x_curr, x_next
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    return {"workload": "simkit.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h, "
-                        "tolerance=1e-6, max_iter=20) on the 8 x 8 x 32 beam (12,288 tets), ElasticPotential "
-                        "closures, lumped M, FP64, host arrays in and out",
-            "steps": steps, "steps_per_s": steps / dt, "ms_per_step": 1e3 * dt / steps,
-            "stepper": "device fast path (one BESolver per (h, M))" if len(pot._steppers) == 1 else "closure path"}
+    out = {"workload": "simkit.backward_euler(x_curr, x_prev, pot.energy, pot.gradient, pot.hessian, M, h, "
+                       "tolerance=1e-6, max_iter=20) on the 8 x 8 x 32 beam (12,288 tets), ElasticPotential "
+                       "closures, lumped M, FP64, host arrays in and out",
+           "steps": steps, "steps_per_s": steps / dt, "ms_per_step": 1e3 * dt / steps,
+           "stepper": "device fast path (one BESolver per (h, M))" if len(pot._steppers) == 1 else "closure path"}
+    if cpu_steps > 0:
+        # the same call on the oracle (simkit's backward_euler / newton_solver with spsolve), same start
+        from oracle import fem, snh as osnh, solvers as osol
+        J, vol = fem.deformation_jacobian(spec.X, spec.T), fem.tet_volumes(spec.X, spec.T)
+        Eo = lambda x: osnh.energy_x(x, J, spec.mu, spec.lam, vol) - float((f.T @ x).item())
+        Go = lambda x: osnh.gradient_x(x, J, spec.mu, spec.lam, vol) - f
+        Ho = lambda x: osnh.hessian_x(x, J, spec.mu, spec.lam, vol)
+        x_prev = spec.X.reshape(-1, 1).copy()
+        x_curr = x_prev.copy()
+        t0 = time.perf_counter()
+        for _ in range(cpu_steps):
+            x_next = osol.backward_euler(x_curr, x_prev, Eo, Go, Ho, M, h, tolerance=1e-6, max_iter=20)
+            x_prev, x_curr = x_curr, x_next
+        cdt = time.perf_counter() - t0
+        out["oracle_steps_per_s"] = cpu_steps / cdt
+        out["oracle_sample"] = (f"the oracle's backward_euler (simkit's algorithm, spsolve) on the host cores, the "
+                                f"first {cpu_steps} steps from rest, same call")
+    return out
 
 
 def batched_summary(instances=128, steps=4, warmup=3, plain_sample=4, train_steps=12, seed=0):
@@ -888,7 +906,7 @@ def main():
         batched = batched_summary()
     dropin = None
     if rank == 0 and not args.small and not args.no_dropin:
-        dropin = dropin_summary()
+        dropin = dropin_summary(cpu_steps=0 if args.no_cpu_baseline else 2)
 
     if rank == 0:
         line = {
