@@ -791,7 +791,7 @@ def main():
     stream = torch.cuda.current_stream()
     # the state the timed steps start from (the end-to-end pass replays the same steps); both passes
     # start with a fresh coarse inverse, so that they rebuild it at the same steps
-    solver._coarse_age = None
+    solver.refresh_coarse()
     X0 = spec.X.reshape(-1)
     x_start = ((X0 + solver.u_curr.cpu().numpy()).reshape(-1, 1), (X0 + solver.u_prev.cpu().numpy()).reshape(-1, 1))
     clocks = ClockSampler(local)
@@ -820,7 +820,7 @@ def main():
     tet_hess_per_s = ws * newton * spec.n_tets / (ms_max / 1000.0)
 
     # profiled pass over the same number of steps (phase times by CUDA events on the launching stream)
-    solver._coarse_age = None
+    solver.refresh_coarse()
     solver.params.profile = 1
     pinfos = [solver.step() for _ in range(args.steps)]
     solver.params.profile = 0
@@ -872,7 +872,7 @@ def main():
     bufs[0][...] = x_start[0]
     bufs[1][...] = x_start[1]
     x_curr, x_prev = bufs[0], bufs[1]
-    solver._coarse_age = None
+    solver.refresh_coarse()
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()

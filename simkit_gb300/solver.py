@@ -165,6 +165,11 @@ class BESolver:
     def _coarse_n_agg(self) -> int:
         return int(self.mesh._coarse_c.n_agg) if getattr(self.mesh, "_coarse_c", None) is not None else 0
 
+    def refresh_coarse(self):
+        """Rebuild the coarse inverse at the next step's first Newton iteration (and count the refresh
+        period from there)."""
+        self._coarse_age = None
+
     def set_contact_planes(self, planes, mass_weighted=True):
         """Contact springs against planes, each (k, p, n) (simkit/energies/contact_springs_plane.py);
         mass_weighted: spring weights are the lumped vertex masses (simkit's M) instead of 1."""
