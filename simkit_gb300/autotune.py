@@ -140,6 +140,7 @@ def tune_batch_policy(bsolver, policies=BATCH_POLICIES, use_cache=True):
         return (int(vk), int(mc)), table[key]["ms"]
     st = bsolver.state()
     steps = bsolver.steps
+    age = getattr(bsolver, "_coarse_age", None)   # every candidate step takes the same refresh decision
     timings = {}
     stream = torch.cuda.current_stream()
     for vk, mc in policies:
@@ -147,6 +148,7 @@ def tune_batch_policy(bsolver, policies=BATCH_POLICIES, use_cache=True):
         best = None
         for _ in range(2):
             bsolver.set_state(st)
+            bsolver._coarse_age = age
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             bsolver.step()
@@ -157,6 +159,7 @@ def tune_batch_policy(bsolver, policies=BATCH_POLICIES, use_cache=True):
         timings[f"{vk},{mc}"] = best
     bsolver.set_state(st)
     bsolver.steps = steps
+    bsolver._coarse_age = age
     vk, mc = map(int, min(timings, key=timings.get).split(","))
     bsolver.params.batch_vec_kb, bsolver.params.batch_min_cluster = vk, mc
     if use_cache:

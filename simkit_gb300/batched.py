@@ -37,7 +37,8 @@ class BatchedBESolver:
     material, gravity direction and pins.  ``coarse``: two-level PCG with
     per-instance aggregates ('auto': 4^3 mesh spacings, or a box size), None for
     the one-level block-Jacobi PCG; ``coarse_refresh``: 'step' (per-instance coarse inverses
-    rebuilt at the first Newton iteration of each step) or 'newton' (at every iteration).
+    rebuilt at the first Newton iteration of each step), 'newton' (at every iteration) or an int k
+    (at the first Newton iteration of every k-th step; the steps between reuse them).
     """
 
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
@@ -78,8 +79,8 @@ class BatchedBESolver:
         if coarse is not None:
             _, self.coarse_boxes = mesh.set_coarse_inst(np.concatenate(pins) == 0, np.array(rows),
                                                         box=4 if coarse == "auto" else int(coarse))
-        if coarse_refresh not in ("step", "newton"):
-            raise ValueError("coarse_refresh must be 'step' or 'newton'")
+        if not (coarse_refresh in ("step", "newton") or (isinstance(coarse_refresh, int) and coarse_refresh >= 1)):
+            raise ValueError("coarse_refresh must be 'step', 'newton' or an int >= 1")
         self._coarse_refresh = coarse_refresh
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
@@ -88,12 +89,15 @@ class BatchedBESolver:
     @classmethod
     def from_device(cls, mesh, inst_rows, inst_tets, mass, f_ext, pinned, dt=1.0 / 60.0, tol=1e-6, max_newton=20,
                     precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, do_line_search=True, ls_threshold=None,
-                    profile=False, integrator="be", graph=True):
+                    profile=False, integrator="be", graph=True, coarse_refresh="step"):
         """A batch over an already concatenated device mesh: ``inst_rows`` / ``inst_tets`` (host
         int arrays, n_inst + 1) delimit the instances; mass (n), f_ext (3n) f64 and pinned (3n) u8
         are device tensors."""
         self = cls.__new__(cls)
         self.graph = graph
+        if not (coarse_refresh in ("step", "newton") or (isinstance(coarse_refresh, int) and coarse_refresh >= 1)):
+            raise ValueError("coarse_refresh must be 'step', 'newton' or an int >= 1")
+        self._coarse_refresh = coarse_refresh
         self.n_inst = len(inst_rows) - 1
         if self.n_inst <= 0:
             raise ValueError("empty batch")
@@ -143,12 +147,19 @@ class BatchedBESolver:
             profile=int(profile), integrator=INTEGRATORS[integrator],
             coarse_refresh=int(getattr(self, "_coarse_refresh", "step") == "newton"))
         self._infos = (StepInfoC * self.n_inst)()
-        self._plans = {}          # device-loop graphs, one per rotation of the state buffers
+        self._coarse_age = None   # steps since the coarse inverses were built (integer refresh period)
+        self._plans = {}          # device-loop graphs, one per rotation of the state buffers (and per
+                                  # refresh decision with an integer refresh period)
         self._plan_key = None     # parameters and contact planes the plans were recorded with
         self._u_warm = None       # fixed buffer the warm start is copied into for the graphs
         init = getattr(self, "_contact_init", (None, True))
         self.set_contact_planes(*init)
         self.steps = 0
+
+    def refresh_coarse(self):
+        """With an integer refresh period: rebuild the per-instance coarse inverses at the next step
+        (and count the period from there)."""
+        self._coarse_age = None
 
     def set_contact_planes(self, planes, mass_weighted=True):
         """Contact springs against planes, each (k, p, n), for every instance."""
@@ -178,6 +189,11 @@ class BatchedBESolver:
                       u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
                       u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
         total = StepInfoC()
+        k = getattr(self, "_coarse_refresh", "step")
+        if isinstance(k, int):
+            rebuild = self._coarse_age is None or self._coarse_age + 1 >= k
+            self.params.coarse_refresh = 0 if rebuild else -1
+            self._coarse_age = 0 if rebuild else self._coarse_age + 1
         # a one-instance batch with coarse data inverts its coarse operator with a cooperative grid
         # launch, which stays on the host-driven path
         if self.graph and not self.params.profile and not (self.n_inst == 1 and bool(self.mesh.c.coarse)):
@@ -205,18 +221,23 @@ class BatchedBESolver:
         return [conv(c) for c in self._infos], conv(total)
 
     def _params_key(self):
+        """The parameters and contact planes the graphs depend on, less the per-step refresh decision
+        (graphs for both decisions are kept)."""
+        refresh = self.params.coarse_refresh
+        self.params.coarse_refresh = 0
         raw = ctypes.string_at(ctypes.addressof(self.params), ctypes.sizeof(self.params))
+        self.params.coarse_refresh = refresh
         planes = ctypes.string_at(ctypes.addressof(self._planes), ctypes.sizeof(self._planes)) if self._planes else b""
         return raw + planes
 
     def _plan(self, st):
-        """The graph for this state binding (recorded on first use; all of them again after a
-        change of parameters or contact planes)."""
+        """The graph for this state binding and refresh decision (recorded on first use; all of them
+        again after a change of the other parameters or of the contact planes)."""
         key = self._params_key()
         if key != self._plan_key:
             self.release_plans()
             self._plan_key = key
-        bind = (st.u, st.u_curr, st.u_prev, st.u_prev2, st.u_prev3, st.u_warm)
+        bind = (st.u, st.u_curr, st.u_prev, st.u_prev2, st.u_prev3, st.u_warm, self.params.coarse_refresh)
         plan = self._plans.get(bind)
         if plan is None:
             h = ctypes.c_void_p()

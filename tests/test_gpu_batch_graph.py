@@ -44,6 +44,22 @@ def test_graph_step_equals_host_driven_step(coarse, precision):
     assert tg.launches > 0
 
 
+def test_graph_step_with_a_coarse_refresh_period():
+    """Per-instance coarse inverses rebuilt every second step: the graph path keeps one graph per state
+    rotation and refresh decision (a period of 2 against 3 rotations meets all six) and takes bitwise
+    the host-driven path's steps."""
+    from simkit_gb300.beams import beam_batch
+    specs = beam_batch(8, seed=3, nx_range=(4, 8), ny_range=(4, 6), nz_range=(8, 16))
+    g, h = _pair(specs, coarse="auto", coarse_refresh=2)
+    for _ in range(7):
+        ig, tg = g.step()
+        ih, th = h.step()
+        assert tg.status == 0 and th.status == 0
+        _same_records(ig, tg, ih, th)
+        assert torch.equal(g.u_curr, h.u_curr)
+    assert len(g._plans) == 6          # three rotations x (rebuild, reuse)
+
+
 def test_graph_step_bdf2_with_contact_and_warm_start():
     from simkit_gb300.beams import beam_batch
     specs = beam_batch(6, seed=9, nx_range=(4, 8), ny_range=(4, 6), nz_range=(8, 16))
