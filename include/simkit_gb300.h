@@ -368,8 +368,8 @@ typedef struct skg_be_state {
   const double* f_ext;      /* (3n) external force */
   const uint8_t* pinned;    /* (3n) 1 = DOF held at its rest position */
   const double* u_warm;     /* (3n) optional Newton initial guess (batched step): used per
-                               instance only if the incremental potential there is below its
-                               value at x_tilde; the relative residual stays judged against
+                               instance only if the gradient norm there is below the one at
+                               x_tilde; the relative residual stays judged against
                                ||g(x_tilde)|| */
   const double* u_prev2;    /* (3n) displacement at step k-2 (BDF2 only) */
   const double* u_prev3;    /* (3n) displacement at step k-3 (BDF2 only) */

@@ -1692,13 +1692,12 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
   SKG_TRY(split());
   SKG_TRY(energy(nullptr, nullptr, nullptr, ecur.data()));
   if (st->u_warm) {
-    // energy-judged warm start: keep it per instance only if the incremental potential
-    // (the function Newton minimises) is lower there than at x_tilde
+    // residual-judged warm start: keep it per instance only where its gradient norm is below the
+    // one at x_tilde (the start then begins Newton at a relative residual below 1)
     SKG_CUDA(cudaMemcpyAsync(st->u, st->u_warm, nd * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    SKG_TRY(split());
-    SKG_TRY(energy(nullptr, nullptr, nullptr, etry.data()));
+    SKG_TRY(gradient());
     for (int i = 0; i < ni; ++i) {
-      mask[i] = (isfinite(etry[2 * i]) && etry[2 * i] < ecur[2 * i]) ? 1 : 0;
+      mask[i] = (isfinite(gg[i]) && sqrt(gg[i]) < g0[i]) ? 1 : 0;
       infos[i].warm_used = mask[i];
     }
     SKG_CUDA(cudaMemcpyAsync(bw.mask, mask.data(), ni, cudaMemcpyHostToDevice, s));
@@ -1934,10 +1933,10 @@ __global__ void __launch_bounds__(kCtlThreads) k_bctl_begin(BatchCtl c, CtlParam
   if (threadIdx.x < 8) c.ctr[threadIdx.x] = 0;
 }
 
-// energy-judged warm start: keep it where the incremental potential is below its value at x_tilde
+// residual-judged warm start: kept per instance where its gradient norm is below the one at x_tilde (g0)
 __global__ void __launch_bounds__(kCtlThreads) k_bctl_warm(BatchCtl c) {
   for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
-    const bool keep = isfinite(c.e2[2 * i]) && c.e2[2 * i] < c.ecur[2 * i];
+    const bool keep = isfinite(c.gg[i]) && sqrt(c.gg[i]) < c.g0[i];
     c.mask[i] = keep ? 1 : 0;
     c.info[i].warm_used = keep ? 1 : 0;
   }
@@ -2245,8 +2244,7 @@ static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const 
   launches++;
   if (st->u_warm) {
     SKG_CUDA(cudaMemcpyAsync(st->u, st->u_warm, nd * sizeof(double), cudaMemcpyDeviceToDevice, s0));
-    SKG_TRY(split(s0));
-    SKG_TRY(energy(nullptr, nullptr, nullptr, s0));
+    SKG_TRY(gradient(s0));
     k_bctl_warm<<<1, kCtlThreads, 0, s0>>>(ctl);
     SKG_LAUNCHED();
     k_choose_start<<<blocks_for(n), kBlock, 0, s0>>>(st->u, st->u_warm, w.ut, bw.mask, bt->vert_inst, n);

@@ -320,7 +320,7 @@ class BeamServer:
 
     max_cohort: requests per cohort; max_live: requests in flight; hbm_reserve_gb: HBM
     left free; net: a trained ``WarmStartMLP`` (the learned warm start with its
-    energy-judged fallback) or None for plain Newton starts; coarse: two-level PCG with
+    residual-judged fallback) or None for plain Newton starts; coarse: two-level PCG with
     per-shape aggregates (built with the templates)."""
 
     def __init__(self, max_cohort=512, max_live=2048, hbm_reserve_gb=16.0, net=None, device="cuda",

@@ -9,10 +9,10 @@ and backward passes runs on the tcgen05 tensor-core kernel
 (``skg_mlp_gemm``); training uses Adam on FP32 master weights.
 
 The network only proposes a starting point: ``BatchedBESolver.step`` keeps it
-for an instance only if the incremental potential (the function Newton
-minimises) is lower there than at ``x_tilde`` - otherwise that instance falls
-back to ``x_tilde`` - and Newton always runs to the same relative residual,
-measured against ``||g(x_tilde)||``.  So the network changes the iteration
+for an instance only if the gradient norm there is below the one at ``x_tilde``
+(the residual-judged fallback) - otherwise that instance falls back to
+``x_tilde`` - and Newton always runs to the same relative residual, measured
+against ``||g(x_tilde)||``.  So the network changes the iteration
 count, never the converged answer.
 """
 

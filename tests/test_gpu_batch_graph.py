@@ -2,7 +2,7 @@
 decisions in control kernels, Newton iterations and line-search trials as conditional graph nodes)
 against the host-driven batched step, which makes the same decisions with the same arithmetic on the
 host: bitwise the same positions and the same per-instance records, for backward Euler and BDF2, with
-the learned warm start's energy-judged choice, with contact planes, and when the PCG is starved."""
+the learned warm start's residual-judged choice, with contact planes, and when the PCG is starved."""
 
 import numpy as np
 import pytest

@@ -179,7 +179,7 @@ def test_warm_start_training_and_effect():
         d = (results["learned"][0] - results["plain"][0]).abs().max().item()
         assert d <= 1e-6 * results["plain"][0].abs().max().item() + 1e-12
     print(f"\nloss {first:.3e} -> {last:.3e}; newton iterations {its}; prediction kept {np.mean(kept):.2f}")
-    # the prediction is only kept where it lowers the incremental potential, so it cannot make an
+    # the prediction is only kept where it lowers the gradient norm, so it cannot make an
     # instance worse by more than Newton's own variation (measured on a GB300: 289 learned against 288
     # plain Newton iterations, the prediction kept for 4% of the instance-steps): at most 1% more
     assert its["learned"] <= its["plain"] + max(2, 0.01 * its["plain"])
