@@ -742,7 +742,7 @@ def main():
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the timing of the drop-in backward_euler call in the headline line")
     ap.add_argument("--no-graph", action="store_true",
-                    help="batched and serving workloads: the host-driven Newton loop instead of the device loop")
+                    help="the host-driven Newton loop instead of the device loop (a recorded CUDA graph per step)")
     ap.add_argument("--ref-layers", type=int, default=2,
                     help="cube layers of the workload beam in the CPU reference sample (2: 12,288 tets, "
                          "about 1 s per measured step)")
@@ -782,7 +782,7 @@ def main():
     workload = SMALL_WORKLOAD if args.small else WORKLOAD
     coarse = None if args.coarse == "none" else (args.coarse if args.coarse == "auto" else int(args.coarse))
     solver_kw = dict(precision=args.precision, pcg_mode=args.pcg_mode, pcg_rtol=args.pcg_rtol_single,
-                     coarse=coarse, coarse_refresh=args.coarse_refresh)
+                     coarse=coarse, coarse_refresh=args.coarse_refresh, device_loop=not args.no_graph)
     solver = BESolver.from_spec(spec, **solver_kw)
     nb = solver.mesh.nb
     for _ in range(args.warmup):
@@ -796,6 +796,8 @@ def main():
     else:
         variant, variant_us = args.pcg_variant, {}
         solver.params.pcg_variant = variant
+    # the device-loop graphs of every state rotation and refresh decision, recorded before any timing
+    n_plans = solver.prepare_plans()
 
     barrier = ranks.barrier
     stream = torch.cuda.current_stream()
@@ -927,6 +929,7 @@ def main():
             "config": {"workload": workload, "tets": spec.n_tets, "verts": spec.n_verts, "blocks": nb,
                        "precision": args.precision, "pcg_mode": args.pcg_mode, "pcg_rtol": args.pcg_rtol_single,
                        "pcg_variant": variant, "pcg_variant_us_per_iter": variant_us,
+                       "newton_loop": "device (one CUDA graph per step)" if n_plans else "host",
                        "coarse_box": solver.coarse_box, "coarse_refresh": args.coarse_refresh,
                        "tol": 1e-6, "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2, no flush"},
             "tet_hessians_per_s": tet_hess_per_s,

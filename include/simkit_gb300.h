@@ -447,6 +447,22 @@ int skg_be_batch_plan_create(const skg_tet_mesh* mesh, const skg_batch* batch, c
 int skg_be_batch_plan_step(skg_batch_plan* plan, skg_step_info* infos_h, skg_step_info* total_h, void* stream);
 int skg_be_batch_plan_destroy(skg_batch_plan* plan);
 
+/* skg_be_step with the Newton loop on the device: skg_be_plan_create records one call for these
+ * buffers into an executable CUDA graph (the batch control kernels over one instance make the
+ * decisions, the reductions are skg_be_step's own, the PCG takes its forcing term from device
+ * memory); skg_be_plan_step launches it and synchronizes once to return the record skg_be_step
+ * returns, for bitwise the same step (no phase times).  Same lifetime rules as the batch plan;
+ * the plan allocates a few KB of device control state.  skg_be_plan_eligible returns 1 when the
+ * parameters can be recorded: no profiling, no Newton record, stop_rule 0, and a PCG form that
+ * runs as grid launches (the cluster form of small meshes and mode 0 need the host loop);
+ * skg_be_plan_create returns SKG_ERR_ARG otherwise.  No counterpart in simkit, whose Newton loop
+ * is host Python (solvers/newton.py:46-69). */
+int skg_be_plan_eligible(const skg_tet_mesh* mesh, const skg_be_params* params);
+int skg_be_plan_create(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state,
+                       void* workspace, skg_batch_plan** plan_h);
+int skg_be_plan_step(skg_batch_plan* plan, skg_step_info* info_h, void* stream);
+int skg_be_plan_destroy(skg_batch_plan* plan);
+
 /* ---------------------------------------------------------------------- */
 /* generic sparse solve: replaces spsolve in newton_solver (newton.py:52)   */
 /* ---------------------------------------------------------------------- */

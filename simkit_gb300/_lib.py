@@ -140,6 +140,10 @@ _SIGNATURES = {
     "skg_be_batch_plan_create": (c_i32, [P(TetMeshC), P(BatchC), P(BEParamsC), P(BEStateC), c_vp, P(c_vp)]),
     "skg_be_batch_plan_step": (c_i32, [c_vp, P(StepInfoC), P(StepInfoC), c_vp]),
     "skg_be_batch_plan_destroy": (c_i32, [c_vp]),
+    "skg_be_plan_eligible": (c_i32, [P(TetMeshC), P(BEParamsC)]),
+    "skg_be_plan_create": (c_i32, [P(TetMeshC), P(BEParamsC), P(BEStateC), c_vp, P(c_vp)]),
+    "skg_be_plan_step": (c_i32, [c_vp, P(StepInfoC), c_vp]),
+    "skg_be_plan_destroy": (c_i32, [c_vp]),
     "skg_pcg_workspace_size": (c_i64, [c_i64]),
     "skg_pcg_bsr64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_i32, P(c_i32), c_vp, c_vp]),
     "skg_mlp_gemm": (c_i32, [c_vp, c_i64, c_i64, c_vp, c_i32, c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp,

@@ -646,14 +646,15 @@ __global__ void __launch_bounds__(kBlock) k_energy(EnergyArgs<R> a) {
   double acc[2] = {0.0, 0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t total = a.tet.t + (DIRECT ? 0 : a.n);
-  const R step = R(a.step);
+  const double stepd = a.step_dev ? *a.step_dev : a.step;
+  const R step = R(stepd);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += stride) {
     if (i < a.tet.t) {
       const double val = tet_energy_term<R, DIRECT>(a, i, step);
       acc[0] += val;
       acc[1] += fabs(val);
     } else {
-      vertex_energy_terms<R>(a, i - a.tet.t, a.step, acc);
+      vertex_energy_terms<R>(a, i - a.tet.t, stepd, acc);
     }
   }
   grid_sum<2, kBlock>(acc, a.partials, a.counter, a.out);

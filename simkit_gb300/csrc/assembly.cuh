@@ -164,6 +164,7 @@ template <typename R> struct EnergyArgs {
   unsigned* counter;
   double* out;          // out[0] = energy, out[1] = magnitude
   Contact contact;
+  const double* step_dev = nullptr;   // when set, the step is read here (device-decided line search)
 };
 
 struct Workspace {

@@ -185,7 +185,8 @@ template <typename R>
 __global__ void __launch_bounds__(kBlock) k_pcg_init(Bsr<R> A, const double* __restrict__ b, double bsign,
                                                      const uint8_t* __restrict__ pinned, PcgVecs<R> v,
                                                      double rtol, int max_iter, double* partials,
-                                                     unsigned* counter, double* scal) {
+                                                     unsigned* counter, double* scal,
+                                                     const double* __restrict__ rtol_dev = nullptr) {
   double acc[3] = {0.0, 0.0, 0.0};
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A.nbr; i += stride) {
@@ -207,6 +208,7 @@ __global__ void __launch_bounds__(kBlock) k_pcg_init(Bsr<R> A, const double* __r
   acc[2] = acc[1];
   if (grid_sum<3, kBlock>(acc, partials, counter, scal + S_TMP) && threadIdx.x == 0) {
     const double rz = scal[S_TMP], rr = scal[S_TMP + 1], bb = scal[S_TMP + 2];
+    if (rtol_dev) rtol = *rtol_dev;   // the forcing term decided on the device
     scal[S_RZ] = rz;
     scal[S_RR] = rr;
     scal[S_BB] = bb;
@@ -909,21 +911,32 @@ template <typename R> static int64_t cluster_rows_limit() {
   return (int64_t)kClusterMax * (kClusterSmemBudget / (kClusterVals * (int64_t)sizeof(R)));
 }
 
+// the PCG form a solve of nbr block rows runs in: 3 (auto) becomes the cluster form (2) up to
+// kClusterAutoRows, above it the two-level grid form (7) with whole-mesh coarse data, else the
+// one-level grid form (5); the cluster form falls back to 5 past what one cluster holds
+template <typename R>
+static int resolve_pcg_mode(int mode, int64_t nbr, bool grid_form) {
+  if (mode == 7 && !grid_form) mode = 5;
+  if (mode == 3) mode = nbr <= kClusterAutoRows ? 2 : (grid_form ? 7 : 5);
+  if (mode == 2 && nbr > cluster_rows_limit<R>()) mode = 5;
+  return mode;
+}
+
 // read = false: the solve is enqueued and its scalars (iterations, status, residual) are left in scal
-// for the caller to read with its next host round trip
+// for the caller to read with its next host round trip.  rtol_dev: the relative tolerance is read
+// from device memory when the solve starts (rtol is then ignored)
 template <typename R>
 static int pcg_solve(const Bsr<R>& A, const double* b, double bsign, const uint8_t* pinned, PcgVecs<R> v,
                      double rtol, int max_iter, int mode, double* partials, unsigned* counter, double* scal,
                      cudaStream_t s, PcgResult* res, int variant = 0, const CoarseDev* cd = nullptr,
-                     bool read = true) {
+                     bool read = true, const double* rtol_dev = nullptr) {
   const int rb = reduce_blocks(A.nbr);
   const bool grid_form = cd && !cd->inst_agg;
-  if (mode == 7 && !grid_form) mode = 5;
-  if (mode == 3) mode = A.nbr <= kClusterAutoRows ? 2 : (grid_form ? 7 : 5);
-  if (mode == 2 && A.nbr > cluster_rows_limit<R>()) mode = 5;
+  mode = resolve_pcg_mode<R>(mode, A.nbr, grid_form);
+  if (rtol_dev && (mode == 0 || mode == 2)) return fail(SKG_ERR_ARG, "pcg: a device tolerance needs a grid form");
   res->launches = 0;
   if (mode != 2) {
-    k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal);
+    k_pcg_init<R><<<rb, kBlock, 0, s>>>(A, b, bsign, pinned, v, rtol, max_iter, partials, counter, scal, rtol_dev);
     SKG_LAUNCHED();
     res->launches = 1;
   }
@@ -1046,6 +1059,18 @@ static int read_scalars(const double* dev, double* host, int count, cudaStream_t
   return SKG_OK;
 }
 
+// whether a single-mesh step runs the two-level PCG: the whole-mesh form with the grid kernel (mode 7,
+// or mode 3 above the cluster size), the per-instance form with the cluster kernel (mode 2, or mode 3 up
+// to the cluster size)
+template <typename R>
+static bool single_two_level(const skg_tet_mesh* m, const skg_be_params* prm) {
+  const int64_t n = m->n_verts;
+  const bool inst_form = m->coarse && m->coarse->inst_agg;
+  const bool small = n <= kClusterAutoRows && n <= cluster_rows_limit<R>();
+  return m->coarse && (inst_form ? (prm->pcg_mode == 2 || prm->pcg_mode == 3) && small && m->coarse->n_inst == 1
+                                 : prm->pcg_mode == 7 || (prm->pcg_mode == 3 && n > kClusterAutoRows));
+}
+
 template <typename R>
 static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be_state* st, Workspace& w,
                    skg_step_info* info, cudaStream_t s) {
@@ -1129,14 +1154,9 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
 
   info->newton_iters = 0; info->pcg_iters = 0; info->ls_trials = 0; info->status = SKG_OK;
   info->min_alpha = 1.0;
-  // two-level PCG when the mesh has coarse data: the whole-mesh form with the grid kernel (mode 7, or
-  // mode 3 above the cluster size), the per-instance form with the cluster kernel (mode 2, or mode 3
-  // up to the cluster size)
+  // two-level PCG when the mesh has coarse data
   const bool inst_form = m->coarse && m->coarse->inst_agg;
-  const bool small = n <= kClusterAutoRows && n <= cluster_rows_limit<R>();
-  const bool two_level =
-      m->coarse && (inst_form ? (prm->pcg_mode == 2 || prm->pcg_mode == 3) && small && m->coarse->n_inst == 1
-                              : prm->pcg_mode == 7 || (prm->pcg_mode == 3 && n > kClusterAutoRows));
+  const bool two_level = single_two_level<R>(m, prm);
   CoarseDev cdev{};
   if (two_level) cdev = make_coarse_dev(m, w);
   double gg;
@@ -1243,6 +1263,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
     pr.iters = (int)hs[S_ITERS];
     pr.status = (int)hs[S_STATUS];
     info->pcg_iters += pr.iters;
+    info->newton_iters = it + 1;   // a failed solve counts as the iteration it ended
     if (record) nrec->pcg_iters_h[it] = pr.iters;
     if (pr.status != 0) {
       info->status = pr.status;
@@ -1955,7 +1976,12 @@ __global__ void __launch_bounds__(kCtlThreads) k_bctl_newton(BatchCtl c, CtlPara
   for (int i = threadIdx.x; i < c.ni; i += blockDim.x) {
     c.active[i] = 0;
     skg_step_info& f = c.info[i];
-    if (it >= p.max_newton || f.status != SKG_OK || !(c.g0[i] > 0.0)) continue;
+    if (f.status != SKG_OK) continue;
+    if (!isfinite(c.gg[i])) {   // as the host loop: a non-finite gradient ends the step
+      f.status = SKG_ERR_NONFINITE;
+      continue;
+    }
+    if (it >= p.max_newton || !(c.g0[i] > 0.0)) continue;
     const double res = sqrt(c.gg[i]) / c.g0[i];
     f.residual = res;
     if (res < p.tol || sqrt(c.gg[i]) < 1e-10 * c.fnorm[i]) continue;
@@ -2100,6 +2126,7 @@ struct skg_batch_plan {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cap[3] = {nullptr, nullptr, nullptr};
+  void* own = nullptr;            // device control state the plan allocated (single-mesh plans)
   skg_step_info* info = nullptr;  // device: n_inst records, then the total
   int32_t* ctr = nullptr;         // device loop counters
   int ni = 0;
@@ -2352,6 +2379,246 @@ static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const 
   return SKG_OK;
 }
 
+// ---------------------------------------------- single mesh, device loop --
+// One skg_be_step recorded as a graph: the Newton loop and the line search are conditional WHILE
+// nodes decided by the batch control kernels over one instance, the reductions are the whole-mesh
+// ones of the host loop (gradient norm, energy, slope) writing into the control state, and the PCG
+// reads its forcing term from it.  The same kernels in the same order with the same arithmetic as
+// be_step: the two take bitwise the same steps.
+
+// the PCG's iterations and status for the search control kernel
+__global__ void k_sctl_pcg(const double* __restrict__ scal, int32_t* pit, int32_t* pst) {
+  pit[0] = (int32_t)scal[S_ITERS];
+  pst[0] = (int32_t)scal[S_STATUS];
+}
+
+// u += steps[0] * dx on free DOFs when the search accepted a step
+template <typename R>
+__global__ void k_apply_step_ctl(double* __restrict__ u, const R* __restrict__ dx, const double* __restrict__ steps,
+                                 const uint8_t* __restrict__ accept, int64_t n, const uint8_t* __restrict__ pinned) {
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= n || !accept[0]) return;
+  const double step = steps[0];
+  const Vec3<R> d = ld3c(dx, v);
+  const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (!(pinned && pinned[3 * v + c])) u[3 * v + c] += step * dd[c];
+}
+
+// control state of one instance: flags, per-instance scalars (two slots each: the slope buffer takes
+// g.dx and dx.dx), counters and two step records (the instance's, then the total); base null: sizes only
+static BatchCtl carve_single_ctl(void* base, int64_t* bytes) {
+  Carve cv(base);
+  BatchCtl c{};
+  c.ni = 1;
+  c.active = cv.take<uint8_t>(16); c.mask = cv.take<uint8_t>(16); c.accept = cv.take<uint8_t>(16);
+  c.eta = cv.take<double>(2); c.steps = cv.take<double>(2); c.gg = cv.take<double>(2);
+  c.slope = cv.take<double>(2); c.e2 = cv.take<double>(2); c.g0 = cv.take<double>(2);
+  c.fnorm = cv.take<double>(2); c.res_prev = cv.take<double>(2); c.eta_prev = cv.take<double>(2);
+  c.ecur = cv.take<double>(2);
+  c.pit = cv.take<int32_t>(2); c.pst = cv.take<int32_t>(2); c.ctr = cv.take<int32_t>(8);
+  c.info = cv.take<skg_step_info>(2);
+  *bytes = cv.off;
+  return c;
+}
+
+// whether skg_be_step with these parameters can be recorded: no profiling, no Newton record,
+// the relative-residual stop rule, and a PCG form that takes its tolerance from the device
+template <typename R>
+static bool single_plan_eligible(const skg_tet_mesh* m, const skg_be_params* prm) {
+  if (prm->profile || prm->record || prm->stop_rule != 0) return false;
+  const bool two_level = single_two_level<R>(m, prm);
+  const bool grid_form = two_level && !m->coarse->inst_agg;
+  const int mode = resolve_pcg_mode<R>(prm->pcg_mode, m->n_verts, grid_form);
+  return mode == 1 || mode == 4 || mode == 5 || mode == 7;
+}
+
+template <typename R>
+static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be_state* st,
+                               void* wsbase, skg_batch_plan* plan) {
+  const int64_t n = m->n_verts, nd = 3 * n;
+  const bool mixed = sizeof(R) == 4;
+  Workspace w = carve_workspace(m, prm->precision, wsbase);
+  R* hbuf = mixed ? (R*)w.hbuf32 : (R*)w.hbuf64;
+  R* rec = mixed ? (R*)w.rec32 : (R*)w.rec64;
+  R* jinv = mixed ? (R*)w.jinv32 : (R*)w.jinv64;
+  PcgVecs<R> pv;
+  R** vv = mixed ? (R**)w.vec32 : (R**)w.vec64;
+  pv.x = vv[0]; pv.r = vv[1]; pv.z = vv[2]; pv.p = vv[3]; pv.q = vv[4]; pv.s = vv[5];
+  Bsr<R> A{n, m->bsr_rowptr, m->bsr_col, nullptr, jinv, rec};
+  A.keep = (int64_t)(kKeepFrac * (double)m->n_blocks);
+  int64_t ctl_bytes = 0;
+  carve_single_ctl(nullptr, &ctl_bytes);
+  SKG_CUDA(cudaMalloc(&plan->own, ctl_bytes));
+  SKG_CUDA(cudaMemset(plan->own, 0, ctl_bytes));
+  const BatchCtl c = carve_single_ctl(plan->own, &ctl_bytes);
+  plan->info = c.info;
+  plan->ctr = c.ctr;
+  plan->ni = 1;
+  const bool inst_form = m->coarse && m->coarse->inst_agg;
+  const bool two_level = single_two_level<R>(m, prm);
+  CoarseDev cdev{};
+  if (two_level) cdev = make_coarse_dev(m, w);
+  Contact contact;
+  SKG_TRY(make_contact(prm, st, &contact));
+  CtlParams cpar{};
+  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
+  cpar.ls_threshold = prm->ls_threshold; cpar.eps_r = mixed ? 5.96e-8 : 1.11e-16;
+  cpar.max_newton = prm->max_newton; cpar.ls_max_iter = prm->ls_max_iter; cpar.do_line_search = prm->do_line_search;
+  cpar.coarse_refresh = prm->coarse_refresh; cpar.two_level = two_level;
+  cpar.has_fext = 0;   // the host loop's stop rule: the relative residual alone
+
+  cudaStream_t s0 = plan->cap[0], s1 = plan->cap[1], s2 = plan->cap[2];
+  double inv_h2 = 0.0;
+  int launches = 0;
+  SKG_CUDA(cudaGraphCreate(&plan->graph, 0));
+  SKG_CUDA(cudaStreamBeginCaptureToGraph(s0, plan->graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+
+  // ---- before the loop: target, first gradient and energy
+  SKG_CUDA(cudaMemsetAsync(w.counter, 0, 16 * sizeof(unsigned), s0));
+  SKG_TRY(launch_target(prm, st, nd, w.ut, s0, &inv_h2));
+  launches++;
+  GradArgs ga{};
+  ga.n = n; ga.v2t_ptr = m->v2t_ptr; ga.v2t = m->v2t; ga.fbuf = w.fbuf; ga.mass = st->mass; ga.inv_h2 = inv_h2;
+  ga.u = st->u; ga.ut = w.ut; ga.f_ext = st->f_ext; ga.pinned = st->pinned; ga.g = w.g;
+  ga.partials = w.partials; ga.counter = w.counter; ga.out = c.gg;
+  ga.contact = contact;
+  EnergyArgs<R> ea{};
+  if constexpr (sizeof(R) == 4) ea.tet = make_tet_args32(m, st->u, w.uh, w.ul);
+  else ea.tet = make_tet_args64(m, st->u);
+  ea.n = n; ea.mass = st->mass; ea.inv_h2 = inv_h2; ea.ut = w.ut; ea.f_ext = st->f_ext; ea.pinned = st->pinned;
+  ea.contact = contact;
+  ea.partials = w.partials; ea.counter = w.counter; ea.out = c.e2;
+  const bool dff = mixed && (m->material == kMatSNH || m->material == kMatMMNH || m->material == kMatLE);
+  if (dff) {
+    SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s0));
+    launches++;
+  }
+  auto gradient = [&](cudaStream_t s) -> int {
+    if (dff) {
+      SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
+      SKG_TRY(launch_forces_df(make_tet_args64(m, st->u), m->dinv32, w.dinv_lo, w.uh, w.ul, w.fbuf, s));
+      launches++;
+    } else {
+      SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
+    }
+    SKG_TRY(launch_vertex_gradient(ga, s, dff));
+    launches += 2;
+    return SKG_OK;
+  };
+  auto energy = [&](const R* dx, const double* step_dev, cudaStream_t s) -> int {
+    ea.dx = dx;
+    ea.step = 0.0;
+    ea.step_dev = step_dev;
+    SKG_TRY(launch_energy<R>(ea, false, s));
+    launches++;
+    return SKG_OK;
+  };
+  auto split = [&](cudaStream_t s) -> int {
+    if (!mixed) return SKG_OK;
+    launches++;
+    return launch_split(st->u, n, w.uh, w.ul, s);
+  };
+  SKG_TRY(gradient(s0));
+  SKG_TRY(split(s0));
+  SKG_TRY(energy(nullptr, nullptr, s0));
+  k_bctl_begin<<<1, kCtlThreads, 0, s0>>>(c, cpar);
+  SKG_LAUNCHED();
+  cudaGraphConditionalHandle h_loop;
+  SKG_TRY(capture_handle(s0, &h_loop));
+  k_bctl_newton<<<1, kCtlThreads, 0, s0>>>(c, cpar, h_loop);
+  SKG_LAUNCHED();
+  launches += 2;
+  plan->l_pre = launches;
+
+  // ---- the Newton loop
+  cudaGraph_t body = nullptr;
+  SKG_TRY(add_conditional(s0, h_loop, cudaGraphCondTypeWhile, &body));
+  SKG_CUDA(cudaStreamBeginCaptureToGraph(s1, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  launches = 0;
+  if constexpr (sizeof(R) == 4) {
+    int hl = 1;
+    SKG_TRY(launch_tet_hessian<float>(make_tet_args32(m, st->u, w.uh, w.ul), 1, 1, (float*)hbuf, s1,
+                                      HessLate{w.hlate, w.hlate_n, &hl}));
+    launches += hl;
+  } else {
+    SKG_TRY(launch_tet_hessian<double>(make_tet_args64(m, st->u), 1, 1, (double*)hbuf, s1));
+    launches++;
+  }
+  AsmArgs<R> aa = make_asm_args<R>(m, hbuf, nullptr, jinv);
+  aa.rec = rec;
+  aa.mass = st->mass;
+  aa.inv_h2 = inv_h2;
+  aa.contact = contact;
+  aa.u = st->u;
+  aa.pinned = st->pinned;
+  aa.cmode = two_level && !inst_form ? cdev.mode : nullptr;
+  aa.colpack = two_level && inst_form ? cdev.colpack : nullptr;
+  SKG_TRY(launch_assemble<R>(aa, s1));
+  launches++;
+  if (two_level) {
+    cudaGraphConditionalHandle h_ref;
+    SKG_TRY(capture_handle(s1, &h_ref));
+    k_bctl_refresh<<<1, 1, 0, s1>>>(c, cpar, h_ref);
+    SKG_LAUNCHED();
+    launches++;
+    cudaGraph_t rbody = nullptr;
+    SKG_TRY(add_conditional(s1, h_ref, cudaGraphCondTypeIf, &rbody));
+    SKG_CUDA(cudaStreamBeginCaptureToGraph(s2, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    SKG_TRY(coarse_refresh<R>(A, cdev, w.scal, s2));
+    SKG_CUDA(cudaStreamEndCapture(s2, &rbody));
+    plan->l_refresh = 2;
+  }
+  // dx = -H^-1 g to the forcing term k_bctl_newton left in c.eta
+  PcgResult pr{};
+  SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, 0.0, prm->pcg_max_iter, prm->pcg_mode, w.partials, w.counter,
+                       w.scal, s1, &pr, prm->pcg_variant, two_level ? &cdev : nullptr, false, c.eta));
+  launches += pr.launches;
+  k_sctl_pcg<<<1, 1, 0, s1>>>(w.scal, c.pit, c.pst);
+  SKG_LAUNCHED();
+  k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s1>>>(w.g, pv.x, n, w.partials, w.counter, c.slope);
+  SKG_LAUNCHED();
+  cudaGraphConditionalHandle h_ls;
+  SKG_TRY(capture_handle(s1, &h_ls));
+  k_bctl_search<<<1, kCtlThreads, 0, s1>>>(c, cpar, h_ls);
+  SKG_LAUNCHED();
+  launches += 3;
+  {
+    cudaGraph_t lbody = nullptr;
+    SKG_TRY(add_conditional(s1, h_ls, cudaGraphCondTypeWhile, &lbody));
+    SKG_CUDA(cudaStreamBeginCaptureToGraph(s2, lbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    const int before = launches;
+    SKG_TRY(energy(pv.x, c.steps, s2));
+    k_bctl_trial<<<1, kCtlThreads, 0, s2>>>(c, cpar, h_ls);
+    SKG_LAUNCHED();
+    launches++;
+    plan->l_trial = launches - before;
+    launches = before;
+    SKG_CUDA(cudaStreamEndCapture(s2, &lbody));
+  }
+  k_bctl_searched<<<1, kCtlThreads, 0, s1>>>(c);
+  SKG_LAUNCHED();
+  k_apply_step_ctl<R><<<blocks_for(n), kBlock, 0, s1>>>(st->u, pv.x, c.steps, c.accept, n, st->pinned);
+  SKG_LAUNCHED();
+  launches += 2;
+  SKG_TRY(split(s1));
+  SKG_TRY(gradient(s1));
+  k_bctl_newton<<<1, kCtlThreads, 0, s1>>>(c, cpar, h_loop);
+  SKG_LAUNCHED();
+  launches++;
+  SKG_CUDA(cudaStreamEndCapture(s1, &body));
+  plan->l_iter = launches;
+
+  // ---- after the loop
+  k_bctl_final<<<1, kCtlThreads, 0, s0>>>(c, cpar);
+  SKG_LAUNCHED();
+  plan->l_post = 1;
+  SKG_CUDA(cudaStreamEndCapture(s0, &plan->graph));
+  SKG_CUDA(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
+  return SKG_OK;
+}
+
 // ends any capture still open on the plan's streams (after a failure part-way through)
 static void abandon_capture(skg_batch_plan* plan) {
   for (int k = 2; k >= 0; --k) {
@@ -2370,6 +2637,7 @@ static void release_plan(skg_batch_plan* plan) {
   if (plan->graph) cudaGraphDestroy(plan->graph);
   for (int k = 0; k < 3; ++k)
     if (plan->cap[k]) cudaStreamDestroy(plan->cap[k]);
+  if (plan->own) cudaFree(plan->own);
   delete plan;
 }
 
@@ -2480,6 +2748,59 @@ int skg_be_batch_plan_step(skg_batch_plan* plan, skg_step_info* infos_h, skg_ste
 }
 
 int skg_be_batch_plan_destroy(skg_batch_plan* plan) {
+  release_plan(plan);
+  return SKG_OK;
+}
+
+int skg_be_plan_eligible(const skg_tet_mesh* mesh, const skg_be_params* params) {
+  if (!params || check_mesh(mesh, params->precision) != SKG_OK) return 0;
+  return (params->precision == SKG_MIXED ? single_plan_eligible<float>(mesh, params)
+                                         : single_plan_eligible<double>(mesh, params)) ? 1 : 0;
+}
+
+int skg_be_plan_create(const skg_tet_mesh* mesh, const skg_be_params* params, const skg_be_state* state,
+                       void* workspace, skg_batch_plan** plan_h) {
+  if (!plan_h) return fail(SKG_ERR_ARG, "be plan: null plan pointer");
+  *plan_h = nullptr;
+  if (!params || !state || !workspace) return fail(SKG_ERR_ARG, "be plan: null argument");
+  SKG_TRY(check_mesh(mesh, params->precision));
+  if (!(params->dt > 0.0)) return fail(SKG_ERR_ARG, "be plan: dt must be positive");
+  if (!state->u || !state->u_curr || !state->u_prev || !state->mass) return fail(SKG_ERR_ARG, "be plan: null state");
+  SKG_TRY(check_integrator(params, state));
+  if (params->do_line_search && !(params->ls_alpha > 0.0 && params->ls_alpha <= 0.5))
+    return fail(SKG_ERR_ARG, "line search alpha must lie in (0, 0.5]");
+  if (params->do_line_search && !(params->ls_beta > 0.0 && params->ls_beta < 1.0))
+    return fail(SKG_ERR_ARG, "line search beta must lie in (0, 1)");
+  if (!skg_be_plan_eligible(mesh, params))
+    return fail(SKG_ERR_ARG, "be plan: these parameters need the host loop (profiling, a Newton record, "
+                             "stop_rule 1 or a PCG form without a device tolerance)");
+  skg_batch_plan* plan = new skg_batch_plan();
+  for (int k = 0; k < 3; ++k) {
+    if (cudaStreamCreateWithFlags(&plan->cap[k], cudaStreamNonBlocking) != cudaSuccess) {
+      release_plan(plan);
+      return fail(SKG_ERR_CUDA, "be plan: stream creation failed");
+    }
+  }
+  const int r = params->precision == SKG_MIXED ? capture_single_step<float>(mesh, params, state, workspace, plan)
+                                               : capture_single_step<double>(mesh, params, state, workspace, plan);
+  if (r != SKG_OK) {
+    abandon_capture(plan);
+    release_plan(plan);
+    return r;
+  }
+  *plan_h = plan;
+  return SKG_OK;
+}
+
+int skg_be_plan_step(skg_batch_plan* plan, skg_step_info* info_h, void* stream) {
+  if (!plan || !plan->exec || !info_h || plan->ni != 1) return fail(SKG_ERR_ARG, "be plan step: bad argument");
+  skg_step_info total;
+  SKG_TRY(skg_be_batch_plan_step(plan, info_h, &total, stream));
+  info_h->launches = total.launches;
+  return SKG_OK;
+}
+
+int skg_be_plan_destroy(skg_batch_plan* plan) {
   release_plan(plan);
   return SKG_OK;
 }

@@ -93,13 +93,17 @@ class BESolver:
         'newton' (at every Newton iteration) or an int k (default 4: at the first Newton iteration
         of every k-th step; the steps between reuse it: the preconditioner stays SPD, only less
         fresh, and on the 786,432-tet beam the PCG iteration count did not change)
+    device_loop : run each step as a recorded CUDA graph with the Newton loop and line search decided
+        on the device (``skg_be_plan_*``: one host synchronisation per step instead of two per Newton
+        iteration, bitwise the same steps) when the parameters allow it (the grid PCG forms; profiled
+        steps, Newton records and simkit's stop rule take the host loop)
     """
 
     def __init__(self, X, T, mu, lam, rho=1000.0, gravity=(0.0, -9.8, 0.0), pinned=(), dt=1.0 / 60.0,
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
                  material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None):
+                 coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None, device_loop=True):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.check_orientation()
@@ -161,6 +165,10 @@ class BESolver:
         self.set_contact_planes(contact_planes, contact_mass_weighted)
         self.steps = 0
         self._host = None
+        self.device_loop = bool(device_loop)
+        self._plans = {}          # device-loop graphs, one per rotation of the state buffers and refresh flag
+        self._plan_key = None     # parameters, contact planes and mesh arrays the plans were recorded with
+        self._eligible = None     # (key, whether those parameters can be recorded)
 
     def _coarse_n_agg(self) -> int:
         return int(self.mesh._coarse_c.n_agg) if getattr(self.mesh, "_coarse_c", None) is not None else 0
@@ -182,30 +190,109 @@ class BESolver:
     def from_spec(cls, spec, **kw):
         return cls(spec.X, spec.T, spec.mu, spec.lam, rho=spec.rho, gravity=spec.gravity, pinned=spec.pinned, **kw)
 
-    def step(self, stream=None) -> StepInfo:
+    def _state(self):
         bdf2 = self.integrator == "bdf2"
-        st = BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
-                      mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
-                      u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
-                      u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
+        return BEStateC(u=self.u_next.data_ptr(), u_curr=self.u_curr.data_ptr(), u_prev=self.u_prev.data_ptr(),
+                        mass=self.mass.data_ptr(), f_ext=self.f_ext.data_ptr(), pinned=self.pinned.data_ptr(),
+                        u_prev2=self.u_prev2.data_ptr() if bdf2 else None,
+                        u_prev3=self.u_prev3.data_ptr() if bdf2 else None, x_rest=self.mesh.X.data_ptr())
+
+    def _rotate(self):
+        """History after a step: [prev3 <- prev2 <-] prev <- curr <- next (next becomes scratch)."""
+        if self.integrator == "bdf2":
+            self.u_prev3, self.u_prev2, self.u_prev, self.u_curr, self.u_next = (
+                self.u_prev2, self.u_prev, self.u_curr, self.u_next, self.u_prev3)
+        else:
+            self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+
+    def prepare_plans(self) -> int:
+        """Record now the device-loop graphs of every rotation of the state buffers and both coarse
+        refresh decisions, so that no later step records one; returns how many exist (0 when the
+        parameters take the host loop)."""
+        if not self.device_loop:
+            return 0
+        rotations = 5 if self.integrator == "bdf2" else 3
+        flags = (0, -1) if isinstance(self.coarse_refresh, int) else (self.params.coarse_refresh,)
+        keep = self.params.coarse_refresh
+        try:
+            for _ in range(rotations):
+                for f in flags:
+                    self.params.coarse_refresh = f
+                    if self._plan(self._state()) is None:
+                        return 0
+                self._rotate()
+        finally:
+            self.params.coarse_refresh = keep
+        return len(self._plans)
+
+    def step(self, stream=None) -> StepInfo:
+        st = self._state()
         info = StepInfoC()
         if isinstance(self.coarse_refresh, int):
             rebuild = self._coarse_age is None or self._coarse_age + 1 >= self.coarse_refresh
             self.params.coarse_refresh = 0 if rebuild else -1
             self._coarse_age = 0 if rebuild else self._coarse_age + 1
-        check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
-                                      ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),
-                                      _stream_ptr(stream)))
-        # rotate history: [prev3 <- prev2 <-] prev <- curr <- next
-        if bdf2:
-            self.u_prev3, self.u_prev2, self.u_prev, self.u_curr, self.u_next = (
-                self.u_prev2, self.u_prev, self.u_curr, self.u_next, self.u_prev3)
+        plan = self._plan(st) if self.device_loop else None
+        if plan is not None:
+            check(_lib.load().skg_be_plan_step(plan, ctypes.byref(info), _stream_ptr(stream)))
         else:
-            self.u_prev, self.u_curr, self.u_next = self.u_curr, self.u_next, self.u_prev
+            check(_lib.load().skg_be_step(ctypes.byref(self.mesh.c), ctypes.byref(self.params), ctypes.byref(st),
+                                          ctypes.c_void_p(self.workspace.data_ptr()), ctypes.byref(info),
+                                          _stream_ptr(stream)))
+        self._rotate()
         self.steps += 1
         return StepInfo(info.newton_iters, info.pcg_iters, info.ls_trials, info.status, info.residual0,
                         info.residual, info.min_alpha, info.energy, info.launches, info.t_hessian_ms,
                         info.t_assemble_ms, info.t_pcg_ms, info.t_gradient_ms, info.t_energy_ms)
+
+    def _params_key(self):
+        """What the device-loop graphs depend on besides the state buffers: the parameters (less the
+        per-step refresh decision: graphs for both decisions are kept), the contact planes and the
+        mesh's device arrays."""
+        refresh = self.params.coarse_refresh
+        self.params.coarse_refresh = 0
+        raw = ctypes.string_at(ctypes.addressof(self.params), ctypes.sizeof(self.params))
+        self.params.coarse_refresh = refresh
+        planes = ctypes.string_at(ctypes.addressof(self._planes), ctypes.sizeof(self._planes)) if self._planes else b""
+        mesh = ctypes.string_at(ctypes.addressof(self.mesh.c), ctypes.sizeof(self.mesh.c))
+        coarse = getattr(self.mesh, "_coarse_c", None)
+        cbytes = ctypes.string_at(ctypes.addressof(coarse), ctypes.sizeof(coarse)) if coarse is not None else b""
+        return raw + planes + mesh + cbytes
+
+    def _plan(self, st):
+        """The device-loop graph for this state binding and refresh decision (recorded on first use, all
+        of them again after a change of the parameters, planes or mesh arrays), or None when the
+        parameters need the host loop (profiling, a Newton record, simkit's stop rule, the cluster PCG
+        of small meshes)."""
+        key = self._params_key()
+        if self._eligible is None or self._eligible[0] != key:
+            ok = bool(_lib.load().skg_be_plan_eligible(ctypes.byref(self.mesh.c), ctypes.byref(self.params)))
+            self._eligible = (key, ok)
+        if not self._eligible[1]:
+            return None
+        if key != self._plan_key:
+            self.release_plans()
+            self._plan_key = key
+        bind = (st.u, st.u_curr, st.u_prev, st.u_prev2, st.u_prev3, self.params.coarse_refresh)
+        plan = self._plans.get(bind)
+        if plan is None:
+            h = ctypes.c_void_p()
+            check(_lib.load().skg_be_plan_create(ctypes.byref(self.mesh.c), ctypes.byref(self.params),
+                                                 ctypes.byref(st), ctypes.c_void_p(self.workspace.data_ptr()),
+                                                 ctypes.byref(h)))
+            plan = self._plans[bind] = h
+        return plan
+
+    def release_plans(self):
+        for h in getattr(self, "_plans", {}).values():
+            _lib.load().skg_be_plan_destroy(h)
+        self._plans = {}
+
+    def __del__(self):
+        try:
+            self.release_plans()
+        except Exception:
+            pass
 
     def step_host(self, x_curr: np.ndarray, x_prev: np.ndarray, out: np.ndarray = None, stream=None,
                   x_prev2: np.ndarray = None, x_prev3: np.ndarray = None):
