@@ -4,7 +4,8 @@
 ``simkit/integrators/backward_euler.py:27-91``) with the stable neo-Hookean
 closures, gravity, pinned DOFs held at rest, and Newton iterated until the
 relative residual ``||g(x)|| / ||g(x_tilde)||`` falls below ``tol`` - all on
-the GPU through ``skg_be_step``.  Positions stay in HBM between steps.
+the GPU through ``skg_be_step`` (or its recorded graph, ``skg_be_plan_*``).  Positions
+stay in HBM between steps.
 """
 
 from __future__ import annotations
