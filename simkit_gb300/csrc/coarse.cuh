@@ -370,6 +370,11 @@ template <typename R> struct ZCoarse {
   }
 };
 
+#ifndef SKG_ROW_LOADS
+#define SKG_ROW_LOADS 12
+#endif
+constexpr int kRowLoads = SKG_ROW_LOADS;
+
 // e = A_c^-1 (P^T r) for the rows of this CTA's warps (one row per warp, rows dealt to the blocks
 // in turn so that every block gets nc / gridDim of them), pc += (P^T r) . e over those rows, from
 // P^T r staged in shared memory (rcf: np floats)
@@ -383,10 +388,20 @@ __device__ __forceinline__ void coarse_rows_product(const CoarseDev& c, const fl
     // it stays in L2 beside the kept records and the vectors
     const float4* Mr = reinterpret_cast<const float4*>(c.M + (int64_t)row * c.np);
     float s = 0.f;
-#pragma unroll 5
-    for (int j = lane; j < (c.np >> 2); j += 32) {
-      const float4 m = __ldcg(Mr + j), x = r4[j];
-      s = fmaf(m.x, x.x, fmaf(m.y, x.y, fmaf(m.z, x.z, fmaf(m.w, x.w, s))));
+    // kRowLoads loads of the row in flight per lane before the first is used (the row is ~23 float4
+    // per lane at 2,850 coarse unknowns: two rounds of L2 latency), summed in the order of j
+    const int n4 = c.np >> 2;
+    for (int j0 = lane; j0 < n4; j0 += 32 * kRowLoads) {
+      float4 m[kRowLoads];
+#pragma unroll
+      for (int u = 0; u < kRowLoads; ++u)
+        m[u] = j0 + 32 * u < n4 ? __ldcg(Mr + j0 + 32 * u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < kRowLoads; ++u)
+        if (j0 + 32 * u < n4) {
+          const float4 x = r4[j0 + 32 * u];
+          s = fmaf(m[u].x, x.x, fmaf(m[u].y, x.y, fmaf(m[u].z, x.z, fmaf(m[u].w, x.w, s))));
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
