@@ -358,6 +358,11 @@ typedef struct skg_be_params {
                                (solvers/newton.py:43-75): at least one iteration, stop once
                                ||alpha dx|| < tol, at most max_newton iterations, no status */
   skg_newton_record* record; /* host pointer, or NULL: skg_be_step fills it per Newton iteration */
+  double ew_gamma;          /* pcg_rtol < 0: after the first Newton iteration the forcing term is
+                               Eisenstat-Walker choice 2, ew_gamma (r_k / r_{k-1})^ew_alpha, raised to
+                               ew_gamma eta_{k-1}^ew_alpha when that is above 0.1; 0 = 0.9 */
+  double ew_alpha;          /* its exponent in [1, 2] (quarter steps are evaluated exactly alike on
+                               the host and the device); 0 = 2 */
 } skg_be_params;
 
 typedef struct skg_be_state {

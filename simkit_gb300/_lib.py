@@ -77,6 +77,7 @@ class BEParamsC(ctypes.Structure):
         ("pcg_variant", c_i32), ("batch_min_cluster", c_i32), ("batch_vec_kb", c_i32), ("integrator", c_i32),
         ("n_planes", c_i32), ("contact_mass_weighted", c_i32), ("planes", ctypes.POINTER(ContactPlaneC)),
         ("coarse_refresh", c_i32), ("stop_rule", c_i32), ("record", ctypes.POINTER(NewtonRecordC)),
+        ("ew_gamma", c_dbl), ("ew_alpha", c_dbl),
     ]
 
 

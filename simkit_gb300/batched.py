@@ -44,7 +44,7 @@ class BatchedBESolver:
     def __init__(self, specs, dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1,
                  pcg_max_iter=4000, do_line_search=True, ls_threshold=None, profile=False, device="cuda",
                  integrator="be", material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh="step", graph=True):
+                 coarse="auto", coarse_refresh="step", graph=True, ew_gamma=0.9, ew_alpha=1.25):
         _lib.load()
         self.graph = graph
         self.n_inst = len(specs)
@@ -82,6 +82,7 @@ class BatchedBESolver:
         if not (coarse_refresh in ("step", "newton") or (isinstance(coarse_refresh, int) and coarse_refresh >= 1)):
             raise ValueError("coarse_refresh must be 'step', 'newton' or an int >= 1")
         self._coarse_refresh = coarse_refresh
+        self._ew = (ew_gamma, ew_alpha)
         self._setup(mesh, np.array(rows, np.int32), np.array(tets, np.int32), up(np.concatenate(masses)),
                     up(np.concatenate(fexts)), up(np.concatenate(pins)), dt, tol, max_newton, precision, pcg_rtol,
                     pcg_max_iter, do_line_search, ls_threshold, profile, integrator)
@@ -89,7 +90,7 @@ class BatchedBESolver:
     @classmethod
     def from_device(cls, mesh, inst_rows, inst_tets, mass, f_ext, pinned, dt=1.0 / 60.0, tol=1e-6, max_newton=20,
                     precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, do_line_search=True, ls_threshold=None,
-                    profile=False, integrator="be", graph=True, coarse_refresh="step"):
+                    profile=False, integrator="be", graph=True, coarse_refresh="step", ew_gamma=0.9, ew_alpha=1.25):
         """A batch over an already concatenated device mesh: ``inst_rows`` / ``inst_tets`` (host
         int arrays, n_inst + 1) delimit the instances; mass (n), f_ext (3n) f64 and pinned (3n) u8
         are device tensors."""
@@ -98,6 +99,7 @@ class BatchedBESolver:
         if not (coarse_refresh in ("step", "newton") or (isinstance(coarse_refresh, int) and coarse_refresh >= 1)):
             raise ValueError("coarse_refresh must be 'step', 'newton' or an int >= 1")
         self._coarse_refresh = coarse_refresh
+        self._ew = (ew_gamma, ew_alpha)
         self.n_inst = len(inst_rows) - 1
         if self.n_inst <= 0:
             raise ValueError("empty batch")
@@ -145,7 +147,8 @@ class BatchedBESolver:
             ls_max_iter=100, pcg_mode=2,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
             profile=int(profile), integrator=INTEGRATORS[integrator],
-            coarse_refresh=int(getattr(self, "_coarse_refresh", "step") == "newton"))
+            coarse_refresh=int(getattr(self, "_coarse_refresh", "step") == "newton"),
+            ew_gamma=self._ew[0], ew_alpha=self._ew[1])
         self._infos = (StepInfoC * self.n_inst)()
         self._coarse_age = None   # steps since the coarse inverses were built (integer refresh period)
         self._plans = {}          # device-loop graphs, one per rotation of the state buffers (and per

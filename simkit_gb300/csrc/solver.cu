@@ -1059,6 +1059,30 @@ static int read_scalars(const double* dev, double* host, int count, cudaStream_t
   return SKG_OK;
 }
 
+// Eisenstat-Walker choice 2 after the first iteration: eta = gamma (r_k / r_{k-1})^alpha, raised to
+// the safeguard gamma eta_{k-1}^alpha when that is above 0.1.  Exponents in quarter steps over [1, 2]
+// are evaluated by square roots and products (correctly rounded on the host and the device alike, so
+// the host loops and the control kernels take the same decisions); others by pow.
+__host__ __device__ inline double ew_pow(double q, double a) {
+  if (a == 2.0) return q * q;
+  if (a == 1.0) return q;
+  const double r2 = sqrt(q), r4 = sqrt(r2);
+  if (a == 1.5) return q * r2;
+  if (a == 1.25) return q * r4;
+  if (a == 1.75) return q * r2 * r4;
+  return pow(q, a);
+}
+
+__host__ __device__ inline double ew_forcing(double q, double eta_prev, double gamma, double alpha) {
+  double e = gamma * ew_pow(q, alpha);
+  const double safe = gamma * ew_pow(eta_prev, alpha);
+  if (safe > 0.1 && safe > e) e = safe;
+  return e;
+}
+
+static inline double ew_gamma(const skg_be_params* p) { return p->ew_gamma > 0.0 ? p->ew_gamma : 0.9; }
+static inline double ew_alpha(const skg_be_params* p) { return p->ew_alpha > 0.0 ? p->ew_alpha : 2.0; }
+
 // whether a single-mesh step runs the two-level PCG: the whole-mesh form with the grid kernel (mode 7,
 // or mode 3 above the cluster size), the per-instance form with the cluster kernel (mode 2, or mode 3 up
 // to the cluster size)
@@ -1198,10 +1222,7 @@ static int be_step(const skg_tet_mesh* m, const skg_be_params* prm, const skg_be
       if (it == 0) {
         eta = eta_max * (res < 1.0 ? res : 1.0);   // 1 from x_tilde; a closer start gets a tighter first solve
       } else {
-        const double q = res / res_prev;
-        eta = 0.9 * q * q;
-        const double safe = 0.9 * eta_prev * eta_prev;
-        if (safe > 0.1 && safe > eta) eta = safe;
+        eta = ew_forcing(res / res_prev, eta_prev, ew_gamma(prm), ew_alpha(prm));
       }
       const double reach = 0.25 * prm->tol / res;
       if (eta < reach) eta = reach;
@@ -1748,10 +1769,7 @@ static int be_step_batched(const skg_tet_mesh* m, const skg_batch* bt, const skg
         if (it == 0) {
           e = emax * (res < 1.0 ? res : 1.0);   // a start closer than x_tilde gets a tighter first solve
         } else {
-          const double q = res / res_prev[i];
-          e = 0.9 * q * q;
-          const double safe = 0.9 * eta_prev[i] * eta_prev[i];
-          if (safe > 0.1 && safe > e) e = safe;
+          e = ew_forcing(res / res_prev[i], eta_prev[i], ew_gamma(prm), ew_alpha(prm));
         }
         const double reach = 0.25 * prm->tol / res;
         if (e < reach) e = reach;
@@ -1901,7 +1919,7 @@ constexpr int kCtlThreads = 512;
 enum { kCtrIter = 0, kCtrTrial = 1, kCtrTrials = 2, kCtrRefresh = 3 };
 
 struct CtlParams {
-  double tol, pcg_rtol, ls_alpha, ls_beta, ls_threshold, eps_r;
+  double tol, pcg_rtol, ls_alpha, ls_beta, ls_threshold, eps_r, ew_gamma, ew_alpha;
   int max_newton, ls_max_iter, do_line_search, coarse_refresh, has_fext, two_level;
 };
 
@@ -1991,10 +2009,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_bctl_newton(BatchCtl c, CtlPara
       if (it == 0) {
         e = emax * (res < 1.0 ? res : 1.0);   // as the host loop: the first forcing scales with the start's residual
       } else {
-        const double q = res / c.res_prev[i];
-        e = 0.9 * q * q;
-        const double safe = 0.9 * c.eta_prev[i] * c.eta_prev[i];
-        if (safe > 0.1 && safe > e) e = safe;
+        e = ew_forcing(res / c.res_prev[i], c.eta_prev[i], p.ew_gamma, p.ew_alpha);
       }
       const double reach = 0.25 * p.tol / res;
       if (e < reach) e = reach;
@@ -2203,7 +2218,7 @@ static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const 
   Contact contact;
   SKG_TRY(make_contact(prm, st, &contact));
   CtlParams cpar{};
-  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
+  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ew_gamma = ew_gamma(prm); cpar.ew_alpha = ew_alpha(prm); cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
   cpar.ls_threshold = prm->ls_threshold; cpar.eps_r = mixed ? 5.96e-8 : 1.11e-16;
   cpar.max_newton = prm->max_newton; cpar.ls_max_iter = prm->ls_max_iter; cpar.do_line_search = prm->do_line_search;
   cpar.coarse_refresh = prm->coarse_refresh; cpar.has_fext = st->f_ext != nullptr; cpar.two_level = two_level;
@@ -2463,7 +2478,7 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
   Contact contact;
   SKG_TRY(make_contact(prm, st, &contact));
   CtlParams cpar{};
-  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
+  cpar.tol = prm->tol; cpar.pcg_rtol = prm->pcg_rtol; cpar.ew_gamma = ew_gamma(prm); cpar.ew_alpha = ew_alpha(prm); cpar.ls_alpha = prm->ls_alpha; cpar.ls_beta = prm->ls_beta;
   cpar.ls_threshold = prm->ls_threshold; cpar.eps_r = mixed ? 5.96e-8 : 1.11e-16;
   cpar.max_newton = prm->max_newton; cpar.ls_max_iter = prm->ls_max_iter; cpar.do_line_search = prm->do_line_search;
   cpar.coarse_refresh = prm->coarse_refresh; cpar.two_level = two_level;

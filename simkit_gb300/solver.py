@@ -94,6 +94,12 @@ class BESolver:
         'newton' (at every Newton iteration) or an int k (default 4: at the first Newton iteration
         of every k-th step; the steps between reuse it: the preconditioner stays SPD, only less
         fresh, and on the 786,432-tet beam the PCG iteration count did not change)
+    ew_gamma, ew_alpha : Eisenstat-Walker choice 2 (with pcg_rtol < 0), after the first Newton
+        iteration eta = ew_gamma (r_k / r_{k-1})^ew_alpha, safeguarded; exponents in quarter steps
+        over [1, 2] are evaluated alike on the host and the device.  On the 786,432-tet beam the
+        Newton residual falls about as far as each linear solve's tolerance, so the exponent sets the
+        trade of Newton iterations against PCG iterations: 1.25 (6.15 Newton, 164 PCG iterations
+        per step) ran 80.6 steps/s, 2 (5.45, 207) 71.5
     device_loop : run each step as a recorded CUDA graph with the Newton loop and line search decided
         on the device (``skg_be_plan_*``: one host synchronisation per step instead of two per Newton
         iteration, bitwise the same steps) when the parameters allow it (the grid PCG forms; profiled
@@ -104,7 +110,8 @@ class BESolver:
                  tol=1e-6, max_newton=20, precision="mixed", pcg_rtol=-0.1, pcg_max_iter=4000, pcg_mode=3,
                  do_line_search=True, ls_threshold=None, profile=False, device="cuda", integrator="be",
                  material="stable-neo-hookean", contact_planes=None, contact_mass_weighted=True,
-                 coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None, device_loop=True):
+                 coarse="auto", coarse_refresh=4, coarse_form="auto", mass=None, f_ext=None, device_loop=True,
+                 ew_gamma=0.9, ew_alpha=1.25):
         _lib.load()
         self.mesh = TetMesh(X, T, mu, lam, device=device)
         self.mesh.check_orientation()
@@ -162,7 +169,7 @@ class BESolver:
             ls_max_iter=100, pcg_mode=pcg_mode,
             ls_threshold=(-1.0 if precision == "mixed" else 1e-12) if ls_threshold is None else ls_threshold,
             profile=int(profile), integrator=INTEGRATORS[integrator],
-            coarse_refresh=int(coarse_refresh == "newton"))
+            coarse_refresh=int(coarse_refresh == "newton"), ew_gamma=ew_gamma, ew_alpha=ew_alpha)
         self.set_contact_planes(contact_planes, contact_mass_weighted)
         self.steps = 0
         self._host = None

@@ -133,12 +133,14 @@ def test_degenerate_and_inverted_rest_tets_are_refused():
         BESolver(spec.X, Ti, spec.mu, spec.lam, pinned=spec.pinned)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-4)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 2e-4)])
 def test_step_recovers_from_inverted_elements_like_the_oracle(precision, tol):
     """Two tets inverted in the initial state (a tip vertex pushed through its neighbours on the host):
     one step agrees with the FP64 oracle's step from the same state (which needs 7 Newton iterations).
-    Measured on a GB300: 1.3e-14 (FP64) and 2.6e-5 (mixed: FP32 Hessians, the same 1e-6 relative
-    residual stop) of the displacement, which here is 1.5 cells."""
+    Measured on a GB300: 1.3e-14 (FP64) and, in mixed precision (FP32 Hessians, the same 1e-6 relative
+    residual stop), 2.6e-5 with the Eisenstat-Walker exponent 2 and 1.04e-4 with 1.25 of the
+    displacement, which here is 1.5 cells: two solutions that each meet the stop rule on this
+    ill-conditioned state differ by that much."""
     from oracle import rollout
     from simkit_gb300.beams import make_beam
     from simkit_gb300.solver import BESolver
