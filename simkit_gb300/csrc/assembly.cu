@@ -461,13 +461,11 @@ __global__ void __launch_bounds__(128) k_tet_forces(TetArgs<double> a, int disp,
 // displacement form): the f_a of k_tet_forces evaluated in double-float
 // arithmetic (dfloat.cuh) from the FP32 hi/lo splits of u (uh, ul) and of Dinv
 // (dinv_hi = dinv32, dinv_lo), so that only the three material loads touch the
-// FP64 units.  Written as (hi, lo) pairs for k_vertex_gradient<true>.
-__global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const float* __restrict__ dinv_hi,
-                                                       const float* __restrict__ dinv_lo,
-                                                       const float* __restrict__ uh, const float* __restrict__ ul,
-                                                       float2* __restrict__ fbuf) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= a.t) return;
+// FP64 units.  Written as (hi, lo) pairs for k_vertex_gradient<true>.  This function: the 12
+// components of tet e (vertex-major: f[3 b + i]) into f.
+__device__ __forceinline__ void tet_forces_df(const TetArgs<double>& a, const float* __restrict__ dinv_hi,
+                                              const float* __restrict__ dinv_lo, const float* __restrict__ uh,
+                                              const float* __restrict__ ul, int64_t e, float2* f) {
   const int4 v = __ldg(a.tets + e);
   DF du[9], D[9], G[9], P[9], gN[12];
   {
@@ -493,7 +491,6 @@ __global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const 
   else
     snh_pk1_disp<DF>(G, mu, lam, P);
   shape_grads(D, gN);
-  float2* f = fbuf + 12 * e;
 #pragma unroll
   for (int b = 0; b < 4; ++b)
 #pragma unroll
@@ -501,6 +498,23 @@ __global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const 
       const DF s = vol * (P[3 * i] * gN[3 * b] + P[3 * i + 1] * gN[3 * b + 1] + P[3 * i + 2] * gN[3 * b + 2]);
       f[3 * b + i] = make_float2(s.hi, s.lo);
     }
+}
+
+__global__ void __launch_bounds__(128) k_tet_forces_df(TetArgs<double> a, const float* __restrict__ dinv_hi,
+                                                       const float* __restrict__ dinv_lo,
+                                                       const float* __restrict__ uh, const float* __restrict__ ul,
+                                                       float2* __restrict__ fbuf) {
+  // the block's 128 tets' forces are staged here and written out as one contiguous span (per-thread
+  // stores of a tet's 12 pairs at a 96-byte stride made every warp store touch 32 sectors)
+  __shared__ __align__(16) float2 stage[128 * 12];
+  const int64_t e0 = blockIdx.x * (int64_t)blockDim.x;
+  const int64_t e = e0 + threadIdx.x;
+  if (e < a.t) tet_forces_df(a, dinv_hi, dinv_lo, uh, ul, e, stage + 12 * threadIdx.x);
+  __syncthreads();
+  const int nt = (int)min((int64_t)blockDim.x, a.t - e0);
+  float4* dst = reinterpret_cast<float4*>(fbuf + 12 * e0);
+  const float4* src = reinterpret_cast<const float4*>(stage);
+  for (int k = threadIdx.x; k < 6 * nt; k += blockDim.x) dst[k] = src[k];
 }
 
 // low parts of Dinv for the double-float forces: dinv = dinv32 + dinv_lo to ~48 bits
@@ -522,7 +536,9 @@ __global__ void __launch_bounds__(kBlock) k_vertex_gradient(GradArgs a) {
     double acc[3] = {0.0, 0.0, 0.0};
     if constexpr (DFB) {
       DF s[3] = {DF(0.f, 0.f), DF(0.f, 0.f), DF(0.f, 0.f)};
-      for (int k = __ldg(a.v2t_ptr + v); k < __ldg(a.v2t_ptr + v + 1); ++k) {
+      const int kb = __ldg(a.v2t_ptr + v), ke = __ldg(a.v2t_ptr + v + 1);
+#pragma unroll 4
+      for (int k = kb; k < ke; ++k) {
         const int code = __ldg(a.v2t + k);
         const float2* f = reinterpret_cast<const float2*>(a.fbuf) + 12 * (int64_t)(code >> 2) + 3 * (code & 3);
 #pragma unroll
