@@ -70,3 +70,31 @@ def test_host_loop_where_the_device_loop_does_not_apply():
     small = BESolver.from_spec(make_beam(8, 3, 3), device_loop=True)
     assert lib.skg_be_plan_eligible(small.mesh.c, small.params) == 0
     assert small.step().converged and len(small._plans) == 0
+
+
+def test_device_loop_bdf2_with_contact_equals_host_loop():
+    """BDF2 (five displacement levels rotate, five graphs) with a floor contact plane."""
+    spec = _spec()
+    floor = [(1.0e4, (0.0, -0.01, 0.0), (0.0, 1.0, 0.0))]
+    g, h = _pair(spec, integrator="bdf2", contact_planes=floor, coarse_refresh=3)
+    for _ in range(6):
+        ig, ih = g.step(), h.step()
+        assert ig.converged and ih.converged, (ig, ih)
+        _same(ig, ih)
+        assert np.array_equal(g.u_curr.cpu().numpy(), h.u_curr.cpu().numpy())
+    assert len(g._plans) >= 5
+
+
+def test_prepare_plans_records_every_rotation_up_front():
+    """Three state rotations x (rebuild, reuse) recorded before the first step; stepping adds none."""
+    spec = _spec()
+    g, h = _pair(spec, coarse_refresh=2)
+    assert g.prepare_plans() == 6
+    for _ in range(4):
+        ig, ih = g.step(), h.step()
+        _same(ig, ih)
+    assert len(g._plans) == 6
+    assert np.array_equal(g.u_curr.cpu().numpy(), h.u_curr.cpu().numpy())
+    g.params.tol = 1e-7            # a parameter change re-records on the next step
+    g.step()
+    assert len(g._plans) == 1
