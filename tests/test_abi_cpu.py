@@ -55,6 +55,50 @@ def test_error_path_without_gpu(libpath):
     assert lib.skg_psd_project(None, None, 1, 13, 0, None) == _lib.SKG_ERR_ARG
 
 
+def test_device_loop_eligibility_without_gpu(libpath):
+    """skg_be_plan_eligible is host logic over the mesh and parameter records (no device access):
+    the grid PCG forms qualify; profiling, a Newton record, simkit's stop rule, mode 0 and the cluster
+    form of meshes up to 24,576 block rows take the host loop; an invalid mesh is not eligible."""
+    from simkit_gb300 import _lib
+    lib = _lib.load()
+    dummy = 256   # non-null placeholders: only sizes, flags and null checks are read
+
+    def mesh(n, coarse=None):
+        m = _lib.TetMeshC(n_verts=n, n_tets=6 * n, n_blocks=15 * n, material=0)
+        for f in ("tets", "dinv", "dinv32", "vol", "mu", "lam", "mat32", "bsr_rowptr", "bsr_col", "bsr_diag",
+                  "bsr_row", "hc_ptr", "hc_src", "v2t_ptr", "v2t"):
+            setattr(m, f, dummy)
+        if coarse is not None:
+            m.coarse = ctypes.pointer(coarse)
+        return m
+
+    grid_coarse = _lib.CoarseC(n_agg=475, n_cblocks=1000, mode=dummy, cb_ptr=dummy, cb_slot=dummy, cb_rc=dummy)
+    p = _lib.BEParamsC(dt=1.0 / 60.0, tol=1e-6, max_newton=20, precision=_lib.SKG_MIXED, pcg_rtol=-0.25,
+                       pcg_max_iter=4000, do_line_search=1, ls_alpha=0.01, ls_beta=0.5, ls_max_iter=100,
+                       pcg_mode=3, ls_threshold=-1.0)
+    big_two_level, big_one_level, small = mesh(140481, grid_coarse), mesh(140481), mesh(2000)
+    assert lib.skg_be_plan_eligible(big_two_level, p) == 1     # mode 3 -> two-level grid form
+    assert lib.skg_be_plan_eligible(big_one_level, p) == 1     # mode 3 -> one-level grid form
+    assert lib.skg_be_plan_eligible(small, p) == 0             # mode 3 -> one thread-block cluster
+    p.pcg_mode = 5
+    assert lib.skg_be_plan_eligible(small, p) == 1
+    p.pcg_mode = 0
+    assert lib.skg_be_plan_eligible(big_one_level, p) == 0     # kernel per phase: host-read stops
+    p.pcg_mode = 3
+    p.profile = 1
+    assert lib.skg_be_plan_eligible(big_two_level, p) == 0
+    p.profile = 0
+    p.stop_rule = 1
+    assert lib.skg_be_plan_eligible(big_two_level, p) == 0
+    p.stop_rule = 0
+    rec = _lib.NewtonRecordC()
+    p.record = ctypes.pointer(rec)
+    assert lib.skg_be_plan_eligible(big_two_level, p) == 0
+    p.record = None
+    assert lib.skg_be_plan_eligible(mesh(0), p) == 0            # sizes the mesh check refuses
+    assert lib.skg_be_plan_create(big_two_level, p, None, None, None) == _lib.SKG_ERR_ARG
+
+
 def test_pattern_builder_matches_scipy():
     """The host pattern builder reproduces scipy's pattern of J^T blockdiag(He) J."""
     from simkit_gb300 import _lib
