@@ -1929,6 +1929,7 @@ struct BatchCtl {
   double *eta, *steps, *gg, *slope, *e2, *g0, *fnorm, *res_prev, *eta_prev, *ecur;
   int32_t *pit, *pst, *ctr;
   skg_step_info* info;
+  const double* pscal = nullptr;   // one-instance plans: the PCG's iterations and status read from its scalars
 };
 
 static BatchCtl make_ctl(const BatchWs& bw, int ni) {
@@ -2043,10 +2044,12 @@ __global__ void __launch_bounds__(kCtlThreads) k_bctl_search(BatchCtl c, CtlPara
     c.accept[i] = 0;
     if (!c.active[i]) continue;
     skg_step_info& f = c.info[i];
-    f.pcg_iters += c.pit[i];
+    const int32_t pit = c.pscal ? (int32_t)c.pscal[S_ITERS] : c.pit[i];
+    const int32_t pst = c.pscal ? (int32_t)c.pscal[S_STATUS] : c.pst[i];
+    f.pcg_iters += pit;
     f.newton_iters = it + 1;
-    if (c.pst[i] != 0) {
-      f.status = c.pst[i];
+    if (pst != 0) {
+      f.status = pst;
       c.active[i] = 0;
       continue;
     }
@@ -2401,24 +2404,41 @@ static int capture_batch_step(const skg_tet_mesh* m, const skg_batch* bt, const 
 // reads its forcing term from it.  The same kernels in the same order with the same arithmetic as
 // be_step: the two take bitwise the same steps.
 
-// the PCG's iterations and status for the search control kernel
-__global__ void k_sctl_pcg(const double* __restrict__ scal, int32_t* pit, int32_t* pst) {
-  pit[0] = (int32_t)scal[S_ITERS];
-  pst[0] = (int32_t)scal[S_STATUS];
-}
-
-// u += steps[0] * dx on free DOFs when the search accepted a step
-template <typename R>
-__global__ void k_apply_step_ctl(double* __restrict__ u, const R* __restrict__ dx, const double* __restrict__ steps,
-                                 const uint8_t* __restrict__ accept, int64_t n, const uint8_t* __restrict__ pinned) {
+// The end of a Newton iteration of the one-instance device loop: the search bookkeeping of
+// k_bctl_searched (an exhausted search sets the status; the iteration counter), u += steps[0] dx on
+// free DOFs when the search accepted a step (k_apply_step's arithmetic), and with SPLIT the hi/lo
+// split of u for the FP32 kernels (k_split's)
+template <typename R, bool SPLIT>
+__global__ void k_sctl_apply(BatchCtl c, double* __restrict__ u, const R* __restrict__ dx, int64_t n,
+                             const uint8_t* __restrict__ pinned, float* __restrict__ uh, float* __restrict__ ul) {
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (v >= n || !accept[0]) return;
-  const double step = steps[0];
-  const Vec3<R> d = ld3c(dx, v);
-  const double dd[3] = {double(d.x), double(d.y), double(d.z)};
+  if (v == 0) {
+    if (c.mask[0]) {
+      c.info[0].status = SKG_ERR_LINESEARCH;
+      c.active[0] = 0;
+    }
+    c.ctr[kCtrIter] += 1;
+  }
+  if (v >= n) return;
+  if (c.accept[0]) {
+    const double step = c.steps[0];
+    const Vec3<R> d = ld3c(dx, v);
+    const double dd[3] = {double(d.x), double(d.y), double(d.z)};
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-    if (!(pinned && pinned[3 * v + c])) u[3 * v + c] += step * dd[c];
+    for (int k = 0; k < 3; ++k)
+      if (!(pinned && pinned[3 * v + k])) u[3 * v + k] += step * dd[k];
+  }
+  if constexpr (SPLIT) {
+    float h[3], l[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double x = u[3 * v + k];
+      h[k] = float(x);
+      l[k] = float(x - double(h[k]));
+    }
+    reinterpret_cast<float4*>(uh)[v] = make_float4(h[0], h[1], h[2], 0.f);
+    reinterpret_cast<float4*>(ul)[v] = make_float4(l[0], l[1], l[2], 0.f);
+  }
 }
 
 // control state of one instance: flags, per-instance scalars (two slots each: the slope buffer takes
@@ -2467,7 +2487,8 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
   carve_single_ctl(nullptr, &ctl_bytes);
   SKG_CUDA(cudaMalloc(&plan->own, ctl_bytes));
   SKG_CUDA(cudaMemset(plan->own, 0, ctl_bytes));
-  const BatchCtl c = carve_single_ctl(plan->own, &ctl_bytes);
+  BatchCtl c = carve_single_ctl(plan->own, &ctl_bytes);
+  c.pscal = w.scal;
   plan->info = c.info;
   plan->ctr = c.ctr;
   plan->ni = 1;
@@ -2510,11 +2531,11 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
     SKG_TRY(launch_dinv_lo(m, w.dinv_lo, s0));
     launches++;
   }
-  auto gradient = [&](cudaStream_t s) -> int {
+  auto gradient = [&](cudaStream_t s, bool split_done) -> int {   // split_done: uh, ul already hold u
     if (dff) {
-      SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
+      if (!split_done) SKG_TRY(launch_split(st->u, n, w.uh, w.ul, s));
       SKG_TRY(launch_forces_df(make_tet_args64(m, st->u), m->dinv32, w.dinv_lo, w.uh, w.ul, w.fbuf, s));
-      launches++;
+      launches += split_done ? 0 : 1;
     } else {
       SKG_TRY(launch_forces(make_tet_args64(m, st->u), 1, w.fbuf, s));
     }
@@ -2535,7 +2556,7 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
     launches++;
     return launch_split(st->u, n, w.uh, w.ul, s);
   };
-  SKG_TRY(gradient(s0));
+  SKG_TRY(gradient(s0, false));
   SKG_TRY(split(s0));
   SKG_TRY(energy(nullptr, nullptr, s0));
   k_bctl_begin<<<1, kCtlThreads, 0, s0>>>(c, cpar);
@@ -2590,15 +2611,13 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
   SKG_TRY(pcg_solve<R>(A, w.g, -1.0, st->pinned, pv, 0.0, prm->pcg_max_iter, prm->pcg_mode, w.partials, w.counter,
                        w.scal, s1, &pr, prm->pcg_variant, two_level ? &cdev : nullptr, false, c.eta));
   launches += pr.launches;
-  k_sctl_pcg<<<1, 1, 0, s1>>>(w.scal, c.pit, c.pst);
-  SKG_LAUNCHED();
   k_dot_g<R><<<reduce_blocks(n), kBlock, 0, s1>>>(w.g, pv.x, n, w.partials, w.counter, c.slope);
   SKG_LAUNCHED();
   cudaGraphConditionalHandle h_ls;
   SKG_TRY(capture_handle(s1, &h_ls));
   k_bctl_search<<<1, kCtlThreads, 0, s1>>>(c, cpar, h_ls);
   SKG_LAUNCHED();
-  launches += 3;
+  launches += 2;
   {
     cudaGraph_t lbody = nullptr;
     SKG_TRY(add_conditional(s1, h_ls, cudaGraphCondTypeWhile, &lbody));
@@ -2612,13 +2631,10 @@ static int capture_single_step(const skg_tet_mesh* m, const skg_be_params* prm, 
     launches = before;
     SKG_CUDA(cudaStreamEndCapture(s2, &lbody));
   }
-  k_bctl_searched<<<1, kCtlThreads, 0, s1>>>(c);
+  k_sctl_apply<R, sizeof(R) == 4><<<blocks_for(n), kBlock, 0, s1>>>(c, st->u, pv.x, n, st->pinned, w.uh, w.ul);
   SKG_LAUNCHED();
-  k_apply_step_ctl<R><<<blocks_for(n), kBlock, 0, s1>>>(st->u, pv.x, c.steps, c.accept, n, st->pinned);
-  SKG_LAUNCHED();
-  launches += 2;
-  SKG_TRY(split(s1));
-  SKG_TRY(gradient(s1));
+  launches++;
+  SKG_TRY(gradient(s1, mixed));
   k_bctl_newton<<<1, kCtlThreads, 0, s1>>>(c, cpar, h_loop);
   SKG_LAUNCHED();
   launches++;
