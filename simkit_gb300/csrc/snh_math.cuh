@@ -339,11 +339,32 @@ enum : int { kMatSNH = 0, kMatMMNH = 1, kMatARAP = 2, kMatFCR = 3, kMatLE = 4 };
 // --------------------------------------------------------------------------
 template <typename R> SK_HD void jacobi_rotate(R& app, R& aqq, R& apq, R& arp, R& arq, R* W, int p, int q) {
   if (apq == R(0)) return;
-  const R theta = (aqq - app) / (R(2) * apq);
-  const R at = sk_abs(theta);
-  R t = (at > R(1e18)) ? R(0.5) / theta : R(1) / (at + sk_sqrt(at * at + R(1)));
-  if (theta < R(0) && at <= R(1e18)) t = -t;
-  const R c = R(1) / sk_sqrt(t * t + R(1));
+  R t, c;
+  bool fast = false;
+#if defined(__CUDA_ARCH__)
+  // FP32 on the device: the rotation only has to be orthogonal to working precision (c = 1/sqrt(1+t^2),
+  // s = t c), not correctly rounded, so the approximate divide and reciprocal square root serve
+  if constexpr (sizeof(R) == 4) {
+    const float theta = __fdividef(aqq - app, 2.f * apq);
+    const float at = fabsf(theta);
+    if (at > 1e18f) {
+      t = __fdividef(0.5f, theta);
+    } else {
+      const float s2 = fmaf(at, at, 1.f);
+      t = __fdividef(1.f, at + s2 * rsqrtf(s2));
+      if (theta < 0.f) t = -t;
+    }
+    c = rsqrtf(fmaf(t, t, 1.f));
+    fast = true;
+  }
+#endif
+  if (!fast) {
+    const R theta = (aqq - app) / (R(2) * apq);
+    const R at = sk_abs(theta);
+    t = (at > R(1e18)) ? R(0.5) / theta : R(1) / (at + sk_sqrt(at * at + R(1)));
+    if (theta < R(0) && at <= R(1e18)) t = -t;
+    c = R(1) / sk_sqrt(t * t + R(1));
+  }
   const R s = t * c;
   app -= t * apq;
   aqq += t * apq;
