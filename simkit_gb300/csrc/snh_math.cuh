@@ -412,6 +412,20 @@ template <typename R> SK_HD void any_perp(const R* a, R* out) {
   out[2] = v[2] / n;
 }
 
+// norm n = sqrt(q) and its reciprocal i (i unused when n is 0); FP32 on the device from the
+// approximate reciprocal square root, otherwise the correctly rounded square root and divide
+template <typename R> SK_HD void unit_scale(R q, R& n, R& i) {
+#if defined(__CUDA_ARCH__)
+  if constexpr (sizeof(R) == 4) {
+    i = q > 0.f ? rsqrtf(q) : 0.f;
+    n = q * i;
+    return;
+  }
+#endif
+  n = sk_sqrt(q);
+  i = n > R(0) ? R(1) / n : R(0);
+}
+
 template <typename R> SK_HD void svd3_rv(const R* F, R* U, R* s, R* V) {
   R S[6];
   S[0] = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
@@ -440,21 +454,23 @@ template <typename R> SK_HD void svd3_rv(const R* F, R* U, R* s, R* V) {
   for (int i = 0; i < 3; ++i)
     for (int k = 0; k < 3; ++k) b[3 * i + k] = F[3 * i] * V[k] + F[3 * i + 1] * V[3 + k] + F[3 * i + 2] * V[6 + k];
   R u0[3] = {b[0], b[3], b[6]};
-  R n0 = sk_sqrt(u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2]);
   R fscale = R(0);
   for (int k = 0; k < 9; ++k) fscale = sk_max(fscale, sk_abs(F[k]));
   const R tiny = Eps<R>::v * Eps<R>::v * (fscale > R(0) ? fscale : R(1));
+  R n0, i0;
+  unit_scale(u0[0] * u0[0] + u0[1] * u0[1] + u0[2] * u0[2], n0, i0);
   if (n0 > tiny) {
-    u0[0] /= n0; u0[1] /= n0; u0[2] /= n0;
+    u0[0] *= i0; u0[1] *= i0; u0[2] *= i0;
   } else {
     n0 = R(0); u0[0] = R(1); u0[1] = R(0); u0[2] = R(0);
   }
   R u1[3] = {b[1], b[4], b[7]};
   const R d01 = u0[0] * u1[0] + u0[1] * u1[1] + u0[2] * u1[2];
   u1[0] -= d01 * u0[0]; u1[1] -= d01 * u0[1]; u1[2] -= d01 * u0[2];
-  R n1 = sk_sqrt(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2]);
+  R n1, i1;
+  unit_scale(u1[0] * u1[0] + u1[1] * u1[1] + u1[2] * u1[2], n1, i1);
   if (n1 > tiny) {
-    u1[0] /= n1; u1[1] /= n1; u1[2] /= n1;
+    u1[0] *= i1; u1[1] *= i1; u1[2] *= i1;
   } else {
     n1 = R(0);
     any_perp(u0, u1);
